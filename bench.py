@@ -1,0 +1,317 @@
+#!/usr/bin/env python3
+"""Benchmark: FP64 finite-volume residual ("velocity") throughput.
+
+Workload (default): 2D Euler four-quadrant Riemann problem (IC2), 1024x1024
+cells on [0,1]^2, WENO5 + Rusanov, FP64, state = IC + seeded U[-1e-3, 1e-3]
+noise, transmissive (Neumann) boundaries; one step = one velocity()
+evaluation of the whole mesh.  value = Gcell/s with the state resident in
+HBM; e2e = the same metric through the host-buffer C-ABI call
+(pda_velocity_host: H2D state copy, kernels, D2H velocity copy per step).
+
+--impl reference times the reference's CPU algorithm for the same workload
+on all host cores (the oracle restatement; the reference C++ itself is not
+compiled on the GPU host).  Under torchrun with N>1 each rank runs an
+independent replica (the path does not shard); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+N_CELLS_SIDE = 1024
+NDPC = 4
+BYTES_PER_CELL = 16 * NDPC  # read U once + write V once (FP64)
+# Algorithmic FP64 operations per cell of the face-once WENO5 + Rusanov 2D
+# Euler velocity (counted from the kernel source: per face 4 x 2 one-sided
+# WENO5 values at 71 flops + 4 divisions each, one Rusanov flux at 65 flops
+# + 10 divisions + 3 square roots; two faces per cell plus the 24-flop
+# balance; a division or square root counts as one operation).
+FLOPS_PER_CELL = 2 * (4 * 2 * (71 + 4) + 65 + 10 + 3) + 24
+L2_FLUSH_BYTES = 256 << 20
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(pda, torch, stream):
+    mesh = pda.create_full_mesh((N_CELLS_SIDE, N_CELLS_SIDE), (0.0, 1.0, 0.0, 1.0), 7)
+    prob = pda.create_problem(mesh, pda.Euler2d.Riemann, pda.InviscidFluxReconstruction.Weno5, 2, stream=stream)
+    U0 = prob.initialConditionHost()
+    rng = np.random.default_rng(20261203)
+    U = U0 + rng.uniform(-1e-3, 1e-3, U0.shape)
+    return mesh, prob, U
+
+
+def cpu_baseline(pda, mesh, U, budget_s=10.0, threads=0):
+    """The oracle (C restatement of the reference algorithm) on the host cores."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle_py
+    orc = oracle_py.load()
+    used = orc.set_threads(threads if threads > 0 else (os.cpu_count() or 1))
+    g, x, y, z, _, _ = mesh._arrays()
+    om = orc.mesh_from_arrays(2, 7, g, x, y, z, (mesh.dx(), mesh.dy(), 0.0))
+    op = orc.problem(om, 1, 4, 2, 2)
+    op.velocity(U)  # warm-up
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while time.perf_counter() < t_end or len(times) < 2:
+        t0 = time.perf_counter()
+        op.velocity(U)
+        times.append(time.perf_counter() - t0)
+    cells = N_CELLS_SIDE * N_CELLS_SIDE
+    med = statistics.median(times)
+    import platform
+    return {"value": cells / med / 1e9, "unit": "Gcell/s", "cores": used, "kind": "port",
+            "sample": f"{len(times)} velocity() calls of the same 1024^2 Riemann WENO5 workload on {used} "
+                      f"threads of {platform.machine()} ({os.cpu_count()} logical CPUs); median "
+                      f"{med * 1e3:.1f} ms/call"}
+
+
+def run_reference(args):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return 0
+    import importlib
+    ge = importlib.import_module("__graft_entry__")
+    pda = ge.package()
+    mesh = pda.create_full_mesh((N_CELLS_SIDE, N_CELLS_SIDE), (0.0, 1.0, 0.0, 1.0), 7)
+    # host-only calls: the initial condition and the mesh arrays need no GPU
+    prob = pda.create_problem(mesh, pda.Euler2d.Riemann, pda.InviscidFluxReconstruction.Weno5, 2, stream=0)
+    U0 = prob.initialConditionHost()
+    rng = np.random.default_rng(20261203)
+    U = U0 + rng.uniform(-1e-3, 1e-3, U0.shape)
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle_py
+    orc = oracle_py.load()
+    used = orc.set_threads(os.cpu_count() or 1)
+    g, x, y, z, _, _ = mesh._arrays()
+    om = orc.mesh_from_arrays(2, 7, g, x, y, z, (mesh.dx(), mesh.dy(), 0.0))
+    op = orc.problem(om, 1, 4, 2, 2)
+    for _ in range(args.warmup):
+        op.velocity(U)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        op.velocity(U)
+        ts.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(ts) / len(ts)
+    cells = N_CELLS_SIDE * N_CELLS_SIDE
+    value = cells / (ms * 1e-3) / 1e9
+    import platform
+    line = {"impl": "reference", "metric": "FV residual Gcell/s", "value": value, "unit": "Gcell/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (Riemann IC2 + seeded U[-1e-3,1e-3] noise)",
+            "config": workload_config(),
+            "cpu_baseline": {"value": value, "unit": "Gcell/s", "cores": used, "kind": "port",
+                             "sample": f"{args.steps} full 1024^2 velocity() calls on {used} threads of "
+                                       f"{platform.machine()}; reference C++ not compiled on the GPU host "
+                                       f"(C restatement timed, bit-identical results)"},
+            "e2e": {"value": value, "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def workload_config():
+    return {"workload": "euler2d_riemann_ic2_weno5_velocity_1024x1024", "cells": N_CELLS_SIDE ** 2,
+            "dofs": NDPC * N_CELLS_SIDE ** 2, "scheme": "WENO5+Rusanov", "boundary": "Neumann (transmissive)",
+            "l2": "256 MiB write between timed steps (outside the per-step events)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import importlib
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ge = importlib.import_module("__graft_entry__")
+    pda = ge.package()
+    stream = torch.cuda.Stream()
+    mesh, prob, Uh = build_workload(pda, torch, stream)
+    cells = N_CELLS_SIDE ** 2
+    with torch.cuda.stream(stream):
+        U = torch.from_numpy(Uh).cuda()
+        V = prob.createVelocity()
+        flush = torch.empty(L2_FLUSH_BYTES // 8, dtype=torch.float64, device="cuda")
+    stream.synchronize()
+
+    def step():
+        prob.velocity(U, 0.0, V)
+
+    for _ in range(args.warmup):
+        step()
+    stream.synchronize()
+    # ---- timed region: K steps, per-step events, L2 flushed before each
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    l0 = prob.launch_count()
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                step()
+                ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    launches = (prob.launch_count() - l0) // args.steps
+    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    value = world * cells / (ms * 1e-3) / 1e9
+
+    # ---- e2e: host buffers through the C ABI (pinned), H2D + kernels + D2H
+    Uhp = torch.from_numpy(Uh).pin_memory()
+    Vhp = torch.empty(prob.totalDofSampleMesh(), dtype=torch.float64).pin_memory()
+    import ctypes as C
+    L = pda.lib()
+    for _ in range(3):
+        pda._check(L.pda_velocity_host(prob._h, C.c_void_p(Uhp.data_ptr()), 0.0, C.c_void_p(Vhp.data_ptr())))
+    te = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pda._check(L.pda_velocity_host(prob._h, C.c_void_p(Uhp.data_ptr()), 0.0, C.c_void_p(Vhp.data_ptr())))
+        te.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * sum(te) / len(te)
+    assert torch.equal(Vhp, V.cpu()), "host-buffer path differs from the device path"
+
+    # ---- per-kernel device times (dominant kernel) and roofline
+    prof = prob.profile_velocity(U, V, reps=max(5, args.steps // 2))
+    face_ms = (prof["faces_x"] + prof["faces_y"]) / 2
+    hbm_peak, peak_src = measured_peaks()
+    # faces kernel, one launch = one axis over N faces: reads U (32 B/cell) and
+    # writes the face fluxes (32 B/face); half the cell's flops
+    face_bytes = cells * (8 * NDPC) + (cells + N_CELLS_SIDE) * (8 * NDPC)
+    achieved_gbs = face_bytes / (face_ms * 1e-3) / 1e9
+    fp64_peak = pda.measure_fp64_peak()
+    flops_face_launch = cells * (FLOPS_PER_CELL - 24) / 2
+    fp64_ach = flops_face_launch / (face_ms * 1e-3)
+    step_fp64 = cells * FLOPS_PER_CELL / (ms * 1e-3)
+
+    line = {
+        "metric": "FV residual Gcell/s", "value": value, "unit": "Gcell/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (Riemann IC2 + seeded U[-1e-3,1e-3] noise)", "config": workload_config(),
+        "e2e": {"value": world * cells / (e2e_ms * 1e-3) / 1e9, "unit": "Gcell/s",
+                "h2d_bytes_per_step": int(Uhp.numel() * 8), "d2h_bytes_per_step": int(Vhp.numel() * 8),
+                "ms_per_step": e2e_ms},
+        "gpu_launches": int(launches * args.steps),
+        "roofline": {"bound": "hbm", "kernel": "k_struct_faces<Euler2d,Weno5,axis>",
+                     "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved_gbs / hbm_peak, "traffic": None, "peak_source": peak_src,
+                     "binding_roof": "fp64",
+                     "fp64": {"achieved_tflops": fp64_ach / 1e12, "peak_tflops": fp64_peak / 1e12,
+                              "frac": fp64_ach / fp64_peak, "peak_source": "measured FMA probe (pda_measure_fp64_peak)",
+                              "step_achieved_tflops": step_fp64 / 1e12,
+                              "algorithmic_flops_per_cell": FLOPS_PER_CELL},
+                     "kernel_ms": prof},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(pda, mesh, Uh, budget_s=args.cpu_budget)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

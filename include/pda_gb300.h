@@ -1,0 +1,230 @@
+/*
+ * pda_gb300.h -- C ABI of the GB300-native finite-volume residual/Jacobian
+ * engine (drop-in for pressio-demoapps' cell-centered Euler/shallow-water
+ * problems).
+ *
+ * Conventions
+ *   - Every function returns PDA_OK (0) or a negative pda_status; the message
+ *     of the last failure on the calling thread is pda_last_error().
+ *     No C++ exception crosses this boundary and nothing calls exit().
+ *   - Pointers named d_* are device (GB300 HBM) pointers; h_* are host.
+ *   - State U and residual V are array-of-structures doubles:
+ *       U[cell * ndpc + dof]   cell = stencil-mesh id   (totalDofStencilMesh)
+ *       V[row  * ndpc + dof]   row  = sample-mesh row   (totalDofSampleMesh)
+ *     exactly as the reference's Eigen vectors.
+ *   - The Jacobian is CSR (int32 row pointers and column indices, double
+ *     values) with the same row/column order and sparsity as the reference's
+ *     Eigen::SparseMatrix<double, RowMajor, int32>; the pattern is built once
+ *     and the evaluation calls overwrite the values in place.
+ *   - A problem object is bound to one CUDA stream; calls on it are
+ *     asynchronous with respect to the host (except *_host variants) and it
+ *     is not safe to call one object from two threads at once (as the
+ *     reference, whose const methods mutate internal buffers).
+ *   - The mesh must outlive every problem created from it (as the reference,
+ *     which keeps a reference to the mesh).
+ *
+ * Reference interfaces replaced (pressio-demoapps v0.16.0, paths relative to
+ * include/pressiodemoapps/):
+ */
+#ifndef PDA_GB300_H_
+#define PDA_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int pda_status;
+#define PDA_OK 0
+#define PDA_ERR_INVALID_ARGUMENT -1
+#define PDA_ERR_IO -2
+#define PDA_ERR_CUDA -3
+#define PDA_ERR_UNSUPPORTED -4
+#define PDA_ERR_OUT_OF_MEMORY -5
+#define PDA_ERR_INTERNAL -6
+
+/* problem families (euler1d.hpp:64, euler2d.hpp:67, euler3d.hpp:64, swe2d.hpp:66) */
+#define PDA_EULER1D 0
+#define PDA_EULER2D 1
+#define PDA_EULER3D 2
+#define PDA_SWE2D 3
+
+/* InviscidFluxReconstruction (schemes_info.hpp:61-63) */
+#define PDA_FIRST_ORDER 0
+#define PDA_WENO3 1
+#define PDA_WENO5 2
+
+/* problem enums, same integer values as the reference enums */
+#define PDA_EULER1D_PERIODIC_SMOOTH 0 /* Euler1d::PeriodicSmooth */
+#define PDA_EULER1D_SOD 1             /* Euler1d::Sod */
+#define PDA_EULER1D_LAX 2             /* Euler1d::Lax */
+#define PDA_EULER1D_SHU_OSHER 3       /* Euler1d::ShuOsher */
+#define PDA_EULER2D_PERIODIC_SMOOTH 0 /* Euler2d::PeriodicSmooth */
+#define PDA_EULER2D_SEDOV_FULL 2      /* Euler2d::SedovFull */
+#define PDA_EULER2D_RIEMANN 4         /* Euler2d::Riemann */
+#define PDA_EULER3D_PERIODIC_SMOOTH 0 /* Euler3d::PeriodicSmooth */
+#define PDA_SWE2D_SLIP_WALL 0         /* Swe2d::SlipWall */
+
+typedef struct pda_mesh pda_mesh;
+typedef struct pda_problem pda_problem;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *pda_last_error(void);
+
+/* Library version string. */
+const char *pda_version(void);
+
+/* ---------------------------------------------------------------- meshes */
+
+/* Replaces load_cellcentered_uniform_mesh_eigen(dir) (mesh.hpp:87-91,
+ * impl/mesh_ccu.hpp:359-448, impl/mesh_read_{info,connectivity,coords}.hpp).
+ * Reads info.dat, connectivity.dat and coordinates.dat.  Missing files are
+ * PDA_ERR_IO (the reference calls exit(EXIT_FAILURE)). */
+pda_status pda_mesh_load(const char *dir, pda_mesh **out);
+
+/* Native in-memory equivalent of meshing_scripts/create_full_mesh.py
+ * (natural row ordering; create_full_mesh.py:32-218 with
+ * _impl/{one_dim_mesh,natural_order_mesh_2d,natural_order_mesh_3d}.py).
+ * n[3] cells per axis (1 for absent axes, dim = number of n > 1 axes as the
+ * script decides), bounds[6] = {xL,xR,yL,yR,zL,zR}, stencil in {3,5,7},
+ * periodic[3] flags.  The result equals loading the files the script would
+ * write (coordinates and dx pass through the same %.14f text rounding).
+ * Extension: 3D meshes with stencil 7 (absent in the reference). */
+pda_status pda_mesh_create_full(const int n[3], const double bounds[6], int stencil,
+                                const int periodic[3], pda_mesh **out);
+
+/* Equivalent of meshing_scripts/create_sample_mesh.py (lines 28-213): sample
+ * mesh of the given full-mesh cell ids plus all their stencil neighbours,
+ * renumbered in sorted full-mesh order.  stencil_gids_out (may be NULL)
+ * receives the full-mesh id of every stencil-mesh cell (the
+ * stencil_mesh_gids.dat file), sized pda_mesh_sizes()'s stencil size. */
+pda_status pda_mesh_create_sample(const pda_mesh *full, const int64_t *sample_gids, int64_t n,
+                                  pda_mesh **out, int64_t *stencil_gids_out);
+
+/* Write info.dat / connectivity.dat / coordinates.dat in the reference's
+ * text format (create_full_mesh.py:150-218). */
+pda_status pda_mesh_write(const pda_mesh *m, const char *dir);
+
+/* dims[0]=dimensionality, dims[1]=stencilSize, dims[2]=graph columns,
+ * sizes[0]=stencilMeshSize, sizes[1]=sampleMeshSize, sizes[2]=#inner rows,
+ * sizes[3]=#near-boundary rows; dx[3], dxInv[3]; flags[0]=isFullyPeriodic,
+ * flags[1]=structured natural-order full mesh (mesh_ccu.hpp:115-159). */
+pda_status pda_mesh_info(const pda_mesh *m, int dims[3], int64_t sizes[4], double dx[3],
+                         double dxinv[3], int flags[2]);
+
+/* Copies of graph() (row-major int32), viewX/Y/Z(), graphRowsOfCellsAwayFromBd(),
+ * graphRowsOfCellsNearBd().  Any pointer may be NULL. */
+pda_status pda_mesh_arrays(const pda_mesh *m, int32_t *graph, double *x, double *y, double *z,
+                           int32_t *inner_rows, int32_t *near_bd_rows);
+
+void pda_mesh_free(pda_mesh *m);
+
+/* -------------------------------------------------------------- problems */
+
+/* Replaces create_problem_eigen(mesh, family enum, scheme [, icFlag [, params]])
+ * (euler1d.hpp:82-99, euler2d.hpp:88-173, euler3d.hpp:80-122,
+ * swe2d.hpp:143-195) and the PublicProblemEigenMixinCpp constructor
+ * (adapter_cpp.hpp:80-88).  ic_flag <= 0 selects the reference default (1).
+ * Parameters are (name, value) pairs with the reference's names
+ * (impl/euler_2d_parametrization_helpers.hpp:104-109,
+ * impl/swe_2d_parametrization_helpers.hpp:97-102); an unknown name is
+ * PDA_ERR_INVALID_ARGUMENT as in the reference.  stream is a cudaStream_t
+ * (NULL = legacy default stream).  Device memory for internal tables is
+ * allocated here and in pda_jacobian_pattern. */
+pda_status pda_problem_create(const pda_mesh *mesh, int family, int problem, int scheme,
+                              int ic_flag, const char *const *param_names,
+                              const double *param_values, int n_params, void *stream,
+                              pda_problem **out);
+
+/* Equivalent of createSlipWall SWE factory create_slip_wall_swe_2d_problem_eigen
+ * (swe2d.hpp:278-308): gravity, coriolis, pulse magnitude. */
+pda_status pda_problem_create_swe_slip_wall(const pda_mesh *mesh, int scheme, double gravity,
+                                            double coriolis, double pulse_magnitude,
+                                            void *stream, pda_problem **out);
+
+void pda_problem_free(pda_problem *p);
+
+/* numDofPerCell(), totalDofSampleMesh(), totalDofStencilMesh()
+ * (adapter_cpp.hpp:93-103). */
+pda_status pda_problem_sizes(const pda_problem *p, int *ndpc, int64_t *dofs_sample,
+                             int64_t *dofs_stencil);
+
+/* queryParameter(name) (euler_2d_prob_class.hpp:188-195, swe_2d_prob_class.hpp:169-179),
+ * also gamma(), gravity(), coriolis(). */
+pda_status pda_query_parameter(const pda_problem *p, const char *name, double *value);
+
+/* initialCondition() (euler_2d_prob_class.hpp:184-186): computed on the
+ * host with the reference's formulas, written to a device / host buffer of
+ * totalDofStencilMesh doubles. */
+pda_status pda_initial_condition(pda_problem *p, double *d_U);
+pda_status pda_initial_condition_host(const pda_problem *p, double *h_U);
+
+/* rightHandSide / operator() / rhs / velocity (adapter_cpp.hpp:162-199,
+ * adapter_py.hpp:153-158): V = f(U, t). */
+pda_status pda_velocity(pda_problem *p, const double *d_U, double t, double *d_V);
+
+/* The same call with host buffers: copies U in, evaluates, copies V out
+ * (synchronous).  This is what a caller holding Eigen/numpy vectors uses. */
+pda_status pda_velocity_host(pda_problem *p, const double *h_U, double t, double *h_V);
+
+/* createJacobian() (adapter_cpp.hpp:121-124; pattern from initializeJacobian,
+ * euler_2d_prob_class.hpp:223-237, :314-387): number of rows
+ * (totalDofSampleMesh), columns (totalDofStencilMesh) and stored entries. */
+pda_status pda_jacobian_shape(pda_problem *p, int64_t *rows, int64_t *cols, int64_t *nnz);
+
+/* Copy the CSR pattern (row pointers rows+1, column indices nnz) into device
+ * buffers / host buffers. */
+pda_status pda_jacobian_pattern(pda_problem *p, int32_t *d_rowptr, int32_t *d_colidx);
+pda_status pda_jacobian_pattern_host(pda_problem *p, int32_t *h_rowptr, int32_t *h_colidx);
+
+/* rightHandSideAndJacobian / rhsAndJacobian / operator()(U,t,V,J,true)
+ * (adapter_cpp.hpp:201-221): V and the CSR values (nnz doubles, in the
+ * pattern's order) are overwritten. */
+pda_status pda_velocity_and_jacobian(pda_problem *p, const double *d_U, double t, double *d_V,
+                                     double *d_J);
+pda_status pda_velocity_and_jacobian_host(pda_problem *p, const double *h_U, double t,
+                                          double *h_V, double *h_J);
+
+/* jacobian(U, t, J) (adapter_cpp.hpp:223-229): V goes to internal scratch. */
+pda_status pda_jacobian(pda_problem *p, const double *d_U, double t, double *d_J);
+
+/* applyJacobian(U, B, t, R) (adapter_cpp.hpp:231-259): recomputes J at U and
+ * forms R = J * B for a column-major B of n_cols columns (ld = rows of B =
+ * totalDofStencilMesh, R ld = totalDofSampleMesh). */
+pda_status pda_apply_jacobian(pda_problem *p, const double *d_U, double t, const double *d_B,
+                              int n_cols, double *d_R);
+
+/* --------------------------------------------------------------- steppers */
+
+/* Explicit time integration on the device with the vendored Pressio
+ * steppers' update formulas: SSP-RK3
+ * (ode_explicit_stepper_without_mass_matrix.hpp:230-282) and RK4 (:284-336).
+ * U is advanced in place by n_steps steps of size dt from t0.  When
+ * use_graph != 0 each step is captured once into a CUDA graph and replayed. */
+pda_status pda_advance_ssprk3(pda_problem *p, double *d_U, double t0, double dt, int64_t n_steps,
+                              int use_graph);
+pda_status pda_advance_rk4(pda_problem *p, double *d_U, double t0, double dt, int64_t n_steps,
+                           int use_graph);
+
+/* --------------------------------------------------------- diagnostics
+ * (no counterpart in the reference: measurement support for benchmarks) */
+
+/* Number of kernels this library launched since the problem was created. */
+int64_t pda_problem_launch_count(const pda_problem *p);
+
+/* Evaluate the velocity reps times with CUDA events between the kernels of
+ * the structured path; ms[5] receives the mean device time of the face
+ * kernels along x, y, z, the balance kernel and the near-boundary row
+ * kernel (0 where absent). */
+pda_status pda_profile_velocity(pda_problem *p, const double *d_U, double *d_V, int reps,
+                                double ms[5]);
+
+/* Measured FP64 FMA throughput of the current device (FLOP/s, FMA = 2). */
+pda_status pda_measure_fp64_peak(double *flops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PDA_GB300_H_ */

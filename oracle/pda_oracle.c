@@ -1,0 +1,1243 @@
+/*
+ * Test infrastructure only (the oracle): plain-C restatement of the
+ * pressio-demoapps (v0.16.0) cell-centered finite-volume residual and
+ * Jacobian, per graph row exactly as the reference's loops do it (each face
+ * computed from the cell's own stencil, ghost values filled per near-boundary
+ * row, Jacobian accumulated with coeffRef semantics).  Only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU baseline call it; it is pinned
+ * against the reference's own results (tests/golden, generated by the
+ * reference itself) by tests/test_oracle.py.
+ *
+ * Reference files followed (paths under include/pressiodemoapps/):
+ *   mesh:        impl/mesh_ccu.hpp:161-448, impl/mesh_read_{info,connectivity,coords}.hpp
+ *   WENO:        impl/weno5.hpp:56-434, impl/weno3.hpp:56-246, weno.hpp:300-368
+ *   fluxes:      impl/euler_rusanov_flux_values_function.hpp:54-208,
+ *                impl/euler_rusanov_flux_jacobian_function.hpp:54-406,
+ *                impl/swe_rusanov_flux_values_function.hpp:54-97,
+ *                impl/swe_rusanov_flux_jacobian_function.hpp:54-137
+ *   ghosts:      impl/euler_1d_ghost_filler.hpp:81-144,
+ *                impl/euler_2d_ghost_filler_neumann.hpp:101-276,
+ *                impl/swe_2d_ghost_filler_inviscid_wall.hpp:99-278
+ *   stencils:    impl/functor_fill_stencil.hpp, impl/functor_reconstruct_from_{state,stencil}.hpp
+ *   balance:     impl/mixin_directional_flux_balance.hpp:68-84,
+ *                impl/mixin_directional_flux_balance_jacobian.hpp:120-372
+ *   problems:    impl/{euler_1d,euler_2d,euler_3d,swe_2d}_prob_class.hpp
+ *   ICs:         impl/euler_{1d,2d,3d}_initial_condition.hpp, impl/swe_2d_initial_condition.hpp
+ *   steppers:    tests_cpp/pressio/include/pressio/ode/impl/ode_explicit_stepper_without_mass_matrix.hpp:230-336
+ * Extension beyond the reference: 3D WENO5 (the reference throws "missing
+ * impl", functor_reconstruct_from_state.hpp:662-664), restated from the 2D
+ * WENO5 path with third-layer graph columns 13..18.
+ */
+#include "pda_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static __thread char g_err[512];
+const char *orc_last_error(void) { return g_err; }
+static void seterr(const char *m) { snprintf(g_err, sizeof g_err, "%s", m); }
+
+/* ------------------------------------------------------------------ mesh */
+struct orc_mesh {
+  int dim, stencil, ncols;
+  int64_t nst, nsm;
+  int32_t *g;
+  double *x, *y, *z;
+  double dx[3], dxi[3];
+  int32_t *inner, *nearbd;
+  int64_t ninner, nnear;
+  int fullyPeriodic;
+};
+
+#define G(m, r, c) ((m)->g[(int64_t)(r) * (m)->ncols + (c)])
+
+static void classify(orc_mesh *m) {
+  m->inner = malloc(sizeof(int32_t) * (m->nsm + 1));
+  m->nearbd = malloc(sizeof(int32_t) * (m->nsm + 1));
+  m->ninner = m->nnear = 0;
+  m->fullyPeriodic = 1;
+  for (int64_t r = 0; r < m->nsm; ++r) {
+    int bd = 0;
+    for (int c = 1; c < m->ncols; ++c)
+      if (G(m, r, c) == -1) bd = 1;
+    if (bd) {
+      m->nearbd[m->nnear++] = (int32_t)r;
+      m->fullyPeriodic = 0;
+    } else {
+      m->inner[m->ninner++] = (int32_t)r;
+    }
+  }
+}
+
+orc_mesh *orc_mesh_load(const char *dir) {
+  char path[4096];
+  orc_mesh *m = calloc(1, sizeof *m);
+  snprintf(path, sizeof path, "%s/info.dat", dir);
+  FILE *f = fopen(path, "r");
+  if (!f) {
+    seterr("info.dat not found");
+    free(m);
+    return NULL;
+  }
+  char key[128], val[128];
+  while (fscanf(f, "%127s %127s", key, val) == 2) {
+    if (!strcmp(key, "dim")) m->dim = atoi(val);
+    else if (!strcmp(key, "dx")) { m->dx[0] = strtod(val, NULL); m->dxi[0] = 1. / m->dx[0]; }
+    else if (!strcmp(key, "dy")) { m->dx[1] = strtod(val, NULL); m->dxi[1] = 1. / m->dx[1]; }
+    else if (!strcmp(key, "dz")) { m->dx[2] = strtod(val, NULL); m->dxi[2] = 1. / m->dx[2]; }
+    else if (!strcmp(key, "sampleMeshSize")) m->nsm = atoll(val);
+    else if (!strcmp(key, "stencilMeshSize")) m->nst = atoll(val);
+    else if (!strcmp(key, "stencilSize")) m->stencil = atoi(val);
+  }
+  fclose(f);
+  m->ncols = 1 + (m->stencil - 1) * m->dim;
+  m->g = malloc(sizeof(int32_t) * m->nsm * m->ncols);
+  snprintf(path, sizeof path, "%s/connectivity.dat", dir);
+  f = fopen(path, "r");
+  if (!f) {
+    seterr("connectivity.dat not found");
+    return NULL;
+  }
+  for (int64_t k = 0; k < m->nsm * m->ncols; ++k) {
+    long v;
+    if (fscanf(f, "%ld", &v) != 1) {
+      seterr("short connectivity.dat");
+      fclose(f);
+      return NULL;
+    }
+    m->g[k] = (int32_t)v;
+  }
+  fclose(f);
+  m->x = calloc(m->nst, sizeof(double));
+  m->y = calloc(m->nst, sizeof(double));
+  m->z = calloc(m->nst, sizeof(double));
+  snprintf(path, sizeof path, "%s/coordinates.dat", dir);
+  f = fopen(path, "r");
+  if (!f) {
+    seterr("coordinates.dat not found");
+    return NULL;
+  }
+  char line[512];
+  while (fgets(line, sizeof line, f)) {
+    long gid;
+    double a, b, c = 0;
+    int n = sscanf(line, "%ld %lf %lf %lf", &gid, &a, &b, &c);
+    if (n < 3) continue;
+    m->x[gid] = a;
+    m->y[gid] = b;
+    m->z[gid] = (m->dim == 3) ? c : 0.0;
+  }
+  fclose(f);
+  classify(m);
+  return m;
+}
+
+orc_mesh *orc_mesh_from_arrays(int dim, int stencil, int64_t nsm, int64_t nst, const int32_t *graph,
+                               const double *x, const double *y, const double *z, const double dx[3]) {
+  orc_mesh *m = calloc(1, sizeof *m);
+  m->dim = dim;
+  m->stencil = stencil;
+  m->ncols = 1 + (stencil - 1) * dim;
+  m->nsm = nsm;
+  m->nst = nst;
+  m->g = malloc(sizeof(int32_t) * nsm * m->ncols);
+  memcpy(m->g, graph, sizeof(int32_t) * nsm * m->ncols);
+  m->x = malloc(sizeof(double) * nst);
+  m->y = malloc(sizeof(double) * nst);
+  m->z = malloc(sizeof(double) * nst);
+  memcpy(m->x, x, sizeof(double) * nst);
+  memcpy(m->y, y, sizeof(double) * nst);
+  memcpy(m->z, z, sizeof(double) * nst);
+  for (int a = 0; a < 3; ++a) {
+    m->dx[a] = dx[a];
+    m->dxi[a] = a < dim ? 1. / dx[a] : 0.;
+  }
+  classify(m);
+  return m;
+}
+
+void orc_mesh_free(orc_mesh *m) {
+  if (!m) return;
+  free(m->g); free(m->x); free(m->y); free(m->z); free(m->inner); free(m->nearbd);
+  free(m);
+}
+
+void orc_mesh_counts(const orc_mesh *m, int64_t out[4]) {
+  out[0] = m->nst; out[1] = m->nsm; out[2] = m->ninner; out[3] = m->nnear;
+}
+
+/* ------------------------------------------------------------ reconstruction */
+static void weno5_impl(double *uNeg, double *uPos, double qim2, double qim1, double qi, double qip1,
+                       double qip2, double qip3) {
+  const double epsilon = 1e-6, one = 1, two = 2, three = 3;
+  const double four = two * two, five = three + two, six = three * two, seven = four + three;
+  const double ten = five * two, eleven = five + six, twelve = six * two, thirteen = six + seven;
+  const double oneOvfour = one / four, oneOvsix = one / six, oneOvten = one / ten;
+  const double threeOvten = three / ten, sixOvten = six / ten, thirteenOvtwelve = thirteen / twelve;
+  {
+    const double p0 = (two * qim2 - seven * qim1 + eleven * qi) * oneOvsix;
+    const double p1 = (-qim1 + five * qi + two * qip1) * oneOvsix;
+    const double p2 = (two * qi + five * qip1 - qip2) * oneOvsix;
+    const double B0 = thirteenOvtwelve * (qim2 - two * qim1 + qi) * (qim2 - two * qim1 + qi) +
+                      oneOvfour * (qim2 - four * qim1 + three * qi) * (qim2 - four * qim1 + three * qi);
+    const double B1 = thirteenOvtwelve * (qim1 - two * qi + qip1) * (qim1 - two * qi + qip1) +
+                      oneOvfour * (qim1 - qip1) * (qim1 - qip1);
+    const double B2 = thirteenOvtwelve * (qi - two * qip1 + qip2) * (qi - two * qip1 + qip2) +
+                      oneOvfour * (three * qi - four * qip1 + qip2) * (three * qi - four * qip1 + qip2);
+    const double a0 = oneOvten / (epsilon * epsilon + 2. * epsilon * B0 + B0 * B0);
+    const double a1 = sixOvten / (epsilon * epsilon + 2. * epsilon * B1 + B1 * B1);
+    const double a2 = threeOvten / (epsilon * epsilon + 2. * epsilon * B2 + B2 * B2);
+    const double s = one / (a0 + a1 + a2);
+    *uNeg = (a0 * s) * p0 + (a1 * s) * p1 + (a2 * s) * p2;
+  }
+  {
+    const double p0 = (-qim1 + five * qi + two * qip1) * oneOvsix;
+    const double p1 = (two * qi + five * qip1 - qip2) * oneOvsix;
+    const double p2 = (eleven * qip1 - seven * qip2 + two * qip3) * oneOvsix;
+    const double B0 = thirteenOvtwelve * (qim1 - two * qi + qip1) * (qim1 - two * qi + qip1) +
+                      oneOvfour * (qim1 - four * qi + three * qip1) * (qim1 - four * qi + three * qip1);
+    const double B1 = thirteenOvtwelve * (qi - two * qip1 + qip2) * (qi - two * qip1 + qip2) +
+                      oneOvfour * (qi - qip2) * (qi - qip2);
+    const double B2 = thirteenOvtwelve * (qip1 - two * qip2 + qip3) * (qip1 - two * qip2 + qip3) +
+                      oneOvfour * (three * qip1 - four * qip2 + qip3) * (three * qip1 - four * qip2 + qip3);
+    const double a0 = threeOvten / (epsilon * epsilon + 2. * epsilon * B0 + B0 * B0);
+    const double a1 = sixOvten / (epsilon * epsilon + 2. * epsilon * B1 + B1 * B1);
+    const double a2 = oneOvten / (epsilon * epsilon + 2. * epsilon * B2 + B2 * B2);
+    const double s = one / (a0 + a1 + a2);
+    *uPos = (a0 * s) * p0 + (a1 * s) * p1 + (a2 * s) * p2;
+  }
+}
+
+/* weno5WithGrad: gN[0..5] w.r.t. q_{i-2..i+3} (gN[5] = 0), gP (gP[0] = 0) */
+static void weno5_grad_impl(double *uNeg, double *uPos, double *gN, double *gP, double qim2, double qim1,
+                            double qi, double qip1, double qip2, double qip3) {
+  const double epsilon = 1e-6, one = 1, two = 2, three = 3;
+  const double four = two * two, five = three + two, six = three * two, seven = four + three;
+  const double ten = five * two, eleven = five + six, twelve = six * two, thirteen = six + seven;
+  const double oneOvfour = one / four, oneOvsix = one / six, oneOvten = one / ten;
+  const double threeOvten = three / ten, sixOvten = six / ten, thirteenOvtwelve = thirteen / twelve;
+  {
+    const double p0 = (two * qim2 - seven * qim1 + eleven * qi) * oneOvsix;
+    const double p1 = (-qim1 + five * qi + two * qip1) * oneOvsix;
+    const double p2 = (two * qi + five * qip1 - qip2) * oneOvsix;
+    const double dp0[5] = {1. / 3., -7. / 6., 11. / 6., 0., 0.};
+    const double dp1[5] = {0., -1. / 6., 5. / 6., 1. / 3., 0.};
+    const double dp2[5] = {0., 0., 1. / 3., 5. / 6., -1. / 6.};
+    const double B0 = thirteenOvtwelve * pow(qim2 - two * qim1 + qi, two) + oneOvfour * pow(qim2 - four * qim1 + three * qi, two);
+    const double B1 = thirteenOvtwelve * pow(qim1 - two * qi + qip1, two) + oneOvfour * pow(qim1 - qip1, two);
+    const double B2 = thirteenOvtwelve * pow(qi - two * qip1 + qip2, two) + oneOvfour * pow(three * qi - four * qip1 + qip2, two);
+    double dB0[5], dB1[5], dB2[5];
+    dB0[0] = (13. * (qim2 - 2. * qim1 + qi)) / 6. + (qim2 - 4. * qim1 + 3. * qi) / 2.;
+    dB0[1] = -(13. * (qim2 - 2. * qim1 + qi)) / 3. - 2. * (qim2 - 4. * qim1 + 3. * qi);
+    dB0[2] = (13. * (qim2 - 2. * qim1 + qi)) / 6. + (3. * (qim2 - 4. * qim1 + 3. * qi)) / 2.;
+    dB0[3] = 0.; dB0[4] = 0.;
+    dB1[0] = 0.;
+    dB1[1] = (13. * (qip1 + qim1 - 2. * qi)) / 6. + (qim1 - qip1) / 2.;
+    dB1[2] = -(13. * (qip1 + qim1 - 2. * qi)) / 3.;
+    dB1[3] = (13. * (qip1 + qim1 - 2. * qi)) / 6. - (qim1 - qip1) / 2.;
+    dB1[4] = 0.;
+    dB2[0] = 0.; dB2[1] = 0.;
+    dB2[2] = (13. * (qip2 - 2. * qip1 + qi)) / 6. + (3. * (qip2 - 4. * qip1 + 3. * qi)) / 2.;
+    dB2[3] = -(13. * (qip2 - 2. * qip1 + qi)) / 3. - 2. * (qip2 - 4. * qip1 + 3. * qi);
+    dB2[4] = (13. * (qip2 - 2. * qip1 + qi)) / 6. + (qip2 - 4. * qip1 + 3. * qi) / 2.;
+    const double a0 = oneOvten / pow(epsilon + B0, two);
+    const double a1 = sixOvten / pow(epsilon + B1, two);
+    const double a2 = threeOvten / pow(epsilon + B2, two);
+    const double s = one / (a0 + a1 + a2);
+    double da0[5], da1[5], da2[5], das[5];
+    for (int i = 0; i < 5; i++) {
+      da0[i] = -1. / (5. * pow(B0 + epsilon, 3.)) * dB0[i];
+      da1[i] = -6. / (5. * pow(B1 + epsilon, 3.)) * dB1[i];
+      da2[i] = -3. / (5. * pow(B2 + epsilon, 3.)) * dB2[i];
+      das[i] = -1. / pow(a2 + a1 + a0, 2.) * (da0[i] + da1[i] + da2[i]);
+    }
+    const double w0 = a0 * s, w1 = a1 * s, w2 = a2 * s;
+    for (int i = 0; i < 5; i++) {
+      gN[i] = (da0[i] * s + das[i] * a0) * p0 + dp0[i] * w0;
+      gN[i] += (da1[i] * s + das[i] * a1) * p1 + dp1[i] * w1;
+      gN[i] += (da2[i] * s + das[i] * a2) * p2 + dp2[i] * w2;
+    }
+    gN[5] = 0.;
+    *uNeg = w0 * p0 + w1 * p1 + w2 * p2;
+  }
+  {
+    const double p0 = (-qim1 + five * qi + two * qip1) * oneOvsix;
+    const double p1 = (two * qi + five * qip1 - qip2) * oneOvsix;
+    const double p2 = (eleven * qip1 - seven * qip2 + two * qip3) * oneOvsix;
+    const double dp0[5] = {-1. / 6., 5. / 6., 1. / 3., 0., 0.};
+    const double dp1[5] = {0., 1. / 3., 5. / 6., -1. / 6., 0.};
+    const double dp2[5] = {0., 0., 11. / 6., -7. / 6., 1. / 3.};
+    const double B0 = thirteenOvtwelve * pow(qim1 - two * qi + qip1, two) + oneOvfour * pow(qim1 - four * qi + three * qip1, two);
+    const double B1 = thirteenOvtwelve * pow(qi - two * qip1 + qip2, two) + oneOvfour * pow(qi - qip2, two);
+    const double B2 = thirteenOvtwelve * pow(qip1 - two * qip2 + qip3, two) + oneOvfour * pow(three * qip1 - four * qip2 + qip3, two);
+    double dB0[5], dB1[5], dB2[5];
+    dB0[0] = (3. * qip1 + qim1 - 4. * qi) / 2. + (13. * (qip1 + qim1 - 2. * qi)) / 6.;
+    dB0[1] = -2. * (3. * qip1 + qim1 - 4. * qi) - (13. * (qip1 + qim1 - 2 * qi)) / 3.;
+    dB0[2] = (3. * (3. * qip1 + qim1 - 4. * qi)) / 2. + (13. * (qip1 + qim1 - 2. * qi)) / 6.;
+    dB0[3] = 0.; dB0[4] = 0.;
+    dB1[0] = 0.;
+    dB1[1] = (13. * (qip2 - 2 * qip1 + qi)) / 6. + (qi - qip2) / 2.;
+    dB1[2] = -(13. * (qip2 - 2. * qip1 + qi)) / 3.;
+    dB1[3] = (13. * (qip2 - 2. * qip1 + qi)) / 6. - (qi - qip2) / 2.;
+    dB1[4] = 0.;
+    dB2[0] = 0.; dB2[1] = 0.;
+    dB2[2] = (13. * (qip3 - 2. * qip2 + qip1)) / 6. + (3. * (qip3 - 4. * qip2 + 3. * qip1)) / 2.;
+    dB2[3] = -(13. * (qip3 - 2. * qip2 + qip1)) / 3. - 2. * (qip3 - 4. * qip2 + 3. * qip1);
+    dB2[4] = (13. * (qip3 - 2. * qip2 + qip1)) / 6. + (qip3 - 4. * qip2 + 3. * qip1) / 2.;
+    const double a0 = threeOvten / pow(epsilon + B0, two);
+    const double a1 = sixOvten / pow(epsilon + B1, two);
+    const double a2 = oneOvten / pow(epsilon + B2, two);
+    const double s = one / (a0 + a1 + a2);
+    double da0[5], da1[5], da2[5], das[5];
+    for (int i = 0; i < 5; i++) {
+      da0[i] = -3. / (5. * pow(B0 + epsilon, 3.)) * dB0[i];
+      da1[i] = -6. / (5. * pow(B1 + epsilon, 3.)) * dB1[i];
+      da2[i] = -1. / (5. * pow(B2 + epsilon, 3.)) * dB2[i];
+      das[i] = -1. / pow(a2 + a1 + a0, 2.) * (da0[i] + da1[i] + da2[i]);
+    }
+    const double w0 = a0 * s, w1 = a1 * s, w2 = a2 * s;
+    for (int i = 0; i < 5; i++) {
+      gP[i + 1] = (da0[i] * s + das[i] * a0) * p0 + dp0[i] * w0;
+      gP[i + 1] += (da1[i] * s + das[i] * a1) * p1 + dp1[i] * w1;
+      gP[i + 1] += (da2[i] * s + das[i] * a2) * p2 + dp2[i] * w2;
+    }
+    gP[0] = 0.;
+    *uPos = w0 * p0 + w1 * p1 + w2 * p2;
+  }
+}
+
+static void weno3_impl(double *uNeg, double *uPos, double qim1, double qi, double qip1, double qip2) {
+  const double epsilon = 1.e-6, one = 1., two = 2., three = 3.;
+  const double oneOvtwo = one / two, oneOvthree = one / three, twoOvthree = two / three;
+  {
+    const double p0 = (-qim1 + three * qi) * oneOvtwo;
+    const double p1 = (qi + qip1) * oneOvtwo;
+    const double B0 = (qim1 - qi) * (qim1 - qi);
+    const double B1 = (qi - qip1) * (qi - qip1);
+    const double a0 = oneOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
+    const double a1 = twoOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
+    const double s = one / (a0 + a1);
+    *uNeg = (a0 * s) * p0 + (a1 * s) * p1;
+  }
+  {
+    const double p0 = (qi + qip1) * oneOvtwo;
+    const double p1 = (three * qip1 - qip2) * oneOvtwo;
+    const double B0 = (qi - qip1) * (qi - qip1);
+    const double B1 = (qip1 - qip2) * (qip1 - qip2);
+    const double a0 = twoOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
+    const double a1 = oneOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
+    const double s = one / (a0 + a1);
+    *uPos = (a0 * s) * p0 + (a1 * s) * p1;
+  }
+}
+
+static void weno3_grad_impl(double *uNeg, double *uPos, double *gN, double *gP, double qim1, double qi,
+                            double qip1, double qip2) {
+  const double epsilon = 1e-6, one = 1, two = 2, three = 3;
+  const double oneOvtwo = one / two, oneOvthree = one / three, twoOvthree = two / three;
+  {
+    const double p0 = (-qim1 + three * qi) * oneOvtwo;
+    const double p1 = (qi + qip1) * oneOvtwo;
+    const double dp0[3] = {-1. / 2., 3. / 2., 0.};
+    const double dp1[3] = {0., 1. / 2., 1. / 2.};
+    const double B0 = (qim1 - qi) * (qim1 - qi);
+    const double B1 = (qi - qip1) * (qi - qip1);
+    const double a0 = oneOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
+    const double a1 = twoOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
+    const double s = one / (a0 + a1);
+    double da0[3], da1[3], das[3];
+    da0[0] = -4. * (qim1 - qi) / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 3));
+    da0[1] = 4. * (qim1 - qi) / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 3.));
+    da0[2] = 0.;
+    da1[0] = 0.;
+    da1[1] = -8. * (qi - qip1) / (3. * pow(pow(qi - qip1, 2.) + epsilon, 3.));
+    da1[2] = 8. * (qi - qip1) / (3. * pow(pow(qi - qip1, 2.) + epsilon, 3.));
+    das[0] = (4. * (qim1 - qi)) / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 3.) * pow(2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)) + 1. / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 2.)), 2.));
+    das[1] = -((4. * (qim1 - qi)) / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 3.)) - (8. * (qi - qip1)) / (3. * pow(pow(qi - qip1, 2.) + epsilon, 3.))) / pow(2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)) + 1. / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 2.)), 2.);
+    das[2] = -(8. * (qi - qip1)) / (3. * pow(2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)) + 1. / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 2.)), 2.) * pow(pow(qi - qip1, 2.) + epsilon, 3.));
+    const double w0 = a0 * s, w1 = a1 * s;
+    for (int i = 0; i < 3; i++) {
+      gN[i] = (da0[i] * s + das[i] * a0) * p0 + dp0[i] * w0;
+      gN[i] += (da1[i] * s + das[i] * a1) * p1 + dp1[i] * w1;
+    }
+    gN[3] = 0.;
+    *uNeg = w0 * p0 + w1 * p1;
+  }
+  {
+    const double p0 = (qi + qip1) * oneOvtwo;
+    const double p1 = (three * qip1 - qip2) * oneOvtwo;
+    const double B0 = (qi - qip1) * (qi - qip1);
+    const double B1 = (qip1 - qip2) * (qip1 - qip2);
+    const double a0 = twoOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
+    const double a1 = oneOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
+    const double s = one / (a0 + a1);
+    const double w0 = a0 * s, w1 = a1 * s;
+    const double dp0[3] = {1. / 2., 1 / 2., 0.};
+    const double dp1[3] = {0., 3. / 2., -1. / 2.};
+    double da0[3], da1[3], das[3];
+    da0[0] = -8. * (qi - qip1) / (3. * pow(pow(qi - qip1, 2.) + epsilon, 3.));
+    da0[1] = 8. * (qi - qip1) / (3. * pow(pow(qi - qip1, 2.) + epsilon, 3.));
+    da0[2] = 0.;
+    da1[0] = 0.;
+    da1[1] = -4. * (qip1 - qip2) / (3. * pow(pow(qip1 - qip2, 2.) + epsilon, 3.));
+    da1[2] = 4. * (qip1 - qip2) / (3. * pow(pow(qip1 - qip2, 2) + epsilon, 3.));
+    das[0] = 8. * (qi - qip1) / (3. * pow(pow(qi - qip1, 2.) + epsilon, 3.) * pow(1. / (3. * pow(pow(qip1 - qip2, 2.) + epsilon, 2.)) + 2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)), 2.));
+    das[1] = -(8. * (qi - qip1) / (3 * pow(pow(qi - qip1, 2.) + epsilon, 3.)) - 4. * (qip1 - qip2) / (3. * pow(pow(qip1 - qip2, 2.) + epsilon, 3.))) / pow(1. / (3. * pow(pow(qip1 - qip2, 2.) + epsilon, 2.)) + 2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)), 2.);
+    das[2] = -4. * (qip1 - qip2) / (3. * pow(1. / (3. * pow(pow(qip1 - qip2, 2.) + epsilon, 2.)) + 2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)), 2.) * pow(pow(qip1 - qip2, 2.) + epsilon, 3.));
+    for (int i = 0; i < 3; i++) {
+      gP[i + 1] = (da0[i] * s + das[i] * a0) * p0 + dp0[i] * w0;
+      gP[i + 1] += (da1[i] * s + das[i] * a1) * p1 + dp1[i] * w1;
+    }
+    gP[0] = 0.;
+    *uPos = w0 * p0 + w1 * p1;
+  }
+}
+
+void orc_weno5(const double q[7], double o[4]) {
+  weno5_impl(&o[0], &o[1], q[0], q[1], q[2], q[3], q[4], q[5]);
+  weno5_impl(&o[2], &o[3], q[1], q[2], q[3], q[4], q[5], q[6]);
+}
+void orc_weno3(const double q[5], double o[4]) {
+  weno3_impl(&o[0], &o[1], q[0], q[1], q[2], q[3]);
+  weno3_impl(&o[2], &o[3], q[1], q[2], q[3], q[4]);
+}
+
+/* ------------------------------------------------------------------ fluxes */
+/* generic-normal Euler flux for nd = 3 (1D), 4 (2D), 5 (3D) */
+static void euler_flux(int nd, double *F, const double *qL, const double *qR, const double *n, double gamma) {
+  const double one = 1, two = 2, half = one / two, es = 1.e-30;
+  if (nd == 3) {
+    const double rL = qL[0], uL = qL[1] / (rL + es);
+    const double pL = (gamma - 1) * (qL[2] - half * rL * (uL * uL));
+    const double HL = (qL[2] + pL) / rL;
+    const double FL[3] = {rL * uL, rL * uL * uL + pL, rL * uL * HL};
+    const double rR = qR[0], uR = qR[1] / (rR + es);
+    const double pR = (gamma - 1) * (qR[2] - half * rR * (uR * uR));
+    const double HR = (qR[2] + pR) / rR;
+    const double FR[3] = {rR * uR, rR * uR * uR + pR, rR * uR * HR};
+    const double RT = sqrt(rR / (rL));
+    const double u = (uL + RT * uR) / (1. + RT);
+    const double H = (HL + RT * HR) / (1. + RT);
+    const double a = sqrt((gamma - 1.) * (H - half * (u * u)));
+    const double smax = fabs(u) + a;
+    for (int i = 0; i < 3; ++i) F[i] = half * (FL[i] + FR[i] + smax * (qL[i] - qR[i]));
+    return;
+  }
+  const int nv = nd - 2; /* velocity components */
+  double vL[3] = {0, 0, 0}, vR[3] = {0, 0, 0};
+  const double rL = qL[0], rR = qR[0];
+  for (int k = 0; k < nv; ++k) vL[k] = qL[1 + k] / (rL + es);
+  for (int k = 0; k < nv; ++k) vR[k] = qR[1 + k] / (rR + es);
+  double unL, unR, ksL, ksR;
+  if (nv == 2) {
+    unL = vL[0] * n[0] + vL[1] * n[1];
+    unR = vR[0] * n[0] + vR[1] * n[1];
+    ksL = vL[0] * vL[0] + vL[1] * vL[1];
+    ksR = vR[0] * vR[0] + vR[1] * vR[1];
+  } else {
+    unL = vL[0] * n[0] + vL[1] * n[1] + vL[2] * n[2];
+    unR = vR[0] * n[0] + vR[1] * n[1] + vR[2] * n[2];
+    ksL = vL[0] * vL[0] + vL[1] * vL[1] + vL[2] * vL[2];
+    ksR = vR[0] * vR[0] + vR[1] * vR[1] + vR[2] * vR[2];
+  }
+  const double pL = (gamma - 1) * (qL[nd - 1] - half * rL * (ksL));
+  const double HL = (qL[nd - 1] + pL) / rL;
+  const double pR = (gamma - 1) * (qR[nd - 1] - half * rR * (ksR));
+  const double HR = (qR[nd - 1] + pR) / rR;
+  double FL[5], FR[5];
+  FL[0] = rL * unL;
+  FR[0] = rR * unR;
+  for (int k = 0; k < nv; ++k) {
+    FL[1 + k] = rL * unL * vL[k] + pL * n[k];
+    FR[1 + k] = rR * unR * vR[k] + pR * n[k];
+  }
+  FL[nd - 1] = rL * unL * HL;
+  FR[nd - 1] = rR * unR * HR;
+  const double RT = sqrt(rR / (rL));
+  double vr[3];
+  for (int k = 0; k < nv; ++k) vr[k] = (vL[k] + RT * vR[k]) / (1. + RT);
+  const double H = (HL + RT * HR) / (1. + RT);
+  double ks;
+  if (nv == 2) ks = vr[0] * vr[0] + vr[1] * vr[1];
+  else ks = vr[0] * vr[0] + vr[1] * vr[1] + vr[2] * vr[2];
+  const double a = sqrt((gamma - 1.) * (H - half * (ks)));
+  const double smax = sqrt(ks) + a;
+  for (int i = 0; i < nd; ++i) F[i] = half * (FL[i] + FR[i] + smax * (qL[i] - qR[i]));
+}
+
+static void swe_flux(double *F, const double *qL, const double *qR, const double *n, double gravity) {
+  const double one = 1, two = 2, half = one / two, es = 1.e-30;
+  const double hL = qL[0], uL = qL[1] / (hL + es), vL = qL[2] / (hL + es);
+  const double unL = uL * n[0] + vL * n[1];
+  const double pL = 0.5 * gravity * hL * hL;
+  const double FL[3] = {hL * unL, hL * unL * uL + pL * n[0], hL * unL * vL + pL * n[1]};
+  const double hR = qR[0], uR = qR[1] / (hR + es), vR = qR[2] / (hR + es);
+  const double unR = uR * n[0] + vR * n[1];
+  const double pR = 0.5 * gravity * hR * hR;
+  const double FR[3] = {hR * unR, hR * unR * uR + pR * n[0], hR * unR * vR + pR * n[1]};
+  const double um = (unL * pow(hL, 0.5) + unR * pow(hR, 0.5)) / (pow(hL, 0.5) + pow(hR, 0.5) + es);
+  const double hm = 0.5 * (hL + hR);
+  const double smax = sqrt(um * um) + sqrt(pow(sqrt(gravity * hm), 2.));
+  for (int i = 0; i < 3; ++i) F[i] = half * (FL[i] + FR[i] + smax * (qL[i] - qR[i]));
+}
+
+/* Euler flux Jacobians (row-major nd x nd) */
+static void euler_flux_jac(int nd, double *JL, double *JR, const double *qL, const double *qR, const double *n,
+                           double gamma) {
+  const double one = 1, two = 2, three = 3, half = one / two, es = 1.e-30;
+  const double gm1 = gamma - one;
+  if (nd == 3) {
+    const double rL = qL[0], uL = qL[1] / (rL + es);
+    const double pL = gm1 * (qL[2] - half * rL * (uL * uL));
+    const double HL = (qL[2] + pL) / rL;
+    const double aL = sqrt(gm1 * (HL - half * (uL * uL)));
+    const double rR = qR[0], uR = qR[1] / (rR + es);
+    const double pR = gm1 * (qR[2] - half * rR * (uR * uR));
+    const double HR = (qR[2] + pR) / rR;
+    const double aR = sqrt(gm1 * (HR - half * (uR * uR)));
+    const double r = sqrt(rR * rL), RT = sqrt(rR / (rL));
+    const double u = (uL + RT * uR) / (one + RT), H = (HL + RT * HR) / (one + RT);
+    const double a = sqrt(gm1 * (H - half * (u * u)));
+    const double smax = fabs(u) + a;
+    const double VMagSqrRoe = u * u + es, VMagSqrL = uL * uL, VVRoeL = uL * u, VMagSqrR = uR * uR, VVRoeR = uR * u;
+    const double uRelRoe = u / sqrt(VMagSqrRoe);
+    double gL[3], gR[3];
+    gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe + half * gm1 / a * (half * (VMagSqrRoe + VVRoeL) + half * (HL - H) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
+    gL[1] = one / (rL + r) * (uRelRoe - half * (gm1 * (u + gm1 * uL)) / (a));
+    gL[2] = half / (rL + r) * gamma * gm1 / (a);
+    gR[0] = one / (rR + r) * (-half * (uR + u) * uRelRoe + half * gm1 / a * (half * (VMagSqrRoe + VVRoeR) + half * (HR - H) - aR * aR / gm1 + half * (gamma - two) * VMagSqrR));
+    gR[1] = one / (rR + r) * (uRelRoe - half * (gm1 * (u + gm1 * uR)) / (a));
+    gR[2] = half / (rR + r) * gamma * gm1 / (a);
+    double *Js[2] = {JL, JR};
+    const double *gs[2] = {gL, gR};
+    const double us[2] = {uL, uR}, Hs[2] = {HL, HR};
+    for (int side = 0; side < 2; ++side) {
+      double *J = Js[side];
+      const double uX = us[side], HX = Hs[side];
+      J[0] = 0; J[1] = half; J[2] = 0;
+      J[3] = half * (half * gm1 * uX * uX - uX * uX);
+      J[4] = half * ((three - gamma) * uX);
+      J[5] = half * gm1;
+      J[6] = half * ((half * gm1 * uX * uX - HX) * uX);
+      J[7] = half * (HX - gm1 * uX * uX);
+      J[8] = half * gamma * uX;
+      for (int i = 0; i < 3; i++) {
+        if (side == 0) J[i * 3 + i] += half * smax;
+        else J[i * 3 + i] -= half * smax;
+        for (int j = 0; j < 3; j++) J[i * 3 + j] += half * gs[side][j] * (qL[i] - qR[i]);
+      }
+    }
+    return;
+  }
+  const int nv = nd - 2;
+  double vL[3] = {0, 0, 0}, vR[3] = {0, 0, 0}, v[3] = {0, 0, 0};
+  const double rL = qL[0], rR = qR[0];
+  for (int k = 0; k < nv; ++k) { vL[k] = qL[1 + k] / (rL + es); vR[k] = qR[1 + k] / (rR + es); }
+  double unL, unR, ksL, ksR;
+  if (nv == 2) {
+    unL = vL[0] * n[0] + vL[1] * n[1]; unR = vR[0] * n[0] + vR[1] * n[1];
+    ksL = vL[0] * vL[0] + vL[1] * vL[1]; ksR = vR[0] * vR[0] + vR[1] * vR[1];
+  } else {
+    unL = vL[0] * n[0] + vL[1] * n[1] + vL[2] * n[2]; unR = vR[0] * n[0] + vR[1] * n[1] + vR[2] * n[2];
+    ksL = vL[0] * vL[0] + vL[1] * vL[1] + vL[2] * vL[2]; ksR = vR[0] * vR[0] + vR[1] * vR[1] + vR[2] * vR[2];
+  }
+  const double pL = gm1 * (qL[nd - 1] - half * rL * (ksL));
+  const double HL = (qL[nd - 1] + pL) / rL;
+  const double aL = sqrt(gm1 * (HL - half * (ksL)));
+  const double pR = gm1 * (qR[nd - 1] - half * rR * (ksR));
+  const double HR = (qR[nd - 1] + pR) / rR;
+  const double aR = sqrt(gm1 * (HR - half * (ksR)));
+  const double r = sqrt(rR * rL), RT = sqrt(rR / (rL));
+  for (int k = 0; k < nv; ++k) v[k] = (vL[k] + RT * vR[k]) / (one + RT);
+  const double H = (HL + RT * HR) / (one + RT);
+  double ks, VMagSqrRoe, VVRoeL, VVRoeR;
+  if (nv == 2) {
+    ks = v[0] * v[0] + v[1] * v[1];
+    VMagSqrRoe = v[0] * v[0] + v[1] * v[1] + es;
+    VVRoeL = vL[0] * v[0] + vL[1] * v[1];
+    VVRoeR = vR[0] * v[0] + vR[1] * v[1];
+  } else {
+    ks = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    VMagSqrRoe = v[0] * v[0] + v[1] * v[1] + v[2] * v[2] + es;
+    VVRoeL = vL[0] * v[0] + vL[1] * v[1] + vL[2] * v[2];
+    VVRoeR = vR[0] * v[0] + vR[1] * v[1] + vR[2] * v[2];
+  }
+  const double a = sqrt(gm1 * (H - half * (ks)));
+  const double smax = sqrt(ks) + a;
+  double rel[3];
+  for (int k = 0; k < nv; ++k) rel[k] = v[k] / sqrt(VMagSqrRoe);
+  double gL[5], gR[5];
+  {
+    double sL = -half * (vL[0] + v[0]) * rel[0] - half * (vL[1] + v[1]) * rel[1];
+    double sR = -half * (vR[0] + v[0]) * rel[0] - half * (vR[1] + v[1]) * rel[1];
+    if (nv == 3) {
+      sL = sL - half * (vL[2] + v[2]) * rel[2];
+      sR = sR - half * (vR[2] + v[2]) * rel[2];
+    }
+    gL[0] = one / (rL + r) * (sL + half * gm1 / a * (half * (VMagSqrRoe + VVRoeL) + half * (HL - H) - aL * aL / gm1 + half * (gamma - two) * ksL));
+    gR[0] = one / (rR + r) * (sR + half * gm1 / a * (half * (VMagSqrRoe + VVRoeR) + half * (HR - H) - aR * aR / gm1 + half * (gamma - two) * ksR));
+    for (int k = 0; k < nv; ++k) {
+      gL[1 + k] = one / (rL + r) * (rel[k] - half * (gm1 * (v[k] + gm1 * vL[k])) / (a));
+      gR[1 + k] = one / (rR + r) * (rel[k] - half * (gm1 * (v[k] + gm1 * vR[k])) / (a));
+    }
+    gL[nd - 1] = half / (rL + r) * gamma * gm1 / (a);
+    gR[nd - 1] = half / (rR + r) * gamma * gm1 / (a);
+  }
+  double *Js[2] = {JL, JR};
+  const double *gs[2] = {gL, gR};
+  const double *vs[2] = {vL, vR};
+  const double uns[2] = {unL, unR}, Hs[2] = {HL, HR}, kss[2] = {ksL, ksR};
+  for (int side = 0; side < 2; ++side) {
+    double *J = Js[side];
+    const double *vX = vs[side];
+    const double unX = uns[side], HX = Hs[side], VMagSqrX = kss[side];
+    J[0] = 0;
+    for (int k = 0; k < nv; ++k) J[1 + k] = half * n[k];
+    J[nd - 1] = 0;
+    for (int row = 0; row < nv; ++row) {
+      J[(1 + row) * nd + 0] = half * (half * gm1 * VMagSqrX * n[row] - vX[row] * unX);
+      for (int col = 0; col < nv; ++col) {
+        if (col == row) J[(1 + row) * nd + 1 + col] = half * (vX[row] * n[row] - gm1 * vX[row] * n[row] + unX);
+        else J[(1 + row) * nd + 1 + col] = half * (vX[row] * n[col] - gm1 * vX[col] * n[row]);
+      }
+      J[(1 + row) * nd + nd - 1] = half * gm1 * n[row];
+    }
+    J[(nd - 1) * nd + 0] = half * ((half * gm1 * VMagSqrX - HX) * unX);
+    for (int k = 0; k < nv; ++k) J[(nd - 1) * nd + 1 + k] = half * (HX * n[k] - gm1 * vX[k] * unX);
+    J[(nd - 1) * nd + nd - 1] = half * gamma * unX;
+    for (int i = 0; i < nd; i++) {
+      if (side == 0) J[i * nd + i] += half * smax;
+      else J[i * nd + i] -= half * smax;
+      for (int j = 0; j < nd; j++) J[i * nd + j] += half * gs[side][j] * (qL[i] - qR[i]);
+    }
+  }
+}
+
+static void swe_flux_jac(double *JL, double *JR, const double *qL, const double *qR, const double *n, double g) {
+  const double es = 1.e-30;
+  const double hL = qL[0], uL = qL[1] / (hL + es), vL = qL[2] / (hL + es);
+  const double unL = uL * n[0] + vL * n[1];
+  const double hR = qR[0], uR = qR[1] / (hR + es), vR = qR[2] / (hR + es);
+  const double unR = uR * n[0] + vR * n[1];
+  const double hm = 0.5 * (hL + hR);
+  const double um = (unL * pow(hL, 0.5) + unR * pow(hR, 0.5)) / (pow(hL, 0.5) + pow(hR, 0.5) + es);
+  const double smax = fabs(um) + fabs(pow(g * hm, 0.5));
+  const double termL = (n[0] * qL[1] + n[1] * qL[2]) / pow(qL[0], 2.);
+  const double termR = (n[0] * qR[1] + n[1] * qR[2]) / pow(qR[0], 2.);
+  const double hL_sqrt = pow(hL, 0.5), hR_sqrt = pow(hR, 0.5);
+  const double hsqrt_un = hL_sqrt * unL + hR_sqrt * unR + es;
+  double dL[3], dR[3];
+  dL[0] = -fabs(hsqrt_un) / (2. * hL_sqrt * pow(hL_sqrt + hR_sqrt, 2.)) +
+          (0.5 * unL / hL_sqrt - hL_sqrt * termL) * hsqrt_un / ((hL_sqrt + hR_sqrt) * fabs(hsqrt_un)) +
+          g / (pow(2., 3. / 2.) * pow(g * (hL + hR), 0.5));
+  dL[1] = n[0] * hsqrt_un / (hL_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
+  dL[2] = n[1] * hsqrt_un / (hL_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
+  dR[0] = -fabs(hsqrt_un) / (2. * hR_sqrt * pow(hL_sqrt + hR_sqrt, 2.)) +
+          (0.5 * unR / hR_sqrt - hR_sqrt * termR) * hsqrt_un / ((hL_sqrt + hR_sqrt) * fabs(hsqrt_un)) +
+          g / (pow(2., 3. / 2.) * pow(g * (hL + hR), 0.5));
+  dR[1] = n[0] * hsqrt_un / (hR_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
+  dR[2] = n[1] * hsqrt_un / (hR_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
+  JL[0] = -0.5 * dL[0] * (qR[0] - qL[0]) + 0.5 * (n[0] * uL + n[1] * vL - qL[0] * termL) + 0.5 * smax;
+  JL[1] = 0.5 * n[0] - 0.5 * dL[1] * (qR[0] - qL[0]);
+  JL[2] = 0.5 * n[1] - 0.5 * dL[2] * (qR[0] - qL[0]);
+  JL[3] = 0.5 * (g * n[0] * qL[0] - qL[1] * termL) - 0.5 * dL[0] * (qR[1] - qL[1]);
+  JL[4] = n[0] * uL + 0.5 * n[1] * vL + 0.5 * smax - 0.5 * dL[1] * (qR[1] - qL[1]);
+  JL[5] = 0.5 * n[1] * uL - 0.5 * dL[2] * (qR[1] - qL[1]);
+  JL[6] = 0.5 * (g * n[1] * qL[0] - qL[2] * termL) - 0.5 * dL[0] * (qR[2] - qL[2]);
+  JL[7] = 0.5 * n[0] * vL - 0.5 * dL[1] * (qR[2] - qL[2]);
+  JL[8] = n[1] * vL + 0.5 * n[0] * uL + 0.5 * smax - 0.5 * dL[2] * (qR[2] - qL[2]);
+  JR[0] = -0.5 * dR[0] * (qR[0] - qL[0]) + 0.5 * (n[0] * uR + n[1] * vR - qR[0] * termR) - 0.5 * smax;
+  JR[1] = 0.5 * n[0] - 0.5 * dR[1] * (qR[0] - qL[0]);
+  JR[2] = 0.5 * n[1] - 0.5 * dR[2] * (qR[0] - qL[0]);
+  JR[3] = 0.5 * (g * n[0] * qR[0] - qR[1] * termR) - 0.5 * dR[0] * (qR[1] - qL[1]);
+  JR[4] = n[0] * uR + 0.5 * n[1] * vR - 0.5 * smax - 0.5 * dR[1] * (qR[1] - qL[1]);
+  JR[5] = 0.5 * n[1] * uR - 0.5 * dR[2] * (qR[1] - qL[1]);
+  JR[6] = 0.5 * (g * n[1] * qR[0] - qR[2] * termR) - 0.5 * dR[0] * (qR[2] - qL[2]);
+  JR[7] = 0.5 * n[0] * vR - 0.5 * dR[1] * (qR[2] - qL[2]);
+  JR[8] = n[1] * vR + 0.5 * n[0] * uR - 0.5 * smax - 0.5 * dR[2] * (qR[2] - qL[2]);
+}
+
+/* ---------------------------------------------------------------- problem */
+enum { E1 = 0, E2 = 1, E3 = 2, SW = 3 };
+
+struct orc_problem {
+  const orc_mesh *m;
+  int fam, prob, scheme, ic, nd, dim, h, stencil;
+  double icp[10], gamma, gravity, coriolis;
+  int32_t *rowptr, *colidx;
+  int64_t nnz;
+  int patternReady;
+};
+
+/* graph column of the neighbour at distance k+1 on the minus/plus side of axis ax */
+static int colm(int dim, int ax, int k) {
+  if (dim == 1) return 1 + 2 * k;
+  if (dim == 2) return (ax == 0 ? 1 : 4) + 4 * k;
+  return (ax == 0 ? 1 : ax == 1 ? 4 : 5) + 6 * k;
+}
+static int colp(int dim, int ax, int k) {
+  if (dim == 1) return 2 + 2 * k;
+  if (dim == 2) return (ax == 0 ? 3 : 2) + 4 * k;
+  return (ax == 0 ? 3 : ax == 1 ? 2 : 6) + 6 * k;
+}
+
+/* Ghost values of one near-boundary row for the scheme stencil stSz: ghost
+ * array [side][layer][dof] with sides (minus, plus) per axis. */
+static void fill_ghosts(const orc_problem *p, int64_t r, const double *U, double *gh, int stSz) {
+  const orc_mesh *m = p->m;
+  const int nd = p->nd, L = (stSz - 1) / 2;
+  const int cell = G(m, r, 0);
+  for (int ax = 0; ax < p->dim; ++ax) {
+    for (int side = 0; side < 2; ++side) {
+      double *g = gh + ((size_t)(ax * 2 + side)) * (size_t)(L > 0 ? L : 1) * nd;
+      const int minus = side == 0;
+      int same[3], opp[3];
+      for (int k = 0; k < 3; ++k) {
+        same[k] = (k < (m->stencil - 1) / 2) ? G(m, r, minus ? colm(p->dim, ax, k) : colp(p->dim, ax, k)) : 0;
+        opp[k] = (k < (m->stencil - 1) / 2) ? G(m, r, minus ? colp(p->dim, ax, k) : colm(p->dim, ax, k)) : 0;
+      }
+      for (int layer = 0; layer < L; ++layer) {
+        if (same[layer] != -1) continue;
+        int src = cell;
+        if (p->fam == E1) {
+          /* Ghost1dNeumannFiller */
+          src = layer == 0 ? cell : opp[layer - 1];
+        } else {
+          /* Ghost2dNeumannFiller / InviscidWallFiller */
+          if (layer == 0) src = cell;
+          else if (layer == 1) src = (same[0] == -1) ? opp[0] : same[0];
+          else {
+            src = cell;
+            if (same[1] != -1 && same[0] != -1) src = same[1];
+            if (same[1] == -1 && same[0] != -1) src = cell;
+            if (same[1] == -1 && same[0] == -1) src = opp[1];
+          }
+        }
+        for (int d = 0; d < nd; ++d) {
+          double v = U[(int64_t)src * nd + d];
+          if (p->fam == SW && d == (ax == 0 ? 1 : 2)) v = -v;
+          g[layer * nd + d] = v;
+        }
+      }
+    }
+  }
+}
+
+/* stencil values (positions -h..h) for one axis of row r: st[(s)*nd + d] */
+static void fill_stencil(const orc_problem *p, int64_t r, int ax, int h, const double *U, const double *gh,
+                         int L, double *st) {
+  const orc_mesh *m = p->m;
+  const int nd = p->nd;
+  const int cell = G(m, r, 0);
+  for (int d = 0; d < nd; ++d) st[h * nd + d] = U[(int64_t)cell * nd + d];
+  for (int k = 1; k <= h; ++k) {
+    const int cm = G(m, r, colm(p->dim, ax, k - 1)), cp = G(m, r, colp(p->dim, ax, k - 1));
+    for (int d = 0; d < nd; ++d) {
+      st[(h - k) * nd + d] = (cm == -1) ? gh[((ax * 2 + 0) * L + (k - 1)) * nd + d] : U[(int64_t)cm * nd + d];
+      st[(h + k) * nd + d] = (cp == -1) ? gh[((ax * 2 + 1) * L + (k - 1)) * nd + d] : U[(int64_t)cp * nd + d];
+    }
+  }
+}
+
+static void normal_of(int dim, int ax, double *n) {
+  n[0] = n[1] = n[2] = 0;
+  n[ax] = 1;
+  (void)dim;
+}
+
+static void flux(const orc_problem *p, int ax, double *F, const double *qL, const double *qR) {
+  double n[3];
+  normal_of(p->dim, ax, n);
+  if (p->fam == SW) swe_flux(F, qL, qR, n, p->gravity);
+  else euler_flux(p->nd, F, qL, qR, n, p->gamma);
+}
+
+static void flux_jac(const orc_problem *p, int ax, double *JL, double *JR, const double *qL, const double *qR) {
+  double n[3];
+  normal_of(p->dim, ax, n);
+  if (p->fam == SW) swe_flux_jac(JL, JR, qL, qR, n, p->gravity);
+  else euler_flux_jac(p->nd, JL, JR, qL, qR, n, p->gamma);
+}
+
+/* reconstruct the face between stencil positions c-1 and c (values only) */
+static void recon(int scheme, int nd, const double *st, int c, double *uN, double *uP) {
+  for (int d = 0; d < nd; ++d) {
+    if (scheme == 0) {
+      uN[d] = st[(c - 1) * nd + d];
+      uP[d] = st[c * nd + d];
+    } else if (scheme == 1) {
+      weno3_impl(&uN[d], &uP[d], st[(c - 2) * nd + d], st[(c - 1) * nd + d], st[c * nd + d], st[(c + 1) * nd + d]);
+    } else {
+      weno5_impl(&uN[d], &uP[d], st[(c - 3) * nd + d], st[(c - 2) * nd + d], st[(c - 1) * nd + d],
+                 st[c * nd + d], st[(c + 1) * nd + d], st[(c + 2) * nd + d]);
+    }
+  }
+}
+
+/* with gradients: gN/gP [nd][2h] */
+static void recon_grad(int scheme, int nd, const double *st, int c, double *uN, double *uP, double *gN,
+                       double *gP) {
+  const int G2 = 2 * (scheme + 1);
+  for (int d = 0; d < nd; ++d) {
+    if (scheme == 0) {
+      uN[d] = st[(c - 1) * nd + d];
+      uP[d] = st[c * nd + d];
+      gN[d * G2 + 0] = 1; gN[d * G2 + 1] = 0;
+      gP[d * G2 + 0] = 0; gP[d * G2 + 1] = 1;
+    } else if (scheme == 1) {
+      weno3_grad_impl(&uN[d], &uP[d], gN + d * G2, gP + d * G2, st[(c - 2) * nd + d], st[(c - 1) * nd + d],
+                      st[c * nd + d], st[(c + 1) * nd + d]);
+    } else {
+      weno5_grad_impl(&uN[d], &uP[d], gN + d * G2, gP + d * G2, st[(c - 3) * nd + d], st[(c - 2) * nd + d],
+                      st[(c - 1) * nd + d], st[c * nd + d], st[(c + 1) * nd + d], st[(c + 2) * nd + d]);
+    }
+  }
+}
+
+static int cmp_i32(const void *a, const void *b) {
+  const int32_t x = *(const int32_t *)a, y = *(const int32_t *)b;
+  return (x > y) - (x < y);
+}
+
+/* initializeJacobian: per row self + neighbours, sorted distinct */
+static void build_pattern(orc_problem *p) {
+  if (p->patternReady) return;
+  const orc_mesh *m = p->m;
+  const int nd = p->nd;
+  char *near = calloc(m->nsm, 1);
+  for (int64_t e = 0; e < m->nnear; ++e) near[m->nearbd[e]] = 1;
+  int32_t *nb = malloc(sizeof(int32_t) * m->nsm * 20);
+  int *cnt = malloc(sizeof(int) * m->nsm);
+  int64_t nnz = 0;
+  for (int64_t r = 0; r < m->nsm; ++r) {
+    int32_t *b = nb + r * 20;
+    int c = 0;
+    b[c++] = G(m, r, 0);
+    if (near[r]) {
+      for (int i = 1; i <= 2 * p->dim; ++i)
+        if (G(m, r, i) != -1) b[c++] = G(m, r, i);
+    } else {
+      for (int i = 1; i <= 2 * p->dim * p->h; ++i) b[c++] = G(m, r, i);
+    }
+    qsort(b, c, sizeof(int32_t), cmp_i32);
+    int u = 0;
+    for (int i = 0; i < c; ++i)
+      if (u == 0 || b[i] != b[u - 1]) b[u++] = b[i];
+    cnt[r] = u;
+    nnz += (int64_t)u * nd * nd;
+  }
+  p->nnz = nnz;
+  p->rowptr = malloc(sizeof(int32_t) * (m->nsm * nd + 1));
+  p->colidx = malloc(sizeof(int32_t) * (nnz > 0 ? nnz : 1));
+  int64_t q = 0;
+  for (int64_t r = 0; r < m->nsm; ++r)
+    for (int k = 0; k < nd; ++k) {
+      p->rowptr[r * nd + k] = (int32_t)q;
+      for (int i = 0; i < cnt[r]; ++i)
+        for (int j = 0; j < nd; ++j) p->colidx[q++] = nb[r * 20 + i] * nd + j;
+    }
+  p->rowptr[m->nsm * nd] = (int32_t)q;
+  free(near); free(nb); free(cnt);
+  p->patternReady = 1;
+}
+
+static int find_col(const orc_problem *p, int64_t row, int32_t col) {
+  int lo = p->rowptr[row], hi = p->rowptr[row + 1] - 1;
+  while (lo <= hi) {
+    const int mid = (lo + hi) / 2;
+    if (p->colidx[mid] == col) return mid;
+    if (p->colidx[mid] < col) lo = mid + 1;
+    else hi = mid - 1;
+  }
+  return -1;
+}
+
+/* coeffRef(row, col) += v */
+#define JADD(row, col, v) vals[find_col(p, (row), (col))] += (v)
+
+orc_problem *orc_problem_create(const orc_mesh *m, int family, int problem, int scheme, int icflag, int np,
+                                const char *const *names, const double *vals) {
+  orc_problem *p = calloc(1, sizeof *p);
+  p->m = m;
+  p->fam = family;
+  p->prob = problem;
+  p->scheme = scheme;
+  p->ic = icflag <= 0 ? 1 : icflag;
+  p->nd = family == E1 ? 3 : family == E2 ? 4 : family == E3 ? 5 : 3;
+  p->dim = family == E1 ? 1 : family == E3 ? 3 : 2;
+  p->h = scheme + 1;
+  p->stencil = 2 * p->h + 1;
+  p->gamma = 1.4;
+  p->gravity = 9.8;
+  p->coriolis = -3.;
+  if (family == E2) {
+    const double d[10] = {9, 0.1, 10., 1., 0.4, 1.5, 0.0, 0.0, 1.5, 0.029};
+    memcpy(p->icp, d, sizeof d);
+  } else if (family == SW) {
+    const double d[9] = {1. / 8, 1, 1, 1. / 10, -2, -2, 1. / 8, 2, 2};
+    memcpy(p->icp, d, sizeof d);
+  }
+  for (int i = 0; i < np; ++i) {
+    const char *s = names[i];
+    const double v = vals[i];
+    if (family == E2) {
+      if (!strcmp(s, "gamma")) p->gamma = v;
+      else if (!strcmp(s, "riemannTopRightPressure")) p->icp[p->ic == 1 ? 4 : 5] = v;
+      else if (!strcmp(s, "riemannTopRightXVel")) p->icp[6] = v;
+      else if (!strcmp(s, "riemannTopRightYVel")) p->icp[7] = v;
+      else if (!strcmp(s, "riemannTopRightDensity")) p->icp[8] = v;
+      else if (!strcmp(s, "riemannBotLeftPressure")) p->icp[9] = v;
+      else { seterr("unknown parameter"); free(p); return NULL; }
+    } else if (family == SW) {
+      static const char *nm[9] = {"pulseMagnitude", "pulseX", "pulseY", "pulseMagnitude1", "pulseX1",
+                                  "pulseY1", "pulseMagnitude2", "pulseX2", "pulseY2"};
+      if (!strcmp(s, "gravity")) { p->gravity = v; continue; }
+      if (!strcmp(s, "coriolis")) { p->coriolis = v; continue; }
+      int k = -1;
+      for (int j = 0; j < 9; ++j)
+        if (!strcmp(s, nm[j])) k = j;
+      if (k < 0) { seterr("unknown parameter"); free(p); return NULL; }
+      p->icp[k] = v;
+    } else {
+      seterr("no parameters for this family");
+      free(p);
+      return NULL;
+    }
+  }
+  return p;
+}
+
+void orc_problem_free(orc_problem *p) {
+  if (!p) return;
+  free(p->rowptr);
+  free(p->colidx);
+  free(p);
+}
+
+void orc_sizes(const orc_problem *p, int64_t out[4]) {
+  build_pattern((orc_problem *)p);
+  out[0] = p->nd;
+  out[1] = p->m->nsm * p->nd;
+  out[2] = p->m->nst * p->nd;
+  out[3] = p->nnz;
+}
+
+static double energy(double gm1inv, const double *prim, int n) {
+  const double one = 1, two = 2, half = one / two;
+  if (n == 3) return prim[2] * gm1inv + half * prim[0] * (prim[1] * prim[1]);
+  if (n == 4) return prim[3] * gm1inv + half * prim[0] * (prim[1] * prim[1] + prim[2] * prim[2]);
+  return prim[4] * gm1inv + half * prim[0] * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3]);
+}
+
+void orc_initial_condition(const orc_problem *p, double *U) {
+  const orc_mesh *m = p->m;
+  const double *x = m->x, *y = m->y, *z = m->z;
+  const int nd = p->nd;
+  memset(U, 0, sizeof(double) * m->nst * nd);
+  if (p->fam == E1) {
+    const double gm1inv = 1. / (p->gamma - 1.);
+    double prim[3] = {0, 0, 0};
+    for (int64_t i = 0; i < m->nst; ++i) {
+      if (p->prob == 0) { prim[0] = 1 + 0.2 * sin(M_PI * x[i]); prim[1] = 1; prim[2] = 1; }
+      else if (p->prob == 1) {
+        if (x[i] <= 0) { prim[0] = 1; prim[1] = 0; prim[2] = 1; }
+        if (x[i] > 0) { prim[0] = 0.125; prim[1] = 0; prim[2] = 0.1; }
+      } else if (p->prob == 2) {
+        if (x[i] <= 0) { prim[0] = 0.445; prim[1] = 0.698; prim[2] = 3.528; }
+        else if (x[i] > 0) { prim[0] = 0.5; prim[1] = 0; prim[2] = 0.571; }
+      } else {
+        if (x[i] <= -4.) { prim[0] = 27. / 7.; prim[1] = 2.629369; prim[2] = 31. / 3.; }
+        else { prim[0] = 1. + (1. / 5.) * sin(5. * x[i]); prim[1] = 0; prim[2] = 1; }
+      }
+      U[i * 3] = prim[0];
+      U[i * 3 + 1] = prim[0] * prim[1];
+      U[i * 3 + 2] = energy(gm1inv, prim, 3);
+    }
+  } else if (p->fam == E2) {
+    const double gamma = p->gamma, gm1inv = 1. / (gamma - 1.);
+    double prim[4] = {0, 0, 0, 0};
+    double st[4][4];
+    double x0 = 0.5, y0 = 0.5;
+    if (p->prob == 4 && p->ic == 2) {
+      const double pTR = p->icp[5], uTR = p->icp[6], vTR = p->icp[7], rTR = p->icp[8], pBL = p->icp[9];
+      const double one = 1, two = 2, four = 4;
+      const double eps = (gamma - one) / (gamma + one);
+      const double fac13 = pTR / pBL;
+      const double fac43 = (one / (two * (one + two * eps))) * (eps * (fac13 + one) + sqrt(pow(eps * (fac13 + one), 2) + four * (one + two * eps) * fac13));
+      const double pTL = fac43 * pBL, pBR = pTL, vTL = vTR, uBR = uTR;
+      const double rTL = rTR * (pTL / pTR + eps) / (1 + eps * pTL / rTR), rBR = rTL;
+      const double psi21 = (pTL - pTR) * (rTL - rTR) / (rTL * rTR);
+      const double uTL = sqrt(psi21) + uTR;
+      const double psi41 = (pBR - pTR) * (rBR - rTR) / (rBR * rTR);
+      const double vBR = sqrt(psi41) + vTR;
+      const double rBL = rTL * (pBL - pTL) / ((pBL - pTL) - psi41 * rTL);
+      const double a[4][4] = {{rTR, uTR, vTR, pTR}, {rTL, uTL, vTL, pTL}, {rBL, uTL, vBR, pBL}, {rBR, uBR, vBR, pBR}};
+      memcpy(st, a, sizeof a);
+      x0 = 0.8; y0 = 0.8;
+    } else if (p->prob == 4) {
+      const double a[4][4] = {{0.5313, 0, 0, p->icp[4]}, {1, 0.7276, 0, 1}, {0.8, 0, 0, 1}, {1, 0, 0.7276, 1}};
+      memcpy(st, a, sizeof a);
+    }
+    for (int64_t i = 0; i < m->nst; ++i) {
+      if (p->prob == 0) {
+        prim[0] = 1 + (1. / 5.) * sin(M_PI * (x[i] + y[i]));
+        prim[1] = prim[2] = prim[3] = 1;
+      } else if (p->prob == 4) {
+        int q = -1;
+        if (x[i] >= x0 && y[i] >= y0) q = 0;
+        else if (x[i] < x0 && y[i] >= y0) q = 1;
+        else if (x[i] < x0 && y[i] < y0) q = 2;
+        else if (x[i] > x0 && y[i] < y0) q = 3;
+        if (q >= 0) memcpy(prim, st[q], sizeof prim);
+      } else {
+        continue;
+      }
+      U[i * 4] = prim[0];
+      U[i * 4 + 1] = prim[0] * prim[1];
+      U[i * 4 + 2] = prim[0] * prim[2];
+      U[i * 4 + 3] = energy(gm1inv, prim, 4);
+    }
+  } else if (p->fam == E3) {
+    const double gm1inv = 1. / (p->gamma - 1.);
+    double prim[5];
+    for (int64_t i = 0; i < m->nst; ++i) {
+      prim[0] = 1.0 + 0.2 * sin(M_PI * (x[i] + y[i] + z[i]));
+      prim[1] = prim[2] = prim[3] = 1.0;
+      prim[4] = 1.;
+      for (int d = 0; d < 4; ++d) U[i * 5 + d] = prim[0] * (d == 0 ? 1. : prim[d]);
+      U[i * 5] = prim[0];
+      U[i * 5 + 4] = energy(gm1inv, prim, 5);
+    }
+  } else {
+    const double *c = p->icp;
+    for (int64_t i = 0; i < m->nst; ++i) {
+      if (p->ic == 1) {
+        const double dx1 = x[i] - c[1], dy1 = y[i] - c[2];
+        const double r = sqrt(dx1 * dx1 + dy1 * dy1);
+        U[i * 3] = 1. + c[0] * exp(-(r * r));
+      } else {
+        const double dx1 = x[i] - c[4], dy1 = y[i] - c[5], r1 = sqrt(dx1 * dx1 + dy1 * dy1);
+        const double dx2 = x[i] - c[7], dy2 = y[i] - c[8], r2 = sqrt(dx2 * dx2 + dy2 * dy2);
+        U[i * 3] = 1. + c[3] * exp(-(r1 * r1)) + c[6] * exp(-(r2 * r2));
+      }
+      U[i * 3 + 1] = 0;
+      U[i * 3 + 2] = 0;
+    }
+  }
+}
+
+/* --------------------------------------------------------------- velocity */
+static void row_velocity(const orc_problem *p, int64_t r, const double *U, double *V, double *gh, int isNear) {
+  const orc_mesh *m = p->m;
+  const int nd = p->nd, h = p->h, S = 2 * h + 1;
+  double st[7 * 5], uN[5], uP[5], fL[5], fR[5];
+  if (isNear) fill_ghosts(p, r, U, gh, p->stencil);
+  for (int d = 0; d < nd; ++d) V[r * nd + d] = 0.;
+  for (int ax = 0; ax < p->dim; ++ax) {
+    fill_stencil(p, r, ax, h, U, gh, h, st);
+    recon(p->scheme, nd, st, h, uN, uP);
+    flux(p, ax, fL, uN, uP);
+    recon(p->scheme, nd, st, h + 1, uN, uP);
+    flux(p, ax, fR, uN, uP);
+    for (int d = 0; d < nd; ++d) V[r * nd + d] += m->dxi[ax] * (fL[d] - fR[d]);
+  }
+  (void)S;
+  if (p->fam == SW) {
+    const int64_t u = (int64_t)G(m, r, 0) * 3;
+    V[r * 3 + 1] -= p->coriolis * U[u + 2] / U[u];
+    V[r * 3 + 2] += p->coriolis * U[u + 1] / U[u];
+  }
+}
+
+void orc_velocity(orc_problem *p, const double *U, double t, double *V) {
+  const orc_mesh *m = p->m;
+  (void)t;
+#pragma omp parallel
+  {
+    double gh[3 * 2 * 3 * 5];
+#pragma omp for schedule(static)
+    for (int64_t e = 0; e < m->nnear; ++e) row_velocity(p, m->nearbd[e], U, V, gh, 1);
+#pragma omp for schedule(static)
+    for (int64_t e = 0; e < m->ninner; ++e) row_velocity(p, m->inner[e], U, V, gh, 0);
+  }
+}
+
+/* ------------------------------------------------------ velocity + jacobian */
+static void row_vj_inner(const orc_problem *p, int64_t r, const double *U, double *V, double *vals) {
+  const orc_mesh *m = p->m;
+  const int nd = p->nd, h = p->h, G2 = 2 * h;
+  double st[7 * 5], uN[5], uP[5], fL[5], fR[5];
+  double gLN[5 * 6], gLP[5 * 6], gRN[5 * 6], gRP[5 * 6];
+  double JLN[25], JLP[25], JRN[25], JRP[25];
+  for (int d = 0; d < nd; ++d) V[r * nd + d] = 0.;
+  for (int ax = 0; ax < p->dim; ++ax) {
+    const double hinv = m->dxi[ax];
+    fill_stencil(p, r, ax, h, U, NULL, 1, st);
+    recon_grad(p->scheme, nd, st, h, uN, uP, gLN, gLP);
+    flux(p, ax, fL, uN, uP);
+    flux_jac(p, ax, JLN, JLP, uN, uP);
+    recon_grad(p->scheme, nd, st, h + 1, uN, uP, gRN, gRP);
+    flux(p, ax, fR, uN, uP);
+    flux_jac(p, ax, JRN, JRP, uN, uP);
+    /* column (cell) of stencil position s */
+    int32_t cols[7];
+    cols[h] = G(m, r, 0);
+    for (int k = 1; k <= h; ++k) {
+      cols[h - k] = G(m, r, colm(p->dim, ax, k - 1));
+      cols[h + k] = G(m, r, colp(p->dim, ax, k - 1));
+    }
+    for (int k = 0; k < nd; ++k) {
+      const int64_t row = r * nd + k;
+      for (int j = 0; j < nd; ++j) {
+        const double ln = JLN[k * nd + j], lp = JLP[k * nd + j], rn = JRN[k * nd + j], rp = JRP[k * nd + j];
+        if (p->scheme == 0) {
+          JADD(row, cols[0] * nd + j, ln * hinv);
+          JADD(row, cols[1] * nd + j, (lp - rn) * hinv);
+          JADD(row, cols[2] * nd + j, -rp * hinv);
+        } else {
+          for (int s = 0; s < G2; ++s) {
+            JADD(row, cols[s] * nd + j, ln * gLN[j * G2 + s] * hinv);
+            JADD(row, cols[s] * nd + j, lp * gLP[j * G2 + s] * hinv);
+          }
+          for (int s = 0; s < G2; ++s) {
+            JADD(row, cols[s + 1] * nd + j, -(rn * gRN[j * G2 + s] * hinv));
+            JADD(row, cols[s + 1] * nd + j, -(rp * gRP[j * G2 + s] * hinv));
+          }
+        }
+      }
+    }
+    for (int d = 0; d < nd; ++d) V[r * nd + d] += hinv * (fL[d] - fR[d]);
+  }
+  if (p->fam == SW) {
+    const int64_t c = (int64_t)G(m, r, 0) * 3;
+    V[r * 3 + 1] -= p->coriolis * U[c + 2] / U[c];
+    V[r * 3 + 2] += p->coriolis * U[c + 1] / U[c];
+    JADD(r * 3 + 1, c, p->coriolis * U[c + 2] / (U[c] * U[c]));
+    JADD(r * 3 + 1, c + 2, -p->coriolis / U[c]);
+    JADD(r * 3 + 2, c + 1, p->coriolis / U[c]);
+    JADD(r * 3 + 2, c, -p->coriolis * U[c + 1] / (U[c] * U[c]));
+  }
+}
+
+static void row_vj_near(const orc_problem *p, int64_t r, const double *U, double *V, double *vals, double *gh) {
+  const orc_mesh *m = p->m;
+  const int nd = p->nd, h = p->h;
+  double st[7 * 5], st1[3 * 5], uN[5], uP[5], fL[5], fR[5];
+  double JLN[25], JLP[25], JRN[25], JRP[25];
+  fill_ghosts(p, r, U, gh, p->stencil);
+  for (int d = 0; d < nd; ++d) V[r * nd + d] = 0.;
+  for (int ax = 0; ax < p->dim; ++ax) {
+    const double hinv = m->dxi[ax];
+    fill_stencil(p, r, ax, h, U, gh, h, st);
+    recon(p->scheme, nd, st, h, uN, uP);
+    flux(p, ax, fL, uN, uP);
+    recon(p->scheme, nd, st, h + 1, uN, uP);
+    flux(p, ax, fR, uN, uP);
+    for (int d = 0; d < nd; ++d) V[r * nd + d] += hinv * (fL[d] - fR[d]);
+    /* first-order Jacobian, ghost layer 0 of the same ghost arrays */
+    fill_stencil(p, r, ax, 1, U, gh, h, st1);
+    flux_jac(p, ax, JLN, JLP, st1, st1 + nd);
+    flux_jac(p, ax, JRN, JRP, st1 + nd, st1 + 2 * nd);
+    double fac[5] = {1, 1, 1, 1, 1};
+    if (p->fam == SW) fac[ax == 0 ? 1 : 2] = -1;
+    const int32_t l0 = G(m, r, colm(p->dim, ax, 0)), r0 = G(m, r, colp(p->dim, ax, 0)), ci = G(m, r, 0);
+    for (int k = 0; k < nd; ++k)
+      for (int j = 0; j < nd; ++j) JADD(r * nd + k, ci * nd + j, (JLP[k * nd + j] - JRN[k * nd + j]) * hinv);
+    if (l0 != -1)
+      for (int k = 0; k < nd; ++k)
+        for (int j = 0; j < nd; ++j) JADD(r * nd + k, l0 * nd + j, JLN[k * nd + j] * hinv);
+    if (r0 != -1)
+      for (int k = 0; k < nd; ++k)
+        for (int j = 0; j < nd; ++j) JADD(r * nd + k, r0 * nd + j, -JRP[k * nd + j] * hinv);
+    if (l0 == -1)
+      for (int k = 0; k < nd; ++k)
+        for (int j = 0; j < nd; ++j) JADD(r * nd + k, ci * nd + j, (fac[j] * JLN[k * nd + j]) * hinv);
+    if (r0 == -1)
+      for (int k = 0; k < nd; ++k)
+        for (int j = 0; j < nd; ++j) JADD(r * nd + k, ci * nd + j, (fac[j] * -JRP[k * nd + j]) * hinv);
+  }
+  if (p->fam == SW) {
+    const int64_t c = (int64_t)G(m, r, 0) * 3;
+    V[r * 3 + 1] -= p->coriolis * U[c + 2] / U[c];
+    V[r * 3 + 2] += p->coriolis * U[c + 1] / U[c];
+    JADD(r * 3 + 1, c, p->coriolis * U[c + 2] / (U[c] * U[c]));
+    JADD(r * 3 + 1, c + 2, -p->coriolis / U[c]);
+    JADD(r * 3 + 2, c + 1, p->coriolis / U[c]);
+    JADD(r * 3 + 2, c, -p->coriolis * U[c + 1] / (U[c] * U[c]));
+  }
+}
+
+void orc_velocity_and_jacobian(orc_problem *p, const double *U, double t, double *V, int32_t *rowptr,
+                               int32_t *colidx, double *vals) {
+  const orc_mesh *m = p->m;
+  (void)t;
+  build_pattern(p);
+  memcpy(rowptr, p->rowptr, sizeof(int32_t) * (m->nsm * p->nd + 1));
+  memcpy(colidx, p->colidx, sizeof(int32_t) * p->nnz);
+  memset(vals, 0, sizeof(double) * p->nnz);
+#pragma omp parallel
+  {
+    double gh[3 * 2 * 3 * 5];
+#pragma omp for schedule(static)
+    for (int64_t e = 0; e < m->nnear; ++e) row_vj_near(p, m->nearbd[e], U, V, vals, gh);
+#pragma omp for schedule(static)
+    for (int64_t e = 0; e < m->ninner; ++e) row_vj_inner(p, m->inner[e], U, V, vals);
+  }
+}
+
+/* --------------------------------------------------------------- steppers */
+void orc_ssprk3(orc_problem *p, double *U, double t0, double dt, int64_t nsteps) {
+  const int64_t n = p->m->nst * p->nd;
+  double *aux = malloc(sizeof(double) * n), *r = malloc(sizeof(double) * n);
+  double t = t0;
+  const double one = 1, three = 3, four = 4, two = 2;
+  const double oneOvThree = one / three, twoOvThree = two / three, threeOvFour = three / four, fourInv = one / four;
+  for (int64_t s = 0; s < nsteps; ++s) {
+    orc_velocity(p, U, t, r);
+    for (int64_t i = 0; i < n; ++i) aux[i] = U[i] + dt * r[i];
+    orc_velocity(p, aux, t + dt, r);
+    const double c1 = fourInv * dt;
+    for (int64_t i = 0; i < n; ++i) aux[i] = fourInv * aux[i] + threeOvFour * U[i] + c1 * r[i];
+    orc_velocity(p, aux, t + dt / two, r);
+    const double c2 = twoOvThree * dt;
+    for (int64_t i = 0; i < n; ++i) U[i] = oneOvThree * U[i] + twoOvThree * aux[i] + c2 * r[i];
+    t = t + dt;
+  }
+  free(aux);
+  free(r);
+}
+
+void orc_rk4(orc_problem *p, double *U, double t0, double dt, int64_t nsteps) {
+  const int64_t n = p->m->nst * p->nd;
+  double *aux = malloc(sizeof(double) * n), *r1 = malloc(sizeof(double) * n), *r2 = malloc(sizeof(double) * n),
+         *r3 = malloc(sizeof(double) * n), *r4 = malloc(sizeof(double) * n);
+  const double dt2 = dt / 2., dt6 = dt / (2. * 3.), dt3 = dt / 3.;
+  double t = t0;
+  for (int64_t s = 0; s < nsteps; ++s) {
+    orc_velocity(p, U, t, r1);
+    for (int64_t i = 0; i < n; ++i) aux[i] = U[i] + dt2 * r1[i];
+    orc_velocity(p, aux, t + dt2, r2);
+    for (int64_t i = 0; i < n; ++i) aux[i] = U[i] + dt2 * r2[i];
+    orc_velocity(p, aux, t + dt2, r3);
+    for (int64_t i = 0; i < n; ++i) aux[i] = U[i] + dt * r3[i];
+    orc_velocity(p, aux, t + dt, r4);
+    for (int64_t i = 0; i < n; ++i) U[i] = U[i] + dt6 * r1[i] + dt3 * r2[i] + dt3 * r3[i] + dt6 * r4[i];
+    t = t + dt;
+  }
+  free(aux); free(r1); free(r2); free(r3); free(r4);
+}
+
+int orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}

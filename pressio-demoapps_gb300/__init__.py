@@ -1,0 +1,519 @@
+"""GB300-native finite-volume residual / Jacobian engine with the
+pressio-demoapps problem API.
+
+This module is the Python face of ``libpda_gb300.so`` (C ABI declared in
+``include/pda_gb300.h``).  It mirrors the reference's Python bindings
+(src_py/main_binder.cc, adapter_py.hpp): ``load_cellcentered_uniform_mesh``,
+``create_problem``, and problem objects with ``initialCondition``,
+``createState``, ``createVelocity``/``createRightHandSide``, ``velocity``/
+``rightHandSide``, ``createJacobian``, ``jacobian``,
+``rightHandSideAndJacobian``, ``applyJacobian`` ... operating on CUDA tensors
+(float64) that stay resident on the GPU.  PyTorch supplies device memory and
+streams only; all arithmetic runs in the library's own CUDA kernels.
+
+There is no CPU fallback: if the shared library is missing the import of a
+problem fails with a RuntimeError naming the build step.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libpda_gb300.so")
+
+# ------------------------------------------------------------------- enums
+
+
+class Euler1d(enum.IntEnum):
+    PeriodicSmooth = 0
+    Sod = 1
+    Lax = 2
+    ShuOsher = 3
+
+
+class Euler2d(enum.IntEnum):
+    PeriodicSmooth = 0
+    KelvinHelmholtz = 1
+    SedovFull = 2
+    SedovSymmetry = 3
+    Riemann = 4
+    NormalShock = 5
+    DoubleMachReflection = 6
+    CrossShock = 7
+    testingonlyneumann = 8
+
+
+class Euler3d(enum.IntEnum):
+    PeriodicSmooth = 0
+    SedovSymmetry = 1
+
+
+class Swe2d(enum.IntEnum):
+    SlipWall = 0
+    CustomBCs = 1
+
+
+class InviscidFluxReconstruction(enum.IntEnum):
+    FirstOrder = 0
+    Weno3 = 1
+    Weno5 = 2
+
+
+class InviscidFluxScheme(enum.IntEnum):
+    Rusanov = 0
+
+
+_FAMILY = {Euler1d: 0, Euler2d: 1, Euler3d: 2, Swe2d: 3}
+
+# -------------------------------------------------------------- the library
+
+_lib = None
+
+_SIGS = {
+    "pda_last_error": (C.c_char_p, []),
+    "pda_version": (C.c_char_p, []),
+    "pda_mesh_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    "pda_mesh_create_full": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_int,
+                                       C.POINTER(C.c_int), C.POINTER(C.c_void_p)]),
+    "pda_mesh_create_sample": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.c_int64,
+                                         C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]),
+    "pda_mesh_write": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "pda_mesh_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int64),
+                                C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "pda_mesh_arrays": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_void_p]),
+    "pda_mesh_free": (None, [C.c_void_p]),
+    "pda_problem_create": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                     C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.c_int,
+                                     C.c_void_p, C.POINTER(C.c_void_p)]),
+    "pda_problem_create_swe_slip_wall": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double,
+                                                   C.c_double, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "pda_problem_free": (None, [C.c_void_p]),
+    "pda_problem_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int64),
+                                    C.POINTER(C.c_int64)]),
+    "pda_query_parameter": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_double)]),
+    "pda_initial_condition": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "pda_initial_condition_host": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "pda_velocity": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]),
+    "pda_velocity_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]),
+    "pda_jacobian_shape": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                     C.POINTER(C.c_int64)]),
+    "pda_jacobian_pattern": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "pda_jacobian_pattern_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "pda_velocity_and_jacobian": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
+                                            C.c_void_p]),
+    "pda_velocity_and_jacobian_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
+                                                 C.c_void_p]),
+    "pda_jacobian": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]),
+    "pda_apply_jacobian": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_int,
+                                     C.c_void_p]),
+    "pda_advance_ssprk3": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64,
+                                     C.c_int]),
+    "pda_advance_rk4": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64,
+                                  C.c_int]),
+    "pda_problem_launch_count": (C.c_int64, [C.c_void_p]),
+    "pda_profile_velocity": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                       C.POINTER(C.c_double)]),
+    "pda_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
+}
+
+
+def lib():
+    """Load libpda_gb300.so (built by build_lib.py); raise if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} not found: build it first (python -c 'import __graft_entry__ as g; g.build()')")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class PdaError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"pda error {code}: {msg}")
+        self.code = code
+
+
+def _check(rc):
+    if rc != 0:
+        raise PdaError(rc, lib().pda_last_error().decode())
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+# -------------------------------------------------------------------- meshes
+
+
+class CellCenteredUniformMesh:
+    """Mesh handle (mirror of pressiodemoapps.CellCenteredUniformMesh)."""
+
+    def __init__(self, handle):
+        self._h = C.c_void_p(handle) if not isinstance(handle, C.c_void_p) else handle
+        dims = (C.c_int * 3)()
+        sizes = (C.c_int64 * 4)()
+        dx = (C.c_double * 3)()
+        dxi = (C.c_double * 3)()
+        flags = (C.c_int * 2)()
+        _check(lib().pda_mesh_info(self._h, dims, sizes, dx, dxi, flags))
+        self._dim, self._stencil, self._ncols = dims[0], dims[1], dims[2]
+        self._sizes = tuple(sizes)
+        self._dx = tuple(dx)
+        self._dxinv = tuple(dxi)
+        self._fully_periodic = bool(flags[0])
+        self._structured = bool(flags[1])
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.pda_mesh_free(self._h)
+            self._h = None
+
+    def dimensionality(self):
+        return self._dim
+
+    def stencilSize(self):
+        return self._stencil
+
+    def stencilMeshSize(self):
+        return self._sizes[0]
+
+    def sampleMeshSize(self):
+        return self._sizes[1]
+
+    def numCellsInner(self):
+        return self._sizes[2]
+
+    def numCellsNearBd(self):
+        return self._sizes[3]
+
+    def isFullyPeriodic(self):
+        return self._fully_periodic
+
+    def isStructured(self):
+        return self._structured
+
+    def dx(self):
+        return self._dx[0]
+
+    def dy(self):
+        return self._dx[1]
+
+    def dz(self):
+        return self._dx[2]
+
+    def dxInv(self):
+        return self._dxinv[0]
+
+    def dyInv(self):
+        return self._dxinv[1]
+
+    def dzInv(self):
+        return self._dxinv[2]
+
+    def _arrays(self):
+        import numpy as np
+        g = np.empty((self._sizes[1], self._ncols), dtype=np.int32)
+        x = np.empty(self._sizes[0])
+        y = np.empty(self._sizes[0])
+        z = np.empty(self._sizes[0])
+        inner = np.empty(self._sizes[2], dtype=np.int32)
+        near = np.empty(self._sizes[3], dtype=np.int32)
+        vp = lambda a: a.ctypes.data_as(C.c_void_p)
+        _check(lib().pda_mesh_arrays(self._h, vp(g), vp(x), vp(y), vp(z), vp(inner), vp(near)))
+        return g, x, y, z, inner, near
+
+    def graph(self):
+        return self._arrays()[0]
+
+    def viewX(self):
+        return self._arrays()[1]
+
+    def viewY(self):
+        return self._arrays()[2]
+
+    def viewZ(self):
+        return self._arrays()[3]
+
+    def graphRowsOfCellsAwayFromBd(self):
+        return self._arrays()[4]
+
+    def graphRowsOfCellsNearBd(self):
+        return self._arrays()[5]
+
+    def write(self, directory):
+        _check(lib().pda_mesh_write(self._h, os.fsencode(directory)))
+
+
+def load_cellcentered_uniform_mesh(directory) -> CellCenteredUniformMesh:
+    h = C.c_void_p()
+    _check(lib().pda_mesh_load(os.fsencode(str(directory)), C.byref(h)))
+    return CellCenteredUniformMesh(h)
+
+
+def create_full_mesh(n, bounds, stencil_size=3, periodic=(False, False, False)):
+    """In-memory equivalent of meshing_scripts/create_full_mesh.py."""
+    nn = list(n) + [1] * (3 - len(n))
+    bb = list(bounds) + [0.0] * (6 - len(bounds))
+    pp = [int(bool(p)) for p in periodic] + [0] * (3 - len(periodic))
+    h = C.c_void_p()
+    _check(lib().pda_mesh_create_full((C.c_int * 3)(*nn), (C.c_double * 6)(*bb), int(stencil_size),
+                                      (C.c_int * 3)(*pp), C.byref(h)))
+    return CellCenteredUniformMesh(h)
+
+
+def create_sample_mesh(full: CellCenteredUniformMesh, sample_gids):
+    """Equivalent of meshing_scripts/create_sample_mesh.py; returns
+    (sample mesh, stencil-mesh gids w.r.t. the full mesh)."""
+    import numpy as np
+    g = np.ascontiguousarray(np.asarray(sample_gids, dtype=np.int64))
+    st = np.empty(full.stencilMeshSize(), dtype=np.int64)
+    h = C.c_void_p()
+    _check(lib().pda_mesh_create_sample(full._h, g.ctypes.data_as(C.POINTER(C.c_int64)), len(g),
+                                        C.byref(h), st.ctypes.data_as(C.POINTER(C.c_int64))))
+    m = CellCenteredUniformMesh(h)
+    return m, st[: m.stencilMeshSize()].copy()
+
+
+# ------------------------------------------------------------------- problems
+
+
+class CsrJacobian:
+    """Device CSR matrix with the reference's Eigen row-major layout."""
+
+    def __init__(self, rowptr, colidx, values, shape):
+        self.rowptr = rowptr
+        self.colidx = colidx
+        self.values = values
+        self.shape = shape
+
+    def nonZeros(self):
+        return int(self.values.numel())
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        return sp.csr_matrix((self.values.cpu().numpy(), self.colidx.cpu().numpy(),
+                              self.rowptr.cpu().numpy()), shape=self.shape)
+
+
+class Problem:
+    """Device problem object (mirror of PublicProblemEigenMixinCpp /
+    the reference's Python problem classes)."""
+
+    def __init__(self, mesh, family, handle, stream):
+        self._mesh = mesh  # the mesh must outlive the problem
+        self._family = family
+        self._h = handle
+        self._stream = stream
+        nd = C.c_int()
+        ds = C.c_int64()
+        dst = C.c_int64()
+        _check(lib().pda_problem_sizes(self._h, C.byref(nd), C.byref(ds), C.byref(dst)))
+        self._ndpc, self._ds, self._dst = nd.value, ds.value, dst.value
+        self._pattern = None
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.pda_problem_free(self._h)
+            self._h = None
+
+    # sizes
+    def numDofPerCell(self):
+        return self._ndpc
+
+    def totalDofSampleMesh(self):
+        return self._ds
+
+    def totalDofStencilMesh(self):
+        return self._dst
+
+    def queryParameter(self, name):
+        v = C.c_double()
+        _check(lib().pda_query_parameter(self._h, name.encode(), C.byref(v)))
+        return v.value
+
+    def gamma(self):
+        return self.queryParameter("gamma")
+
+    def gravity(self):
+        return self.queryParameter("gravity")
+
+    def coriolis(self):
+        return self.queryParameter("coriolis")
+
+    # buffers
+    def _empty(self, n):
+        import torch
+        return torch.empty(n, dtype=torch.float64, device="cuda")
+
+    def initialCondition(self):
+        import torch
+        u = torch.empty(self._dst, dtype=torch.float64, device="cuda")
+        _check(lib().pda_initial_condition(self._h, _ptr(u)))
+        return u
+
+    def initialConditionHost(self):
+        import numpy as np
+        u = np.empty(self._dst)
+        _check(lib().pda_initial_condition_host(self._h, u.ctypes.data_as(C.c_void_p)))
+        return u
+
+    def createState(self):
+        import torch
+        return torch.zeros(self._dst, dtype=torch.float64, device="cuda")
+
+    def createVelocity(self):
+        import torch
+        return torch.zeros(self._ds, dtype=torch.float64, device="cuda")
+
+    createRightHandSide = createVelocity
+    createRhs = createVelocity
+
+    @staticmethod
+    def _check_vec(t, n, what):
+        import torch
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64
+                and t.is_contiguous() and t.numel() == n):
+            raise ValueError(f"{what}: expected a contiguous float64 CUDA tensor of {n} entries")
+
+    # evaluation
+    def velocity(self, state, t, V):
+        self._check_vec(state, self._dst, "state")
+        self._check_vec(V, self._ds, "velocity")
+        _check(lib().pda_velocity(self._h, _ptr(state), float(t), _ptr(V)))
+
+    rightHandSide = velocity
+    rhs = velocity
+
+    def __call__(self, state, t, V, J=None, computeJacobian=False):
+        if J is not None and computeJacobian:
+            self.rightHandSideAndJacobian(state, t, V, J)
+        else:
+            self.velocity(state, t, V)
+
+    def velocity_host(self, state_np, t, V_np):
+        """Host-buffer call through the C ABI (H2D, kernels, D2H)."""
+        _check(lib().pda_velocity_host(self._h, state_np.ctypes.data_as(C.c_void_p), float(t),
+                                       V_np.ctypes.data_as(C.c_void_p)))
+
+    def _shape(self):
+        r, c, n = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(lib().pda_jacobian_shape(self._h, C.byref(r), C.byref(c), C.byref(n)))
+        return r.value, c.value, n.value
+
+    def createJacobian(self) -> CsrJacobian:
+        import torch
+        rows, cols, nnz = self._shape()
+        rp = torch.empty(rows + 1, dtype=torch.int32, device="cuda")
+        ci = torch.empty(nnz, dtype=torch.int32, device="cuda")
+        _check(lib().pda_jacobian_pattern(self._h, _ptr(rp), _ptr(ci)))
+        vals = torch.zeros(nnz, dtype=torch.float64, device="cuda")
+        return CsrJacobian(rp, ci, vals, (rows, cols))
+
+    def jacobianPatternHost(self):
+        import numpy as np
+        rows, cols, nnz = self._shape()
+        rp = np.empty(rows + 1, dtype=np.int32)
+        ci = np.empty(nnz, dtype=np.int32)
+        _check(lib().pda_jacobian_pattern_host(self._h, rp.ctypes.data_as(C.c_void_p),
+                                               ci.ctypes.data_as(C.c_void_p)))
+        return rp, ci
+
+    def rightHandSideAndJacobian(self, state, t, V, J: CsrJacobian):
+        self._check_vec(state, self._dst, "state")
+        self._check_vec(V, self._ds, "velocity")
+        _check(lib().pda_velocity_and_jacobian(self._h, _ptr(state), float(t), _ptr(V),
+                                               _ptr(J.values)))
+
+    def jacobian(self, state, t, J: CsrJacobian):
+        self._check_vec(state, self._dst, "state")
+        _check(lib().pda_jacobian(self._h, _ptr(state), float(t), _ptr(J.values)))
+
+    def applyJacobian(self, state, operand, t, result):
+        """result = J(state) @ operand; operand/result column-major
+        (n x k tensors are passed transposed-contiguous as k columns)."""
+        import torch
+        if operand.dim() == 1:
+            B = operand.contiguous()
+            k = 1
+            R = result
+        else:
+            B = operand.t().contiguous()
+            k = operand.shape[1]
+            R = torch.empty((k, self._ds), dtype=torch.float64, device="cuda")
+        _check(lib().pda_apply_jacobian(self._h, _ptr(state), float(t), _ptr(B), k, _ptr(R)))
+        if operand.dim() != 1:
+            result.copy_(R.t())
+
+    # time integration
+    def advance_ssprk3(self, state, t0, dt, nsteps, use_graph=True):
+        self._check_vec(state, self._dst, "state")
+        _check(lib().pda_advance_ssprk3(self._h, _ptr(state), float(t0), float(dt), int(nsteps),
+                                        int(bool(use_graph))))
+
+    def advance_rk4(self, state, t0, dt, nsteps, use_graph=True):
+        self._check_vec(state, self._dst, "state")
+        _check(lib().pda_advance_rk4(self._h, _ptr(state), float(t0), float(dt), int(nsteps),
+                                     int(bool(use_graph))))
+
+    def launch_count(self):
+        return lib().pda_problem_launch_count(self._h)
+
+    def profile_velocity(self, state, V, reps=10):
+        """Mean device ms of the velocity kernels: faces x/y/z, balance, near-boundary rows."""
+        ms = (C.c_double * 5)()
+        _check(lib().pda_profile_velocity(self._h, _ptr(state), _ptr(V), int(reps), ms))
+        return dict(faces_x=ms[0], faces_y=ms[1], faces_z=ms[2], balance=ms[3], near_rows=ms[4])
+
+
+def measure_fp64_peak():
+    """Measured FP64 FMA throughput of the current GPU in FLOP/s."""
+    v = C.c_double()
+    _check(lib().pda_measure_fp64_peak(C.byref(v)))
+    return v.value
+
+
+def _stream_handle(stream):
+    if stream is None:
+        try:
+            import torch
+            if torch.cuda.is_available():
+                return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        except Exception:
+            pass
+        return C.c_void_p(0)
+    if isinstance(stream, int):
+        return C.c_void_p(stream)
+    return C.c_void_p(stream.cuda_stream)
+
+
+def create_problem(mesh, problem_enum, scheme=InviscidFluxReconstruction.FirstOrder, icFlag=1,
+                   params=None, stream=None) -> Problem:
+    """Mirror of pressiodemoapps.create_problem(mesh, enum, scheme[, icFlag[, params]])."""
+    fam = _FAMILY[type(problem_enum)]
+    names = list((params or {}).keys())
+    vals = [float(params[k]) for k in names]
+    cn = (C.c_char_p * max(1, len(names)))(*[n.encode() for n in names])
+    cv = (C.c_double * max(1, len(vals)))(*vals)
+    h = C.c_void_p()
+    s = _stream_handle(stream)
+    _check(lib().pda_problem_create(mesh._h, fam, int(problem_enum), int(scheme), int(icFlag), cn, cv,
+                                    len(names), s, C.byref(h)))
+    return Problem(mesh, fam, h, s)
+
+
+def create_slip_wall_swe_2d_problem(mesh, scheme, gravity, coriolis, pulse_magnitude, stream=None):
+    """Mirror of create_slip_wall_swe_2d_problem_eigen (swe2d.hpp:278-308)."""
+    h = C.c_void_p()
+    s = _stream_handle(stream)
+    _check(lib().pda_problem_create_swe_slip_wall(mesh._h, int(scheme), float(gravity), float(coriolis),
+                                                  float(pulse_magnitude), s, C.byref(h)))
+    return Problem(mesh, 3, h, s)

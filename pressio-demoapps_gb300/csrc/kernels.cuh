@@ -1,0 +1,445 @@
+// Kernel templates for the residual ("velocity") and the CSR Jacobian of the
+// cell-centered finite-volume problems.
+//
+// Two formulations are used:
+//  * "rows" kernels evaluate one graph row per thread exactly like the
+//    reference's per-cell loops (both faces of a cell computed from the
+//    cell's own stencil).  They serve the cells within the stencil half-width
+//    of a non-periodic boundary, whose ghost values depend on the row
+//    (impl/euler_2d_prob_class.hpp:1045-1113, :833-988), and every row of a
+//    sample mesh.  Each row's stencil is pre-resolved on the host into a
+//    table of source cells (the ghost-fill rule folded in), so a single
+//    kernel serves every boundary condition that mirrors cells.
+//  * "structured" kernels evaluate each face of a natural-order full mesh
+//    exactly once (the reference computes every interior face twice, once
+//    from each side, with identical arguments) and then balance the face
+//    fluxes per cell in the reference's axis order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "numerics.cuh"
+#include "types.hpp"
+
+namespace pda {
+
+template <int FAM> struct Fam;
+template <> struct Fam<Euler1d> {
+  static constexpr int dim = 1, ndpc = 3;
+  template <int AXIS>
+  static PDA_HD void flux(double F[3], const double qL[3], const double qR[3], const Phys &p) {
+    euler3_flux(F, qL, qR, p.gamma);
+  }
+  template <int AXIS>
+  static PDA_HD void flux_jac(double JL[9], double JR[9], const double qL[3], const double qR[3],
+                              const Phys &p) {
+    euler3_flux_jac(JL, JR, qL, qR, p.gamma);
+  }
+};
+template <> struct Fam<Euler2d> {
+  static constexpr int dim = 2, ndpc = 4;
+  template <int AXIS>
+  static PDA_HD void flux(double F[4], const double qL[4], const double qR[4], const Phys &p) {
+    euler4_flux<AXIS>(F, qL, qR, p.gamma);
+  }
+  template <int AXIS>
+  static PDA_HD void flux_jac(double JL[16], double JR[16], const double qL[4], const double qR[4],
+                              const Phys &p) {
+    euler4_flux_jac<AXIS>(JL, JR, qL, qR, p.gamma);
+  }
+};
+template <> struct Fam<Euler3d> {
+  static constexpr int dim = 3, ndpc = 5;
+  template <int AXIS>
+  static PDA_HD void flux(double F[5], const double qL[5], const double qR[5], const Phys &p) {
+    euler5_flux<AXIS>(F, qL, qR, p.gamma);
+  }
+  template <int AXIS>
+  static PDA_HD void flux_jac(double JL[25], double JR[25], const double qL[5], const double qR[5],
+                              const Phys &p) {
+    euler5_flux_jac<AXIS>(JL, JR, qL, qR, p.gamma);
+  }
+};
+template <> struct Fam<Swe2d> {
+  static constexpr int dim = 2, ndpc = 3;
+  template <int AXIS>
+  static PDA_HD void flux(double F[3], const double qL[3], const double qR[3], const Phys &p) {
+    swe_flux<AXIS>(F, qL, qR, p.gravity);
+  }
+  template <int AXIS>
+  static PDA_HD void flux_jac(double JL[9], double JR[9], const double qL[3], const double qR[3],
+                              const Phys &p) {
+    swe_flux_jac<AXIS>(JL, JR, qL, qR, p.gravity);
+  }
+};
+
+// Reconstruct the two states of the face between q[H-1] and q[H] from 2H
+// consecutive cell states (H = scheme half-width).  Mirrors
+// impl/functor_reconstruct_from_state.hpp:419-499 and weno.hpp:300-328.
+template <int NDPC, int SCHEME>
+PDA_HD void reconstruct_face(double uNeg[NDPC], double uPos[NDPC], const double (*q)[NDPC]) {
+#pragma unroll
+  for (int d = 0; d < NDPC; ++d) {
+    if constexpr (SCHEME == FirstOrder) {
+      uNeg[d] = q[0][d];
+      uPos[d] = q[1][d];
+    } else if constexpr (SCHEME == Weno3) {
+      weno3_face(uNeg[d], uPos[d], q[0][d], q[1][d], q[2][d], q[3][d]);
+    } else {
+      weno5_face(uNeg[d], uPos[d], q[0][d], q[1][d], q[2][d], q[3][d], q[4][d], q[5][d]);
+    }
+  }
+}
+
+// Same with the gradient of each reconstructed value with respect to the 2H
+// cell values (per dof): g[d][s].  FirstOrder gradients are {1,0} / {0,1}
+// (functor_reconstruct_from_state.hpp:523-536).
+template <int NDPC, int SCHEME>
+PDA_HD void reconstruct_face_grad(double uNeg[NDPC], double uPos[NDPC],
+                                  double gNeg[NDPC][2 * SchemeTraits<SCHEME>::h],
+                                  double gPos[NDPC][2 * SchemeTraits<SCHEME>::h],
+                                  const double (*q)[NDPC]) {
+#pragma unroll
+  for (int d = 0; d < NDPC; ++d) {
+    if constexpr (SCHEME == FirstOrder) {
+      uNeg[d] = q[0][d];
+      uPos[d] = q[1][d];
+      gNeg[d][0] = 1.;
+      gNeg[d][1] = 0.;
+      gPos[d][0] = 0.;
+      gPos[d][1] = 1.;
+    } else if constexpr (SCHEME == Weno3) {
+      weno3_face_grad(uNeg[d], uPos[d], gNeg[d], gPos[d], q[0][d], q[1][d], q[2][d], q[3][d]);
+    } else {
+      weno5_face_grad(uNeg[d], uPos[d], gNeg[d], gPos[d], q[0][d], q[1][d], q[2][d], q[3][d],
+                      q[4][d], q[5][d]);
+    }
+  }
+}
+
+template <int NDPC>
+__device__ __forceinline__ void load_cell(double q[NDPC], const double *__restrict__ U, int c,
+                                          bool flip, int reflectDof) {
+#pragma unroll
+  for (int d = 0; d < NDPC; ++d) q[d] = __ldg(U + (size_t)c * NDPC + d);
+  if (flip && reflectDof >= 0) {
+#pragma unroll
+    for (int d = 0; d < NDPC; ++d)
+      if (d == reflectDof) q[d] = -q[d];
+  }
+}
+
+// Reference per-cell V (velocityOnlyNearBdCellsImpl / velocityOnlyInnerCellsImpl)
+template <int FAM, int SCHEME>
+__global__ void __launch_bounds__(128)
+k_rows_velocity(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U, double *__restrict__ V) {
+  using F = Fam<FAM>;
+  constexpr int NDPC = F::ndpc, DIM = F::dim, H = SchemeTraits<SCHEME>::h, S = 2 * H + 1;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= t.nrows) return;
+  double v[NDPC];
+#pragma unroll
+  for (int d = 0; d < NDPC; ++d) v[d] = 0.;
+#pragma unroll
+  for (int ax = 0; ax < DIM; ++ax) {
+    double q[S][NDPC];
+    const size_t base = ((size_t)e * DIM + ax) * S;
+#pragma unroll
+    for (int s = 0; s < S; ++s) load_cell<NDPC>(q[s], U, t.src[base + s], t.flip[base + s], m.reflect[ax]);
+    double uN[NDPC], uP[NDPC], fL[NDPC], fR[NDPC];
+    reconstruct_face<NDPC, SCHEME>(uN, uP, q);
+    if (ax == 0) F::template flux<0>(fL, uN, uP, p);
+    if constexpr (DIM > 1) if (ax == 1) F::template flux<1>(fL, uN, uP, p);
+    if constexpr (DIM > 2) if (ax == 2) F::template flux<2>(fL, uN, uP, p);
+    reconstruct_face<NDPC, SCHEME>(uN, uP, q + 1);
+    if (ax == 0) F::template flux<0>(fR, uN, uP, p);
+    if constexpr (DIM > 1) if (ax == 1) F::template flux<1>(fR, uN, uP, p);
+    if constexpr (DIM > 2) if (ax == 2) F::template flux<2>(fR, uN, uP, p);
+    const double hinv = m.hinv[ax];
+#pragma unroll
+    for (int d = 0; d < NDPC; ++d) v[d] += hinv * (fL[d] - fR[d]);
+  }
+  const int r = t.rows[e];
+  if constexpr (FAM == Swe2d) {
+    // swe_2d_prob_class.hpp:983-994
+    const int c = t.cell[e];
+    const double u0 = __ldg(U + (size_t)c * 3), u1 = __ldg(U + (size_t)c * 3 + 1),
+                 u2 = __ldg(U + (size_t)c * 3 + 2);
+    v[1] -= p.coriolis * u2 / u0;
+    v[2] += p.coriolis * u1 / u0;
+  }
+#pragma unroll
+  for (int d = 0; d < NDPC; ++d) V[(size_t)r * NDPC + d] = v[d];
+}
+
+// ---------------------------------------------------------------------------
+// Structured full mesh: faces once, then per-cell balance.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int wrap(int i, int n, int periodic) {
+  if (periodic) {
+    i %= n;
+    if (i < 0) i += n;
+  }
+  return i;
+}
+
+// One thread per face normal to AXIS inside the box; face f lies between
+// cells f-1 and f.  Output Fx laid out [outer][mid][f - lo] with the face
+// axis fastest.
+template <int FAM, int SCHEME, int AXIS>
+__global__ void __launch_bounds__(128)
+k_struct_faces(Box b, Phys p, const double *__restrict__ U, double *__restrict__ Fout) {
+  using F = Fam<FAM>;
+  constexpr int NDPC = F::ndpc, H = SchemeTraits<SCHEME>::h;
+  const int nf[3] = {b.hi[0] - b.lo[0] + (AXIS == 0), b.hi[1] - b.lo[1] + (AXIS == 1),
+                     b.hi[2] - b.lo[2] + (AXIS == 2)};
+  const long total = (long)nf[0] * nf[1] * nf[2];
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  int id[3];
+  id[0] = (int)(t % nf[0]);
+  id[1] = (int)((t / nf[0]) % nf[1]);
+  id[2] = (int)(t / ((long)nf[0] * nf[1]));
+  int c[3] = {id[0] + b.lo[0], id[1] + b.lo[1], id[2] + b.lo[2]};
+  double q[2 * H][NDPC];
+#pragma unroll
+  for (int s = 0; s < 2 * H; ++s) {
+    int cc[3] = {c[0], c[1], c[2]};
+    cc[AXIS] = wrap(c[AXIS] - H + s, b.n[AXIS], b.periodic[AXIS]);
+    const long cell = cc[0] + (long)b.n[0] * (cc[1] + (long)b.n[1] * cc[2]);
+#pragma unroll
+    for (int d = 0; d < NDPC; ++d) q[s][d] = __ldg(U + cell * NDPC + d);
+  }
+  double uN[NDPC], uP[NDPC], f[NDPC];
+  reconstruct_face<NDPC, SCHEME>(uN, uP, q);
+  F::template flux<AXIS>(f, uN, uP, p);
+#pragma unroll
+  for (int d = 0; d < NDPC; ++d) Fout[t * NDPC + d] = f[d];
+}
+
+// V for every box cell from the face fluxes, in the reference's axis order
+// (x, then y, then z, then the shallow-water Coriolis source).
+template <int FAM>
+__global__ void __launch_bounds__(256)
+k_struct_balance(Box b, MeshArgs m, Phys p, const double *__restrict__ U,
+                 const double *__restrict__ Fx, const double *__restrict__ Fy,
+                 const double *__restrict__ Fz, double *__restrict__ V) {
+  using F = Fam<FAM>;
+  constexpr int NDPC = F::ndpc, DIM = F::dim;
+  const int nb[3] = {b.hi[0] - b.lo[0], b.hi[1] - b.lo[1], b.hi[2] - b.lo[2]};
+  const long total = (long)nb[0] * nb[1] * nb[2];
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const int i = (int)(t % nb[0]);
+  const int j = (int)((t / nb[0]) % nb[1]);
+  const int k = (int)(t / ((long)nb[0] * nb[1]));
+  double v[NDPC];
+#pragma unroll
+  for (int d = 0; d < NDPC; ++d) v[d] = 0.;
+  {
+    const long f0 = (i + (long)(nb[0] + 1) * (j + (long)nb[1] * k)) * NDPC;
+#pragma unroll
+    for (int d = 0; d < NDPC; ++d) v[d] += m.hinv[0] * (Fx[f0 + d] - Fx[f0 + NDPC + d]);
+  }
+  if constexpr (DIM > 1) {
+    const long f0 = (i + (long)nb[0] * (j + (long)(nb[1] + 1) * k)) * NDPC;
+    const long f1 = f0 + (long)nb[0] * NDPC;
+#pragma unroll
+    for (int d = 0; d < NDPC; ++d) v[d] += m.hinv[1] * (Fy[f0 + d] - Fy[f1 + d]);
+  }
+  if constexpr (DIM > 2) {
+    const long f0 = (i + (long)nb[0] * (j + (long)nb[1] * k)) * NDPC;
+    const long f1 = f0 + (long)nb[0] * nb[1] * NDPC;
+#pragma unroll
+    for (int d = 0; d < NDPC; ++d) v[d] += m.hinv[2] * (Fz[f0 + d] - Fz[f1 + d]);
+  }
+  const long cell = (i + b.lo[0]) + (long)b.n[0] * ((j + b.lo[1]) + (long)b.n[1] * (k + b.lo[2]));
+  if constexpr (FAM == Swe2d) {
+    const double u0 = __ldg(U + cell * 3), u1 = __ldg(U + cell * 3 + 1), u2 = __ldg(U + cell * 3 + 2);
+    v[1] -= p.coriolis * u2 / u0;
+    v[2] += p.coriolis * u1 / u0;
+  }
+#pragma unroll
+  for (int d = 0; d < NDPC; ++d) V[cell * NDPC + d] = v[d];
+}
+
+// ---------------------------------------------------------------------------
+// V and J, reference per-cell formulation, rows whose stencil is entirely
+// inside the domain (velocityAndJacInnerCellsImpl, euler_2d_prob_class.hpp:
+// 632-720; scatter: mixin_directional_flux_balance_jacobian.hpp:120-285).
+// J values are accumulated in place at the block offsets of the CSR row, in
+// the reference's order, so repeated neighbours on tiny periodic meshes sum
+// exactly as Eigen's coeffRef does.
+// ---------------------------------------------------------------------------
+template <int FAM, int SCHEME>
+__global__ void __launch_bounds__(64)
+k_rows_vj_inner(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U,
+                const int *__restrict__ rowptr, double *__restrict__ V, double *__restrict__ J) {
+  using F = Fam<FAM>;
+  constexpr int NDPC = F::ndpc, DIM = F::dim, H = SchemeTraits<SCHEME>::h, S = 2 * H + 1;
+  constexpr int G = 2 * H;  // gradient length per face
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= t.nrows) return;
+  const int r = t.rows[e];
+  // zero this row block's entries
+#pragma unroll 1
+  for (int k = 0; k < NDPC; ++k)
+    for (int q = rowptr[r * NDPC + k]; q < rowptr[r * NDPC + k + 1]; ++q) J[q] = 0.;
+  double v[NDPC];
+#pragma unroll
+  for (int d = 0; d < NDPC; ++d) v[d] = 0.;
+#pragma unroll 1
+  for (int ax = 0; ax < DIM; ++ax) {
+    double q[S][NDPC];
+    int pos[S];
+    const size_t base = ((size_t)e * DIM + ax) * S;
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      load_cell<NDPC>(q[s], U, t.src[base + s], false, -1);
+      pos[s] = t.jpos[base + s];
+    }
+    double uN[NDPC], uP[NDPC], fL[NDPC], fR[NDPC];
+    double gLN[NDPC][G], gLP[NDPC][G], gRN[NDPC][G], gRP[NDPC][G];
+    double JLN[NDPC * NDPC], JLP[NDPC * NDPC], JRN[NDPC * NDPC], JRP[NDPC * NDPC];
+    reconstruct_face_grad<NDPC, SCHEME>(uN, uP, gLN, gLP, q);
+    if (ax == 0) { F::template flux<0>(fL, uN, uP, p); F::template flux_jac<0>(JLN, JLP, uN, uP, p); }
+    if constexpr (DIM > 1) if (ax == 1) { F::template flux<1>(fL, uN, uP, p); F::template flux_jac<1>(JLN, JLP, uN, uP, p); }
+    if constexpr (DIM > 2) if (ax == 2) { F::template flux<2>(fL, uN, uP, p); F::template flux_jac<2>(JLN, JLP, uN, uP, p); }
+    reconstruct_face_grad<NDPC, SCHEME>(uN, uP, gRN, gRP, q + 1);
+    if (ax == 0) { F::template flux<0>(fR, uN, uP, p); F::template flux_jac<0>(JRN, JRP, uN, uP, p); }
+    if constexpr (DIM > 1) if (ax == 1) { F::template flux<1>(fR, uN, uP, p); F::template flux_jac<1>(JRN, JRP, uN, uP, p); }
+    if constexpr (DIM > 2) if (ax == 2) { F::template flux<2>(fR, uN, uP, p); F::template flux_jac<2>(JRN, JRP, uN, uP, p); }
+    const double hinv = m.hinv[ax];
+#pragma unroll
+    for (int d = 0; d < NDPC; ++d) v[d] += hinv * (fL[d] - fR[d]);
+    // scatter, reference order: for k, for j: left face (+=) then right face (-=)
+#pragma unroll 1
+    for (int k = 0; k < NDPC; ++k) {
+      const int rb = rowptr[r * NDPC + k];
+#pragma unroll 1
+      for (int j = 0; j < NDPC; ++j) {
+        const double ln = JLN[k * NDPC + j], lp = JLP[k * NDPC + j];
+        const double rn = JRN[k * NDPC + j], rp = JRP[k * NDPC + j];
+        if constexpr (SCHEME == FirstOrder) {
+          J[rb + pos[0] + j] += ln * hinv;
+          J[rb + pos[1] + j] += (lp - rn) * hinv;
+          J[rb + pos[2] + j] += -rp * hinv;
+        } else {
+#pragma unroll
+          for (int s = 0; s < G; ++s) {
+            J[rb + pos[s] + j] += ln * gLN[j][s] * hinv;
+            J[rb + pos[s] + j] += lp * gLP[j][s] * hinv;
+          }
+#pragma unroll
+          for (int s = 0; s < G; ++s) {
+            J[rb + pos[s + 1] + j] -= rn * gRN[j][s] * hinv;
+            J[rb + pos[s + 1] + j] -= rp * gRP[j][s] * hinv;
+          }
+        }
+      }
+    }
+  }
+  if constexpr (FAM == Swe2d) {
+    // swe_2d_prob_class.hpp:997-1012
+    const int c = t.cell[e];
+    const double u0 = __ldg(U + (size_t)c * 3), u1 = __ldg(U + (size_t)c * 3 + 1),
+                 u2 = __ldg(U + (size_t)c * 3 + 2);
+    v[1] -= p.coriolis * u2 / u0;
+    v[2] += p.coriolis * u1 / u0;
+    const int self = t.jpos[((size_t)e * DIM + 0) * S + H];
+    const int rb1 = rowptr[r * 3 + 1], rb2 = rowptr[r * 3 + 2];
+    J[rb1 + self + 0] += p.coriolis * u2 / (u0 * u0);
+    J[rb1 + self + 2] += -p.coriolis / u0;
+    J[rb2 + self + 1] += p.coriolis / u0;
+    J[rb2 + self + 0] += -p.coriolis * u1 / (u0 * u0);
+  }
+#pragma unroll
+  for (int d = 0; d < NDPC; ++d) V[(size_t)r * NDPC + d] = v[d];
+}
+
+// V and J for rows near a non-periodic boundary: V with the scheme's stencil
+// (ghosts folded into the table), J first order with the ghost dependence
+// folded into the diagonal block by the BC factors
+// (velocityAndJacNearBDCellsImplDifferentScheme, euler_2d_prob_class.hpp:
+// 833-988; ComputeDirectionalFluxBalanceFirstOrderJacobianOnBoundaryCell,
+// mixin_directional_flux_balance_jacobian.hpp:287-372).
+template <int FAM, int SCHEME>
+__global__ void __launch_bounds__(64)
+k_rows_vj_nearbd(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U,
+                 const int *__restrict__ rowptr, double *__restrict__ V, double *__restrict__ J) {
+  using F = Fam<FAM>;
+  constexpr int NDPC = F::ndpc, DIM = F::dim, H = SchemeTraits<SCHEME>::h, S = 2 * H + 1;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= t.nrows) return;
+  const int r = t.rows[e];
+#pragma unroll 1
+  for (int k = 0; k < NDPC; ++k)
+    for (int q = rowptr[r * NDPC + k]; q < rowptr[r * NDPC + k + 1]; ++q) J[q] = 0.;
+  double v[NDPC];
+#pragma unroll
+  for (int d = 0; d < NDPC; ++d) v[d] = 0.;
+#pragma unroll 1
+  for (int ax = 0; ax < DIM; ++ax) {
+    const double hinv = m.hinv[ax];
+    {  // velocity with the scheme's stencil
+      double q[S][NDPC];
+      const size_t base = ((size_t)e * DIM + ax) * S;
+#pragma unroll
+      for (int s = 0; s < S; ++s) load_cell<NDPC>(q[s], U, t.src[base + s], t.flip[base + s], m.reflect[ax]);
+      double uN[NDPC], uP[NDPC], fL[NDPC], fR[NDPC];
+      reconstruct_face<NDPC, SCHEME>(uN, uP, q);
+      if (ax == 0) F::template flux<0>(fL, uN, uP, p);
+      if constexpr (DIM > 1) if (ax == 1) F::template flux<1>(fL, uN, uP, p);
+      if constexpr (DIM > 2) if (ax == 2) F::template flux<2>(fL, uN, uP, p);
+      reconstruct_face<NDPC, SCHEME>(uN, uP, q + 1);
+      if (ax == 0) F::template flux<0>(fR, uN, uP, p);
+      if constexpr (DIM > 1) if (ax == 1) F::template flux<1>(fR, uN, uP, p);
+      if constexpr (DIM > 2) if (ax == 2) F::template flux<2>(fR, uN, uP, p);
+#pragma unroll
+      for (int d = 0; d < NDPC; ++d) v[d] += hinv * (fL[d] - fR[d]);
+    }
+    {  // first-order Jacobian with BC factors
+      double q[3][NDPC];
+      const size_t base = ((size_t)e * DIM + ax) * 3;
+#pragma unroll
+      for (int s = 0; s < 3; ++s) load_cell<NDPC>(q[s], U, t.src1[base + s], t.flip1[base + s], m.reflect[ax]);
+      double JLN[NDPC * NDPC], JLP[NDPC * NDPC], JRN[NDPC * NDPC], JRP[NDPC * NDPC];
+      if (ax == 0) { F::template flux_jac<0>(JLN, JLP, q[0], q[1], p); F::template flux_jac<0>(JRN, JRP, q[1], q[2], p); }
+      if constexpr (DIM > 1) if (ax == 1) { F::template flux_jac<1>(JLN, JLP, q[0], q[1], p); F::template flux_jac<1>(JRN, JRP, q[1], q[2], p); }
+      if constexpr (DIM > 2) if (ax == 2) { F::template flux_jac<2>(JLN, JLP, q[0], q[1], p); F::template flux_jac<2>(JRN, JRP, q[1], q[2], p); }
+      const int pl = t.jpos1[base + 0], pc = t.jpos1[base + 1], pr = t.jpos1[base + 2];
+      const double *fac = t.jfac + ((size_t)e * DIM + ax) * NDPC;
+#pragma unroll 1
+      for (int k = 0; k < NDPC; ++k) {
+        const int rb = rowptr[r * NDPC + k];
+        for (int j = 0; j < NDPC; ++j) J[rb + pc + j] += (JLP[k * NDPC + j] - JRN[k * NDPC + j]) * hinv;
+        if (pl >= 0)
+          for (int j = 0; j < NDPC; ++j) J[rb + pl + j] += JLN[k * NDPC + j] * hinv;
+        if (pr >= 0)
+          for (int j = 0; j < NDPC; ++j) J[rb + pr + j] += -JRP[k * NDPC + j] * hinv;
+        if (pl < 0)
+          for (int j = 0; j < NDPC; ++j) J[rb + pc + j] += (fac[j] * JLN[k * NDPC + j]) * hinv;
+        if (pr < 0)
+          for (int j = 0; j < NDPC; ++j) J[rb + pc + j] += (fac[j] * -JRP[k * NDPC + j]) * hinv;
+      }
+    }
+  }
+  if constexpr (FAM == Swe2d) {
+    const int c = t.cell[e];
+    const double u0 = __ldg(U + (size_t)c * 3), u1 = __ldg(U + (size_t)c * 3 + 1),
+                 u2 = __ldg(U + (size_t)c * 3 + 2);
+    v[1] -= p.coriolis * u2 / u0;
+    v[2] += p.coriolis * u1 / u0;
+    const int self = t.jpos1[((size_t)e * DIM + 0) * 3 + 1];
+    const int rb1 = rowptr[r * 3 + 1], rb2 = rowptr[r * 3 + 2];
+    J[rb1 + self + 0] += p.coriolis * u2 / (u0 * u0);
+    J[rb1 + self + 2] += -p.coriolis / u0;
+    J[rb2 + self + 1] += p.coriolis / u0;
+    J[rb2 + self + 0] += -p.coriolis * u1 / (u0 * u0);
+  }
+#pragma unroll
+  for (int d = 0; d < NDPC; ++d) V[(size_t)r * NDPC + d] = v[d];
+}
+
+}  // namespace pda

@@ -1,0 +1,11 @@
+// Kernel instantiations and launchers for the Euler2d family.
+#define PDA_FAM ::pda::Euler2d
+#include "family_impl.cuh"
+
+namespace pda {
+const Launchers &launchers_euler2d() {
+  static const Launchers L = {fam_impl::rows_velocity, fam_impl::struct_velocity,
+                              fam_impl::rows_vj_inner, fam_impl::rows_vj_nearbd};
+  return L;
+}
+}  // namespace pda

@@ -1,0 +1,43 @@
+// Host-callable launchers, one set per problem family (kernels_<family>.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "types.hpp"
+
+namespace pda {
+
+struct Launchers {
+  // reference per-row velocity over a row table
+  void (*rows_velocity)(int scheme, const RowTable &t, const MeshArgs &m, const Phys &p,
+                        const double *U, double *V, cudaStream_t s);
+  // structured interior: faces once per axis into F[axis], then balance into V
+  // ev (may be null): dim+2 events recorded before the first face launch,
+  // after each face launch and after the balance launch
+  void (*struct_velocity)(int scheme, const Box &b, const MeshArgs &m, const Phys &p,
+                          const double *U, double *const F[3], double *V, cudaStream_t s,
+                          int *launches, cudaEvent_t *ev);
+  // V and J for inner rows / near-boundary rows
+  void (*rows_vj_inner)(int scheme, const RowTable &t, const MeshArgs &m, const Phys &p,
+                        const double *U, const int *rowptr, double *V, double *J, cudaStream_t s);
+  void (*rows_vj_nearbd)(int scheme, const RowTable &t, const MeshArgs &m, const Phys &p,
+                         const double *U, const int *rowptr, double *V, double *J, cudaStream_t s);
+};
+
+const Launchers &launchers_euler1d();
+const Launchers &launchers_euler2d();
+const Launchers &launchers_euler3d();
+const Launchers &launchers_swe2d();
+
+// generic device utilities (util.cu)
+void launch_axpby_stage(int kind, double *out, const double *a, const double *b, const double *c,
+                        double ca, double cb, double cc, double cd, const double *d, const double *e,
+                        long n, cudaStream_t s);
+// FP64 FMA throughput probe: returns FLOP/s measured with CUDA events
+double measure_fp64_fma_rate(int blocks, int threads, int iters, cudaStream_t s);
+void launch_csr_spmm(long rows, const int *rowptr, const int *colidx, const double *vals,
+                     const double *B, long ldb, int ncols, double *R, long ldr, cudaStream_t s);
+
+inline int div_up(long a, long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace pda

@@ -1,0 +1,767 @@
+// Point-wise numerics of the cell-centered finite-volume hot path, shared by
+// every kernel of this library: WENO3/WENO5 face reconstruction (with and
+// without the analytic gradient), the Rusanov flux for the Euler and
+// shallow-water equations and its analytic Jacobians.
+//
+// Every expression below keeps the operand order and association of the
+// reference implementation so that, compiled without FMA contraction
+// (nvcc -fmad=false), each value is bit-identical to the reference's
+// double-precision result.  The few places that cannot be bit-identical are
+// marked "deviation" and are within the stated parity tolerance.
+//
+// Reference (pressio-demoapps, include/pressiodemoapps/...):
+//   impl/weno5.hpp:56-178   weno5           -> weno5_face
+//   impl/weno5.hpp:180-434  weno5WithGrad   -> weno5_face_grad
+//   impl/weno3.hpp:56-132   weno3           -> weno3_face
+//   impl/weno3.hpp:134-246  weno3WithGrad   -> weno3_face_grad
+//   impl/euler_rusanov_flux_values_function.hpp:54-208   -> euler*_flux
+//   impl/euler_rusanov_flux_jacobian_function.hpp:54-406 -> euler*_flux_jac
+//   impl/swe_rusanov_flux_values_function.hpp:54-97      -> swe_flux
+//   impl/swe_rusanov_flux_jacobian_function.hpp:54-137   -> swe_flux_jac
+#pragma once
+
+#include <math.h>
+
+#if defined(__CUDACC__)
+#define PDA_HD __host__ __device__ __forceinline__
+#else
+#define PDA_HD inline
+#endif
+
+namespace pda {
+
+enum Scheme : int { FirstOrder = 0, Weno3 = 1, Weno5 = 2 };
+
+// half-width of the reconstruction stencil: 1, 2, 3
+template <int S> struct SchemeTraits;
+template <> struct SchemeTraits<FirstOrder> { static constexpr int h = 1; };
+template <> struct SchemeTraits<Weno3> { static constexpr int h = 2; };
+template <> struct SchemeTraits<Weno5> { static constexpr int h = 3; };
+
+PDA_HD double sq(double x) { return x * x; }
+// deviation: the reference evaluates std::pow(x, 3.) (glibc); here (x*x)*x,
+// which differs by at most a few ulp.  Used only on the Jacobian path.
+PDA_HD double cube(double x) { return (x * x) * x; }
+
+// ---------------------------------------------------------------------------
+// WENO5, one face i+1/2: uNeg from q_{i-2..i+2}, uPos from q_{i-1..i+3}.
+// ---------------------------------------------------------------------------
+PDA_HD void weno5_face(double &uNeg, double &uPos, double qim2, double qim1,
+                       double qi, double qip1, double qip2, double qip3) {
+  constexpr double epsilon = 1e-6;
+  constexpr double two = 2., three = 3., four = 4., five = 5., seven = 7.,
+                   eleven = 11.;
+  constexpr double oneOvfour = 1. / 4., oneOvsix = 1. / 6.,
+                   oneOvten = 1. / 10., threeOvten = 3. / 10.,
+                   sixOvten = 6. / 10., thirteenOvtwelve = 13. / 12.;
+  {
+    const double p0 = (two * qim2 - seven * qim1 + eleven * qi) * oneOvsix;
+    const double p1 = (-qim1 + five * qi + two * qip1) * oneOvsix;
+    const double p2 = (two * qi + five * qip1 - qip2) * oneOvsix;
+    const double B0 = thirteenOvtwelve * (qim2 - two * qim1 + qi) * (qim2 - two * qim1 + qi) +
+                      oneOvfour * (qim2 - four * qim1 + three * qi) * (qim2 - four * qim1 + three * qi);
+    const double B1 = thirteenOvtwelve * (qim1 - two * qi + qip1) * (qim1 - two * qi + qip1) +
+                      oneOvfour * (qim1 - qip1) * (qim1 - qip1);
+    const double B2 = thirteenOvtwelve * (qi - two * qip1 + qip2) * (qi - two * qip1 + qip2) +
+                      oneOvfour * (three * qi - four * qip1 + qip2) * (three * qi - four * qip1 + qip2);
+    const double alpha0 = oneOvten / (epsilon * epsilon + 2. * epsilon * B0 + B0 * B0);
+    const double alpha1 = sixOvten / (epsilon * epsilon + 2. * epsilon * B1 + B1 * B1);
+    const double alpha2 = threeOvten / (epsilon * epsilon + 2. * epsilon * B2 + B2 * B2);
+    const double alphaSInv = 1. / (alpha0 + alpha1 + alpha2);
+    const double w0 = alpha0 * alphaSInv;
+    const double w1 = alpha1 * alphaSInv;
+    const double w2 = alpha2 * alphaSInv;
+    uNeg = w0 * p0 + w1 * p1 + w2 * p2;
+  }
+  {
+    const double p0 = (-qim1 + five * qi + two * qip1) * oneOvsix;
+    const double p1 = (two * qi + five * qip1 - qip2) * oneOvsix;
+    const double p2 = (eleven * qip1 - seven * qip2 + two * qip3) * oneOvsix;
+    const double B0 = thirteenOvtwelve * (qim1 - two * qi + qip1) * (qim1 - two * qi + qip1) +
+                      oneOvfour * (qim1 - four * qi + three * qip1) * (qim1 - four * qi + three * qip1);
+    const double B1 = thirteenOvtwelve * (qi - two * qip1 + qip2) * (qi - two * qip1 + qip2) +
+                      oneOvfour * (qi - qip2) * (qi - qip2);
+    const double B2 = thirteenOvtwelve * (qip1 - two * qip2 + qip3) * (qip1 - two * qip2 + qip3) +
+                      oneOvfour * (three * qip1 - four * qip2 + qip3) * (three * qip1 - four * qip2 + qip3);
+    const double alpha0 = threeOvten / (epsilon * epsilon + 2. * epsilon * B0 + B0 * B0);
+    const double alpha1 = sixOvten / (epsilon * epsilon + 2. * epsilon * B1 + B1 * B1);
+    const double alpha2 = oneOvten / (epsilon * epsilon + 2. * epsilon * B2 + B2 * B2);
+    const double alphaSInv = 1. / (alpha0 + alpha1 + alpha2);
+    const double w0 = alpha0 * alphaSInv;
+    const double w1 = alpha1 * alphaSInv;
+    const double w2 = alpha2 * alphaSInv;
+    uPos = w0 * p0 + w1 * p1 + w2 * p2;
+  }
+}
+
+// WENO5 with the gradient of the two face values with respect to the six
+// stencil values q_{i-2..i+3}: gNeg[5] == 0, gPos[0] == 0.
+PDA_HD void weno5_face_grad(double &uNeg, double &uPos, double gNeg[6],
+                            double gPos[6], double qim2, double qim1, double qi,
+                            double qip1, double qip2, double qip3) {
+  constexpr double epsilon = 1e-6;
+  constexpr double two = 2., three = 3., four = 4., five = 5., seven = 7.,
+                   eleven = 11.;
+  constexpr double oneOvfour = 1. / 4., oneOvsix = 1. / 6.,
+                   oneOvten = 1. / 10., threeOvten = 3. / 10.,
+                   sixOvten = 6. / 10., thirteenOvtwelve = 13. / 12.;
+  {
+    const double p0 = (two * qim2 - seven * qim1 + eleven * qi) * oneOvsix;
+    const double p1 = (-qim1 + five * qi + two * qip1) * oneOvsix;
+    const double p2 = (two * qi + five * qip1 - qip2) * oneOvsix;
+    const double dp0[5] = {1. / 3., -7. / 6., 11. / 6., 0., 0.};
+    const double dp1[5] = {0., -1. / 6., 5. / 6., 1. / 3., 0.};
+    const double dp2[5] = {0., 0., 1. / 3., 5. / 6., -1. / 6.};
+    const double B0 = thirteenOvtwelve * sq(qim2 - two * qim1 + qi) +
+                      oneOvfour * sq(qim2 - four * qim1 + three * qi);
+    const double B1 = thirteenOvtwelve * sq(qim1 - two * qi + qip1) +
+                      oneOvfour * sq(qim1 - qip1);
+    const double B2 = thirteenOvtwelve * sq(qi - two * qip1 + qip2) +
+                      oneOvfour * sq(three * qi - four * qip1 + qip2);
+    double dB0[5], dB1[5], dB2[5];
+    dB0[0] = (13. * (qim2 - 2. * qim1 + qi)) / 6. + (qim2 - 4. * qim1 + 3. * qi) / 2.;
+    dB0[1] = -(13. * (qim2 - 2. * qim1 + qi)) / 3. - 2. * (qim2 - 4. * qim1 + 3. * qi);
+    dB0[2] = (13. * (qim2 - 2. * qim1 + qi)) / 6. + (3. * (qim2 - 4. * qim1 + 3. * qi)) / 2.;
+    dB0[3] = 0.;
+    dB0[4] = 0.;
+    dB1[0] = 0.;
+    dB1[1] = (13. * (qip1 + qim1 - 2. * qi)) / 6. + (qim1 - qip1) / 2.;
+    dB1[2] = -(13. * (qip1 + qim1 - 2. * qi)) / 3.;
+    dB1[3] = (13. * (qip1 + qim1 - 2. * qi)) / 6. - (qim1 - qip1) / 2.;
+    dB1[4] = 0.;
+    dB2[0] = 0.;
+    dB2[1] = 0.;
+    dB2[2] = (13. * (qip2 - 2. * qip1 + qi)) / 6. + (3. * (qip2 - 4. * qip1 + 3. * qi)) / 2.;
+    dB2[3] = -(13. * (qip2 - 2. * qip1 + qi)) / 3. - 2. * (qip2 - 4. * qip1 + 3. * qi);
+    dB2[4] = (13. * (qip2 - 2. * qip1 + qi)) / 6. + (qip2 - 4. * qip1 + 3. * qi) / 2.;
+    const double alpha0 = oneOvten / sq(epsilon + B0);
+    const double alpha1 = sixOvten / sq(epsilon + B1);
+    const double alpha2 = threeOvten / sq(epsilon + B2);
+    const double alphaSInv = 1. / (alpha0 + alpha1 + alpha2);
+    const double c0 = -1. / (5. * cube(B0 + epsilon));
+    const double c1 = -6. / (5. * cube(B1 + epsilon));
+    const double c2 = -3. / (5. * cube(B2 + epsilon));
+    const double cS = -1. / sq(alpha2 + alpha1 + alpha0);
+    const double w0 = alpha0 * alphaSInv;
+    const double w1 = alpha1 * alphaSInv;
+    const double w2 = alpha2 * alphaSInv;
+    for (int i = 0; i < 5; i++) {
+      const double da0 = c0 * dB0[i];
+      const double da1 = c1 * dB1[i];
+      const double da2 = c2 * dB2[i];
+      const double daS = cS * (da0 + da1 + da2);
+      double g = (da0 * alphaSInv + daS * alpha0) * p0 + dp0[i] * w0;
+      g += (da1 * alphaSInv + daS * alpha1) * p1 + dp1[i] * w1;
+      g += (da2 * alphaSInv + daS * alpha2) * p2 + dp2[i] * w2;
+      gNeg[i] = g;
+    }
+    gNeg[5] = 0.;
+    uNeg = w0 * p0 + w1 * p1 + w2 * p2;
+  }
+  {
+    const double p0 = (-qim1 + five * qi + two * qip1) * oneOvsix;
+    const double p1 = (two * qi + five * qip1 - qip2) * oneOvsix;
+    const double p2 = (eleven * qip1 - seven * qip2 + two * qip3) * oneOvsix;
+    const double dp0[5] = {-1. / 6., 5. / 6., 1. / 3., 0., 0.};
+    const double dp1[5] = {0., 1. / 3., 5. / 6., -1. / 6., 0.};
+    const double dp2[5] = {0., 0., 11. / 6., -7. / 6., 1. / 3.};
+    const double B0 = thirteenOvtwelve * sq(qim1 - two * qi + qip1) +
+                      oneOvfour * sq(qim1 - four * qi + three * qip1);
+    const double B1 = thirteenOvtwelve * sq(qi - two * qip1 + qip2) +
+                      oneOvfour * sq(qi - qip2);
+    const double B2 = thirteenOvtwelve * sq(qip1 - two * qip2 + qip3) +
+                      oneOvfour * sq(three * qip1 - four * qip2 + qip3);
+    double dB0[5], dB1[5], dB2[5];
+    dB0[0] = (3. * qip1 + qim1 - 4. * qi) / 2. + (13. * (qip1 + qim1 - 2. * qi)) / 6.;
+    dB0[1] = -2. * (3. * qip1 + qim1 - 4. * qi) - (13. * (qip1 + qim1 - 2 * qi)) / 3.;
+    dB0[2] = (3. * (3. * qip1 + qim1 - 4. * qi)) / 2. + (13. * (qip1 + qim1 - 2. * qi)) / 6.;
+    dB0[3] = 0.;
+    dB0[4] = 0.;
+    dB1[0] = 0.;
+    dB1[1] = (13. * (qip2 - 2 * qip1 + qi)) / 6. + (qi - qip2) / 2.;
+    dB1[2] = -(13. * (qip2 - 2. * qip1 + qi)) / 3.;
+    dB1[3] = (13. * (qip2 - 2. * qip1 + qi)) / 6. - (qi - qip2) / 2.;
+    dB1[4] = 0.;
+    dB2[0] = 0.;
+    dB2[1] = 0.;
+    dB2[2] = (13. * (qip3 - 2. * qip2 + qip1)) / 6. + (3. * (qip3 - 4. * qip2 + 3. * qip1)) / 2.;
+    dB2[3] = -(13. * (qip3 - 2. * qip2 + qip1)) / 3. - 2. * (qip3 - 4. * qip2 + 3. * qip1);
+    dB2[4] = (13. * (qip3 - 2. * qip2 + qip1)) / 6. + (qip3 - 4. * qip2 + 3. * qip1) / 2.;
+    const double alpha0 = threeOvten / sq(epsilon + B0);
+    const double alpha1 = sixOvten / sq(epsilon + B1);
+    const double alpha2 = oneOvten / sq(epsilon + B2);
+    const double alphaSInv = 1. / (alpha0 + alpha1 + alpha2);
+    const double c0 = -3. / (5. * cube(B0 + epsilon));
+    const double c1 = -6. / (5. * cube(B1 + epsilon));
+    const double c2 = -1. / (5. * cube(B2 + epsilon));
+    const double cS = -1. / sq(alpha2 + alpha1 + alpha0);
+    const double w0 = alpha0 * alphaSInv;
+    const double w1 = alpha1 * alphaSInv;
+    const double w2 = alpha2 * alphaSInv;
+    for (int i = 0; i < 5; i++) {
+      const double da0 = c0 * dB0[i];
+      const double da1 = c1 * dB1[i];
+      const double da2 = c2 * dB2[i];
+      const double daS = cS * (da0 + da1 + da2);
+      double g = (da0 * alphaSInv + daS * alpha0) * p0 + dp0[i] * w0;
+      g += (da1 * alphaSInv + daS * alpha1) * p1 + dp1[i] * w1;
+      g += (da2 * alphaSInv + daS * alpha2) * p2 + dp2[i] * w2;
+      gPos[i + 1] = g;
+    }
+    gPos[0] = 0.;
+    uPos = w0 * p0 + w1 * p1 + w2 * p2;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// WENO3, one face i+1/2: uNeg from q_{i-1..i+1}, uPos from q_{i..i+2}.
+// ---------------------------------------------------------------------------
+PDA_HD void weno3_face(double &uNeg, double &uPos, double qim1, double qi,
+                       double qip1, double qip2) {
+  constexpr double epsilon = 1.e-6;
+  constexpr double two = 2., three = 3.;
+  constexpr double oneOvtwo = 1. / 2., oneOvthree = 1. / 3., twoOvthree = 2. / 3.;
+  {
+    const double p0 = (-qim1 + three * qi) * oneOvtwo;
+    const double p1 = (qi + qip1) * oneOvtwo;
+    const double B0 = (qim1 - qi) * (qim1 - qi);
+    const double B1 = (qi - qip1) * (qi - qip1);
+    const double alpha0 = oneOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
+    const double alpha1 = twoOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
+    const double alphaSInv = 1. / (alpha0 + alpha1);
+    const double w0 = alpha0 * alphaSInv;
+    const double w1 = alpha1 * alphaSInv;
+    uNeg = w0 * p0 + w1 * p1;
+  }
+  {
+    const double p0 = (qi + qip1) * oneOvtwo;
+    const double p1 = (three * qip1 - qip2) * oneOvtwo;
+    const double B0 = (qi - qip1) * (qi - qip1);
+    const double B1 = (qip1 - qip2) * (qip1 - qip2);
+    const double alpha0 = twoOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
+    const double alpha1 = oneOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
+    const double alphaSInv = 1. / (alpha0 + alpha1);
+    const double w0 = alpha0 * alphaSInv;
+    const double w1 = alpha1 * alphaSInv;
+    uPos = w0 * p0 + w1 * p1;
+  }
+}
+
+// WENO3 with gradients with respect to q_{i-1..i+2}: gNeg[3] == 0, gPos[0] == 0.
+PDA_HD void weno3_face_grad(double &uNeg, double &uPos, double gNeg[4],
+                            double gPos[4], double qim1, double qi, double qip1,
+                            double qip2) {
+  constexpr double epsilon = 1e-6;
+  constexpr double two = 2., three = 3.;
+  constexpr double oneOvtwo = 1. / 2., oneOvthree = 1. / 3., twoOvthree = 2. / 3.;
+  {
+    const double p0 = (-qim1 + three * qi) * oneOvtwo;
+    const double p1 = (qi + qip1) * oneOvtwo;
+    const double dp0[3] = {-1. / 2., 3. / 2., 0.};
+    const double dp1[3] = {0., 1. / 2., 1. / 2.};
+    const double B0 = (qim1 - qi) * (qim1 - qi);
+    const double B1 = (qi - qip1) * (qi - qip1);
+    const double alpha0 = oneOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
+    const double alpha1 = twoOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
+    const double alphaSInv = 1. / (alpha0 + alpha1);
+    const double e0 = sq(qim1 - qi) + epsilon;  // pow(pow(qim1-qi,2.)+eps, .)
+    const double e1 = sq(qi - qip1) + epsilon;
+    const double A = 2. / (3. * sq(e1)) + 1. / (3. * sq(e0));
+    double da0[3], da1[3], daS[3];
+    da0[0] = -4. * (qim1 - qi) / (3. * cube(e0));
+    da0[1] = 4. * (qim1 - qi) / (3. * cube(e0));
+    da0[2] = 0.;
+    da1[0] = 0.;
+    da1[1] = -8. * (qi - qip1) / (3. * cube(e1));
+    da1[2] = 8. * (qi - qip1) / (3. * cube(e1));
+    daS[0] = (4. * (qim1 - qi)) / (3. * cube(e0) * sq(A));
+    daS[1] = -((4. * (qim1 - qi)) / (3. * cube(e0)) - (8. * (qi - qip1)) / (3. * cube(e1))) / sq(A);
+    daS[2] = -(8. * (qi - qip1)) / (3. * sq(A) * cube(e1));
+    const double w0 = alpha0 * alphaSInv;
+    const double w1 = alpha1 * alphaSInv;
+    for (int i = 0; i < 3; i++) {
+      double g = (da0[i] * alphaSInv + daS[i] * alpha0) * p0 + dp0[i] * w0;
+      g += (da1[i] * alphaSInv + daS[i] * alpha1) * p1 + dp1[i] * w1;
+      gNeg[i] = g;
+    }
+    gNeg[3] = 0.;
+    uNeg = w0 * p0 + w1 * p1;
+  }
+  {
+    const double p0 = (qi + qip1) * oneOvtwo;
+    const double p1 = (three * qip1 - qip2) * oneOvtwo;
+    const double B0 = (qi - qip1) * (qi - qip1);
+    const double B1 = (qip1 - qip2) * (qip1 - qip2);
+    const double alpha0 = twoOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
+    const double alpha1 = oneOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
+    const double alphaSInv = 1. / (alpha0 + alpha1);
+    const double w0 = alpha0 * alphaSInv;
+    const double w1 = alpha1 * alphaSInv;
+    const double dp0[3] = {1. / 2., 1 / 2., 0.};
+    const double dp1[3] = {0., 3. / 2., -1. / 2.};
+    const double e0 = sq(qi - qip1) + epsilon;
+    const double e1 = sq(qip1 - qip2) + epsilon;
+    const double A = 1. / (3. * sq(e1)) + 2. / (3. * sq(e0));
+    double da0[3], da1[3], daS[3];
+    da0[0] = -8. * (qi - qip1) / (3. * cube(e0));
+    da0[1] = 8. * (qi - qip1) / (3. * cube(e0));
+    da0[2] = 0.;
+    da1[0] = 0.;
+    da1[1] = -4. * (qip1 - qip2) / (3. * cube(e1));
+    da1[2] = 4. * (qip1 - qip2) / (3. * cube(e1));
+    daS[0] = 8. * (qi - qip1) / (3. * cube(e0) * sq(A));
+    daS[1] = -(8. * (qi - qip1) / (3 * cube(e0)) - 4. * (qip1 - qip2) / (3. * cube(e1))) / sq(A);
+    daS[2] = -4. * (qip1 - qip2) / (3. * sq(A) * cube(e1));
+    for (int i = 0; i < 3; i++) {
+      double g = (da0[i] * alphaSInv + daS[i] * alpha0) * p0 + dp0[i] * w0;
+      g += (da1[i] * alphaSInv + daS[i] * alpha1) * p1 + dp1[i] * w1;
+      gPos[i + 1] = g;
+    }
+    gPos[0] = 0.;
+    uPos = w0 * p0 + w1 * p1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Rusanov flux for the Euler equations.  The 2D/3D versions are specialised on
+// the face normal (axis-aligned unit vectors); products with 0 and 1 are
+// elided, which changes no value other than the sign of an exact zero.
+// ---------------------------------------------------------------------------
+PDA_HD void euler3_flux(double F[3], const double qL[3], const double qR[3],
+                        double gamma) {
+  constexpr double half = 1. / 2.;
+  constexpr double es = 1.e-30;
+  const double rL = qL[0];
+  const double uL = qL[1] / (rL + es);
+  const double pL = (gamma - 1) * (qL[2] - half * rL * (uL * uL));
+  const double HL = (qL[2] + pL) / rL;
+  const double FL0 = rL * uL, FL1 = rL * uL * uL + pL, FL2 = rL * uL * HL;
+  const double rR = qR[0];
+  const double uR = qR[1] / (rR + es);
+  const double pR = (gamma - 1) * (qR[2] - half * rR * (uR * uR));
+  const double HR = (qR[2] + pR) / rR;
+  const double FR0 = rR * uR, FR1 = rR * uR * uR + pR, FR2 = rR * uR * HR;
+  const double RT = sqrt(rR / (rL));
+  const double u = (uL + RT * uR) / (1. + RT);
+  const double H = (HL + RT * HR) / (1. + RT);
+  const double a = sqrt((gamma - 1.) * (H - half * (u * u)));
+  const double smax = fabs(u) + a;
+  F[0] = half * (FL0 + FR0 + smax * (qL[0] - qR[0]));
+  F[1] = half * (FL1 + FR1 + smax * (qL[1] - qR[1]));
+  F[2] = half * (FL2 + FR2 + smax * (qL[2] - qR[2]));
+}
+
+template <int AXIS>
+PDA_HD void euler4_flux(double F[4], const double qL[4], const double qR[4],
+                        double gamma) {
+  constexpr double half = 1. / 2.;
+  constexpr double es = 1.e-30;
+  const double rL = qL[0];
+  const double uL = qL[1] / (rL + es);
+  const double vL = qL[2] / (rL + es);
+  const double unL = AXIS == 0 ? uL : vL;
+  const double pL = (gamma - 1) * (qL[3] - half * rL * (uL * uL + vL * vL));
+  const double HL = (qL[3] + pL) / rL;
+  double FL[4];
+  FL[0] = rL * unL;
+  FL[1] = AXIS == 0 ? rL * unL * uL + pL : rL * unL * uL;
+  FL[2] = AXIS == 1 ? rL * unL * vL + pL : rL * unL * vL;
+  FL[3] = rL * unL * HL;
+  const double rR = qR[0];
+  const double uR = qR[1] / (rR + es);
+  const double vR = qR[2] / (rR + es);
+  const double unR = AXIS == 0 ? uR : vR;
+  const double pR = (gamma - 1) * (qR[3] - half * rR * (uR * uR + vR * vR));
+  const double HR = (qR[3] + pR) / rR;
+  double FR[4];
+  FR[0] = rR * unR;
+  FR[1] = AXIS == 0 ? rR * unR * uR + pR : rR * unR * uR;
+  FR[2] = AXIS == 1 ? rR * unR * vR + pR : rR * unR * vR;
+  FR[3] = rR * unR * HR;
+  const double RT = sqrt(rR / (rL));
+  const double u = (uL + RT * uR) / (1. + RT);
+  const double v = (vL + RT * vR) / (1. + RT);
+  const double H = (HL + RT * HR) / (1. + RT);
+  const double a = sqrt((gamma - 1.) * (H - half * (u * u + v * v)));
+  const double smax = sqrt(u * u + v * v) + a;
+#pragma unroll
+  for (int d = 0; d < 4; ++d) F[d] = half * (FL[d] + FR[d] + smax * (qL[d] - qR[d]));
+}
+
+template <int AXIS>
+PDA_HD void euler5_flux(double F[5], const double qL[5], const double qR[5],
+                        double gamma) {
+  constexpr double half = 1. / 2.;
+  constexpr double es = 1.e-30;
+  const double rL = qL[0];
+  const double uL = qL[1] / (rL + es);
+  const double vL = qL[2] / (rL + es);
+  const double wL = qL[3] / (rL + es);
+  const double unL = AXIS == 0 ? uL : (AXIS == 1 ? vL : wL);
+  const double pL = (gamma - 1) * (qL[4] - half * rL * (uL * uL + vL * vL + wL * wL));
+  const double HL = (qL[4] + pL) / rL;
+  double FL[5];
+  FL[0] = rL * unL;
+  FL[1] = AXIS == 0 ? rL * unL * uL + pL : rL * unL * uL;
+  FL[2] = AXIS == 1 ? rL * unL * vL + pL : rL * unL * vL;
+  FL[3] = AXIS == 2 ? rL * unL * wL + pL : rL * unL * wL;
+  FL[4] = rL * unL * HL;
+  const double rR = qR[0];
+  const double uR = qR[1] / (rR + es);
+  const double vR = qR[2] / (rR + es);
+  const double wR = qR[3] / (rR + es);
+  const double unR = AXIS == 0 ? uR : (AXIS == 1 ? vR : wR);
+  const double pR = (gamma - 1) * (qR[4] - half * rR * (uR * uR + vR * vR + wR * wR));
+  const double HR = (qR[4] + pR) / rR;
+  double FR[5];
+  FR[0] = rR * unR;
+  FR[1] = AXIS == 0 ? rR * unR * uR + pR : rR * unR * uR;
+  FR[2] = AXIS == 1 ? rR * unR * vR + pR : rR * unR * vR;
+  FR[3] = AXIS == 2 ? rR * unR * wR + pR : rR * unR * wR;
+  FR[4] = rR * unR * HR;
+  const double RT = sqrt(rR / (rL));
+  const double u = (uL + RT * uR) / (1. + RT);
+  const double v = (vL + RT * vR) / (1. + RT);
+  const double w = (wL + RT * wR) / (1. + RT);
+  const double H = (HL + RT * HR) / (1. + RT);
+  const double a = sqrt((gamma - 1.) * (H - half * (u * u + v * v + w * w)));
+  const double smax = sqrt(u * u + v * v + w * w) + a;
+#pragma unroll
+  for (int d = 0; d < 5; ++d) F[d] = half * (FL[d] + FR[d] + smax * (qL[d] - qR[d]));
+}
+
+// Shallow-water Rusanov flux.  deviation: the reference's std::pow(h, 0.5) is
+// evaluated as sqrt(h) (correctly rounded; glibc pow agrees except in rare
+// near-midpoint cases, a 1-ulp difference).
+template <int AXIS>
+PDA_HD void swe_flux(double F[3], const double qL[3], const double qR[3],
+                     double gravity) {
+  constexpr double half = 1. / 2.;
+  constexpr double es = 1.e-30;
+  const double hL = qL[0];
+  const double uL = qL[1] / (hL + es);
+  const double vL = qL[2] / (hL + es);
+  const double unL = AXIS == 0 ? uL : vL;
+  const double pL = 0.5 * gravity * hL * hL;
+  double FL[3];
+  FL[0] = hL * unL;
+  FL[1] = AXIS == 0 ? hL * unL * uL + pL : hL * unL * uL;
+  FL[2] = AXIS == 1 ? hL * unL * vL + pL : hL * unL * vL;
+  const double hR = qR[0];
+  const double uR = qR[1] / (hR + es);
+  const double vR = qR[2] / (hR + es);
+  const double unR = AXIS == 0 ? uR : vR;
+  const double pR = 0.5 * gravity * hR * hR;
+  double FR[3];
+  FR[0] = hR * unR;
+  FR[1] = AXIS == 0 ? hR * unR * uR + pR : hR * unR * uR;
+  FR[2] = AXIS == 1 ? hR * unR * vR + pR : hR * unR * vR;
+  const double hm = 0.5 * (hL + hR);
+  const double sL = sqrt(hL), sR = sqrt(hR);
+  const double um = (unL * sL + unR * sR) / (sL + sR + es);
+  const double sg = sqrt(gravity * hm);
+  const double smax = sqrt(um * um) + sqrt(sg * sg);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) F[d] = half * (FL[d] + FR[d] + smax * (qL[d] - qR[d]));
+}
+
+// ---------------------------------------------------------------------------
+// Analytic Rusanov flux Jacobians JL = dF/dqL, JR = dF/dqR (row-major n x n).
+// These keep the reference's generic normal vector n.
+// ---------------------------------------------------------------------------
+PDA_HD void euler3_flux_jac(double JL[9], double JR[9], const double qL[3],
+                            const double qR[3], double gamma) {
+  constexpr double one = 1., two = 2., three = 3., half = 1. / 2.;
+  constexpr double es = 1.e-30;
+  const double gm1 = gamma - one;
+  const double rL = qL[0];
+  const double uL = qL[1] / (rL + es);
+  const double pL = gm1 * (qL[2] - half * rL * (uL * uL));
+  const double HL = (qL[2] + pL) / rL;
+  const double aL = sqrt(gm1 * (HL - half * (uL * uL)));
+  const double rR = qR[0];
+  const double uR = qR[1] / (rR + es);
+  const double pR = gm1 * (qR[2] - half * rR * (uR * uR));
+  const double HR = (qR[2] + pR) / rR;
+  const double aR = sqrt(gm1 * (HR - half * (uR * uR)));
+  const double r = sqrt(rR * rL);
+  const double RT = sqrt(rR / (rL));
+  const double u = (uL + RT * uR) / (one + RT);
+  const double H = (HL + RT * HR) / (one + RT);
+  const double a = sqrt(gm1 * (H - half * (u * u)));
+  const double smax = fabs(u) + a;
+  const double VMagSqrRoe = u * u + es;
+  const double VMagSqrL = uL * uL;
+  const double VVRoeL = uL * u;
+  const double VMagSqrR = uR * uR;
+  const double VVRoeR = uR * u;
+  const double uRelRoe = u / sqrt(VMagSqrRoe);
+  double gL[3], gR[3];
+  gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe + half * gm1 / a * (half * (VMagSqrRoe + VVRoeL) + half * (HL - H) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
+  gL[1] = one / (rL + r) * (uRelRoe - half * (gm1 * (u + gm1 * uL)) / (a));
+  gL[2] = half / (rL + r) * gamma * gm1 / (a);
+  gR[0] = one / (rR + r) * (-half * (uR + u) * uRelRoe + half * gm1 / a * (half * (VMagSqrRoe + VVRoeR) + half * (HR - H) - aR * aR / gm1 + half * (gamma - two) * VMagSqrR));
+  gR[1] = one / (rR + r) * (uRelRoe - half * (gm1 * (u + gm1 * uR)) / (a));
+  gR[2] = half / (rR + r) * gamma * gm1 / (a);
+  JL[0] = 0;
+  JL[1] = half;
+  JL[2] = 0;
+  JL[3] = half * (half * gm1 * uL * uL - uL * uL);
+  JL[4] = half * ((three - gamma) * uL);
+  JL[5] = half * gm1;
+  JL[6] = half * ((half * gm1 * uL * uL - HL) * uL);
+  JL[7] = half * (HL - gm1 * uL * uL);
+  JL[8] = half * gamma * uL;
+  for (int i = 0; i < 3; i++) {
+    JL[i * 3 + i] += half * smax;
+    for (int j = 0; j < 3; j++) JL[i * 3 + j] += half * gL[j] * (qL[i] - qR[i]);
+  }
+  JR[0] = 0;
+  JR[1] = half;
+  JR[2] = 0;
+  JR[3] = half * (half * gm1 * uR * uR - uR * uR);
+  JR[4] = half * ((three - gamma) * uR);
+  JR[5] = half * gm1;
+  JR[6] = half * ((half * gm1 * uR * uR - HR) * uR);
+  JR[7] = half * (HR - gm1 * uR * uR);
+  JR[8] = half * gamma * uR;
+  for (int i = 0; i < 3; i++) {
+    JR[i * 3 + i] -= half * smax;
+    for (int j = 0; j < 3; j++) JR[i * 3 + j] += half * gR[j] * (qL[i] - qR[i]);
+  }
+}
+
+template <int AXIS>
+PDA_HD void euler4_flux_jac(double JL[16], double JR[16], const double qL[4],
+                            const double qR[4], double gamma) {
+  constexpr double one = 1., two = 2., half = 1. / 2.;
+  constexpr double es = 1.e-30;
+  const double n[2] = {AXIS == 0 ? 1. : 0., AXIS == 1 ? 1. : 0.};
+  const double gm1 = gamma - one;
+  const double rL = qL[0];
+  const double uL = qL[1] / (rL + es);
+  const double vL = qL[2] / (rL + es);
+  const double unL = uL * n[0] + vL * n[1];
+  const double pL = gm1 * (qL[3] - half * rL * (uL * uL + vL * vL));
+  const double HL = (qL[3] + pL) / rL;
+  const double aL = sqrt(gm1 * (HL - half * (uL * uL + vL * vL)));
+  const double rR = qR[0];
+  const double uR = qR[1] / (rR + es);
+  const double vR = qR[2] / (rR + es);
+  const double unR = uR * n[0] + vR * n[1];
+  const double pR = gm1 * (qR[3] - half * rR * (uR * uR + vR * vR));
+  const double HR = (qR[3] + pR) / rR;
+  const double aR = sqrt(gm1 * (HR - half * (uR * uR + vR * vR)));
+  const double r = sqrt(rR * rL);
+  const double RT = sqrt(rR / (rL));
+  const double u = (uL + RT * uR) / (one + RT);
+  const double v = (vL + RT * vR) / (one + RT);
+  const double H = (HL + RT * HR) / (one + RT);
+  const double a = sqrt(gm1 * (H - half * (u * u + v * v)));
+  const double smax = sqrt(u * u + v * v) + a;
+  const double VMagSqrRoe = u * u + v * v + es;
+  const double VMagSqrL = uL * uL + vL * vL;
+  const double VVRoeL = uL * u + vL * v;
+  const double VMagSqrR = uR * uR + vR * vR;
+  const double VVRoeR = uR * u + vR * v;
+  const double uRelRoe = u / sqrt(VMagSqrRoe);
+  const double vRelRoe = v / sqrt(VMagSqrRoe);
+  double gL[4], gR[4];
+  gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe - half * (vL + v) * vRelRoe + half * gm1 / a * (half * (VMagSqrRoe + VVRoeL) + half * (HL - H) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
+  gL[1] = one / (rL + r) * (uRelRoe - half * (gm1 * (u + gm1 * uL)) / (a));
+  gL[2] = one / (rL + r) * (vRelRoe - half * (gm1 * (v + gm1 * vL)) / (a));
+  gL[3] = half / (rL + r) * gamma * gm1 / (a);
+  gR[0] = one / (rR + r) * (-half * (uR + u) * uRelRoe - half * (vR + v) * vRelRoe + half * gm1 / a * (half * (VMagSqrRoe + VVRoeR) + half * (HR - H) - aR * aR / gm1 + half * (gamma - two) * VMagSqrR));
+  gR[1] = one / (rR + r) * (uRelRoe - half * (gm1 * (u + gm1 * uR)) / (a));
+  gR[2] = one / (rR + r) * (vRelRoe - half * (gm1 * (v + gm1 * vR)) / (a));
+  gR[3] = half / (rR + r) * gamma * gm1 / (a);
+  // left
+  JL[0] = 0;
+  JL[1] = half * n[0];
+  JL[2] = half * n[1];
+  JL[3] = 0;
+  JL[4] = half * (half * gm1 * VMagSqrL * n[0] - uL * unL);
+  JL[5] = half * (uL * n[0] - gm1 * uL * n[0] + unL);
+  JL[6] = half * (uL * n[1] - gm1 * vL * n[0]);
+  JL[7] = half * gm1 * n[0];
+  JL[8] = half * (half * gm1 * VMagSqrL * n[1] - vL * unL);
+  JL[9] = half * (vL * n[0] - gm1 * uL * n[1]);
+  JL[10] = half * (vL * n[1] - gm1 * vL * n[1] + unL);
+  JL[11] = half * gm1 * n[1];
+  JL[12] = half * ((half * gm1 * VMagSqrL - HL) * unL);
+  JL[13] = half * (HL * n[0] - gm1 * uL * unL);
+  JL[14] = half * (HL * n[1] - gm1 * vL * unL);
+  JL[15] = half * gamma * unL;
+  for (int i = 0; i < 4; i++) {
+    JL[i * 4 + i] += half * smax;
+    for (int j = 0; j < 4; j++) JL[i * 4 + j] += half * gL[j] * (qL[i] - qR[i]);
+  }
+  // right
+  JR[0] = 0;
+  JR[1] = half * n[0];
+  JR[2] = half * n[1];
+  JR[3] = 0;
+  JR[4] = half * (half * gm1 * VMagSqrR * n[0] - uR * unR);
+  JR[5] = half * (uR * n[0] - gm1 * uR * n[0] + unR);
+  JR[6] = half * (uR * n[1] - gm1 * vR * n[0]);
+  JR[7] = half * gm1 * n[0];
+  JR[8] = half * (half * gm1 * VMagSqrR * n[1] - vR * unR);
+  JR[9] = half * (vR * n[0] - gm1 * uR * n[1]);
+  JR[10] = half * (vR * n[1] - gm1 * vR * n[1] + unR);
+  JR[11] = half * gm1 * n[1];
+  JR[12] = half * ((half * gm1 * VMagSqrR - HR) * unR);
+  JR[13] = half * (HR * n[0] - gm1 * uR * unR);
+  JR[14] = half * (HR * n[1] - gm1 * vR * unR);
+  JR[15] = half * gamma * unR;
+  for (int i = 0; i < 4; i++) {
+    JR[i * 4 + i] -= half * smax;
+    for (int j = 0; j < 4; j++) JR[i * 4 + j] += half * gR[j] * (qL[i] - qR[i]);
+  }
+}
+
+template <int AXIS>
+PDA_HD void euler5_flux_jac(double JL[25], double JR[25], const double qL[5],
+                            const double qR[5], double gamma) {
+  constexpr double one = 1., two = 2., half = 1. / 2.;
+  constexpr double es = 1.e-30;
+  const double n[3] = {AXIS == 0 ? 1. : 0., AXIS == 1 ? 1. : 0., AXIS == 2 ? 1. : 0.};
+  const double gm1 = gamma - one;
+  const double rL = qL[0];
+  const double uL = qL[1] / (rL + es);
+  const double vL = qL[2] / (rL + es);
+  const double wL = qL[3] / (rL + es);
+  const double unL = uL * n[0] + vL * n[1] + wL * n[2];
+  const double pL = gm1 * (qL[4] - half * rL * (uL * uL + vL * vL + wL * wL));
+  const double HL = (qL[4] + pL) / rL;
+  const double aL = sqrt(gm1 * (HL - half * (uL * uL + vL * vL + wL * wL)));
+  const double rR = qR[0];
+  const double uR = qR[1] / (rR + es);
+  const double vR = qR[2] / (rR + es);
+  const double wR = qR[3] / (rR + es);
+  const double unR = uR * n[0] + vR * n[1] + wR * n[2];
+  const double pR = gm1 * (qR[4] - half * rR * (uR * uR + vR * vR + wR * wR));
+  const double HR = (qR[4] + pR) / rR;
+  const double aR = sqrt(gm1 * (HR - half * (uR * uR + vR * vR + wR * wR)));
+  const double r = sqrt(rR * rL);
+  const double RT = sqrt(rR / (rL));
+  const double u = (uL + RT * uR) / (one + RT);
+  const double v = (vL + RT * vR) / (one + RT);
+  const double w = (wL + RT * wR) / (one + RT);
+  const double H = (HL + RT * HR) / (one + RT);
+  const double a = sqrt(gm1 * (H - half * (u * u + v * v + w * w)));
+  const double smax = sqrt(u * u + v * v + w * w) + a;
+  const double VMagSqrRoe = u * u + v * v + w * w + es;
+  const double VMagSqrL = uL * uL + vL * vL + wL * wL;
+  const double VVRoeL = uL * u + vL * v + wL * w;
+  const double VMagSqrR = uR * uR + vR * vR + wR * wR;
+  const double VVRoeR = uR * u + vR * v + wR * w;
+  const double uRelRoe = u / sqrt(VMagSqrRoe);
+  const double vRelRoe = v / sqrt(VMagSqrRoe);
+  const double wRelRoe = w / sqrt(VMagSqrRoe);
+  double gL[5], gR[5];
+  gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe - half * (vL + v) * vRelRoe - half * (wL + w) * wRelRoe + half * gm1 / a * (half * (VMagSqrRoe + VVRoeL) + half * (HL - H) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
+  gL[1] = one / (rL + r) * (uRelRoe - half * (gm1 * (u + gm1 * uL)) / (a));
+  gL[2] = one / (rL + r) * (vRelRoe - half * (gm1 * (v + gm1 * vL)) / (a));
+  gL[3] = one / (rL + r) * (wRelRoe - half * (gm1 * (w + gm1 * wL)) / (a));
+  gL[4] = half / (rL + r) * gamma * gm1 / (a);
+  gR[0] = one / (rR + r) * (-half * (uR + u) * uRelRoe - half * (vR + v) * vRelRoe - half * (wR + w) * wRelRoe + half * gm1 / a * (half * (VMagSqrRoe + VVRoeR) + half * (HR - H) - aR * aR / gm1 + half * (gamma - two) * VMagSqrR));
+  gR[1] = one / (rR + r) * (uRelRoe - half * (gm1 * (u + gm1 * uR)) / (a));
+  gR[2] = one / (rR + r) * (vRelRoe - half * (gm1 * (v + gm1 * vR)) / (a));
+  gR[3] = one / (rR + r) * (wRelRoe - half * (gm1 * (w + gm1 * wR)) / (a));
+  gR[4] = half / (rR + r) * gamma * gm1 / (a);
+  // left and right use the same template; X = L or R
+#define PDA_FILL_J5(J, uX, vX, wX, unX, HX, VMagSqrX)                 \
+  J[0] = 0;                                                           \
+  J[1] = half * n[0];                                                 \
+  J[2] = half * n[1];                                                 \
+  J[3] = half * n[2];                                                 \
+  J[4] = 0;                                                           \
+  J[5] = half * (half * gm1 * VMagSqrX * n[0] - uX * unX);            \
+  J[6] = half * (uX * n[0] - gm1 * uX * n[0] + unX);                  \
+  J[7] = half * (uX * n[1] - gm1 * vX * n[0]);                        \
+  J[8] = half * (uX * n[2] - gm1 * wX * n[0]);                        \
+  J[9] = half * gm1 * n[0];                                           \
+  J[10] = half * (half * gm1 * VMagSqrX * n[1] - vX * unX);           \
+  J[11] = half * (vX * n[0] - gm1 * uX * n[1]);                       \
+  J[12] = half * (vX * n[1] - gm1 * vX * n[1] + unX);                 \
+  J[13] = half * (vX * n[2] - gm1 * wX * n[1]);                       \
+  J[14] = half * gm1 * n[1];                                          \
+  J[15] = half * (half * gm1 * VMagSqrX * n[2] - wX * unX);           \
+  J[16] = half * (wX * n[0] - gm1 * uX * n[2]);                       \
+  J[17] = half * (wX * n[1] - gm1 * vX * n[2]);                       \
+  J[18] = half * (wX * n[2] - gm1 * wX * n[2] + unX);                 \
+  J[19] = half * gm1 * n[2];                                          \
+  J[20] = half * ((half * gm1 * VMagSqrX - HX) * unX);                \
+  J[21] = half * (HX * n[0] - gm1 * uX * unX);                        \
+  J[22] = half * (HX * n[1] - gm1 * vX * unX);                        \
+  J[23] = half * (HX * n[2] - gm1 * wX * unX);                        \
+  J[24] = half * gamma * unX;
+  PDA_FILL_J5(JL, uL, vL, wL, unL, HL, VMagSqrL)
+  for (int i = 0; i < 5; i++) {
+    JL[i * 5 + i] += half * smax;
+    for (int j = 0; j < 5; j++) JL[i * 5 + j] += half * gL[j] * (qL[i] - qR[i]);
+  }
+  PDA_FILL_J5(JR, uR, vR, wR, unR, HR, VMagSqrR)
+#undef PDA_FILL_J5
+  for (int i = 0; i < 5; i++) {
+    JR[i * 5 + i] -= half * smax;
+    for (int j = 0; j < 5; j++) JR[i * 5 + j] += half * gR[j] * (qL[i] - qR[i]);
+  }
+}
+
+// Shallow-water Rusanov flux Jacobian (generic normal).  deviation: pow(x,0.5)
+// -> sqrt(x); pow(2,3/2) is the correctly rounded constant 2*sqrt(2).
+template <int AXIS>
+PDA_HD void swe_flux_jac(double JL[9], double JR[9], const double qL[3],
+                         const double qR[3], double g) {
+  constexpr double es = 1.e-30;
+  const double n[2] = {AXIS == 0 ? 1. : 0., AXIS == 1 ? 1. : 0.};
+  const double hL = qL[0];
+  const double uL = qL[1] / (hL + es);
+  const double vL = qL[2] / (hL + es);
+  const double unL = uL * n[0] + vL * n[1];
+  const double hR = qR[0];
+  const double uR = qR[1] / (hR + es);
+  const double vR = qR[2] / (hR + es);
+  const double unR = uR * n[0] + vR * n[1];
+  const double hm = 0.5 * (hL + hR);
+  const double hL_sqrt = sqrt(hL);
+  const double hR_sqrt = sqrt(hR);
+  const double um = (unL * hL_sqrt + unR * hR_sqrt) / (hL_sqrt + hR_sqrt + es);
+  const double smax = fabs(um) + fabs(sqrt(g * hm));
+  const double termL = (n[0] * qL[1] + n[1] * qL[2]) / sq(qL[0]);
+  const double termR = (n[0] * qR[1] + n[1] * qR[2]) / sq(qR[0]);
+  const double hsqrt_un = hL_sqrt * unL + hR_sqrt * unR + es;
+  const double two_pow_1p5 = 2. * sqrt(2.);
+  double dL[3], dR[3];
+  dL[0] = -fabs(hsqrt_un) / (2. * hL_sqrt * sq(hL_sqrt + hR_sqrt)) +
+          (0.5 * unL / hL_sqrt - hL_sqrt * termL) * hsqrt_un / ((hL_sqrt + hR_sqrt) * fabs(hsqrt_un)) +
+          g / (two_pow_1p5 * sqrt(g * (hL + hR)));
+  dL[1] = n[0] * hsqrt_un / (hL_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
+  dL[2] = n[1] * hsqrt_un / (hL_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
+  dR[0] = -fabs(hsqrt_un) / (2. * hR_sqrt * sq(hL_sqrt + hR_sqrt)) +
+          (0.5 * unR / hR_sqrt - hR_sqrt * termR) * hsqrt_un / ((hL_sqrt + hR_sqrt) * fabs(hsqrt_un)) +
+          g / (two_pow_1p5 * sqrt(g * (hL + hR)));
+  dR[1] = n[0] * hsqrt_un / (hR_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
+  dR[2] = n[1] * hsqrt_un / (hR_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
+  JL[0] = -0.5 * dL[0] * (qR[0] - qL[0]) + 0.5 * (n[0] * uL + n[1] * vL - qL[0] * termL) + 0.5 * smax;
+  JL[1] = 0.5 * n[0] - 0.5 * dL[1] * (qR[0] - qL[0]);
+  JL[2] = 0.5 * n[1] - 0.5 * dL[2] * (qR[0] - qL[0]);
+  JL[3] = 0.5 * (g * n[0] * qL[0] - qL[1] * termL) - 0.5 * dL[0] * (qR[1] - qL[1]);
+  JL[4] = n[0] * uL + 0.5 * n[1] * vL + 0.5 * smax - 0.5 * dL[1] * (qR[1] - qL[1]);
+  JL[5] = 0.5 * n[1] * uL - 0.5 * dL[2] * (qR[1] - qL[1]);
+  JL[6] = 0.5 * (g * n[1] * qL[0] - qL[2] * termL) - 0.5 * dL[0] * (qR[2] - qL[2]);
+  JL[7] = 0.5 * n[0] * vL - 0.5 * dL[1] * (qR[2] - qL[2]);
+  JL[8] = n[1] * vL + 0.5 * n[0] * uL + 0.5 * smax - 0.5 * dL[2] * (qR[2] - qL[2]);
+  JR[0] = -0.5 * dR[0] * (qR[0] - qL[0]) + 0.5 * (n[0] * uR + n[1] * vR - qR[0] * termR) - 0.5 * smax;
+  JR[1] = 0.5 * n[0] - 0.5 * dR[1] * (qR[0] - qL[0]);
+  JR[2] = 0.5 * n[1] - 0.5 * dR[2] * (qR[0] - qL[0]);
+  JR[3] = 0.5 * (g * n[0] * qR[0] - qR[1] * termR) - 0.5 * dR[0] * (qR[1] - qL[1]);
+  JR[4] = n[0] * uR + 0.5 * n[1] * vR - 0.5 * smax - 0.5 * dR[1] * (qR[1] - qL[1]);
+  JR[5] = 0.5 * n[1] * uR - 0.5 * dR[2] * (qR[1] - qL[1]);
+  JR[6] = 0.5 * (g * n[1] * qR[0] - qR[2] * termR) - 0.5 * dR[0] * (qR[2] - qL[2]);
+  JR[7] = 0.5 * n[0] * vR - 0.5 * dR[1] * (qR[2] - qL[2]);
+  JR[8] = n[1] * vR + 0.5 * n[0] * uR - 0.5 * smax - 0.5 * dR[2] * (qR[2] - qL[2]);
+}
+
+}  // namespace pda

@@ -1,0 +1,1156 @@
+// Device problem object: parameters, initial conditions, boundary stencil
+// tables, the CSR pattern, kernel dispatch, steppers and the C ABI.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "internal.hpp"
+#include "launch.hpp"
+
+namespace pda {
+
+static thread_local std::string g_last_error;
+void set_last_error(const std::string &m) { g_last_error = m; }
+
+#define PDA_CUDA(x)                                                                           \
+  do {                                                                                        \
+    cudaError_t e_ = (x);                                                                     \
+    if (e_ != cudaSuccess)                                                                    \
+      throw ::pda::Error(PDA_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));      \
+  } while (0)
+
+template <class T> struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    if (count <= n && p) return;
+    release();
+    if (count == 0) return;
+    cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      throw Error(e == cudaErrorMemoryAllocation ? PDA_ERR_OUT_OF_MEMORY : PDA_ERR_CUDA,
+                  std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    n = count;
+  }
+  void upload(const std::vector<T> &v) {
+    alloc(v.size());
+    if (!v.empty()) PDA_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  }
+};
+
+// Host copy + device copy of a row table.
+struct Table {
+  std::vector<int> rows, cell, src, jpos, src1, jpos1;
+  std::vector<uint8_t> flip, flip1;
+  std::vector<double> jfac;
+  DevBuf<int> d_rows, d_cell, d_src, d_jpos, d_src1, d_jpos1;
+  DevBuf<uint8_t> d_flip, d_flip1;
+  DevBuf<double> d_jfac;
+  RowTable t{};
+  bool dirty = true;
+  int hostRows() const { return (int)rows.size(); }
+  // copy the host tables to the device if they changed since the last copy
+  void sync() {
+    if (!dirty) return;
+    upload();
+    dirty = false;
+  }
+  void upload() {
+    d_rows.upload(rows);
+    d_cell.upload(cell);
+    d_src.upload(src);
+    d_flip.upload(flip);
+    d_jpos.upload(jpos);
+    d_src1.upload(src1);
+    d_flip1.upload(flip1);
+    d_jpos1.upload(jpos1);
+    d_jfac.upload(jfac);
+    t.nrows = (int)rows.size();
+    t.rows = d_rows.p;
+    t.cell = d_cell.p;
+    t.src = d_src.p;
+    t.flip = d_flip.p;
+    t.jpos = jpos.empty() ? nullptr : d_jpos.p;
+    t.src1 = src1.empty() ? nullptr : d_src1.p;
+    t.flip1 = flip1.empty() ? nullptr : d_flip1.p;
+    t.jpos1 = jpos1.empty() ? nullptr : d_jpos1.p;
+    t.jfac = jfac.empty() ? nullptr : d_jfac.p;
+  }
+};
+
+enum BcKind { BC_NONE = 0, BC_MIRROR2D = 1, BC_NEUMANN1D = 2 };
+
+}  // namespace pda
+
+struct pda_mesh {
+  pda::Mesh m;
+};
+
+struct pda_problem {
+  const pda::Mesh *mesh = nullptr;
+  int family = 0, probEnum = 0, scheme = 0, icFlag = 1;
+  std::vector<double> icParams, physParams;
+  pda::Phys phys{};
+  pda::MeshArgs margs{};
+  cudaStream_t stream = nullptr;
+  int ndpc = 0, dim = 0, h = 0;
+  int64_t dofsSample = 0, dofsStencil = 0;
+  int bc = pda::BC_NONE;
+  const pda::Launchers *L = nullptr;
+  // velocity
+  bool useStruct = false;
+  pda::Box box{};
+  pda::DevBuf<double> F[3];
+  pda::Table nearT;   // near-boundary rows: V stencil (+ J first-order tables)
+  pda::Table innerT;  // inner rows (sample meshes for V; every mesh for V+J)
+  bool innerBuiltV = false, innerBuiltJ = false, nearBuiltJ = false;
+  // Jacobian
+  bool patternBuilt = false;
+  std::vector<int> rowptr, colidx;
+  std::vector<std::vector<int32_t>> rowBlocks;  // sorted unique cell ids per graph row
+  pda::DevBuf<int> d_rowptr, d_colidx;
+  pda::DevBuf<double> d_Jscratch, d_Vscratch;
+  // host-buffer entry points and steppers
+  pda::DevBuf<double> d_U, d_V, d_J;
+  pda::DevBuf<double> aux, r[4];
+  cudaGraphExec_t stepGraph = nullptr;
+  int stepGraphKind = -1;
+  double stepGraphDt = 0;
+  double *stepGraphU = nullptr;
+  int64_t stepGraphLaunches = 0;
+  int64_t launches = 0;
+  ~pda_problem() {
+    if (stepGraph) cudaGraphExecDestroy(stepGraph);
+  }
+};
+
+namespace pda {
+namespace {
+
+// ---------------------------------------------------------------- params
+constexpr int kInvalid = -1;
+
+// impl/euler_2d_parametrization_helpers.hpp:60-160
+int euler2d_ic_index(int probEn, int icFlag, const std::string &s) {
+  if (probEn == 5 /*NormalShock*/ && icFlag == 1 && s == "mach") return 0;
+  if (probEn == 7 /*CrossShock*/ && icFlag == 1) {
+    if (s == "crossShockDensity") return 1;
+    if (s == "crossShockInletXVel") return 2;
+    if (s == "crossShockBottomYVel") return 3;
+  }
+  if (probEn == 4 /*Riemann*/) {
+    if (icFlag == 1 && s == "riemannTopRightPressure") return 4;
+    if (icFlag == 2) {
+      if (s == "riemannTopRightPressure") return 5;
+      if (s == "riemannTopRightXVel") return 6;
+      if (s == "riemannTopRightYVel") return 7;
+      if (s == "riemannTopRightDensity") return 8;
+      if (s == "riemannBotLeftPressure") return 9;
+    }
+  }
+  return kInvalid;
+}
+
+// impl/swe_2d_parametrization_helpers.hpp:104-128
+int swe_ic_index(int icFlag, const std::string &s) {
+  if (icFlag == 1) {
+    if (s == "pulseMagnitude") return 0;
+    if (s == "pulseX") return 1;
+    if (s == "pulseY") return 2;
+  } else if (icFlag == 2) {
+    if (s == "pulseMagnitude1") return 3;
+    if (s == "pulseX1") return 4;
+    if (s == "pulseY1") return 5;
+    if (s == "pulseMagnitude2") return 6;
+    if (s == "pulseX2") return 7;
+    if (s == "pulseY2") return 8;
+  }
+  return kInvalid;
+}
+
+// -------------------------------------------------------- initial conditions
+double energy2(double gm1inv, const double *prim, int n) {
+  // euler_compute_energy.hpp:55-110 (prim[last] = p)
+  constexpr double half = 1. / 2.;
+  if (n == 3) {
+    const double usq = prim[1] * prim[1];
+    return prim[2] * gm1inv + half * prim[0] * (usq);
+  }
+  if (n == 4) {
+    const double usq = prim[1] * prim[1], vsq = prim[2] * prim[2];
+    return prim[3] * gm1inv + half * prim[0] * (usq + vsq);
+  }
+  const double usq = prim[1] * prim[1], vsq = prim[2] * prim[2], wsq = prim[3] * prim[3];
+  return prim[4] * gm1inv + half * prim[0] * (usq + vsq + wsq);
+}
+
+void initial_condition(const pda_problem &P, std::vector<double> &st) {
+  const Mesh &m = *P.mesh;
+  const int64_t N = m.stencilMeshSize;
+  st.assign((size_t)N * P.ndpc, 0.0);
+  const double *x = m.x.data(), *y = m.y.data(), *z = m.z.data();
+  if (P.family == PDA_EULER1D) {
+    // impl/euler_1d_initial_condition.hpp
+    const double gamma = P.phys.gamma;
+    const double gm1inv = 1. / (gamma - 1.);
+    double prim[3] = {0, 0, 0};
+    for (int64_t i = 0; i < N; ++i) {
+      if (P.probEnum == 0) {
+        prim[0] = 1. + 0.2 * std::sin(M_PI * x[i]);
+        prim[1] = 1.;
+        prim[2] = 1.;
+      } else if (P.probEnum == 1) {
+        if (x[i] <= 0.) { prim[0] = 1.; prim[1] = 0.; prim[2] = 1.; }
+        if (x[i] > 0.) { prim[0] = 0.125; prim[1] = 0.; prim[2] = 0.1; }
+      } else if (P.probEnum == 2) {
+        if (x[i] <= 0.) { prim[0] = 0.445; prim[1] = 0.698; prim[2] = 3.528; }
+        else if (x[i] > 0.) { prim[0] = 0.5; prim[1] = 0.; prim[2] = 0.571; }
+      } else {
+        if (x[i] <= -4.) { prim[0] = 27. / 7.; prim[1] = 2.629369; prim[2] = 31. / 3.; }
+        else { prim[0] = 1. + (1. / 5.) * std::sin(5. * x[i]); prim[1] = 0.; prim[2] = 1.; }
+      }
+      st[i * 3] = prim[0];
+      st[i * 3 + 1] = prim[0] * prim[1];
+      st[i * 3 + 2] = energy2(gm1inv, prim, 3);
+    }
+  } else if (P.family == PDA_EULER2D) {
+    const double gamma = P.phys.gamma;
+    const double gm1inv = 1. / (gamma - 1.);
+    double prim[4] = {0, 0, 0, 0};
+    if (P.probEnum == 0) {
+      // sin2dEulerIC (impl/euler_2d_initial_condition.hpp:57-83)
+      for (int64_t i = 0; i < N; ++i) {
+        prim[0] = 1. + (1. / 5.) * std::sin(M_PI * (x[i] + y[i]));
+        prim[1] = prim[2] = prim[3] = 1.;
+        st[i * 4] = prim[0];
+        st[i * 4 + 1] = prim[0] * prim[1];
+        st[i * 4 + 2] = prim[0] * prim[2];
+        st[i * 4 + 3] = energy2(gm1inv, prim, 4);
+      }
+    } else if (P.probEnum == 4 && P.icFlag == 1) {
+      // riemann2dIC1 (:256-297)
+      const double pTR = P.icParams[4];
+      const double x0 = 1. / 2., y0 = 1. / 2.;
+      for (int64_t i = 0; i < N; ++i) {
+        if (x[i] >= x0 && y[i] >= y0) { prim[0] = 0.5313; prim[1] = 0.; prim[2] = 0.; prim[3] = pTR; }
+        else if (x[i] < x0 && y[i] >= y0) { prim[0] = 1.; prim[1] = 0.7276; prim[2] = 0.; prim[3] = 1.; }
+        else if (x[i] < x0 && y[i] < y0) { prim[0] = 0.8; prim[1] = 0.; prim[2] = 0.; prim[3] = 1.; }
+        else if (x[i] > x0 && y[i] < y0) { prim[0] = 1.; prim[1] = 0.; prim[2] = 0.7276; prim[3] = 1.; }
+        st[i * 4] = prim[0];
+        st[i * 4 + 1] = prim[0] * prim[1];
+        st[i * 4 + 2] = prim[0] * prim[2];
+        st[i * 4 + 3] = energy2(gm1inv, prim, 4);
+      }
+    } else if (P.probEnum == 4 && P.icFlag == 2) {
+      // riemann2dIC2 (:309-380): unspecified quadrants from the compatibility relations
+      const double topRightPressure = P.icParams[5], topRightXVel = P.icParams[6],
+                   topRightYVel = P.icParams[7], topRightDensity = P.icParams[8],
+                   botLeftPressure = P.icParams[9];
+      PDA_REQUIRE(!(topRightPressure <= botLeftPressure), PDA_ERR_INVALID_ARGUMENT,
+                  "INVALID: riemannTopRightPressure <= riemannBotLeftPressure");
+      const double one = 1., two = 2., four = 4.;
+      const double x0 = 0.8, y0 = 0.8;
+      const double eps = (gamma - one) / (gamma + one);
+      const double fac13 = topRightPressure / botLeftPressure;
+      const double fac43 = (one / (two * (one + two * eps))) *
+                           (eps * (fac13 + one) +
+                            std::sqrt(std::pow(eps * (fac13 + one), 2) + four * (one + two * eps) * fac13));
+      const double topLeftPressure = fac43 * botLeftPressure;
+      const double botRightPressure = topLeftPressure;
+      const double topLeftYVel = topRightYVel;
+      const double botRightXVel = topRightXVel;
+      const double topLeftDensity = topRightDensity * (topLeftPressure / topRightPressure + eps) /
+                                    (1 + eps * topLeftPressure / topRightDensity);
+      const double botRightDensity = topLeftDensity;
+      const double psi21_sq = (topLeftPressure - topRightPressure) * (topLeftDensity - topRightDensity) /
+                              (topLeftDensity * topRightDensity);
+      const double topLeftXVel = std::sqrt(psi21_sq) + topRightXVel;
+      const double psi41_sq = (botRightPressure - topRightPressure) * (botRightDensity - topRightDensity) /
+                              (botRightDensity * topRightDensity);
+      const double botRightYVel = std::sqrt(psi41_sq) + topRightYVel;
+      const double botLeftXVel = topLeftXVel;
+      const double botLeftYVel = botRightYVel;
+      const double botLeftDensity = topLeftDensity * (botLeftPressure - topLeftPressure) /
+                                    ((botLeftPressure - topLeftPressure) - psi41_sq * topLeftDensity);
+      for (int64_t i = 0; i < N; ++i) {
+        if (x[i] >= x0 && y[i] >= y0) {
+          prim[0] = topRightDensity; prim[1] = topRightXVel; prim[2] = topRightYVel; prim[3] = topRightPressure;
+        } else if (x[i] < x0 && y[i] >= y0) {
+          prim[0] = topLeftDensity; prim[1] = topLeftXVel; prim[2] = topLeftYVel; prim[3] = topLeftPressure;
+        } else if (x[i] < x0 && y[i] < y0) {
+          prim[0] = botLeftDensity; prim[1] = botLeftXVel; prim[2] = botLeftYVel; prim[3] = botLeftPressure;
+        } else if (x[i] > x0 && y[i] < y0) {
+          prim[0] = botRightDensity; prim[1] = botRightXVel; prim[2] = botRightYVel; prim[3] = botRightPressure;
+        }
+        st[i * 4] = prim[0];
+        st[i * 4 + 1] = prim[0] * prim[1];
+        st[i * 4 + 2] = prim[0] * prim[2];
+        st[i * 4 + 3] = energy2(gm1inv, prim, 4);
+      }
+    } else if (P.probEnum == 8) {
+      // testingonlyneumann: no initial condition (zeros)
+    } else {
+      throw Error(PDA_ERR_UNSUPPORTED, "Euler2d: initial condition not available for this problem");
+    }
+  } else if (P.family == PDA_EULER3D) {
+    // euler3dsmoothInitialCondition (impl/euler_3d_initial_condition.hpp:57-85)
+    const double gamma = P.phys.gamma;
+    const double gm1inv = 1. / (gamma - 1.);
+    double prim[5];
+    for (int64_t i = 0; i < N; ++i) {
+      prim[0] = 1.0 + 0.2 * std::sin(M_PI * (x[i] + y[i] + z[i]));
+      prim[1] = prim[2] = prim[3] = 1.0;
+      prim[4] = 1.;
+      st[i * 5] = prim[0];
+      st[i * 5 + 1] = prim[0] * prim[1];
+      st[i * 5 + 2] = prim[0] * prim[2];
+      st[i * 5 + 3] = prim[0] * prim[3];
+      st[i * 5 + 4] = energy2(gm1inv, prim, 5);
+    }
+  } else {
+    // GaussianPulse / DoubleGaussianPulse (impl/swe_2d_initial_condition.hpp:55-106)
+    const std::vector<double> &c = P.icParams;
+    for (int64_t i = 0; i < N; ++i) {
+      if (P.icFlag == 1) {
+        const double dx1 = x[i] - c[1], dy1 = y[i] - c[2];
+        const double r = std::sqrt(dx1 * dx1 + dy1 * dy1);
+        st[i * 3] = 1. + c[0] * std::exp(-(r * r));
+      } else {
+        const double dx1 = x[i] - c[4], dy1 = y[i] - c[5];
+        const double r1 = std::sqrt(dx1 * dx1 + dy1 * dy1);
+        const double dx2 = x[i] - c[7], dy2 = y[i] - c[8];
+        const double r2 = std::sqrt(dx2 * dx2 + dy2 * dy2);
+        st[i * 3] = 1. + c[3] * std::exp(-(r1 * r1)) + c[6] * std::exp(-(r2 * r2));
+      }
+      st[i * 3 + 1] = 0.;
+      st[i * 3 + 2] = 0.;
+    }
+  }
+}
+
+// ------------------------------------------------------- stencil tables
+// graph column of the neighbour at distance k+1 on the minus / plus side of
+// an axis (functor_reconstruct_from_state.hpp:257-262, :432-437, :614-619).
+int col_minus(int dim, int ax, int k) {
+  if (dim == 1) return 1 + 2 * k;
+  if (dim == 2) return (ax == 0 ? 1 : 4) + 4 * k;
+  return (ax == 0 ? 1 : ax == 1 ? 4 : 5) + 6 * k;
+}
+int col_plus(int dim, int ax, int k) {
+  if (dim == 1) return 2 + 2 * k;
+  if (dim == 2) return (ax == 0 ? 3 : 2) + 4 * k;
+  return (ax == 0 ? 3 : ax == 1 ? 2 : 6) + 6 * k;
+}
+
+// Source cell of ghost layer L on one side of row r, following the ghost
+// fillers: Ghost2dNeumannFiller (euler_2d_ghost_filler_neumann.hpp:101-276)
+// and InviscidWallFiller (swe_2d_ghost_filler_inviscid_wall.hpp:99-278), which
+// share the index rule, and Ghost1dNeumannFiller
+// (euler_1d_ghost_filler.hpp:81-144), whose second and third layers copy the
+// opposite-side neighbours also for the second cell from the wall.
+int ghost_source(const Mesh &m, int bc, int64_t r, int ax, bool minusSide, int L) {
+  auto same = [&](int k) {
+    return m.g(r, minusSide ? col_minus(m.dim, ax, k) : col_plus(m.dim, ax, k));
+  };
+  auto opp = [&](int k) {
+    return m.g(r, minusSide ? col_plus(m.dim, ax, k) : col_minus(m.dim, ax, k));
+  };
+  const int cell = m.g(r, 0);
+  if (bc == BC_NEUMANN1D) {
+    if (L == 0) return cell;
+    return opp(L - 1);
+  }
+  if (bc == BC_MIRROR2D) {
+    if (L == 0) return cell;
+    if (L == 1) return same(0) == -1 ? opp(0) : same(0);
+    const int m0 = same(0), m1 = same(1);
+    int ind = cell;
+    if (m1 != -1 && m0 != -1) ind = m1;
+    if (m1 == -1 && m0 != -1) ind = cell;
+    if (m1 == -1 && m0 == -1) ind = opp(1);
+    return ind;
+  }
+  throw Error(PDA_ERR_UNSUPPORTED, "this problem has no ghost-cell rule for meshes with boundaries");
+}
+
+// Stencil of the scheme (positions -h..h) for every row of the table.
+void build_stencil(const pda_problem &P, Table &T, const std::vector<int32_t> &rowList, bool allowGhost) {
+  const Mesh &m = *P.mesh;
+  const int S = 2 * P.h + 1, D = P.dim;
+  T.rows.assign(rowList.begin(), rowList.end());
+  T.cell.resize(rowList.size());
+  T.src.assign(rowList.size() * D * S, 0);
+  T.flip.assign(rowList.size() * D * S, 0);
+  for (size_t e = 0; e < rowList.size(); ++e) {
+    const int64_t r = rowList[e];
+    T.cell[e] = m.g(r, 0);
+    for (int ax = 0; ax < D; ++ax) {
+      const size_t base = (e * D + ax) * S;
+      T.src[base + P.h] = m.g(r, 0);
+      for (int k = 1; k <= P.h; ++k) {
+        for (int side = 0; side < 2; ++side) {
+          const bool minus = side == 0;
+          const int c = m.g(r, minus ? col_minus(D, ax, k - 1) : col_plus(D, ax, k - 1));
+          const size_t pos = base + (minus ? P.h - k : P.h + k);
+          if (c != -1) {
+            T.src[pos] = c;
+          } else {
+            PDA_REQUIRE(allowGhost, PDA_ERR_INTERNAL, "unexpected boundary neighbour in an inner row");
+            const int gsrc = ghost_source(m, P.bc, r, ax, minus, k - 1);
+            PDA_REQUIRE(gsrc >= 0, PDA_ERR_INVALID_ARGUMENT,
+                        "mesh too small for the ghost layers of this scheme");
+            T.src[pos] = gsrc;
+            T.flip[pos] = 1;
+          }
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------ CSR pattern
+// initializeJacobian (euler_2d_prob_class.hpp:223-237, :314-387 and the
+// 1d/3d/swe analogues): Eigen setFromTriplets + makeCompressed gives, per row,
+// the sorted distinct columns.
+void build_pattern(pda_problem &P) {
+  if (P.patternBuilt) return;
+  const Mesh &m = *P.mesh;
+  const int nd = P.ndpc;
+  const int nnbInner = 2 * P.dim * P.h;
+  std::vector<char> isNear(m.sampleMeshSize, 0);
+  for (int32_t r : m.nearBd) isNear[r] = 1;
+  P.rowBlocks.assign(m.sampleMeshSize, {});
+  int64_t nnz = 0;
+  for (int64_t r = 0; r < m.sampleMeshSize; ++r) {
+    std::vector<int32_t> &b = P.rowBlocks[r];
+    b.push_back(m.g(r, 0));
+    if (isNear[r]) {
+      for (int i = 1; i <= 2 * P.dim; ++i)
+        if (m.g(r, i) != -1) b.push_back(m.g(r, i));
+    } else {
+      for (int i = 1; i <= nnbInner; ++i) b.push_back(m.g(r, i));
+    }
+    std::sort(b.begin(), b.end());
+    b.erase(std::unique(b.begin(), b.end()), b.end());
+    nnz += (int64_t)b.size() * nd * nd;
+  }
+  PDA_REQUIRE(nnz < INT32_MAX, PDA_ERR_UNSUPPORTED, "Jacobian has more than 2^31-1 entries (int32 CSR)");
+  P.rowptr.assign((size_t)m.sampleMeshSize * nd + 1, 0);
+  P.colidx.resize((size_t)nnz);
+  int64_t q = 0;
+  for (int64_t r = 0; r < m.sampleMeshSize; ++r) {
+    const std::vector<int32_t> &b = P.rowBlocks[r];
+    for (int k = 0; k < nd; ++k) {
+      P.rowptr[(size_t)r * nd + k] = (int)q;
+      for (int32_t c : b)
+        for (int j = 0; j < nd; ++j) P.colidx[q++] = c * nd + j;
+    }
+  }
+  P.rowptr[(size_t)m.sampleMeshSize * nd] = (int)q;
+  P.patternBuilt = true;
+}
+
+void pattern_to_device(pda_problem &P) {
+  build_pattern(P);
+  if (P.d_rowptr.p && P.d_rowptr.n == P.rowptr.size()) return;
+  P.d_rowptr.upload(P.rowptr);
+  P.d_colidx.upload(P.colidx);
+}
+
+int block_offset(const pda_problem &P, int64_t r, int32_t cell) {
+  const std::vector<int32_t> &b = P.rowBlocks[r];
+  auto it = std::lower_bound(b.begin(), b.end(), cell);
+  if (it == b.end() || *it != cell) throw Error(PDA_ERR_INTERNAL, "cell missing from CSR row pattern");
+  return (int)(it - b.begin()) * P.ndpc;
+}
+
+// BC factors of fillJacFactorsForCellBd (euler_2d_prob_class.hpp:1115-1129,
+// swe_2d_prob_class.hpp:839-854; 1d all ones, euler_1d_prob_class.hpp:608-610)
+void jac_factors(const pda_problem &P, int ax, double *f) {
+  for (int j = 0; j < P.ndpc; ++j) f[j] = 1.;
+  if (P.family == PDA_SWE2D) f[ax == 0 ? 1 : 2] = -1.;
+}
+
+void build_inner_table(pda_problem &P, bool withJ) {
+  if (withJ ? P.innerBuiltJ : P.innerBuiltV) return;
+  const Mesh &m = *P.mesh;
+  build_stencil(P, P.innerT, m.inner, false);
+  if (withJ) {
+    build_pattern(P);
+    P.innerT.jpos.resize(P.innerT.src.size());
+    const int S = 2 * P.h + 1;
+    for (size_t e = 0; e < m.inner.size(); ++e)
+      for (int ax = 0; ax < P.dim; ++ax)
+        for (int s = 0; s < S; ++s) {
+          const size_t pos = (e * P.dim + ax) * S + s;
+          P.innerT.jpos[pos] = block_offset(P, m.inner[e], P.innerT.src[pos]);
+        }
+    P.innerBuiltJ = true;
+  }
+  P.innerT.dirty = true;
+  P.innerBuiltV = true;
+}
+
+void build_near_table(pda_problem &P, bool withJ) {
+  const Mesh &m = *P.mesh;
+  if (!withJ) {
+    build_stencil(P, P.nearT, m.nearBd, true);
+    P.nearT.dirty = true;
+    return;
+  }
+  if (P.nearBuiltJ) return;
+  build_pattern(P);
+  Table &T = P.nearT;
+  const size_t n = m.nearBd.size();
+  T.src1.assign(n * P.dim * 3, 0);
+  T.flip1.assign(n * P.dim * 3, 0);
+  T.jpos1.assign(n * P.dim * 3, -1);
+  T.jfac.assign(n * P.dim * P.ndpc, 1.0);
+  for (size_t e = 0; e < n; ++e) {
+    const int64_t r = m.nearBd[e];
+    for (int ax = 0; ax < P.dim; ++ax) {
+      const size_t base = (e * P.dim + ax) * 3;
+      T.src1[base + 1] = m.g(r, 0);
+      T.jpos1[base + 1] = block_offset(P, r, m.g(r, 0));
+      const int cm = m.g(r, col_minus(P.dim, ax, 0)), cp = m.g(r, col_plus(P.dim, ax, 0));
+      if (cm != -1) {
+        T.src1[base] = cm;
+        T.jpos1[base] = block_offset(P, r, cm);
+      } else {
+        T.src1[base] = ghost_source(m, P.bc, r, ax, true, 0);
+        T.flip1[base] = 1;
+      }
+      if (cp != -1) {
+        T.src1[base + 2] = cp;
+        T.jpos1[base + 2] = block_offset(P, r, cp);
+      } else {
+        T.src1[base + 2] = ghost_source(m, P.bc, r, ax, false, 0);
+        T.flip1[base + 2] = 1;
+      }
+      jac_factors(P, ax, &T.jfac[(e * P.dim + ax) * P.ndpc]);
+    }
+  }
+  T.dirty = true;
+  P.nearBuiltJ = true;
+}
+
+void check_launch(pda_problem &P, int n = 1) {
+  P.launches += n;
+  PDA_CUDA(cudaGetLastError());
+}
+
+// --------------------------------------------------------------- evaluation
+void velocity(pda_problem &P, const double *U, double *V, cudaEvent_t *ev = nullptr) {
+  if (P.useStruct) {
+    const Box &b = P.box;
+    double *Fb[3] = {nullptr, nullptr, nullptr};
+    for (int a = 0; a < P.dim; ++a) {
+      long nf = 1;
+      for (int c = 0; c < 3; ++c) nf *= (long)(b.hi[c] - b.lo[c] + (c == a ? 1 : 0));
+      P.F[a].alloc((size_t)nf * P.ndpc);
+      Fb[a] = P.F[a].p;
+    }
+    int nl = 0;
+    P.L->struct_velocity(P.scheme, b, P.margs, P.phys, U, Fb, V, P.stream, &nl, ev);
+    check_launch(P, nl);
+  } else {
+    build_inner_table(P, false);
+    P.innerT.sync();
+    if (P.innerT.t.nrows > 0) {
+      P.L->rows_velocity(P.scheme, P.innerT.t, P.margs, P.phys, U, V, P.stream);
+      check_launch(P);
+    }
+  }
+  P.nearT.sync();
+  if (P.nearT.t.nrows > 0) {
+    P.L->rows_velocity(P.scheme, P.nearT.t, P.margs, P.phys, U, V, P.stream);
+    check_launch(P);
+  }
+  if (ev) cudaEventRecord(ev[P.dim + 2], P.stream);
+}
+
+void velocity_and_jacobian(pda_problem &P, const double *U, double *V, double *J) {
+  build_inner_table(P, true);
+  build_near_table(P, true);
+  pattern_to_device(P);
+  P.innerT.sync();
+  P.nearT.sync();
+  if (P.innerT.t.nrows > 0) {
+    P.L->rows_vj_inner(P.scheme, P.innerT.t, P.margs, P.phys, U, P.d_rowptr.p, V, J, P.stream);
+    check_launch(P);
+  }
+  if (P.nearT.t.nrows > 0) {
+    P.L->rows_vj_nearbd(P.scheme, P.nearT.t, P.margs, P.phys, U, P.d_rowptr.p, V, J, P.stream);
+    check_launch(P);
+  }
+}
+
+// ------------------------------------------------------------------ create
+void create_problem(pda_problem &P, const Mesh &m, int family, int probEn, int scheme, int icFlag,
+                    const char *const *names, const double *vals, int np, void *stream) {
+  PDA_REQUIRE(family >= 0 && family <= 3, PDA_ERR_INVALID_ARGUMENT, "invalid problem family");
+  PDA_REQUIRE(scheme >= 0 && scheme <= 2, PDA_ERR_INVALID_ARGUMENT, "invalid reconstruction scheme");
+  PDA_REQUIRE(np >= 0 && (np == 0 || (names && vals)), PDA_ERR_INVALID_ARGUMENT, "invalid parameter arrays");
+  const int dims[4] = {1, 2, 3, 2};
+  const int ndpcs[4] = {3, 4, 5, 3};
+  PDA_REQUIRE(m.dim == dims[family], PDA_ERR_INVALID_ARGUMENT, "mesh dimensionality does not match the problem");
+  P.mesh = &m;
+  P.family = family;
+  P.probEnum = probEn;
+  P.scheme = scheme;
+  P.icFlag = icFlag <= 0 ? 1 : icFlag;
+  P.dim = dims[family];
+  P.ndpc = ndpcs[family];
+  P.h = scheme + 1;
+  // stencilSizeCompatibleWithInviscidFluxReconstruction (schemes_info.hpp:96-104)
+  PDA_REQUIRE(m.stencil >= 2 * P.h + 1, PDA_ERR_INVALID_ARGUMENT,
+              "mesh stencil size too small for the reconstruction scheme");
+  P.stream = (cudaStream_t)stream;
+  P.dofsSample = m.sampleMeshSize * P.ndpc;
+  P.dofsStencil = m.stencilMeshSize * P.ndpc;
+  P.phys = Phys{1.4, 9.8, -3.0};
+  for (int a = 0; a < 3; ++a) {
+    P.margs.hinv[a] = m.dxInv[a];
+    P.margs.reflect[a] = -1;
+  }
+  P.margs.dim = P.dim;
+  std::vector<std::pair<std::string, double>> params;
+  for (int i = 0; i < np; ++i) {
+    PDA_REQUIRE(names[i], PDA_ERR_INVALID_ARGUMENT, "null parameter name");
+    params.emplace_back(names[i], vals[i]);
+  }
+  if (family == PDA_EULER1D) {
+    // euler_1d_prob_class.hpp:97-112 (gamma hard-wired 1.4)
+    PDA_REQUIRE(probEn >= 0 && probEn <= 3, PDA_ERR_INVALID_ARGUMENT, "invalid Euler1d problem");
+    PDA_REQUIRE(params.empty(), PDA_ERR_INVALID_ARGUMENT, "Euler1d takes no parameters");
+    P.physParams = {1.4};
+    P.bc = probEn == 0 ? BC_NONE : BC_NEUMANN1D;
+  } else if (family == PDA_EULER3D) {
+    PDA_REQUIRE(probEn == 0, PDA_ERR_UNSUPPORTED, "Euler3d: only PeriodicSmooth is supported");
+    PDA_REQUIRE(params.empty(), PDA_ERR_INVALID_ARGUMENT, "Euler3d takes no parameters");
+    P.physParams = {1.4};
+    P.bc = BC_NONE;
+  } else if (family == PDA_EULER2D) {
+    // euler2d.hpp:88-173; impl/euler_2d_parametrization_helpers.hpp:75-93
+    PDA_REQUIRE(probEn == 0 || probEn == 2 || probEn == 4 || probEn == 8, PDA_ERR_UNSUPPORTED,
+                "Euler2d: supported problems are PeriodicSmooth, SedovFull (Neumann BCs), Riemann");
+    const bool validIc = (probEn == 4) ? (P.icFlag == 1 || P.icFlag == 2) : P.icFlag == 1;
+    PDA_REQUIRE(validIc, PDA_ERR_INVALID_ARGUMENT, "Euler2d: invalid icFlag for the given problem enum");
+    P.physParams = {1.4};
+    P.icParams = {9, 0.1, 10., 1., 0.4, 1.5, 0.0, 0.0, 1.5, 0.029};
+    if (!params.empty())
+      PDA_REQUIRE(probEn == 4 || probEn == 5, PDA_ERR_INVALID_ARGUMENT,
+                  "Euler2d: custom parametrization only valid for Euler2d::{Riemann, NormalShock}");
+    for (auto &kv : params) {
+      if (kv.first == "gamma") {
+        P.physParams[0] = kv.second;
+        continue;
+      }
+      const int idx = euler2d_ic_index(probEn, P.icFlag, kv.first);
+      PDA_REQUIRE(idx != kInvalid, PDA_ERR_INVALID_ARGUMENT, "Euler2d: invalid parameter name " + kv.first);
+      P.icParams[idx] = kv.second;
+    }
+    P.bc = probEn == 0 ? BC_NONE : BC_MIRROR2D;
+    if (probEn == 2) PDA_REQUIRE(false, PDA_ERR_UNSUPPORTED, "Euler2d::SedovFull initial condition not available");
+  } else {
+    // swe2d.hpp:143-195; impl/swe_2d_parametrization_helpers.hpp:59-95
+    PDA_REQUIRE(probEn == 0, PDA_ERR_UNSUPPORTED, "Swe2d: only SlipWall is supported");
+    PDA_REQUIRE(P.icFlag == 1 || P.icFlag == 2, PDA_ERR_INVALID_ARGUMENT,
+                "2D swe: for Swed2d::SlipWall, invalid icFlag");
+    P.physParams = {9.8, -3.};
+    P.icParams = {1. / 8, 1, 1, 1. / 10, -2, -2, 1. / 8, 2, 2};
+    for (auto &kv : params) {
+      if (kv.first == "gravity") { P.physParams[0] = kv.second; continue; }
+      if (kv.first == "coriolis") { P.physParams[1] = kv.second; continue; }
+      const int idx = swe_ic_index(P.icFlag, kv.first);
+      PDA_REQUIRE(idx != kInvalid, PDA_ERR_INVALID_ARGUMENT,
+                  "2D swe: create_problem_eigen: one or more params in user-provided map is invalid");
+      P.icParams[idx] = kv.second;
+    }
+    P.bc = BC_MIRROR2D;
+    P.margs.reflect[0] = 1;
+    P.margs.reflect[1] = 2;
+  }
+  if (family == PDA_SWE2D) {
+    P.phys.gravity = P.physParams[0];
+    P.phys.coriolis = P.physParams[1];
+  } else {
+    P.phys.gamma = P.physParams[0];
+  }
+  if (P.bc == BC_NONE)
+    PDA_REQUIRE(m.nearBd.empty(), PDA_ERR_UNSUPPORTED,
+                "this problem defines no boundary conditions: the mesh must be fully periodic");
+  switch (family) {
+    case PDA_EULER1D: P.L = &launchers_euler1d(); break;
+    case PDA_EULER2D: P.L = &launchers_euler2d(); break;
+    case PDA_EULER3D: P.L = &launchers_euler3d(); break;
+    default: P.L = &launchers_swe2d(); break;
+  }
+  // structured interior box
+  P.useStruct = false;
+  if (m.structured) {
+    const int hm = (m.stencil - 1) / 2;
+    Box b{};
+    long cells = 1;
+    for (int a = 0; a < 3; ++a) {
+      b.n[a] = a < P.dim ? m.n[a] : 1;
+      b.periodic[a] = a < P.dim ? m.periodic[a] : 0;
+      if (a >= P.dim || b.periodic[a]) {
+        b.lo[a] = 0;
+        b.hi[a] = b.n[a];
+      } else {
+        b.lo[a] = std::min(hm, b.n[a]);
+        b.hi[a] = std::max(b.lo[a], b.n[a] - hm);
+      }
+      cells *= (long)(b.hi[a] - b.lo[a]);
+    }
+    if (cells == (long)m.inner.size()) {
+      P.box = b;
+      P.useStruct = true;
+    }
+  }
+  build_near_table(P, false);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ steppers
+namespace {
+
+void stepper_buffers(pda_problem &P, int nr) {
+  P.aux.alloc(P.dofsStencil);
+  for (int i = 0; i < nr; ++i) P.r[i].alloc(P.dofsSample);
+}
+
+// One step of SSP-RK3 (ode_explicit_stepper_without_mass_matrix.hpp:230-282).
+void ssprk3_step(pda_problem &P, double *U, double t, double dt) {
+  const long n = (long)P.dofsStencil;
+  double *r0 = P.r[0].p, *aux = P.aux.p;
+  velocity(P, U, r0);
+  launch_axpby_stage(0, aux, U, r0, nullptr, 0., dt, 0., 0., nullptr, nullptr, n, P.stream);
+  check_launch(P);
+  velocity(P, aux, r0);
+  const double fourInv = 1. / 4., threeOvFour = 3. / 4.;
+  launch_axpby_stage(1, aux, U, r0, nullptr, fourInv, threeOvFour, fourInv * dt, 0., nullptr, nullptr, n,
+                     P.stream);
+  check_launch(P);
+  velocity(P, aux, r0);
+  const double oneOvThree = 1. / 3., twoOvThree = 2. / 3.;
+  launch_axpby_stage(1, U, aux, r0, nullptr, oneOvThree, twoOvThree, twoOvThree * dt, 0., nullptr, nullptr,
+                     n, P.stream);
+  check_launch(P);
+  (void)t;
+}
+
+// One step of RK4 (ode_explicit_stepper_without_mass_matrix.hpp:284-336).
+void rk4_step(pda_problem &P, double *U, double t, double dt) {
+  const long n = (long)P.dofsStencil;
+  const double dt2 = dt / 2., dt6 = dt / 6., dt3 = dt / 3.;
+  double *aux = P.aux.p;
+  velocity(P, U, P.r[0].p);
+  launch_axpby_stage(0, aux, U, P.r[0].p, nullptr, 0., dt2, 0., 0., nullptr, nullptr, n, P.stream);
+  check_launch(P);
+  velocity(P, aux, P.r[1].p);
+  launch_axpby_stage(0, aux, U, P.r[1].p, nullptr, 0., dt2, 0., 0., nullptr, nullptr, n, P.stream);
+  check_launch(P);
+  velocity(P, aux, P.r[2].p);
+  launch_axpby_stage(0, aux, U, P.r[2].p, nullptr, 0., dt, 0., 0., nullptr, nullptr, n, P.stream);
+  check_launch(P);
+  velocity(P, aux, P.r[3].p);
+  launch_axpby_stage(2, U, P.r[0].p, P.r[1].p, P.r[2].p, 0., dt3, 0., dt6, P.r[3].p, nullptr, n, P.stream);
+  check_launch(P);
+  (void)t;
+}
+
+void advance(pda_problem &P, int kind, double *U, double t0, double dt, int64_t nsteps, bool useGraph) {
+  PDA_REQUIRE(P.dofsSample == P.dofsStencil, PDA_ERR_UNSUPPORTED,
+              "time integration needs a full mesh (sample meshes integrate in a reduced space)");
+  PDA_REQUIRE(nsteps >= 0, PDA_ERR_INVALID_ARGUMENT, "negative step count");
+  stepper_buffers(P, kind == 0 ? 1 : 4);
+  auto step = [&](double t) {
+    if (kind == 0) ssprk3_step(P, U, t, dt);
+    else rk4_step(P, U, t, dt);
+  };
+  if (!useGraph || P.stream == nullptr) {
+    double t = t0;
+    for (int64_t s = 0; s < nsteps; ++s) {
+      step(t);
+      t = t + dt;
+    }
+    return;
+  }
+  // Capture one step and replay it: the kernels do not depend on t for the
+  // supported boundary conditions.  The graph bakes in U and dt.
+  if (P.stepGraph && (P.stepGraphKind != kind || P.stepGraphDt != dt || P.stepGraphU != U)) {
+    cudaGraphExecDestroy(P.stepGraph);
+    P.stepGraph = nullptr;
+  }
+  if (!P.stepGraph) {
+    // lazily built tables and buffers must exist before capture
+    velocity(P, U, P.r[0].p);
+    PDA_CUDA(cudaStreamSynchronize(P.stream));
+    cudaGraph_t g;
+    PDA_CUDA(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
+    const int64_t before = P.launches;
+    try {
+      step(t0);
+    } catch (...) {
+      cudaStreamEndCapture(P.stream, &g);
+      throw;
+    }
+    PDA_CUDA(cudaStreamEndCapture(P.stream, &g));
+    P.stepGraphLaunches = P.launches - before;
+    P.launches = before;
+    PDA_CUDA(cudaGraphInstantiate(&P.stepGraph, g, 0));
+    cudaGraphDestroy(g);
+    P.stepGraphKind = kind;
+    P.stepGraphDt = dt;
+    P.stepGraphU = U;
+  }
+  for (int64_t s = 0; s < nsteps; ++s) PDA_CUDA(cudaGraphLaunch(P.stepGraph, P.stream));
+  P.launches += nsteps * P.stepGraphLaunches;
+}
+
+}  // namespace
+}  // namespace pda
+
+// ===================================================================== C ABI
+using pda::Error;
+
+#define PDA_API_BEGIN try {
+#define PDA_API_END                                   \
+  return PDA_OK;                                      \
+  }                                                   \
+  catch (const pda::Error &e) {                       \
+    pda::set_last_error(e.what());                    \
+    return e.code;                                    \
+  }                                                   \
+  catch (const std::bad_alloc &) {                    \
+    pda::set_last_error("host out of memory");        \
+    return PDA_ERR_OUT_OF_MEMORY;                     \
+  }                                                   \
+  catch (const std::exception &e) {                   \
+    pda::set_last_error(e.what());                    \
+    return PDA_ERR_INTERNAL;                          \
+  }
+
+extern "C" {
+
+const char *pda_last_error(void) { return pda::g_last_error.c_str(); }
+const char *pda_version(void) { return "pda_gb300 0.1.0"; }
+
+pda_status pda_mesh_load(const char *dir, pda_mesh **out) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(dir && out, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  std::unique_ptr<pda_mesh> m(new pda_mesh);
+  m->m = pda::mesh_load(dir);
+  *out = m.release();
+  PDA_API_END
+}
+
+pda_status pda_mesh_create_full(const int n[3], const double bounds[6], int stencil, const int periodic[3],
+                                pda_mesh **out) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(n && bounds && periodic && out, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  std::unique_ptr<pda_mesh> m(new pda_mesh);
+  m->m = pda::mesh_generate_full(n, bounds, stencil, periodic);
+  *out = m.release();
+  PDA_API_END
+}
+
+pda_status pda_mesh_create_sample(const pda_mesh *full, const int64_t *gids, int64_t n, pda_mesh **out,
+                                  int64_t *stencil_gids_out) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(full && out && (n == 0 || gids), PDA_ERR_INVALID_ARGUMENT, "null argument");
+  PDA_REQUIRE(n > 0, PDA_ERR_INVALID_ARGUMENT, "empty sample mesh");
+  std::vector<int64_t> g(gids, gids + n), st;
+  std::unique_ptr<pda_mesh> m(new pda_mesh);
+  m->m = pda::mesh_sample(full->m, g, &st);
+  if (stencil_gids_out) std::copy(st.begin(), st.end(), stencil_gids_out);
+  *out = m.release();
+  PDA_API_END
+}
+
+pda_status pda_mesh_write(const pda_mesh *m, const char *dir) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(m && dir, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  pda::mesh_write(m->m, dir);
+  PDA_API_END
+}
+
+pda_status pda_mesh_info(const pda_mesh *mm, int dims[3], int64_t sizes[4], double dx[3], double dxinv[3],
+                         int flags[2]) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(mm, PDA_ERR_INVALID_ARGUMENT, "null mesh");
+  const pda::Mesh &m = mm->m;
+  if (dims) { dims[0] = m.dim; dims[1] = m.stencil; dims[2] = m.ncols; }
+  if (sizes) {
+    sizes[0] = m.stencilMeshSize;
+    sizes[1] = m.sampleMeshSize;
+    sizes[2] = (int64_t)m.inner.size();
+    sizes[3] = (int64_t)m.nearBd.size();
+  }
+  for (int a = 0; a < 3; ++a) {
+    if (dx) dx[a] = m.dx[a];
+    if (dxinv) dxinv[a] = m.dxInv[a];
+  }
+  if (flags) { flags[0] = m.fullyPeriodic; flags[1] = m.structured; }
+  PDA_API_END
+}
+
+pda_status pda_mesh_arrays(const pda_mesh *mm, int32_t *graph, double *x, double *y, double *z,
+                           int32_t *inner_rows, int32_t *near_bd_rows) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(mm, PDA_ERR_INVALID_ARGUMENT, "null mesh");
+  const pda::Mesh &m = mm->m;
+  if (graph) std::copy(m.graph.begin(), m.graph.end(), graph);
+  if (x) std::copy(m.x.begin(), m.x.end(), x);
+  if (y) std::copy(m.y.begin(), m.y.end(), y);
+  if (z) std::copy(m.z.begin(), m.z.end(), z);
+  if (inner_rows) std::copy(m.inner.begin(), m.inner.end(), inner_rows);
+  if (near_bd_rows) std::copy(m.nearBd.begin(), m.nearBd.end(), near_bd_rows);
+  PDA_API_END
+}
+
+void pda_mesh_free(pda_mesh *m) { delete m; }
+
+pda_status pda_problem_create(const pda_mesh *mesh, int family, int problem, int scheme, int ic_flag,
+                              const char *const *names, const double *vals, int np, void *stream,
+                              pda_problem **out) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(mesh && out, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  std::unique_ptr<pda_problem> p(new pda_problem);
+  pda::create_problem(*p, mesh->m, family, problem, scheme, ic_flag, names, vals, np, stream);
+  *out = p.release();
+  PDA_API_END
+}
+
+pda_status pda_problem_create_swe_slip_wall(const pda_mesh *mesh, int scheme, double gravity, double coriolis,
+                                            double pulse, void *stream, pda_problem **out) {
+  const char *names[3] = {"gravity", "coriolis", "pulseMagnitude"};
+  const double vals[3] = {gravity, coriolis, pulse};
+  return pda_problem_create(mesh, PDA_SWE2D, PDA_SWE2D_SLIP_WALL, scheme, 1, names, vals, 3, stream, out);
+}
+
+void pda_problem_free(pda_problem *p) { delete p; }
+
+pda_status pda_problem_sizes(const pda_problem *p, int *ndpc, int64_t *ds, int64_t *dst) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p, PDA_ERR_INVALID_ARGUMENT, "null problem");
+  if (ndpc) *ndpc = p->ndpc;
+  if (ds) *ds = p->dofsSample;
+  if (dst) *dst = p->dofsStencil;
+  PDA_API_END
+}
+
+pda_status pda_query_parameter(const pda_problem *p, const char *name, double *value) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p && name && value, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  const std::string s(name);
+  if (p->family == PDA_SWE2D) {
+    if (s == "gravity") { *value = p->physParams[0]; return PDA_OK; }
+    if (s == "coriolis") { *value = p->physParams[1]; return PDA_OK; }
+    const int idx = pda::swe_ic_index(p->icFlag, s);
+    PDA_REQUIRE(idx >= 0, PDA_ERR_INVALID_ARGUMENT, "unknown parameter " + s);
+    *value = p->icParams[idx];
+  } else {
+    if (s == "gamma") { *value = p->physParams[0]; return PDA_OK; }
+    PDA_REQUIRE(p->family == PDA_EULER2D, PDA_ERR_INVALID_ARGUMENT, "unknown parameter " + s);
+    const int idx = pda::euler2d_ic_index(p->probEnum, p->icFlag, s);
+    PDA_REQUIRE(idx >= 0, PDA_ERR_INVALID_ARGUMENT, "unknown parameter " + s);
+    *value = p->icParams[idx];
+  }
+  PDA_API_END
+}
+
+pda_status pda_initial_condition_host(const pda_problem *p, double *hU) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p && hU, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  std::vector<double> st;
+  pda::initial_condition(*p, st);
+  std::copy(st.begin(), st.end(), hU);
+  PDA_API_END
+}
+
+pda_status pda_initial_condition(pda_problem *p, double *dU) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p && dU, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  std::vector<double> st;
+  pda::initial_condition(*p, st);
+  PDA_CUDA(cudaMemcpyAsync(dU, st.data(), st.size() * sizeof(double), cudaMemcpyHostToDevice, p->stream));
+  PDA_CUDA(cudaStreamSynchronize(p->stream));
+  PDA_API_END
+}
+
+pda_status pda_velocity(pda_problem *p, const double *dU, double t, double *dV) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p && dU && dV, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  (void)t;
+  pda::velocity(*p, dU, dV);
+  PDA_API_END
+}
+
+pda_status pda_velocity_host(pda_problem *p, const double *hU, double t, double *hV) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p && hU && hV, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  (void)t;
+  p->d_U.alloc(p->dofsStencil);
+  p->d_V.alloc(p->dofsSample);
+  PDA_CUDA(cudaMemcpyAsync(p->d_U.p, hU, p->dofsStencil * sizeof(double), cudaMemcpyHostToDevice, p->stream));
+  pda::velocity(*p, p->d_U.p, p->d_V.p);
+  PDA_CUDA(cudaMemcpyAsync(hV, p->d_V.p, p->dofsSample * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+  PDA_CUDA(cudaStreamSynchronize(p->stream));
+  PDA_API_END
+}
+
+pda_status pda_jacobian_shape(pda_problem *p, int64_t *rows, int64_t *cols, int64_t *nnz) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p, PDA_ERR_INVALID_ARGUMENT, "null problem");
+  pda::build_pattern(*p);
+  if (rows) *rows = p->dofsSample;
+  if (cols) *cols = p->dofsStencil;
+  if (nnz) *nnz = (int64_t)p->colidx.size();
+  PDA_API_END
+}
+
+pda_status pda_jacobian_pattern(pda_problem *p, int32_t *drp, int32_t *dci) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p && drp && dci, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  pda::pattern_to_device(*p);
+  PDA_CUDA(cudaMemcpyAsync(drp, p->d_rowptr.p, p->rowptr.size() * sizeof(int), cudaMemcpyDeviceToDevice,
+                           p->stream));
+  PDA_CUDA(cudaMemcpyAsync(dci, p->d_colidx.p, p->colidx.size() * sizeof(int), cudaMemcpyDeviceToDevice,
+                           p->stream));
+  PDA_CUDA(cudaStreamSynchronize(p->stream));
+  PDA_API_END
+}
+
+pda_status pda_jacobian_pattern_host(pda_problem *p, int32_t *hrp, int32_t *hci) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p && hrp && hci, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  pda::build_pattern(*p);
+  std::copy(p->rowptr.begin(), p->rowptr.end(), hrp);
+  std::copy(p->colidx.begin(), p->colidx.end(), hci);
+  PDA_API_END
+}
+
+pda_status pda_velocity_and_jacobian(pda_problem *p, const double *dU, double t, double *dV, double *dJ) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p && dU && dV && dJ, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  (void)t;
+  pda::velocity_and_jacobian(*p, dU, dV, dJ);
+  PDA_API_END
+}
+
+pda_status pda_velocity_and_jacobian_host(pda_problem *p, const double *hU, double t, double *hV,
+                                          double *hJ) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p && hU && hV && hJ, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  (void)t;
+  pda::build_pattern(*p);
+  p->d_U.alloc(p->dofsStencil);
+  p->d_V.alloc(p->dofsSample);
+  p->d_J.alloc(p->colidx.size());
+  PDA_CUDA(cudaMemcpyAsync(p->d_U.p, hU, p->dofsStencil * sizeof(double), cudaMemcpyHostToDevice, p->stream));
+  pda::velocity_and_jacobian(*p, p->d_U.p, p->d_V.p, p->d_J.p);
+  PDA_CUDA(cudaMemcpyAsync(hV, p->d_V.p, p->dofsSample * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+  PDA_CUDA(cudaMemcpyAsync(hJ, p->d_J.p, p->colidx.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+  PDA_CUDA(cudaStreamSynchronize(p->stream));
+  PDA_API_END
+}
+
+pda_status pda_jacobian(pda_problem *p, const double *dU, double t, double *dJ) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p && dU && dJ, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  (void)t;
+  p->d_Vscratch.alloc(p->dofsSample);
+  pda::velocity_and_jacobian(*p, dU, p->d_Vscratch.p, dJ);
+  PDA_API_END
+}
+
+pda_status pda_apply_jacobian(pda_problem *p, const double *dU, double t, const double *dB, int ncols,
+                              double *dR) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p && dU && dB && dR && ncols >= 1, PDA_ERR_INVALID_ARGUMENT, "invalid argument");
+  (void)t;
+  pda::pattern_to_device(*p);
+  p->d_Vscratch.alloc(p->dofsSample);
+  p->d_Jscratch.alloc(p->colidx.size());
+  pda::velocity_and_jacobian(*p, dU, p->d_Vscratch.p, p->d_Jscratch.p);
+  pda::launch_csr_spmm(p->dofsSample, p->d_rowptr.p, p->d_colidx.p, p->d_Jscratch.p, dB, p->dofsStencil, ncols,
+                       dR, p->dofsSample, p->stream);
+  pda::check_launch(*p);
+  PDA_API_END
+}
+
+pda_status pda_advance_ssprk3(pda_problem *p, double *dU, double t0, double dt, int64_t n, int use_graph) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p && dU, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  pda::advance(*p, 0, dU, t0, dt, n, use_graph != 0);
+  PDA_API_END
+}
+
+pda_status pda_advance_rk4(pda_problem *p, double *dU, double t0, double dt, int64_t n, int use_graph) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p && dU, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  pda::advance(*p, 1, dU, t0, dt, n, use_graph != 0);
+  PDA_API_END
+}
+
+int64_t pda_problem_launch_count(const pda_problem *p) { return p ? p->launches : 0; }
+
+pda_status pda_profile_velocity(pda_problem *p, const double *dU, double *dV, int reps, double *ms) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p && dU && dV && ms && reps > 0, PDA_ERR_INVALID_ARGUMENT, "invalid argument");
+  const int ne = p->dim + 3;
+  std::vector<cudaEvent_t> ev(ne);
+  for (auto &e : ev) PDA_CUDA(cudaEventCreate(&e));
+  std::vector<double> acc(ne - 1, 0.0);
+  for (int r = 0; r < reps; ++r) {
+    pda::velocity(*p, dU, dV, p->useStruct ? ev.data() : nullptr);
+    if (!p->useStruct) break;
+    PDA_CUDA(cudaEventSynchronize(ev[ne - 1]));
+    for (int k = 0; k + 1 < ne; ++k) {
+      float t = 0;
+      PDA_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+      acc[k] += t;
+    }
+  }
+  for (int k = 0; k < 5; ++k) ms[k] = 0.0;
+  // order: faces x, faces y, faces z, balance, near-boundary rows
+  for (int a = 0; a < p->dim; ++a) ms[a] = acc[a] / reps;
+  ms[3] = acc[p->dim] / reps;
+  ms[4] = acc[p->dim + 1] / reps;
+  for (auto &e : ev) cudaEventDestroy(e);
+  PDA_API_END
+}
+
+pda_status pda_measure_fp64_peak(double *flops_per_s) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(flops_per_s, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  int dev = 0, sms = 0;
+  PDA_CUDA(cudaGetDevice(&dev));
+  PDA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  *flops_per_s = pda::measure_fp64_fma_rate(sms * 8, 256, 4096, nullptr);
+  PDA_CUDA(cudaGetLastError());
+  PDA_API_END
+}
+
+}  // extern "C"

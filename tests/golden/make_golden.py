@@ -1,0 +1,317 @@
+"""Generate the golden fixtures under tests/golden/ from the reference.
+
+Runs only where the reference checkout exists (it reads REF, default
+/root/reference).  It
+  1. runs the reference's own mesh scripts (meshing_scripts/create_full_mesh.py,
+     create_sample_mesh.py) into tests/golden/meshes/<name>/,
+  2. evaluates the reference itself through oracle/_ref/libpdaref.so (built by
+     ``make -C oracle ref`` from the reference headers) on seeded inputs and
+     stores initial conditions, velocities and CSR Jacobians in
+     tests/golden/cases/<case>.npz,
+  3. copies the reference tests' own known answers (WENO KATs, Sod / Riemann /
+     shallow-water trajectory golds, mesh-generator golds) into
+     tests/golden/gold/, checking on the way that the reference shim
+     reproduces them.
+
+Usage:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import re
+import shutil
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = os.environ.get("PDA_REFERENCE", "/root/reference")
+MESHES = os.path.join(HERE, "meshes")
+CASES = os.path.join(HERE, "cases")
+GOLD = os.path.join(HERE, "gold")
+SEED = 20261203
+
+# name -> create_full_mesh.py arguments
+FULL_MESHES = {
+    "m1d_s3_100": "-n 100 1 --bounds -0.5 0.5 -s 3",
+    "m1d_s5_100": "-n 100 1 --bounds -0.5 0.5 -s 5",
+    "m1d_s7_100": "-n 100 1 --bounds -0.5 0.5 -s 7",
+    "m1d_s7_7": "-n 7 1 --bounds -0.5 0.5 -s 7",
+    "m1d_s7_40_per": "-n 40 1 --bounds -1.0 1.0 -s 7 --periodic x",
+    "m2d_s3_20": "-n 20 20 --bounds 0.0 1.0 0.0 1.0 -s 3",
+    "m2d_s5_20": "-n 20 20 --bounds 0.0 1.0 0.0 1.0 -s 5",
+    "m2d_s7_20": "-n 20 20 --bounds 0.0 1.0 0.0 1.0 -s 7",
+    "m2d_s7_13x11_perx": "-n 13 11 --bounds 0.0 1.0 0.0 1.0 -s 7 --periodic x",
+    "m2d_s7_16_per": "-n 16 16 --bounds -1.0 1.0 -1.0 1.0 -s 7 --periodic x y",
+    "m2d_s7_6_per": "-n 6 6 --bounds -1.0 1.0 -1.0 1.0 -s 7 --periodic x y",
+    "m2d_s3_25": "-n 25 25 --bounds -5.0 5.0 -5.0 5.0 -s 3",
+    "m2d_s5_25": "-n 25 25 --bounds -5.0 5.0 -5.0 5.0 -s 5",
+    "m2d_s7_25": "-n 25 25 --bounds -5.0 5.0 -5.0 5.0 -s 7",
+    "m2d_s3_10": "-n 10 10 --bounds 0.0 1.0 0.0 1.0 -s 3",
+    "m2d_s5_10": "-n 10 10 --bounds 0.0 1.0 0.0 1.0 -s 5",
+    "m2d_s7_10": "-n 10 10 --bounds 0.0 1.0 0.0 1.0 -s 7",
+    "m3d_s3_8_per": "-n 8 8 8 --bounds -1.0 1.0 -1.0 1.0 -1.0 1.0 -s 3 --periodic x y z",
+    "m3d_s5_8_per": "-n 8 8 8 --bounds -1.0 1.0 -1.0 1.0 -1.0 1.0 -s 5 --periodic x y z",
+    "m3d_s5_6x5x7_per": "-n 6 5 7 --bounds -1.0 1.0 -1.0 1.0 -1.0 1.0 -s 5 --periodic x y z",
+}
+
+# sample meshes: name -> (full mesh, gids source)
+SAMPLE_MESHES = {
+    "s2d_s3_10": ("m2d_s3_10", "tests_cpp/eigen_2d_euler_sample_mesh_test1/firstorder/sample_mesh_gids.dat"),
+    "s2d_s5_10": ("m2d_s5_10", "tests_cpp/eigen_2d_euler_sample_mesh_test1/weno3/sample_mesh_gids.dat"),
+    "s2d_s7_10": ("m2d_s7_10", "tests_cpp/eigen_2d_euler_sample_mesh_test1/weno5/sample_mesh_gids.dat"),
+    "s2d_s7_20": ("m2d_s7_20", "tests_cpp/eigen_2d_swe_jacobian_fd_with_sample_mesh/sample_mesh_gids.dat"),
+    "s2d_s7_25_rand": ("m2d_s7_25", "random:40"),
+}
+
+# case -> (mesh, family, problem, scheme, icflag, params)
+E1, E2, E3, SW = 0, 1, 2, 3
+CASE_LIST = {
+    "sod_fo": ("m1d_s3_100", E1, 1, 0, 1, {}),
+    "sod_w3": ("m1d_s5_100", E1, 1, 1, 1, {}),
+    "sod_w5": ("m1d_s7_100", E1, 1, 2, 1, {}),
+    "sod_w5_s7_fo": ("m1d_s7_100", E1, 1, 0, 1, {}),
+    "sod_w5_tiny": ("m1d_s7_7", E1, 1, 2, 1, {}),
+    "lax_w5": ("m1d_s7_100", E1, 2, 2, 1, {}),
+    "e1d_smooth_w5": ("m1d_s7_40_per", E1, 0, 2, 1, {}),
+    "riemann_fo": ("m2d_s3_20", E2, 4, 0, 2, {}),
+    "riemann_w3": ("m2d_s7_20", E2, 4, 1, 2, {}),
+    "riemann_w5": ("m2d_s7_20", E2, 4, 2, 2, {}),
+    "riemann_w3_s5": ("m2d_s5_20", E2, 4, 1, 2, {}),
+    "riemann_ic1_w5": ("m2d_s7_20", E2, 4, 2, 1, {}),
+    "riemann_params_w5": ("m2d_s7_20", E2, 4, 2, 2,
+                          {"riemannTopRightPressure": 1.2, "riemannTopRightDensity": 1.1,
+                           "riemannBotLeftPressure": 0.05, "gamma": 1.3}),
+    "riemann_perx_w5": ("m2d_s7_13x11_perx", E2, 4, 2, 2, {}),
+    "e2d_smooth_w5": ("m2d_s7_16_per", E2, 0, 2, 1, {}),
+    "e2d_smooth_w3": ("m2d_s7_16_per", E2, 0, 1, 1, {}),
+    "e2d_smooth_w5_tiny": ("m2d_s7_6_per", E2, 0, 2, 1, {}),
+    "swe_fo": ("m2d_s3_25", SW, 0, 0, 1, {}),
+    "swe_w3": ("m2d_s5_25", SW, 0, 1, 1, {}),
+    "swe_w5": ("m2d_s7_25", SW, 0, 2, 1, {}),
+    "swe_ic2_w5": ("m2d_s7_25", SW, 0, 2, 2,
+                   {"gravity": 7.5, "coriolis": -2.0, "pulseMagnitude1": 0.15, "pulseX2": 1.5}),
+    "e3d_smooth_fo": ("m3d_s3_8_per", E3, 0, 0, 1, {}),
+    "e3d_smooth_w3": ("m3d_s5_8_per", E3, 0, 1, 1, {}),
+    "e3d_smooth_w3_odd": ("m3d_s5_6x5x7_per", E3, 0, 1, 1, {}),
+    "sample_riemann_fo": ("s2d_s3_10", E2, 4, 0, 2, {}),
+    "sample_riemann_w3": ("s2d_s5_10", E2, 4, 1, 2, {}),
+    "sample_riemann_w5": ("s2d_s7_10", E2, 4, 2, 2, {}),
+    "sample_swe_w5": ("s2d_s7_20", SW, 0, 2, 1, {}),
+    "sample_swe_w5_rand": ("s2d_s7_25_rand", SW, 0, 2, 1, {"coriolis": -1.5}),
+}
+
+
+def run(cmd):
+    subprocess.run(cmd, shell=True, check=True, stdout=subprocess.DEVNULL)
+
+
+def make_meshes():
+    os.makedirs(MESHES, exist_ok=True)
+    py = sys.executable
+    for name, args in FULL_MESHES.items():
+        d = os.path.join(MESHES, name)
+        os.makedirs(d, exist_ok=True)
+        run(f"{py} {REF}/meshing_scripts/create_full_mesh.py {args} --outDir {d}")
+    rng = np.random.default_rng(SEED)
+    for name, (full, src) in SAMPLE_MESHES.items():
+        d = os.path.join(MESHES, name)
+        os.makedirs(d, exist_ok=True)
+        gfile = os.path.join(d, "sample_mesh_gids.dat")
+        if src.startswith("random:"):
+            k = int(src.split(":")[1])
+            ncell = int(re.search(r"sampleMeshSize\s+(\d+)", open(os.path.join(MESHES, full, "info.dat")).read()).group(1))
+            gids = np.sort(rng.choice(ncell, size=k, replace=False))
+            np.savetxt(gfile, gids, fmt="%8d")
+        else:
+            shutil.copy(os.path.join(REF, src), gfile)
+        run(f"{py} {REF}/meshing_scripts/create_sample_mesh.py --fullMeshDir {os.path.join(MESHES, full)} "
+            f"--sampleMeshIndices {gfile} --outDir {d}")
+
+
+class Ref:
+    def __init__(self):
+        path = os.path.join(REPO, "oracle", "_ref", "libpdaref.so")
+        if not os.path.exists(path):
+            subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "ref", f"REF={REF}"], check=True)
+        L = C.CDLL(path)
+        L.ref_create.restype = C.c_void_p
+        L.ref_create.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                 C.POINTER(C.c_char_p), C.POINTER(C.c_double)]
+        L.ref_last_error.restype = C.c_char_p
+        for f in ("ref_destroy",):
+            getattr(L, f).argtypes = [C.c_void_p]
+        L.ref_sizes.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
+        L.ref_ic.argtypes = [C.c_void_p, C.c_void_p]
+        L.ref_velocity.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]
+        L.ref_velocity_and_jacobian.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p,
+                                                C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ref_ssprk3.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_long]
+        L.ref_rk4.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_long]
+        L.ref_weno5.argtypes = [C.c_void_p, C.c_void_p]
+        L.ref_weno3.argtypes = [C.c_void_p, C.c_void_p]
+        self.L = L
+
+    def create(self, mesh, fam, prob, scheme, ic, params):
+        names = list(params)
+        cn = (C.c_char_p * max(1, len(names)))(*[n.encode() for n in names])
+        cv = (C.c_double * max(1, len(names)))(*[float(params[n]) for n in names])
+        h = self.L.ref_create(os.path.join(MESHES, mesh).encode(), fam, prob, scheme, ic, len(names), cn, cv)
+        if not h:
+            raise RuntimeError(self.L.ref_last_error().decode())
+        s = (C.c_long * 4)()
+        self.L.ref_sizes(h, s)
+        return h, tuple(s)
+
+
+def vp(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def make_cases(ref: Ref):
+    os.makedirs(CASES, exist_ok=True)
+    rng = np.random.default_rng(SEED)
+    manifest = {}
+    for case, (mesh, fam, prob, scheme, ic, params) in CASE_LIST.items():
+        h, (ndpc, ds, dst, nnz) = ref.create(mesh, fam, prob, scheme, ic, params)
+        U0 = np.empty(dst)
+        ref.L.ref_ic(h, vp(U0))
+        noise = rng.uniform(-1e-3, 1e-3, dst)
+        U1 = U0 + noise
+        V0 = np.empty(ds)
+        V1 = np.empty(ds)
+        ref.L.ref_velocity(h, vp(U0), 0.0, vp(V0))
+        ref.L.ref_velocity(h, vp(U1), 0.0, vp(V1))
+        Vj = np.empty(ds)
+        rp = np.empty(ds + 1, dtype=np.int32)
+        ci = np.empty(nnz, dtype=np.int32)
+        jv = np.empty(nnz)
+        ref.L.ref_velocity_and_jacobian(h, vp(U1), 0.0, vp(Vj), vp(rp), vp(ci), vp(jv))
+        ref.L.ref_destroy(h)
+        np.savez_compressed(os.path.join(CASES, case + ".npz"), U0=U0, U1=U1, V0=V0, V1=V1, Vj=Vj,
+                            rowptr=rp, colidx=ci, jvals=jv)
+        manifest[case] = dict(mesh=mesh, family=fam, problem=prob, scheme=scheme, icflag=ic,
+                              params=params, ndpc=ndpc, dofs_sample=ds, dofs_stencil=dst, nnz=nnz)
+        print(f"case {case}: dofs {ds}/{dst} nnz {nnz}")
+    return manifest
+
+
+def extract_kat():
+    """WENO known answers from tests_cpp/weno5/main.cc:12-25 and weno3/main.cc."""
+    def nums(block):
+        return [float(x) for x in re.findall(r"[-+]?\d+\.\d*(?:e[-+]?\d+)?", block)]
+    src5 = open(os.path.join(REF, "tests_cpp/weno5/main.cc")).read()
+    q5 = nums(re.search(r"vec_t q\{([^}]*)\}", src5).group(1))
+    g5 = nums(re.search(r"goldF =\s*\{([^}]*)\}", src5).group(1))
+    src3 = open(os.path.join(REF, "tests_cpp/weno3/main.cc")).read()
+    q3 = nums(re.search(r"vec_t q\{([^}]*)\}", src3).group(1))
+    g3 = nums(re.search(r"goldF =\s*\{([^}]*)\}", src3).group(1))
+    return dict(weno5_q=q5, weno5_gold=g5, weno3_q=q3, weno3_gold=g3, tol=1e-13)
+
+
+def make_gold(ref: Ref):
+    os.makedirs(GOLD, exist_ok=True)
+    kat = extract_kat()
+    for tag, q, g in (("weno5", kat["weno5_q"], kat["weno5_gold"]), ("weno3", kat["weno3_q"], kat["weno3_gold"])):
+        out = np.empty(4)
+        getattr(ref.L, "ref_" + tag)(vp(np.array(q)), vp(out))
+        assert np.all(np.abs(out - np.array(g)) <= 1e-13), (tag, out, g)
+    json.dump(kat, open(os.path.join(GOLD, "weno_kat.json"), "w"), indent=1)
+
+    traj = {}
+    # Sod: RK4 dt=1e-3, 100 steps, last snapshot (tests_cpp/eigen_1d_euler_sod_explicit/main.cc)
+    for scheme, tag, mesh in ((0, "firstorder", "m1d_s3_100"), (1, "weno3", "m1d_s5_100"), (2, "weno5", "m1d_s7_100")):
+        gold = np.loadtxt(os.path.join(REF, f"tests_cpp/eigen_1d_euler_sod_explicit/{tag}/gold.txt"))
+        h, s = ref.create(mesh, E1, 1, scheme, 1, {})
+        U = np.empty(s[2])
+        ref.L.ref_ic(h, vp(U))
+        ref.L.ref_rk4(h, vp(U), 0.0, 1e-3, 100)
+        ref.L.ref_destroy(h)
+        assert np.allclose(U, gold, rtol=1e-9, atol=1e-11), ("sod", tag)
+        traj[f"sod_{tag}"] = dict(mesh=mesh, family=E1, problem=1, scheme=scheme, icflag=1, stepper="rk4",
+                                  dt=1e-3, steps=100, rtol=1e-9, atol=1e-11)
+        np.save(os.path.join(GOLD, f"sod_{tag}.npy"), gold)
+    # Riemann IC2: SSPRK3 dt=0.01 for StepCount(0.6/dt) steps, observer every 10 steps
+    # (tests_cpp/eigen_2d_euler_riemann_explicit/main.cc:18-30, compare.py:43-55)
+    nsteps = int(0.6 / 0.01)
+    saved = (nsteps // 10) * 10
+    for scheme, tag, mesh in ((0, "firstorder", "m2d_s3_20"), (1, "weno3", "m2d_s7_20"), (2, "weno5", "m2d_s7_20")):
+        rho_g = np.loadtxt(os.path.join(REF, f"tests_cpp/eigen_2d_euler_riemann_explicit/{tag}/rho_gold.txt"))
+        p_g = np.loadtxt(os.path.join(REF, f"tests_cpp/eigen_2d_euler_riemann_explicit/{tag}/p_gold.txt"))
+        h, s = ref.create(mesh, E2, 4, scheme, 2, {})
+        U = np.empty(s[2])
+        ref.L.ref_ic(h, vp(U))
+        ref.L.ref_ssprk3(h, vp(U), 0.0, 0.01, saved)
+        ref.L.ref_destroy(h)
+        D = U.reshape(-1, 4)
+        rho = D[:, 0]
+        u, v = D[:, 1] / rho, D[:, 2] / rho
+        p = ((5. + 2.) / 5. - 1.) * (D[:, 3] - rho * (u ** 2 + v ** 2) * 0.5)
+        assert np.allclose(rho, rho_g, rtol=1e-10, atol=1e-12), ("riemann rho", tag)
+        assert np.allclose(p, p_g, rtol=1e-10, atol=1e-12), ("riemann p", tag)
+        traj[f"riemann_{tag}"] = dict(mesh=mesh, family=E2, problem=4, scheme=scheme, icflag=2, stepper="ssprk3",
+                                      dt=0.01, steps=saved, rtol=1e-10, atol=1e-12)
+        np.savez(os.path.join(GOLD, f"riemann_{tag}.npz"), rho=rho_g, p=p_g)
+    # SWE slip wall: RK4 dt=0.01 for StepCount(2/dt) steps, observer every 10
+    # (tests_cpp/eigen_2d_swe_slip_wall_explicit/main.cc, compare.py)
+    nsteps = int(2. / 0.01)
+    saved = (nsteps // 10) * 10
+    for scheme, tag, mesh in ((0, "firstorder", "m2d_s3_25"), (1, "weno3", "m2d_s5_25"), (2, "weno5", "m2d_s7_25")):
+        h_g = np.loadtxt(os.path.join(REF, f"tests_cpp/eigen_2d_swe_slip_wall_explicit/{tag}/h_gold.txt"))
+        h, s = ref.create(mesh, SW, 0, scheme, 1, {})
+        U = np.empty(s[2])
+        ref.L.ref_ic(h, vp(U))
+        ref.L.ref_rk4(h, vp(U), 0.0, 0.01, saved)
+        ref.L.ref_destroy(h)
+        hh = U.reshape(-1, 3)[:, 0]
+        assert np.allclose(hh, h_g, rtol=1e-10, atol=1e-12), ("swe", tag)
+        traj[f"swe_{tag}"] = dict(mesh=mesh, family=SW, problem=0, scheme=scheme, icflag=1, stepper="rk4",
+                                  dt=0.01, steps=saved, rtol=1e-10, atol=1e-12)
+        np.save(os.path.join(GOLD, f"swe_{tag}.npy"), h_g)
+    json.dump(traj, open(os.path.join(GOLD, "trajectories.json"), "w"), indent=1)
+
+    # mesh-generator golds (tests_mesh/mesh_generation_full_{1,2,3}d/*/*_gold.dat),
+    # with the generator arguments their test.cmake files pass
+    mg = os.path.join(GOLD, "mesh_generation")
+    os.makedirs(mg, exist_ok=True)
+    args = {}
+    bounds = {1: [0.0, 1.0], 2: [0.0, 1.0, 0.0, 1.0], 3: [0.0, 1.0, 0.0, 2.0, 0.0, 3.0]}
+    for dim, dd in ((1, "mesh_generation_full_1d"), (2, "mesh_generation_full_2d"), (3, "mesh_generation_full_3d")):
+        base = os.path.join(REF, "tests_mesh", dd)
+        for sub in sorted(os.listdir(base)):
+            src = os.path.join(base, sub)
+            if not os.path.isdir(src):
+                continue
+            cm = open(os.path.join(src, "CMakeLists.txt")).read()
+            val = lambda k, d=None: (re.search(r"-D%s=(\S+)" % k, cm).group(1).strip('"') if re.search(r"-D%s=" % k, cm) else d)
+            n = [int(val("nx")), int(val("ny", 1)), int(val("nz", 1))]
+            per = val("PER")
+            if dim == 1:
+                p3 = [per not in ("0", "none"), False, False]
+            elif dim == 2:
+                p3 = [per in ("all", "onlyx"), per in ("all", "onlyy"), False]
+            else:
+                p3 = [per not in ("0", "none")] * 3
+            args[sub] = dict(dim=dim, n=n, stencil=int(val("ss")), periodic=p3, bounds=bounds[dim])
+            dst = os.path.join(mg, sub)
+            os.makedirs(dst, exist_ok=True)
+            for f in ("info", "connectivity", "coordinates"):
+                shutil.copy(os.path.join(src, f + "_gold.dat"), os.path.join(dst, f + ".dat"))
+    json.dump(args, open(os.path.join(mg, "args.json"), "w"), indent=1)
+
+
+def main():
+    make_meshes()
+    ref = Ref()
+    manifest = make_cases(ref)
+    json.dump(manifest, open(os.path.join(HERE, "manifest.json"), "w"), indent=1)
+    make_gold(ref)
+    print("done")
+
+
+if __name__ == "__main__":
+    main()
