@@ -189,7 +189,7 @@ def run_reference(args):
 
 
 def workload_config():
-    return {"workload": "euler2d_riemann_ic2_weno5_velocity_1024x1024", "cells": N_CELLS_SIDE ** 2,
+    return {"workload": f"euler2d_riemann_ic2_weno5_velocity_{N_CELLS_SIDE}x{N_CELLS_SIDE}", "cells": N_CELLS_SIDE ** 2,
             "dofs": NDPC * N_CELLS_SIDE ** 2, "scheme": "WENO5+Rusanov", "boundary": "Neumann (transmissive)",
             "l2": "256 MiB write between timed steps (outside the per-step events)"}
 
@@ -202,7 +202,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer measurement (profiling runs)")
+    ap.add_argument("--n", type=int, default=1024, help="cells per side (1024 = the benchmark workload)")
     args = ap.parse_args()
+    global N_CELLS_SIDE
+    N_CELLS_SIDE = args.n
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
@@ -255,6 +259,8 @@ def main():
     value = world * cells / (ms * 1e-3) / 1e9
 
     # ---- e2e: host buffers through the C ABI (pinned), H2D + kernels + D2H
+    if args.no_e2e:
+        args.steps_e2e = 0
     Uhp = torch.from_numpy(Uh).pin_memory()
     Vhp = torch.empty(prob.totalDofSampleMesh(), dtype=torch.float64).pin_memory()
     import ctypes as C
@@ -262,7 +268,7 @@ def main():
     for _ in range(3):
         pda._check(L.pda_velocity_host(prob._h, C.c_void_p(Uhp.data_ptr()), 0.0, C.c_void_p(Vhp.data_ptr())))
     te = []
-    for _ in range(args.steps):
+    for _ in range(args.steps if not args.no_e2e else 1):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()

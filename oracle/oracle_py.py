@@ -46,6 +46,7 @@ def load():
         L.orc_rk4.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64]
         L.orc_weno5.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_weno3.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_set_cube_mode.argtypes = [C.c_int]
         L.orc_set_threads.restype = C.c_int
         L.orc_set_threads.argtypes = [C.c_int]
         _L = L
@@ -140,6 +141,10 @@ class Oracle:
         o = np.empty(4)
         self.L.orc_weno3(_vp(np.ascontiguousarray(q5, dtype=np.float64)), _vp(o))
         return o
+
+    def set_cube_mode(self, correctly_rounded):
+        """0: x^3 by pow (the reference); 1: correctly rounded (the library)."""
+        self.L.orc_set_cube_mode(int(bool(correctly_rounded)))
 
     def set_threads(self, n):
         return self.L.orc_set_threads(n)

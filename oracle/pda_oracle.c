@@ -172,6 +172,17 @@ void orc_mesh_counts(const orc_mesh *m, int64_t out[4]) {
 }
 
 /* ------------------------------------------------------------ reconstruction */
+/* x^3 as the reference evaluates it (glibc pow(x, 3.)), or correctly rounded
+ * (Dekker two-product), the library's documented evaluation; the switch lets
+ * tests check the library's Jacobian bit for bit. */
+static int g_cube_cr = 0;
+static double cube3(double x) {
+  if (!g_cube_cr) return pow(x, 3.);
+  const double p = x * x, e = fma(x, x, -p), c = p * x, ce = fma(p, x, -c);
+  return c + (ce + e * x);
+}
+void orc_set_cube_mode(int correctly_rounded) { g_cube_cr = correctly_rounded; }
+
 static void weno5_impl(double *uNeg, double *uPos, double qim2, double qim1, double qi, double qip1,
                        double qip2, double qip3) {
   const double epsilon = 1e-6, one = 1, two = 2, three = 3;
@@ -251,9 +262,9 @@ static void weno5_grad_impl(double *uNeg, double *uPos, double *gN, double *gP, 
     const double s = one / (a0 + a1 + a2);
     double da0[5], da1[5], da2[5], das[5];
     for (int i = 0; i < 5; i++) {
-      da0[i] = -1. / (5. * pow(B0 + epsilon, 3.)) * dB0[i];
-      da1[i] = -6. / (5. * pow(B1 + epsilon, 3.)) * dB1[i];
-      da2[i] = -3. / (5. * pow(B2 + epsilon, 3.)) * dB2[i];
+      da0[i] = -1. / (5. * cube3(B0 + epsilon)) * dB0[i];
+      da1[i] = -6. / (5. * cube3(B1 + epsilon)) * dB1[i];
+      da2[i] = -3. / (5. * cube3(B2 + epsilon)) * dB2[i];
       das[i] = -1. / pow(a2 + a1 + a0, 2.) * (da0[i] + da1[i] + da2[i]);
     }
     const double w0 = a0 * s, w1 = a1 * s, w2 = a2 * s;
@@ -295,9 +306,9 @@ static void weno5_grad_impl(double *uNeg, double *uPos, double *gN, double *gP, 
     const double s = one / (a0 + a1 + a2);
     double da0[5], da1[5], da2[5], das[5];
     for (int i = 0; i < 5; i++) {
-      da0[i] = -3. / (5. * pow(B0 + epsilon, 3.)) * dB0[i];
-      da1[i] = -6. / (5. * pow(B1 + epsilon, 3.)) * dB1[i];
-      da2[i] = -1. / (5. * pow(B2 + epsilon, 3.)) * dB2[i];
+      da0[i] = -3. / (5. * cube3(B0 + epsilon)) * dB0[i];
+      da1[i] = -6. / (5. * cube3(B1 + epsilon)) * dB1[i];
+      da2[i] = -1. / (5. * cube3(B2 + epsilon)) * dB2[i];
       das[i] = -1. / pow(a2 + a1 + a0, 2.) * (da0[i] + da1[i] + da2[i]);
     }
     const double w0 = a0 * s, w1 = a1 * s, w2 = a2 * s;
@@ -351,15 +362,15 @@ static void weno3_grad_impl(double *uNeg, double *uPos, double *gN, double *gP, 
     const double a1 = twoOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
     const double s = one / (a0 + a1);
     double da0[3], da1[3], das[3];
-    da0[0] = -4. * (qim1 - qi) / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 3));
-    da0[1] = 4. * (qim1 - qi) / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 3.));
+    da0[0] = -4. * (qim1 - qi) / (3. * cube3(pow(qim1 - qi, 2.) + epsilon));
+    da0[1] = 4. * (qim1 - qi) / (3. * cube3(pow(qim1 - qi, 2.) + epsilon));
     da0[2] = 0.;
     da1[0] = 0.;
-    da1[1] = -8. * (qi - qip1) / (3. * pow(pow(qi - qip1, 2.) + epsilon, 3.));
-    da1[2] = 8. * (qi - qip1) / (3. * pow(pow(qi - qip1, 2.) + epsilon, 3.));
-    das[0] = (4. * (qim1 - qi)) / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 3.) * pow(2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)) + 1. / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 2.)), 2.));
-    das[1] = -((4. * (qim1 - qi)) / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 3.)) - (8. * (qi - qip1)) / (3. * pow(pow(qi - qip1, 2.) + epsilon, 3.))) / pow(2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)) + 1. / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 2.)), 2.);
-    das[2] = -(8. * (qi - qip1)) / (3. * pow(2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)) + 1. / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 2.)), 2.) * pow(pow(qi - qip1, 2.) + epsilon, 3.));
+    da1[1] = -8. * (qi - qip1) / (3. * cube3(pow(qi - qip1, 2.) + epsilon));
+    da1[2] = 8. * (qi - qip1) / (3. * cube3(pow(qi - qip1, 2.) + epsilon));
+    das[0] = (4. * (qim1 - qi)) / (3. * cube3(pow(qim1 - qi, 2.) + epsilon) * pow(2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)) + 1. / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 2.)), 2.));
+    das[1] = -((4. * (qim1 - qi)) / (3. * cube3(pow(qim1 - qi, 2.) + epsilon)) - (8. * (qi - qip1)) / (3. * cube3(pow(qi - qip1, 2.) + epsilon))) / pow(2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)) + 1. / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 2.)), 2.);
+    das[2] = -(8. * (qi - qip1)) / (3. * pow(2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)) + 1. / (3. * pow(pow(qim1 - qi, 2.) + epsilon, 2.)), 2.) * cube3(pow(qi - qip1, 2.) + epsilon));
     const double w0 = a0 * s, w1 = a1 * s;
     for (int i = 0; i < 3; i++) {
       gN[i] = (da0[i] * s + das[i] * a0) * p0 + dp0[i] * w0;
@@ -380,15 +391,15 @@ static void weno3_grad_impl(double *uNeg, double *uPos, double *gN, double *gP, 
     const double dp0[3] = {1. / 2., 1 / 2., 0.};
     const double dp1[3] = {0., 3. / 2., -1. / 2.};
     double da0[3], da1[3], das[3];
-    da0[0] = -8. * (qi - qip1) / (3. * pow(pow(qi - qip1, 2.) + epsilon, 3.));
-    da0[1] = 8. * (qi - qip1) / (3. * pow(pow(qi - qip1, 2.) + epsilon, 3.));
+    da0[0] = -8. * (qi - qip1) / (3. * cube3(pow(qi - qip1, 2.) + epsilon));
+    da0[1] = 8. * (qi - qip1) / (3. * cube3(pow(qi - qip1, 2.) + epsilon));
     da0[2] = 0.;
     da1[0] = 0.;
-    da1[1] = -4. * (qip1 - qip2) / (3. * pow(pow(qip1 - qip2, 2.) + epsilon, 3.));
-    da1[2] = 4. * (qip1 - qip2) / (3. * pow(pow(qip1 - qip2, 2) + epsilon, 3.));
-    das[0] = 8. * (qi - qip1) / (3. * pow(pow(qi - qip1, 2.) + epsilon, 3.) * pow(1. / (3. * pow(pow(qip1 - qip2, 2.) + epsilon, 2.)) + 2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)), 2.));
-    das[1] = -(8. * (qi - qip1) / (3 * pow(pow(qi - qip1, 2.) + epsilon, 3.)) - 4. * (qip1 - qip2) / (3. * pow(pow(qip1 - qip2, 2.) + epsilon, 3.))) / pow(1. / (3. * pow(pow(qip1 - qip2, 2.) + epsilon, 2.)) + 2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)), 2.);
-    das[2] = -4. * (qip1 - qip2) / (3. * pow(1. / (3. * pow(pow(qip1 - qip2, 2.) + epsilon, 2.)) + 2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)), 2.) * pow(pow(qip1 - qip2, 2.) + epsilon, 3.));
+    da1[1] = -4. * (qip1 - qip2) / (3. * cube3(pow(qip1 - qip2, 2.) + epsilon));
+    da1[2] = 4. * (qip1 - qip2) / (3. * cube3(pow(qip1 - qip2, 2) + epsilon));
+    das[0] = 8. * (qi - qip1) / (3. * cube3(pow(qi - qip1, 2.) + epsilon) * pow(1. / (3. * pow(pow(qip1 - qip2, 2.) + epsilon, 2.)) + 2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)), 2.));
+    das[1] = -(8. * (qi - qip1) / (3 * cube3(pow(qi - qip1, 2.) + epsilon)) - 4. * (qip1 - qip2) / (3. * cube3(pow(qip1 - qip2, 2.) + epsilon))) / pow(1. / (3. * pow(pow(qip1 - qip2, 2.) + epsilon, 2.)) + 2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)), 2.);
+    das[2] = -4. * (qip1 - qip2) / (3. * pow(1. / (3. * pow(pow(qip1 - qip2, 2.) + epsilon, 2.)) + 2. / (3. * pow(pow(qi - qip1, 2.) + epsilon, 2.)), 2.) * cube3(pow(qip1 - qip2, 2.) + epsilon));
     for (int i = 0; i < 3; i++) {
       gP[i + 1] = (da0[i] * s + das[i] * a0) * p0 + dp0[i] * w0;
       gP[i + 1] += (da1[i] * s + das[i] * a1) * p1 + dp1[i] * w1;
@@ -1240,4 +1251,27 @@ int orc_set_threads(int n) {
   (void)n;
   return 1;
 #endif
+}
+
+/* ------------------------------------------------ point-wise test exports */
+void orc_weno5_face_grad(const double q[6], double u[2], double gN[6], double gP[6]) {
+  weno5_grad_impl(&u[0], &u[1], gN, gP, q[0], q[1], q[2], q[3], q[4], q[5]);
+}
+void orc_weno3_face_grad(const double q[4], double u[2], double gN[4], double gP[4]) {
+  weno3_grad_impl(&u[0], &u[1], gN, gP, q[0], q[1], q[2], q[3]);
+}
+void orc_weno5_face(const double q[6], double u[2]) { weno5_impl(&u[0], &u[1], q[0], q[1], q[2], q[3], q[4], q[5]); }
+void orc_weno3_face(const double q[4], double u[2]) { weno3_impl(&u[0], &u[1], q[0], q[1], q[2], q[3]); }
+/* family 0..3, axis; F[nd]; JL/JR row-major nd x nd */
+void orc_point_flux(int family, int ax, const double *qL, const double *qR, double param, double *F, double *JL,
+                    double *JR) {
+  orc_problem p;
+  memset(&p, 0, sizeof p);
+  p.fam = family;
+  p.nd = family == E1 ? 3 : family == E2 ? 4 : family == E3 ? 5 : 3;
+  p.dim = family == E1 ? 1 : family == E3 ? 3 : 2;
+  p.gamma = param;
+  p.gravity = param;
+  flux(&p, ax, F, qL, qR);
+  flux_jac(&p, ax, JL, JR, qL, qR);
 }

@@ -35,6 +35,15 @@ void orc_ssprk3(orc_problem *p, double *U, double t0, double dt, int64_t nsteps)
 void orc_rk4(orc_problem *p, double *U, double t0, double dt, int64_t nsteps);
 void orc_weno5(const double q7[7], double out4[4]);
 void orc_weno3(const double q5[5], double out4[4]);
+/* point-wise functions, exported for tests of the device numerics */
+void orc_weno5_face(const double q[6], double u[2]);
+void orc_weno3_face(const double q[4], double u[2]);
+void orc_weno5_face_grad(const double q[6], double u[2], double gN[6], double gP[6]);
+void orc_weno3_face_grad(const double q[4], double u[2], double gN[4], double gP[4]);
+void orc_point_flux(int family, int ax, const double *qL, const double *qR, double param, double *F,
+                    double *JL, double *JR);
+/* 0: pow(x, 3.) as the reference (default); 1: correctly rounded x^3 */
+void orc_set_cube_mode(int correctly_rounded);
 /* OpenMP threads for the CPU baseline (<= 0: all). Returns the count used. */
 int orc_set_threads(int n);
 

@@ -3,6 +3,7 @@
 #pragma once
 
 #include "kernels.cuh"
+#include "tiles.cuh"
 #include "launch.hpp"
 
 namespace pda {
@@ -34,7 +35,20 @@ void faces_s(const Box &b, const Phys &p, const double *U, double *Fo, cudaStrea
   long nf = 1;
   for (int a = 0; a < 3; ++a) nf *= (long)(b.hi[a] - b.lo[a] + (a == AXIS ? 1 : 0));
   if (nf > 0) {
-    k_struct_faces<FAM, SCHEME, AXIS><<<div_up(nf, 128), 128, 0, s>>>(b, p, U, Fo);
+    if constexpr (SCHEME == FirstOrder) {
+      k_struct_faces<FAM, SCHEME, AXIS><<<div_up(nf, 128), 128, 0, s>>>(b, p, U, Fo);
+    } else {
+      // tiled kernel: lines of the other two axes in grid x, face chunks in grid y
+      constexpr int NR = 2;
+      using Cfg = TileCfg<SCHEME>;
+      long lines = 1;
+      for (int a = 0; a < 3; ++a)
+        if (a != AXIS) lines *= (long)(b.hi[a] - b.lo[a]);
+      const int nfa = b.hi[AXIS] - b.lo[AXIS] + 1;
+      dim3 grid(div_up(lines, NR), div_up(nfa, Cfg::TW));
+      dim3 block(Cfg::LANES, NR);
+      k_faces_tile<FAM, SCHEME, AXIS, NR><<<grid, block, 0, s>>>(b, p, U, Fo);
+    }
     ++*launches;
   }
   if (ev) cudaEventRecord(ev[AXIS + 1], s);

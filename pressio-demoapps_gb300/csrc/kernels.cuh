@@ -176,12 +176,24 @@ k_rows_velocity(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U, do
 // ---------------------------------------------------------------------------
 // Structured full mesh: faces once, then per-cell balance.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int wrap(int i, int n, int periodic) {
-  if (periodic) {
-    i %= n;
-    if (i < 0) i += n;
+// cell index along an axis for a position that may lie outside [0, n)
+__device__ __forceinline__ int map_cell(int c, int n, int mode, bool &mirrored) {
+  mirrored = false;
+  if (mode == 1) {
+    c %= n;
+    if (c < 0) c += n;
+  } else if (mode == 2) {
+    if (c < 0) {
+      c = -c - 1;
+      mirrored = true;
+    } else if (c >= n) {
+      c = 2 * n - 1 - c;
+      mirrored = true;
+    }
   }
-  return i;
+  // interior boxes never leave the mesh for faces that are written; clamp
+  // the loads of unused tile tails
+  return c < 0 ? 0 : (c >= n ? n - 1 : c);
 }
 
 // One thread per face normal to AXIS inside the box; face f lies between
@@ -206,10 +218,14 @@ k_struct_faces(Box b, Phys p, const double *__restrict__ U, double *__restrict__
 #pragma unroll
   for (int s = 0; s < 2 * H; ++s) {
     int cc[3] = {c[0], c[1], c[2]};
-    cc[AXIS] = wrap(c[AXIS] - H + s, b.n[AXIS], b.periodic[AXIS]);
+    bool mir;
+    cc[AXIS] = map_cell(c[AXIS] - H + s, b.n[AXIS], b.mode[AXIS], mir);
     const long cell = cc[0] + (long)b.n[0] * (cc[1] + (long)b.n[1] * cc[2]);
 #pragma unroll
-    for (int d = 0; d < NDPC; ++d) q[s][d] = __ldg(U + cell * NDPC + d);
+    for (int d = 0; d < NDPC; ++d) {
+      q[s][d] = __ldg(U + cell * NDPC + d);
+      if (mir && d == b.reflect[AXIS]) q[s][d] = -q[s][d];
+    }
   }
   double uN[NDPC], uP[NDPC], f[NDPC];
   reconstruct_face<NDPC, SCHEME>(uN, uP, q);

@@ -39,9 +39,19 @@ template <> struct SchemeTraits<Weno3> { static constexpr int h = 2; };
 template <> struct SchemeTraits<Weno5> { static constexpr int h = 3; };
 
 PDA_HD double sq(double x) { return x * x; }
-// deviation: the reference evaluates std::pow(x, 3.) (glibc); here (x*x)*x,
-// which differs by at most a few ulp.  Used only on the Jacobian path.
-PDA_HD double cube(double x) { return (x * x) * x; }
+// x^3 for the reference's std::pow(x, 3.) (glibc pow, correctly rounded in
+// all but pathological near-midpoint cases).  Computed with Dekker's exact
+// two-product: x*x = p + e and p*x = c + ce exactly, so x^3 = c + ce + e*x
+// with an error of order 2^-106 before the final rounding; the result is the
+// correctly rounded cube except when x^3 lies within that distance of a
+// rounding midpoint.  Used only on the Jacobian path.
+PDA_HD double cube(double x) {
+  const double p = x * x;
+  const double e = fma(x, x, -p);
+  const double c = p * x;
+  const double ce = fma(p, x, -c);
+  return c + (ce + e * x);
+}
 
 // ---------------------------------------------------------------------------
 // WENO5, one face i+1/2: uNeg from q_{i-2..i+2}, uPos from q_{i-1..i+3}.

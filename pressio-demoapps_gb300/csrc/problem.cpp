@@ -116,6 +116,7 @@ struct pda_problem {
   const pda::Launchers *L = nullptr;
   // velocity
   bool useStruct = false;
+  bool structAll = false;  // the structured box covers every cell (mirror boundaries)
   pda::Box box{};
   pda::DevBuf<double> F[3];
   pda::Table nearT;   // near-boundary rows: V stencil (+ J first-order tables)
@@ -578,10 +579,12 @@ void velocity(pda_problem &P, const double *U, double *V, cudaEvent_t *ev = null
       check_launch(P);
     }
   }
-  P.nearT.sync();
-  if (P.nearT.t.nrows > 0) {
-    P.L->rows_velocity(P.scheme, P.nearT.t, P.margs, P.phys, U, V, P.stream);
-    check_launch(P);
+  if (!P.structAll) {
+    P.nearT.sync();
+    if (P.nearT.t.nrows > 0) {
+      P.L->rows_velocity(P.scheme, P.nearT.t, P.margs, P.phys, U, V, P.stream);
+      check_launch(P);
+    }
   }
   if (ev) cudaEventRecord(ev[P.dim + 2], P.stream);
 }
@@ -703,25 +706,49 @@ void create_problem(pda_problem &P, const Mesh &m, int family, int probEn, int s
     case PDA_EULER3D: P.L = &launchers_euler3d(); break;
     default: P.L = &launchers_swe2d(); break;
   }
-  // structured interior box
+  // Structured box.  With the 2D mirror boundary conditions (Neumann, slip
+  // wall) the ghost layers are exact mirror images of interior cells
+  // (Ghost2dNeumannFiller / InviscidWallFiller with at least 2*h cells per
+  // axis), so the box covers the whole mesh and boundary faces are computed
+  // from mirrored loads; otherwise it covers the inner rows and the
+  // near-boundary rows go through the per-row kernel.
   P.useStruct = false;
+  P.structAll = false;
   if (m.structured) {
     const int hm = (m.stencil - 1) / 2;
+    bool mirror = P.bc == BC_MIRROR2D;
+    for (int a = 0; a < P.dim; ++a)
+      if (!m.periodic[a] && m.n[a] < 2 * hm + 1) mirror = false;
     Box b{};
     long cells = 1;
     for (int a = 0; a < 3; ++a) {
       b.n[a] = a < P.dim ? m.n[a] : 1;
-      b.periodic[a] = a < P.dim ? m.periodic[a] : 0;
-      if (a >= P.dim || b.periodic[a]) {
+      b.reflect[a] = -1;
+      if (a >= P.dim) {
+        b.mode[a] = 0;
+        b.lo[a] = 0;
+        b.hi[a] = 1;
+      } else if (m.periodic[a]) {
+        b.mode[a] = 1;
         b.lo[a] = 0;
         b.hi[a] = b.n[a];
+      } else if (mirror) {
+        b.mode[a] = 2;
+        b.lo[a] = 0;
+        b.hi[a] = b.n[a];
+        b.reflect[a] = P.margs.reflect[a];
       } else {
+        b.mode[a] = 0;
         b.lo[a] = std::min(hm, b.n[a]);
         b.hi[a] = std::max(b.lo[a], b.n[a] - hm);
       }
       cells *= (long)(b.hi[a] - b.lo[a]);
     }
-    if (cells == (long)m.inner.size()) {
+    if (mirror && cells == (long)m.sampleMeshSize) {
+      P.box = b;
+      P.useStruct = true;
+      P.structAll = true;
+    } else if (!mirror && cells == (long)m.inner.size()) {
       P.box = b;
       P.useStruct = true;
     }

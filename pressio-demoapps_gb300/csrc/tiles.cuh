@@ -1,0 +1,180 @@
+// Tiled face kernels for WENO3 / WENO5 on natural-order full meshes.
+//
+// The FP64 pipe bounds this path on GB300, so the kernels minimise FP64
+// operations while keeping every value bit-identical to the reference:
+//  * each face is computed once (the reference computes it from both cells);
+//  * the smoothness indicators of a cell triple (WENO5) or pair (WENO3) and
+//    the alpha terms built from them enter up to three one-sided
+//    reconstructions of neighbouring faces with identical expression trees
+//    (impl/weno5.hpp:112-178, impl/weno3.hpp:82-131), so they are computed
+//    once per cell into shared memory and reused;
+//  * boundary faces of the mirror-type boundary conditions (2D Neumann and
+//    slip wall, whose ghost layers are exact mirror images,
+//    euler_2d_ghost_filler_neumann.hpp:101-276,
+//    swe_2d_ghost_filler_inviscid_wall.hpp:99-278) are computed in the same
+//    pass by mirrored loads, so no per-row boundary kernel is needed.
+//
+// Block: LANES threads along the face axis x NR lines; a block produces TW
+// faces of each of its NR lines (TW = LANES - 3 for WENO5, LANES - 2 for
+// WENO3).  Loads along y/z are strided gathers of whole 32-40 byte cells, so
+// no sector is fetched for nothing.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace pda {
+
+template <int SCHEME> struct TileCfg;
+template <> struct TileCfg<Weno5> {
+  static constexpr int H = 3, LANES = 64, TW = LANES - 3, NCELL = TW + 5, NA = 5;
+};
+template <> struct TileCfg<Weno3> {
+  static constexpr int H = 2, LANES = 64, TW = LANES - 2, NCELL = TW + 3, NA = 2;
+};
+
+template <int FAM, int SCHEME, int AXIS, int NR>
+__global__ void __launch_bounds__(TileCfg<SCHEME>::LANES *NR)
+k_faces_tile(Box b, Phys p, const double *__restrict__ U, double *__restrict__ Fout) {
+  using F = Fam<FAM>;
+  using C = TileCfg<SCHEME>;
+  constexpr int NDPC = F::ndpc, LANES = C::LANES, TW = C::TW, NCELL = C::NCELL, H = C::H, NA = C::NA;
+  constexpr int A1 = AXIS == 0 ? 1 : 0, A2 = AXIS == 2 ? 1 : 2;  // the two other axes
+  __shared__ double sU[NR][NDPC][NCELL + 1];
+  __shared__ double sA[NR][NDPC][NA][LANES];
+
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int nb1 = b.hi[A1] - b.lo[A1], nb2 = b.hi[A2] - b.lo[A2];
+  const int nf = b.hi[AXIS] - b.lo[AXIS] + 1;
+  const long line = (long)blockIdx.x * NR + ty;
+  const bool lineOk = line < (long)nb1 * nb2;
+  const int c1 = lineOk ? b.lo[A1] + (int)(line % nb1) : b.lo[A1];
+  const int c2 = lineOk ? b.lo[A2] + (int)(line / nb1) : b.lo[A2];
+  const int f0 = b.lo[AXIS] + blockIdx.y * TW;  // first face of the tile
+  long stride[3];
+  stride[0] = 1;
+  stride[1] = b.n[0];
+  stride[2] = (long)b.n[0] * b.n[1];
+  const long base = (long)c1 * stride[A1] + (long)c2 * stride[A2];
+
+  // ---- phase A: cells f0-H .. f0+TW+H-2 of this line into shared memory
+  for (int k = tx; k < NCELL; k += LANES) {
+    bool mir;
+    const int c = map_cell(f0 - H + k, b.n[AXIS], b.mode[AXIS], mir);
+    const double *src = U + (base + (long)c * stride[AXIS]) * NDPC;
+#pragma unroll
+    for (int d = 0; d < NDPC; ++d) {
+      double v = __ldg(src + d);
+      if (mir && d == b.reflect[AXIS]) v = -v;
+      sU[ty][d][k] = v;
+    }
+  }
+  __syncthreads();
+
+  // ---- phase B: per-cell alpha terms
+  constexpr double epsilon = 1e-6;
+  if constexpr (SCHEME == Weno5) {
+    // center c = f0 - 2 + tx uses cells c-1, c, c+1 = sU[tx .. tx+2]
+    constexpr double two = 2., three = 3., four = 4.;
+    constexpr double oneOvfour = 1. / 4., oneOvten = 1. / 10., threeOvten = 3. / 10., sixOvten = 6. / 10.,
+                     thirteenOvtwelve = 13. / 12.;
+    if (tx + 2 < NCELL) {
+#pragma unroll
+      for (int d = 0; d < NDPC; ++d) {
+        const double a = sU[ty][d][tx], m = sU[ty][d][tx + 1], c = sU[ty][d][tx + 2];
+        const double X = a - two * m + c;
+        const double D = thirteenOvtwelve * X * X;
+        const double YL = a - four * m + three * c;
+        const double YC = a - c;
+        const double YR = three * a - four * m + c;
+        const double BL = D + oneOvfour * YL * YL;
+        const double BC = D + oneOvfour * YC * YC;
+        const double BR = D + oneOvfour * YR * YR;
+        const double dL = epsilon * epsilon + 2. * epsilon * BL + BL * BL;
+        const double dC = epsilon * epsilon + 2. * epsilon * BC + BC * BC;
+        const double dR = epsilon * epsilon + 2. * epsilon * BR + BR * BR;
+        sA[ty][d][0][tx] = oneOvten / dL;    // uNeg alpha0 of face c+1+1/2
+        sA[ty][d][1][tx] = threeOvten / dL;  // uPos alpha0 of face c+1/2
+        sA[ty][d][2][tx] = sixOvten / dC;    // uNeg alpha1 of face c+1/2, uPos alpha1 of face c-1/2
+        sA[ty][d][3][tx] = threeOvten / dR;  // uNeg alpha2 of face c-1/2
+        sA[ty][d][4][tx] = oneOvten / dR;    // uPos alpha2 of face c-2+1/2
+      }
+    }
+  } else {
+    // pair k = (f0 - 2 + tx, f0 - 1 + tx) uses cells sU[tx], sU[tx+1]
+    constexpr double two = 2., oneOvthree = 1. / 3., twoOvthree = 2. / 3.;
+    if (tx + 1 < NCELL) {
+#pragma unroll
+      for (int d = 0; d < NDPC; ++d) {
+        const double a = sU[ty][d][tx], c = sU[ty][d][tx + 1];
+        const double B = (a - c) * (a - c);
+        const double den = epsilon * epsilon + two * epsilon * B + B * B;
+        sA[ty][d][0][tx] = oneOvthree / den;
+        sA[ty][d][1][tx] = twoOvthree / den;
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- phase C: face f = f0 + tx between cells f-1 and f
+  const int f = f0 + tx;
+  if (!lineOk || tx >= TW || f > b.hi[AXIS]) return;
+  double uN[NDPC], uP[NDPC];
+  if constexpr (SCHEME == Weno5) {
+    constexpr double two = 2., five = 5., seven = 7., eleven = 11., oneOvsix = 1. / 6.;
+#pragma unroll
+    for (int d = 0; d < NDPC; ++d) {
+      // left cell i = f-1: cells i-2..i+3 = sU[tx .. tx+5]; centers i-1..i+2 = sA[.][tx .. tx+3]
+      const double qim2 = sU[ty][d][tx], qim1 = sU[ty][d][tx + 1], qi = sU[ty][d][tx + 2];
+      const double qip1 = sU[ty][d][tx + 3], qip2 = sU[ty][d][tx + 4], qip3 = sU[ty][d][tx + 5];
+      const double p0 = (two * qim2 - seven * qim1 + eleven * qi) * oneOvsix;
+      const double p1 = (-qim1 + five * qi + two * qip1) * oneOvsix;
+      const double p2 = (two * qi + five * qip1 - qip2) * oneOvsix;
+      const double p3 = (eleven * qip1 - seven * qip2 + two * qip3) * oneOvsix;
+      {
+        const double a0 = sA[ty][d][0][tx], a1 = sA[ty][d][2][tx + 1], a2 = sA[ty][d][3][tx + 2];
+        const double s = 1. / (a0 + a1 + a2);
+        uN[d] = (a0 * s) * p0 + (a1 * s) * p1 + (a2 * s) * p2;
+      }
+      {
+        const double a0 = sA[ty][d][1][tx + 1], a1 = sA[ty][d][2][tx + 2], a2 = sA[ty][d][4][tx + 3];
+        const double s = 1. / (a0 + a1 + a2);
+        uP[d] = (a0 * s) * p1 + (a1 * s) * p2 + (a2 * s) * p3;
+      }
+    }
+  } else {
+    constexpr double three = 3., oneOvtwo = 1. / 2.;
+#pragma unroll
+    for (int d = 0; d < NDPC; ++d) {
+      // left cell i = f-1: cells i-1..i+2 = sU[tx .. tx+3]; pairs i-1, i, i+1 = sA[.][tx .. tx+2]
+      const double qim1 = sU[ty][d][tx], qi = sU[ty][d][tx + 1], qip1 = sU[ty][d][tx + 2],
+                   qip2 = sU[ty][d][tx + 3];
+      const double p0 = (-qim1 + three * qi) * oneOvtwo;
+      const double p1 = (qi + qip1) * oneOvtwo;
+      const double p2 = (three * qip1 - qip2) * oneOvtwo;
+      {
+        const double a0 = sA[ty][d][0][tx], a1 = sA[ty][d][1][tx + 1];
+        const double s = 1. / (a0 + a1);
+        uN[d] = (a0 * s) * p0 + (a1 * s) * p1;
+      }
+      {
+        const double a0 = sA[ty][d][1][tx + 1], a1 = sA[ty][d][0][tx + 2];
+        const double s = 1. / (a0 + a1);
+        uP[d] = (a0 * s) * p1 + (a1 * s) * p2;
+      }
+    }
+  }
+  double fl[NDPC];
+  F::template flux<AXIS>(fl, uN, uP, p);
+  // output layout of k_struct_faces: face axis index fastest within its line
+  // ordering [A2][A1][face] for AXIS=0, [k][face][i] for AXIS=1, [face][j][i] for AXIS=2
+  const int fi = f - b.lo[AXIS];
+  const int i1 = c1 - b.lo[A1], i2 = c2 - b.lo[A2];
+  long o;
+  if (AXIS == 0) o = fi + (long)nf * (i1 + (long)nb1 * i2);
+  else if (AXIS == 1) o = i1 + (long)nb1 * (fi + (long)nf * i2);
+  else o = i1 + (long)nb1 * (i2 + (long)nb2 * fi);
+#pragma unroll
+  for (int d = 0; d < NDPC; ++d) Fout[o * NDPC + d] = fl[d];
+}
+
+}  // namespace pda

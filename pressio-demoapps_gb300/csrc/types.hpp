@@ -36,11 +36,16 @@ struct MeshArgs {
   int reflect[3];  // dof negated in a mirrored ghost for a face normal to each axis (-1: none)
 };
 
+// Structured box of a natural-order full mesh: cells [lo, hi) per axis,
+// faces normal to an axis at [lo, hi].  mode per axis: 0 = the box stays
+// inside the mesh, 1 = periodic, 2 = mirror images outside the mesh (the 2D
+// Neumann and slip-wall ghost layers), with dof reflect[axis] negated in
+// mirrored cells.
 struct Box {
-  int n[3];       // cells per axis (1 for absent axes)
-  int lo[3];      // first box cell per axis
-  int hi[3];      // one past the last box cell per axis
-  int periodic[3];
+  int n[3];
+  int lo[3], hi[3];
+  int mode[3];
+  int reflect[3];
 };
 
 }  // namespace pda

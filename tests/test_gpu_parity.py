@@ -26,6 +26,13 @@ MANIFEST = json.load(open(os.path.join(GOLDEN, "manifest.json")))
 TRAJ = json.load(open(os.path.join(GOLDEN, "gold", "trajectories.json")))
 
 
+def oracle_mod():
+    import sys
+    sys.path.insert(0, os.path.join(GOLDEN, "..", "..", "oracle"))
+    import oracle_py
+    return oracle_py
+
+
 def _torch():
     import torch
     assert torch.cuda.is_available(), "GPU tests need CUDA"
@@ -58,8 +65,14 @@ def test_velocity_matches_reference(pda, case):
         U = torch.from_numpy(g[uk]).cuda()
         V = p.createVelocity()
         p.velocity(U, 0.0, V)
-        ok, worst = v_close(V.cpu().numpy(), g[vk], m["ndpc"])
+        v = V.cpu().numpy()
+        ok, worst = v_close(v, g[vk], m["ndpc"])
         assert ok, f"{case} {vk}: worst relative error {worst:.3e}"
+        if m["family"] != 3:
+            # Euler velocities follow the reference's operation order exactly
+            # (the shallow-water flux takes sqrt for glibc's pow(h, 0.5))
+            assert np.array_equal(v, g[vk]), f"{case} {vk}: not bit-identical"
+
 
 
 @pytest.mark.parametrize("case", sorted(MANIFEST))
@@ -76,8 +89,28 @@ def test_jacobian_matches_reference(pda, case):
     p.rightHandSideAndJacobian(U, 0.0, V, J)
     ok, worst = v_close(V.cpu().numpy(), g["Vj"], m["ndpc"])
     assert ok, f"{case} V (V+J path): worst {worst:.3e}"
-    ok, worst = j_close(J.values.cpu().numpy(), g["jvals"], g["rowptr"])
+    # J within 1e-12 of the row scale: the WENO weight derivatives cancel
+    # terms far larger than the entries, and the reference's own x^3 (glibc
+    # pow, not always correctly rounded) moves entries by up to ~1e-13 of it
+    jv = J.values.cpu().numpy()
+    ok, worst = j_close(jv, g["jvals"], g["rowptr"], floor_frac=1.0)
     assert ok, f"{case} J: worst {worst:.3e}"
+    # ... and bit for bit equal to the oracle evaluated with a correctly
+    # rounded x^3, the library's documented arithmetic
+    orc = oracle_mod().load()
+    orc.set_cube_mode(1)
+    try:
+        op = orc.problem(orc.mesh_load(mesh_dir(m["mesh"])), m["family"], m["problem"], m["scheme"], m["icflag"],
+                         m.get("params"))
+        Vo, _, _, jo = op.velocity_and_jacobian(g["U1"])
+    finally:
+        orc.set_cube_mode(0)
+    if m["family"] != 3:
+        assert np.array_equal(jv, jo), f"{case}: J differs from the oracle ({np.sum(jv != jo)} entries)"
+        assert np.array_equal(V.cpu().numpy(), Vo)
+    else:
+        ok, worst = j_close(jv, jo, g["rowptr"], rtol=1e-13, floor_frac=1.0)
+        assert ok, f"{case}: J vs oracle worst {worst:.3e}"
     # jacobian() alone gives the same values
     J2 = p.createJacobian()
     p.jacobian(U, 0.0, J2)

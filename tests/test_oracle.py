@@ -65,3 +65,22 @@ def test_oracle_trajectory_gold(oracle, name):
     else:
         gold = np.load(os.path.join(GOLDEN, "gold", name + ".npy"))
         assert np.allclose(U.reshape(-1, 3)[:, 0], gold, rtol=t["rtol"], atol=t["atol"])
+
+
+@pytest.mark.parametrize("case", sorted(MANIFEST))
+def test_correctly_rounded_cube_stays_within_the_jacobian_tolerance(oracle, case):
+    """The library evaluates the reference's pow(x, 3.) as a correctly rounded
+    cube.  Evaluated that way, the oracle's Jacobian stays within 1e-12 of the
+    row scale of the reference's (velocities are unaffected)."""
+    from conftest import j_close
+    m = MANIFEST[case]
+    g = golden_case(case)
+    oracle.set_cube_mode(1)
+    try:
+        p = _problem(oracle, m)
+        V, rp, ci, jv = p.velocity_and_jacobian(g["U1"])
+    finally:
+        oracle.set_cube_mode(0)
+    assert np.array_equal(V, g["Vj"])
+    ok, worst = j_close(jv, g["jvals"], rp, floor_frac=1.0)
+    assert ok, worst
