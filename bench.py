@@ -188,6 +188,152 @@ def run_reference(args):
     return 0
 
 
+def _time_gpu(torch, stream, fn, reps, warm=2):
+    for _ in range(warm):
+        fn()
+    stream.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    with torch.cuda.stream(stream):
+        for a, b in ev:
+            a.record(stream)
+            fn()
+            b.record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev) / reps
+
+
+def _cpu_rate(fn, budget_s):
+    fn()
+    ts = []
+    t_end = time.perf_counter() + budget_s
+    while time.perf_counter() < t_end or not ts:
+        t0 = time.perf_counter()
+        fn()
+        ts.append(time.perf_counter() - t0)
+    return statistics.median(ts), len(ts)
+
+
+def extra_workloads(pda, torch, stream, cpu=True):
+    """Secondary configurations (one line each): Jacobian nnz/s at 1024^2, 3D
+    WENO5 velocity at 256^3, 3D WENO5 Jacobian at 96^3, 1D Sod SSP-RK3 2000 steps."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle_py
+    orc = oracle_py.load() if cpu else None
+    threads = orc.set_threads(os.cpu_count() or 1) if cpu else 0
+    out = {}
+    rng = np.random.default_rng(20261203)
+
+    def oracle_problem(mesh, fam, prob, scheme, ic, dim, st):
+        g, x, y, z, _, _ = mesh._arrays()
+        om = orc.mesh_from_arrays(dim, st, g, x, y, z, (mesh.dx(), mesh.dy(), mesh.dz()))
+        return om, orc.problem(om, fam, prob, scheme, ic)
+
+    # -- 2D Euler Riemann WENO5 Jacobian (V + CSR J), 1024^2
+    n = 1024
+    mesh = pda.create_full_mesh((n, n), (0.0, 1.0, 0.0, 1.0), 7)
+    prob = pda.create_problem(mesh, pda.Euler2d.Riemann, pda.InviscidFluxReconstruction.Weno5, 2, stream=stream)
+    Uh = prob.initialConditionHost() + rng.uniform(-1e-3, 1e-3, 4 * n * n)
+    with torch.cuda.stream(stream):
+        U = torch.from_numpy(Uh).cuda()
+        V = prob.createVelocity()
+        J = prob.createJacobian()
+    ms = _time_gpu(torch, stream, lambda: prob.rightHandSideAndJacobian(U, 0.0, V, J), 5)
+    nnz = J.nonZeros()
+    w = {"config": "euler2d_riemann_ic2_weno5_jacobian_1024x1024", "ms_per_call": ms, "nnz": nnz,
+         "value": nnz / (ms * 1e-3) / 1e9, "unit": "Gnnz/s (V + CSR J per call)",
+         "gcell_per_s": n * n / (ms * 1e-3) / 1e9}
+    del U, V, J, prob
+    torch.cuda.empty_cache()
+    if cpu:
+        ns = 256
+        m2 = pda.create_full_mesh((ns, ns), (0.0, 1.0, 0.0, 1.0), 7)
+        p2 = pda.create_problem(m2, pda.Euler2d.Riemann, pda.InviscidFluxReconstruction.Weno5, 2, stream=0)
+        U2 = p2.initialConditionHost() + rng.uniform(-1e-3, 1e-3, 4 * ns * ns)
+        om, op = oracle_problem(m2, 1, 4, 2, 2, 2, 7)
+        med, k = _cpu_rate(lambda: op.velocity_and_jacobian(U2), 5.0)
+        w["cpu_baseline"] = {"value": op.nnz / med / 1e9, "unit": "Gnnz/s", "cores": threads, "kind": "port",
+                             "sample": f"{k} V+J calls at 256^2 (same problem/scheme), median {med*1e3:.1f} ms"}
+    out["jacobian_2d"] = w
+
+    # -- 3D Euler smooth periodic WENO5 velocity, 256^3
+    n = 256
+    mesh = pda.create_full_mesh((n, n, n), (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0), 7, (True, True, True))
+    prob = pda.create_problem(mesh, pda.Euler3d.PeriodicSmooth, pda.InviscidFluxReconstruction.Weno5, stream=stream)
+    with torch.cuda.stream(stream):
+        U = prob.initialCondition()
+        V = prob.createVelocity()
+    ms = _time_gpu(torch, stream, lambda: prob.velocity(U, 0.0, V), 5)
+    prof = prob.profile_velocity(U, V, reps=3)
+    w = {"config": "euler3d_smooth_periodic_weno5_velocity_256^3", "ms_per_call": ms,
+         "value": n ** 3 / (ms * 1e-3) / 1e9, "unit": "Gcell/s", "kernel_ms": prof}
+    del U, V, prob
+    torch.cuda.empty_cache()
+    if cpu:
+        ns = 64
+        m3 = pda.create_full_mesh((ns, ns, ns), (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0), 7, (True, True, True))
+        om, op = oracle_problem(m3, 2, 0, 2, 1, 3, 7)
+        U3 = op.initial_condition()
+        med, k = _cpu_rate(lambda: op.velocity(U3), 5.0)
+        w["cpu_baseline"] = {"value": ns ** 3 / med / 1e9, "unit": "Gcell/s", "cores": threads, "kind": "port",
+                             "sample": f"{k} velocity calls at 64^3 (same problem/scheme), median {med*1e3:.1f} ms"}
+    out["velocity_3d"] = w
+
+    # -- 3D Euler WENO5 Jacobian, 96^3
+    n = 96
+    mesh = pda.create_full_mesh((n, n, n), (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0), 7, (True, True, True))
+    prob = pda.create_problem(mesh, pda.Euler3d.PeriodicSmooth, pda.InviscidFluxReconstruction.Weno5, stream=stream)
+    with torch.cuda.stream(stream):
+        U = prob.initialCondition()
+        V = prob.createVelocity()
+        J = prob.createJacobian()
+    ms = _time_gpu(torch, stream, lambda: prob.rightHandSideAndJacobian(U, 0.0, V, J), 3)
+    nnz = J.nonZeros()
+    w = {"config": "euler3d_smooth_periodic_weno5_jacobian_96^3", "ms_per_call": ms, "nnz": nnz,
+         "value": nnz / (ms * 1e-3) / 1e9, "unit": "Gnnz/s (V + CSR J per call)"}
+    del U, V, J, prob
+    torch.cuda.empty_cache()
+    if cpu:
+        ns = 24
+        m3 = pda.create_full_mesh((ns, ns, ns), (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0), 7, (True, True, True))
+        om, op = oracle_problem(m3, 2, 0, 2, 1, 3, 7)
+        U3 = op.initial_condition()
+        med, k = _cpu_rate(lambda: op.velocity_and_jacobian(U3), 5.0)
+        w["cpu_baseline"] = {"value": op.nnz / med / 1e9, "unit": "Gnnz/s", "cores": threads, "kind": "port",
+                             "sample": f"{k} V+J calls at 24^3 (same problem/scheme), median {med*1e3:.1f} ms"}
+    out["jacobian_3d"] = w
+
+    # -- 1D Sod, WENO5, SSP-RK3 dt=1e-4, 2000 steps (CUDA-graph steps)
+    mesh = pda.create_full_mesh((1000,), (-0.5, 0.5), 7)
+    prob = pda.create_problem(mesh, pda.Euler1d.Sod, pda.InviscidFluxReconstruction.Weno5, stream=stream)
+    with torch.cuda.stream(stream):
+        U = prob.initialCondition()
+    prob.advance_ssprk3(U, 0.0, 1e-4, 10)  # capture + warm-up
+    stream.synchronize()
+    with torch.cuda.stream(stream):
+        U = prob.initialCondition()
+    stream.synchronize()
+    t0 = time.perf_counter()
+    prob.advance_ssprk3(U, 0.0, 1e-4, 2000)
+    stream.synchronize()
+    wall = time.perf_counter() - t0
+    w = {"config": "euler1d_sod_weno5_ssprk3_dt1e-4_2000_steps_1000_cells", "wall_ms": wall * 1e3,
+         "value": 3 * 2000 * 1000 / wall / 1e9, "unit": "Gcell-updates/s",
+         "note": "whole run timed on the host clock, steps replayed from a CUDA graph"}
+    if cpu:
+        om, op = oracle_problem(mesh, 0, 1, 2, 1, 1, 7)
+        orc.set_threads(1)
+        Uo = op.initial_condition()
+        t0 = time.perf_counter()
+        op.ssprk3(Uo, 0.0, 1e-4, 2000)
+        cw = time.perf_counter() - t0
+        orc.set_threads(os.cpu_count() or 1)
+        w["cpu_baseline"] = {"value": 3 * 2000 * 1000 / cw / 1e9, "unit": "Gcell-updates/s", "cores": 1,
+                             "kind": "port", "sample": f"the full 2000-step run, 1 thread, {cw*1e3:.0f} ms"}
+        w["final_state_matches_oracle"] = bool(np.allclose(U.cpu().numpy(), Uo, rtol=1e-12, atol=1e-13))
+    out["sod_1d_ssprk3"] = w
+    return out
+
+
 def workload_config():
     return {"workload": f"euler2d_riemann_ic2_weno5_velocity_{N_CELLS_SIDE}x{N_CELLS_SIDE}", "cells": N_CELLS_SIDE ** 2,
             "dofs": NDPC * N_CELLS_SIDE ** 2, "scheme": "WENO5+Rusanov", "boundary": "Neumann (transmissive)",
@@ -204,6 +350,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer measurement (profiling runs)")
     ap.add_argument("--n", type=int, default=1024, help="cells per side (1024 = the benchmark workload)")
+    ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
     args = ap.parse_args()
     global N_CELLS_SIDE
     N_CELLS_SIDE = args.n
@@ -285,10 +432,11 @@ def main():
     # writes the face fluxes (32 B/face); half the cell's flops
     face_bytes = cells * (8 * NDPC) + (cells + N_CELLS_SIDE) * (8 * NDPC)
     achieved_gbs = face_bytes / (face_ms * 1e-3) / 1e9
-    fp64_peak = pda.measure_fp64_peak()
-    flops_face_launch = cells * (FLOPS_PER_CELL - 24) / 2
-    fp64_ach = flops_face_launch / (face_ms * 1e-3)
-    step_fp64 = cells * FLOPS_PER_CELL / (ms * 1e-3)
+    fp64_peak = pda.measure_fp64_peak()  # FLOP/s with an FMA counted as 2
+    fp64_inst_peak = fp64_peak / 2.0      # FP64 instructions per second (DFMA/DMUL/DADD)
+    ops_face_launch = cells * (FLOPS_PER_CELL - 24) / 2
+    ops_ach = ops_face_launch / (face_ms * 1e-3)
+    step_ops = cells * FLOPS_PER_CELL / (ms * 1e-3)
 
     line = {
         "metric": "FV residual Gcell/s", "value": value, "unit": "Gcell/s", "n_gpus": world,
@@ -303,15 +451,24 @@ def main():
                      "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved_gbs / hbm_peak, "traffic": None, "peak_source": peak_src,
                      "binding_roof": "fp64",
-                     "fp64": {"achieved_tflops": fp64_ach / 1e12, "peak_tflops": fp64_peak / 1e12,
-                              "frac": fp64_ach / fp64_peak, "peak_source": "measured FMA probe (pda_measure_fp64_peak)",
-                              "step_achieved_tflops": step_fp64 / 1e12,
-                              "algorithmic_flops_per_cell": FLOPS_PER_CELL},
+                     "fp64": {"achieved_gops": ops_ach / 1e9, "peak_ginst_per_s": fp64_inst_peak / 1e9,
+                              "frac": ops_ach / fp64_inst_peak, "peak_tflops_fma2": fp64_peak / 1e12,
+                              "peak_source": "measured DFMA probe (pda_measure_fp64_peak)",
+                              "note": "algorithmic FP64 ops (add/mul/div/sqrt = 1) per second of the face kernel "
+                                      "against the FP64 instruction issue rate; divisions and square roots "
+                                      "execute several instructions each, so the pipe is busier than frac "
+                                      "(ncu: 86 % FP64 pipe busy, profiles/)",
+                              "step_achieved_gops": step_ops / 1e9,
+                              "algorithmic_ops_per_cell": FLOPS_PER_CELL},
                      "kernel_ms": prof},
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pda, mesh, Uh, budget_s=args.cpu_budget)
+    if rank == 0 and not args.no_extra:
+        del U, V, flush
+        torch.cuda.empty_cache()
+        line["workloads"] = extra_workloads(pda, torch, stream, cpu=not args.no_cpu_baseline)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -143,7 +143,14 @@ def test_gpu_3d_matches_oracle(oracle, pda, tmp_path, scheme):
 
 @pytest.mark.gpu
 def test_gpu_3d_weno5_jacobian_finite_differences_96(pda):
-    """Config size for the 3D Jacobian (96^3, WENO5, periodic): FD agreement."""
+    """Config size for the 3D Jacobian (96^3, WENO5, periodic): FD agreement.
+
+    The Rusanov flux takes max(|uL|+cL, |uR|+cR), which has a kink; among the
+    2.6M faces a random direction of length 1e-8 crosses it at a few, where
+    the one-sided difference legitimately differs from J.a by up to
+    |d lambda| |uR - uL| / dx.  So the bound is per row: all but a handful of
+    the 4.4M rows agree to 1e-6 of the scale, and none is off by more than 1e-3
+    (an error in J itself shows up in a whole class of rows, not a handful)."""
     import torch
     n = 96
     m3 = pda.create_full_mesh((n, n, n), (-1, 1, -1, 1, -1, 1), 7, (True, True, True))
@@ -162,5 +169,8 @@ def test_gpu_3d_weno5_jacobian_finite_differences_96(pda):
     fd = (V1 - V0) / eps
     R = torch.empty_like(V)
     p.applyJacobian(U, a, 0.0, R)
-    err = (R - fd).abs().max().item() / max(1.0, R.abs().max().item())
-    assert err < 1e-5, err
+    scale = max(1.0, R.abs().max().item())
+    dev = (R - fd).abs() / scale
+    n_off = int((dev > 1e-6).sum().item())
+    assert n_off <= 32, (n_off, dev.max().item())
+    assert dev.max().item() < 1e-3, dev.max().item()
