@@ -168,6 +168,30 @@ pda_status pda_velocity(pda_problem *p, const double *d_U, double t, double *d_V
  * (synchronous).  This is what a caller holding Eigen/numpy vectors uses. */
 pda_status pda_velocity_host(pda_problem *p, const double *h_U, double t, double *h_V);
 
+/* Allocation-free variant of pda_velocity (no counterpart in the reference).
+ * For callers that may not allocate device memory while evaluating the
+ * right-hand side: code inside a stream capture it owns, fixed-budget
+ * real-time loops, hosts whose pool allocator forbids library allocations.
+ * pda_velocity allocates its face-flux buffers on a problem's first call;
+ * this entry point puts them in one static device array of
+ * PDA_NOALLOC_SCRATCH_DOUBLES doubles (32 MiB) inside the library instead
+ * and calls no allocator.  Same kernels, same results as pda_velocity.
+ *  - Covers full meshes on the structured face pass (natural-order full
+ *    meshes); sample meshes return PDA_ERR_UNSUPPORTED.  A mesh whose face
+ *    scratch exceeds the limit returns PDA_ERR_INVALID_ARGUMENT with the
+ *    required size in pda_last_error().
+ *  - Problems with near-boundary rows (non-mirror boundary conditions) need
+ *    their row table on the device: one pda_velocity call uploads it, until
+ *    then PDA_ERR_UNSUPPORTED.
+ *  - The first call on each device looks up the array's device address
+ *    (this may load the module that holds it); make that first call before
+ *    any stream capture or allocation-free section begins.
+ *  - Nothing in the array needs to start at zero.  The array is shared by all
+ *    problems of the process on a device: calls that overlap in time (other
+ *    streams or threads without ordering between them) race on it. */
+#define PDA_NOALLOC_SCRATCH_DOUBLES (4u * 1024u * 1024u)
+pda_status pda_velocity_noalloc(pda_problem *p, const double *d_U, double t, double *d_V);
+
 /* createJacobian() (adapter_cpp.hpp:121-124; pattern from initializeJacobian,
  * euler_2d_prob_class.hpp:223-237, :314-387): number of rows
  * (totalDofSampleMesh), columns (totalDofStencilMesh) and stored entries. */

@@ -30,6 +30,7 @@ SOURCES = [
     "kernels_euler3d.cu",
     "kernels_euler1d.cu",
     "util.cu",
+    "noalloc.cu",
     "mesh.cpp",
     "problem.cpp",
 ]

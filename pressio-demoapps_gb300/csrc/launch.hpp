@@ -38,6 +38,10 @@ double measure_fp64_fma_rate(int blocks, int threads, int iters, cudaStream_t s)
 void launch_csr_spmm(long rows, const int *rowptr, const int *colidx, const double *vals,
                      const double *B, long ldb, int ncols, double *R, long ldr, cudaStream_t s);
 
+// device address of the static face-flux scratch (noalloc.cu) on the
+// current device, looked up once per device
+cudaError_t noalloc_face_scratch(double **out);
+
 inline int div_up(long a, long b) { return (int)((a + b - 1) / b); }
 
 }  // namespace pda

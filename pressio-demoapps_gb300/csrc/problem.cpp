@@ -1034,6 +1034,48 @@ pda_status pda_velocity(pda_problem *p, const double *dU, double t, double *dV) 
   PDA_API_END
 }
 
+pda_status pda_velocity_noalloc(pda_problem *p, const double *dU, double t, double *dV) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(p && dU && dV, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  (void)t;
+  pda_problem &P = *p;
+  PDA_REQUIRE(P.useStruct, PDA_ERR_UNSUPPORTED,
+              "pda_velocity_noalloc: only full meshes evaluated by the structured face pass are supported "
+              "(sample meshes have no face scratch: use pda_velocity)");
+  // the near-boundary row table is uploaded by the first pda_velocity call;
+  // uploading it here would allocate
+  const bool nearResident = P.structAll || P.nearT.hostRows() == 0 || !P.nearT.dirty;
+  PDA_REQUIRE(nearResident, PDA_ERR_UNSUPPORTED,
+              "pda_velocity_noalloc: the near-boundary row table of this problem is not on the device yet; "
+              "one pda_velocity call on the problem uploads it");
+  // face regions, each rounded up to 32 doubles (256 bytes)
+  size_t off[3] = {0, 0, 0}, need = 0;
+  for (int a = 0; a < P.dim; ++a) {
+    size_t nf = 1;
+    for (int c = 0; c < 3; ++c) nf *= (size_t)(P.box.hi[c] - P.box.lo[c] + (c == a ? 1 : 0));
+    off[a] = need;
+    need += (nf * (size_t)P.ndpc + 31) / 32 * 32;
+  }
+  if (need > (size_t)PDA_NOALLOC_SCRATCH_DOUBLES)
+    throw pda::Error(PDA_ERR_INVALID_ARGUMENT,
+                     "pda_velocity_noalloc: this mesh needs " + std::to_string(need) +
+                         " doubles of face scratch, more than the static limit of " +
+                         std::to_string((size_t)PDA_NOALLOC_SCRATCH_DOUBLES) +
+                         " (PDA_NOALLOC_SCRATCH_DOUBLES); use pda_velocity");
+  double *scratch = nullptr;
+  PDA_CUDA(pda::noalloc_face_scratch(&scratch));
+  double *Fb[3] = {nullptr, nullptr, nullptr};
+  for (int a = 0; a < P.dim; ++a) Fb[a] = scratch + off[a];
+  int nl = 0;
+  P.L->struct_velocity(P.scheme, P.box, P.margs, P.phys, dU, Fb, dV, P.stream, &nl, nullptr);
+  pda::check_launch(P, nl);
+  if (!P.structAll && P.nearT.t.nrows > 0) {
+    P.L->rows_velocity(P.scheme, P.nearT.t, P.margs, P.phys, dU, dV, P.stream);
+    pda::check_launch(P);
+  }
+  PDA_API_END
+}
+
 pda_status pda_velocity_host(pda_problem *p, const double *hU, double t, double *hV) {
   PDA_API_BEGIN
   PDA_REQUIRE(p && hU && hV, PDA_ERR_INVALID_ARGUMENT, "null argument");
