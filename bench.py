@@ -37,6 +37,10 @@ BYTES_PER_CELL = 16 * NDPC  # read U once + write V once (FP64)
 # WENO5 values at 71 flops + 4 divisions each, one Rusanov flux at 65 flops
 # + 10 divisions + 3 square roots; two faces per cell plus the 24-flop
 # balance; a division or square root counts as one operation).
+# DRAM bytes (read + write) per cell of one face launch, measured by ncu on
+# k_faces_tile at 2048^2 (x-axis launch: 135.4 MB read + 85.4 MB written);
+# traffic grows in proportion to the cells, so it scales to other sizes
+FACE_TRAFFIC_BYTES_PER_CELL = (135.4e6 + 85.4e6) / 2048 ** 2
 FLOPS_PER_CELL = 2 * (4 * 2 * (71 + 4) + 65 + 10 + 3) + 24
 L2_FLUSH_BYTES = 256 << 20
 
@@ -331,7 +335,99 @@ def extra_workloads(pda, torch, stream, cpu=True):
                              "kind": "port", "sample": f"the full 2000-step run, 1 thread, {cw*1e3:.0f} ms"}
         w["final_state_matches_oracle"] = bool(np.allclose(U.cpu().numpy(), Uo, rtol=1e-12, atol=1e-13))
     out["sod_1d_ssprk3"] = w
+
+    # -- 3D Euler smooth periodic WENO5, SSP-RK3 at CFL 0.4, 256^3 (a few of the 200 steps)
+    n = 256
+    mesh = pda.create_full_mesh((n, n, n), (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0), 7, (True, True, True))
+    prob = pda.create_problem(mesh, pda.Euler3d.PeriodicSmooth, pda.InviscidFluxReconstruction.Weno5, stream=stream)
+    # max over cells of |u_axis| + c on the IC (u = 1, p = 1, rho >= 0.8)
+    dt = 0.4 * (2.0 / n) / (1.0 + (1.4 * 1.0 / 0.8) ** 0.5)
+    with torch.cuda.stream(stream):
+        U = prob.initialCondition()
+    prob.advance_ssprk3(U, 0.0, dt, 1)  # capture + warm-up
+    k3 = 2
+    ms = _time_gpu(torch, stream, lambda: prob.advance_ssprk3(U, 0.0, dt, k3), 1, warm=0)
+    w = {"config": "euler3d_smooth_periodic_weno5_ssprk3_cfl0.4_256^3", "dt": dt, "steps_timed": k3,
+         "ms_per_step": ms / k3, "value": 3 * n ** 3 * k3 / (ms * 1e-3) / 1e9, "unit": "Gcell-updates/s",
+         "projected_200_steps_s": 200 * ms / k3 * 1e-3}
+    del U, prob
+    torch.cuda.empty_cache()
+    if cpu:
+        ns = 64
+        m3 = pda.create_full_mesh((ns, ns, ns), (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0), 7, (True, True, True))
+        om, op = oracle_problem(m3, 2, 0, 2, 1, 3, 7)
+        U3 = op.initial_condition()
+        med, k = _cpu_rate(lambda: op.ssprk3(U3, 0.0, dt, 1), 5.0)
+        w["cpu_baseline"] = {"value": 3 * ns ** 3 / med / 1e9, "unit": "Gcell-updates/s", "cores": threads,
+                             "kind": "port", "sample": f"{k} SSP-RK3 steps at 64^3, median {med*1e3:.1f} ms"}
+    out["ssprk3_3d"] = w
+
+    out["batched_swe"] = batched_swe_workload(pda, torch, stream, orc if cpu else None, threads)
     return out
+
+
+def batched_swe_workload(pda, torch, stream, orc, threads, n_inst=512, steps=3):
+    """512 shallow-water slip-wall instances on [-5,5]^2, n drawn seeded from
+    {64, 96, ..., 512}, gravity ~ U[5,10], coriolis ~ U[-4,-1], pulse
+    magnitude ~ U[0.05,0.2]; WENO5, SSP-RK3 dt = 0.005.  Times a few of the
+    500 steps of the whole batch (one CUDA graph per step), the same steps
+    launched instance by instance, and the oracle on a sample of instances."""
+    brng = np.random.default_rng(512)
+    ns = brng.choice(np.arange(64, 513, 32), size=n_inst)
+    grav = brng.uniform(5.0, 10.0, n_inst)
+    cor = brng.uniform(-4.0, -1.0, n_inst)
+    amp = brng.uniform(0.05, 0.2, n_inst)
+    meshes = {int(n): pda.create_full_mesh((int(n), int(n)), (-5.0, 5.0, -5.0, 5.0), 7) for n in sorted(set(ns))}
+    t0 = time.perf_counter()
+    probs = [pda.create_problem(meshes[int(ns[i])], pda.Swe2d.SlipWall, pda.InviscidFluxReconstruction.Weno5, 1,
+                                {"gravity": grav[i], "coriolis": cor[i], "pulseMagnitude": amp[i]}, stream=stream)
+             for i in range(n_inst)]
+    B = pda.create_batch(probs, stream=stream)
+    U = B.initialCondition()
+    setup_s = time.perf_counter() - t0
+    tune = B.autotune(U, reps=2)
+    shapes = [B.tile_shape(a) for a in range(2)]
+    dt = 0.005
+    B.advance_ssprk3(U, 0.0, dt, 1)  # capture + warm-up
+    l0 = B.launch_count()
+    ms = _time_gpu(torch, stream, lambda: B.advance_ssprk3(U, 0.0, dt, steps), 1, warm=0)
+    launches = (B.launch_count() - l0) // steps
+    cells = B.totalCells
+    w = {"config": "batched_swe_slipwall_weno5_ssprk3_dt0.005_512_instances_n64-512",
+         "instances": n_inst, "total_cells": cells, "steps_timed": steps, "ms_per_step": ms / steps,
+         "value": 3 * cells * steps / (ms * 1e-3) / 1e9, "unit": "Gcell-updates/s",
+         "projected_500_steps_s": 500 * ms / steps * 1e-3, "launches_per_step": launches,
+         "tile_shapes": {"x": shapes[0], "y": shapes[1]},
+         "autotune_ms": {"x": tune[0].tolist(), "y": tune[1].tolist()}, "setup_s": setup_s}
+    # the same step, one problem (one CUDA graph) at a time
+    views = [B.instance(U, i) for i in range(n_inst)]
+    for i, p in enumerate(probs):
+        p.advance_ssprk3(views[i], 0.0, dt, 1)
+    ms1 = _time_gpu(torch, stream, lambda: [p.advance_ssprk3(views[i], 0.0, dt, 1) for i, p in enumerate(probs)],
+                    1, warm=0)
+    w["per_instance_launch_ms_per_step"] = ms1
+    w["batching_speedup"] = ms1 / (ms / steps)
+    if orc is not None:
+        sample = [int(i) for i in np.argsort(ns)[[0, n_inst // 2, n_inst - 1]]]
+        tot_cells, tot_s = 0, 0.0
+        import tempfile
+        for i in sample:
+            n = int(ns[i])
+            d = tempfile.mkdtemp()
+            meshes[n].write(d)
+            om = orc.mesh_load(d)
+            op = orc.problem(om, 3, 0, 2, 1, {"gravity": grav[i], "coriolis": cor[i], "pulseMagnitude": amp[i]})
+            Uo = op.initial_condition()
+            t0 = time.perf_counter()
+            op.ssprk3(Uo, 0.0, dt, 1)
+            tot_s += time.perf_counter() - t0
+            tot_cells += 3 * n * n
+        w["cpu_baseline"] = {"value": tot_cells / tot_s / 1e9, "unit": "Gcell-updates/s", "cores": threads,
+                             "kind": "port", "sample": "one SSP-RK3 step of the smallest, median and largest "
+                             f"instance (n = {[int(ns[i]) for i in sample]}), {tot_s*1e3:.0f} ms"}
+    del U, B, probs, views
+    torch.cuda.empty_cache()
+    return w
 
 
 def workload_config():
@@ -447,9 +543,12 @@ def main():
                 "h2d_bytes_per_step": int(Uhp.numel() * 8), "d2h_bytes_per_step": int(Vhp.numel() * 8),
                 "ms_per_step": e2e_ms},
         "gpu_launches": int(launches * args.steps),
-        "roofline": {"bound": "hbm", "kernel": "k_struct_faces<Euler2d,Weno5,axis>",
+        "roofline": {"bound": "hbm", "kernel": "k_faces_tile<Euler2d,Weno5,axis>",
                      "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved_gbs / hbm_peak, "traffic": None, "peak_source": peak_src,
+                     "frac": achieved_gbs / hbm_peak, "traffic": FACE_TRAFFIC_BYTES_PER_CELL * cells,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_faces_tile "
+                                       "launch at 2048^2 (profiles/), scaled per cell to this launch",
+                     "peak_source": peak_src,
                      "binding_roof": "fp64",
                      "fp64": {"achieved_gops": ops_ach / 1e9, "peak_ginst_per_s": fp64_inst_peak / 1e9,
                               "frac": ops_ach / fp64_inst_peak, "peak_tflops_fma2": fp64_peak / 1e12,

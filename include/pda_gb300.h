@@ -231,6 +231,44 @@ pda_status pda_advance_ssprk3(pda_problem *p, double *d_U, double t0, double dt,
 pda_status pda_advance_rk4(pda_problem *p, double *d_U, double t0, double dt, int64_t n_steps,
                            int use_graph);
 
+/* ----------------------------------------------------------------- batches
+ * (no counterpart in the reference, whose callers loop over problem objects)
+ *
+ * A batch advances many independent problems -- one family and scheme,
+ * uneven mesh sizes, own parameters (e.g. the shallow-water gravity,
+ * Coriolis and pulse of each instance) -- with one launch per residual phase
+ * over all instances.  Instances must be full natural-order meshes whose
+ * boundaries are periodic or mirror images (2D Neumann, slip wall).  The
+ * problems must outlive the batch; their own entry points stay usable.
+ *
+ * Packed layout: instance i owns dofs [offsets[i], offsets[i] + its
+ * totalDofStencilMesh) of one device vector (offsets from
+ * pda_batch_offsets, n+1 values, each instance starting on a 256-byte
+ * boundary); entries between instances are not read by the residual and are
+ * left untouched in V. */
+typedef struct pda_batch pda_batch;
+pda_status pda_batch_create(pda_problem *const *problems, int n, void *stream, pda_batch **out);
+void pda_batch_free(pda_batch *b);
+pda_status pda_batch_sizes(const pda_batch *b, int *n, int64_t *total_dofs, int64_t *total_cells);
+pda_status pda_batch_offsets(const pda_batch *b, int64_t *offsets);
+/* every instance's initialCondition() at its packed offset (zeros between) */
+pda_status pda_batch_initial_condition(pda_batch *b, double *d_U);
+/* every instance's velocity; bit-identical to pda_velocity on each problem */
+pda_status pda_batch_velocity(pda_batch *b, const double *d_U, double t, double *d_V);
+/* n_steps SSP-RK3 steps of size dt for all instances (the single-problem
+ * stage formulas); use_graph != 0 replays one captured step */
+pda_status pda_batch_advance_ssprk3(pda_batch *b, double *d_U, double t0, double dt, int64_t n_steps,
+                                    int use_graph);
+/* Tile shapes of the face kernels (threads along the face axis x lines per
+ * block).  The autotuner times every compiled shape per axis on d_U (reps
+ * launches each) and keeps the fastest; ms (may be NULL) receives the mean
+ * times [axis][shape]. */
+int pda_batch_num_tile_shapes(const pda_batch *b);
+pda_status pda_batch_set_tile_shape(pda_batch *b, int axis, int shape);
+pda_status pda_batch_tile_shape(const pda_batch *b, int axis, int *shape, int *lanes, int *lines);
+pda_status pda_batch_autotune(pda_batch *b, const double *d_U, int reps, double *ms);
+int64_t pda_batch_launch_count(const pda_batch *b);
+
 /* --------------------------------------------------------- diagnostics
  * (no counterpart in the reference: measurement support for benchmarks) */
 

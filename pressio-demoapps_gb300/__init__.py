@@ -117,6 +117,21 @@ _SIGS = {
     "pda_profile_velocity": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                        C.POINTER(C.c_double)]),
     "pda_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
+    "pda_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "pda_batch_free": (None, [C.c_void_p]),
+    "pda_batch_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int64),
+                                  C.POINTER(C.c_int64)]),
+    "pda_batch_offsets": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "pda_batch_initial_condition": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "pda_batch_velocity": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]),
+    "pda_batch_advance_ssprk3": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64,
+                                           C.c_int]),
+    "pda_batch_num_tile_shapes": (C.c_int, [C.c_void_p]),
+    "pda_batch_set_tile_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "pda_batch_tile_shape": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                       C.POINTER(C.c_int)]),
+    "pda_batch_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "pda_batch_launch_count": (C.c_int64, [C.c_void_p]),
 }
 
 
@@ -517,3 +532,81 @@ def create_slip_wall_swe_2d_problem(mesh, scheme, gravity, coriolis, pulse_magni
     _check(lib().pda_problem_create_swe_slip_wall(mesh._h, int(scheme), float(gravity), float(coriolis),
                                                   float(pulse_magnitude), s, C.byref(h)))
     return Problem(mesh, 3, h, s)
+
+
+class ProblemBatch:
+    """Many independent problems (one family and scheme, uneven meshes and
+    parameters) advanced together: one launch per residual phase over all
+    instances.  No counterpart in the reference, whose callers loop over
+    problem objects.  The state is one packed device vector; instance i owns
+    ``U[offsets[i] : offsets[i] + problems[i].totalDofStencilMesh()]``."""
+
+    def __init__(self, problems, stream=None):
+        self._problems = list(problems)  # the problems must outlive the batch
+        n = len(self._problems)
+        arr = (C.c_void_p * max(1, n))(*[p._h.value for p in self._problems])
+        h = C.c_void_p()
+        self._stream = _stream_handle(stream)
+        _check(lib().pda_batch_create(arr, n, self._stream, C.byref(h)))
+        self._h = h
+        nn, td, tc = C.c_int(), C.c_int64(), C.c_int64()
+        _check(lib().pda_batch_sizes(self._h, C.byref(nn), C.byref(td), C.byref(tc)))
+        self.size, self.totalDofs, self.totalCells = nn.value, td.value, tc.value
+        off = (C.c_int64 * (n + 1))()
+        _check(lib().pda_batch_offsets(self._h, off))
+        self.offsets = [int(x) for x in off]
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.pda_batch_free(self._h)
+            self._h = None
+
+    def createState(self):
+        import torch
+        return torch.zeros(self.totalDofs, dtype=torch.float64, device="cuda")
+
+    def initialCondition(self):
+        u = self.createState()
+        _check(lib().pda_batch_initial_condition(self._h, _ptr(u)))
+        return u
+
+    def instance(self, U, i):
+        """View of instance i inside a packed vector."""
+        return U[self.offsets[i]: self.offsets[i] + self._problems[i].totalDofStencilMesh()]
+
+    def velocity(self, U, t, V):
+        Problem._check_vec(U, self.totalDofs, "state")
+        Problem._check_vec(V, self.totalDofs, "velocity")
+        _check(lib().pda_batch_velocity(self._h, _ptr(U), float(t), _ptr(V)))
+
+    def advance_ssprk3(self, U, t0, dt, n_steps, use_graph=True):
+        Problem._check_vec(U, self.totalDofs, "state")
+        _check(lib().pda_batch_advance_ssprk3(self._h, _ptr(U), float(t0), float(dt), int(n_steps),
+                                              int(bool(use_graph))))
+
+    def num_tile_shapes(self):
+        return lib().pda_batch_num_tile_shapes(self._h)
+
+    def set_tile_shape(self, axis, shape):
+        _check(lib().pda_batch_set_tile_shape(self._h, int(axis), int(shape)))
+
+    def tile_shape(self, axis):
+        s, la, li = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().pda_batch_tile_shape(self._h, int(axis), C.byref(s), C.byref(la), C.byref(li)))
+        return s.value, la.value, li.value
+
+    def autotune(self, U, reps=3):
+        """Time every compiled tile shape per axis on U and keep the fastest;
+        returns the mean times [axis][shape] in ms."""
+        import numpy as np
+        ns = self.num_tile_shapes()
+        ms = np.zeros(3 * ns)
+        _check(lib().pda_batch_autotune(self._h, _ptr(U), int(reps), ms.ctypes.data_as(C.c_void_p)))
+        return ms.reshape(3, ns)
+
+    def launch_count(self):
+        return int(lib().pda_batch_launch_count(self._h))
+
+
+def create_batch(problems, stream=None) -> ProblemBatch:
+    return ProblemBatch(problems, stream)

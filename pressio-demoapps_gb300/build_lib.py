@@ -33,6 +33,7 @@ SOURCES = [
     "noalloc.cu",
     "mesh.cpp",
     "problem.cpp",
+    "batch.cpp",
 ]
 
 

@@ -1,0 +1,80 @@
+// Batched structured velocity: many independent problem instances (uneven
+// mesh sizes, own parameters) in one launch per phase.
+//
+// Work is cut into tiles (the single-problem tile of tiles.cuh: NR lines x
+// TW faces of one instance), numbered instance by instance; per-instance
+// prefix sums of tile counts let each block find its instance by binary
+// search.  The kernels are persistent: a grid of (resident blocks per SM x
+// SMs) loops over all tiles of all instances, so small instances no longer
+// leave most of the GPU idle and one launch replaces one per instance.  Each
+// tile runs exactly the single-problem code, so every instance's residual is
+// bit-identical to evaluating that problem alone.
+#pragma once
+
+#include "kernels.cuh"
+#include "tiles.cuh"
+
+namespace pda {
+
+// Largest i in [0, n) with start[i] <= t (start[0] = 0 <= t < start[n]);
+// skips instances that own no tiles.
+__device__ __forceinline__ int batch_find(const long *__restrict__ start, int n, long t) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(start + mid) <= t) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <int FAM, int SCHEME, int AXIS, int NR, int LANES>
+__global__ void __launch_bounds__(LANES *NR)
+k_batch_faces_tile(BatchArgs a, const double *__restrict__ U, double *__restrict__ F) {
+  __shared__ FaceTileSmem<FAM, SCHEME, NR, LANES> sm;
+  const long total = a.totalTiles[AXIS];
+  for (long t = blockIdx.x; t < total; t += gridDim.x) {
+    const int it = batch_find(a.tileStart[AXIS], a.nItems, t);
+    const BatchItem &bi = a.items[it];
+    const Box b = bi.b;
+    const Phys p = bi.p;
+    const long local = t - a.tileStart[AXIS][it];
+    const long g = bi.groups[AXIS];
+    face_tile<FAM, SCHEME, AXIS, NR, LANES>(sm, b, p, U + bi.uOff, F + bi.fOff[AXIS], local % g,
+                                            (int)(local / g));
+    __syncthreads();  // the next tile reuses the shared buffers
+  }
+}
+
+// first order: one face per thread, kFoFacesPerTile faces per tile
+template <int FAM, int AXIS>
+__global__ void __launch_bounds__(kFoFacesPerTile)
+k_batch_faces_fo(BatchArgs a, const double *__restrict__ U, double *__restrict__ F) {
+  const long total = a.totalTiles[AXIS];
+  for (long t = blockIdx.x; t < total; t += gridDim.x) {
+    const int it = batch_find(a.tileStart[AXIS], a.nItems, t);
+    const BatchItem &bi = a.items[it];
+    const Box b = bi.b;
+    const Phys p = bi.p;
+    const long face = (t - a.tileStart[AXIS][it]) * kFoFacesPerTile + threadIdx.x;
+    struct_face<FAM, FirstOrder, AXIS>(b, p, U + bi.uOff, F + bi.fOff[AXIS], face);
+  }
+}
+
+template <int FAM>
+__global__ void __launch_bounds__(kBalanceBlock)
+k_batch_balance(BatchArgs a, const double *__restrict__ U, const double *__restrict__ F,
+                double *__restrict__ V) {
+  for (long blk = blockIdx.x; blk < a.totalBlocks; blk += gridDim.x) {
+    const int it = batch_find(a.blockStart, a.nItems, blk);
+    const BatchItem &bi = a.items[it];
+    const Box b = bi.b;
+    const MeshArgs m = bi.m;
+    const Phys p = bi.p;
+    const long cell = (blk - a.blockStart[it]) * kBalanceBlock + threadIdx.x;
+    balance_cell<FAM>(b, m, p, U + bi.uOff, F + bi.fOff[0], F + bi.fOff[1], F + bi.fOff[2], V + bi.uOff,
+                      cell);
+  }
+}
+
+}  // namespace pda

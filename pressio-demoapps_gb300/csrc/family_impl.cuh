@@ -4,6 +4,8 @@
 
 #include "kernels.cuh"
 #include "tiles.cuh"
+#include "batch.cuh"
+#include "jfaces.cuh"
 #include "launch.hpp"
 
 namespace pda {
@@ -99,6 +101,109 @@ void rows_vj_nearbd(int scheme, const RowTable &t, const MeshArgs &m, const Phys
     case Weno3: k_rows_vj_nearbd<FAM, Weno3><<<g, 64, 0, s>>>(t, m, p, U, rowptr, V, J); break;
     default: k_rows_vj_nearbd<FAM, Weno5><<<g, 64, 0, s>>>(t, m, p, U, rowptr, V, J); break;
   }
+}
+
+
+// ------------------------------------------------------------------ batches
+// persistent grid: resident blocks per SM x SMs (cached per kernel; one GPU
+// model per process), never more blocks than tiles
+template <class K>
+long persistent_grid(K kernel, int threads, long work) {
+  static long grid = 0;
+  if (grid == 0) {
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, 0);
+    grid = (long)(occ > 0 ? occ : 1) * (sms > 0 ? sms : 1);
+  }
+  return work < grid ? work : grid;
+}
+
+template <int SCHEME, int AXIS, int NR, int LANES>
+void batch_tile_launch(const BatchArgs &a, const double *U, double *Fo, cudaStream_t s) {
+  auto k = k_batch_faces_tile<FAM, SCHEME, AXIS, NR, LANES>;
+  const long g = persistent_grid(k, LANES * NR, a.totalTiles[AXIS]);
+  if (g > 0) k<<<(unsigned)g, dim3(LANES, NR), 0, s>>>(a, U, Fo);
+}
+
+template <int SCHEME, int AXIS>
+void batch_faces_axis(int shape, const BatchArgs &a, const double *U, double *Fo, cudaStream_t s) {
+  if constexpr (SCHEME == FirstOrder) {
+    auto k = k_batch_faces_fo<FAM, AXIS>;
+    const long g = persistent_grid(k, kFoFacesPerTile, a.totalTiles[AXIS]);
+    if (g > 0) k<<<(unsigned)g, kFoFacesPerTile, 0, s>>>(a, U, Fo);
+  } else {
+    static_assert(kTileShapes[0].lanes == 64 && kTileShapes[0].nr == 2, "shape table");
+    if (shape == 0 || F::dim != 2) {
+      batch_tile_launch<SCHEME, AXIS, 2, 64>(a, U, Fo, s);
+    } else {
+      if constexpr (F::dim == 2) {
+        static_assert(kTileShapes[1].lanes == 32 && kTileShapes[1].nr == 4, "shape table");
+        static_assert(kTileShapes[2].lanes == 128 && kTileShapes[2].nr == 1, "shape table");
+        static_assert(kTileShapes[3].lanes == 64 && kTileShapes[3].nr == 1, "shape table");
+        if (shape == 1) batch_tile_launch<SCHEME, AXIS, 4, 32>(a, U, Fo, s);
+        else if (shape == 2) batch_tile_launch<SCHEME, AXIS, 1, 128>(a, U, Fo, s);
+        else batch_tile_launch<SCHEME, AXIS, 1, 64>(a, U, Fo, s);
+      }
+    }
+  }
+}
+
+template <int SCHEME>
+void batch_faces_s(int axis, int shape, const BatchArgs &a, const double *U, double *Fo, cudaStream_t s) {
+  if (axis == 0) batch_faces_axis<SCHEME, 0>(shape, a, U, Fo, s);
+  if constexpr (F::dim > 1)
+    if (axis == 1) batch_faces_axis<SCHEME, 1>(shape, a, U, Fo, s);
+  if constexpr (F::dim > 2)
+    if (axis == 2) batch_faces_axis<SCHEME, 2>(shape, a, U, Fo, s);
+}
+
+void batch_faces(int scheme, int axis, int shape, const BatchArgs &a, const double *U, double *Fo,
+                 cudaStream_t s) {
+  switch (scheme) {
+    case FirstOrder: batch_faces_s<FirstOrder>(axis, shape, a, U, Fo, s); break;
+    case Weno3: batch_faces_s<Weno3>(axis, shape, a, U, Fo, s); break;
+    default: batch_faces_s<Weno5>(axis, shape, a, U, Fo, s); break;
+  }
+}
+
+void batch_balance(const BatchArgs &a, const double *U, const double *Fo, double *V, cudaStream_t s) {
+  auto k = k_batch_balance<FAM>;
+  const long g = persistent_grid(k, kBalanceBlock, a.totalBlocks);
+  if (g > 0) k<<<(unsigned)g, kBalanceBlock, 0, s>>>(a, U, Fo, V);
+}
+
+int batch_num_shapes() { return F::dim == 2 ? kNumTileShapes : 1; }
+
+
+// ----------------------------------------------------- Jacobian, faces once
+template <int SCHEME>
+void struct_vj_s(const Box &b, const MeshArgs &m, const Phys &p, const double *U, double *const T[3],
+                 const int *rowptr, double *V, double *J, cudaStream_t s, int *launches) {
+  long nc = 1;
+  for (int a = 0; a < 3; ++a) nc *= (long)(b.hi[a] - b.lo[a]);
+  if (nc <= 0) return;
+  auto nfaces = [&](int ax) {
+    long nf = 1;
+    for (int a = 0; a < 3; ++a) nf *= (long)(b.hi[a] - b.lo[a] + (a == ax ? 1 : 0));
+    return nf;
+  };
+  k_jfaces<FAM, SCHEME, 0><<<div_up(nfaces(0), 128), 128, 0, s>>>(b, p, m.hinv[0], U, T[0]);
+  if constexpr (F::dim > 1) k_jfaces<FAM, SCHEME, 1><<<div_up(nfaces(1), 128), 128, 0, s>>>(b, p, m.hinv[1], U, T[1]);
+  if constexpr (F::dim > 2) k_jfaces<FAM, SCHEME, 2><<<div_up(nfaces(2), 128), 128, 0, s>>>(b, p, m.hinv[2], U, T[2]);
+  k_jassemble<FAM, SCHEME><<<div_up(nc, 128), 128, 0, s>>>(b, m, p, U, T[0], T[1], T[2], rowptr, V, J);
+  *launches += F::dim + 1;
+}
+
+void struct_vj(int scheme, const Box &b, const MeshArgs &m, const Phys &p, const double *U, double *const T[3],
+               const int *rowptr, double *V, double *J, cudaStream_t s, int *launches) {
+  if (scheme == Weno3) struct_vj_s<Weno3>(b, m, p, U, T, rowptr, V, J, s, launches);
+  else if (scheme == Weno5) struct_vj_s<Weno5>(b, m, p, U, T, rowptr, V, J, s, launches);
+}
+
+int jface_components(int scheme) {
+  return scheme == Weno3 ? JFaceLayout<FAM, Weno3>::NCOMP : (scheme == Weno5 ? JFaceLayout<FAM, Weno5>::NCOMP : 0);
 }
 
 }  // namespace

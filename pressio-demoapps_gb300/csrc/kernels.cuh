@@ -200,14 +200,13 @@ __device__ __forceinline__ int map_cell(int c, int n, int mode, bool &mirrored) 
 // cells f-1 and f.  Output Fx laid out [outer][mid][f - lo] with the face
 // axis fastest.
 template <int FAM, int SCHEME, int AXIS>
-__global__ void __launch_bounds__(128)
-k_struct_faces(Box b, Phys p, const double *__restrict__ U, double *__restrict__ Fout) {
+__device__ __forceinline__ void struct_face(const Box &b, const Phys &p, const double *__restrict__ U,
+                                            double *__restrict__ Fout, long t) {
   using F = Fam<FAM>;
   constexpr int NDPC = F::ndpc, H = SchemeTraits<SCHEME>::h;
   const int nf[3] = {b.hi[0] - b.lo[0] + (AXIS == 0), b.hi[1] - b.lo[1] + (AXIS == 1),
                      b.hi[2] - b.lo[2] + (AXIS == 2)};
   const long total = (long)nf[0] * nf[1] * nf[2];
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= total) return;
   int id[3];
   id[0] = (int)(t % nf[0]);
@@ -234,18 +233,23 @@ k_struct_faces(Box b, Phys p, const double *__restrict__ U, double *__restrict__
   for (int d = 0; d < NDPC; ++d) Fout[t * NDPC + d] = f[d];
 }
 
+template <int FAM, int SCHEME, int AXIS>
+__global__ void __launch_bounds__(128)
+k_struct_faces(Box b, Phys p, const double *__restrict__ U, double *__restrict__ Fout) {
+  struct_face<FAM, SCHEME, AXIS>(b, p, U, Fout, (long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // V for every box cell from the face fluxes, in the reference's axis order
 // (x, then y, then z, then the shallow-water Coriolis source).
 template <int FAM>
-__global__ void __launch_bounds__(256)
-k_struct_balance(Box b, MeshArgs m, Phys p, const double *__restrict__ U,
-                 const double *__restrict__ Fx, const double *__restrict__ Fy,
-                 const double *__restrict__ Fz, double *__restrict__ V) {
+__device__ __forceinline__ void balance_cell(const Box &b, const MeshArgs &m, const Phys &p,
+                                             const double *__restrict__ U, const double *__restrict__ Fx,
+                                             const double *__restrict__ Fy, const double *__restrict__ Fz,
+                                             double *__restrict__ V, long t) {
   using F = Fam<FAM>;
   constexpr int NDPC = F::ndpc, DIM = F::dim;
   const int nb[3] = {b.hi[0] - b.lo[0], b.hi[1] - b.lo[1], b.hi[2] - b.lo[2]};
   const long total = (long)nb[0] * nb[1] * nb[2];
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= total) return;
   const int i = (int)(t % nb[0]);
   const int j = (int)((t / nb[0]) % nb[1]);
@@ -278,6 +282,14 @@ k_struct_balance(Box b, MeshArgs m, Phys p, const double *__restrict__ U,
   }
 #pragma unroll
   for (int d = 0; d < NDPC; ++d) V[cell * NDPC + d] = v[d];
+}
+
+template <int FAM>
+__global__ void __launch_bounds__(256)
+k_struct_balance(Box b, MeshArgs m, Phys p, const double *__restrict__ U,
+                 const double *__restrict__ Fx, const double *__restrict__ Fy,
+                 const double *__restrict__ Fz, double *__restrict__ V) {
+  balance_cell<FAM>(b, m, p, U, Fx, Fy, Fz, V, (long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------

@@ -5,7 +5,10 @@
 namespace pda {
 const Launchers &launchers_swe2d() {
   static const Launchers L = {fam_impl::rows_velocity, fam_impl::struct_velocity,
-                              fam_impl::rows_vj_inner, fam_impl::rows_vj_nearbd};
+                              fam_impl::rows_vj_inner, fam_impl::rows_vj_nearbd,
+                              fam_impl::batch_faces, fam_impl::batch_balance,
+                              fam_impl::batch_num_shapes, fam_impl::struct_vj,
+                              fam_impl::jface_components};
   return L;
 }
 }  // namespace pda

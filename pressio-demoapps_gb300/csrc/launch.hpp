@@ -22,6 +22,18 @@ struct Launchers {
                         const double *U, const int *rowptr, double *V, double *J, cudaStream_t s);
   void (*rows_vj_nearbd)(int scheme, const RowTable &t, const MeshArgs &m, const Phys &p,
                          const double *U, const int *rowptr, double *V, double *J, cudaStream_t s);
+  // batches: faces normal to one axis of every instance with tile shape
+  // `shape` (index into kTileShapes), then the balance of every instance
+  void (*batch_faces)(int scheme, int axis, int shape, const BatchArgs &a, const double *U, double *F,
+                      cudaStream_t s);
+  void (*batch_balance)(const BatchArgs &a, const double *U, const double *F, double *V, cudaStream_t s);
+  int (*batch_num_shapes)();  // tile shapes compiled for this family
+  // V + J of the inner box with faces computed once (WENO3 / WENO5):
+  // T[axis] holds jface_components(scheme) doubles per face of that axis
+  void (*struct_vj)(int scheme, const Box &b, const MeshArgs &m, const Phys &p, const double *U,
+                    double *const T[3], const int *rowptr, double *V, double *J, cudaStream_t s,
+                    int *launches);
+  int (*jface_components)(int scheme);
 };
 
 const Launchers &launchers_euler1d();

@@ -1,0 +1,162 @@
+// Host-side state of a device problem (pda_problem) and the small device
+// buffer / row-table helpers it is built from; shared by problem.cpp and
+// batch.cpp.  Nothing here crosses the C ABI.
+#pragma once
+
+#include <cstdint>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "internal.hpp"
+#include "launch.hpp"
+
+namespace pda {
+
+#define PDA_CUDA(x)                                                                           \
+  do {                                                                                        \
+    cudaError_t e_ = (x);                                                                     \
+    if (e_ != cudaSuccess)                                                                    \
+      throw ::pda::Error(PDA_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));      \
+  } while (0)
+
+template <class T> struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    if (count <= n && p) return;
+    release();
+    if (count == 0) return;
+    cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      throw Error(e == cudaErrorMemoryAllocation ? PDA_ERR_OUT_OF_MEMORY : PDA_ERR_CUDA,
+                  std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    n = count;
+  }
+  void upload(const std::vector<T> &v) {
+    alloc(v.size());
+    if (!v.empty()) PDA_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  }
+};
+
+// Host copy + device copy of a row table.
+struct Table {
+  std::vector<int> rows, cell, src, jpos, src1, jpos1;
+  std::vector<uint8_t> flip, flip1;
+  std::vector<double> jfac;
+  DevBuf<int> d_rows, d_cell, d_src, d_jpos, d_src1, d_jpos1;
+  DevBuf<uint8_t> d_flip, d_flip1;
+  DevBuf<double> d_jfac;
+  RowTable t{};
+  bool dirty = true;
+  int hostRows() const { return (int)rows.size(); }
+  // copy the host tables to the device if they changed since the last copy
+  void sync() {
+    if (!dirty) return;
+    upload();
+    dirty = false;
+  }
+  void upload() {
+    d_rows.upload(rows);
+    d_cell.upload(cell);
+    d_src.upload(src);
+    d_flip.upload(flip);
+    d_jpos.upload(jpos);
+    d_src1.upload(src1);
+    d_flip1.upload(flip1);
+    d_jpos1.upload(jpos1);
+    d_jfac.upload(jfac);
+    t.nrows = (int)rows.size();
+    t.rows = d_rows.p;
+    t.cell = d_cell.p;
+    t.src = d_src.p;
+    t.flip = d_flip.p;
+    t.jpos = jpos.empty() ? nullptr : d_jpos.p;
+    t.src1 = src1.empty() ? nullptr : d_src1.p;
+    t.flip1 = flip1.empty() ? nullptr : d_flip1.p;
+    t.jpos1 = jpos1.empty() ? nullptr : d_jpos1.p;
+    t.jfac = jfac.empty() ? nullptr : d_jfac.p;
+  }
+};
+
+enum BcKind { BC_NONE = 0, BC_MIRROR2D = 1, BC_NEUMANN1D = 2 };
+
+}  // namespace pda
+
+struct pda_mesh {
+  pda::Mesh m;
+};
+
+struct pda_problem {
+  const pda::Mesh *mesh = nullptr;
+  int family = 0, probEnum = 0, scheme = 0, icFlag = 1;
+  std::vector<double> icParams, physParams;
+  pda::Phys phys{};
+  pda::MeshArgs margs{};
+  cudaStream_t stream = nullptr;
+  int ndpc = 0, dim = 0, h = 0;
+  int64_t dofsSample = 0, dofsStencil = 0;
+  int bc = pda::BC_NONE;
+  const pda::Launchers *L = nullptr;
+  // velocity
+  bool useStruct = false;
+  bool structAll = false;  // the structured box covers every cell (mirror boundaries)
+  pda::Box box{};
+  pda::DevBuf<double> F[3];
+  // Jacobian, faces once on the inner box (jfaces.cuh)
+  bool jStruct = false;
+  pda::Box jbox{};
+  pda::DevBuf<double> JT[3];
+  pda::Table nearT;   // near-boundary rows: V stencil (+ J first-order tables)
+  pda::Table innerT;  // inner rows (sample meshes for V; every mesh for V+J)
+  bool innerBuiltV = false, innerBuiltJ = false, nearBuiltJ = false;
+  // Jacobian
+  bool patternBuilt = false;
+  std::vector<int> rowptr, colidx;
+  std::vector<std::vector<int32_t>> rowBlocks;  // sorted unique cell ids per graph row
+  pda::DevBuf<int> d_rowptr, d_colidx;
+  pda::DevBuf<double> d_Jscratch, d_Vscratch;
+  // host-buffer entry points and steppers
+  pda::DevBuf<double> d_U, d_V, d_J;
+  pda::DevBuf<double> aux, r[4];
+  cudaGraphExec_t stepGraph = nullptr;
+  int stepGraphKind = -1;
+  double stepGraphDt = 0;
+  double *stepGraphU = nullptr;
+  int64_t stepGraphLaunches = 0;
+  int64_t launches = 0;
+  ~pda_problem() {
+    if (stepGraph) cudaGraphExecDestroy(stepGraph);
+  }
+};
+
+// C ABI bodies: exceptions become a status code + the thread-local message
+#define PDA_API_BEGIN try {
+#define PDA_API_END                                   \
+  return PDA_OK;                                      \
+  }                                                   \
+  catch (const pda::Error &e) {                       \
+    pda::set_last_error(e.what());                    \
+    return e.code;                                    \
+  }                                                   \
+  catch (const std::bad_alloc &) {                    \
+    pda::set_last_error("host out of memory");        \
+    return PDA_ERR_OUT_OF_MEMORY;                     \
+  }                                                   \
+  catch (const std::exception &e) {                   \
+    pda::set_last_error(e.what());                    \
+    return PDA_ERR_INTERNAL;                          \
+  }

@@ -24,32 +24,43 @@
 
 namespace pda {
 
-template <int SCHEME> struct TileCfg;
-template <> struct TileCfg<Weno5> {
-  static constexpr int H = 3, LANES = 64, TW = LANES - 3, NCELL = TW + 5, NA = 5;
+template <int SCHEME, int LANES_ = 64> struct TileCfg;
+template <int LANES_> struct TileCfg<Weno5, LANES_> {
+  static constexpr int H = 3, LANES = LANES_, TW = LANES - 3, NCELL = TW + 5, NA = 5;
 };
-template <> struct TileCfg<Weno3> {
-  static constexpr int H = 2, LANES = 64, TW = LANES - 2, NCELL = TW + 3, NA = 2;
+template <int LANES_> struct TileCfg<Weno3, LANES_> {
+  static constexpr int H = 2, LANES = LANES_, TW = LANES - 2, NCELL = TW + 3, NA = 2;
 };
 
-template <int FAM, int SCHEME, int AXIS, int NR>
-__global__ void __launch_bounds__(TileCfg<SCHEME>::LANES *NR)
-k_faces_tile(Box b, Phys p, const double *__restrict__ U, double *__restrict__ Fout) {
+// shared memory of one tile: the cells of NR lines and their alpha terms
+template <int FAM, int SCHEME, int NR, int LANES> struct FaceTileSmem {
+  using C = TileCfg<SCHEME, LANES>;
+  double sU[NR][Fam<FAM>::ndpc][C::NCELL + 1];
+  double sA[NR][Fam<FAM>::ndpc][C::NA][LANES];
+};
+
+// One tile: lines lineGroup*NR .. +NR-1 of the box (the lines run along AXIS,
+// numbered with the first other axis fastest), faces chunk*TW .. +TW-1 of
+// each line.  Called by every thread of a LANES x NR block.
+template <int FAM, int SCHEME, int AXIS, int NR, int LANES>
+__device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &sm, const Box &b, const Phys &p,
+                                          const double *__restrict__ U, double *__restrict__ Fout,
+                                          long lineGroup, int chunk) {
   using F = Fam<FAM>;
-  using C = TileCfg<SCHEME>;
-  constexpr int NDPC = F::ndpc, LANES = C::LANES, TW = C::TW, NCELL = C::NCELL, H = C::H, NA = C::NA;
+  using C = TileCfg<SCHEME, LANES>;
+  constexpr int NDPC = F::ndpc, TW = C::TW, NCELL = C::NCELL, H = C::H;
   constexpr int A1 = AXIS == 0 ? 1 : 0, A2 = AXIS == 2 ? 1 : 2;  // the two other axes
-  __shared__ double sU[NR][NDPC][NCELL + 1];
-  __shared__ double sA[NR][NDPC][NA][LANES];
+  auto &sU = sm.sU;
+  auto &sA = sm.sA;
 
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int nb1 = b.hi[A1] - b.lo[A1], nb2 = b.hi[A2] - b.lo[A2];
   const int nf = b.hi[AXIS] - b.lo[AXIS] + 1;
-  const long line = (long)blockIdx.x * NR + ty;
+  const long line = lineGroup * NR + ty;
   const bool lineOk = line < (long)nb1 * nb2;
   const int c1 = lineOk ? b.lo[A1] + (int)(line % nb1) : b.lo[A1];
   const int c2 = lineOk ? b.lo[A2] + (int)(line / nb1) : b.lo[A2];
-  const int f0 = b.lo[AXIS] + blockIdx.y * TW;  // first face of the tile
+  const int f0 = b.lo[AXIS] + chunk * TW;  // first face of the tile
   long stride[3];
   stride[0] = 1;
   stride[1] = b.n[0];
@@ -175,6 +186,14 @@ k_faces_tile(Box b, Phys p, const double *__restrict__ U, double *__restrict__ F
   else o = i1 + (long)nb1 * (i2 + (long)nb2 * fi);
 #pragma unroll
   for (int d = 0; d < NDPC; ++d) Fout[o * NDPC + d] = fl[d];
+}
+
+// grid: x = line groups of NR lines, y = face chunks of TW faces
+template <int FAM, int SCHEME, int AXIS, int NR, int LANES = 64>
+__global__ void __launch_bounds__(LANES *NR)
+k_faces_tile(Box b, Phys p, const double *__restrict__ U, double *__restrict__ Fout) {
+  __shared__ FaceTileSmem<FAM, SCHEME, NR, LANES> sm;
+  face_tile<FAM, SCHEME, AXIS, NR, LANES>(sm, b, p, U, Fout, (long)blockIdx.x, (int)blockIdx.y);
 }
 
 }  // namespace pda

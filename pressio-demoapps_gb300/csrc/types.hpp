@@ -48,4 +48,37 @@ struct Box {
   int reflect[3];
 };
 
+// ---------------------------------------------------------------------------
+// Batches of independent problems of one family and scheme on structured
+// full meshes (uneven sizes and parameters), evaluated by one launch per
+// phase over all instances.
+// ---------------------------------------------------------------------------
+struct BatchItem {
+  Box b;
+  MeshArgs m;
+  Phys p;
+  long uOff;       // first dof of the instance in the packed state / residual
+  long fOff[3];    // first double of the instance's faces normal to each axis
+  long groups[3];  // tile line groups per axis for the current tile shape
+};
+
+// Tile shapes the batch autotuner chooses from: LANES threads along the face
+// axis x NR lines per block.  Shape 0 is the single-problem default.
+struct TileShape {
+  int lanes, nr;
+};
+constexpr int kNumTileShapes = 4;
+constexpr TileShape kTileShapes[kNumTileShapes] = {{64, 2}, {32, 4}, {128, 1}, {64, 1}};
+constexpr int kFoFacesPerTile = 128;  // first order: faces per tile (one per thread)
+
+struct BatchArgs {
+  const BatchItem *items;     // device array [nItems]
+  int nItems;
+  const long *tileStart[3];   // device prefix sums [nItems + 1] of tiles per axis
+  const long *blockStart;     // device prefix sums [nItems + 1] of balance blocks
+  long totalTiles[3];
+  long totalBlocks;
+};
+constexpr int kBalanceBlock = 256;
+
 }  // namespace pda

@@ -9,7 +9,8 @@ path is pinned two ways:
   the oracle -- bit-identical to the reference -- bit for bit, for all three
   axis pairs;
 * finite differences: on the fully periodic mesh J.a ~ (V(U + eps a) - V(U))/eps
-  (eps 1e-8), as tests_cpp/eigen_3d_euler_jacobian_fd_xyz_periodic does.
+  (eps 1e-8), as tests_cpp/eigen_3d_euler_jacobian_fd_xyz_periodic does, and
+  central differences at the 96^3 size.
 
 CPU tests pin the oracle; GPU tests compare the library against it."""
 from __future__ import annotations
@@ -145,12 +146,15 @@ def test_gpu_3d_matches_oracle(oracle, pda, tmp_path, scheme):
 def test_gpu_3d_weno5_jacobian_finite_differences_96(pda):
     """Config size for the 3D Jacobian (96^3, WENO5, periodic): FD agreement.
 
-    The Rusanov flux takes max(|uL|+cL, |uR|+cR), which has a kink; among the
-    2.6M faces a random direction of length 1e-8 crosses it at a few, where
-    the one-sided difference legitimately differs from J.a by up to
-    |d lambda| |uR - uL| / dx.  So the bound is per row: all but a handful of
-    the 4.4M rows agree to 1e-6 of the scale, and none is off by more than 1e-3
-    (an error in J itself shows up in a whole class of rows, not a handful)."""
+    Central differences with eps = 1e-7: the one-sided difference with 1e-8
+    used on small meshes carries a truncation error that grows with the mesh
+    (measured with the oracle: 1.4e-6 of the scale at 24^3, 6e-6 at 48^3,
+    1.3e-5 at 96^3), while the central one stays near 1e-8.  The Rusanov flux
+    takes max(|uL|+cL, |uR|+cR), which has a kink; a random direction may
+    cross it at a few of the 2.6M faces, where the difference legitimately
+    departs from J.a.  So: all but a handful of the 4.4M rows agree to 1e-6
+    of the scale, and none is off by more than 1e-3 (an error in J itself
+    shows up in a whole class of rows, not a handful)."""
     import torch
     n = 96
     m3 = pda.create_full_mesh((n, n, n), (-1, 1, -1, 1, -1, 1), 7, (True, True, True))
@@ -161,12 +165,12 @@ def test_gpu_3d_weno5_jacobian_finite_differences_96(pda):
     p.rightHandSideAndJacobian(U, 0.0, V, J)
     gen = torch.Generator(device="cuda").manual_seed(1)
     a = torch.rand(U.shape, generator=gen, device="cuda", dtype=torch.float64) * 2 - 1
-    eps = 1e-8
-    V1 = p.createVelocity()
-    p.velocity(U + eps * a, 0.0, V1)
-    V0 = p.createVelocity()
-    p.velocity(U, 0.0, V0)
-    fd = (V1 - V0) / eps
+    eps = 1e-7
+    Vp = p.createVelocity()
+    p.velocity(U + eps * a, 0.0, Vp)
+    Vm = p.createVelocity()
+    p.velocity(U - eps * a, 0.0, Vm)
+    fd = (Vp - Vm) / (2 * eps)
     R = torch.empty_like(V)
     p.applyJacobian(U, a, 0.0, R)
     scale = max(1.0, R.abs().max().item())
