@@ -217,22 +217,29 @@ def _cpu_rate(fn, budget_s):
     return statistics.median(ts), len(ts)
 
 
-def extra_workloads(pda, torch, stream, cpu=True):
-    """Secondary configurations (one line each): Jacobian nnz/s at 1024^2, 3D
-    WENO5 velocity at 256^3, 3D WENO5 Jacobian at 96^3, 1D Sod SSP-RK3 2000 steps."""
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import oracle_py
-    orc = oracle_py.load() if cpu else None
-    threads = orc.set_threads(os.cpu_count() or 1) if cpu else 0
-    out = {}
-    rng = np.random.default_rng(20261203)
+class _Ctx:
+    """What every secondary workload needs: the package, torch, the stream,
+    the oracle (None without CPU baselines) and its thread count."""
 
-    def oracle_problem(mesh, fam, prob, scheme, ic, dim, st):
+    def __init__(self, pda, torch, stream, cpu):
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import oracle_py
+        self.pda, self.torch, self.stream = pda, torch, stream
+        self.orc = oracle_py.load() if cpu else None
+        self.threads = self.orc.set_threads(os.cpu_count() or 1) if cpu else 0
+        self.rng = np.random.default_rng(20261203)
+
+    def oracle_problem(self, mesh, fam, prob, scheme, ic, dim, st):
         g, x, y, z, _, _ = mesh._arrays()
-        om = orc.mesh_from_arrays(dim, st, g, x, y, z, (mesh.dx(), mesh.dy(), mesh.dz()))
-        return om, orc.problem(om, fam, prob, scheme, ic)
+        om = self.orc.mesh_from_arrays(dim, st, g, x, y, z, (mesh.dx(), mesh.dy(), mesh.dz()))
+        return om, self.orc.problem(om, fam, prob, scheme, ic)
 
-    # -- 2D Euler Riemann WENO5 Jacobian (V + CSR J), 1024^2
+
+def wl_jacobian_2d(c):
+    """2D Euler Riemann WENO5 Jacobian (V + CSR J), 1024^2"""
+    pda, torch, stream, orc, threads, rng = c.pda, c.torch, c.stream, c.orc, c.threads, c.rng
+    cpu = orc is not None
+    oracle_problem = c.oracle_problem
     n = 1024
     mesh = pda.create_full_mesh((n, n), (0.0, 1.0, 0.0, 1.0), 7)
     prob = pda.create_problem(mesh, pda.Euler2d.Riemann, pda.InviscidFluxReconstruction.Weno5, 2, stream=stream)
@@ -257,9 +264,14 @@ def extra_workloads(pda, torch, stream, cpu=True):
         med, k = _cpu_rate(lambda: op.velocity_and_jacobian(U2), 5.0)
         w["cpu_baseline"] = {"value": op.nnz / med / 1e9, "unit": "Gnnz/s", "cores": threads, "kind": "port",
                              "sample": f"{k} V+J calls at 256^2 (same problem/scheme), median {med*1e3:.1f} ms"}
-    out["jacobian_2d"] = w
+    return w
 
-    # -- 3D Euler smooth periodic WENO5 velocity, 256^3
+
+def wl_velocity_3d(c):
+    """3D Euler smooth periodic WENO5 velocity, 256^3"""
+    pda, torch, stream, orc, threads, rng = c.pda, c.torch, c.stream, c.orc, c.threads, c.rng
+    cpu = orc is not None
+    oracle_problem = c.oracle_problem
     n = 256
     mesh = pda.create_full_mesh((n, n, n), (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0), 7, (True, True, True))
     prob = pda.create_problem(mesh, pda.Euler3d.PeriodicSmooth, pda.InviscidFluxReconstruction.Weno5, stream=stream)
@@ -280,9 +292,14 @@ def extra_workloads(pda, torch, stream, cpu=True):
         med, k = _cpu_rate(lambda: op.velocity(U3), 5.0)
         w["cpu_baseline"] = {"value": ns ** 3 / med / 1e9, "unit": "Gcell/s", "cores": threads, "kind": "port",
                              "sample": f"{k} velocity calls at 64^3 (same problem/scheme), median {med*1e3:.1f} ms"}
-    out["velocity_3d"] = w
+    return w
 
-    # -- 3D Euler WENO5 Jacobian, 96^3
+
+def wl_jacobian_3d(c):
+    """3D Euler WENO5 Jacobian, 96^3"""
+    pda, torch, stream, orc, threads, rng = c.pda, c.torch, c.stream, c.orc, c.threads, c.rng
+    cpu = orc is not None
+    oracle_problem = c.oracle_problem
     n = 96
     mesh = pda.create_full_mesh((n, n, n), (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0), 7, (True, True, True))
     prob = pda.create_problem(mesh, pda.Euler3d.PeriodicSmooth, pda.InviscidFluxReconstruction.Weno5, stream=stream)
@@ -304,9 +321,14 @@ def extra_workloads(pda, torch, stream, cpu=True):
         med, k = _cpu_rate(lambda: op.velocity_and_jacobian(U3), 5.0)
         w["cpu_baseline"] = {"value": op.nnz / med / 1e9, "unit": "Gnnz/s", "cores": threads, "kind": "port",
                              "sample": f"{k} V+J calls at 24^3 (same problem/scheme), median {med*1e3:.1f} ms"}
-    out["jacobian_3d"] = w
+    return w
 
-    # -- 1D Sod, WENO5, SSP-RK3 dt=1e-4, 2000 steps (CUDA-graph steps)
+
+def wl_sod_1d_ssprk3(c):
+    """1D Sod, WENO5, SSP-RK3 dt=1e-4, 2000 steps (CUDA-graph steps)"""
+    pda, torch, stream, orc, threads, rng = c.pda, c.torch, c.stream, c.orc, c.threads, c.rng
+    cpu = orc is not None
+    oracle_problem = c.oracle_problem
     mesh = pda.create_full_mesh((1000,), (-0.5, 0.5), 7)
     prob = pda.create_problem(mesh, pda.Euler1d.Sod, pda.InviscidFluxReconstruction.Weno5, stream=stream)
     with torch.cuda.stream(stream):
@@ -334,9 +356,14 @@ def extra_workloads(pda, torch, stream, cpu=True):
         w["cpu_baseline"] = {"value": 3 * 2000 * 1000 / cw / 1e9, "unit": "Gcell-updates/s", "cores": 1,
                              "kind": "port", "sample": f"the full 2000-step run, 1 thread, {cw*1e3:.0f} ms"}
         w["final_state_matches_oracle"] = bool(np.allclose(U.cpu().numpy(), Uo, rtol=1e-12, atol=1e-13))
-    out["sod_1d_ssprk3"] = w
+    return w
 
-    # -- 3D Euler smooth periodic WENO5, SSP-RK3 at CFL 0.4, 256^3 (a few of the 200 steps)
+
+def wl_ssprk3_3d(c):
+    """3D Euler smooth periodic WENO5, SSP-RK3 at CFL 0.4, 256^3 (a few of the 200 steps)"""
+    pda, torch, stream, orc, threads, rng = c.pda, c.torch, c.stream, c.orc, c.threads, c.rng
+    cpu = orc is not None
+    oracle_problem = c.oracle_problem
     n = 256
     mesh = pda.create_full_mesh((n, n, n), (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0), 7, (True, True, True))
     prob = pda.create_problem(mesh, pda.Euler3d.PeriodicSmooth, pda.InviscidFluxReconstruction.Weno5, stream=stream)
@@ -360,9 +387,24 @@ def extra_workloads(pda, torch, stream, cpu=True):
         med, k = _cpu_rate(lambda: op.ssprk3(U3, 0.0, dt, 1), 5.0)
         w["cpu_baseline"] = {"value": 3 * ns ** 3 / med / 1e9, "unit": "Gcell-updates/s", "cores": threads,
                              "kind": "port", "sample": f"{k} SSP-RK3 steps at 64^3, median {med*1e3:.1f} ms"}
-    out["ssprk3_3d"] = w
+    return w
 
-    out["batched_swe"] = batched_swe_workload(pda, torch, stream, orc if cpu else None, threads)
+
+def wl_batched_swe(c):
+    return batched_swe_workload(c.pda, c.torch, c.stream, c.orc, c.threads)
+
+
+WORKLOADS = {"jacobian_2d": wl_jacobian_2d, "velocity_3d": wl_velocity_3d, "jacobian_3d": wl_jacobian_3d,
+             "sod_1d_ssprk3": wl_sod_1d_ssprk3, "ssprk3_3d": wl_ssprk3_3d, "batched_swe": wl_batched_swe}
+
+
+def extra_workloads(pda, torch, stream, cpu=True, names=None):
+    """Secondary configurations, one JSON object each (default: all)."""
+    c = _Ctx(pda, torch, stream, cpu)
+    out = {}
+    for name in names or list(WORKLOADS):
+        out[name] = WORKLOADS[name](c)
+        torch.cuda.empty_cache()
     return out
 
 
@@ -447,6 +489,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer measurement (profiling runs)")
     ap.add_argument("--n", type=int, default=1024, help="cells per side (1024 = the benchmark workload)")
     ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
+    ap.add_argument("--workload", action="append", choices=sorted(WORKLOADS),
+                    help="run only this secondary workload (repeatable; for profiling), no headline line")
     args = ap.parse_args()
     global N_CELLS_SIDE
     N_CELLS_SIDE = args.n
@@ -464,6 +508,10 @@ def main():
     ge = importlib.import_module("__graft_entry__")
     pda = ge.package()
     stream = torch.cuda.Stream()
+    if args.workload:
+        print(json.dumps({"workloads": extra_workloads(pda, torch, stream, cpu=not args.no_cpu_baseline,
+                                                       names=args.workload)}))
+        return 0
     mesh, prob, Uh = build_workload(pda, torch, stream)
     cells = N_CELLS_SIDE ** 2
     with torch.cuda.stream(stream):

@@ -269,6 +269,20 @@ pda_status pda_batch_tile_shape(const pda_batch *b, int axis, int *shape, int *l
 pda_status pda_batch_autotune(pda_batch *b, const double *d_U, int reps, double *ms);
 int64_t pda_batch_launch_count(const pda_batch *b);
 
+/* ------------------------------------------------- learned-manifold ROM
+ * (no counterpart in the reference; building blocks of the autoencoder
+ * trained on snapshots of the batched full-order model)
+ *
+ * BF16 tensor-core GEMM on tcgen05 with fp32 accumulation in tensor memory:
+ * C[M x N] = A[M x K] * B[N x K]^T (+ bias[N]; epilogue 0 none, 1 bias,
+ * 2 bias + ELU), A and B row-major bf16 (uint16 storage), K a multiple of 64.
+ * Outputs (any may be NULL, not both of d_outF / d_outB): fp32 and / or bf16
+ * row-major [M x N], d_preact = fp32 value before the activation.
+ * Synchronous on `stream` (cudaStream_t, NULL = legacy default). */
+pda_status pda_tc_gemm_bf16(const void *d_A, const void *d_B, int64_t M, int64_t N, int64_t K,
+                            const float *d_bias, int epilogue, float *d_outF, void *d_outB,
+                            float *d_preact, void *stream);
+
 /* --------------------------------------------------------- diagnostics
  * (no counterpart in the reference: measurement support for benchmarks) */
 

@@ -132,6 +132,8 @@ _SIGS = {
                                        C.POINTER(C.c_int)]),
     "pda_batch_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "pda_batch_launch_count": (C.c_int64, [C.c_void_p]),
+    "pda_tc_gemm_bf16": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_int,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 
@@ -610,3 +612,18 @@ class ProblemBatch:
 
 def create_batch(problems, stream=None) -> ProblemBatch:
     return ProblemBatch(problems, stream)
+
+
+def tc_gemm_bf16(A, B, bias=None, epilogue=0, out_f32=True, out_bf16=False, preact=False, stream=None):
+    """C = A @ B.T (+ bias, ELU) on the tcgen05 tensor cores; A [M,K], B [N,K]
+    bf16 CUDA tensors, K a multiple of 64.  Returns (C_f32, C_bf16, preact)."""
+    import torch
+    M, K = A.shape
+    N = B.shape[0]
+    oF = torch.empty(M, N, dtype=torch.float32, device=A.device) if out_f32 else None
+    oB = torch.empty(M, N, dtype=torch.bfloat16, device=A.device) if out_bf16 else None
+    pa = torch.empty(M, N, dtype=torch.float32, device=A.device) if preact else None
+    vp = lambda t: C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
+    _check(lib().pda_tc_gemm_bf16(vp(A), vp(B), M, N, K, vp(bias), int(epilogue), vp(oF), vp(oB), vp(pa),
+                                  _stream_handle(stream)))
+    return oF, oB, pa

@@ -31,6 +31,7 @@ SOURCES = [
     "kernels_euler1d.cu",
     "util.cu",
     "noalloc.cu",
+    "mlp.cu",
     "mesh.cpp",
     "problem.cpp",
     "batch.cpp",

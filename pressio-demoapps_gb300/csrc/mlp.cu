@@ -1,0 +1,69 @@
+// Autoencoder building blocks for the learned-manifold ROM: the tcgen05 BF16
+// GEMM launcher and the elementwise / reduction kernels of training (ELU
+// backward, bias gradients, transposes, MSE, Adam).
+#include <cstdint>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "../../include/pda_gb300.h"
+#include "internal.hpp"
+#include "tc_gemm.cuh"
+
+namespace pda {
+
+static __device__ int g_tc_err;
+
+cudaError_t tc_gemm(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K, const float *bias,
+                    int epi, float *outF, __nv_bfloat16 *outB, float *preact, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(tc::k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  int *err = nullptr;
+  cudaError_t e = cudaGetSymbolAddress((void **)&err, g_tc_err);
+  if (e != cudaSuccess) return e;
+  dim3 grid((unsigned)((N + tc::BN - 1) / tc::BN), (unsigned)((M + tc::BM - 1) / tc::BM));
+  tc::k_gemm_tn<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(A, B, M, N, K, bias, epi, outF, outB, preact, err);
+  return cudaGetLastError();
+}
+
+// 1 if any tensor-core GEMM gave up waiting since the last call; clears it
+int tc_gemm_error_and_clear() {
+  int h = 0;
+  if (cudaMemcpyFromSymbol(&h, g_tc_err, sizeof(int)) != cudaSuccess) return -1;
+  const int z = 0;
+  cudaMemcpyToSymbol(g_tc_err, &z, sizeof(int));
+  return h;
+}
+
+}  // namespace pda
+
+extern "C" {
+
+pda_status pda_tc_gemm_bf16(const void *d_A, const void *d_B, int64_t M, int64_t N, int64_t K, const float *d_bias,
+                            int epilogue, float *d_outF, void *d_outB, float *d_preact, void *stream) {
+  if (!d_A || !d_B || M <= 0 || N <= 0 || K <= 0 || K % pda::tc::BK != 0 || epilogue < 0 || epilogue > 2 ||
+      (epilogue != 0 && !d_bias) || (!d_outF && !d_outB) ||
+      ((uintptr_t)d_A & 15u) != 0 || ((uintptr_t)d_B & 15u) != 0) {
+    pda::set_last_error("pda_tc_gemm_bf16: invalid argument (K must be a multiple of 64, A/B 16-byte aligned)");
+    return PDA_ERR_INVALID_ARGUMENT;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = pda::tc_gemm((const __nv_bfloat16 *)d_A, (const __nv_bfloat16 *)d_B, M, N, K, d_bias, epilogue,
+                               d_outF, (__nv_bfloat16 *)d_outB, d_preact, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    pda::set_last_error(std::string("pda_tc_gemm_bf16: ") + cudaGetErrorString(e));
+    return PDA_ERR_CUDA;
+  }
+  if (pda::tc_gemm_error_and_clear() != 0) {
+    pda::set_last_error("pda_tc_gemm_bf16: a tensor-core wait timed out");
+    return PDA_ERR_CUDA;
+  }
+  return PDA_OK;
+}
+
+}  // extern "C"
