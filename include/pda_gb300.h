@@ -283,6 +283,57 @@ pda_status pda_tc_gemm_bf16(const void *d_A, const void *d_B, int64_t M, int64_t
                             const float *d_bias, int epilogue, float *d_outF, void *d_outB,
                             float *d_preact, void *stream);
 
+/* MLP autoencoder for the learned manifold, trained on the device with the
+ * tcgen05 GEMM (bf16 operands, fp32 accumulation) and Adam (fp32 masters):
+ *   encoder n -> ha (ELU) -> hb (ELU) -> latent;  decoder latent -> hb (ELU)
+ *   -> ha (ELU) -> n (full-width output); loss = mean squared error.
+ * n, ha, hb multiples of 64; latent <= 64 (padded to 64 inside).  Data are
+ * bf16 rows [ns x n] on the device (uint16 storage).  Layers 0..5 in the
+ * order above; padded shapes: W [out x in], b [out]. */
+typedef struct pda_ae pda_ae;
+pda_status pda_ae_create(int64_t n, int latent, int ha, int hb, uint64_t seed, void *stream, pda_ae **out);
+void pda_ae_free(pda_ae *ae);
+/* epochs of minibatch Adam over a seeded permutation; losses[epoch] = mean
+ * batch loss (may be NULL); batch a multiple of 64 */
+pda_status pda_ae_train(pda_ae *ae, const void *d_data, int64_t ns, int batch, int epochs, double lr,
+                        uint64_t seed, double *losses);
+/* Y = decoder(encoder(X)) (fp32 [rows x n]); Z (may be NULL) = latent [rows x latent] */
+pda_status pda_ae_reconstruct(pda_ae *ae, const void *d_X, int64_t rows, float *d_Y, float *d_Z);
+/* loss and all parameter gradients of one batch, no update (gradient checks);
+ * d_grads = concatenation over layers of [W, b] with padded shapes */
+pda_status pda_ae_gradients(pda_ae *ae, const void *d_X, int batch, double *loss, float *d_grads);
+pda_status pda_ae_layer(pda_ae *ae, int layer, float *d_W, float *d_b, int64_t *out_in);
+pda_status pda_ae_set_layer(pda_ae *ae, int layer, const float *d_W, const float *d_b);
+
+/* Hyper-reduced LSPG on the device (no counterpart in pressio-demoapps; the
+ * algorithm of Pressio's LspgUnsteadyResidualJacobianPolicyHypRed,
+ * rom/impl/lspg_unsteady_rj_policy_hypred.hpp:180-264, with BDF1 and a
+ * Gauss-Newton solver whose normal equations are formed and factored in
+ * FP64).  sample_problem is a problem on a sample mesh; sample_to_stencil[i]
+ * is the stencil-mesh index of sample cell i.  Trial spaces:
+ *   affine: y = uref + Phi x         (d_phi: stencil dofs x k, row-major)
+ *   mlp:    y = uref + scale * (W3 elu(W2 elu(W1 x + b1) + b2) + b3)
+ *           (W1: h1 x k, W2: h2 x h1, W3: stencil dofs x h2, row-major fp32;
+ *            h1 = 256; the decoder's output rows at the stencil cells)
+ * k must be one of 2, 4, 6, 8, 10, 12, 16, 20, 24, 32. */
+typedef struct pda_lspg pda_lspg;
+pda_status pda_lspg_create_affine(pda_problem *sample_problem, const int64_t *sample_to_stencil, int k,
+                                  const double *d_uref, const double *d_phi, pda_lspg **out);
+pda_status pda_lspg_create_mlp(pda_problem *sample_problem, const int64_t *sample_to_stencil, int k, int h1,
+                               int h2, const double *d_uref, const double *d_scale, const float *d_W1,
+                               const float *d_b1, const float *d_W2, const float *d_b2, const float *d_W3,
+                               const float *d_b3, pda_lspg **out);
+void pda_lspg_free(pda_lspg *rom);
+/* y (stencil dofs) of latent x (k doubles, device) */
+pda_status pda_lspg_decode(pda_lspg *rom, const double *d_x, double *d_y);
+/* n_steps BDF1 steps of size dt from latent d_x (updated in place), at most
+ * gn_iters Gauss-Newton iterations per step (stopping early once the
+ * correction norm is below tol); use_graph != 0 replays one captured step.
+ * info (may be NULL) receives {last correction norm, iterations of the last
+ * step, residual norm at the last iterate, max over steps of that norm}. */
+pda_status pda_lspg_advance_bdf1(pda_lspg *rom, double *d_x, double dt, int64_t n_steps, int gn_iters,
+                                 double tol, int use_graph, double *info);
+
 /* --------------------------------------------------------- diagnostics
  * (no counterpart in the reference: measurement support for benchmarks) */
 

@@ -134,6 +134,24 @@ _SIGS = {
     "pda_batch_launch_count": (C.c_int64, [C.c_void_p]),
     "pda_tc_gemm_bf16": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_int,
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "pda_ae_create": (C.c_int, [C.c_int64, C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_void_p,
+                                C.POINTER(C.c_void_p)]),
+    "pda_ae_free": (None, [C.c_void_p]),
+    "pda_ae_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_double, C.c_uint64,
+                               C.c_void_p]),
+    "pda_ae_reconstruct": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "pda_ae_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_void_p]),
+    "pda_ae_layer": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "pda_ae_set_layer": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "pda_lspg_create_affine": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                         C.POINTER(C.c_void_p)]),
+    "pda_lspg_create_mlp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.POINTER(C.c_void_p)]),
+    "pda_lspg_free": (None, [C.c_void_p]),
+    "pda_lspg_decode": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "pda_lspg_advance_bdf1": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int64, C.c_int, C.c_double,
+                                        C.c_int, C.c_void_p]),
 }
 
 
@@ -627,3 +645,126 @@ def tc_gemm_bf16(A, B, bias=None, epilogue=0, out_f32=True, out_bf16=False, prea
     _check(lib().pda_tc_gemm_bf16(vp(A), vp(B), M, N, K, vp(bias), int(epilogue), vp(oF), vp(oB), vp(pa),
                                   _stream_handle(stream)))
     return oF, oB, pa
+
+
+# ------------------------------------------------------- learned-manifold ROM
+def _vp(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
+
+
+class AutoEncoder:
+    """MLP autoencoder trained on the device (tcgen05 BF16 GEMMs, fp32
+    accumulation, Adam): n -> ha -> hb -> latent -> hb -> ha -> n, ELU.
+    No counterpart in the reference."""
+
+    LAYERS = 6
+
+    def __init__(self, n, latent, ha=1024, hb=256, seed=0, stream=None):
+        h = C.c_void_p()
+        self._stream = _stream_handle(stream)
+        _check(lib().pda_ae_create(int(n), int(latent), int(ha), int(hb), int(seed), self._stream, C.byref(h)))
+        self._h = h
+        self.n, self.latent, self.ha, self.hb = int(n), int(latent), int(ha), int(hb)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.pda_ae_free(self._h)
+            self._h = None
+
+    def train(self, data, batch=256, epochs=1, lr=1e-3, seed=0):
+        import numpy as np
+        import torch
+        assert data.dtype == torch.bfloat16 and data.is_cuda and data.is_contiguous() and data.shape[1] == self.n
+        losses = np.zeros(max(1, epochs))
+        _check(lib().pda_ae_train(self._h, _vp(data), data.shape[0], int(batch), int(epochs), float(lr), int(seed),
+                                  losses.ctypes.data_as(C.c_void_p)))
+        return losses[:epochs]
+
+    def reconstruct(self, X):
+        import torch
+        rows = X.shape[0]
+        Y = torch.empty(rows, self.n, dtype=torch.float32, device=X.device)
+        Z = torch.empty(rows, self.latent, dtype=torch.float32, device=X.device)
+        _check(lib().pda_ae_reconstruct(self._h, _vp(X), rows, _vp(Y), _vp(Z)))
+        return Y, Z
+
+    def layer_shape(self, l):
+        import numpy as np
+        oi = np.zeros(2, dtype=np.int64)
+        _check(lib().pda_ae_layer(self._h, int(l), C.c_void_p(0), C.c_void_p(0), oi.ctypes.data_as(C.c_void_p)))
+        return int(oi[0]), int(oi[1])
+
+    def layer(self, l):
+        import torch
+        o, i = self.layer_shape(l)
+        W = torch.empty(o, i, dtype=torch.float32, device="cuda")
+        b = torch.empty(o, dtype=torch.float32, device="cuda")
+        _check(lib().pda_ae_layer(self._h, int(l), _vp(W), _vp(b), C.c_void_p(0)))
+        return W, b
+
+    def set_layer(self, l, W, b):
+        _check(lib().pda_ae_set_layer(self._h, int(l), _vp(W.contiguous()), _vp(b.contiguous())))
+
+    def gradients(self, X):
+        import torch
+        total = sum(o * i + o for o, i in (self.layer_shape(l) for l in range(self.LAYERS)))
+        g = torch.empty(total, dtype=torch.float32, device=X.device)
+        loss = C.c_double()
+        _check(lib().pda_ae_gradients(self._h, _vp(X), X.shape[0], C.byref(loss), _vp(g)))
+        return loss.value, g
+
+    def decoder(self):
+        """Decoder weights with real sizes: W1 [hb x k], W2 [ha x hb], W3 [n x ha]."""
+        W1, b1 = self.layer(3)
+        W2, b2 = self.layer(4)
+        W3, b3 = self.layer(5)
+        return (W1[:, : self.latent].contiguous(), b1, W2, b2, W3, b3)
+
+
+class LspgRom:
+    """Hyper-reduced LSPG (BDF1, Gauss-Newton, FP64 normal equations) on a
+    sample-mesh problem with an affine or MLP-decoder trial manifold."""
+
+    def __init__(self, handle, problem, keep):
+        self._h, self._problem, self._keep = handle, problem, keep
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.pda_lspg_free(self._h)
+            self._h = None
+
+    @staticmethod
+    def affine(sample_problem, sample_to_stencil, uref, phi):
+        import numpy as np
+        s2 = np.ascontiguousarray(sample_to_stencil, dtype=np.int64)
+        k = phi.shape[1]
+        h = C.c_void_p()
+        _check(lib().pda_lspg_create_affine(sample_problem._h, s2.ctypes.data_as(C.c_void_p), int(k), _vp(uref),
+                                            _vp(phi.contiguous()), C.byref(h)))
+        return LspgRom(h, sample_problem, (s2, k, uref.numel()))
+
+    @staticmethod
+    def mlp(sample_problem, sample_to_stencil, uref, scale, W1, b1, W2, b2, W3, b3):
+        import numpy as np
+        s2 = np.ascontiguousarray(sample_to_stencil, dtype=np.int64)
+        k = W1.shape[1]
+        h = C.c_void_p()
+        ts = [t.contiguous() for t in (W1, b1, W2, b2, W3, b3)]
+        _check(lib().pda_lspg_create_mlp(sample_problem._h, s2.ctypes.data_as(C.c_void_p), int(k),
+                                         int(W1.shape[0]), int(W2.shape[0]), _vp(uref), _vp(scale),
+                                         *[_vp(t) for t in ts], C.byref(h)))
+        return LspgRom(h, sample_problem, (s2, k, uref.numel()))
+
+    def decode(self, x):
+        import torch
+        y = torch.empty(self._keep[2], dtype=torch.float64, device="cuda")
+        _check(lib().pda_lspg_decode(self._h, _vp(x), _vp(y)))
+        return y
+
+    def advance_bdf1(self, x, dt, n_steps, gn_iters=5, tol=1e-10, use_graph=True):
+        import numpy as np
+        info = np.zeros(4)
+        _check(lib().pda_lspg_advance_bdf1(self._h, _vp(x), float(dt), int(n_steps), int(gn_iters), float(tol),
+                                           int(bool(use_graph)), info.ctypes.data_as(C.c_void_p)))
+        return {"last_correction": info[0], "iters_last_step": int(info[1]), "residual": info[2],
+                "max_residual": info[3]}

@@ -32,6 +32,8 @@ SOURCES = [
     "util.cu",
     "noalloc.cu",
     "mlp.cu",
+    "rom.cu",
+    "ae.cu",
     "mesh.cpp",
     "problem.cpp",
     "batch.cpp",

@@ -1,6 +1,7 @@
 // Autoencoder building blocks for the learned-manifold ROM: the tcgen05 BF16
 // GEMM launcher and the elementwise / reduction kernels of training (ELU
 // backward, bias gradients, transposes, MSE, Adam).
+#include <algorithm>
 #include <cstdint>
 
 #include <cuda_bf16.h>
@@ -9,6 +10,8 @@
 #include "../../include/pda_gb300.h"
 #include "internal.hpp"
 #include "tc_gemm.cuh"
+
+#include <string>
 
 namespace pda {
 
@@ -26,7 +29,50 @@ cudaError_t tc_gemm(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long
   cudaError_t e = cudaGetSymbolAddress((void **)&err, g_tc_err);
   if (e != cudaSuccess) return e;
   dim3 grid((unsigned)((N + tc::BN - 1) / tc::BN), (unsigned)((M + tc::BM - 1) / tc::BM));
-  tc::k_gemm_tn<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(A, B, M, N, K, bias, epi, outF, outB, preact, err);
+  const int kt = (int)(K / tc::BK);
+  tc::k_gemm_tn<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(A, B, M, N, K, bias, epi, outF, outB, preact, err, kt,
+                                                          nullptr);
+  return cudaGetLastError();
+}
+
+// Same, splitting K over `splits` CTAs per output tile when the tiles alone
+// would leave most SMs idle (few output tiles, long K); the partial sums go to
+// `work` (splits * M * N floats) and are added in split order, so the result
+// does not depend on scheduling.
+cudaError_t tc_gemm_splitk(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K,
+                           const float *bias, int epi, float *outF, __nv_bfloat16 *outB, float *preact, float *work,
+                           long workFloats, cudaStream_t s) {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  const long tiles = ((N + tc::BN - 1) / tc::BN) * ((M + tc::BM - 1) / tc::BM);
+  const int kt = (int)(K / tc::BK);
+  int splits = 1;
+  if (tiles < 2L * sms && kt >= 32) {
+    splits = (int)std::min<long>((2L * sms + tiles - 1) / tiles, kt / 16);
+    while (splits > 1 && (long)splits * M * N > workFloats) --splits;
+  }
+  if (splits <= 1) return tc_gemm(A, B, M, N, K, bias, epi, outF, outB, preact, s);
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(tc::k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  int *err = nullptr;
+  cudaError_t e = cudaGetSymbolAddress((void **)&err, g_tc_err);
+  if (e != cudaSuccess) return e;
+  const int per = (kt + splits - 1) / splits;
+  dim3 grid((unsigned)((N + tc::BN - 1) / tc::BN), (unsigned)((M + tc::BM - 1) / tc::BM), (unsigned)splits);
+  tc::k_gemm_tn<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(A, B, M, N, K, nullptr, tc::EPI_NONE, nullptr, nullptr,
+                                                          nullptr, err, per, work);
+  const long total = M * N;
+  tc::k_splitk_reduce<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(M, N, splits, work, bias, epi, outF, outB,
+                                                                       preact);
   return cudaGetLastError();
 }
 
@@ -52,9 +98,20 @@ pda_status pda_tc_gemm_bf16(const void *d_A, const void *d_B, int64_t M, int64_t
     return PDA_ERR_INVALID_ARGUMENT;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = pda::tc_gemm((const __nv_bfloat16 *)d_A, (const __nv_bfloat16 *)d_B, M, N, K, d_bias, epilogue,
-                               d_outF, (__nv_bfloat16 *)d_outB, d_preact, s);
+  // split-K scratch for shapes with few output tiles and a long K
+  float *work = nullptr;
+  const long workFloats = 32L * M * N;
+  if ((K / pda::tc::BK) >= 32 && ((M + 127) / 128) * ((N + 127) / 128) < 304 &&
+      cudaMalloc((void **)&work, (size_t)workFloats * sizeof(float)) != cudaSuccess) {
+    work = nullptr;
+    cudaGetLastError();
+  }
+  cudaError_t e = work ? pda::tc_gemm_splitk((const __nv_bfloat16 *)d_A, (const __nv_bfloat16 *)d_B, M, N, K, d_bias,
+                                             epilogue, d_outF, (__nv_bfloat16 *)d_outB, d_preact, work, workFloats, s)
+                       : pda::tc_gemm((const __nv_bfloat16 *)d_A, (const __nv_bfloat16 *)d_B, M, N, K, d_bias,
+                                      epilogue, d_outF, (__nv_bfloat16 *)d_outB, d_preact, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (work) cudaFree(work);
   if (e != cudaSuccess) {
     pda::set_last_error(std::string("pda_tc_gemm_bf16: ") + cudaGetErrorString(e));
     return PDA_ERR_CUDA;

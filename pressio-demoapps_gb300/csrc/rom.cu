@@ -1,0 +1,542 @@
+// Hyper-reduced LSPG (BDF1, Gauss-Newton with FP64 normal equations) on the
+// device, over a sample-mesh problem, with an affine trial space
+// (y = u_ref + Phi x) or a nonlinear manifold given by an MLP decoder
+// (y = u_ref + scale * dec(x), dec = W3 elu(W2 elu(W1 x + b1) + b2) + b3
+// evaluated only at the stencil-mesh rows).
+//
+// Per time step n -> n+1 and Gauss-Newton iteration (Pressio's
+// LspgUnsteadyResidualJacobianPolicyHypRed, lspg_unsteady_rj_policy_hypred.hpp:
+// 180-264, with the BDF1 constants c_np1 = 1, c_n = -1, c_f = -1 of
+// ode_constants.hpp:61-63):
+//   y      = trial state at the current latent x (stencil rows), D = dy/dx
+//   V, Jf  = sample-mesh velocity and Jacobian at y (the library's kernels)
+//   R      = cf V + (y - y_n)|sample                 cf = -dt
+//   JR     = cf (Jf D) + D|sample
+//   (JR^T JR) dx = JR^T R,  x <- x - dx               (FP64, Cholesky)
+// Each kernel reads a per-step "converged" flag and returns at once after the
+// correction fell below the tolerance, so a fixed number of iterations can be
+// captured in one CUDA graph per step.
+#include <cmath>
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "problem_impl.hpp"
+
+namespace pda {
+namespace rom {
+
+constexpr int KMAX = 32;        // latent dimension limit
+constexpr int ROWS_PER_BLOCK = 128;
+
+struct Flags {
+  int converged;   // correction below tolerance in this step
+  int iters;       // iterations taken in this step
+  double lastCorr;  // norm of the last correction
+  double lastRes;   // residual norm at the last iterate
+  double maxRes;    // max over steps of the residual norm at the step's last iterate
+};
+
+// ------------------------------------------------------------ trial spaces
+template <int K>
+__global__ void k_decode_affine(long nst, const double *__restrict__ uref, const double *__restrict__ phi,
+                                const double *__restrict__ x, double *__restrict__ y, const Flags *f) {
+  if (f->converged) return;
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nst) return;
+  double acc = 0.;
+#pragma unroll
+  for (int c = 0; c < K; ++c) acc += phi[i * K + c] * x[c];
+  y[i] = uref[i] + acc;
+}
+
+__device__ __forceinline__ float elu_f(float a) { return a > 0.f ? a : expm1f(a); }
+__device__ __forceinline__ float delu_f(float a) { return a > 0.f ? 1.f : expf(a); }
+
+// hidden layers: every block recomputes layer 1 (h1 x k, tiny) in shared
+// memory, then its slice of layer 2: h2[r] and T2[r][c] = elu'(a2_r) (W2 T1)_rc
+// with T1 = diag(elu'(a1)) W1.  Output Z[r][0] = h2, Z[r][1 + c] = T2.
+template <int K, int H1>
+__global__ void __launch_bounds__(256)
+k_decode_hidden(int h2, const float *__restrict__ W1, const float *__restrict__ b1, const float *__restrict__ W2,
+                const float *__restrict__ b2, const double *__restrict__ x, float *__restrict__ Z, const Flags *f) {
+  if (f->converged) return;
+  __shared__ float sh1[H1];
+  __shared__ float sT1[H1][K];
+  __shared__ float sx[K];
+  if (threadIdx.x < K) sx[threadIdx.x] = (float)x[threadIdx.x];
+  __syncthreads();
+  for (int r = threadIdx.x; r < H1; r += blockDim.x) {
+    float a = b1[r];
+#pragma unroll
+    for (int c = 0; c < K; ++c) a += W1[r * K + c] * sx[c];
+    sh1[r] = elu_f(a);
+    const float d = delu_f(a);
+#pragma unroll
+    for (int c = 0; c < K; ++c) sT1[r][c] = d * W1[r * K + c];
+  }
+  __syncthreads();
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= h2) return;
+  float a = b2[r];
+  float t[K];
+#pragma unroll
+  for (int c = 0; c < K; ++c) t[c] = 0.f;
+  const float *w = W2 + (long)r * H1;
+  for (int j = 0; j < H1; ++j) {
+    const float wj = w[j];
+    a += wj * sh1[j];
+#pragma unroll
+    for (int c = 0; c < K; ++c) t[c] += wj * sT1[j][c];
+  }
+  const float d = delu_f(a);
+  constexpr int ld = 1 + K;
+  Z[(long)r * ld] = elu_f(a);
+#pragma unroll
+  for (int c = 0; c < K; ++c) Z[(long)r * ld + 1 + c] = d * t[c];
+}
+
+// output layer at the stencil rows: one warp per row, the [h2 | T2] block
+// staged in shared memory by every block (h2 x (1+k) floats)
+template <int K>
+__global__ void __launch_bounds__(256)
+k_decode_out(int h2, long nst, const float *__restrict__ W3, const float *__restrict__ b3,
+             const double *__restrict__ uref, const double *__restrict__ scale, const float *__restrict__ Z,
+             double *__restrict__ y, double *__restrict__ D, const Flags *f) {
+  if (f->converged) return;
+  extern __shared__ float sZ[];
+  constexpr int ld = 1 + K;
+  for (int i = threadIdx.x; i < h2 * ld; i += blockDim.x) sZ[i] = Z[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const long warps = (long)gridDim.x * (blockDim.x >> 5);
+  for (long row = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < nst; row += warps) {
+    float acc[ld];
+#pragma unroll
+    for (int c = 0; c < ld; ++c) acc[c] = 0.f;
+    const float *w = W3 + row * h2;
+    for (int j = lane; j < h2; j += 32) {
+      const float wj = w[j];
+      const float *z = sZ + j * ld;
+#pragma unroll
+      for (int c = 0; c < ld; ++c) acc[c] += wj * z[c];
+    }
+#pragma unroll
+    for (int c = 0; c < ld; ++c)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+    if (lane == 0) {
+      const double s = scale[row];
+      y[row] = uref[row] + s * (double)(acc[0] + b3[row]);
+#pragma unroll
+      for (int c = 0; c < K; ++c) D[row * K + c] = s * (double)acc[1 + c];
+    }
+  }
+}
+
+// ---------------------------------------------------- LSPG residual / normal eqs
+// one thread per sample dof row r (sample cell r / ndpc, dof r % ndpc):
+// R_r and JR_r, then this block's partial sums of JR^T JR (upper triangle)
+// and JR^T R, in a fixed order
+template <int K>
+__global__ void __launch_bounds__(ROWS_PER_BLOCK)
+k_lspg_rows(int ndpc, long ns, const int *__restrict__ s2st, const double *__restrict__ y,
+            const double *__restrict__ D, const double *__restrict__ V, const int *__restrict__ rowptr,
+            const int *__restrict__ colidx, const double *__restrict__ J, double cf, double *__restrict__ yn,
+            int first, double *__restrict__ partial, const Flags *f) {
+  if (f->converged) return;
+  __shared__ double sJR[ROWS_PER_BLOCK][K + 1];  // column K holds R
+  const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = threadIdx.x;
+  if (r < ns) {
+    const long st = (long)s2st[r / ndpc] * ndpc + r % ndpc;  // stencil dof of this sample dof
+    const double ynp1 = y[st];
+    if (first) yn[r] = ynp1;  // first iteration of a step: y_n = y(x_n)
+    const double helper = 1. * ynp1 + (-1.) * yn[r];
+    sJR[t][K] = cf * V[r] + 1. * helper;
+    double jd[K];
+#pragma unroll
+    for (int c = 0; c < K; ++c) jd[c] = 0.;
+    for (int q = rowptr[r]; q < rowptr[r + 1]; ++q) {
+      const double jv = J[q];
+      const double *d = D + (long)colidx[q] * K;
+#pragma unroll
+      for (int c = 0; c < K; ++c) jd[c] += jv * d[c];
+    }
+#pragma unroll
+    for (int c = 0; c < K; ++c) sJR[t][c] = cf * jd[c] + 1. * D[st * K + c];
+  } else {
+#pragma unroll
+    for (int c = 0; c <= K; ++c) sJR[t][c] = 0.;
+  }
+  __syncthreads();
+  // partial sums: upper triangle of JR^T JR (row-major), then JR^T R, then R^T R
+  constexpr int ntri = K * (K + 1) / 2, ne = ntri + K + 1;
+  for (int e = t; e < ne; e += blockDim.x) {
+    int a, b;
+    if (e < ntri) {
+      a = 0;
+      int rem = e;
+      while (rem >= K - a) {
+        rem -= K - a;
+        ++a;
+      }
+      b = a + rem;
+    } else if (e < ntri + K) {
+      a = e - ntri;
+      b = K;
+    } else {
+      a = K;
+      b = K;
+    }
+    double s = 0.;
+    for (int i = 0; i < ROWS_PER_BLOCK; ++i) s += sJR[i][a] * sJR[i][b];
+    partial[(long)blockIdx.x * ne + e] = s;
+  }
+}
+
+// one block: reduce the partial sums in block order, factor, solve, update
+template <int K>
+__global__ void __launch_bounds__(256)
+k_lspg_solve(int nblocks, const double *__restrict__ partial, double *__restrict__ x, double tol, Flags *f) {
+  if (f->converged) return;
+  constexpr int k = K;
+  __shared__ double H[K][K];
+  __shared__ double g[K];
+  __shared__ double red[K + 1];
+  __shared__ double rr;
+  constexpr int ntri = K * (K + 1) / 2, ne = ntri + K + 1;
+  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+    double s = 0.;
+    for (int b = 0; b < nblocks; ++b) s += partial[(long)b * ne + e];
+    if (e < ntri) {
+      int a = 0, rem = e;
+      while (rem >= k - a) {
+        rem -= k - a;
+        ++a;
+      }
+      const int b2 = a + rem;
+      H[a][b2] = s;
+      H[b2][a] = s;
+    } else if (e < ntri + K) {
+      g[e - ntri] = s;
+    } else {
+      rr = s;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // Cholesky H = L L^T in place (lower triangle), then L L^T dx = g
+    bool ok = true;
+    for (int j = 0; j < k && ok; ++j) {
+      double d = H[j][j];
+      for (int p = 0; p < j; ++p) d -= H[j][p] * H[j][p];
+      if (!(d > 0.)) {
+        ok = false;
+        break;
+      }
+      const double l = sqrt(d);
+      H[j][j] = l;
+      for (int i = j + 1; i < k; ++i) {
+        double s = H[i][j];
+        for (int p = 0; p < j; ++p) s -= H[i][p] * H[j][p];
+        H[i][j] = s / l;
+      }
+    }
+    double corr = 0.;
+    if (ok) {
+      for (int i = 0; i < k; ++i) {
+        double s = g[i];
+        for (int p = 0; p < i; ++p) s -= H[i][p] * red[p];
+        red[i] = s / H[i][i];
+      }
+      for (int i = k - 1; i >= 0; --i) {
+        double s = red[i];
+        for (int p = i + 1; p < k; ++p) s -= H[p][i] * red[p];
+        red[i] = s / H[i][i];
+      }
+      for (int i = 0; i < k; ++i) {
+        x[i] -= red[i];
+        corr += red[i] * red[i];
+      }
+    }
+    f->iters += 1;
+    f->lastCorr = sqrt(corr);
+    f->lastRes = sqrt(rr);
+    if (!(f->lastRes <= f->maxRes)) f->maxRes = f->lastRes;
+    if (!ok || sqrt(corr) < tol) f->converged = 1;
+  }
+}
+
+__global__ void k_step_begin(Flags *f) {
+  f->converged = 0;
+  f->iters = 0;
+}
+
+}  // namespace rom
+}  // namespace pda
+
+// ------------------------------------------------------------------ object
+struct pda_lspg {
+  pda_problem *P = nullptr;
+  int kind = 0;  // 0 affine, 1 MLP decoder
+  int k = 0, ndpc = 0, h1 = 0, h2 = 0;
+  long nst = 0, ns = 0, nSampleCells = 0;
+  pda::DevBuf<int> s2st;
+  pda::DevBuf<double> uref, phi, scale;
+  pda::DevBuf<float> W1, b1, W2, b2, W3, b3, Z;
+  pda::DevBuf<double> y, D, V, J, yn, partial, xn;
+  pda::DevBuf<pda::rom::Flags> flags;
+  int nblocks = 0;
+  int64_t nnz = 0;
+  cudaGraphExec_t graph = nullptr;
+  double graphDt = 0;
+  double *graphX = nullptr;
+  int graphIters = 0;
+  double graphTol = 0;
+  ~pda_lspg() {
+    if (graph) cudaGraphExecDestroy(graph);
+  }
+};
+
+namespace pda {
+namespace rom {
+namespace {
+
+int decode_grid(long nst) {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return (int)std::min<long>(div_up(nst, 8), 2L * sms);
+}
+
+template <int K>
+void decode_k(pda_lspg &L, const double *x, double *y, cudaStream_t s) {
+  Flags *f = L.flags.p;
+  if (L.kind == 0) {
+    k_decode_affine<K><<<div_up(L.nst, 256), 256, 0, s>>>(L.nst, L.uref.p, L.phi.p, x, y, f);
+  } else {
+    k_decode_hidden<K, 256><<<div_up(L.h2, 256), 256, 0, s>>>(L.h2, L.W1.p, L.b1.p, L.W2.p, L.b2.p, x, L.Z.p, f);
+    const int smem = L.h2 * (1 + K) * (int)sizeof(float);
+    k_decode_out<K><<<decode_grid(L.nst), 256, smem, s>>>(L.h2, L.nst, L.W3.p, L.b3.p, L.uref.p, L.scale.p, L.Z.p,
+                                                            y, L.D.p, f);
+  }
+}
+
+template <int K>
+void gn_iteration_k(pda_lspg &L, double *x, double dt, double tol, int first, cudaStream_t s) {
+  Flags *f = L.flags.p;
+  decode_k<K>(L, x, L.y.p, s);
+  // sample-mesh velocity and Jacobian at y (the library's own kernels); they
+  // run unconditionally, cheap next to the rest once converged
+  const pda_status st = pda_velocity_and_jacobian(L.P, L.y.p, 0.0, L.V.p, L.J.p);
+  if (st != PDA_OK) throw Error(st, pda_last_error());
+  k_lspg_rows<K><<<L.nblocks, ROWS_PER_BLOCK, 0, s>>>(L.ndpc, L.ns, L.s2st.p, L.y.p, L.D.p, L.V.p,
+                                                      L.P->d_rowptr.p, L.P->d_colidx.p, L.J.p, -dt, L.yn.p, first,
+                                                      L.partial.p, f);
+  k_lspg_solve<K><<<1, 256, 0, s>>>(L.nblocks, L.partial.p, x, tol, f);
+}
+
+#define PDA_ROM_K_SWITCH(k, CALL) \
+  switch (k) {                    \
+    case 2: CALL(2); break;       \
+    case 4: CALL(4); break;       \
+    case 6: CALL(6); break;       \
+    case 8: CALL(8); break;       \
+    case 10: CALL(10); break;     \
+    case 12: CALL(12); break;     \
+    case 16: CALL(16); break;     \
+    case 20: CALL(20); break;     \
+    case 24: CALL(24); break;     \
+    case 32: CALL(32); break;     \
+    default: throw Error(PDA_ERR_UNSUPPORTED, "latent dimension not compiled"); \
+  }
+
+bool k_supported(int k) {
+  return k == 2 || k == 4 || k == 6 || k == 8 || k == 10 || k == 12 || k == 16 || k == 20 || k == 24 || k == 32;
+}
+
+void gn_iteration(pda_lspg &L, double *x, double dt, double tol, int first, cudaStream_t s) {
+#define PDA_ROM_GN(K) gn_iteration_k<K>(L, x, dt, tol, first, s)
+  PDA_ROM_K_SWITCH(L.k, PDA_ROM_GN)
+#undef PDA_ROM_GN
+}
+
+void decode(pda_lspg &L, const double *x, double *y, cudaStream_t s) {
+#define PDA_ROM_DEC(K) decode_k<K>(L, x, y, s)
+  PDA_ROM_K_SWITCH(L.k, PDA_ROM_DEC)
+#undef PDA_ROM_DEC
+}
+
+void bdf1_step(pda_lspg &L, double *x, double dt, double tol, int iters, cudaStream_t s) {
+  k_step_begin<<<1, 1, 0, s>>>(L.flags.p);
+  for (int it = 0; it < iters; ++it) gn_iteration(L, x, dt, tol, it == 0 ? 1 : 0, s);
+  PDA_CUDA(cudaGetLastError());
+}
+
+void common_setup(pda_lspg &L, pda_problem *P, const int64_t *s2st, int k) {
+  PDA_REQUIRE(P && s2st, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  PDA_REQUIRE(k_supported(k), PDA_ERR_UNSUPPORTED,
+              "latent dimension must be one of 2, 4, 6, 8, 10, 12, 16, 20, 24, 32");
+  L.P = P;
+  L.k = k;
+  L.ndpc = P->ndpc;
+  L.nst = P->dofsStencil;
+  L.ns = P->dofsSample;
+  L.nSampleCells = L.ns / L.ndpc;
+  std::vector<int> m((size_t)L.nSampleCells);
+  for (long i = 0; i < L.nSampleCells; ++i) {
+    PDA_REQUIRE(s2st[i] >= 0 && s2st[i] < L.nst / L.ndpc, PDA_ERR_INVALID_ARGUMENT,
+                "sample-to-stencil index out of range");
+    m[(size_t)i] = (int)s2st[i];
+  }
+  L.s2st.upload(m);
+  int64_t rows = 0, cols = 0, nnz = 0;
+  pda_status st = pda_jacobian_shape(P, &rows, &cols, &nnz);
+  if (st != PDA_OK) throw Error(st, pda_last_error());
+  L.nnz = nnz;
+  L.y.alloc((size_t)L.nst);
+  L.D.alloc((size_t)L.nst * k);
+  L.V.alloc((size_t)L.ns);
+  L.J.alloc((size_t)std::max<int64_t>(nnz, 1));
+  L.yn.alloc((size_t)L.ns);
+  L.nblocks = div_up(L.ns, ROWS_PER_BLOCK);
+  L.partial.alloc((size_t)L.nblocks * (k * (k + 1) / 2 + k + 1));
+  L.flags.alloc(1);
+  L.xn.alloc((size_t)k);
+  PDA_CUDA(cudaMemset(L.flags.p, 0, sizeof(Flags)));
+  PDA_CUDA(cudaMemset(L.y.p, 0, (size_t)L.nst * sizeof(double)));
+  // build the sample problem's tables and CSR pattern now (they allocate)
+  st = pda_velocity_and_jacobian(P, L.y.p, 0.0, L.V.p, L.J.p);
+  if (st != PDA_OK) throw Error(st, pda_last_error());
+  PDA_CUDA(cudaDeviceSynchronize());
+}
+
+template <class T> void upload_dev(DevBuf<T> &b, const T *d_src, size_t n) {
+  b.alloc(n);
+  PDA_CUDA(cudaMemcpy(b.p, d_src, n * sizeof(T), cudaMemcpyDeviceToDevice));
+}
+
+}  // namespace
+}  // namespace rom
+}  // namespace pda
+
+using pda::Error;
+
+extern "C" {
+
+pda_status pda_lspg_create_affine(pda_problem *sample_problem, const int64_t *sample_to_stencil, int k,
+                                  const double *d_uref, const double *d_phi, pda_lspg **out) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(out && d_uref && d_phi, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  std::unique_ptr<pda_lspg> L(new pda_lspg);
+  L->kind = 0;
+  pda::rom::common_setup(*L, sample_problem, sample_to_stencil, k);
+  pda::rom::upload_dev(L->uref, d_uref, (size_t)L->nst);
+  pda::rom::upload_dev(L->phi, d_phi, (size_t)L->nst * k);
+  // D is the constant basis
+  PDA_CUDA(cudaMemcpy(L->D.p, d_phi, (size_t)L->nst * k * sizeof(double), cudaMemcpyDeviceToDevice));
+  *out = L.release();
+  PDA_API_END
+}
+
+pda_status pda_lspg_create_mlp(pda_problem *sample_problem, const int64_t *sample_to_stencil, int k, int h1,
+                               int h2, const double *d_uref, const double *d_scale, const float *d_W1,
+                               const float *d_b1, const float *d_W2, const float *d_b2, const float *d_W3,
+                               const float *d_b3, pda_lspg **out) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(out && d_uref && d_scale && d_W1 && d_b1 && d_W2 && d_b2 && d_W3 && d_b3, PDA_ERR_INVALID_ARGUMENT,
+              "null argument");
+  PDA_REQUIRE(h1 == 256, PDA_ERR_UNSUPPORTED, "decoder first hidden width must be 256");
+  PDA_REQUIRE(h2 >= 1 && h2 * (1 + k) * (int)sizeof(float) <= 200 * 1024, PDA_ERR_UNSUPPORTED,
+              "decoder second hidden width too large");
+  std::unique_ptr<pda_lspg> L(new pda_lspg);
+  L->kind = 1;
+  L->h1 = h1;
+  L->h2 = h2;
+  pda::rom::common_setup(*L, sample_problem, sample_to_stencil, k);
+  pda::rom::upload_dev(L->uref, d_uref, (size_t)L->nst);
+  pda::rom::upload_dev(L->scale, d_scale, (size_t)L->nst);
+  pda::rom::upload_dev(L->W1, d_W1, (size_t)h1 * k);
+  pda::rom::upload_dev(L->b1, d_b1, (size_t)h1);
+  pda::rom::upload_dev(L->W2, d_W2, (size_t)h2 * h1);
+  pda::rom::upload_dev(L->b2, d_b2, (size_t)h2);
+  pda::rom::upload_dev(L->W3, d_W3, (size_t)L->nst * h2);
+  pda::rom::upload_dev(L->b3, d_b3, (size_t)L->nst);
+  L->Z.alloc((size_t)h2 * (1 + k));
+  const int smem = h2 * (1 + k) * (int)sizeof(float);
+  if (smem > 48 * 1024) {
+#define PDA_ROM_ATTR(K) \
+  PDA_CUDA(cudaFuncSetAttribute(pda::rom::k_decode_out<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem))
+    PDA_ROM_K_SWITCH(k, PDA_ROM_ATTR)
+#undef PDA_ROM_ATTR
+  }
+  *out = L.release();
+  PDA_API_END
+}
+
+void pda_lspg_free(pda_lspg *L) { delete L; }
+
+pda_status pda_lspg_decode(pda_lspg *L, const double *d_x, double *d_y) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(L && d_x && d_y, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  cudaStream_t s = L->P->stream;
+  pda::rom::k_step_begin<<<1, 1, 0, s>>>(L->flags.p);
+  pda::rom::decode(*L, d_x, d_y, s);
+  PDA_CUDA(cudaGetLastError());
+  PDA_CUDA(cudaStreamSynchronize(s));
+  PDA_API_END
+}
+
+pda_status pda_lspg_advance_bdf1(pda_lspg *L, double *d_x, double dt, int64_t n_steps, int gn_iters, double tol,
+                                 int use_graph, double *info) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(L && d_x && n_steps >= 0 && gn_iters >= 1, PDA_ERR_INVALID_ARGUMENT, "invalid argument");
+  cudaStream_t s = L->P->stream;
+  if (!use_graph || s == nullptr) {
+    for (int64_t n = 0; n < n_steps; ++n) pda::rom::bdf1_step(*L, d_x, dt, tol, gn_iters, s);
+  } else {
+    if (L->graph && (L->graphDt != dt || L->graphX != d_x || L->graphIters != gn_iters || L->graphTol != tol)) {
+      cudaGraphExecDestroy(L->graph);
+      L->graph = nullptr;
+    }
+    if (!L->graph) {
+      PDA_CUDA(cudaStreamSynchronize(s));
+      cudaGraph_t g;
+      PDA_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      try {
+        pda::rom::bdf1_step(*L, d_x, dt, tol, gn_iters, s);
+      } catch (...) {
+        cudaStreamEndCapture(s, &g);
+        throw;
+      }
+      PDA_CUDA(cudaStreamEndCapture(s, &g));
+      PDA_CUDA(cudaGraphInstantiate(&L->graph, g, 0));
+      cudaGraphDestroy(g);
+      L->graphDt = dt;
+      L->graphX = d_x;
+      L->graphIters = gn_iters;
+      L->graphTol = tol;
+    }
+    for (int64_t n = 0; n < n_steps; ++n) PDA_CUDA(cudaGraphLaunch(L->graph, s));
+  }
+  if (info) {
+    pda::rom::Flags hf;
+    PDA_CUDA(cudaMemcpyAsync(&hf, L->flags.p, sizeof(hf), cudaMemcpyDeviceToHost, s));
+    PDA_CUDA(cudaStreamSynchronize(s));
+    info[0] = hf.lastCorr;
+    info[1] = (double)hf.iters;
+    info[2] = hf.lastRes;
+    info[3] = hf.maxRes;
+  }
+  PDA_API_END
+}
+
+}  // extern "C"

@@ -25,6 +25,8 @@
 
 #include <cuda_bf16.h>
 
+#include "tc_gemm_api.hpp"
+
 namespace pda {
 namespace tc {
 
@@ -33,8 +35,6 @@ constexpr int TILE_BYTES = BM * BK * 2;                    // one operand slice
 constexpr int SMEM_BYTES = STAGES * 2 * TILE_BYTES + 1024;  // + alignment slack
 constexpr uint32_t TMEM_COLS = 128;
 constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
-
-enum Epilogue : int { EPI_NONE = 0, EPI_BIAS = 1, EPI_BIAS_ELU = 2 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -100,11 +100,13 @@ __device__ __forceinline__ void load_slice(uint32_t sdst, const __nv_bfloat16 *_
 
 // K must be a multiple of 64; outF (fp32) and outB (bf16) are optional
 // row-major [M x N] outputs (ldc = N); preact (optional, fp32) receives the
-// value before the activation.
+// value before the activation.  Split K: CTA z of gridDim.z covers K slices
+// [z * kSlices, (z + 1) * kSlices) and, when `partial` is given, stores its
+// raw fp32 sums to partial[z][M][N] (no epilogue; k_splitk_reduce finishes).
 __global__ void __launch_bounds__(THREADS)
 k_gemm_tn(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__ B, long M, long N, long K,
           const float *__restrict__ bias, int epi, float *__restrict__ outF, __nv_bfloat16 *__restrict__ outB,
-          float *__restrict__ preact, int *__restrict__ err) {
+          float *__restrict__ preact, int *__restrict__ err, int kSlices, float *__restrict__ partial) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t mbar[STAGES];
   __shared__ uint32_t tmem_slot;
@@ -132,7 +134,9 @@ k_gemm_tn(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__
   const uint32_t tmem = tmem_slot;
   constexpr uint32_t idesc = instr_desc(BM, BN);
 
-  const int KT = (int)(K / BK);
+  const int KTall = (int)(K / BK);
+  const int kBegin = (int)blockIdx.z * kSlices;
+  const int KT = max(0, min(kSlices, KTall - kBegin));
   for (int kt = 0; kt < KT; ++kt) {
     const int st = kt & 1;
     const uint32_t sA = sbase + (uint32_t)(st * 2 * TILE_BYTES), sB = sA + TILE_BYTES;
@@ -142,8 +146,8 @@ k_gemm_tn(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__
       __syncthreads();
       if (abort_flag) break;
     }
-    load_slice(sA, A, M, K, m0, (long)kt * BK);
-    load_slice(sB, B, N, K, n0, (long)kt * BK);
+    load_slice(sA, A, M, K, m0, (long)(kBegin + kt) * BK);
+    load_slice(sB, B, N, K, n0, (long)(kBegin + kt) * BK);
     asm volatile("cp.async.commit_group;\n" ::: "memory");
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
@@ -188,7 +192,14 @@ k_gemm_tn(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__
             "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-      if (row < M) {
+      if (row < M && partial) {
+        float *pp = partial + (long)blockIdx.z * M * N + row * N;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const long col = n0 + c0 + j;
+          if (col < N) pp[col] = __uint_as_float(r[j]);
+        }
+      } else if (row < M) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const long col = n0 + c0 + j;
@@ -204,6 +215,12 @@ k_gemm_tn(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__
       }
     }
   }
+  if (!abort_flag && KT == 0 && partial) {
+    // an empty split contributes zeros
+    const long row = m0 + warp * 32 + lane;
+    if (row < M)
+      for (long col = n0; col < n0 + BN && col < N; ++col) partial[(long)blockIdx.z * M * N + row * N + col] = 0.f;
+  }
   if (abort_flag && threadIdx.x == 0) atomicExch(err, 1);
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
@@ -211,6 +228,21 @@ k_gemm_tn(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
+}
+
+// sum the split-K partials in split order, then the epilogue of k_gemm_tn
+__global__ void k_splitk_reduce(long M, long N, int splits, const float *__restrict__ partial,
+                                const float *__restrict__ bias, int epi, float *__restrict__ outF,
+                                __nv_bfloat16 *__restrict__ outB, float *__restrict__ preact) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M * N) return;
+  float v = 0.f;
+  for (int z = 0; z < splits; ++z) v += partial[(long)z * M * N + i];
+  if (epi != EPI_NONE) v += bias[i % N];
+  if (preact) preact[i] = v;
+  if (epi == EPI_BIAS_ELU) v = elu(v);
+  if (outF) outF[i] = v;
+  if (outB) outB[i] = __float2bfloat16_rn(v);
 }
 
 }  // namespace tc

@@ -1,0 +1,153 @@
+"""Learned-manifold ROM pieces on the GPU against the CPU oracles:
+
+* autoencoder gradients (tcgen05 BF16 GEMMs, fp32 accumulation) against
+  oracle/mlp_oracle.py replaying the same bf16 roundings in float64 --
+  tolerance: per layer ||g - g_ref|| <= 3e-2 ||g_ref|| (the device accumulates
+  in fp32 and a bf16 rounding on either side may land one bf16 ulp apart), loss
+  within 1e-3;
+* training lowers the loss on a low-rank data set;
+* hyper-reduced LSPG (BDF1, Gauss-Newton) with an affine basis and with an MLP
+  decoder against oracle/lspg_oracle.py on the same sample-mesh problem --
+  latent trajectories within 1e-8 relative (FP64 on both sides, different
+  summation orders in J D and the normal equations); graph replay equals the
+  eager path bit for bit."""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ORACLE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle")
+sys.path.insert(0, ORACLE)
+
+
+def _bf16(torch, a):
+    return torch.from_numpy(np.asarray(a, dtype=np.float32)).cuda().to(torch.bfloat16)
+
+
+@pytest.mark.gpu
+def test_autoencoder_gradients_match_oracle(pda):
+    import torch
+    import mlp_oracle
+    n, k, ha, hb, B = 192, 4, 128, 64, 64
+    ae = pda.AutoEncoder(n, k, ha, hb, seed=3)
+    rng = np.random.default_rng(5)
+    X = rng.normal(0, 0.5, (B, n))
+    Xd = _bf16(torch, X)
+    loss, g = ae.gradients(Xd)
+    Ws, bs = [], []
+    for l in range(6):
+        W, b = ae.layer(l)
+        Ws.append(W.double().cpu().numpy())
+        bs.append(b.double().cpu().numpy())
+    lref, gW, gb = mlp_oracle.loss_and_gradients(Ws, bs, Xd.float().cpu().numpy(), bf16=True)
+    assert abs(loss - lref) <= 1e-3 * lref
+    g = g.double().cpu().numpy()
+    off = 0
+    for l in range(6):
+        o, i = Ws[l].shape
+        gw = g[off: off + o * i].reshape(o, i)
+        off += o * i
+        gbb = g[off: off + o]
+        off += o
+        for got, ref in ((gw, gW[l]), (gbb, gb[l])):
+            nr = np.linalg.norm(ref)
+            if nr == 0:
+                assert np.linalg.norm(got) == 0
+            else:
+                assert np.linalg.norm(got - ref) <= 3e-2 * nr, (l, np.linalg.norm(got - ref) / nr)
+
+
+@pytest.mark.gpu
+def test_autoencoder_training_reduces_loss(pda):
+    import torch
+    n, k = 256, 4
+    rng = np.random.default_rng(0)
+    basis = rng.normal(0, 1, (3, n))
+    coef = rng.uniform(-1, 1, (1024, 3))
+    X = np.tanh(0.5 * coef @ basis)
+    ae = pda.AutoEncoder(n, k, 256, 128, seed=1)
+    losses = ae.train(_bf16(torch, X), batch=128, epochs=60, lr=2e-3, seed=2)
+    assert np.all(np.isfinite(losses))
+    assert losses[-1] < 0.1 * losses[0], losses[[0, -1]]
+    Y, Z = ae.reconstruct(_bf16(torch, X[:200]))
+    err = np.linalg.norm(Y.cpu().numpy() - X[:200]) / np.linalg.norm(X[:200])
+    assert err < 0.2, err
+    assert Z.shape == (200, k)
+
+
+def _sample_problem(pda, oracle, n=24, frac=0.3, seed=0):
+    full = pda.create_full_mesh((n, n), (-5, 5, -5, 5), 7, (False, False))
+    rng = np.random.default_rng(seed)
+    gids = np.sort(rng.choice(n * n, int(frac * n * n), replace=False))
+    sm, st = pda.create_sample_mesh(full, gids)
+    params = {"gravity": 7.0, "coriolis": -2.0, "pulseMagnitude": 0.15}
+    import torch
+    stream = torch.cuda.Stream()
+    ps = pda.create_problem(sm, pda.Swe2d.SlipWall, pda.InviscidFluxReconstruction.Weno5, 1, params, stream=stream)
+    g, x, y, z, _, _ = sm._arrays()
+    om = oracle.mesh_from_arrays(2, 7, g, x, y, z, (sm.dx(), sm.dy(), sm.dz()))
+    po = oracle.problem(om, 3, 0, 2, 1, params)
+    s2st = np.searchsorted(st, gids)
+    return full, sm, st, ps, po, om, s2st, rng
+
+
+@pytest.mark.gpu
+def test_lspg_affine_matches_oracle_and_graph(pda, oracle):
+    import torch
+    import lspg_oracle
+    full, sm, st, ps, po, om, s2st, rng = _sample_problem(pda, oracle)
+    nst = len(st) * 3
+    k = 6
+    uref = np.zeros(nst)
+    uref[0::3] = 1.0
+    phi, _ = np.linalg.qr(rng.normal(0, 1, (nst, k)))
+    phi *= 0.3
+    x0 = np.array([0.1, -0.05, 0.02, 0.0, 0.01, -0.02])
+    dt, steps = 0.01, 4
+    xr, traj = lspg_oracle.lspg_bdf1(po, s2st, lspg_oracle.affine_decoder(uref, phi), x0, dt, steps, iters=8,
+                                     tol=1e-12)
+    rom = pda.LspgRom.affine(ps, s2st, torch.from_numpy(uref).cuda(), torch.from_numpy(phi).cuda())
+    xd = torch.from_numpy(x0).cuda()
+    info = rom.advance_bdf1(xd, dt, steps, gn_iters=8, tol=1e-12, use_graph=False)
+    assert np.allclose(xd.cpu().numpy(), xr, rtol=1e-8, atol=1e-12), (xd.cpu().numpy(), xr)
+    assert info["iters_last_step"] >= 1
+    xg = torch.from_numpy(x0).cuda()
+    rom.advance_bdf1(xg, dt, steps, gn_iters=8, tol=1e-12, use_graph=True)
+    assert torch.equal(xg, xd)
+    y = rom.decode(xd)
+    assert np.allclose(y.cpu().numpy(), uref + phi @ xd.cpu().numpy(), rtol=0, atol=1e-14)
+
+
+@pytest.mark.gpu
+def test_lspg_mlp_decoder_matches_oracle(pda, oracle):
+    import torch
+    import lspg_oracle
+    full, sm, st, ps, po, om, s2st, rng = _sample_problem(pda, oracle, seed=1)
+    nst = len(st) * 3
+    k, h1, h2 = 4, 256, 128
+    W1 = rng.normal(0, 0.5, (h1, k)).astype(np.float32)
+    b1 = rng.normal(0, 0.1, h1).astype(np.float32)
+    W2 = rng.normal(0, 0.1, (h2, h1)).astype(np.float32)
+    b2 = rng.normal(0, 0.1, h2).astype(np.float32)
+    W3 = rng.normal(0, 0.1, (nst, h2)).astype(np.float32)
+    b3 = rng.normal(0, 0.1, nst).astype(np.float32)
+    uref = np.zeros(nst)
+    uref[0::3] = 1.0
+    scale = np.full(nst, 0.05)
+    ts = [torch.from_numpy(a).cuda() for a in (W1, b1, W2, b2, W3, b3)]
+    rom = pda.LspgRom.mlp(ps, s2st, torch.from_numpy(uref).cuda(), torch.from_numpy(scale).cuda(), *ts)
+    x0 = np.array([0.2, -0.1, 0.05, 0.1])
+    # the decoder: float32 on the device, float64 in the oracle
+    y = rom.decode(torch.from_numpy(x0).cuda()).cpu().numpy()
+    dec = lspg_oracle.mlp_decoder(uref, scale, *[a.astype(np.float64) for a in (W1, b1, W2, b2, W3, b3)])
+    yref, _ = dec(x0)
+    assert np.max(np.abs(y - yref)) <= 1e-6 * np.max(np.abs(yref - uref))
+    dt, steps = 0.01, 3
+    xr, _ = lspg_oracle.lspg_bdf1(po, s2st, dec, x0, dt, steps, iters=8, tol=1e-10)
+    xd = torch.from_numpy(x0).cuda()
+    rom.advance_bdf1(xd, dt, steps, gn_iters=8, tol=1e-10, use_graph=True)
+    # float32 decoder evaluation: the latent agrees to the decoder's precision
+    assert np.allclose(xd.cpu().numpy(), xr, rtol=1e-4, atol=1e-6), (xd.cpu().numpy(), xr)

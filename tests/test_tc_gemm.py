@@ -8,7 +8,8 @@ from __future__ import annotations
 
 import pytest
 
-SHAPES = [(128, 128, 64), (256, 384, 128), (200, 130, 192), (96, 12, 64), (256, 1024, 4096), (384, 256, 1024)]
+SHAPES = [(128, 128, 64), (256, 384, 128), (200, 130, 192), (96, 12, 64), (256, 1024, 4096), (384, 256, 1024),
+          (128, 256, 16384), (200, 100, 8192)]  # the last two take the split-K path
 
 
 @pytest.mark.gpu
