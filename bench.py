@@ -394,8 +394,123 @@ def wl_batched_swe(c):
     return batched_swe_workload(c.pda, c.torch, c.stream, c.orc, c.threads)
 
 
+def _rom_module():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("pda_gb300_rom", os.path.join(REPO, "pressio-demoapps_gb300",
+                                                                                 "rom.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int(os.environ.get("PDA_ROM_EPOCHS", 40)),
+               batch=256, lr=1e-3, dt=0.005, rom_ratio=4, gn_iters=3):
+    """Learned-manifold hyper-reduced LSPG on 2D SWE slip wall 256^2: 48
+    Latin-hypercube training points (gravity, coriolis, pulse), 400 FOM
+    snapshots each (SSP-RK3 dt 0.005, batched device FOM), MLP autoencoder
+    latent 12, hidden 256 / 1024, ELU, full-width output, trained on the device
+    (BF16 tcgen05 GEMMs, fp32 accumulation, Adam); sample mesh 1 % of the cells
+    (fixed seed) + WENO5 stencils; LSPG BDF1 with Gauss-Newton (FP64 normal
+    equations) on 8 held-out points; wall time and relative L2 error against
+    the single-point GPU FOM, and the same for POD-LSPG with the same latent
+    size (the method without the learned part)."""
+    R = _rom_module()
+    pda, torch = c.pda, c.torch
+    out = {"config": "swe_slipwall_256^2_weno5_learned_lspg_bdf1_latent12", "train_points": n_train,
+           "snapshots_per_point": n_snap, "test_points": n_test, "latent": latent, "epochs": epochs,
+           "dt_fom": dt, "dt_rom": dt * rom_ratio, "gn_iters_max": gn_iters}
+    setup = R.SweSetup(pda, n)
+    train = R.latin_hypercube(n_train, seed=5)
+    test = R.uniform_points(n_test, seed=6)
+    t0 = time.perf_counter()
+    S = setup.snapshots(train, dt, n_snap)
+    torch.cuda.synchronize()
+    out["snapshots_s"] = time.perf_counter() - t0
+    scale = setup.normalization(S)
+    X = setup.training_data(S, scale)
+    phi = R.pod_basis(S, setup.uref, latent)
+    del S
+    torch.cuda.empty_cache()
+    ae = pda.AutoEncoder(setup.N, latent, 1024, 256, seed=1, stream=setup.stream)
+    t0 = time.perf_counter()
+    losses = R.train_schedule(ae, X, epochs, batch=batch, lr=lr, seed=2)
+    out["train_s"] = time.perf_counter() - t0
+    out["loss_first_last"] = [float(losses[0]), float(losses[-1])]
+    del X
+    torch.cuda.empty_cache()
+    learned = R.LearnedRom(setup, ae, scale)
+    sm, gids, st, s2st = setup.sample_mesh(0.01, seed=7)
+    out["sample_cells"], out["stencil_cells"] = int(len(gids)), int(len(st))
+    fdec, _fp = learned.full_decoder()
+    fp_aff = setup.problem({"gravity": 9.8, "coriolis": -3.0, "pulseMagnitude": 0.125})
+    faff = pda.LspgRom.affine(fp_aff, np.arange(n * n), setup.uref, phi)
+    checkpoints = [100, 200, 300, 400]
+    rom_cps = [cp // rom_ratio for cp in checkpoints]
+
+    def run_point(p, rom_kind):
+        ps = setup.problem(p, mesh=sm)
+        U0 = setup.problem(p).initialCondition()
+        if rom_kind == "learned":
+            rom, x0, dec = learned.lspg(ps, s2st, st), learned.encode(U0), fdec
+        else:
+            rom, x0, dec = R.affine_lspg(setup, phi, ps, s2st, st), (phi.T @ (U0 - setup.uref)).contiguous(), faff
+        lat, wall, maxres = R.run_rom(rom, x0, dt * rom_ratio, rom_cps, setup.stream, gn_iters=gn_iters, tol=1e-8)
+        return lat, wall, maxres, dec
+
+    # residual threshold for the FOM fallback: 5x the largest residual seen on a training point
+    _, _, res_train, _ = run_point(train[0], "learned")
+    threshold = 5.0 * res_train
+    out["fallback_residual_threshold"] = threshold
+    pts = []
+    for p in test:
+        states, fom_wall = setup.fom_trajectory(p, dt, checkpoints)
+        rec = {"params": p, "fom_s": fom_wall}
+        for kind in ("learned", "pod"):
+            lat, wall, maxres, dec = run_point(p, kind)
+            errs = [R.rel_l2(dec.decode(lat[cp // rom_ratio]), states[cp]) for cp in checkpoints]
+            errp = [R.rel_l2(dec.decode(lat[cp // rom_ratio]), states[cp], setup.uref) for cp in checkpoints]
+            rec[kind] = {"rom_s": wall, "speedup": fom_wall / wall, "rel_l2_state": errs,
+                         "rel_l2_perturbation": errp, "max_residual": maxres}
+        rec["learned"]["fallback"] = bool(rec["learned"]["max_residual"] > threshold)
+        pts.append(rec)
+    out["points"] = pts
+    L = [q["learned"] for q in pts]
+    P = [q["pod"] for q in pts]
+    fom = [q["fom_s"] for q in pts]
+    out["summary"] = {
+        "fom_s_per_point": float(np.mean(fom)),
+        "rom_s_per_point": float(np.mean([q["rom_s"] for q in L])),
+        "speedup": float(np.sum(fom) / np.sum([q["rom_s"] for q in L])),
+        "rel_l2_state_final_mean": float(np.mean([q["rel_l2_state"][-1] for q in L])),
+        "rel_l2_state_max": float(np.max([max(q["rel_l2_state"]) for q in L])),
+        "rel_l2_perturbation_final_mean": float(np.mean([q["rel_l2_perturbation"][-1] for q in L])),
+        "pod_rel_l2_state_final_mean": float(np.mean([q["rel_l2_state"][-1] for q in P])),
+        "pod_rel_l2_perturbation_final_mean": float(np.mean([q["rel_l2_perturbation"][-1] for q in P])),
+        "pod_speedup": float(np.sum(fom) / np.sum([q["rom_s"] for q in P])),
+        "fallbacks": int(sum(q["fallback"] for q in L)),
+    }
+    if c.orc is not None:
+        # the FOM on the host cores (oracle), one point, a bounded number of steps
+        import tempfile
+        d = tempfile.mkdtemp()
+        setup.mesh.write(d)
+        om = c.orc.mesh_load(d)
+        op = c.orc.problem(om, 3, 0, 2, 1, test[0])
+        Uo = op.initial_condition()
+        t0 = time.perf_counter()
+        op.ssprk3(Uo, 0.0, dt, 20)
+        cw = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": cw / 20 * n_snap, "unit": "s per FOM trajectory (400 steps)",
+                               "cores": c.threads, "kind": "port",
+                               "sample": f"20 SSP-RK3 steps of one test point on the host, {cw:.2f} s, x20"}
+    del ae, learned, fdec, faff
+    torch.cuda.empty_cache()
+    return out
+
+
 WORKLOADS = {"jacobian_2d": wl_jacobian_2d, "velocity_3d": wl_velocity_3d, "jacobian_3d": wl_jacobian_3d,
-             "sod_1d_ssprk3": wl_sod_1d_ssprk3, "ssprk3_3d": wl_ssprk3_3d, "batched_swe": wl_batched_swe}
+             "sod_1d_ssprk3": wl_sod_1d_ssprk3, "ssprk3_3d": wl_ssprk3_3d, "batched_swe": wl_batched_swe,
+             "rom_swe": wl_rom_swe}
 
 
 def extra_workloads(pda, torch, stream, cpu=True, names=None):

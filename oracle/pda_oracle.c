@@ -715,8 +715,11 @@ static void fill_ghosts(const orc_problem *p, int64_t r, const double *U, double
       for (int layer = 0; layer < L; ++layer) {
         if (same[layer] != -1) continue;
         int src = cell;
-        if (p->fam == E1) {
-          /* Ghost1dNeumannFiller */
+        const int sedovSym = p->fam == E2 && p->prob == 3;
+        const int normalShock = p->fam == E2 && p->prob == 5;
+        if (p->fam == E1 || sedovSym || normalShock) {
+          /* Ghost1dNeumannFiller; Sedov2dSymmetryGhostFiller
+             (euler_2d_ghost_filler_sedov2d_sym.hpp:87-206) */
           src = layer == 0 ? cell : opp[layer - 1];
         } else {
           /* Ghost2dNeumannFiller / InviscidWallFiller */
@@ -732,6 +735,10 @@ static void fill_ghosts(const orc_problem *p, int64_t r, const double *U, double
         for (int d = 0; d < nd; ++d) {
           double v = U[(int64_t)src * nd + d];
           if (p->fam == SW && d == (ax == 0 ? 1 : 2)) v = -v;
+          /* Sedov symmetry: reflective on the left (x momentum) and bottom (y momentum) */
+          if (sedovSym && minus && d == (ax == 0 ? 1 : 2)) v = -v;
+          /* normal shock: reflective top and bottom (y momentum) */
+          if (normalShock && ax == 1 && d == 2) v = -v;
           g[layer * nd + d] = v;
         }
       }
@@ -898,6 +905,7 @@ orc_problem *orc_problem_create(const orc_mesh *m, int family, int problem, int 
     const double v = vals[i];
     if (family == E2) {
       if (!strcmp(s, "gamma")) p->gamma = v;
+      else if (!strcmp(s, "mach")) p->icp[0] = v;
       else if (!strcmp(s, "riemannTopRightPressure")) p->icp[p->ic == 1 ? 4 : 5] = v;
       else if (!strcmp(s, "riemannTopRightXVel")) p->icp[6] = v;
       else if (!strcmp(s, "riemannTopRightYVel")) p->icp[7] = v;
@@ -993,6 +1001,59 @@ void orc_initial_condition(const orc_problem *p, double *U) {
     } else if (p->prob == 4) {
       const double a[4][4] = {{0.5313, 0, 0, p->icp[4]}, {1, 0.7276, 0, 1}, {0.8, 0, 0, 1}, {1, 0, 0.7276, 1}};
       memcpy(st, a, sizeof a);
+    }
+    if (p->prob == 1) {
+      /* KelvinHelmholtzIC, impl/euler_2d_initial_condition.hpp:87-125 */
+      const double gm1 = gamma - 1.;
+      for (int64_t i = 0; i < m->nst; ++i) {
+        const double freq = 4., mag = 0.025;
+        const double pert = mag * cos(2. * 3.14159265 / 10. * freq * x[i]);
+        double *u = U + i * 4;
+        if (y[i] > -2 + pert && y[i] < 2 + pert) { u[0] = 2.; u[1] = u[0] * 0.5; u[2] = 0.; }
+        else { u[0] = 1.; u[1] = -u[0] * 0.5; u[2] = 0.; }
+        u[3] = 2.5 / (gm1) + 0.5 / u[0] * (u[1] * u[1] + u[2] * u[2]);
+      }
+      return;
+    }
+    if (p->prob == 5) {
+      /* normalShock2dIC (impl/euler_2d_initial_condition.hpp:391-436),
+         Rankine-Hugoniot relations (impl/euler_rankine_hugoniot.hpp:55-145) */
+      const double one = 1., two = 2., six = 6., half = one / two;
+      const double xShock = one / six, gm1i = one / (gamma - one), M = p->icp[0];
+      const double pre[4] = {gamma, 0., 0., one};
+      const double M2 = M * M;
+      const double rhoPost = pre[0] * (gamma + one) * M2 / (two + (gamma - one) * M2);
+      const double pPost = pre[3] * (one + two * gamma / (gamma + one) * (M2 - one));
+      const double aPre = sqrt(gamma * pre[3] / pre[0]), aPost = sqrt(gamma * pPost / rhoPost);
+      const double machRel = sqrt((one + half * (gamma - one) * M2) / (gamma * M2 - half * (gamma - one)));
+      const double velPost = machRel * aPost - M * aPre + 0.;
+      const double post[4] = {rhoPost, -velPost * cos(0.), -velPost * sin(0.), pPost};
+      for (int64_t i = 0; i < m->nst; ++i) {
+        const double *q = x[i] < xShock ? post : pre;
+        U[i * 4] = q[0];
+        U[i * 4 + 1] = q[0] * q[1];
+        U[i * 4 + 2] = q[0] * q[2];
+        U[i * 4 + 3] = energy(gm1i, q, 4);
+      }
+      return;
+    }
+    if (p->prob == 2 || p->prob == 3) {
+      /* sedov2dIC / sedov2dsymmetryIC, impl/euler_2d_initial_condition.hpp:131-249 */
+      const double one = 1., two = 2., gm1 = gamma - one, gm1i = one / gm1;
+      const double dx = m->dx[0], dy = m->dx[1];
+      const int sym = p->prob == 3;
+      const double sRad = sym ? 3. * (dx < dy ? dx : dy) : two * (dx < dy ? dx : dy);
+      for (int64_t i = 0; i < m->nst; ++i) {
+        const double myR = sqrt(x[i] * x[i] + y[i] * y[i]);
+        prim[0] = one; prim[1] = 0.; prim[2] = 0.;
+        if (myR <= sRad) prim[3] = sym ? gm1 * 0.851072 / (M_PI * sRad * sRad) : (gm1) / (M_PI * sRad * sRad);
+        else prim[3] = sym ? 2.5e-5 : 5.e-5;
+        U[i * 4] = prim[0];
+        U[i * 4 + 1] = prim[0] * prim[1];
+        U[i * 4 + 2] = prim[0] * prim[2];
+        U[i * 4 + 3] = energy(gm1i, prim, 4);
+      }
+      return;
     }
     for (int64_t i = 0; i < m->nst; ++i) {
       if (p->prob == 0) {
@@ -1156,6 +1217,12 @@ static void row_vj_near(const orc_problem *p, int64_t r, const double *U, double
     flux_jac(p, ax, JRN, JRP, st1 + nd, st1 + 2 * nd);
     double fac[5] = {1, 1, 1, 1, 1};
     if (p->fam == SW) fac[ax == 0 ? 1 : 2] = -1;
+    if (p->fam == E2 && p->prob == 3) {
+      /* fillJacFactorsForCellBd, euler_2d_prob_class.hpp:1129-1148 */
+      if (ax == 0 && G(m, r, colm(2, 0, 0)) == -1) fac[1] = -1;
+      else if (ax == 1 && G(m, r, colm(2, 1, 0)) == -1) fac[2] = -1;
+    }
+    if (p->fam == E2 && p->prob == 5 && ax == 1) fac[2] = -1; /* euler_2d_prob_class.hpp:1150-1162 */
     const int32_t l0 = G(m, r, colm(p->dim, ax, 0)), r0 = G(m, r, colp(p->dim, ax, 0)), ci = G(m, r, 0);
     for (int k = 0; k < nd; ++k)
       for (int j = 0; j < nd; ++j) JADD(r * nd + k, ci * nd + j, (JLP[k * nd + j] - JRN[k * nd + j]) * hinv);

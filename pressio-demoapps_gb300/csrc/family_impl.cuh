@@ -87,8 +87,16 @@ void rows_vj_inner(int scheme, const RowTable &t, const MeshArgs &m, const Phys 
   const int g = div_up(t.nrows, 64);
   switch (scheme) {
     case FirstOrder: k_rows_vj_inner<FAM, FirstOrder><<<g, 64, 0, s>>>(t, m, p, U, rowptr, V, J); break;
-    case Weno3: k_rows_vj_inner<FAM, Weno3><<<g, 64, 0, s>>>(t, m, p, U, rowptr, V, J); break;
-    default: k_rows_vj_inner<FAM, Weno5><<<g, 64, 0, s>>>(t, m, p, U, rowptr, V, J); break;
+    case Weno3: {
+      using RP = RowPar<FAM, Weno3>;
+      k_rows_vj_inner_par<FAM, Weno3><<<div_up(t.nrows, RP::RPB), RP::THREADS, 0, s>>>(t, m, p, U, rowptr, V, J);
+      break;
+    }
+    default: {
+      using RP = RowPar<FAM, Weno5>;
+      k_rows_vj_inner_par<FAM, Weno5><<<div_up(t.nrows, RP::RPB), RP::THREADS, 0, s>>>(t, m, p, U, rowptr, V, J);
+      break;
+    }
   }
 }
 
@@ -96,10 +104,13 @@ void rows_vj_nearbd(int scheme, const RowTable &t, const MeshArgs &m, const Phys
                     const int *rowptr, double *V, double *J, cudaStream_t s) {
   if (t.nrows <= 0) return;
   const int g = div_up(t.nrows, 64);
+  (void)g;
+  const int gp = div_up(t.nrows, NearPar<FAM>::RPB);
+  constexpr int tp = NearPar<FAM>::THREADS;
   switch (scheme) {
-    case FirstOrder: k_rows_vj_nearbd<FAM, FirstOrder><<<g, 64, 0, s>>>(t, m, p, U, rowptr, V, J); break;
-    case Weno3: k_rows_vj_nearbd<FAM, Weno3><<<g, 64, 0, s>>>(t, m, p, U, rowptr, V, J); break;
-    default: k_rows_vj_nearbd<FAM, Weno5><<<g, 64, 0, s>>>(t, m, p, U, rowptr, V, J); break;
+    case FirstOrder: k_rows_vj_nearbd_par<FAM, FirstOrder><<<gp, tp, 0, s>>>(t, m, p, U, rowptr, V, J); break;
+    case Weno3: k_rows_vj_nearbd_par<FAM, Weno3><<<gp, tp, 0, s>>>(t, m, p, U, rowptr, V, J); break;
+    default: k_rows_vj_nearbd_par<FAM, Weno5><<<gp, tp, 0, s>>>(t, m, p, U, rowptr, V, J); break;
   }
 }
 

@@ -386,6 +386,242 @@ k_rows_vj_inner(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U,
   for (int d = 0; d < NDPC; ++d) V[(size_t)r * NDPC + d] = v[d];
 }
 
+// ---------------------------------------------------------------------------
+// V and J of inner rows with the faces of each row computed in parallel:
+// thread (row, face) evaluates one face (WENO value + gradient, flux, flux
+// Jacobians) into shared memory; thread (row, k) then forms dof k of V and
+// row k of the row's J block, accumulating every entry in a local array in
+// exactly the order of k_rows_vj_inner (axes, then per column dof j: left
+// face Neg / Pos over the stencil slots, then right face), and writes each
+// CSR value once.  Bit-identical to k_rows_vj_inner (WENO3 / WENO5); built
+// for sample meshes, whose few rows make the per-row serial formulation and
+// its global read-modify-write chains latency-bound.
+// ---------------------------------------------------------------------------
+template <int FAM, int SCHEME> struct RowFace {
+  static constexpr int NDPC = Fam<FAM>::ndpc, G = 2 * SchemeTraits<SCHEME>::h;
+  double fl[NDPC];
+  double JN[NDPC * NDPC], JP[NDPC * NDPC];
+  double gN[NDPC][G], gP[NDPC][G];
+  double uN[NDPC], uP[NDPC];
+};
+
+template <int FAM, int SCHEME> struct RowPar {
+  static constexpr int NF = 2 * Fam<FAM>::dim, NDPC = Fam<FAM>::ndpc;
+  // few rows per block: sample meshes have few rows and GB300's FP64 units
+  // are narrow, so the rows are spread over as many SMs as possible
+  static constexpr int RPB = 4;
+  static constexpr int THREADS = RPB * NF * NDPC;  // phase 1a: one thread per (row, face, dof)
+};
+
+template <int FAM, int SCHEME>
+__global__ void __launch_bounds__(RowPar<FAM, SCHEME>::THREADS)
+k_rows_vj_inner_par(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U, const int *__restrict__ rowptr,
+                    double *__restrict__ V, double *__restrict__ J) {
+  using F = Fam<FAM>;
+  using RF = RowFace<FAM, SCHEME>;
+  constexpr int NDPC = F::ndpc, DIM = F::dim, H = SchemeTraits<SCHEME>::h, S = 2 * H + 1, G = 2 * H;
+  constexpr int NF = RowPar<FAM, SCHEME>::NF, RPB = RowPar<FAM, SCHEME>::RPB;
+  constexpr int NB = 1 + 2 * DIM * H;  // distinct column blocks of an inner row at most
+  __shared__ RF fd[RPB][NF];
+  const int tid = threadIdx.x;
+  {  // phase 1a: one (face, dof) per thread: reconstruction and its gradient
+    const int rl = tid / (NF * NDPC), f = (tid / NDPC) % NF, d = tid % NDPC, ax = f >> 1, side = f & 1;
+    const int e = blockIdx.x * RPB + rl;
+    if (e < t.nrows) {
+      double q[G][1];
+      const size_t base = ((size_t)e * DIM + ax) * S;
+#pragma unroll
+      for (int s = 0; s < G; ++s) q[s][0] = __ldg(U + (size_t)t.src[base + side + s] * NDPC + d);
+      RF &o = fd[rl][f];
+      double uN[1], uP[1], gN[1][G], gP[1][G];
+      reconstruct_face_grad<1, SCHEME>(uN, uP, gN, gP, q);
+      o.uN[d] = uN[0];
+      o.uP[d] = uP[0];
+#pragma unroll
+      for (int s = 0; s < G; ++s) {
+        o.gN[d][s] = gN[0][s];
+        o.gP[d][s] = gP[0][s];
+      }
+    }
+  }
+  __syncthreads();
+  if (tid < RPB * NF) {  // phase 1b: one face per thread: flux and flux Jacobians
+    const int rl = tid / NF, f = tid % NF, ax = f >> 1;
+    const int e = blockIdx.x * RPB + rl;
+    if (e < t.nrows) {
+      RF &o = fd[rl][f];
+      double uN[NDPC], uP[NDPC];
+#pragma unroll
+      for (int d = 0; d < NDPC; ++d) {
+        uN[d] = o.uN[d];
+        uP[d] = o.uP[d];
+      }
+      if (ax == 0) { F::template flux<0>(o.fl, uN, uP, p); F::template flux_jac<0>(o.JN, o.JP, uN, uP, p); }
+      if constexpr (DIM > 1) if (ax == 1) { F::template flux<1>(o.fl, uN, uP, p); F::template flux_jac<1>(o.JN, o.JP, uN, uP, p); }
+      if constexpr (DIM > 2) if (ax == 2) { F::template flux<2>(o.fl, uN, uP, p); F::template flux_jac<2>(o.JN, o.JP, uN, uP, p); }
+    }
+  }
+  __syncthreads();
+  // phase 2: thread (row, k)
+  for (int w = tid; w < RPB * NDPC; w += blockDim.x) {
+    const int rl = w / NDPC, k = w % NDPC;
+    const int e = blockIdx.x * RPB + rl;
+    if (e >= t.nrows) continue;
+    const int r = t.rows[e];
+    double vk = 0.;
+#pragma unroll
+    for (int ax = 0; ax < DIM; ++ax) vk += m.hinv[ax] * (fd[rl][2 * ax].fl[k] - fd[rl][2 * ax + 1].fl[k]);
+    double acc[NB * NDPC];
+#pragma unroll
+    for (int i = 0; i < NB * NDPC; ++i) acc[i] = 0.;
+#pragma unroll 1
+    for (int ax = 0; ax < DIM; ++ax) {
+      const double hinv = m.hinv[ax];
+      const size_t base = ((size_t)e * DIM + ax) * S;
+      int blk[S];
+#pragma unroll
+      for (int s = 0; s < S; ++s) blk[s] = t.jpos[base + s] / NDPC;
+      const RF &L = fd[rl][2 * ax], &R = fd[rl][2 * ax + 1];
+#pragma unroll 1
+      for (int j = 0; j < NDPC; ++j) {
+        const double ln = L.JN[k * NDPC + j], lp = L.JP[k * NDPC + j];
+        const double rn = R.JN[k * NDPC + j], rp = R.JP[k * NDPC + j];
+#pragma unroll
+        for (int s = 0; s < G; ++s) {
+          acc[blk[s] * NDPC + j] += ln * L.gN[j][s] * hinv;
+          acc[blk[s] * NDPC + j] += lp * L.gP[j][s] * hinv;
+        }
+#pragma unroll
+        for (int s = 0; s < G; ++s) {
+          acc[blk[s + 1] * NDPC + j] -= rn * R.gN[j][s] * hinv;
+          acc[blk[s + 1] * NDPC + j] -= rp * R.gP[j][s] * hinv;
+        }
+      }
+    }
+    if constexpr (FAM == Swe2d) {
+      // swe_2d_prob_class.hpp:983-1012
+      const int c = t.cell[e];
+      const double u0 = __ldg(U + (size_t)c * 3), u1 = __ldg(U + (size_t)c * 3 + 1),
+                   u2 = __ldg(U + (size_t)c * 3 + 2);
+      if (k == 1) vk -= p.coriolis * u2 / u0;
+      if (k == 2) vk += p.coriolis * u1 / u0;
+      const int self = t.jpos[((size_t)e * DIM + 0) * S + H] / NDPC;
+      if (k == 1) {
+        acc[self * 3 + 0] += p.coriolis * u2 / (u0 * u0);
+        acc[self * 3 + 2] += -p.coriolis / u0;
+      }
+      if (k == 2) {
+        acc[self * 3 + 1] += p.coriolis / u0;
+        acc[self * 3 + 0] += -p.coriolis * u1 / (u0 * u0);
+      }
+    }
+    V[(size_t)r * NDPC + k] = vk;
+    const int rb = rowptr[r * NDPC + k];
+    const int n = rowptr[r * NDPC + k + 1] - rb;
+    for (int i = 0; i < n && i < NB * NDPC; ++i) J[rb + i] = acc[i];
+  }
+}
+
+// Near-boundary rows with the faces of each row in parallel (thread per face:
+// the scheme's flux for V and the first-order flux Jacobians for J), then
+// thread (row, k) accumulates row k exactly as k_rows_vj_nearbd does.
+template <int FAM> struct NearFace {
+  static constexpr int NDPC = Fam<FAM>::ndpc;
+  double fl[NDPC];
+  double JN[NDPC * NDPC], JP[NDPC * NDPC];
+};
+
+template <int FAM> struct NearPar {
+  static constexpr int NF = 2 * Fam<FAM>::dim;
+  static constexpr int RPB = 4;  // spread the few near-boundary rows over many SMs
+  static constexpr int THREADS = RPB * NF;
+};
+
+template <int FAM, int SCHEME>
+__global__ void __launch_bounds__(NearPar<FAM>::THREADS)
+k_rows_vj_nearbd_par(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U, const int *__restrict__ rowptr,
+                     double *__restrict__ V, double *__restrict__ J) {
+  using F = Fam<FAM>;
+  constexpr int NDPC = F::ndpc, DIM = F::dim, H = SchemeTraits<SCHEME>::h, S = 2 * H + 1, G = 2 * H;
+  constexpr int NF = NearPar<FAM>::NF, RPB = NearPar<FAM>::RPB, NB = 1 + 2 * DIM;
+  __shared__ NearFace<FAM> fd[RPB][NF];
+  const int tid = threadIdx.x;
+  {
+    const int rl = tid / NF, f = tid % NF, ax = f >> 1, side = f & 1;
+    const int e = blockIdx.x * RPB + rl;
+    if (e < t.nrows) {
+      NearFace<FAM> &o = fd[rl][f];
+      double q[G][NDPC];
+      const size_t base = ((size_t)e * DIM + ax) * S;
+#pragma unroll
+      for (int s = 0; s < G; ++s)
+        load_cell<NDPC>(q[s], U, t.src[base + side + s], t.flip[base + side + s], m.reflect[ax]);
+      double uN[NDPC], uP[NDPC];
+      reconstruct_face<NDPC, SCHEME>(uN, uP, q);
+      double q1[2][NDPC];
+      const size_t b1 = ((size_t)e * DIM + ax) * 3;
+#pragma unroll
+      for (int s = 0; s < 2; ++s)
+        load_cell<NDPC>(q1[s], U, t.src1[b1 + side + s], t.flip1[b1 + side + s], m.reflect[ax]);
+      if (ax == 0) { F::template flux<0>(o.fl, uN, uP, p); F::template flux_jac<0>(o.JN, o.JP, q1[0], q1[1], p); }
+      if constexpr (DIM > 1) if (ax == 1) { F::template flux<1>(o.fl, uN, uP, p); F::template flux_jac<1>(o.JN, o.JP, q1[0], q1[1], p); }
+      if constexpr (DIM > 2) if (ax == 2) { F::template flux<2>(o.fl, uN, uP, p); F::template flux_jac<2>(o.JN, o.JP, q1[0], q1[1], p); }
+    }
+  }
+  __syncthreads();
+  for (int w = tid; w < RPB * NDPC; w += blockDim.x) {
+    const int rl = w / NDPC, k = w % NDPC;
+    const int e = blockIdx.x * RPB + rl;
+    if (e >= t.nrows) continue;
+    const int r = t.rows[e];
+    double vk = 0.;
+#pragma unroll
+    for (int ax = 0; ax < DIM; ++ax) vk += m.hinv[ax] * (fd[rl][2 * ax].fl[k] - fd[rl][2 * ax + 1].fl[k]);
+    double acc[NB * NDPC];
+#pragma unroll
+    for (int i = 0; i < NB * NDPC; ++i) acc[i] = 0.;
+#pragma unroll 1
+    for (int ax = 0; ax < DIM; ++ax) {
+      const double hinv = m.hinv[ax];
+      const size_t b1 = ((size_t)e * DIM + ax) * 3;
+      const int pl = t.jpos1[b1 + 0], pc = t.jpos1[b1 + 1], pr = t.jpos1[b1 + 2];
+      const int bl = pl / NDPC, bc = pc / NDPC, br = pr / NDPC;
+      const double *fac = t.jfac + ((size_t)e * DIM + ax) * NDPC;
+      const NearFace<FAM> &L = fd[rl][2 * ax], &R = fd[rl][2 * ax + 1];
+      // JLN = L.JN, JLP = L.JP, JRN = R.JN, JRP = R.JP
+      for (int j = 0; j < NDPC; ++j) acc[bc * NDPC + j] += (L.JP[k * NDPC + j] - R.JN[k * NDPC + j]) * hinv;
+      if (pl >= 0)
+        for (int j = 0; j < NDPC; ++j) acc[bl * NDPC + j] += L.JN[k * NDPC + j] * hinv;
+      if (pr >= 0)
+        for (int j = 0; j < NDPC; ++j) acc[br * NDPC + j] += -R.JP[k * NDPC + j] * hinv;
+      if (pl < 0)
+        for (int j = 0; j < NDPC; ++j) acc[bc * NDPC + j] += (fac[j] * L.JN[k * NDPC + j]) * hinv;
+      if (pr < 0)
+        for (int j = 0; j < NDPC; ++j) acc[bc * NDPC + j] += (fac[j] * -R.JP[k * NDPC + j]) * hinv;
+    }
+    if constexpr (FAM == Swe2d) {
+      const int c = t.cell[e];
+      const double u0 = __ldg(U + (size_t)c * 3), u1 = __ldg(U + (size_t)c * 3 + 1),
+                   u2 = __ldg(U + (size_t)c * 3 + 2);
+      if (k == 1) vk -= p.coriolis * u2 / u0;
+      if (k == 2) vk += p.coriolis * u1 / u0;
+      const int self = t.jpos1[((size_t)e * DIM + 0) * 3 + 1] / 3;
+      if (k == 1) {
+        acc[self * 3 + 0] += p.coriolis * u2 / (u0 * u0);
+        acc[self * 3 + 2] += -p.coriolis / u0;
+      }
+      if (k == 2) {
+        acc[self * 3 + 1] += p.coriolis / u0;
+        acc[self * 3 + 0] += -p.coriolis * u1 / (u0 * u0);
+      }
+    }
+    V[(size_t)r * NDPC + k] = vk;
+    const int rb = rowptr[r * NDPC + k];
+    const int n = rowptr[r * NDPC + k + 1] - rb;
+    for (int i = 0; i < n && i < NB * NDPC; ++i) J[rb + i] = acc[i];
+  }
+}
+
 // V and J for rows near a non-periodic boundary: V with the scheme's stencil
 // (ghosts folded into the table), J first order with the ghost dependence
 // folded into the diagonal block by the BC factors
@@ -398,12 +634,15 @@ k_rows_vj_nearbd(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U,
                  const int *__restrict__ rowptr, double *__restrict__ V, double *__restrict__ J) {
   using F = Fam<FAM>;
   constexpr int NDPC = F::ndpc, DIM = F::dim, H = SchemeTraits<SCHEME>::h, S = 2 * H + 1;
+  constexpr int NB = 1 + 2 * DIM;  // column blocks of a first-order row at most
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= t.nrows) return;
   const int r = t.rows[e];
-#pragma unroll 1
-  for (int k = 0; k < NDPC; ++k)
-    for (int q = rowptr[r * NDPC + k]; q < rowptr[r * NDPC + k + 1]; ++q) J[q] = 0.;
+  // the row's CSR values, accumulated locally in the order of the reference's
+  // in-place updates and written once at the end: acc[block][k][j]
+  double acc[NB * NDPC * NDPC];
+#pragma unroll
+  for (int i = 0; i < NB * NDPC * NDPC; ++i) acc[i] = 0.;
   double v[NDPC];
 #pragma unroll
   for (int d = 0; d < NDPC; ++d) v[d] = 0.;
@@ -437,19 +676,24 @@ k_rows_vj_nearbd(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U,
       if constexpr (DIM > 1) if (ax == 1) { F::template flux_jac<1>(JLN, JLP, q[0], q[1], p); F::template flux_jac<1>(JRN, JRP, q[1], q[2], p); }
       if constexpr (DIM > 2) if (ax == 2) { F::template flux_jac<2>(JLN, JLP, q[0], q[1], p); F::template flux_jac<2>(JRN, JRP, q[1], q[2], p); }
       const int pl = t.jpos1[base + 0], pc = t.jpos1[base + 1], pr = t.jpos1[base + 2];
+      const int bl = pl / NDPC, bc = pc / NDPC, br = pr / NDPC;
       const double *fac = t.jfac + ((size_t)e * DIM + ax) * NDPC;
 #pragma unroll 1
       for (int k = 0; k < NDPC; ++k) {
-        const int rb = rowptr[r * NDPC + k];
-        for (int j = 0; j < NDPC; ++j) J[rb + pc + j] += (JLP[k * NDPC + j] - JRN[k * NDPC + j]) * hinv;
-        if (pl >= 0)
-          for (int j = 0; j < NDPC; ++j) J[rb + pl + j] += JLN[k * NDPC + j] * hinv;
-        if (pr >= 0)
-          for (int j = 0; j < NDPC; ++j) J[rb + pr + j] += -JRP[k * NDPC + j] * hinv;
+        double *ac = acc + (bc * NDPC + k) * NDPC;
+        for (int j = 0; j < NDPC; ++j) ac[j] += (JLP[k * NDPC + j] - JRN[k * NDPC + j]) * hinv;
+        if (pl >= 0) {
+          double *al = acc + (bl * NDPC + k) * NDPC;
+          for (int j = 0; j < NDPC; ++j) al[j] += JLN[k * NDPC + j] * hinv;
+        }
+        if (pr >= 0) {
+          double *ar = acc + (br * NDPC + k) * NDPC;
+          for (int j = 0; j < NDPC; ++j) ar[j] += -JRP[k * NDPC + j] * hinv;
+        }
         if (pl < 0)
-          for (int j = 0; j < NDPC; ++j) J[rb + pc + j] += (fac[j] * JLN[k * NDPC + j]) * hinv;
+          for (int j = 0; j < NDPC; ++j) ac[j] += (fac[j] * JLN[k * NDPC + j]) * hinv;
         if (pr < 0)
-          for (int j = 0; j < NDPC; ++j) J[rb + pc + j] += (fac[j] * -JRP[k * NDPC + j]) * hinv;
+          for (int j = 0; j < NDPC; ++j) ac[j] += (fac[j] * -JRP[k * NDPC + j]) * hinv;
       }
     }
   }
@@ -459,15 +703,21 @@ k_rows_vj_nearbd(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U,
                  u2 = __ldg(U + (size_t)c * 3 + 2);
     v[1] -= p.coriolis * u2 / u0;
     v[2] += p.coriolis * u1 / u0;
-    const int self = t.jpos1[((size_t)e * DIM + 0) * 3 + 1];
-    const int rb1 = rowptr[r * 3 + 1], rb2 = rowptr[r * 3 + 2];
-    J[rb1 + self + 0] += p.coriolis * u2 / (u0 * u0);
-    J[rb1 + self + 2] += -p.coriolis / u0;
-    J[rb2 + self + 1] += p.coriolis / u0;
-    J[rb2 + self + 0] += -p.coriolis * u1 / (u0 * u0);
+    const int self = t.jpos1[((size_t)e * DIM + 0) * 3 + 1] / 3;
+    acc[(self * 3 + 1) * 3 + 0] += p.coriolis * u2 / (u0 * u0);
+    acc[(self * 3 + 1) * 3 + 2] += -p.coriolis / u0;
+    acc[(self * 3 + 2) * 3 + 1] += p.coriolis / u0;
+    acc[(self * 3 + 2) * 3 + 0] += -p.coriolis * u1 / (u0 * u0);
   }
 #pragma unroll
   for (int d = 0; d < NDPC; ++d) V[(size_t)r * NDPC + d] = v[d];
+#pragma unroll 1
+  for (int k = 0; k < NDPC; ++k) {
+    const int rb = rowptr[r * NDPC + k];
+    const int nb = (rowptr[r * NDPC + k + 1] - rb) / NDPC;
+    for (int b = 0; b < nb && b < NB; ++b)
+      for (int j = 0; j < NDPC; ++j) J[rb + b * NDPC + j] = acc[(b * NDPC + k) * NDPC + j];
+  }
 }
 
 }  // namespace pda

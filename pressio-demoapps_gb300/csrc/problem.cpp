@@ -182,6 +182,81 @@ void initial_condition(const pda_problem &P, std::vector<double> &st) {
         st[i * 4 + 2] = prim[0] * prim[2];
         st[i * 4 + 3] = energy2(gm1inv, prim, 4);
       }
+    } else if (P.probEnum == 1) {
+      // KelvinHelmholtzIC (impl/euler_2d_initial_condition.hpp:87-125)
+      const double one = 1.;
+      const double gammaMinusOne = gamma - one;
+      for (int64_t i = 0; i < N; ++i) {
+        const double freq = 4.;
+        const double mag = 0.025;
+        const double pert = mag * std::cos(2. * 3.14159265 / 10. * freq * x[i]);
+        double *u = &st[i * 4];
+        if (y[i] > -2 + pert && y[i] < 2 + pert) {
+          u[0] = 2.;
+          u[1] = u[0] * 0.5;
+          u[2] = 0.;
+        } else {
+          u[0] = 1.;
+          u[1] = -u[0] * 0.5;
+          u[2] = 0.;
+        }
+        u[3] = 2.5 / (gammaMinusOne) + 0.5 / u[0] * (u[1] * u[1] + u[2] * u[2]);
+      }
+    } else if (P.probEnum == 2 || P.probEnum == 3) {
+      // sedov2dIC / sedov2dsymmetryIC (impl/euler_2d_initial_condition.hpp:131-249)
+      const double zero = 0., one = 1., two = 2.;
+      const double dx = m.dx[0], dy = m.dx[1];
+      const double gammaMinusOne = gamma - one;
+      const double gammaMinusOneInv = one / gammaMinusOne;
+      const bool sym = P.probEnum == 3;
+      const double sRad = sym ? 3. * std::min(dx, dy) : two * std::min(dx, dy);
+      for (int64_t i = 0; i < N; ++i) {
+        const double diffx = x[i], diffy = y[i];
+        const double myR = std::sqrt(diffx * diffx + diffy * diffy);
+        prim[0] = one;
+        prim[1] = zero;
+        prim[2] = zero;
+        if (myR <= sRad) prim[3] = sym ? gammaMinusOne * 0.851072 / (M_PI * sRad * sRad)
+                                       : (gammaMinusOne) / (M_PI * sRad * sRad);
+        else prim[3] = sym ? 2.5e-5 : 5.e-5;
+        st[i * 4] = prim[0];
+        st[i * 4 + 1] = prim[0] * prim[1];
+        st[i * 4 + 2] = prim[0] * prim[2];
+        st[i * 4 + 3] = energy2(gammaMinusOneInv, prim, 4);
+      }
+    } else if (P.probEnum == 5) {
+      // normalShock2dIC (impl/euler_2d_initial_condition.hpp:391-436) with the
+      // Rankine-Hugoniot relations of impl/euler_rankine_hugoniot.hpp:55-145
+      const double zero = 0., one = 1., two = 2., six = 6.;
+      const double angle = zero, xShock = one / six;
+      const double gammaMinusOne = gamma - one, gammaMinusOneInv = one / gammaMinusOne;
+      const double machShock = P.icParams[0];
+      double pre[4] = {gamma, zero, zero, one}, post[4];
+      {
+        const double sinA = std::sin(angle), cosA = std::cos(angle);
+        const double rhoPre = pre[0], velPre = zero, pPre = pre[3];
+        const double machShockSq = machShock * machShock;
+        const double rhoPost = rhoPre * (gamma + one) * machShockSq / (two + (gamma - one) * machShockSq);
+        const double pPost = pPre * (one + two * gamma / (gamma + one) * (machShockSq - one));
+        const double aPre = std::sqrt(gamma * pPre / rhoPre);
+        const double aPost = std::sqrt(gamma * pPost / rhoPost);
+        const double half = one / two;
+        const double num = (one + half * (gamma - one) * machShockSq);
+        const double den = gamma * machShockSq - half * (gamma - one);
+        const double machRelPost = std::sqrt(num / den);
+        const double velPost = machRelPost * aPost - machShock * aPre + velPre;
+        post[0] = rhoPost;
+        post[1] = -velPost * cosA;
+        post[2] = -velPost * sinA;
+        post[3] = pPost;
+      }
+      for (int64_t i = 0; i < N; ++i) {
+        const double *q = x[i] < xShock ? post : pre;
+        st[i * 4] = q[0];
+        st[i * 4 + 1] = q[0] * q[1];
+        st[i * 4 + 2] = q[0] * q[2];
+        st[i * 4 + 3] = energy2(gammaMinusOneInv, q, 4);
+      }
     } else if (P.probEnum == 8) {
       // testingonlyneumann: no initial condition (zeros)
     } else {
@@ -251,7 +326,9 @@ int ghost_source(const Mesh &m, int bc, int64_t r, int ax, bool minusSide, int L
     return m.g(r, minusSide ? col_plus(m.dim, ax, k) : col_minus(m.dim, ax, k));
   };
   const int cell = m.g(r, 0);
-  if (bc == BC_NEUMANN1D) {
+  if (bc == BC_NEUMANN1D || bc == BC_SEDOVSYM || bc == BC_NORMALSHOCK) {
+    // euler_1d_ghost_filler.hpp:104-142, euler_2d_ghost_filler_sedov2d_sym.hpp:87-206,
+    // euler_2d_ghost_filler_normal_shock.hpp:87-205
     if (L == 0) return cell;
     return opp(L - 1);
   }
@@ -266,6 +343,15 @@ int ghost_source(const Mesh &m, int bc, int64_t r, int ax, bool minusSide, int L
     return ind;
   }
   throw Error(PDA_ERR_UNSUPPORTED, "this problem has no ghost-cell rule for meshes with boundaries");
+}
+
+// whether a ghost on this side negates the face-normal momentum (the mesh
+// args' reflect dof): walls of the slip-wall problem on every side, the
+// Sedov symmetry planes on the left and bottom (minus) sides only
+uint8_t ghost_flip(int bc, int ax, bool minusSide) {
+  if (bc == BC_SEDOVSYM) return minusSide ? 1 : 0;
+  if (bc == BC_NORMALSHOCK) return ax == 1 ? 1 : 0;
+  return 1;
 }
 
 // Stencil of the scheme (positions -h..h) for every row of the table.
@@ -295,7 +381,7 @@ void build_stencil(const pda_problem &P, Table &T, const std::vector<int32_t> &r
             PDA_REQUIRE(gsrc >= 0, PDA_ERR_INVALID_ARGUMENT,
                         "mesh too small for the ghost layers of this scheme");
             T.src[pos] = gsrc;
-            T.flip[pos] = 1;
+            T.flip[pos] = ghost_flip(P.bc, ax, minus);
           }
         }
       }
@@ -361,9 +447,18 @@ int block_offset(const pda_problem &P, int64_t r, int32_t cell) {
 
 // BC factors of fillJacFactorsForCellBd (euler_2d_prob_class.hpp:1115-1129,
 // swe_2d_prob_class.hpp:839-854; 1d all ones, euler_1d_prob_class.hpp:608-610)
-void jac_factors(const pda_problem &P, int ax, double *f) {
+void jac_factors(const pda_problem &P, int64_t r, int ax, double *f) {
   for (int j = 0; j < P.ndpc; ++j) f[j] = 1.;
   if (P.family == PDA_SWE2D) f[ax == 0 ? 1 : 2] = -1.;
+  if (P.bc == BC_SEDOVSYM) {
+    // euler_2d_prob_class.hpp:1129-1148: reflective factors on the axis of a
+    // left / bottom boundary, Neumann otherwise
+    const Mesh &m = *P.mesh;
+    if (ax == 0 && m.g(r, col_minus(2, 0, 0)) == -1) f[1] = -1.;
+    else if (ax == 1 && m.g(r, col_minus(2, 1, 0)) == -1) f[2] = -1.;
+  }
+  // euler_2d_prob_class.hpp:1150-1162: reflective along y, Neumann along x
+  if (P.bc == BC_NORMALSHOCK && ax == 1) f[2] = -1.;
 }
 
 void build_inner_table(pda_problem &P, bool withJ) {
@@ -413,16 +508,16 @@ void build_near_table(pda_problem &P, bool withJ) {
         T.jpos1[base] = block_offset(P, r, cm);
       } else {
         T.src1[base] = ghost_source(m, P.bc, r, ax, true, 0);
-        T.flip1[base] = 1;
+        T.flip1[base] = ghost_flip(P.bc, ax, true);
       }
       if (cp != -1) {
         T.src1[base + 2] = cp;
         T.jpos1[base + 2] = block_offset(P, r, cp);
       } else {
         T.src1[base + 2] = ghost_source(m, P.bc, r, ax, false, 0);
-        T.flip1[base + 2] = 1;
+        T.flip1[base + 2] = ghost_flip(P.bc, ax, false);
       }
-      jac_factors(P, ax, &T.jfac[(e * P.dim + ax) * P.ndpc]);
+      jac_factors(P, r, ax, &T.jfac[(e * P.dim + ax) * P.ndpc]);
     }
   }
   T.dirty = true;
@@ -493,13 +588,31 @@ void velocity_and_jacobian(pda_problem &P, const double *U, double *V, double *J
   pattern_to_device(P);
   P.innerT.sync();
   P.nearT.sync();
+  const bool both = P.innerT.t.nrows > 0 && P.nearT.t.nrows > 0;
+  cudaStream_t ns = P.stream;
+  if (both) {
+    // the two row sets are independent (disjoint rows of V and J): fork the
+    // near-boundary rows onto a second stream and join before returning
+    if (!P.side) {
+      PDA_CUDA(cudaStreamCreateWithFlags(&P.side, cudaStreamNonBlocking));
+      PDA_CUDA(cudaEventCreateWithFlags(&P.evFork, cudaEventDisableTiming));
+      PDA_CUDA(cudaEventCreateWithFlags(&P.evJoin, cudaEventDisableTiming));
+    }
+    PDA_CUDA(cudaEventRecord(P.evFork, P.stream));
+    PDA_CUDA(cudaStreamWaitEvent(P.side, P.evFork, 0));
+    ns = P.side;
+  }
+  if (P.nearT.t.nrows > 0) {
+    P.L->rows_vj_nearbd(P.scheme, P.nearT.t, P.margs, P.phys, U, P.d_rowptr.p, V, J, ns);
+    check_launch(P);
+  }
   if (P.innerT.t.nrows > 0) {
     P.L->rows_vj_inner(P.scheme, P.innerT.t, P.margs, P.phys, U, P.d_rowptr.p, V, J, P.stream);
     check_launch(P);
   }
-  if (P.nearT.t.nrows > 0) {
-    P.L->rows_vj_nearbd(P.scheme, P.nearT.t, P.margs, P.phys, U, P.d_rowptr.p, V, J, P.stream);
-    check_launch(P);
+  if (both) {
+    PDA_CUDA(cudaEventRecord(P.evJoin, P.side));
+    PDA_CUDA(cudaStreamWaitEvent(P.stream, P.evJoin, 0));
   }
 }
 
@@ -550,8 +663,10 @@ void create_problem(pda_problem &P, const Mesh &m, int family, int probEn, int s
     P.bc = BC_NONE;
   } else if (family == PDA_EULER2D) {
     // euler2d.hpp:88-173; impl/euler_2d_parametrization_helpers.hpp:75-93
-    PDA_REQUIRE(probEn == 0 || probEn == 2 || probEn == 4 || probEn == 8, PDA_ERR_UNSUPPORTED,
-                "Euler2d: supported problems are PeriodicSmooth, SedovFull (Neumann BCs), Riemann");
+    PDA_REQUIRE((probEn >= 0 && probEn <= 5) || probEn == 8, PDA_ERR_UNSUPPORTED,
+                "Euler2d: supported problems are PeriodicSmooth, KelvinHelmholtz, SedovFull, SedovSymmetry, "
+                "Riemann, NormalShock, testingonlyneumann (DoubleMachReflection and CrossShock: time-dependent "
+                "and inflow ghost states are not implemented)");
     const bool validIc = (probEn == 4) ? (P.icFlag == 1 || P.icFlag == 2) : P.icFlag == 1;
     PDA_REQUIRE(validIc, PDA_ERR_INVALID_ARGUMENT, "Euler2d: invalid icFlag for the given problem enum");
     P.physParams = {1.4};
@@ -568,8 +683,17 @@ void create_problem(pda_problem &P, const Mesh &m, int family, int probEn, int s
       PDA_REQUIRE(idx != kInvalid, PDA_ERR_INVALID_ARGUMENT, "Euler2d: invalid parameter name " + kv.first);
       P.icParams[idx] = kv.second;
     }
-    P.bc = probEn == 0 ? BC_NONE : BC_MIRROR2D;
-    if (probEn == 2) PDA_REQUIRE(false, PDA_ERR_UNSUPPORTED, "Euler2d::SedovFull initial condition not available");
+    // ghost rules per problem (euler_2d_prob_class.hpp:466-560): none for the
+    // periodic problems, Neumann mirrors for SedovFull / Riemann / testing
+    P.bc = (probEn == 0 || probEn == 1) ? BC_NONE
+           : probEn == 3                ? BC_SEDOVSYM
+           : probEn == 5                ? BC_NORMALSHOCK
+                                        : BC_MIRROR2D;
+    if (probEn == 3) {
+      P.margs.reflect[0] = 1;
+      P.margs.reflect[1] = 2;
+    }
+    if (probEn == 5) P.margs.reflect[1] = 2;
   } else {
     // swe2d.hpp:143-195; impl/swe_2d_parametrization_helpers.hpp:59-95
     PDA_REQUIRE(probEn == 0, PDA_ERR_UNSUPPORTED, "Swe2d: only SlipWall is supported");

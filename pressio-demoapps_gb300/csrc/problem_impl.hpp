@@ -92,7 +92,13 @@ struct Table {
   }
 };
 
-enum BcKind { BC_NONE = 0, BC_MIRROR2D = 1, BC_NEUMANN1D = 2 };
+// ghost-cell rules: BC_MIRROR2D = Ghost2dNeumannFiller / InviscidWallFiller,
+// BC_NEUMANN1D = Ghost1dNeumannFiller, BC_SEDOVSYM = Sedov2dSymmetryGhostFiller
+// (layer L >= 1 copies the opposite-side neighbour L-1; reflective on the
+// left and bottom sides, Neumann on the right and top), BC_NORMALSHOCK =
+// NormalShock2dGhostFiller (same layer rule; reflective top and bottom,
+// Neumann left and right)
+enum BcKind { BC_NONE = 0, BC_MIRROR2D = 1, BC_NEUMANN1D = 2, BC_SEDOVSYM = 3, BC_NORMALSHOCK = 4 };
 
 }  // namespace pda
 
@@ -107,6 +113,9 @@ struct pda_problem {
   pda::Phys phys{};
   pda::MeshArgs margs{};
   cudaStream_t stream = nullptr;
+  // second stream + events: inner and near-boundary row kernels run side by side
+  cudaStream_t side = nullptr;
+  cudaEvent_t evFork = nullptr, evJoin = nullptr;
   int ndpc = 0, dim = 0, h = 0;
   int64_t dofsSample = 0, dofsStencil = 0;
   int bc = pda::BC_NONE;
@@ -140,6 +149,9 @@ struct pda_problem {
   int64_t launches = 0;
   ~pda_problem() {
     if (stepGraph) cudaGraphExecDestroy(stepGraph);
+    if (side) cudaStreamDestroy(side);
+    if (evFork) cudaEventDestroy(evFork);
+    if (evJoin) cudaEventDestroy(evJoin);
   }
 };
 

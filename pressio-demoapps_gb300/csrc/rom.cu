@@ -30,7 +30,6 @@ namespace pda {
 namespace rom {
 
 constexpr int KMAX = 32;        // latent dimension limit
-constexpr int ROWS_PER_BLOCK = 128;
 
 struct Flags {
   int converged;   // correction below tolerance in this step
@@ -53,15 +52,25 @@ __global__ void k_decode_affine(long nst, const double *__restrict__ uref, const
   y[i] = uref[i] + acc;
 }
 
+// out[c][r] = in[r][c], R x C floats (set-up only)
+__global__ void k_transpose_f32(const float *__restrict__ in, float *__restrict__ out, long R, long C) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= R * C) return;
+  const long r = i / C, c = i % C;
+  out[c * R + r] = in[i];
+}
+
 __device__ __forceinline__ float elu_f(float a) { return a > 0.f ? a : expm1f(a); }
 __device__ __forceinline__ float delu_f(float a) { return a > 0.f ? 1.f : expf(a); }
 
 // hidden layers: every block recomputes layer 1 (h1 x k, tiny) in shared
 // memory, then its slice of layer 2: h2[r] and T2[r][c] = elu'(a2_r) (W2 T1)_rc
 // with T1 = diag(elu'(a1)) W1.  Output Z[r][0] = h2, Z[r][1 + c] = T2.
+// W2T is W2 transposed ([h1 x h2]) so that the threads of a warp (consecutive
+// output rows) read consecutive addresses
 template <int K, int H1>
-__global__ void __launch_bounds__(256)
-k_decode_hidden(int h2, const float *__restrict__ W1, const float *__restrict__ b1, const float *__restrict__ W2,
+__global__ void __launch_bounds__(64)
+k_decode_hidden(int h2, const float *__restrict__ W1, const float *__restrict__ b1, const float *__restrict__ W2T,
                 const float *__restrict__ b2, const double *__restrict__ x, float *__restrict__ Z, const Flags *f) {
   if (f->converged) return;
   __shared__ float sh1[H1];
@@ -85,9 +94,9 @@ k_decode_hidden(int h2, const float *__restrict__ W1, const float *__restrict__ 
   float t[K];
 #pragma unroll
   for (int c = 0; c < K; ++c) t[c] = 0.f;
-  const float *w = W2 + (long)r * H1;
+#pragma unroll 8
   for (int j = 0; j < H1; ++j) {
-    const float wj = w[j];
+    const float wj = __ldg(W2T + (long)j * h2 + r);
     a += wj * sh1[j];
 #pragma unroll
     for (int c = 0; c < K; ++c) t[c] += wj * sT1[j][c];
@@ -99,8 +108,9 @@ k_decode_hidden(int h2, const float *__restrict__ W1, const float *__restrict__ 
   for (int c = 0; c < K; ++c) Z[(long)r * ld + 1 + c] = d * t[c];
 }
 
-// output layer at the stencil rows: one warp per row, the [h2 | T2] block
-// staged in shared memory by every block (h2 x (1+k) floats)
+// output layer at the stencil rows: one warp per row (lanes over the hidden
+// width, 8 weights in flight per lane), the [h2 | T2] block staged in shared
+// memory by every block (h2 x (1+k) floats)
 template <int K>
 __global__ void __launch_bounds__(256)
 k_decode_out(int h2, long nst, const float *__restrict__ W3, const float *__restrict__ b3,
@@ -118,8 +128,20 @@ k_decode_out(int h2, long nst, const float *__restrict__ W3, const float *__rest
 #pragma unroll
     for (int c = 0; c < ld; ++c) acc[c] = 0.f;
     const float *w = W3 + row * h2;
-    for (int j = lane; j < h2; j += 32) {
-      const float wj = w[j];
+    int j = lane;
+    for (; j + 32 * 7 < h2; j += 32 * 8) {
+      float wv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) wv[u] = __ldg(w + j + 32 * u);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const float *z = sZ + (j + 32 * u) * ld;
+#pragma unroll
+        for (int c = 0; c < ld; ++c) acc[c] += wv[u] * z[c];
+      }
+    }
+    for (; j < h2; j += 32) {
+      const float wj = __ldg(w + j);
       const float *z = sZ + j * ld;
 #pragma unroll
       for (int c = 0; c < ld; ++c) acc[c] += wj * z[c];
@@ -137,43 +159,62 @@ k_decode_out(int h2, long nst, const float *__restrict__ W3, const float *__rest
   }
 }
 
-// ---------------------------------------------------- LSPG residual / normal eqs
-// one thread per sample dof row r (sample cell r / ndpc, dof r % ndpc):
-// R_r and JR_r, then this block's partial sums of JR^T JR (upper triangle)
-// and JR^T R, in a fixed order
 template <int K>
-__global__ void __launch_bounds__(ROWS_PER_BLOCK)
+__device__ void lspg_solve_block(int nblocks, const double *__restrict__ partial, double *__restrict__ x, double tol,
+                                 Flags *f);
+
+// ---------------------------------------------------- LSPG residual / normal eqs
+// Block of RB sample dof rows; thread (row, c) for c < K forms JR[row][c] =
+// cf (Jf D)[row][c] + D[row][c] (its CSR row against column c of D), thread
+// (row, K) the residual R[row]; then this block's partial sums of the upper
+// triangle of JR^T JR, of JR^T R and of R^T R, each in a fixed row order.
+__host__ __device__ constexpr int rows_per_block(int K) { return (K + 1) * 32 <= 1024 ? 32 : 16; }
+
+template <int K>
+__global__ void __launch_bounds__(rows_per_block(K) * (K + 1))
 k_lspg_rows(int ndpc, long ns, const int *__restrict__ s2st, const double *__restrict__ y,
             const double *__restrict__ D, const double *__restrict__ V, const int *__restrict__ rowptr,
             const int *__restrict__ colidx, const double *__restrict__ J, double cf, double *__restrict__ yn,
-            int first, double *__restrict__ partial, const Flags *f) {
+            int first, double *__restrict__ partial, unsigned *__restrict__ ticket, double *__restrict__ x,
+            double tol, Flags *f) {
   if (f->converged) return;
-  __shared__ double sJR[ROWS_PER_BLOCK][K + 1];  // column K holds R
-  const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr int RB = rows_per_block(K);
+  __shared__ double sJR[RB][K + 1];  // column K holds R
   const int t = threadIdx.x;
+  const int rl = t / (K + 1), c = t % (K + 1);
+  const long r = (long)blockIdx.x * RB + rl;
+  double val = 0.;
   if (r < ns) {
     const long st = (long)s2st[r / ndpc] * ndpc + r % ndpc;  // stencil dof of this sample dof
-    const double ynp1 = y[st];
-    if (first) yn[r] = ynp1;  // first iteration of a step: y_n = y(x_n)
-    const double helper = 1. * ynp1 + (-1.) * yn[r];
-    sJR[t][K] = cf * V[r] + 1. * helper;
-    double jd[K];
+    if (c == K) {
+      const double ynp1 = y[st];
+      if (first) yn[r] = ynp1;  // first iteration of a step: y_n = y(x_n)
+      const double helper = 1. * ynp1 + (-1.) * yn[r];
+      val = cf * V[r] + 1. * helper;
+    } else {
+      double jd = 0.;
+      const int q0 = rowptr[r], q1 = rowptr[r + 1];
+      int q = q0;
+      for (; q + 3 < q1; q += 4) {
+        // the four column indices and products' operands loaded before the sums
+        int ci[4];
+        double jv[4], dv[4];
 #pragma unroll
-    for (int c = 0; c < K; ++c) jd[c] = 0.;
-    for (int q = rowptr[r]; q < rowptr[r + 1]; ++q) {
-      const double jv = J[q];
-      const double *d = D + (long)colidx[q] * K;
+        for (int u = 0; u < 4; ++u) {
+          ci[u] = __ldg(colidx + q + u);
+          jv[u] = __ldg(J + q + u);
+        }
 #pragma unroll
-      for (int c = 0; c < K; ++c) jd[c] += jv * d[c];
+        for (int u = 0; u < 4; ++u) dv[u] = __ldg(D + (long)ci[u] * K + c);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) jd += jv[u] * dv[u];
+      }
+      for (; q < q1; ++q) jd += J[q] * D[(long)colidx[q] * K + c];
+      val = cf * jd + 1. * D[st * K + c];
     }
-#pragma unroll
-    for (int c = 0; c < K; ++c) sJR[t][c] = cf * jd[c] + 1. * D[st * K + c];
-  } else {
-#pragma unroll
-    for (int c = 0; c <= K; ++c) sJR[t][c] = 0.;
   }
+  sJR[rl][c] = val;
   __syncthreads();
-  // partial sums: upper triangle of JR^T JR (row-major), then JR^T R, then R^T R
   constexpr int ntri = K * (K + 1) / 2, ne = ntri + K + 1;
   for (int e = t; e < ne; e += blockDim.x) {
     int a, b;
@@ -193,25 +234,41 @@ k_lspg_rows(int ndpc, long ns, const int *__restrict__ s2st, const double *__res
       b = K;
     }
     double s = 0.;
-    for (int i = 0; i < ROWS_PER_BLOCK; ++i) s += sJR[i][a] * sJR[i][b];
+    for (int i = 0; i < RB; ++i) s += sJR[i][a] * sJR[i][b];
     partial[(long)blockIdx.x * ne + e] = s;
   }
+  // the last block to finish reduces the partial sums and solves (ticket
+  // counter; no block waits for another)
+  __shared__ unsigned last;
+  __threadfence();
+  __syncthreads();
+  if (t == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1 ? 1u : 0u;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  lspg_solve_block<K>((int)gridDim.x, partial, x, tol, f);
+  if (t == 0) *ticket = 0u;
 }
 
-// one block: reduce the partial sums in block order, factor, solve, update
+// reduce the partial sums in block order, factor, solve, update (the whole
+// calling block takes part; thread 0 factors)
 template <int K>
-__global__ void __launch_bounds__(256)
-k_lspg_solve(int nblocks, const double *__restrict__ partial, double *__restrict__ x, double tol, Flags *f) {
-  if (f->converged) return;
+__device__ void lspg_solve_block(int nblocks, const double *__restrict__ partial, double *__restrict__ x, double tol,
+                                 Flags *f) {
   constexpr int k = K;
   __shared__ double H[K][K];
   __shared__ double g[K];
   __shared__ double red[K + 1];
   __shared__ double rr;
   constexpr int ntri = K * (K + 1) / 2, ne = ntri + K + 1;
-  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+  const int lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  for (int e = threadIdx.x >> 5; e < ne; e += nwarp) {
+    // lanes take blocks lane, lane + 32, ...; then a fixed shuffle tree
     double s = 0.;
-    for (int b = 0; b < nblocks; ++b) s += partial[(long)b * ne + e];
+    for (int b = lane; b < nblocks; b += 32) s += partial[(long)b * ne + e];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane != 0) continue;
     if (e < ntri) {
       int a = 0, rem = e;
       while (rem >= k - a) {
@@ -228,26 +285,35 @@ k_lspg_solve(int nblocks, const double *__restrict__ partial, double *__restrict
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    // Cholesky H = L L^T in place (lower triangle), then L L^T dx = g
-    bool ok = true;
-    for (int j = 0; j < k && ok; ++j) {
-      double d = H[j][j];
-      for (int p = 0; p < j; ++p) d -= H[j][p] * H[j][p];
-      if (!(d > 0.)) {
-        ok = false;
-        break;
+  __shared__ int ok;
+  if (threadIdx.x == 0) ok = 1;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    // Cholesky H = L L^T in place (lower triangle), one column per step, the
+    // column's rows in parallel over the warp
+    const int lane = threadIdx.x;
+    for (int j = 0; j < k; ++j) {
+      if (lane == 0) {
+        double d = H[j][j];
+        for (int p = 0; p < j; ++p) d -= H[j][p] * H[j][p];
+        if (!(d > 0.)) ok = 0;
+        else H[j][j] = sqrt(d);
       }
-      const double l = sqrt(d);
-      H[j][j] = l;
-      for (int i = j + 1; i < k; ++i) {
+      __syncwarp();
+      if (!ok) break;
+      for (int i = j + 1 + lane; i < k; i += 32) {
         double s = H[i][j];
         for (int p = 0; p < j; ++p) s -= H[i][p] * H[j][p];
-        H[i][j] = s / l;
+        H[i][j] = s / H[j][j];
       }
+      __syncwarp();
     }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
     double corr = 0.;
     if (ok) {
+      // L L^T dx = g
       for (int i = 0; i < k; ++i) {
         double s = g[i];
         for (int p = 0; p < i; ++p) s -= H[i][p] * red[p];
@@ -287,9 +353,10 @@ struct pda_lspg {
   long nst = 0, ns = 0, nSampleCells = 0;
   pda::DevBuf<int> s2st;
   pda::DevBuf<double> uref, phi, scale;
-  pda::DevBuf<float> W1, b1, W2, b2, W3, b3, Z;
+  pda::DevBuf<float> W1, b1, W2, W2T, b2, W3, b3, Z;
   pda::DevBuf<double> y, D, V, J, yn, partial, xn;
   pda::DevBuf<pda::rom::Flags> flags;
+  pda::DevBuf<unsigned> ticket;
   int nblocks = 0;
   int64_t nnz = 0;
   cudaGraphExec_t graph = nullptr;
@@ -323,7 +390,7 @@ void decode_k(pda_lspg &L, const double *x, double *y, cudaStream_t s) {
   if (L.kind == 0) {
     k_decode_affine<K><<<div_up(L.nst, 256), 256, 0, s>>>(L.nst, L.uref.p, L.phi.p, x, y, f);
   } else {
-    k_decode_hidden<K, 256><<<div_up(L.h2, 256), 256, 0, s>>>(L.h2, L.W1.p, L.b1.p, L.W2.p, L.b2.p, x, L.Z.p, f);
+    k_decode_hidden<K, 256><<<div_up(L.h2, 64), 64, 0, s>>>(L.h2, L.W1.p, L.b1.p, L.W2T.p, L.b2.p, x, L.Z.p, f);
     const int smem = L.h2 * (1 + K) * (int)sizeof(float);
     k_decode_out<K><<<decode_grid(L.nst), 256, smem, s>>>(L.h2, L.nst, L.W3.p, L.b3.p, L.uref.p, L.scale.p, L.Z.p,
                                                             y, L.D.p, f);
@@ -338,10 +405,9 @@ void gn_iteration_k(pda_lspg &L, double *x, double dt, double tol, int first, cu
   // run unconditionally, cheap next to the rest once converged
   const pda_status st = pda_velocity_and_jacobian(L.P, L.y.p, 0.0, L.V.p, L.J.p);
   if (st != PDA_OK) throw Error(st, pda_last_error());
-  k_lspg_rows<K><<<L.nblocks, ROWS_PER_BLOCK, 0, s>>>(L.ndpc, L.ns, L.s2st.p, L.y.p, L.D.p, L.V.p,
+  k_lspg_rows<K><<<L.nblocks, rows_per_block(K) * (K + 1), 0, s>>>(L.ndpc, L.ns, L.s2st.p, L.y.p, L.D.p, L.V.p,
                                                       L.P->d_rowptr.p, L.P->d_colidx.p, L.J.p, -dt, L.yn.p, first,
-                                                      L.partial.p, f);
-  k_lspg_solve<K><<<1, 256, 0, s>>>(L.nblocks, L.partial.p, x, tol, f);
+                                                      L.partial.p, L.ticket.p, x, tol, f);
 }
 
 #define PDA_ROM_K_SWITCH(k, CALL) \
@@ -407,9 +473,11 @@ void common_setup(pda_lspg &L, pda_problem *P, const int64_t *s2st, int k) {
   L.V.alloc((size_t)L.ns);
   L.J.alloc((size_t)std::max<int64_t>(nnz, 1));
   L.yn.alloc((size_t)L.ns);
-  L.nblocks = div_up(L.ns, ROWS_PER_BLOCK);
+  L.nblocks = div_up(L.ns, rows_per_block(k));
   L.partial.alloc((size_t)L.nblocks * (k * (k + 1) / 2 + k + 1));
   L.flags.alloc(1);
+  L.ticket.alloc(1);
+  PDA_CUDA(cudaMemset(L.ticket.p, 0, sizeof(unsigned)));
   L.xn.alloc((size_t)k);
   PDA_CUDA(cudaMemset(L.flags.p, 0, sizeof(Flags)));
   PDA_CUDA(cudaMemset(L.y.p, 0, (size_t)L.nst * sizeof(double)));
@@ -467,6 +535,10 @@ pda_status pda_lspg_create_mlp(pda_problem *sample_problem, const int64_t *sampl
   pda::rom::upload_dev(L->W1, d_W1, (size_t)h1 * k);
   pda::rom::upload_dev(L->b1, d_b1, (size_t)h1);
   pda::rom::upload_dev(L->W2, d_W2, (size_t)h2 * h1);
+  L->W2T.alloc((size_t)h2 * h1);
+  pda::rom::k_transpose_f32<<<pda::div_up((long)h2 * h1, 256), 256>>>(L->W2.p, L->W2T.p, h2, h1);
+  PDA_CUDA(cudaGetLastError());
+  PDA_CUDA(cudaDeviceSynchronize());
   pda::rom::upload_dev(L->b2, d_b2, (size_t)h2);
   pda::rom::upload_dev(L->W3, d_W3, (size_t)L->nst * h2);
   pda::rom::upload_dev(L->b3, d_b3, (size_t)L->nst);

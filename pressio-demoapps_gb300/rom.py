@@ -123,6 +123,20 @@ class SweSetup:
         return sm, gids, st, s2st
 
 
+def train_schedule(ae, X, epochs, batch=256, lr=1e-3, seed=2):
+    """Adam in three phases of decreasing step size (60 % of the epochs at lr,
+    25 % at lr / 3, 15 % at lr / 10); returns the per-epoch losses."""
+    e1 = max(1, int(round(0.6 * epochs)))
+    e2 = max(0, int(round(0.25 * epochs)))
+    e3 = max(0, epochs - e1 - e2)
+    out = [ae.train(X, batch=batch, epochs=e1, lr=lr, seed=seed)]
+    if e2:
+        out.append(ae.train(X, batch=batch, epochs=e2, lr=lr / 3, seed=seed + 1))
+    if e3:
+        out.append(ae.train(X, batch=batch, epochs=e3, lr=lr / 10, seed=seed + 2))
+    return np.concatenate(out)
+
+
 def stencil_rows(stencil_gids):
     st = np.asarray(stencil_gids, dtype=np.int64)
     return (st[:, None] * 3 + np.arange(3)[None, :]).reshape(-1)
