@@ -403,8 +403,8 @@ def _rom_module():
     return mod
 
 
-def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int(os.environ.get("PDA_ROM_EPOCHS", 40)),
-               batch=256, lr=1e-3, dt=0.005, rom_ratio=4, gn_iters=3):
+def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int(os.environ.get("PDA_ROM_EPOCHS", 60)),
+               batch=128, lr=1e-3, dt=0.005, rom_ratio=4, gn_iters=3):
     """Learned-manifold hyper-reduced LSPG on 2D SWE slip wall 256^2: 48
     Latin-hypercube training points (gravity, coriolis, pulse), 400 FOM
     snapshots each (SSP-RK3 dt 0.005, batched device FOM), MLP autoencoder
@@ -508,9 +508,44 @@ def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int
     return out
 
 
+def wl_lspg_step(c, n=256, latent=12, steps=20, gn_iters=3):
+    """Latency of one hyper-reduced LSPG step (BDF1, Gauss-Newton, CUDA-graph
+    replay) on the 1 % sample mesh of the 256^2 shallow-water problem, with an
+    affine basis and with an MLP decoder of the config-5 shape (random weights,
+    no training: the step's cost does not depend on the weights' values)."""
+    R = _rom_module()
+    pda, torch = c.pda, c.torch
+    setup = R.SweSetup(pda, n)
+    sm, gids, st, s2st = setup.sample_mesh(0.01, seed=7)
+    ps = setup.problem({"gravity": 7.0, "coriolis": -2.0, "pulseMagnitude": 0.1}, mesh=sm)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    phi = torch.linalg.qr(torch.randn(setup.N, latent, generator=g, device="cuda", dtype=torch.float64))[0] * 0.3
+    W1 = torch.randn(256, latent, generator=g, device="cuda") * 0.3
+    b1 = torch.randn(256, generator=g, device="cuda") * 0.1
+    W2 = torch.randn(1024, 256, generator=g, device="cuda") * 0.05
+    b2 = torch.randn(1024, generator=g, device="cuda") * 0.1
+    W3 = torch.randn(setup.N, 1024, generator=g, device="cuda") * 0.02
+    b3 = torch.randn(setup.N, generator=g, device="cuda") * 0.1
+    scale = torch.full((setup.N,), 0.05, dtype=torch.float64, device="cuda")
+    learned = R.LearnedRom.__new__(R.LearnedRom)
+    learned.setup, learned.scale, learned.dec = setup, scale, (W1, b1, W2, b2, W3, b3)
+    out = {"config": "lspg_bdf1_swe256_sample1pct", "sample_cells": int(len(gids)), "stencil_cells": int(len(st)),
+           "gn_iters": gn_iters, "steps_timed": steps}
+    for kind, rom in (("affine", R.affine_lspg(setup, phi, ps, s2st, st)), ("mlp", learned.lspg(ps, s2st, st))):
+        x = torch.zeros(latent, dtype=torch.float64, device="cuda")
+        rom.advance_bdf1(x, 0.02, 2, gn_iters, 0.0)  # capture + warm-up; tol 0: every iteration runs
+        setup.stream.synchronize()
+        t0 = time.perf_counter()
+        rom.advance_bdf1(x, 0.02, steps, gn_iters, 0.0)
+        setup.stream.synchronize()
+        wall = time.perf_counter() - t0
+        out[kind] = {"ms_per_step": 1e3 * wall / steps, "ms_per_gn_iteration": 1e3 * wall / steps / gn_iters}
+    return out
+
+
 WORKLOADS = {"jacobian_2d": wl_jacobian_2d, "velocity_3d": wl_velocity_3d, "jacobian_3d": wl_jacobian_3d,
              "sod_1d_ssprk3": wl_sod_1d_ssprk3, "ssprk3_3d": wl_ssprk3_3d, "batched_swe": wl_batched_swe,
-             "rom_swe": wl_rom_swe}
+             "rom_swe": wl_rom_swe, "lspg_step": wl_lspg_step}
 
 
 def extra_workloads(pda, torch, stream, cpu=True, names=None):

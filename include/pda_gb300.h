@@ -334,6 +334,20 @@ pda_status pda_lspg_decode(pda_lspg *rom, const double *d_x, double *d_y);
 pda_status pda_lspg_advance_bdf1(pda_lspg *rom, double *d_x, double dt, int64_t n_steps, int gn_iters,
                                  double tol, int use_graph, double *info);
 
+/* Implicit steps on the device (the consumer of the Jacobian in the
+ * reference's implicit tests, tests_cpp/eigen_2d_euler_riemann_implicit/
+ * main.cc:31-44: Pressio's implicit stepper + Newton-Raphson + BiCGSTAB).
+ * scheme 0 = BDF1, 1 = Crank-Nicolson.  Per step, Newton iterations with
+ * J_R = I - c dt Jf (c = 1 or 1/2) stop before updating once the l2 norm of
+ * the correction is below newton_tol (Pressio's default criterion); each
+ * correction is BiCGSTAB with a Jacobi preconditioner to a relative residual
+ * of linear_tol.  Full meshes only.  info (may be NULL) receives {Newton
+ * iterations in total, most in one step, BiCGSTAB iterations in total, worst
+ * final relative linear residual}. */
+pda_status pda_advance_implicit(pda_problem *p, double *d_U, double t0, double dt, int64_t n_steps, int scheme,
+                                double newton_tol, int newton_max_iters, double linear_tol,
+                                int linear_max_iters, double *info);
+
 /* --------------------------------------------------------- diagnostics
  * (no counterpart in the reference: measurement support for benchmarks) */
 

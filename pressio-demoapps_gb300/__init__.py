@@ -149,6 +149,8 @@ _SIGS = {
                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.POINTER(C.c_void_p)]),
     "pda_lspg_free": (None, [C.c_void_p]),
+    "pda_advance_implicit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64, C.c_int,
+                                       C.c_double, C.c_int, C.c_double, C.c_int, C.c_void_p]),
     "pda_lspg_decode": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "pda_lspg_advance_bdf1": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int64, C.c_int, C.c_double,
                                         C.c_int, C.c_void_p]),
@@ -501,6 +503,21 @@ class Problem:
 
     def launch_count(self):
         return lib().pda_problem_launch_count(self._h)
+
+    def advance_implicit(self, state, t0, dt, nsteps, scheme="cn", newton_tol=1e-5, newton_max_iters=100,
+                         linear_tol=1e-12, linear_max_iters=2000):
+        """Crank-Nicolson ("cn") or BDF1 ("bdf1") steps with Newton-Raphson and
+        Jacobi-preconditioned BiCGSTAB on the device (Pressio's implicit stepper
+        + create_newton_solver + iterative::Bicgstab)."""
+        import numpy as np
+        self._check_vec(state, self._dst, "state")
+        info = np.zeros(4)
+        _check(lib().pda_advance_implicit(self._h, _ptr(state), float(t0), float(dt), int(nsteps),
+                                          1 if scheme == "cn" else 0, float(newton_tol), int(newton_max_iters),
+                                          float(linear_tol), int(linear_max_iters),
+                                          info.ctypes.data_as(C.c_void_p)))
+        return {"newton_iters": int(info[0]), "max_newton_per_step": int(info[1]), "linear_iters": int(info[2]),
+                "worst_linear_relres": float(info[3])}
 
     def profile_velocity(self, state, V, reps=10):
         """Mean device ms of the velocity kernels: faces x/y/z, balance, near-boundary rows."""

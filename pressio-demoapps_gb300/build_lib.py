@@ -34,6 +34,7 @@ SOURCES = [
     "mlp.cu",
     "rom.cu",
     "ae.cu",
+    "implicit.cu",
     "mesh.cpp",
     "problem.cpp",
     "batch.cpp",

@@ -912,6 +912,10 @@ void advance(pda_problem &P, int kind, double *U, double t0, double dt, int64_t 
 }  // namespace
 }  // namespace pda
 
+namespace pda {
+void ensure_device_pattern(pda_problem &P) { pattern_to_device(P); }
+}  // namespace pda
+
 // ===================================================================== C ABI
 using pda::Error;
 

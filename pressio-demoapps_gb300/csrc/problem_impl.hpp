@@ -155,6 +155,11 @@ struct pda_problem {
   }
 };
 
+namespace pda {
+// build the CSR pattern of the problem and copy it to the device (once)
+void ensure_device_pattern(pda_problem &P);
+}  // namespace pda
+
 // C ABI bodies: exceptions become a status code + the thread-local message
 #define PDA_API_BEGIN try {
 #define PDA_API_END                                   \

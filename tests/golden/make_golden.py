@@ -293,6 +293,12 @@ def make_gold(ref: Ref):
         np.save(os.path.join(GOLD, f"swe_{tag}.npy"), h_g)
     json.dump(traj, open(os.path.join(GOLD, "trajectories.json"), "w"), indent=1)
 
+    # Crank-Nicolson + Newton + BiCGSTAB gold of the reference's implicit
+    # Riemann test (first order, 20x20, dt 0.02, 30 steps, Newton tolerance 1e-5)
+    src = os.path.join(REF, "tests_cpp/eigen_2d_euler_riemann_implicit/firstorder")
+    np.save(os.path.join(GOLD, "riemann_implicit_fo_rho.npy"), np.loadtxt(os.path.join(src, "rho_gold.txt")))
+    np.save(os.path.join(GOLD, "riemann_implicit_fo_p.npy"), np.loadtxt(os.path.join(src, "p_gold.txt")))
+
     # mesh-generator golds (tests_mesh/mesh_generation_full_{1,2,3}d/*/*_gold.dat),
     # with the generator arguments their test.cmake files pass
     mg = os.path.join(GOLD, "mesh_generation")
