@@ -451,7 +451,7 @@ def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int
         ps = setup.problem(p, mesh=sm)
         U0 = setup.problem(p).initialCondition()
         if rom_kind == "learned":
-            rom, x0, dec = learned.lspg(ps, s2st, st), learned.encode(U0), fdec
+            rom, x0, dec = learned.lspg(ps, s2st, st, tensor_cores=True), learned.encode(U0), fdec
         else:
             rom, x0, dec = R.affine_lspg(setup, phi, ps, s2st, st), (phi.T @ (U0 - setup.uref)).contiguous(), faff
         lat, wall, maxres = R.run_rom(rom, x0, dt * rom_ratio, rom_cps, setup.stream, gn_iters=gn_iters, tol=1e-8)
@@ -531,7 +531,10 @@ def wl_lspg_step(c, n=256, latent=12, steps=20, gn_iters=3):
     learned.setup, learned.scale, learned.dec = setup, scale, (W1, b1, W2, b2, W3, b3)
     out = {"config": "lspg_bdf1_swe256_sample1pct", "sample_cells": int(len(gids)), "stencil_cells": int(len(st)),
            "gn_iters": gn_iters, "steps_timed": steps}
-    for kind, rom in (("affine", R.affine_lspg(setup, phi, ps, s2st, st)), ("mlp", learned.lspg(ps, s2st, st))):
+    learned.dec = tuple(t.to(torch.bfloat16).float() if t.dim() == 2 else t for t in learned.dec)
+    for kind, rom in (("affine", R.affine_lspg(setup, phi, ps, s2st, st)),
+                      ("mlp_fp32", learned.lspg(ps, s2st, st, tensor_cores=False)),
+                      ("mlp_tensor_cores", learned.lspg(ps, s2st, st, tensor_cores=True))):
         x = torch.zeros(latent, dtype=torch.float64, device="cuda")
         rom.advance_bdf1(x, 0.02, 2, gn_iters, 0.0)  # capture + warm-up; tol 0: every iteration runs
         setup.stream.synchronize()

@@ -319,10 +319,14 @@ pda_status pda_ae_set_layer(pda_ae *ae, int layer, const float *d_W, const float
 typedef struct pda_lspg pda_lspg;
 pda_status pda_lspg_create_affine(pda_problem *sample_problem, const int64_t *sample_to_stencil, int k,
                                   const double *d_uref, const double *d_phi, pda_lspg **out);
+/* mode 0: the decoder in fp32 on the CUDA cores; mode 1: the network's own
+ * training numerics -- the output layer as a tcgen05 GEMM with bf16 weights
+ * (which must already be bf16 values) and bf16 activations, fp32
+ * accumulation (latent at most 15, h2 a multiple of 64). */
 pda_status pda_lspg_create_mlp(pda_problem *sample_problem, const int64_t *sample_to_stencil, int k, int h1,
                                int h2, const double *d_uref, const double *d_scale, const float *d_W1,
                                const float *d_b1, const float *d_W2, const float *d_b2, const float *d_W3,
-                               const float *d_b3, pda_lspg **out);
+                               const float *d_b3, int mode, pda_lspg **out);
 void pda_lspg_free(pda_lspg *rom);
 /* y (stencil dofs) of latent x (k doubles, device) */
 pda_status pda_lspg_decode(pda_lspg *rom, const double *d_x, double *d_y);

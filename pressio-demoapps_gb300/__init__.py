@@ -147,7 +147,7 @@ _SIGS = {
                                          C.POINTER(C.c_void_p)]),
     "pda_lspg_create_mlp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                                      C.POINTER(C.c_void_p)]),
+                                      C.c_int, C.POINTER(C.c_void_p)]),
     "pda_lspg_free": (None, [C.c_void_p]),
     "pda_advance_implicit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64, C.c_int,
                                        C.c_double, C.c_int, C.c_double, C.c_int, C.c_void_p]),
@@ -761,7 +761,9 @@ class LspgRom:
         return LspgRom(h, sample_problem, (s2, k, uref.numel()))
 
     @staticmethod
-    def mlp(sample_problem, sample_to_stencil, uref, scale, W1, b1, W2, b2, W3, b3):
+    def mlp(sample_problem, sample_to_stencil, uref, scale, W1, b1, W2, b2, W3, b3, tensor_cores=False):
+        """tensor_cores=True: the output layer as a bf16 tcgen05 GEMM (the
+        trained network's numerics; W3 must hold bf16 values)."""
         import numpy as np
         s2 = np.ascontiguousarray(sample_to_stencil, dtype=np.int64)
         k = W1.shape[1]
@@ -769,7 +771,7 @@ class LspgRom:
         ts = [t.contiguous() for t in (W1, b1, W2, b2, W3, b3)]
         _check(lib().pda_lspg_create_mlp(sample_problem._h, s2.ctypes.data_as(C.c_void_p), int(k),
                                          int(W1.shape[0]), int(W2.shape[0]), _vp(uref), _vp(scale),
-                                         *[_vp(t) for t in ts], C.byref(h)))
+                                         *[_vp(t) for t in ts], int(bool(tensor_cores)), C.byref(h)))
         return LspgRom(h, sample_problem, (s2, k, uref.numel()))
 
     def decode(self, x):

@@ -22,9 +22,11 @@
 #include <string>
 #include <vector>
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "problem_impl.hpp"
+#include "tc_gemm_api.hpp"
 
 namespace pda {
 namespace rom {
@@ -52,6 +54,16 @@ __global__ void k_decode_affine(long nst, const double *__restrict__ uref, const
   y[i] = uref[i] + acc;
 }
 
+// bf16 copy of fp32 values that must already be bf16 values; *bad = 1 otherwise
+__global__ void k_to_bf16_exact(const float *__restrict__ in, __nv_bfloat16 *__restrict__ out, long n,
+                                int *__restrict__ bad) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const __nv_bfloat16 b = __float2bfloat16_rn(in[i]);
+  out[i] = b;
+  if (__bfloat162float(b) != in[i]) *bad = 1;
+}
+
 // out[c][r] = in[r][c], R x C floats (set-up only)
 __global__ void k_transpose_f32(const float *__restrict__ in, float *__restrict__ out, long R, long C) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -66,16 +78,25 @@ __device__ __forceinline__ float delu_f(float a) { return a > 0.f ? 1.f : expf(a
 // hidden layers: every block recomputes layer 1 (h1 x k, tiny) in shared
 // memory, then its slice of layer 2: h2[r] and T2[r][c] = elu'(a2_r) (W2 T1)_rc
 // with T1 = diag(elu'(a1)) W1.  Output Z[r][0] = h2, Z[r][1 + c] = T2.
-// W2T is W2 transposed ([h1 x h2]) so that the threads of a warp (consecutive
-// output rows) read consecutive addresses
+// W2T is W2 transposed ([h1 x h2]).  Block = 64 output rows x 4 threads;
+// thread (row, q) sums j in [q H1/4, (q+1) H1/4), the four partial sums are
+// added in q order.  Every block recomputes layer 1 (h1 x k, tiny).  Output
+// Z[r][0] = h2, Z[r][1 + c] = T2 (fp32), and when Zb is given the same
+// values as bf16 rows [1 + k (padded to 16)][h2] for the tensor-core output
+// layer (B operand, K-major).
+__host__ __device__ constexpr int hidden_rows(int K) { return K <= 16 ? 64 : 16; }
+
 template <int K, int H1>
-__global__ void __launch_bounds__(64)
+__global__ void __launch_bounds__(hidden_rows(K) * 4)
 k_decode_hidden(int h2, const float *__restrict__ W1, const float *__restrict__ b1, const float *__restrict__ W2T,
-                const float *__restrict__ b2, const double *__restrict__ x, float *__restrict__ Z, const Flags *f) {
+                const float *__restrict__ b2, const double *__restrict__ x, float *__restrict__ Z,
+                __nv_bfloat16 *__restrict__ Zb, const Flags *f) {
   if (f->converged) return;
+  constexpr int RPB = hidden_rows(K), PARTS = 4, ld = 1 + K;
   __shared__ float sh1[H1];
   __shared__ float sT1[H1][K];
   __shared__ float sx[K];
+  __shared__ float sp[PARTS][RPB][ld];
   if (threadIdx.x < K) sx[threadIdx.x] = (float)x[threadIdx.x];
   __syncthreads();
   for (int r = threadIdx.x; r < H1; r += blockDim.x) {
@@ -88,24 +109,60 @@ k_decode_hidden(int h2, const float *__restrict__ W1, const float *__restrict__ 
     for (int c = 0; c < K; ++c) sT1[r][c] = d * W1[r * K + c];
   }
   __syncthreads();
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= h2) return;
+  const int rl = threadIdx.x % RPB, q = threadIdx.x / RPB;
+  const int r = blockIdx.x * RPB + rl;
+  float acc[ld];
+#pragma unroll
+  for (int c = 0; c < ld; ++c) acc[c] = 0.f;
+  if (r < h2) {
+    const int j0 = q * (H1 / PARTS);
+#pragma unroll 8
+    for (int j = j0; j < j0 + H1 / PARTS; ++j) {
+      const float wj = __ldg(W2T + (long)j * h2 + r);
+      acc[0] += wj * sh1[j];
+#pragma unroll
+      for (int c = 0; c < K; ++c) acc[1 + c] += wj * sT1[j][c];
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < ld; ++c) sp[q][rl][c] = acc[c];
+  __syncthreads();
+  if (q != 0 || r >= h2) return;
   float a = b2[r];
   float t[K];
 #pragma unroll
   for (int c = 0; c < K; ++c) t[c] = 0.f;
-#pragma unroll 8
-  for (int j = 0; j < H1; ++j) {
-    const float wj = __ldg(W2T + (long)j * h2 + r);
-    a += wj * sh1[j];
+  for (int qq = 0; qq < PARTS; ++qq) {
+    a += sp[qq][rl][0];
 #pragma unroll
-    for (int c = 0; c < K; ++c) t[c] += wj * sT1[j][c];
+    for (int c = 0; c < K; ++c) t[c] += sp[qq][rl][1 + c];
   }
   const float d = delu_f(a);
-  constexpr int ld = 1 + K;
-  Z[(long)r * ld] = elu_f(a);
+  const float h = elu_f(a);
+  Z[(long)r * ld] = h;
 #pragma unroll
   for (int c = 0; c < K; ++c) Z[(long)r * ld + 1 + c] = d * t[c];
+  if (Zb) {
+    Zb[r] = __float2bfloat16_rn(h);
+#pragma unroll
+    for (int c = 0; c < K; ++c) Zb[(long)(1 + c) * h2 + r] = __float2bfloat16_rn(d * t[c]);
+  }
+}
+
+// tensor-core output layer: C [nst x 16] = W3b [nst x h2] Zb^T (fp32);
+// y = uref + scale (C[., 0] + b3), D = scale C[., 1..k]
+template <int K>
+__global__ void k_decode_finish(long nst, const float *__restrict__ C, const float *__restrict__ b3,
+                                const double *__restrict__ uref, const double *__restrict__ scale,
+                                double *__restrict__ y, double *__restrict__ D, const Flags *f) {
+  if (f->converged) return;
+  const long row = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= nst) return;
+  const float *c = C + row * 16;
+  const double s = scale[row];
+  y[row] = uref[row] + s * (double)(c[0] + b3[row]);
+#pragma unroll
+  for (int j = 0; j < K; ++j) D[row * K + j] = s * (double)c[1 + j];
 }
 
 // output layer at the stencil rows: one warp per row (lanes over the hidden
@@ -353,7 +410,9 @@ struct pda_lspg {
   long nst = 0, ns = 0, nSampleCells = 0;
   pda::DevBuf<int> s2st;
   pda::DevBuf<double> uref, phi, scale;
-  pda::DevBuf<float> W1, b1, W2, W2T, b2, W3, b3, Z;
+  pda::DevBuf<float> W1, b1, W2, W2T, b2, W3, b3, Z, C;
+  bool tensorCore = false;
+  pda::DevBuf<__nv_bfloat16> W3b, Zb;
   pda::DevBuf<double> y, D, V, J, yn, partial, xn;
   pda::DevBuf<pda::rom::Flags> flags;
   pda::DevBuf<unsigned> ticket;
@@ -389,8 +448,14 @@ void decode_k(pda_lspg &L, const double *x, double *y, cudaStream_t s) {
   Flags *f = L.flags.p;
   if (L.kind == 0) {
     k_decode_affine<K><<<div_up(L.nst, 256), 256, 0, s>>>(L.nst, L.uref.p, L.phi.p, x, y, f);
+  } else if (L.tensorCore) {
+    k_decode_hidden<K, 256><<<div_up(L.h2, hidden_rows(K)), hidden_rows(K) * 4, 0, s>>>(
+        L.h2, L.W1.p, L.b1.p, L.W2T.p, L.b2.p, x, L.Z.p, L.Zb.p, f);
+    PDA_CUDA(tc_gemm(L.W3b.p, L.Zb.p, L.nst, 16, L.h2, nullptr, tc::EPI_NONE, L.C.p, nullptr, nullptr, s));
+    k_decode_finish<K><<<div_up(L.nst, 256), 256, 0, s>>>(L.nst, L.C.p, L.b3.p, L.uref.p, L.scale.p, y, L.D.p, f);
   } else {
-    k_decode_hidden<K, 256><<<div_up(L.h2, 64), 64, 0, s>>>(L.h2, L.W1.p, L.b1.p, L.W2T.p, L.b2.p, x, L.Z.p, f);
+    k_decode_hidden<K, 256><<<div_up(L.h2, hidden_rows(K)), hidden_rows(K) * 4, 0, s>>>(
+        L.h2, L.W1.p, L.b1.p, L.W2T.p, L.b2.p, x, L.Z.p, nullptr, f);
     const int smem = L.h2 * (1 + K) * (int)sizeof(float);
     k_decode_out<K><<<decode_grid(L.nst), 256, smem, s>>>(L.h2, L.nst, L.W3.p, L.b3.p, L.uref.p, L.scale.p, L.Z.p,
                                                             y, L.D.p, f);
@@ -518,7 +583,7 @@ pda_status pda_lspg_create_affine(pda_problem *sample_problem, const int64_t *sa
 pda_status pda_lspg_create_mlp(pda_problem *sample_problem, const int64_t *sample_to_stencil, int k, int h1,
                                int h2, const double *d_uref, const double *d_scale, const float *d_W1,
                                const float *d_b1, const float *d_W2, const float *d_b2, const float *d_W3,
-                               const float *d_b3, pda_lspg **out) {
+                               const float *d_b3, int mode, pda_lspg **out) {
   PDA_API_BEGIN
   PDA_REQUIRE(out && d_uref && d_scale && d_W1 && d_b1 && d_W2 && d_b2 && d_W3 && d_b3, PDA_ERR_INVALID_ARGUMENT,
               "null argument");
@@ -543,6 +608,32 @@ pda_status pda_lspg_create_mlp(pda_problem *sample_problem, const int64_t *sampl
   pda::rom::upload_dev(L->W3, d_W3, (size_t)L->nst * h2);
   pda::rom::upload_dev(L->b3, d_b3, (size_t)L->nst);
   L->Z.alloc((size_t)h2 * (1 + k));
+  if (mode == 1) {
+    // bf16 output layer on the tensor cores: the weights must be bf16 values
+    PDA_REQUIRE(h2 % 64 == 0 && k + 1 <= 16, PDA_ERR_UNSUPPORTED,
+                "tensor-core decoder: hidden width a multiple of 64 and latent at most 15");
+    L->tensorCore = true;
+    L->W3b.alloc((size_t)L->nst * h2);
+    L->Zb.alloc((size_t)16 * h2);
+    L->C.alloc((size_t)L->nst * 16);
+    PDA_CUDA(cudaMemset(L->Zb.p, 0, (size_t)16 * h2 * sizeof(__nv_bfloat16)));
+    pda::DevBuf<int> bad;
+    bad.alloc(1);
+    PDA_CUDA(cudaMemset(bad.p, 0, sizeof(int)));
+    pda::rom::k_to_bf16_exact<<<pda::div_up(L->nst * (long)h2, 256), 256>>>(L->W3.p, L->W3b.p, L->nst * (long)h2,
+                                                                             bad.p);
+    PDA_CUDA(cudaGetLastError());
+    int hb = 0;
+    PDA_CUDA(cudaMemcpy(&hb, bad.p, sizeof(int), cudaMemcpyDeviceToHost));
+    PDA_REQUIRE(hb == 0, PDA_ERR_INVALID_ARGUMENT,
+                "tensor-core decoder: output-layer weights are not bf16 values (use mode 0)");
+    // one call before any capture: sets the GEMM's shared-memory attribute
+    PDA_CUDA(pda::tc_gemm(L->W3b.p, L->Zb.p, L->nst, 16, h2, nullptr, pda::tc::EPI_NONE, L->C.p, nullptr, nullptr,
+                          nullptr));
+    PDA_CUDA(cudaDeviceSynchronize());
+  } else {
+    PDA_REQUIRE(mode == 0, PDA_ERR_INVALID_ARGUMENT, "mode must be 0 (fp32) or 1 (bf16 tensor cores)");
+  }
   const int smem = h2 * (1 + k) * (int)sizeof(float);
   if (smem > 48 * 1024) {
 #define PDA_ROM_ATTR(K) \

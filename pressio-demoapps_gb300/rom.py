@@ -166,14 +166,16 @@ class LearnedRom:
         _, Z = self.ae.reconstruct(x.contiguous())
         return Z[0].double().contiguous()
 
-    def lspg(self, problem, s2st, stencil_gids):
+    def lspg(self, problem, s2st, stencil_gids, tensor_cores=True):
+        """tensor_cores: the decoder's output layer as a bf16 tcgen05 GEMM (the
+        numerics the network was trained with); False: fp32 on CUDA cores."""
         rows = stencil_rows(stencil_gids)
         import torch
         r = torch.from_numpy(rows).cuda()
         W1, b1, W2, b2, W3, b3 = self.dec
         return self.setup.pda.LspgRom.mlp(problem, s2st, self.setup.uref[r].contiguous(),
                                           self.scale[r].contiguous(), W1, b1, W2, b2, W3[r].contiguous(),
-                                          b3[r].contiguous())
+                                          b3[r].contiguous(), tensor_cores=tensor_cores)
 
     def full_decoder(self):
         """The decoder on every row (error evaluation), through a full-mesh LSPG object."""

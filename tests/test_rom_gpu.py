@@ -151,3 +151,34 @@ def test_lspg_mlp_decoder_matches_oracle(pda, oracle):
     rom.advance_bdf1(xd, dt, steps, gn_iters=8, tol=1e-10, use_graph=True)
     # float32 decoder evaluation: the latent agrees to the decoder's precision
     assert np.allclose(xd.cpu().numpy(), xr, rtol=1e-4, atol=1e-6), (xd.cpu().numpy(), xr)
+
+
+@pytest.mark.gpu
+def test_lspg_mlp_tensor_core_decoder_close_to_fp32(pda, oracle):
+    """Tensor-core output layer (bf16 weights and activations, fp32
+    accumulation: the autoencoder's training numerics) against the fp32
+    decoder: decoded states within 1e-2 of the perturbation scale, latent
+    trajectories within 2e-2."""
+    import torch
+    full, sm, st, ps, po, om, s2st, rng = _sample_problem(pda, oracle, seed=2)
+    nst = len(st) * 3
+    k, h1, h2 = 4, 256, 128
+    def bf(a):
+        return torch.from_numpy(a.astype(np.float32)).cuda().to(torch.bfloat16).float()
+    W1, W2, W3 = bf(rng.normal(0, 0.5, (h1, k))), bf(rng.normal(0, 0.1, (h2, h1))), bf(rng.normal(0, 0.1, (nst, h2)))
+    b1, b2, b3 = (torch.from_numpy(rng.normal(0, 0.1, m).astype(np.float32)).cuda() for m in (h1, h2, nst))
+    uref = np.zeros(nst)
+    uref[0::3] = 1.0
+    ur, sc = torch.from_numpy(uref).cuda(), torch.full((nst,), 0.05, dtype=torch.float64, device="cuda")
+    r32 = pda.LspgRom.mlp(ps, s2st, ur, sc, W1, b1, W2, b2, W3, b3, tensor_cores=False)
+    rtc = pda.LspgRom.mlp(ps, s2st, ur, sc, W1, b1, W2, b2, W3, b3, tensor_cores=True)
+    x0 = torch.tensor([0.2, -0.1, 0.05, 0.1], dtype=torch.float64, device="cuda")
+    y32, ytc = r32.decode(x0), rtc.decode(x0)
+    pert = (y32 - ur).abs().max().item()
+    assert (ytc - y32).abs().max().item() <= 1e-2 * pert
+    xa, xb = x0.clone(), x0.clone()
+    r32.advance_bdf1(xa, 0.01, 3, 6, 1e-10)
+    rtc.advance_bdf1(xb, 0.01, 3, 6, 1e-10)
+    assert torch.allclose(xa, xb, rtol=2e-2, atol=1e-3), (xa, xb)
+    with pytest.raises(pda.PdaError):  # non-bf16 weights are refused in tensor-core mode
+        pda.LspgRom.mlp(ps, s2st, ur, sc, W1, b1, W2, b2, W3 + 1e-4, b3, tensor_cores=True)
