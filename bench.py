@@ -394,6 +394,15 @@ def wl_batched_swe(c):
     return batched_swe_workload(c.pda, c.torch, c.stream, c.orc, c.threads)
 
 
+def _pkg_module(name):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("pda_gb300_" + name,
+                                                  os.path.join(REPO, "pressio-demoapps_gb300", name + ".py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def _rom_module():
     import importlib.util
     spec = importlib.util.spec_from_file_location("pda_gb300_rom", os.path.join(REPO, "pressio-demoapps_gb300",
@@ -519,7 +528,7 @@ def wl_lspg_step(c, n=256, latent=12, steps=20, gn_iters=3):
     sm, gids, st, s2st = setup.sample_mesh(0.01, seed=7)
     ps = setup.problem({"gravity": 7.0, "coriolis": -2.0, "pulseMagnitude": 0.1}, mesh=sm)
     g = torch.Generator(device="cuda").manual_seed(0)
-    phi = torch.linalg.qr(torch.randn(setup.N, latent, generator=g, device="cuda", dtype=torch.float64))[0] * 0.3
+    phi = torch.randn(setup.N, latent, generator=g, device="cuda", dtype=torch.float64) * (0.3 / setup.N ** 0.5)
     W1 = torch.randn(256, latent, generator=g, device="cuda") * 0.3
     b1 = torch.randn(256, generator=g, device="cuda") * 0.1
     W2 = torch.randn(1024, 256, generator=g, device="cuda") * 0.05
@@ -572,11 +581,17 @@ def batched_swe_workload(pda, torch, stream, orc, threads, n_inst=512, steps=3):
     grav = brng.uniform(5.0, 10.0, n_inst)
     cor = brng.uniform(-4.0, -1.0, n_inst)
     amp = brng.uniform(0.05, 0.2, n_inst)
-    meshes = {int(n): pda.create_full_mesh((int(n), int(n)), (-5.0, 5.0, -5.0, 5.0), 7) for n in sorted(set(ns))}
+    # under torchrun every rank advances its share of the instances (no
+    # exchange between instances); timings are max-reduced, work summed
+    multi = _pkg_module("multi")
+    rank, world, _ = rank_info()
+    mine = multi.shard_by_cost([float(n) ** 2 for n in ns], world)[rank]
+    meshes = {int(n): pda.create_full_mesh((int(n), int(n)), (-5.0, 5.0, -5.0, 5.0), 7) for n in sorted(set(ns[mine]))}
     t0 = time.perf_counter()
     probs = [pda.create_problem(meshes[int(ns[i])], pda.Swe2d.SlipWall, pda.InviscidFluxReconstruction.Weno5, 1,
                                 {"gravity": grav[i], "coriolis": cor[i], "pulseMagnitude": amp[i]}, stream=stream)
-             for i in range(n_inst)]
+             for i in mine]
+    n_inst = len(mine)
     B = pda.create_batch(probs, stream=stream)
     U = B.initialCondition()
     setup_s = time.perf_counter() - t0
@@ -585,11 +600,15 @@ def batched_swe_workload(pda, torch, stream, orc, threads, n_inst=512, steps=3):
     dt = 0.005
     B.advance_ssprk3(U, 0.0, dt, 1)  # capture + warm-up
     l0 = B.launch_count()
+    if world > 1:
+        torch.distributed.barrier()
     ms = _time_gpu(torch, stream, lambda: B.advance_ssprk3(U, 0.0, dt, steps), 1, warm=0)
+    ms = multi.max_over_ranks(ms, device="cuda")
     launches = (B.launch_count() - l0) // steps
-    cells = B.totalCells
+    cells = int(multi.sum_over_ranks(B.totalCells, device="cuda"))
     w = {"config": "batched_swe_slipwall_weno5_ssprk3_dt0.005_512_instances_n64-512",
-         "instances": n_inst, "total_cells": cells, "steps_timed": steps, "ms_per_step": ms / steps,
+         "instances": len(ns), "instances_per_rank": n_inst, "ranks": world,
+         "total_cells": cells, "steps_timed": steps, "ms_per_step": ms / steps,
          "value": 3 * cells * steps / (ms * 1e-3) / 1e9, "unit": "Gcell-updates/s",
          "projected_500_steps_s": 500 * ms / steps * 1e-3, "launches_per_step": launches,
          "tile_shapes": {"x": shapes[0], "y": shapes[1]},
@@ -602,8 +621,9 @@ def batched_swe_workload(pda, torch, stream, orc, threads, n_inst=512, steps=3):
                     1, warm=0)
     w["per_instance_launch_ms_per_step"] = ms1
     w["batching_speedup"] = ms1 / (ms / steps)
-    if orc is not None:
-        sample = [int(i) for i in np.argsort(ns)[[0, n_inst // 2, n_inst - 1]]]
+    if orc is not None and rank == 0:
+        nm = ns[mine]
+        sample = [mine[int(i)] for i in np.argsort(nm)[[0, len(nm) // 2, len(nm) - 1]]]
         tot_cells, tot_s = 0, 0.0
         import tempfile
         for i in sample:
@@ -662,8 +682,11 @@ def main():
     pda = ge.package()
     stream = torch.cuda.Stream()
     if args.workload:
-        print(json.dumps({"workloads": extra_workloads(pda, torch, stream, cpu=not args.no_cpu_baseline,
-                                                       names=args.workload)}))
+        res = extra_workloads(pda, torch, stream, cpu=not args.no_cpu_baseline and rank == 0, names=args.workload)
+        if rank == 0:
+            print(json.dumps({"workloads": res}))
+        if world > 1:
+            torch.distributed.destroy_process_group()
         return 0
     mesh, prob, Uh = build_workload(pda, torch, stream)
     cells = N_CELLS_SIDE ** 2

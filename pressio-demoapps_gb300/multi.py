@@ -1,0 +1,45 @@
+"""One process per GPU: partitioning of independent problem instances across
+ranks and the host-side reductions of the timing and metrics.
+
+The path has no exchange step: batched instances (different parameters and
+meshes) are independent, so rank r advances its share of the instances on
+its own GPU and only scalars cross ranks (the slowest rank's time, summed
+work counts).  A single large mesh is replicated, not split, in this build.
+"""
+from __future__ import annotations
+
+
+def shard_by_cost(costs, world):
+    """Deterministic partition of instance indices into `world` shards with
+    balanced total cost (greedy: largest first onto the least-loaded shard,
+    ties to the lower rank); each shard keeps its indices in ascending order."""
+    order = sorted(range(len(costs)), key=lambda i: (-costs[i], i))
+    load = [0.0] * world
+    shards = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        shards[r].append(i)
+        load[r] += costs[i]
+    return [sorted(s) for s in shards]
+
+
+def max_over_ranks(value, device=None):
+    """The largest value over all ranks (a step's time is the slowest rank's)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(value, device=None):
+    """The sum over all ranks (work done by the whole job)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
