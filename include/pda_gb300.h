@@ -61,8 +61,14 @@ typedef int pda_status;
 #define PDA_EULER1D_LAX 2             /* Euler1d::Lax */
 #define PDA_EULER1D_SHU_OSHER 3       /* Euler1d::ShuOsher */
 #define PDA_EULER2D_PERIODIC_SMOOTH 0 /* Euler2d::PeriodicSmooth */
+#define PDA_EULER2D_KELVIN_HELMHOLTZ 1 /* Euler2d::KelvinHelmholtz */
 #define PDA_EULER2D_SEDOV_FULL 2      /* Euler2d::SedovFull */
+#define PDA_EULER2D_SEDOV_SYMMETRY 3  /* Euler2d::SedovSymmetry */
 #define PDA_EULER2D_RIEMANN 4         /* Euler2d::Riemann */
+#define PDA_EULER2D_NORMAL_SHOCK 5    /* Euler2d::NormalShock */
+#define PDA_EULER2D_DOUBLE_MACH_REFLECTION 6 /* Euler2d::DoubleMachReflection */
+#define PDA_EULER2D_CROSS_SHOCK 7     /* Euler2d::CrossShock */
+#define PDA_EULER2D_TESTING_NEUMANN 8 /* Euler2d::testingonlyneumann */
 #define PDA_EULER3D_PERIODIC_SMOOTH 0 /* Euler3d::PeriodicSmooth */
 #define PDA_SWE2D_SLIP_WALL 0         /* Swe2d::SlipWall */
 
@@ -142,6 +148,15 @@ pda_status pda_problem_create(const pda_mesh *mesh, int family, int problem, int
 pda_status pda_problem_create_swe_slip_wall(const pda_mesh *mesh, int scheme, double gravity,
                                             double coriolis, double pulse_magnitude,
                                             void *stream, pda_problem **out);
+
+/* Equivalent of create_cross_shock_problem_eigen(mesh, rec, density,
+ * inletXVel, bottomYVel) (euler2d.hpp:258-285): Euler2d::CrossShock with the
+ * inflow density, inlet x velocity and bottom-inflow y velocity.  The generic
+ * pda_problem_create with PDA_EULER2D_CROSS_SHOCK and no parameters uses the
+ * reference's default values (0.1, 10, 1). */
+pda_status pda_problem_create_cross_shock(const pda_mesh *mesh, int scheme, double density,
+                                          double inlet_x_vel, double bottom_y_vel, void *stream,
+                                          pda_problem **out);
 
 void pda_problem_free(pda_problem *p);
 

@@ -44,6 +44,7 @@ def load():
                                                 C.c_void_p, C.c_void_p]
         L.orc_ssprk3.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64]
         L.orc_rk4.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64]
+        L.orc_ssprk3_py.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64]
         L.orc_weno5.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_weno3.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_set_cube_mode.argtypes = [C.c_int]
@@ -103,6 +104,10 @@ class Problem:
 
     def rk4(self, U, t0, dt, n):
         self.L.orc_rk4(C.c_void_p(self.h), _vp(U), t0, dt, n)
+
+    def ssprk3_py(self, U, t0, dt, n):
+        """SSP-RK3 with the update order of the reference's Python driver."""
+        self.L.orc_ssprk3_py(C.c_void_p(self.h), _vp(U), t0, dt, n)
 
 
 class Oracle:

@@ -680,6 +680,7 @@ struct orc_problem {
   const orc_mesh *m;
   int fam, prob, scheme, ic, nd, dim, h, stencil;
   double icp[10], gamma, gravity, coriolis;
+  double t; /* evaluation time of the current velocity call */
   int32_t *rowptr, *colidx;
   int64_t nnz;
   int patternReady;
@@ -695,6 +696,81 @@ static int colp(int dim, int ax, int k) {
   if (dim == 1) return 2 + 2 * k;
   if (dim == 2) return (ax == 0 ? 3 : 2) + 4 * k;
   return (ax == 0 ? 3 : ax == 1 ? 2 : 6) + 6 * k;
+}
+
+static double energy(double gm1inv, const double *prim, int n);
+
+/* Normal-shock relations for a shock of Mach number M running into gas at
+ * rest, rotated to a shock normal at angle a from the x axis
+ * (impl/euler_rankine_hugoniot.hpp:55-145): prim = {rho, u, v, p}. */
+static void shock_at_rest(const double pre[4], double a, double M, double gamma, double post[4]) {
+  const double M2 = M * M;
+  const double rho = pre[0] * (gamma + 1.) * M2 / (2. + (gamma - 1.) * M2);
+  const double pr = pre[3] * (1. + 2. * gamma / (gamma + 1.) * (M2 - 1.));
+  const double cPre = sqrt(gamma * pre[3] / pre[0]), cPost = sqrt(gamma * pr / rho);
+  const double h = 1. / 2.;
+  const double mRel = sqrt((1. + h * (gamma - 1.) * M2) / (gamma * M2 - h * (gamma - 1.)));
+  const double w = mRel * cPost - M * cPre + 0.;
+  post[0] = rho;
+  post[1] = -w * cos(a);
+  post[2] = -w * sin(a);
+  post[3] = pr;
+}
+
+static void prim_to_cons4(double gm1inv, const double *q, double *u) {
+  u[0] = q[0];
+  u[1] = q[0] * q[1];
+  u[2] = q[0] * q[2];
+  u[3] = energy(gm1inv, q, 4);
+}
+
+/* DoubleMachReflection ghosts (euler_2d_ghost_filler_double_mach_reflection.hpp:
+ * 83-305): copies on the left and right and before the wedge at x = 1/6 on
+ * the bottom, a wall behind it, and on the top the state on either side of
+ * the Mach 10 shock at pi/6 that moves along the wall. */
+static void dmr_ghost(const orc_problem *p, int64_t r, int ax, int minus, int layer, const double *U, int src,
+                      double *g) {
+  const orc_mesh *m = p->m;
+  const int cell = G(m, r, 0);
+  const double wedge = 1. / 6.;
+  if (ax == 1 && !minus) {
+    const double a = M_PI / 6., gm1inv = 1. / (p->gamma - 1.);
+    const double pre[4] = {p->gamma, 0., 0., 1.};
+    double post[4], upre[4], upost[4];
+    shock_at_rest(pre, -a, 10., p->gamma, post);
+    prim_to_cons4(gm1inv, pre, upre);
+    prim_to_cons4(gm1inv, post, upost);
+    const double mult[3] = {1., 2., 3.};
+    const double yg = m->y[cell] + mult[layer] * m->dx[1];
+    const double dist = m->x[cell] - wedge - (10. / cos(a)) * p->t - tan(a) * yg;
+    memcpy(g, dist < 0. ? upost : upre, sizeof(double) * 4);
+    return;
+  }
+  for (int d = 0; d < 4; ++d) g[d] = U[(int64_t)src * 4 + d];
+  if (ax == 1 && minus && !(m->x[cell] < wedge)) g[2] = -g[2];
+}
+
+/* CrossShock ghosts (euler_2d_ghost_filler_cross_shock.hpp:95-248): inflow
+ * state on the left; on the bottom the prescribed momentum (zero normal
+ * momentum for x < 0.5), the cell's density in the first layer and the
+ * prescribed density beyond it, energy from the source cell; copies on the
+ * top and right. */
+static void cross_ghost(const orc_problem *p, int64_t r, int ax, int minus, int layer, const double *U, int src,
+                        double *g) {
+  const orc_mesh *m = p->m;
+  const int cell = G(m, r, 0);
+  const double rho = p->icp[1], uin = p->icp[2], vbot = p->icp[3];
+  if (ax == 0 && minus) {
+    const double q[4] = {rho, uin, 0., 1.};
+    prim_to_cons4(1. / (p->gamma - 1.), q, g);
+    return;
+  }
+  for (int d = 0; d < 4; ++d) g[d] = U[(int64_t)src * 4 + d];
+  if (ax == 1 && minus) {
+    if (layer > 0) g[0] = rho;
+    g[1] = rho * uin;
+    g[2] = m->x[cell] < 0.5 ? 0. : rho * vbot;
+  }
 }
 
 /* Ghost values of one near-boundary row for the scheme stencil stSz: ghost
@@ -717,6 +793,15 @@ static void fill_ghosts(const orc_problem *p, int64_t r, const double *U, double
         int src = cell;
         const int sedovSym = p->fam == E2 && p->prob == 3;
         const int normalShock = p->fam == E2 && p->prob == 5;
+        const int dmr = p->fam == E2 && p->prob == 6, cross = p->fam == E2 && p->prob == 7;
+        if (dmr || cross) {
+          /* same layer rule as the Sedov symmetry filler; the source may be
+             outside a small mesh only where the ghost is a fixed state */
+          const int s = layer == 0 ? cell : opp[layer - 1];
+          if (dmr) dmr_ghost(p, r, ax, minus, layer, U, s < 0 ? cell : s, g + layer * nd);
+          else cross_ghost(p, r, ax, minus, layer, U, s < 0 ? cell : s, g + layer * nd);
+          continue;
+        }
         if (p->fam == E1 || sedovSym || normalShock) {
           /* Ghost1dNeumannFiller; Sedov2dSymmetryGhostFiller
              (euler_2d_ghost_filler_sedov2d_sym.hpp:87-206) */
@@ -906,6 +991,9 @@ orc_problem *orc_problem_create(const orc_mesh *m, int family, int problem, int 
     if (family == E2) {
       if (!strcmp(s, "gamma")) p->gamma = v;
       else if (!strcmp(s, "mach")) p->icp[0] = v;
+      else if (!strcmp(s, "crossShockDensity")) p->icp[1] = v;
+      else if (!strcmp(s, "crossShockInletXVel")) p->icp[2] = v;
+      else if (!strcmp(s, "crossShockBottomYVel")) p->icp[3] = v;
       else if (!strcmp(s, "riemannTopRightPressure")) p->icp[p->ic == 1 ? 4 : 5] = v;
       else if (!strcmp(s, "riemannTopRightXVel")) p->icp[6] = v;
       else if (!strcmp(s, "riemannTopRightYVel")) p->icp[7] = v;
@@ -1037,6 +1125,22 @@ void orc_initial_condition(const orc_problem *p, double *U) {
       }
       return;
     }
+    if (p->prob == 6) {
+      /* doubleMachReflection2dIC (impl/euler_2d_initial_condition.hpp:443-500) */
+      const double a = M_PI / 6., gm1i = 1. / (gamma - 1.);
+      const double pre[4] = {gamma, 0., 0., 1.};
+      double post[4];
+      shock_at_rest(pre, -a, 10., gamma, post);
+      for (int64_t i = 0; i < m->nst; ++i)
+        prim_to_cons4(gm1i, x[i] < 1. / 6. + tan(a) * y[i] ? post : pre, U + i * 4);
+      return;
+    }
+    if (p->prob == 7) {
+      /* crossShockIC (impl/euler_2d_initial_condition.hpp:505-526) */
+      const double q[4] = {p->icp[1], p->icp[2], 0., 1.};
+      for (int64_t i = 0; i < m->nst; ++i) prim_to_cons4(1. / (gamma - 1.), q, U + i * 4);
+      return;
+    }
     if (p->prob == 2 || p->prob == 3) {
       /* sedov2dIC / sedov2dsymmetryIC, impl/euler_2d_initial_condition.hpp:131-249 */
       const double one = 1., two = 2., gm1 = gamma - one, gm1i = one / gm1;
@@ -1128,7 +1232,7 @@ static void row_velocity(const orc_problem *p, int64_t r, const double *U, doubl
 
 void orc_velocity(orc_problem *p, const double *U, double t, double *V) {
   const orc_mesh *m = p->m;
-  (void)t;
+  p->t = t;
 #pragma omp parallel
   {
     double gh[3 * 2 * 3 * 5];
@@ -1223,6 +1327,18 @@ static void row_vj_near(const orc_problem *p, int64_t r, const double *U, double
       else if (ax == 1 && G(m, r, colm(2, 1, 0)) == -1) fac[2] = -1;
     }
     if (p->fam == E2 && p->prob == 5 && ax == 1) fac[2] = -1; /* euler_2d_prob_class.hpp:1150-1162 */
+    if (p->fam == E2 && p->prob == 6 && ax == 1) {
+      /* euler_2d_prob_class.hpp:1164-1193 */
+      const int back = G(m, r, colm(2, 1, 0)) == -1;
+      const int behindWedge = !(m->x[G(m, r, 0)] < 1. / 6.);
+      if (back && behindWedge) fac[2] = -1;
+      if (!back) fac[0] = fac[1] = fac[2] = fac[3] = 0;
+    }
+    if (p->fam == E2 && p->prob == 7) {
+      /* euler_2d_prob_class.hpp:1195-1222 */
+      if (ax == 0 && G(m, r, colm(2, 0, 0)) == -1) fac[0] = fac[1] = fac[2] = fac[3] = 0;
+      if (ax == 1 && G(m, r, colm(2, 1, 0)) == -1) fac[1] = fac[2] = 0;
+    }
     const int32_t l0 = G(m, r, colm(p->dim, ax, 0)), r0 = G(m, r, colp(p->dim, ax, 0)), ci = G(m, r, 0);
     for (int k = 0; k < nd; ++k)
       for (int j = 0; j < nd; ++j) JADD(r * nd + k, ci * nd + j, (JLP[k * nd + j] - JRN[k * nd + j]) * hinv);
@@ -1253,7 +1369,7 @@ static void row_vj_near(const orc_problem *p, int64_t r, const double *U, double
 void orc_velocity_and_jacobian(orc_problem *p, const double *U, double t, double *V, int32_t *rowptr,
                                int32_t *colidx, double *vals) {
   const orc_mesh *m = p->m;
-  (void)t;
+  p->t = t;
   build_pattern(p);
   memcpy(rowptr, p->rowptr, sizeof(int32_t) * (m->nsm * p->nd + 1));
   memcpy(colidx, p->colidx, sizeof(int32_t) * p->nnz);
@@ -1288,6 +1404,30 @@ void orc_ssprk3(orc_problem *p, double *U, double t0, double dt, int64_t nsteps)
   }
   free(aux);
   free(r);
+}
+
+/* SSP-RK3 as the reference's Python driver writes it (pressiodemoapps/
+ * __init__.py:155-185): u1 = u + dt v; u2 = 3/4 u + 1/4 u1 + (1/4 dt) v;
+ * u = 1/3 (u + 2 u2 + (2 dt) v), stage times t, t + dt, t + dt*0.5. */
+void orc_ssprk3_py(orc_problem *p, double *U, double t0, double dt, int64_t nsteps) {
+  const int64_t n = p->m->nst * p->nd;
+  double *u1 = malloc(sizeof(double) * n), *u2 = malloc(sizeof(double) * n), *v = malloc(sizeof(double) * n);
+  const double third = 1. / 3., quarter = 1. / 4., threeQuarters = 3. / 4., two = 2.;
+  double t = t0;
+  for (int64_t s = 0; s < nsteps; ++s) {
+    orc_velocity(p, U, t, v);
+    for (int64_t i = 0; i < n; ++i) u1[i] = U[i] + dt * v[i];
+    orc_velocity(p, u1, t + dt, v);
+    const double c1 = quarter * dt;
+    for (int64_t i = 0; i < n; ++i) u2[i] = threeQuarters * U[i] + quarter * u1[i] + c1 * v[i];
+    orc_velocity(p, u2, t + dt * 0.5, v);
+    const double c2 = two * dt;
+    for (int64_t i = 0; i < n; ++i) U[i] = third * (U[i] + two * u2[i] + c2 * v[i]);
+    t += dt;
+  }
+  free(u1);
+  free(u2);
+  free(v);
 }
 
 void orc_rk4(orc_problem *p, double *U, double t0, double dt, int64_t nsteps) {

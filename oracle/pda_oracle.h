@@ -33,6 +33,7 @@ void orc_velocity_and_jacobian(orc_problem *p, const double *U, double t, double
                                int32_t *colidx, double *vals);
 void orc_ssprk3(orc_problem *p, double *U, double t0, double dt, int64_t nsteps);
 void orc_rk4(orc_problem *p, double *U, double t0, double dt, int64_t nsteps);
+void orc_ssprk3_py(orc_problem *p, double *U, double t0, double dt, int64_t nsteps);
 void orc_weno5(const double q7[7], double out4[4]);
 void orc_weno3(const double q5[5], double out4[4]);
 /* point-wise functions, exported for tests of the device numerics */

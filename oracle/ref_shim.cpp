@@ -7,7 +7,7 @@
 //
 // API surface wrapped: load_cellcentered_uniform_mesh_eigen (mesh.hpp:87),
 // create_problem_eigen (euler1d.hpp:82, euler2d.hpp:88-146, euler3d.hpp:80,
-// swe2d.hpp:170-195), initialCondition, rightHandSide, rightHandSideAndJacobian
+// swe2d.hpp:170-195), create_cross_shock_problem_eigen (euler2d.hpp:258-285), initialCondition, rightHandSide, rightHandSideAndJacobian
 // (adapter_cpp.hpp:193-221).
 #include <cstdint>
 #include <cstring>
@@ -96,6 +96,15 @@ void *ref_create(const char *meshdir, int family, int problem, int scheme, int i
     const mesh_t &mr = *mesh;
     if (family == 0) {
       return make(std::move(mesh), pda::create_problem_eigen(mr, (pda::Euler1d)problem, rec));
+    } else if (family == 1 && problem == 7) {
+      // CrossShock: the generic factory passes no initial-condition
+      // parameters, which this problem reads; use its own factory
+      // (euler2d.hpp:258-299) with the defaults or the given values
+      double v[3] = {0.1, 10., 1.};
+      const char *nm[3] = {"crossShockDensity", "crossShockInletXVel", "crossShockBottomYVel"};
+      for (int k = 0; k < 3; ++k)
+        if (params.count(nm[k])) v[k] = params[nm[k]];
+      return make(std::move(mesh), pda::create_cross_shock_problem_eigen(mr, rec, v[0], v[1], v[2]));
     } else if (family == 1) {
       if (np > 0)
         return make(std::move(mesh), pda::create_problem_eigen(mr, (pda::Euler2d)problem, rec, icflag, params));

@@ -90,6 +90,8 @@ _SIGS = {
                                      C.c_void_p, C.POINTER(C.c_void_p)]),
     "pda_problem_create_swe_slip_wall": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double,
                                                    C.c_double, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "pda_problem_create_cross_shock": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double,
+                                                 C.c_void_p, C.POINTER(C.c_void_p)]),
     "pda_problem_free": (None, [C.c_void_p]),
     "pda_problem_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int64),
                                     C.POINTER(C.c_int64)]),
@@ -569,6 +571,16 @@ def create_slip_wall_swe_2d_problem(mesh, scheme, gravity, coriolis, pulse_magni
     _check(lib().pda_problem_create_swe_slip_wall(mesh._h, int(scheme), float(gravity), float(coriolis),
                                                   float(pulse_magnitude), s, C.byref(h)))
     return Problem(mesh, 3, h, s)
+
+
+def create_cross_shock_problem(mesh, scheme, density=0.1, inletXVel=10.0, bottomYVel=1.0, stream=None):
+    """Mirror of create_cross_shock_problem (euler2d.hpp:258-299; the Python
+    binding's name, src_py/main_binder.cc:476)."""
+    h = C.c_void_p()
+    s = _stream_handle(stream)
+    _check(lib().pda_problem_create_cross_shock(mesh._h, int(scheme), float(density), float(inletXVel),
+                                                float(bottomYVel), s, C.byref(h)))
+    return Problem(mesh, 1, h, s)
 
 
 class ProblemBatch:

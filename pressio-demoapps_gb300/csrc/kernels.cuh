@@ -130,6 +130,30 @@ __device__ __forceinline__ void load_cell(double q[NDPC], const double *__restri
   }
 }
 
+// Stencil entry i of a row table: a mesh cell, or a ghost built from a cell
+// by the entry's recipe (time enters through the moving-shock recipe).
+template <int NDPC>
+__device__ __forceinline__ void load_entry(double q[NDPC], const double *__restrict__ U, int c, uint8_t rid,
+                                           int reflectDof, const MeshArgs &m, const double *gsx,
+                                           const double *gsy, size_t i) {
+  if (rid < 2) {
+    load_cell<NDPC>(q, U, c, rid == 1, reflectDof);
+    return;
+  }
+  const GhostRecipe &g = m.recipes[rid - 2];
+  if (g.op[0] == 3) {
+    const double dist = ((gsx[i] - m.shockX0) - m.shockSpeed * m.time) - m.shockSlope * gsy[i];
+#pragma unroll
+    for (int d = 0; d < NDPC; ++d) q[d] = dist < 0. ? m.post[d] : m.pre[d];
+    return;
+  }
+#pragma unroll
+  for (int d = 0; d < NDPC; ++d) {
+    const uint8_t op = g.op[d];
+    q[d] = op == 2 ? g.val[d] : (op == 1 ? -__ldg(U + (size_t)c * NDPC + d) : __ldg(U + (size_t)c * NDPC + d));
+  }
+}
+
 // Reference per-cell V (velocityOnlyNearBdCellsImpl / velocityOnlyInnerCellsImpl)
 template <int FAM, int SCHEME>
 __global__ void __launch_bounds__(128)
@@ -146,7 +170,8 @@ k_rows_velocity(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U, do
     double q[S][NDPC];
     const size_t base = ((size_t)e * DIM + ax) * S;
 #pragma unroll
-    for (int s = 0; s < S; ++s) load_cell<NDPC>(q[s], U, t.src[base + s], t.flip[base + s], m.reflect[ax]);
+    for (int s = 0; s < S; ++s)
+      load_entry<NDPC>(q[s], U, t.src[base + s], t.flip[base + s], m.reflect[ax], m, t.gsx, t.gsy, base + s);
     double uN[NDPC], uP[NDPC], fL[NDPC], fR[NDPC];
     reconstruct_face<NDPC, SCHEME>(uN, uP, q);
     if (ax == 0) F::template flux<0>(fL, uN, uP, p);
@@ -555,14 +580,16 @@ k_rows_vj_nearbd_par(RowTable t, MeshArgs m, Phys p, const double *__restrict__ 
       const size_t base = ((size_t)e * DIM + ax) * S;
 #pragma unroll
       for (int s = 0; s < G; ++s)
-        load_cell<NDPC>(q[s], U, t.src[base + side + s], t.flip[base + side + s], m.reflect[ax]);
+        load_entry<NDPC>(q[s], U, t.src[base + side + s], t.flip[base + side + s], m.reflect[ax], m, t.gsx, t.gsy,
+                         base + side + s);
       double uN[NDPC], uP[NDPC];
       reconstruct_face<NDPC, SCHEME>(uN, uP, q);
       double q1[2][NDPC];
       const size_t b1 = ((size_t)e * DIM + ax) * 3;
 #pragma unroll
       for (int s = 0; s < 2; ++s)
-        load_cell<NDPC>(q1[s], U, t.src1[b1 + side + s], t.flip1[b1 + side + s], m.reflect[ax]);
+        load_entry<NDPC>(q1[s], U, t.src1[b1 + side + s], t.flip1[b1 + side + s], m.reflect[ax], m, t.gsx1,
+                         t.gsy1, b1 + side + s);
       if (ax == 0) { F::template flux<0>(o.fl, uN, uP, p); F::template flux_jac<0>(o.JN, o.JP, q1[0], q1[1], p); }
       if constexpr (DIM > 1) if (ax == 1) { F::template flux<1>(o.fl, uN, uP, p); F::template flux_jac<1>(o.JN, o.JP, q1[0], q1[1], p); }
       if constexpr (DIM > 2) if (ax == 2) { F::template flux<2>(o.fl, uN, uP, p); F::template flux_jac<2>(o.JN, o.JP, q1[0], q1[1], p); }
@@ -653,7 +680,8 @@ k_rows_vj_nearbd(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U,
       double q[S][NDPC];
       const size_t base = ((size_t)e * DIM + ax) * S;
 #pragma unroll
-      for (int s = 0; s < S; ++s) load_cell<NDPC>(q[s], U, t.src[base + s], t.flip[base + s], m.reflect[ax]);
+      for (int s = 0; s < S; ++s)
+        load_entry<NDPC>(q[s], U, t.src[base + s], t.flip[base + s], m.reflect[ax], m, t.gsx, t.gsy, base + s);
       double uN[NDPC], uP[NDPC], fL[NDPC], fR[NDPC];
       reconstruct_face<NDPC, SCHEME>(uN, uP, q);
       if (ax == 0) F::template flux<0>(fL, uN, uP, p);
@@ -670,7 +698,8 @@ k_rows_vj_nearbd(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U,
       double q[3][NDPC];
       const size_t base = ((size_t)e * DIM + ax) * 3;
 #pragma unroll
-      for (int s = 0; s < 3; ++s) load_cell<NDPC>(q[s], U, t.src1[base + s], t.flip1[base + s], m.reflect[ax]);
+      for (int s = 0; s < 3; ++s)
+        load_entry<NDPC>(q[s], U, t.src1[base + s], t.flip1[base + s], m.reflect[ax], m, t.gsx1, t.gsy1, base + s);
       double JLN[NDPC * NDPC], JLP[NDPC * NDPC], JRN[NDPC * NDPC], JRP[NDPC * NDPC];
       if (ax == 0) { F::template flux_jac<0>(JLN, JLP, q[0], q[1], p); F::template flux_jac<0>(JRN, JRP, q[1], q[2], p); }
       if constexpr (DIM > 1) if (ax == 1) { F::template flux_jac<1>(JLN, JLP, q[0], q[1], p); F::template flux_jac<1>(JRN, JRP, q[1], q[2], p); }

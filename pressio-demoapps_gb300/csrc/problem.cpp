@@ -79,6 +79,30 @@ double energy2(double gm1inv, const double *prim, int n) {
   return prim[4] * gm1inv + half * prim[0] * (usq + vsq + wsq);
 }
 
+// Post-shock primitive state {rho, u, v, p} behind a shock of Mach number
+// `mach` moving into gas at rest, the shock normal at `angle` from the x axis
+// (computePostShockConditionsFromPreshockAtRest over the normal-shock
+// relations, impl/euler_rankine_hugoniot.hpp:55-145).
+void post_shock_at_rest(const double pre[4], double angle, double mach, double gamma, double post[4]) {
+  const double one = 1., two = 2.;
+  const double sinA = std::sin(angle), cosA = std::cos(angle);
+  const double rhoPre = pre[0], velPre = 0., pPre = pre[3];
+  const double machShockSq = mach * mach;
+  const double rhoPost = rhoPre * (gamma + one) * machShockSq / (two + (gamma - one) * machShockSq);
+  const double pPost = pPre * (one + two * gamma / (gamma + one) * (machShockSq - one));
+  const double aPre = std::sqrt(gamma * pPre / rhoPre);
+  const double aPost = std::sqrt(gamma * pPost / rhoPost);
+  const double half = one / two;
+  const double num = (one + half * (gamma - one) * machShockSq);
+  const double den = gamma * machShockSq - half * (gamma - one);
+  const double machRelPost = std::sqrt(num / den);
+  const double velPost = machRelPost * aPost - mach * aPre + velPre;
+  post[0] = rhoPost;
+  post[1] = -velPost * cosA;
+  post[2] = -velPost * sinA;
+  post[3] = pPost;
+}
+
 void initial_condition(const pda_problem &P, std::vector<double> &st) {
   const Mesh &m = *P.mesh;
   const int64_t N = m.stencilMeshSize;
@@ -231,27 +255,39 @@ void initial_condition(const pda_problem &P, std::vector<double> &st) {
       const double angle = zero, xShock = one / six;
       const double gammaMinusOne = gamma - one, gammaMinusOneInv = one / gammaMinusOne;
       const double machShock = P.icParams[0];
-      double pre[4] = {gamma, zero, zero, one}, post[4];
-      {
-        const double sinA = std::sin(angle), cosA = std::cos(angle);
-        const double rhoPre = pre[0], velPre = zero, pPre = pre[3];
-        const double machShockSq = machShock * machShock;
-        const double rhoPost = rhoPre * (gamma + one) * machShockSq / (two + (gamma - one) * machShockSq);
-        const double pPost = pPre * (one + two * gamma / (gamma + one) * (machShockSq - one));
-        const double aPre = std::sqrt(gamma * pPre / rhoPre);
-        const double aPost = std::sqrt(gamma * pPost / rhoPost);
-        const double half = one / two;
-        const double num = (one + half * (gamma - one) * machShockSq);
-        const double den = gamma * machShockSq - half * (gamma - one);
-        const double machRelPost = std::sqrt(num / den);
-        const double velPost = machRelPost * aPost - machShock * aPre + velPre;
-        post[0] = rhoPost;
-        post[1] = -velPost * cosA;
-        post[2] = -velPost * sinA;
-        post[3] = pPost;
-      }
+      const double pre[4] = {gamma, zero, zero, one};
+      double post[4];
+      post_shock_at_rest(pre, angle, machShock, gamma, post);
+      (void)two;
       for (int64_t i = 0; i < N; ++i) {
         const double *q = x[i] < xShock ? post : pre;
+        st[i * 4] = q[0];
+        st[i * 4 + 1] = q[0] * q[1];
+        st[i * 4 + 2] = q[0] * q[2];
+        st[i * 4 + 3] = energy2(gammaMinusOneInv, q, 4);
+      }
+    } else if (P.probEnum == 6) {
+      // doubleMachReflection2dIC (impl/euler_2d_initial_condition.hpp:443-500)
+      const double zero = 0., one = 1., six = 6.;
+      const double xShockBottom = one / six, angle = M_PI / six;
+      const double shockSlope = std::tan(angle);
+      const double gammaMinusOneInv = one / (gamma - one);
+      const double pre[4] = {gamma, zero, zero, one};
+      double post[4];
+      post_shock_at_rest(pre, -angle, 10., gamma, post);
+      for (int64_t i = 0; i < N; ++i) {
+        const double xShock = xShockBottom + shockSlope * y[i];
+        const double *q = x[i] < xShock ? post : pre;
+        st[i * 4] = q[0];
+        st[i * 4 + 1] = q[0] * q[1];
+        st[i * 4 + 2] = q[0] * q[2];
+        st[i * 4 + 3] = energy2(gammaMinusOneInv, q, 4);
+      }
+    } else if (P.probEnum == 7) {
+      // crossShockIC (impl/euler_2d_initial_condition.hpp:505-526)
+      const double gammaMinusOneInv = 1. / (gamma - 1.);
+      const double q[4] = {P.icParams[1], P.icParams[2], 0., 1.};
+      for (int64_t i = 0; i < N; ++i) {
         st[i * 4] = q[0];
         st[i * 4 + 1] = q[0] * q[1];
         st[i * 4 + 2] = q[0] * q[2];
@@ -326,9 +362,11 @@ int ghost_source(const Mesh &m, int bc, int64_t r, int ax, bool minusSide, int L
     return m.g(r, minusSide ? col_plus(m.dim, ax, k) : col_minus(m.dim, ax, k));
   };
   const int cell = m.g(r, 0);
-  if (bc == BC_NEUMANN1D || bc == BC_SEDOVSYM || bc == BC_NORMALSHOCK) {
+  if (bc == BC_NEUMANN1D || bc == BC_SEDOVSYM || bc == BC_NORMALSHOCK || bc == BC_DMR || bc == BC_CROSSSHOCK) {
     // euler_1d_ghost_filler.hpp:104-142, euler_2d_ghost_filler_sedov2d_sym.hpp:87-206,
-    // euler_2d_ghost_filler_normal_shock.hpp:87-205
+    // euler_2d_ghost_filler_normal_shock.hpp:87-205,
+    // euler_2d_ghost_filler_double_mach_reflection.hpp:83-264,
+    // euler_2d_ghost_filler_cross_shock.hpp:95-248
     if (L == 0) return cell;
     return opp(L - 1);
   }
@@ -345,13 +383,72 @@ int ghost_source(const Mesh &m, int bc, int64_t r, int ax, bool minusSide, int L
   throw Error(PDA_ERR_UNSUPPORTED, "this problem has no ghost-cell rule for meshes with boundaries");
 }
 
-// whether a ghost on this side negates the face-normal momentum (the mesh
-// args' reflect dof): walls of the slip-wall problem on every side, the
-// Sedov symmetry planes on the left and bottom (minus) sides only
-uint8_t ghost_flip(int bc, int ax, bool minusSide) {
-  if (bc == BC_SEDOVSYM) return minusSide ? 1 : 0;
-  if (bc == BC_NORMALSHOCK) return ax == 1 ? 1 : 0;
-  return 1;
+// Ghost recipe ids: 0 copies the source cell, 1 negates the face-normal
+// momentum (the mesh args' reflect dof), r >= 2 is the problem's recipe r - 2.
+constexpr uint8_t kCopy = 0, kReflect = 1;
+// double Mach reflection: the moving shock on the top boundary
+constexpr uint8_t kDmrShock = 2;
+// cross shock: inflow state on the left; bottom layer 0 (cell's density and
+// energy) and layers >= 1 (prescribed density, the source's energy), each
+// for x < 0.5 (no normal momentum) and x >= 0.5 (the bottom inflow momentum)
+constexpr uint8_t kCsInflow = 2, kCsBottom0Lo = 3, kCsBottom0Hi = 4, kCsBottom1Lo = 5, kCsBottom1Hi = 6;
+// wedge position of the double Mach reflection (1/6, as the reference writes it)
+const double kDmrWedge = 1. / 6.;
+
+// Recipe of ghost layer L on one side of row r: walls of the slip-wall
+// problem on every side; the Sedov symmetry planes on the left and bottom;
+// the normal-shock walls on the top and bottom; the double Mach reflection
+// wall from the wedge on (euler_2d_ghost_filler_double_mach_reflection.hpp:
+// 133-147) under the moving shock (:115-129); the cross-shock inflow states
+// (euler_2d_ghost_filler_cross_shock.hpp:107-112, :133-147, :173-187).
+uint8_t ghost_recipe(const pda_problem &P, int64_t r, int ax, bool minusSide, int L) {
+  const Mesh &m = *P.mesh;
+  switch (P.bc) {
+    case BC_SEDOVSYM: return minusSide ? kReflect : kCopy;
+    case BC_NORMALSHOCK: return ax == 1 ? kReflect : kCopy;
+    case BC_DMR:
+      if (ax == 0) return kCopy;
+      if (!minusSide) return kDmrShock;
+      return m.x[m.g(r, 0)] < kDmrWedge ? kCopy : kReflect;
+    case BC_CROSSSHOCK: {
+      if (ax == 0) return minusSide ? kCsInflow : kCopy;
+      if (!minusSide) return kCopy;
+      const bool lo = m.x[m.g(r, 0)] < 0.5;
+      if (L == 0) return lo ? kCsBottom0Lo : kCsBottom0Hi;
+      return lo ? kCsBottom1Lo : kCsBottom1Hi;
+    }
+    default: return kReflect;
+  }
+}
+
+// whether the recipe reads its source cell (constant states and the moving
+// shock do not)
+bool recipe_reads_source(const pda_problem &P, uint8_t rid) {
+  if (rid < 2) return true;
+  const GhostRecipe &g = P.recipes[rid - 2];
+  if (g.op[0] == 3) return false;
+  for (int d = 0; d < P.ndpc; ++d)
+    if (g.op[d] != 2) return true;
+  return false;
+}
+
+// Source cell and recipe of one ghost entry; the ghost's position
+// (cell x, cell y + (L + 1) dy: the points where the double Mach reflection
+// filler evaluates the shock distance) when the table keeps positions.
+void ghost_entry(const pda_problem &P, int64_t r, int ax, bool minusSide, int L, int *src, uint8_t *rid,
+                 double *gx, double *gy) {
+  const Mesh &m = *P.mesh;
+  *rid = ghost_recipe(P, r, ax, minusSide, L);
+  *src = m.g(r, 0);
+  if (recipe_reads_source(P, *rid)) {
+    *src = ghost_source(m, P.bc, r, ax, minusSide, L);
+    PDA_REQUIRE(*src >= 0, PDA_ERR_INVALID_ARGUMENT, "mesh too small for the ghost layers of this scheme");
+  }
+  if (gx) {
+    const int c = m.g(r, 0);
+    *gx = m.x[c];
+    *gy = m.y[c] + (L + 1.0) * m.dx[1];
+  }
 }
 
 // Stencil of the scheme (positions -h..h) for every row of the table.
@@ -362,6 +459,8 @@ void build_stencil(const pda_problem &P, Table &T, const std::vector<int32_t> &r
   T.cell.resize(rowList.size());
   T.src.assign(rowList.size() * D * S, 0);
   T.flip.assign(rowList.size() * D * S, 0);
+  T.gsx.assign(P.timeDependent && allowGhost ? rowList.size() * D * S : 0, 0.);
+  T.gsy.assign(T.gsx.size(), 0.);
   for (size_t e = 0; e < rowList.size(); ++e) {
     const int64_t r = rowList[e];
     T.cell[e] = m.g(r, 0);
@@ -377,11 +476,9 @@ void build_stencil(const pda_problem &P, Table &T, const std::vector<int32_t> &r
             T.src[pos] = c;
           } else {
             PDA_REQUIRE(allowGhost, PDA_ERR_INTERNAL, "unexpected boundary neighbour in an inner row");
-            const int gsrc = ghost_source(m, P.bc, r, ax, minus, k - 1);
-            PDA_REQUIRE(gsrc >= 0, PDA_ERR_INVALID_ARGUMENT,
-                        "mesh too small for the ghost layers of this scheme");
-            T.src[pos] = gsrc;
-            T.flip[pos] = ghost_flip(P.bc, ax, minus);
+            const bool pos_ = !T.gsx.empty();
+            ghost_entry(P, r, ax, minus, k - 1, &T.src[pos], &T.flip[pos], pos_ ? &T.gsx[pos] : nullptr,
+                        pos_ ? &T.gsy[pos] : nullptr);
           }
         }
       }
@@ -459,6 +556,26 @@ void jac_factors(const pda_problem &P, int64_t r, int ax, double *f) {
   }
   // euler_2d_prob_class.hpp:1150-1162: reflective along y, Neumann along x
   if (P.bc == BC_NORMALSHOCK && ax == 1) f[2] = -1.;
+  if (P.bc == BC_DMR && ax == 1) {
+    // euler_2d_prob_class.hpp:1164-1193: Neumann along x; along y Neumann
+    // before the wedge and reflective after it on the bottom, Dirichlet
+    // (shock states) on the top
+    const Mesh &m = *P.mesh;
+    const bool back = m.g(r, col_minus(2, 1, 0)) == -1;
+    const double myX = m.x[m.g(r, 0)];
+    if (back && myX >= kDmrWedge) f[2] = -1.;
+    else if (!back)
+      for (int j = 0; j < 4; ++j) f[j] = 0.;
+  }
+  if (P.bc == BC_CROSSSHOCK) {
+    // euler_2d_prob_class.hpp:1195-1222: Dirichlet on the left, Neumann on
+    // the right and top, Dirichlet momentum with Neumann density and energy
+    // on the bottom
+    const Mesh &m = *P.mesh;
+    if (ax == 0 && m.g(r, col_minus(2, 0, 0)) == -1)
+      for (int j = 0; j < 4; ++j) f[j] = 0.;
+    if (ax == 1 && m.g(r, col_minus(2, 1, 0)) == -1) f[1] = f[2] = 0.;
+  }
 }
 
 void build_inner_table(pda_problem &P, bool withJ) {
@@ -496,6 +613,9 @@ void build_near_table(pda_problem &P, bool withJ) {
   T.flip1.assign(n * P.dim * 3, 0);
   T.jpos1.assign(n * P.dim * 3, -1);
   T.jfac.assign(n * P.dim * P.ndpc, 1.0);
+  T.gsx1.assign(P.timeDependent ? n * P.dim * 3 : 0, 0.);
+  T.gsy1.assign(T.gsx1.size(), 0.);
+  const bool keepPos = !T.gsx1.empty();
   for (size_t e = 0; e < n; ++e) {
     const int64_t r = m.nearBd[e];
     for (int ax = 0; ax < P.dim; ++ax) {
@@ -507,15 +627,15 @@ void build_near_table(pda_problem &P, bool withJ) {
         T.src1[base] = cm;
         T.jpos1[base] = block_offset(P, r, cm);
       } else {
-        T.src1[base] = ghost_source(m, P.bc, r, ax, true, 0);
-        T.flip1[base] = ghost_flip(P.bc, ax, true);
+        ghost_entry(P, r, ax, true, 0, &T.src1[base], &T.flip1[base], keepPos ? &T.gsx1[base] : nullptr,
+                    keepPos ? &T.gsy1[base] : nullptr);
       }
       if (cp != -1) {
         T.src1[base + 2] = cp;
         T.jpos1[base + 2] = block_offset(P, r, cp);
       } else {
-        T.src1[base + 2] = ghost_source(m, P.bc, r, ax, false, 0);
-        T.flip1[base + 2] = ghost_flip(P.bc, ax, false);
+        ghost_entry(P, r, ax, false, 0, &T.src1[base + 2], &T.flip1[base + 2],
+                    keepPos ? &T.gsx1[base + 2] : nullptr, keepPos ? &T.gsy1[base + 2] : nullptr);
       }
       jac_factors(P, r, ax, &T.jfac[(e * P.dim + ax) * P.ndpc]);
     }
@@ -524,13 +644,26 @@ void build_near_table(pda_problem &P, bool withJ) {
   P.nearBuiltJ = true;
 }
 
+// the problem's ghost recipes on the device (first evaluation; creation
+// stays host-only)
+void sync_recipes(pda_problem &P) {
+  if (P.recipes.empty() || P.d_recipes.p) return;
+  P.d_recipes.alloc(P.recipes.size());
+  PDA_CUDA(cudaMemcpy(P.d_recipes.p, P.recipes.data(), P.recipes.size() * sizeof(GhostRecipe),
+                      cudaMemcpyHostToDevice));
+  P.margs.recipes = P.d_recipes.p;
+}
+
 void check_launch(pda_problem &P, int n = 1) {
   P.launches += n;
   PDA_CUDA(cudaGetLastError());
 }
 
 // --------------------------------------------------------------- evaluation
-void velocity(pda_problem &P, const double *U, double *V, cudaEvent_t *ev = nullptr) {
+void velocity(pda_problem &P, const double *U, double *V, double t, cudaEvent_t *ev = nullptr) {
+  sync_recipes(P);
+  MeshArgs ma = P.margs;
+  ma.time = t;
   if (P.useStruct) {
     const Box &b = P.box;
     double *Fb[3] = {nullptr, nullptr, nullptr};
@@ -541,27 +674,30 @@ void velocity(pda_problem &P, const double *U, double *V, cudaEvent_t *ev = null
       Fb[a] = P.F[a].p;
     }
     int nl = 0;
-    P.L->struct_velocity(P.scheme, b, P.margs, P.phys, U, Fb, V, P.stream, &nl, ev);
+    P.L->struct_velocity(P.scheme, b, ma, P.phys, U, Fb, V, P.stream, &nl, ev);
     check_launch(P, nl);
   } else {
     build_inner_table(P, false);
     P.innerT.sync();
     if (P.innerT.t.nrows > 0) {
-      P.L->rows_velocity(P.scheme, P.innerT.t, P.margs, P.phys, U, V, P.stream);
+      P.L->rows_velocity(P.scheme, P.innerT.t, ma, P.phys, U, V, P.stream);
       check_launch(P);
     }
   }
   if (!P.structAll) {
     P.nearT.sync();
     if (P.nearT.t.nrows > 0) {
-      P.L->rows_velocity(P.scheme, P.nearT.t, P.margs, P.phys, U, V, P.stream);
+      P.L->rows_velocity(P.scheme, P.nearT.t, ma, P.phys, U, V, P.stream);
       check_launch(P);
     }
   }
   if (ev) cudaEventRecord(ev[P.dim + 2], P.stream);
 }
 
-void velocity_and_jacobian(pda_problem &P, const double *U, double *V, double *J) {
+void velocity_and_jacobian(pda_problem &P, const double *U, double *V, double *J, double t) {
+  sync_recipes(P);
+  MeshArgs ma = P.margs;
+  ma.time = t;
   if (P.jStruct) {
     build_near_table(P, true);
     pattern_to_device(P);
@@ -575,10 +711,10 @@ void velocity_and_jacobian(pda_problem &P, const double *U, double *V, double *J
       T[a] = P.JT[a].p;
     }
     int nl = 0;
-    P.L->struct_vj(P.scheme, P.jbox, P.margs, P.phys, U, T, P.d_rowptr.p, V, J, P.stream, &nl);
+    P.L->struct_vj(P.scheme, P.jbox, ma, P.phys, U, T, P.d_rowptr.p, V, J, P.stream, &nl);
     check_launch(P, nl);
     if (P.nearT.t.nrows > 0) {
-      P.L->rows_vj_nearbd(P.scheme, P.nearT.t, P.margs, P.phys, U, P.d_rowptr.p, V, J, P.stream);
+      P.L->rows_vj_nearbd(P.scheme, P.nearT.t, ma, P.phys, U, P.d_rowptr.p, V, J, P.stream);
       check_launch(P);
     }
     return;
@@ -603,11 +739,11 @@ void velocity_and_jacobian(pda_problem &P, const double *U, double *V, double *J
     ns = P.side;
   }
   if (P.nearT.t.nrows > 0) {
-    P.L->rows_vj_nearbd(P.scheme, P.nearT.t, P.margs, P.phys, U, P.d_rowptr.p, V, J, ns);
+    P.L->rows_vj_nearbd(P.scheme, P.nearT.t, ma, P.phys, U, P.d_rowptr.p, V, J, ns);
     check_launch(P);
   }
   if (P.innerT.t.nrows > 0) {
-    P.L->rows_vj_inner(P.scheme, P.innerT.t, P.margs, P.phys, U, P.d_rowptr.p, V, J, P.stream);
+    P.L->rows_vj_inner(P.scheme, P.innerT.t, ma, P.phys, U, P.d_rowptr.p, V, J, P.stream);
     check_launch(P);
   }
   if (both) {
@@ -618,7 +754,8 @@ void velocity_and_jacobian(pda_problem &P, const double *U, double *V, double *J
 
 // ------------------------------------------------------------------ create
 void create_problem(pda_problem &P, const Mesh &m, int family, int probEn, int scheme, int icFlag,
-                    const char *const *names, const double *vals, int np, void *stream) {
+                    const char *const *names, const double *vals, int np, void *stream,
+                    bool crossShockFactory = false) {
   PDA_REQUIRE(family >= 0 && family <= 3, PDA_ERR_INVALID_ARGUMENT, "invalid problem family");
   PDA_REQUIRE(scheme >= 0 && scheme <= 2, PDA_ERR_INVALID_ARGUMENT, "invalid reconstruction scheme");
   PDA_REQUIRE(np >= 0 && (np == 0 || (names && vals)), PDA_ERR_INVALID_ARGUMENT, "invalid parameter arrays");
@@ -663,15 +800,12 @@ void create_problem(pda_problem &P, const Mesh &m, int family, int probEn, int s
     P.bc = BC_NONE;
   } else if (family == PDA_EULER2D) {
     // euler2d.hpp:88-173; impl/euler_2d_parametrization_helpers.hpp:75-93
-    PDA_REQUIRE((probEn >= 0 && probEn <= 5) || probEn == 8, PDA_ERR_UNSUPPORTED,
-                "Euler2d: supported problems are PeriodicSmooth, KelvinHelmholtz, SedovFull, SedovSymmetry, "
-                "Riemann, NormalShock, testingonlyneumann (DoubleMachReflection and CrossShock: time-dependent "
-                "and inflow ghost states are not implemented)");
+    PDA_REQUIRE(probEn >= 0 && probEn <= 8, PDA_ERR_INVALID_ARGUMENT, "invalid Euler2d problem");
     const bool validIc = (probEn == 4) ? (P.icFlag == 1 || P.icFlag == 2) : P.icFlag == 1;
     PDA_REQUIRE(validIc, PDA_ERR_INVALID_ARGUMENT, "Euler2d: invalid icFlag for the given problem enum");
     P.physParams = {1.4};
     P.icParams = {9, 0.1, 10., 1., 0.4, 1.5, 0.0, 0.0, 1.5, 0.029};
-    if (!params.empty())
+    if (!params.empty() && !crossShockFactory)
       PDA_REQUIRE(probEn == 4 || probEn == 5, PDA_ERR_INVALID_ARGUMENT,
                   "Euler2d: custom parametrization only valid for Euler2d::{Riemann, NormalShock}");
     for (auto &kv : params) {
@@ -688,12 +822,61 @@ void create_problem(pda_problem &P, const Mesh &m, int family, int probEn, int s
     P.bc = (probEn == 0 || probEn == 1) ? BC_NONE
            : probEn == 3                ? BC_SEDOVSYM
            : probEn == 5                ? BC_NORMALSHOCK
+           : probEn == 6                ? BC_DMR
+           : probEn == 7                ? BC_CROSSSHOCK
                                         : BC_MIRROR2D;
     if (probEn == 3) {
       P.margs.reflect[0] = 1;
       P.margs.reflect[1] = 2;
     }
-    if (probEn == 5) P.margs.reflect[1] = 2;
+    if (probEn == 5 || probEn == 6) P.margs.reflect[1] = 2;
+    const double gamma = P.physParams[0], one = 1.;
+    if (probEn == 6) {
+      // DoubleMachReflection2dGhostFiller::computeShockConditions and
+      // distanceFromShock (euler_2d_ghost_filler_double_mach_reflection.hpp:
+      // 272-305, :320-330): Mach 10 shock at pi/6, pre-shock gas at rest
+      const double angle = M_PI / 6.;
+      const double pre[4] = {gamma, 0., 0., 1.};
+      double post[4];
+      post_shock_at_rest(pre, -angle, 10., gamma, post);
+      const double gm1inv = one / (gamma - one);
+      const double *prim[2] = {pre, post};
+      double *cons[2] = {P.margs.pre, P.margs.post};
+      for (int k = 0; k < 2; ++k) {
+        cons[k][0] = prim[k][0];
+        cons[k][1] = prim[k][0] * prim[k][1];
+        cons[k][2] = prim[k][0] * prim[k][2];
+        cons[k][3] = energy2(gm1inv, prim[k], 4);
+      }
+      P.margs.shockX0 = kDmrWedge;
+      P.margs.shockSpeed = 10. / std::cos(angle);
+      P.margs.shockSlope = std::tan(angle);
+      GhostRecipe shock{};
+      shock.op[0] = 3;
+      P.recipes = {shock};
+      P.timeDependent = true;
+    }
+    if (probEn == 7) {
+      // CrossShock2dGhostFiller (euler_2d_ghost_filler_cross_shock.hpp:61-93)
+      const double rho = P.icParams[1], uIn = P.icParams[2], vBot = P.icParams[3];
+      const double prim[4] = {rho, uIn, 0., 1.};
+      const double gm1inv = one / (gamma - one);
+      GhostRecipe inflow{};
+      for (int d = 0; d < 4; ++d) inflow.op[d] = 2;
+      inflow.val[0] = prim[0];
+      inflow.val[1] = prim[0] * prim[1];
+      inflow.val[2] = prim[0] * prim[2];
+      inflow.val[3] = energy2(gm1inv, prim, 4);
+      GhostRecipe b0lo{}, b0hi{}, b1lo{}, b1hi{};
+      for (GhostRecipe *g : {&b0lo, &b0hi, &b1lo, &b1hi}) {
+        g->op[1] = g->op[2] = 2;
+        g->val[1] = rho * uIn;
+      }
+      b0hi.val[2] = b1hi.val[2] = rho * vBot;
+      b1lo.op[0] = b1hi.op[0] = 2;
+      b1lo.val[0] = b1hi.val[0] = rho;
+      P.recipes = {inflow, b0lo, b0hi, b1lo, b1hi};
+    }
   } else {
     // swe2d.hpp:143-195; impl/swe_2d_parametrization_helpers.hpp:59-95
     PDA_REQUIRE(probEn == 0, PDA_ERR_UNSUPPORTED, "Swe2d: only SlipWall is supported");
@@ -824,20 +1007,20 @@ void stepper_buffers(pda_problem &P, int nr) {
 void ssprk3_step(pda_problem &P, double *U, double t, double dt) {
   const long n = (long)P.dofsStencil;
   double *r0 = P.r[0].p, *aux = P.aux.p;
-  velocity(P, U, r0);
+  const double tHalf = t + dt / 2., tNext = t + dt;
+  velocity(P, U, r0, t);
   launch_axpby_stage(0, aux, U, r0, nullptr, 0., dt, 0., 0., nullptr, nullptr, n, P.stream);
   check_launch(P);
-  velocity(P, aux, r0);
+  velocity(P, aux, r0, tNext);
   const double fourInv = 1. / 4., threeOvFour = 3. / 4.;
   launch_axpby_stage(1, aux, U, r0, nullptr, fourInv, threeOvFour, fourInv * dt, 0., nullptr, nullptr, n,
                      P.stream);
   check_launch(P);
-  velocity(P, aux, r0);
+  velocity(P, aux, r0, tHalf);
   const double oneOvThree = 1. / 3., twoOvThree = 2. / 3.;
   launch_axpby_stage(1, U, aux, r0, nullptr, oneOvThree, twoOvThree, twoOvThree * dt, 0., nullptr, nullptr,
                      n, P.stream);
   check_launch(P);
-  (void)t;
 }
 
 // One step of RK4 (ode_explicit_stepper_without_mass_matrix.hpp:284-336).
@@ -845,19 +1028,19 @@ void rk4_step(pda_problem &P, double *U, double t, double dt) {
   const long n = (long)P.dofsStencil;
   const double dt2 = dt / 2., dt6 = dt / 6., dt3 = dt / 3.;
   double *aux = P.aux.p;
-  velocity(P, U, P.r[0].p);
+  const double tHalf = t + dt2, tNext = t + dt;
+  velocity(P, U, P.r[0].p, t);
   launch_axpby_stage(0, aux, U, P.r[0].p, nullptr, 0., dt2, 0., 0., nullptr, nullptr, n, P.stream);
   check_launch(P);
-  velocity(P, aux, P.r[1].p);
+  velocity(P, aux, P.r[1].p, tHalf);
   launch_axpby_stage(0, aux, U, P.r[1].p, nullptr, 0., dt2, 0., 0., nullptr, nullptr, n, P.stream);
   check_launch(P);
-  velocity(P, aux, P.r[2].p);
+  velocity(P, aux, P.r[2].p, tHalf);
   launch_axpby_stage(0, aux, U, P.r[2].p, nullptr, 0., dt, 0., 0., nullptr, nullptr, n, P.stream);
   check_launch(P);
-  velocity(P, aux, P.r[3].p);
+  velocity(P, aux, P.r[3].p, tNext);
   launch_axpby_stage(2, U, P.r[0].p, P.r[1].p, P.r[2].p, 0., dt3, 0., dt6, P.r[3].p, nullptr, n, P.stream);
   check_launch(P);
-  (void)t;
 }
 
 void advance(pda_problem &P, int kind, double *U, double t0, double dt, int64_t nsteps, bool useGraph) {
@@ -869,7 +1052,9 @@ void advance(pda_problem &P, int kind, double *U, double t0, double dt, int64_t 
     if (kind == 0) ssprk3_step(P, U, t, dt);
     else rk4_step(P, U, t, dt);
   };
-  if (!useGraph || P.stream == nullptr) {
+  // time-dependent ghost states take the stage times as kernel arguments:
+  // those problems step eagerly
+  if (!useGraph || P.stream == nullptr || P.timeDependent) {
     double t = t0;
     for (int64_t s = 0; s < nsteps; ++s) {
       step(t);
@@ -877,15 +1062,15 @@ void advance(pda_problem &P, int kind, double *U, double t0, double dt, int64_t 
     }
     return;
   }
-  // Capture one step and replay it: the kernels do not depend on t for the
-  // supported boundary conditions.  The graph bakes in U and dt.
+  // Capture one step and replay it: the kernels do not depend on t for these
+  // boundary conditions.  The graph bakes in U and dt.
   if (P.stepGraph && (P.stepGraphKind != kind || P.stepGraphDt != dt || P.stepGraphU != U)) {
     cudaGraphExecDestroy(P.stepGraph);
     P.stepGraph = nullptr;
   }
   if (!P.stepGraph) {
     // lazily built tables and buffers must exist before capture
-    velocity(P, U, P.r[0].p);
+    velocity(P, U, P.r[0].p, t0);
     PDA_CUDA(cudaStreamSynchronize(P.stream));
     cudaGraph_t g;
     PDA_CUDA(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
@@ -1017,6 +1202,18 @@ pda_status pda_problem_create_swe_slip_wall(const pda_mesh *mesh, int scheme, do
   return pda_problem_create(mesh, PDA_SWE2D, PDA_SWE2D_SLIP_WALL, scheme, 1, names, vals, 3, stream, out);
 }
 
+pda_status pda_problem_create_cross_shock(const pda_mesh *mesh, int scheme, double density, double inlet_x_vel,
+                                          double bottom_y_vel, void *stream, pda_problem **out) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(mesh && out, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  const char *names[3] = {"crossShockDensity", "crossShockInletXVel", "crossShockBottomYVel"};
+  const double vals[3] = {density, inlet_x_vel, bottom_y_vel};
+  std::unique_ptr<pda_problem> p(new pda_problem);
+  pda::create_problem(*p, mesh->m, PDA_EULER2D, 7, scheme, 1, names, vals, 3, stream, true);
+  *out = p.release();
+  PDA_API_END
+}
+
 void pda_problem_free(pda_problem *p) { delete p; }
 
 pda_status pda_problem_sizes(const pda_problem *p, int *ndpc, int64_t *ds, int64_t *dst) {
@@ -1070,22 +1267,23 @@ pda_status pda_initial_condition(pda_problem *p, double *dU) {
 pda_status pda_velocity(pda_problem *p, const double *dU, double t, double *dV) {
   PDA_API_BEGIN
   PDA_REQUIRE(p && dU && dV, PDA_ERR_INVALID_ARGUMENT, "null argument");
-  (void)t;
-  pda::velocity(*p, dU, dV);
+  pda::velocity(*p, dU, dV, t);
   PDA_API_END
 }
 
 pda_status pda_velocity_noalloc(pda_problem *p, const double *dU, double t, double *dV) {
   PDA_API_BEGIN
   PDA_REQUIRE(p && dU && dV, PDA_ERR_INVALID_ARGUMENT, "null argument");
-  (void)t;
   pda_problem &P = *p;
+  pda::MeshArgs ma = P.margs;
+  ma.time = t;
   PDA_REQUIRE(P.useStruct, PDA_ERR_UNSUPPORTED,
               "pda_velocity_noalloc: only full meshes evaluated by the structured face pass are supported "
               "(sample meshes have no face scratch: use pda_velocity)");
   // the near-boundary row table is uploaded by the first pda_velocity call;
   // uploading it here would allocate
-  const bool nearResident = P.structAll || P.nearT.hostRows() == 0 || !P.nearT.dirty;
+  const bool nearResident =
+      (P.structAll || P.nearT.hostRows() == 0 || !P.nearT.dirty) && (P.recipes.empty() || P.d_recipes.p);
   PDA_REQUIRE(nearResident, PDA_ERR_UNSUPPORTED,
               "pda_velocity_noalloc: the near-boundary row table of this problem is not on the device yet; "
               "one pda_velocity call on the problem uploads it");
@@ -1108,10 +1306,10 @@ pda_status pda_velocity_noalloc(pda_problem *p, const double *dU, double t, doub
   double *Fb[3] = {nullptr, nullptr, nullptr};
   for (int a = 0; a < P.dim; ++a) Fb[a] = scratch + off[a];
   int nl = 0;
-  P.L->struct_velocity(P.scheme, P.box, P.margs, P.phys, dU, Fb, dV, P.stream, &nl, nullptr);
+  P.L->struct_velocity(P.scheme, P.box, ma, P.phys, dU, Fb, dV, P.stream, &nl, nullptr);
   pda::check_launch(P, nl);
   if (!P.structAll && P.nearT.t.nrows > 0) {
-    P.L->rows_velocity(P.scheme, P.nearT.t, P.margs, P.phys, dU, dV, P.stream);
+    P.L->rows_velocity(P.scheme, P.nearT.t, ma, P.phys, dU, dV, P.stream);
     pda::check_launch(P);
   }
   PDA_API_END
@@ -1120,11 +1318,10 @@ pda_status pda_velocity_noalloc(pda_problem *p, const double *dU, double t, doub
 pda_status pda_velocity_host(pda_problem *p, const double *hU, double t, double *hV) {
   PDA_API_BEGIN
   PDA_REQUIRE(p && hU && hV, PDA_ERR_INVALID_ARGUMENT, "null argument");
-  (void)t;
   p->d_U.alloc(p->dofsStencil);
   p->d_V.alloc(p->dofsSample);
   PDA_CUDA(cudaMemcpyAsync(p->d_U.p, hU, p->dofsStencil * sizeof(double), cudaMemcpyHostToDevice, p->stream));
-  pda::velocity(*p, p->d_U.p, p->d_V.p);
+  pda::velocity(*p, p->d_U.p, p->d_V.p, t);
   PDA_CUDA(cudaMemcpyAsync(hV, p->d_V.p, p->dofsSample * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
   PDA_CUDA(cudaStreamSynchronize(p->stream));
   PDA_API_END
@@ -1164,8 +1361,7 @@ pda_status pda_jacobian_pattern_host(pda_problem *p, int32_t *hrp, int32_t *hci)
 pda_status pda_velocity_and_jacobian(pda_problem *p, const double *dU, double t, double *dV, double *dJ) {
   PDA_API_BEGIN
   PDA_REQUIRE(p && dU && dV && dJ, PDA_ERR_INVALID_ARGUMENT, "null argument");
-  (void)t;
-  pda::velocity_and_jacobian(*p, dU, dV, dJ);
+  pda::velocity_and_jacobian(*p, dU, dV, dJ, t);
   PDA_API_END
 }
 
@@ -1173,13 +1369,12 @@ pda_status pda_velocity_and_jacobian_host(pda_problem *p, const double *hU, doub
                                           double *hJ) {
   PDA_API_BEGIN
   PDA_REQUIRE(p && hU && hV && hJ, PDA_ERR_INVALID_ARGUMENT, "null argument");
-  (void)t;
   pda::build_pattern(*p);
   p->d_U.alloc(p->dofsStencil);
   p->d_V.alloc(p->dofsSample);
   p->d_J.alloc(p->colidx.size());
   PDA_CUDA(cudaMemcpyAsync(p->d_U.p, hU, p->dofsStencil * sizeof(double), cudaMemcpyHostToDevice, p->stream));
-  pda::velocity_and_jacobian(*p, p->d_U.p, p->d_V.p, p->d_J.p);
+  pda::velocity_and_jacobian(*p, p->d_U.p, p->d_V.p, p->d_J.p, t);
   PDA_CUDA(cudaMemcpyAsync(hV, p->d_V.p, p->dofsSample * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
   PDA_CUDA(cudaMemcpyAsync(hJ, p->d_J.p, p->colidx.size() * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
   PDA_CUDA(cudaStreamSynchronize(p->stream));
@@ -1189,9 +1384,8 @@ pda_status pda_velocity_and_jacobian_host(pda_problem *p, const double *hU, doub
 pda_status pda_jacobian(pda_problem *p, const double *dU, double t, double *dJ) {
   PDA_API_BEGIN
   PDA_REQUIRE(p && dU && dJ, PDA_ERR_INVALID_ARGUMENT, "null argument");
-  (void)t;
   p->d_Vscratch.alloc(p->dofsSample);
-  pda::velocity_and_jacobian(*p, dU, p->d_Vscratch.p, dJ);
+  pda::velocity_and_jacobian(*p, dU, p->d_Vscratch.p, dJ, t);
   PDA_API_END
 }
 
@@ -1199,11 +1393,10 @@ pda_status pda_apply_jacobian(pda_problem *p, const double *dU, double t, const 
                               double *dR) {
   PDA_API_BEGIN
   PDA_REQUIRE(p && dU && dB && dR && ncols >= 1, PDA_ERR_INVALID_ARGUMENT, "invalid argument");
-  (void)t;
   pda::pattern_to_device(*p);
   p->d_Vscratch.alloc(p->dofsSample);
   p->d_Jscratch.alloc(p->colidx.size());
-  pda::velocity_and_jacobian(*p, dU, p->d_Vscratch.p, p->d_Jscratch.p);
+  pda::velocity_and_jacobian(*p, dU, p->d_Vscratch.p, p->d_Jscratch.p, t);
   pda::launch_csr_spmm(p->dofsSample, p->d_rowptr.p, p->d_colidx.p, p->d_Jscratch.p, dB, p->dofsStencil, ncols,
                        dR, p->dofsSample, p->stream);
   pda::check_launch(*p);
@@ -1234,7 +1427,7 @@ pda_status pda_profile_velocity(pda_problem *p, const double *dU, double *dV, in
   for (auto &e : ev) PDA_CUDA(cudaEventCreate(&e));
   std::vector<double> acc(ne - 1, 0.0);
   for (int r = 0; r < reps; ++r) {
-    pda::velocity(*p, dU, dV, p->useStruct ? ev.data() : nullptr);
+    pda::velocity(*p, dU, dV, 0.0, p->useStruct ? ev.data() : nullptr);
     if (!p->useStruct) break;
     PDA_CUDA(cudaEventSynchronize(ev[ne - 1]));
     for (int k = 0; k + 1 < ne; ++k) {

@@ -57,9 +57,10 @@ struct Table {
   std::vector<int> rows, cell, src, jpos, src1, jpos1;
   std::vector<uint8_t> flip, flip1;
   std::vector<double> jfac;
+  std::vector<double> gsx, gsy, gsx1, gsy1;  // moving-shock ghost positions (empty unless used)
   DevBuf<int> d_rows, d_cell, d_src, d_jpos, d_src1, d_jpos1;
   DevBuf<uint8_t> d_flip, d_flip1;
-  DevBuf<double> d_jfac;
+  DevBuf<double> d_jfac, d_gsx, d_gsy, d_gsx1, d_gsy1;
   RowTable t{};
   bool dirty = true;
   int hostRows() const { return (int)rows.size(); }
@@ -79,6 +80,10 @@ struct Table {
     d_flip1.upload(flip1);
     d_jpos1.upload(jpos1);
     d_jfac.upload(jfac);
+    d_gsx.upload(gsx);
+    d_gsy.upload(gsy);
+    d_gsx1.upload(gsx1);
+    d_gsy1.upload(gsy1);
     t.nrows = (int)rows.size();
     t.rows = d_rows.p;
     t.cell = d_cell.p;
@@ -89,6 +94,10 @@ struct Table {
     t.flip1 = flip1.empty() ? nullptr : d_flip1.p;
     t.jpos1 = jpos1.empty() ? nullptr : d_jpos1.p;
     t.jfac = jfac.empty() ? nullptr : d_jfac.p;
+    t.gsx = gsx.empty() ? nullptr : d_gsx.p;
+    t.gsy = gsy.empty() ? nullptr : d_gsy.p;
+    t.gsx1 = gsx1.empty() ? nullptr : d_gsx1.p;
+    t.gsy1 = gsy1.empty() ? nullptr : d_gsy1.p;
   }
 };
 
@@ -97,8 +106,19 @@ struct Table {
 // (layer L >= 1 copies the opposite-side neighbour L-1; reflective on the
 // left and bottom sides, Neumann on the right and top), BC_NORMALSHOCK =
 // NormalShock2dGhostFiller (same layer rule; reflective top and bottom,
-// Neumann left and right)
-enum BcKind { BC_NONE = 0, BC_MIRROR2D = 1, BC_NEUMANN1D = 2, BC_SEDOVSYM = 3, BC_NORMALSHOCK = 4 };
+// Neumann left and right), BC_DMR = DoubleMachReflection2dGhostFiller (same
+// layer rule; moving oblique shock on the top, wall behind the wedge on the
+// bottom), BC_CROSSSHOCK = CrossShock2dGhostFiller (same layer rule; inflow
+// state on the left, prescribed momentum on the bottom)
+enum BcKind {
+  BC_NONE = 0,
+  BC_MIRROR2D = 1,
+  BC_NEUMANN1D = 2,
+  BC_SEDOVSYM = 3,
+  BC_NORMALSHOCK = 4,
+  BC_DMR = 5,
+  BC_CROSSSHOCK = 6
+};
 
 }  // namespace pda
 
@@ -119,6 +139,9 @@ struct pda_problem {
   int ndpc = 0, dim = 0, h = 0;
   int64_t dofsSample = 0, dofsStencil = 0;
   int bc = pda::BC_NONE;
+  bool timeDependent = false;  // ghost states depend on the evaluation time
+  std::vector<pda::GhostRecipe> recipes;  // ghost recipes with ids >= 2
+  pda::DevBuf<pda::GhostRecipe> d_recipes;
   const pda::Launchers *L = nullptr;
   // velocity
   bool useStruct = false;

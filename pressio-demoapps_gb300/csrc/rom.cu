@@ -516,6 +516,9 @@ void common_setup(pda_lspg &L, pda_problem *P, const int64_t *s2st, int k) {
   PDA_REQUIRE(P && s2st, PDA_ERR_INVALID_ARGUMENT, "null argument");
   PDA_REQUIRE(k_supported(k), PDA_ERR_UNSUPPORTED,
               "latent dimension must be one of 2, 4, 6, 8, 10, 12, 16, 20, 24, 32");
+  PDA_REQUIRE(!P->timeDependent, PDA_ERR_UNSUPPORTED,
+              "LSPG steps evaluate the residual at a fixed time: problems with time-dependent ghost states "
+              "(double Mach reflection) are not supported");
   L.P = P;
   L.k = k;
   L.ndpc = P->ndpc;

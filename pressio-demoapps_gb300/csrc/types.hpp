@@ -21,19 +21,37 @@ struct RowTable {
   const int *rows;         // graph row (sample-mesh index) of each entry
   const int *cell;         // stencil-mesh cell id of the row (graph col 0)
   const int *src;          // [nrows][dim][2H+1] stencil source cell per position
-  const uint8_t *flip;     // [nrows][dim][2H+1] 1 = mirrored ghost: negate reflect dof
+  const uint8_t *flip;     // [nrows][dim][2H+1] ghost recipe: 0 copy, 1 negate the reflect dof,
+                           // r >= 2 the mesh args' recipe r - 2
+  const double *gsx;       // [nrows][dim][2H+1] ghost position for the moving-shock recipe (or null)
+  const double *gsy;
   // Jacobian support (may be null for velocity-only tables)
   const int *jpos;         // [nrows][dim][2H+1] block offset in the CSR row, -1 = absent
   const int *src1;         // [nrows][dim][3] first-order stencil (near-boundary rows)
   const uint8_t *flip1;    // [nrows][dim][3]
+  const double *gsx1;      // [nrows][dim][3] (or null)
+  const double *gsy1;
   const int *jpos1;        // [nrows][dim][3] block offset for existing neighbours, -1 = none
   const double *jfac;      // [nrows][dim][ndpc] ghost-to-cell derivative factors
+};
+
+// Ghost state from the source cell, dof by dof: op 0 copy, 1 negate,
+// 2 the constant val; op[0] == 3 marks the moving oblique shock of the double
+// Mach reflection (post-shock state behind it, pre-shock ahead).
+struct GhostRecipe {
+  uint8_t op[5];
+  double val[5];
 };
 
 struct MeshArgs {
   int dim;
   double hinv[3];
   int reflect[3];  // dof negated in a mirrored ghost for a face normal to each axis (-1: none)
+  const GhostRecipe *recipes;  // device table for recipe ids >= 2 (or null)
+  double time;                 // evaluation time (moving-shock recipe)
+  // moving shock: distance = ((x - shockX0) - shockSpeed t) - shockSlope y
+  double shockX0, shockSpeed, shockSlope;
+  double pre[5], post[5];
 };
 
 // Structured box of a natural-order full mesh: cells [lo, hi) per axis,

@@ -61,6 +61,14 @@ FULL_MESHES = {
     "m2d_s3_16_sedsym": "-n 16 16 --bounds 0.0 1.2 0.0 1.2 -s 3",
     "m2d_s7_24x12_nshock": "-n 24 12 --bounds 0.0 2.0 0.0 1.0 -s 7",
     "m2d_s5_24x12_nshock": "-n 24 12 --bounds 0.0 2.0 0.0 1.0 -s 5",
+    # cross-shock and double-Mach-reflection meshes of the reference's explicit tests
+    # (tests_cpp/eigen_2d_euler_{cross_shock,double_mach_reflection}_explicit/test.cmake)
+    "m2d_s3_40x20_cross": "-n 40 20 --bounds 0.0 2.0 0.0 1.0 -s 3",
+    "m2d_s5_40x20_cross": "-n 40 20 --bounds 0.0 2.0 0.0 1.0 -s 5",
+    "m2d_s7_40x20_cross": "-n 40 20 --bounds 0.0 2.0 0.0 1.0 -s 7",
+    "m2d_s3_60x15_dmr": "-n 60 15 --bounds 0.0 4.0 0.0 1.0 -s 3",
+    "m2d_s5_60x15_dmr": "-n 60 15 --bounds 0.0 4.0 0.0 1.0 -s 5",
+    "m2d_s7_60x15_dmr": "-n 60 15 --bounds 0.0 4.0 0.0 1.0 -s 7",
     "m3d_s3_8_per": "-n 8 8 8 --bounds -1.0 1.0 -1.0 1.0 -1.0 1.0 -s 3 --periodic x y z",
     "m3d_s5_8_per": "-n 8 8 8 --bounds -1.0 1.0 -1.0 1.0 -1.0 1.0 -s 5 --periodic x y z",
     "m3d_s5_6x5x7_per": "-n 6 5 7 --bounds -1.0 1.0 -1.0 1.0 -1.0 1.0 -s 5 --periodic x y z",
@@ -74,6 +82,8 @@ SAMPLE_MESHES = {
     "s2d_s7_20": ("m2d_s7_20", "tests_cpp/eigen_2d_swe_jacobian_fd_with_sample_mesh/sample_mesh_gids.dat"),
     "s2d_s7_25_rand": ("m2d_s7_25", "random:40"),
     "s2d_s7_16_sedsym_rand": ("m2d_s7_16_sedsym", "random:40"),
+    "s2d_s7_60x15_dmr_rand": ("m2d_s7_60x15_dmr", "random:60"),
+    "s2d_s5_40x20_cross_rand": ("m2d_s5_40x20_cross", "random:50"),
 }
 
 # case -> (mesh, family, problem, scheme, icflag, params)
@@ -120,7 +130,29 @@ CASE_LIST = {
     "sample_sedovsym_w5": ("s2d_s7_16_sedsym_rand", E2, 3, 2, 1, {}),
     "normalshock_w5": ("m2d_s7_24x12_nshock", E2, 5, 2, 1, {}),
     "normalshock_w3_mach": ("m2d_s5_24x12_nshock", E2, 5, 1, 1, {"mach": 4.0}),
+    "dmr_fo": ("m2d_s3_60x15_dmr", E2, 6, 0, 1, {}),
+    "dmr_w3": ("m2d_s5_60x15_dmr", E2, 6, 1, 1, {}),
+    "dmr_w5": ("m2d_s7_60x15_dmr", E2, 6, 2, 1, {}),
+    "dmr_w5_t0": ("m2d_s7_60x15_dmr", E2, 6, 2, 1, {}),
+    "sample_dmr_w5": ("s2d_s7_60x15_dmr_rand", E2, 6, 2, 1, {}),
+    "cross_fo": ("m2d_s3_40x20_cross", E2, 7, 0, 1, {}),
+    "cross_w3": ("m2d_s5_40x20_cross", E2, 7, 1, 1, {}),
+    "cross_w5": ("m2d_s7_40x20_cross", E2, 7, 2, 1, {}),
+    "cross_params_w5": ("m2d_s7_40x20_cross", E2, 7, 2, 1,
+                        {"crossShockDensity": 0.2, "crossShockInletXVel": 5.0, "crossShockBottomYVel": 2.0}),
+    "sample_cross_w3": ("s2d_s5_40x20_cross_rand", E2, 7, 1, 1, {}),
 }
+
+# evaluation time of a case (time-dependent ghost states: the double Mach
+# reflection's top boundary follows the moving shock)
+CASE_TIME = {"dmr_fo": 0.05, "dmr_w3": 0.08, "dmr_w5": 0.1, "sample_dmr_w5": 0.07}
+
+# Jacobian tolerance (relative to the row's largest entry) where 1e-12 is
+# below the problem's conditioning: across the Mach 10 shock of the double
+# Mach reflection the WENO5 weight derivatives amplify a last-bit difference
+# of x^3 (glibc pow versus a correctly rounded cube) to ~1e-11 of the row
+# scale; the reference evaluated both ways differs by that much
+CASE_JTOL = {"dmr_w5": 3e-11, "dmr_w5_t0": 3e-11}
 
 
 def run(cmd):
@@ -201,20 +233,22 @@ def make_cases(ref: Ref):
         # Sedov states have an energy of ~6e-5 outside the blast: relative
         # noise keeps the pressure positive
         U1 = U0 * (1.0 + noise) if "sedov" in case else U0 + noise
+        t = CASE_TIME.get(case, 0.0)
         V0 = np.empty(ds)
         V1 = np.empty(ds)
-        ref.L.ref_velocity(h, vp(U0), 0.0, vp(V0))
-        ref.L.ref_velocity(h, vp(U1), 0.0, vp(V1))
+        ref.L.ref_velocity(h, vp(U0), t, vp(V0))
+        ref.L.ref_velocity(h, vp(U1), t, vp(V1))
         Vj = np.empty(ds)
         rp = np.empty(ds + 1, dtype=np.int32)
         ci = np.empty(nnz, dtype=np.int32)
         jv = np.empty(nnz)
-        ref.L.ref_velocity_and_jacobian(h, vp(U1), 0.0, vp(Vj), vp(rp), vp(ci), vp(jv))
+        ref.L.ref_velocity_and_jacobian(h, vp(U1), t, vp(Vj), vp(rp), vp(ci), vp(jv))
         ref.L.ref_destroy(h)
         np.savez_compressed(os.path.join(CASES, case + ".npz"), U0=U0, U1=U1, V0=V0, V1=V1, Vj=Vj,
                             rowptr=rp, colidx=ci, jvals=jv)
         manifest[case] = dict(mesh=mesh, family=fam, problem=prob, scheme=scheme, icflag=ic,
-                              params=params, ndpc=ndpc, dofs_sample=ds, dofs_stencil=dst, nnz=nnz)
+                              params=params, ndpc=ndpc, dofs_sample=ds, dofs_stencil=dst, nnz=nnz, t=t,
+                              jtol=CASE_JTOL.get(case, 1e-12))
         print(f"case {case}: dofs {ds}/{dst} nnz {nnz}")
     return manifest
 
@@ -291,13 +325,75 @@ def make_gold(ref: Ref):
         traj[f"swe_{tag}"] = dict(mesh=mesh, family=SW, problem=0, scheme=scheme, icflag=1, stepper="rk4",
                                   dt=0.01, steps=saved, rtol=1e-10, atol=1e-12)
         np.save(os.path.join(GOLD, f"swe_{tag}.npy"), h_g)
+    # Cross shock (defaults 0.1, 10, 1) and double Mach reflection: SSPRK3
+    # dt=1e-3, 100 and 150 steps, observer every 50 steps, density of the last
+    # snapshot (tests_cpp/eigen_2d_euler_cross_shock_explicit/main.cc,
+    # tests_cpp/eigen_2d_euler_double_mach_reflection_explicit/main.cc, compare.py)
+    for base, prob, steps, tags in (("cross", 7, 100, ((0, "firstorder", 3), (1, "weno3", 5), (2, "weno5", 7))),
+                                    ("dmr", 6, 150, ((0, "firstorder", 3), (1, "weno3", 5)))):
+        d = "eigen_2d_euler_cross_shock_explicit" if base == "cross" else "eigen_2d_euler_double_mach_reflection_explicit"
+        for scheme, tag, st in tags:
+            mesh = f"m2d_s{st}_40x20_cross" if base == "cross" else f"m2d_s{st}_60x15_dmr"
+            rho_g = np.loadtxt(os.path.join(REF, "tests_cpp", d, tag, "rho_gold.txt"))
+            h, s = ref.create(mesh, E2, prob, scheme, 1, {})
+            U = np.empty(s[2])
+            ref.L.ref_ic(h, vp(U))
+            ref.L.ref_ssprk3(h, vp(U), 0.0, 1e-3, steps)
+            ref.L.ref_destroy(h)
+            assert np.allclose(U.reshape(-1, 4)[:, 0], rho_g, rtol=1e-10, atol=1e-12), (base, tag)
+            traj[f"{base}_{tag}"] = dict(mesh=mesh, family=E2, problem=prob, scheme=scheme, icflag=1,
+                                         stepper="ssprk3", dt=1e-3, steps=steps, rtol=1e-10, atol=1e-12)
+            np.save(os.path.join(GOLD, f"{base}_{tag}.npy"), rho_g)
     json.dump(traj, open(os.path.join(GOLD, "trajectories.json"), "w"), indent=1)
+
+    # Golds of the reference's Python tests, advanced by the Python driver's
+    # own SSP-RK3 update (pressiodemoapps/__init__.py:155-185) on meshes of
+    # create_full_mesh.py: cross shock 80x40 first order, dt 1e-3, 1000 steps
+    # (tests_py/2d_euler_cross_shock); double Mach reflection 200x50 first
+    # order and WENO3, dt 5e-4, 500 steps (tests_py/2d_double_mach_reflection).
+    # The meshes are regenerated by the tests; only the density golds are kept.
+    pyt = {}
+    for name, sub, prob, scheme, st, n, bounds, dt, steps in (
+            ("cross_py_firstorder", "2d_euler_cross_shock", 7, 0, 3, (80, 40), (0.0, 2.0, 0.0, 1.0), 1e-3, 1000),
+            ("dmr_py_firstorder", "2d_double_mach_reflection/firstorder", 6, 0, 3, (200, 50), (0.0, 4.0, 0.0, 1.0),
+             5e-4, 500),
+            ("dmr_py_weno3", "2d_double_mach_reflection/weno3", 6, 1, 5, (200, 50), (0.0, 4.0, 0.0, 1.0), 5e-4, 500)):
+        src = os.path.join(REF, "tests_py", sub)
+        rho_g = np.loadtxt(os.path.join(src, "rho_gold.txt"))
+        L = ref.L
+        names = (C.c_char_p * 1)()
+        vals = (C.c_double * 1)()
+        h = L.ref_create(src.encode(), E2, prob, scheme, 1, 0, names, vals)
+        sz = (C.c_long * 4)()
+        L.ref_sizes(h, sz)
+        U = np.empty(sz[2])
+        L.ref_ic(h, vp(U))
+        v = np.empty(sz[1])
+        t = 0.0
+        for _ in range(steps):
+            L.ref_velocity(h, vp(U), t, vp(v))
+            u1 = U + dt * v
+            L.ref_velocity(h, vp(u1), t + dt, vp(v))
+            u2 = 3. / 4. * U + 1. / 4. * u1 + 1. / 4. * dt * v
+            L.ref_velocity(h, vp(u2), t + dt * 0.5, vp(v))
+            U = 1. / 3. * (U + 2. * u2 + 2. * dt * v)
+            t += dt
+        L.ref_destroy(h)
+        assert np.allclose(U.reshape(-1, 4)[:, 0], rho_g, rtol=1e-10, atol=1e-12), name
+        pyt[name] = dict(n=list(n), bounds=list(bounds), stencil=st, family=E2, problem=prob, scheme=scheme,
+                         icflag=1, stepper="ssprk3_py", dt=dt, steps=steps, rtol=1e-10, atol=1e-12)
+        np.save(os.path.join(GOLD, name + ".npy"), rho_g)
+    json.dump(pyt, open(os.path.join(GOLD, "py_trajectories.json"), "w"), indent=1)
 
     # Crank-Nicolson + Newton + BiCGSTAB gold of the reference's implicit
     # Riemann test (first order, 20x20, dt 0.02, 30 steps, Newton tolerance 1e-5)
     src = os.path.join(REF, "tests_cpp/eigen_2d_euler_riemann_implicit/firstorder")
     np.save(os.path.join(GOLD, "riemann_implicit_fo_rho.npy"), np.loadtxt(os.path.join(src, "rho_gold.txt")))
     np.save(os.path.join(GOLD, "riemann_implicit_fo_p.npy"), np.loadtxt(os.path.join(src, "p_gold.txt")))
+    # ... and of the implicit double Mach reflection test (first order, 60x15,
+    # Crank-Nicolson dt 0.01, 100 steps, Newton tolerance 1e-5)
+    src = os.path.join(REF, "tests_cpp/eigen_2d_euler_double_mach_reflection_implicit/firstorder")
+    np.save(os.path.join(GOLD, "dmr_implicit_fo_rho.npy"), np.loadtxt(os.path.join(src, "rho_gold.txt")))
 
     # mesh-generator golds (tests_mesh/mesh_generation_full_{1,2,3}d/*/*_gold.dat),
     # with the generator arguments their test.cmake files pass

@@ -15,7 +15,7 @@ import re
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, REPO, golden_case, mesh_dir
+from conftest import GOLDEN, REPO, create_case_problem, golden_case, mesh_dir
 
 MANIFEST = json.load(open(os.path.join(GOLDEN, "manifest.json")))
 
@@ -124,9 +124,7 @@ def test_host_initial_condition_and_pattern(pda, case):
     m = MANIFEST[case]
     g = golden_case(case)
     mesh = pda.load_cellcentered_uniform_mesh(mesh_dir(m["mesh"]))
-    enum = [pda.Euler1d, pda.Euler2d, pda.Euler3d, pda.Swe2d][m["family"]](m["problem"])
-    p = pda.create_problem(mesh, enum, pda.InviscidFluxReconstruction(m["scheme"]), m["icflag"],
-                           m.get("params") or None, stream=0)
+    p = create_case_problem(pda, m, mesh, stream=0)
     assert p.numDofPerCell() == m["ndpc"]
     assert np.array_equal(p.initialConditionHost(), g["U0"])
     rp, ci = p.jacobianPatternHost()

@@ -18,7 +18,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, golden_case, j_close, mesh_dir, v_close
+from conftest import GOLDEN, create_case_problem, golden_case, j_close, mesh_dir, v_close
 
 pytestmark = pytest.mark.gpu
 
@@ -45,9 +45,7 @@ def problem_enum(pda, family, problem):
 
 def make_problem(pda, m, mesh=None):
     mesh = mesh or pda.load_cellcentered_uniform_mesh(mesh_dir(m["mesh"]))
-    p = pda.create_problem(mesh, problem_enum(pda, m["family"], m["problem"]),
-                           pda.InviscidFluxReconstruction(m["scheme"]), m["icflag"], m.get("params") or None)
-    return mesh, p
+    return mesh, create_case_problem(pda, m, mesh)
 
 
 @pytest.mark.parametrize("case", sorted(MANIFEST))
@@ -61,17 +59,18 @@ def test_velocity_matches_reference(pda, case):
     # initial condition (host formulas, reference order): bit-exact
     u0 = p.initialCondition()
     assert np.array_equal(u0.cpu().numpy(), g["U0"])
+    t = m.get("t", 0.0)
     for uk, vk in (("U0", "V0"), ("U1", "V1")):
         U = torch.from_numpy(g[uk]).cuda()
         V = p.createVelocity()
-        p.velocity(U, 0.0, V)
+        p.velocity(U, t, V)
         v = V.cpu().numpy()
         ok, worst = v_close(v, g[vk], m["ndpc"])
         assert ok, f"{case} {vk}: worst relative error {worst:.3e}"
         if m["family"] != 3:
             # Euler velocities follow the reference's operation order exactly
             # (the shallow-water flux takes sqrt for glibc's pow(h, 0.5))
-            assert np.array_equal(v, g[vk]), f"{case} {vk}: not bit-identical"
+            assert np.array_equal(v, g[vk], equal_nan=True), f"{case} {vk}: not bit-identical"
 
 
 
@@ -86,14 +85,15 @@ def test_jacobian_matches_reference(pda, case):
     assert np.array_equal(J.colidx.cpu().numpy(), g["colidx"])
     U = torch.from_numpy(g["U1"]).cuda()
     V = p.createVelocity()
-    p.rightHandSideAndJacobian(U, 0.0, V, J)
+    t = m.get("t", 0.0)
+    p.rightHandSideAndJacobian(U, t, V, J)
     ok, worst = v_close(V.cpu().numpy(), g["Vj"], m["ndpc"])
     assert ok, f"{case} V (V+J path): worst {worst:.3e}"
     # J within 1e-12 of the row scale: the WENO weight derivatives cancel
     # terms far larger than the entries, and the reference's own x^3 (glibc
     # pow, not always correctly rounded) moves entries by up to ~1e-13 of it
     jv = J.values.cpu().numpy()
-    ok, worst = j_close(jv, g["jvals"], g["rowptr"], floor_frac=1.0)
+    ok, worst = j_close(jv, g["jvals"], g["rowptr"], rtol=m.get("jtol", 1e-12), floor_frac=1.0)
     assert ok, f"{case} J: worst {worst:.3e}"
     # ... and bit for bit equal to the oracle evaluated with a correctly
     # rounded x^3, the library's documented arithmetic
@@ -102,19 +102,20 @@ def test_jacobian_matches_reference(pda, case):
     try:
         op = orc.problem(orc.mesh_load(mesh_dir(m["mesh"])), m["family"], m["problem"], m["scheme"], m["icflag"],
                          m.get("params"))
-        Vo, _, _, jo = op.velocity_and_jacobian(g["U1"])
+        Vo, _, _, jo = op.velocity_and_jacobian(g["U1"], t)
     finally:
         orc.set_cube_mode(0)
     if m["family"] != 3:
-        assert np.array_equal(jv, jo), f"{case}: J differs from the oracle ({np.sum(jv != jo)} entries)"
-        assert np.array_equal(V.cpu().numpy(), Vo)
+        assert np.array_equal(jv, jo, equal_nan=True), \
+            f"{case}: J differs from the oracle ({np.sum(jv != jo)} entries)"
+        assert np.array_equal(V.cpu().numpy(), Vo, equal_nan=True)
     else:
         ok, worst = j_close(jv, jo, g["rowptr"], rtol=1e-13, floor_frac=1.0)
         assert ok, f"{case}: J vs oracle worst {worst:.3e}"
     # jacobian() alone gives the same values
     J2 = p.createJacobian()
-    p.jacobian(U, 0.0, J2)
-    assert torch.equal(J.values, J2.values)
+    p.jacobian(U, t, J2)
+    assert torch.equal(torch.nan_to_num(J.values), torch.nan_to_num(J2.values))
 
 
 @pytest.mark.parametrize("name", sorted(TRAJ))
@@ -141,9 +142,34 @@ def test_trajectory_gold(pda, name):
             pr = ((5. + 2.) / 5. - 1.) * (D[:, 3] - rho * (u ** 2 + v ** 2) * 0.5)
             assert np.allclose(rho, gold["rho"], rtol=t["rtol"], atol=t["atol"])
             assert np.allclose(pr, gold["p"], rtol=t["rtol"], atol=t["atol"])
+        elif name.startswith(("cross", "dmr")):
+            gold = np.load(os.path.join(GOLDEN, "gold", name + ".npy"))
+            assert np.allclose(D.reshape(-1, 4)[:, 0], gold, rtol=t["rtol"], atol=t["atol"])
         else:
             gold = np.load(os.path.join(GOLDEN, "gold", name + ".npy"))
             assert np.allclose(D.reshape(-1, 3)[:, 0], gold, rtol=t["rtol"], atol=t["atol"])
+
+
+PYTRAJ = json.load(open(os.path.join(GOLDEN, "gold", "py_trajectories.json")))
+
+
+@pytest.mark.parametrize("name", sorted(PYTRAJ))
+def test_python_driver_trajectory_gold(pda, name):
+    """Golds of the reference's Python tests (cross shock 80x40, 1000 steps;
+    double Mach reflection 200x50, 500 steps, first order and WENO3) on meshes
+    from the library's generator, advanced by the device SSP-RK3.  The device
+    stepper applies Pressio's update order, the Python driver its own: both
+    are the same scheme and the gold's own tolerance (1e-10 relative, 1e-12
+    absolute) holds."""
+    t = PYTRAJ[name]
+    mesh = pda.create_full_mesh(tuple(t["n"]), tuple(t["bounds"]), t["stencil"])
+    p = pda.create_problem(mesh, pda.Euler2d(t["problem"]), pda.InviscidFluxReconstruction(t["scheme"]),
+                           t["icflag"])
+    U = p.initialCondition()
+    p.advance_ssprk3(U, 0.0, t["dt"], t["steps"])
+    rho = U.cpu().numpy().reshape(-1, 4)[:, 0]
+    gold = np.load(os.path.join(GOLDEN, "gold", name + ".npy"))
+    assert np.allclose(rho, gold, rtol=t["rtol"], atol=t["atol"])
 
 
 def test_apply_jacobian_matches_spmv(pda):

@@ -7,6 +7,8 @@ Jacobi-preconditioned BiCGSTAB on the device CSR Jacobian).
   against its gold.  Both solvers stop Newton at a correction of 1e-5 (l2 over
   1600 dofs) and their linear solvers differ, so the states agree to that
   level, not bit for bit: atol 2e-4 over 30 steps.
+* The reference's implicit double Mach reflection test (its gold is the
+  first Newton iterate, see the test).
 * With tight tolerances the device Newton converges to the discrete solution,
   which a host Newton with direct sparse solves on the oracle's residual and
   Jacobian also reaches: agreement to 1e-9."""
@@ -37,6 +39,29 @@ def test_crank_nicolson_riemann_matches_reference_gold(pda):
     pres = (gamma - 1.0) * (D[:, 3] - rho * (u * u + v * v) * 0.5)
     assert np.allclose(rho, np.load(os.path.join(GOLD, "riemann_implicit_fo_rho.npy")), rtol=0, atol=2e-4)
     assert np.allclose(pres, np.load(os.path.join(GOLD, "riemann_implicit_fo_p.npy")), rtol=0, atol=2e-4)
+
+
+@pytest.mark.gpu
+def test_crank_nicolson_double_mach_reflection_matches_reference_gold(pda):
+    """The reference's implicit double Mach reflection test (tests_cpp/
+    eigen_2d_euler_double_mach_reflection_implicit: first order, 60x15, CN,
+    dt 0.01, 100 steps, Newton tolerance 1e-5).  Its gold is the first Newton
+    iterate of the first step: the next residual is NaN (negative pressure
+    behind the over-large first correction), BiCGSTAB on a NaN system returns
+    a zero correction, Newton stops, and every later step stays there.  The
+    device solver behaves the same way; with a tight linear tolerance the
+    first iterate matches the gold's exact solve."""
+    mesh = pda.load_cellcentered_uniform_mesh(os.path.join(MESHES, "m2d_s3_60x15_dmr"))
+    p = pda.create_problem(mesh, pda.Euler2d.DoubleMachReflection, pda.InviscidFluxReconstruction.FirstOrder)
+    U = p.initialCondition()
+    info = p.advance_implicit(U, 0.0, 0.01, 100, scheme="cn", newton_tol=1e-5, linear_tol=1e-14,
+                              linear_max_iters=5000)
+    rho = U.cpu().numpy().reshape(-1, 4)[:, 0]
+    gold = np.load(os.path.join(GOLD, "dmr_implicit_fo_rho.npy"))
+    assert np.allclose(rho, gold, rtol=1e-10, atol=1e-9), np.max(np.abs(rho - gold))
+    # two Newton iterations in the first step (update, then a zero correction),
+    # one in each later step
+    assert info["newton_iters"] == 2 + 99, info
 
 
 def _host_newton(po, U, dt, steps, scheme, tol=1e-13):

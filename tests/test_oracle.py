@@ -34,13 +34,15 @@ def test_oracle_bitwise_against_reference(oracle, case):
     g = golden_case(case)
     p = _problem(oracle, m)
     assert (p.dofs_sample, p.dofs_stencil, p.nnz) == (m["dofs_sample"], m["dofs_stencil"], m["nnz"])
+    t = m.get("t", 0.0)
     assert np.array_equal(p.initial_condition(), g["U0"])
-    assert np.array_equal(p.velocity(g["U0"]), g["V0"])
-    assert np.array_equal(p.velocity(g["U1"]), g["V1"])
-    V, rp, ci, jv = p.velocity_and_jacobian(g["U1"])
+    # NaN where the reference's reconstruction gives a negative pressure
+    assert np.array_equal(p.velocity(g["U0"], t), g["V0"], equal_nan=True)
+    assert np.array_equal(p.velocity(g["U1"], t), g["V1"], equal_nan=True)
+    V, rp, ci, jv = p.velocity_and_jacobian(g["U1"], t)
     assert np.array_equal(rp, g["rowptr"]) and np.array_equal(ci, g["colidx"])
-    assert np.array_equal(V, g["Vj"])
-    assert np.array_equal(jv, g["jvals"])
+    assert np.array_equal(V, g["Vj"], equal_nan=True)
+    assert np.array_equal(jv, g["jvals"], equal_nan=True)
 
 
 @pytest.mark.parametrize("name", sorted(TRAJ))
@@ -62,25 +64,54 @@ def test_oracle_trajectory_gold(oracle, name):
         pr = ((5. + 2.) / 5. - 1.) * (D[:, 3] - rho * (u ** 2 + v ** 2) * 0.5)
         assert np.allclose(rho, gold["rho"], rtol=t["rtol"], atol=t["atol"])
         assert np.allclose(pr, gold["p"], rtol=t["rtol"], atol=t["atol"])
+    elif name.startswith(("cross", "dmr")):
+        gold = np.load(os.path.join(GOLDEN, "gold", name + ".npy"))
+        assert np.allclose(U.reshape(-1, 4)[:, 0], gold, rtol=t["rtol"], atol=t["atol"])
     else:
         gold = np.load(os.path.join(GOLDEN, "gold", name + ".npy"))
         assert np.allclose(U.reshape(-1, 3)[:, 0], gold, rtol=t["rtol"], atol=t["atol"])
+
+
+PYTRAJ = json.load(open(os.path.join(GOLDEN, "gold", "py_trajectories.json")))
+
+
+def generated_mesh(pda, oracle, t):
+    """The case's full mesh from the library's host-side generator (the
+    reference's create_full_mesh.py layout), handed to the oracle."""
+    mesh = pda.create_full_mesh(tuple(t["n"]), tuple(t["bounds"]), t["stencil"])
+    g, x, y, z, _, _ = mesh._arrays()
+    return oracle.mesh_from_arrays(2, t["stencil"], g, x, y, z, (mesh.dx(), mesh.dy(), mesh.dz()))
+
+
+@pytest.mark.parametrize("name", sorted(PYTRAJ))
+def test_oracle_python_driver_gold(pda, oracle, name):
+    """Golds of the reference's Python tests (its driver's SSP-RK3 update
+    order), with the oracle's restatement of that driver."""
+    t = PYTRAJ[name]
+    if t["n"][0] * t["n"][1] > 5000:
+        pytest.skip("the 200x50 double-Mach runs are checked on the device only (runtime)")
+    p = oracle.problem(generated_mesh(pda, oracle, t), t["family"], t["problem"], t["scheme"], t["icflag"])
+    U = p.initial_condition()
+    p.ssprk3_py(U, 0.0, t["dt"], t["steps"])
+    gold = np.load(os.path.join(GOLDEN, "gold", name + ".npy"))
+    assert np.allclose(U.reshape(-1, 4)[:, 0], gold, rtol=t["rtol"], atol=t["atol"])
 
 
 @pytest.mark.parametrize("case", sorted(MANIFEST))
 def test_correctly_rounded_cube_stays_within_the_jacobian_tolerance(oracle, case):
     """The library evaluates the reference's pow(x, 3.) as a correctly rounded
     cube.  Evaluated that way, the oracle's Jacobian stays within 1e-12 of the
-    row scale of the reference's (velocities are unaffected)."""
+    row scale of the reference's (the case's own tolerance across the double
+    Mach reflection's shock; velocities are unaffected)."""
     from conftest import j_close
     m = MANIFEST[case]
     g = golden_case(case)
     oracle.set_cube_mode(1)
     try:
         p = _problem(oracle, m)
-        V, rp, ci, jv = p.velocity_and_jacobian(g["U1"])
+        V, rp, ci, jv = p.velocity_and_jacobian(g["U1"], m.get("t", 0.0))
     finally:
         oracle.set_cube_mode(0)
-    assert np.array_equal(V, g["Vj"])
-    ok, worst = j_close(jv, g["jvals"], rp, floor_frac=1.0)
+    assert np.array_equal(V, g["Vj"], equal_nan=True)
+    ok, worst = j_close(jv, g["jvals"], rp, rtol=m.get("jtol", 1e-12), floor_frac=1.0)
     assert ok, worst
