@@ -70,6 +70,7 @@ typedef int pda_status;
 #define PDA_EULER2D_CROSS_SHOCK 7     /* Euler2d::CrossShock */
 #define PDA_EULER2D_TESTING_NEUMANN 8 /* Euler2d::testingonlyneumann */
 #define PDA_EULER3D_PERIODIC_SMOOTH 0 /* Euler3d::PeriodicSmooth */
+#define PDA_EULER3D_SEDOV_SYMMETRY 1  /* Euler3d::SedovSymmetry (FirstOrder, WENO3) */
 #define PDA_SWE2D_SLIP_WALL 0         /* Swe2d::SlipWall */
 
 typedef struct pda_mesh pda_mesh;

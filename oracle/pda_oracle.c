@@ -791,7 +791,7 @@ static void fill_ghosts(const orc_problem *p, int64_t r, const double *U, double
       for (int layer = 0; layer < L; ++layer) {
         if (same[layer] != -1) continue;
         int src = cell;
-        const int sedovSym = p->fam == E2 && p->prob == 3;
+        const int sedovSym = (p->fam == E2 && p->prob == 3) || (p->fam == E3 && p->prob == 1);
         const int normalShock = p->fam == E2 && p->prob == 5;
         const int dmr = p->fam == E2 && p->prob == 6, cross = p->fam == E2 && p->prob == 7;
         if (dmr || cross) {
@@ -820,8 +820,9 @@ static void fill_ghosts(const orc_problem *p, int64_t r, const double *U, double
         for (int d = 0; d < nd; ++d) {
           double v = U[(int64_t)src * nd + d];
           if (p->fam == SW && d == (ax == 0 ? 1 : 2)) v = -v;
-          /* Sedov symmetry: reflective on the left (x momentum) and bottom (y momentum) */
-          if (sedovSym && minus && d == (ax == 0 ? 1 : 2)) v = -v;
+          /* Sedov symmetry: reflective on the minus side of each axis (that
+             axis' momentum; Ghost3dSedov, impl/euler_3d_ghost_filler_sedov.hpp:58-216) */
+          if (sedovSym && minus && d == ax + 1) v = -v;
           /* normal shock: reflective top and bottom (y momentum) */
           if (normalShock && ax == 1 && d == 2) v = -v;
           g[layer * nd + d] = v;
@@ -1178,6 +1179,17 @@ void orc_initial_condition(const orc_problem *p, double *U) {
       U[i * 4 + 2] = prim[0] * prim[2];
       U[i * 4 + 3] = energy(gm1inv, prim, 4);
     }
+  } else if (p->fam == E3 && p->prob == 1) {
+    /* sedov3dInitialCondition (impl/euler_3d_initial_condition.hpp:87-141) */
+    const double h = fmin(m->dx[0], fmin(m->dx[1], m->dx[2]));
+    const double rad = 3. * h, gm1 = p->gamma - 1.;
+    for (int64_t i = 0; i < m->nst; ++i) {
+      const double rr = sqrt(x[i] * x[i] + y[i] * y[i] + z[i] * z[i]);
+      const double prim[5] = {1., 0., 0., 0., rr <= rad ? (3. * gm1 * 0.851072) / (4. * M_PI * rad * rad * rad) : 2.5e-5};
+      U[i * 5] = prim[0];
+      for (int d = 1; d < 4; ++d) U[i * 5 + d] = prim[0] * prim[d];
+      U[i * 5 + 4] = energy(1. / gm1, prim, 5);
+    }
   } else if (p->fam == E3) {
     const double gm1inv = 1. / (p->gamma - 1.);
     double prim[5];
@@ -1327,6 +1339,8 @@ static void row_vj_near(const orc_problem *p, int64_t r, const double *U, double
       else if (ax == 1 && G(m, r, colm(2, 1, 0)) == -1) fac[2] = -1;
     }
     if (p->fam == E2 && p->prob == 5 && ax == 1) fac[2] = -1; /* euler_2d_prob_class.hpp:1150-1162 */
+    /* euler_3d_prob_class.hpp:626-666, findCellBdType :1017-1043 */
+    if (p->fam == E3 && p->prob == 1 && G(m, r, colm(3, ax, 0)) == -1) fac[1 + ax] = -1;
     if (p->fam == E2 && p->prob == 6 && ax == 1) {
       /* euler_2d_prob_class.hpp:1164-1193 */
       const int back = G(m, r, colm(2, 1, 0)) == -1;

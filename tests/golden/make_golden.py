@@ -69,6 +69,10 @@ FULL_MESHES = {
     "m2d_s3_60x15_dmr": "-n 60 15 --bounds 0.0 4.0 0.0 1.0 -s 3",
     "m2d_s5_60x15_dmr": "-n 60 15 --bounds 0.0 4.0 0.0 1.0 -s 5",
     "m2d_s7_60x15_dmr": "-n 60 15 --bounds 0.0 4.0 0.0 1.0 -s 7",
+    # 3D Sedov symmetry (tests_cpp/eigen_3d_euler_sedov_symmetry/test.cmake bounds)
+    "m3d_s3_8_sedov": "-n 8 8 8 --bounds 0.0 0.4 0.0 0.4 0.0 0.4 -s 3",
+    "m3d_s5_8_sedov": "-n 8 8 8 --bounds 0.0 0.4 0.0 0.4 0.0 0.4 -s 5",
+    "m3d_s5_6x5x7_sedov": "-n 6 5 7 --bounds 0.0 0.4 0.0 0.4 0.0 0.4 -s 5",
     "m3d_s3_8_per": "-n 8 8 8 --bounds -1.0 1.0 -1.0 1.0 -1.0 1.0 -s 3 --periodic x y z",
     "m3d_s5_8_per": "-n 8 8 8 --bounds -1.0 1.0 -1.0 1.0 -1.0 1.0 -s 5 --periodic x y z",
     "m3d_s5_6x5x7_per": "-n 6 5 7 --bounds -1.0 1.0 -1.0 1.0 -1.0 1.0 -s 5 --periodic x y z",
@@ -84,6 +88,7 @@ SAMPLE_MESHES = {
     "s2d_s7_16_sedsym_rand": ("m2d_s7_16_sedsym", "random:40"),
     "s2d_s7_60x15_dmr_rand": ("m2d_s7_60x15_dmr", "random:60"),
     "s2d_s5_40x20_cross_rand": ("m2d_s5_40x20_cross", "random:50"),
+    "s3d_s5_8_sedov_rand": ("m3d_s5_8_sedov", "random:40"),
 }
 
 # case -> (mesh, family, problem, scheme, icflag, params)
@@ -141,6 +146,10 @@ CASE_LIST = {
     "cross_params_w5": ("m2d_s7_40x20_cross", E2, 7, 2, 1,
                         {"crossShockDensity": 0.2, "crossShockInletXVel": 5.0, "crossShockBottomYVel": 2.0}),
     "sample_cross_w3": ("s2d_s5_40x20_cross_rand", E2, 7, 1, 1, {}),
+    "sedov3d_fo": ("m3d_s3_8_sedov", E3, 1, 0, 1, {}),
+    "sedov3d_w3": ("m3d_s5_8_sedov", E3, 1, 1, 1, {}),
+    "sedov3d_w3_odd": ("m3d_s5_6x5x7_sedov", E3, 1, 1, 1, {}),
+    "sample_sedov3d_w3": ("s3d_s5_8_sedov_rand", E3, 1, 1, 1, {}),
 }
 
 # evaluation time of a case (time-dependent ghost states: the double Mach
@@ -346,44 +355,69 @@ def make_gold(ref: Ref):
             np.save(os.path.join(GOLD, f"{base}_{tag}.npy"), rho_g)
     json.dump(traj, open(os.path.join(GOLD, "trajectories.json"), "w"), indent=1)
 
-    # Golds of the reference's Python tests, advanced by the Python driver's
-    # own SSP-RK3 update (pressiodemoapps/__init__.py:155-185) on meshes of
-    # create_full_mesh.py: cross shock 80x40 first order, dt 1e-3, 1000 steps
-    # (tests_py/2d_euler_cross_shock); double Mach reflection 200x50 first
-    # order and WENO3, dt 5e-4, 500 steps (tests_py/2d_double_mach_reflection).
-    # The meshes are regenerated by the tests; only the density golds are kept.
-    pyt = {}
-    for name, sub, prob, scheme, st, n, bounds, dt, steps in (
-            ("cross_py_firstorder", "2d_euler_cross_shock", 7, 0, 3, (80, 40), (0.0, 2.0, 0.0, 1.0), 1e-3, 1000),
-            ("dmr_py_firstorder", "2d_double_mach_reflection/firstorder", 6, 0, 3, (200, 50), (0.0, 4.0, 0.0, 1.0),
-             5e-4, 500),
-            ("dmr_py_weno3", "2d_double_mach_reflection/weno3", 6, 1, 5, (200, 50), (0.0, 4.0, 0.0, 1.0), 5e-4, 500)):
-        src = os.path.join(REF, "tests_py", sub)
-        rho_g = np.loadtxt(os.path.join(src, "rho_gold.txt"))
-        L = ref.L
-        names = (C.c_char_p * 1)()
-        vals = (C.c_double * 1)()
-        h = L.ref_create(src.encode(), E2, prob, scheme, 1, 0, names, vals)
+    # Golds on meshes the tests regenerate (too large to keep as fixtures):
+    # * the reference's Python tests, advanced by the Python driver's own
+    #   SSP-RK3 update (pressiodemoapps/__init__.py:155-185): cross shock 80x40
+    #   first order, dt 1e-3, 1000 steps (tests_py/2d_euler_cross_shock); double
+    #   Mach reflection 200x50 first order and WENO3, dt 5e-4, 500 steps
+    #   (tests_py/2d_double_mach_reflection) -- density golds;
+    # * 3D Sedov symmetry, SSP-RK3 dt 1e-4, 250 steps, on [0, 0.4]^3 with 20^3
+    #   and 20x25x28 cells, first order and WENO3, whole-state golds at rtol
+    #   1e-8 / atol 1e-10 (tests_cpp/eigen_3d_euler_sedov_symmetry, compare.py).
+    gen = {}
+    runs = [
+        ("cross_py_firstorder", "tests_py/2d_euler_cross_shock/rho_gold.txt", E2, 7, 0, 3, (80, 40),
+         (0.0, 2.0, 0.0, 1.0), "ssprk3_py", 1e-3, 1000, "rho", 1e-10, 1e-12),
+        ("dmr_py_firstorder", "tests_py/2d_double_mach_reflection/firstorder/rho_gold.txt", E2, 6, 0, 3,
+         (200, 50), (0.0, 4.0, 0.0, 1.0), "ssprk3_py", 5e-4, 500, "rho", 1e-10, 1e-12),
+        ("dmr_py_weno3", "tests_py/2d_double_mach_reflection/weno3/rho_gold.txt", E2, 6, 1, 5, (200, 50),
+         (0.0, 4.0, 0.0, 1.0), "ssprk3_py", 5e-4, 500, "rho", 1e-10, 1e-12),
+    ]
+    for tag, scheme, st in (("firstorder", 0, 3), ("weno3", 1, 5)):
+        for shape, n in (("equal", (20, 20, 20)), ("not_equal", (20, 25, 28))):
+            runs.append((f"sedov3d_{tag}_{shape}",
+                         f"tests_cpp/eigen_3d_euler_sedov_symmetry/{tag}_nxnynz_{shape}/gold_state.txt", E3, 1,
+                         scheme, st, n, (0.0, 0.4, 0.0, 0.4, 0.0, 0.4), "ssprk3", 1e-4, 250, "state", 1e-8,
+                         1e-10))
+    import tempfile
+    for (name, gsrc, fam, prob, scheme, st, n, bounds, stepper, dt, steps, field, rtol, atol) in runs:
+        gold = np.loadtxt(os.path.join(REF, gsrc))
+        with tempfile.TemporaryDirectory() as tmp:
+            nargs = " ".join(str(v) for v in n)
+            bargs = " ".join(str(v) for v in bounds)
+            run(f"{sys.executable} {REF}/meshing_scripts/create_full_mesh.py -n {nargs} --bounds {bargs} "
+                f"-s {st} --outDir {tmp}")
+            L = ref.L
+            names = (C.c_char_p * 1)()
+            vals = (C.c_double * 1)()
+            h = L.ref_create(tmp.encode(), fam, prob, scheme, 1, 0, names, vals)
+            assert h, L.ref_last_error()
         sz = (C.c_long * 4)()
         L.ref_sizes(h, sz)
         U = np.empty(sz[2])
         L.ref_ic(h, vp(U))
-        v = np.empty(sz[1])
-        t = 0.0
-        for _ in range(steps):
-            L.ref_velocity(h, vp(U), t, vp(v))
-            u1 = U + dt * v
-            L.ref_velocity(h, vp(u1), t + dt, vp(v))
-            u2 = 3. / 4. * U + 1. / 4. * u1 + 1. / 4. * dt * v
-            L.ref_velocity(h, vp(u2), t + dt * 0.5, vp(v))
-            U = 1. / 3. * (U + 2. * u2 + 2. * dt * v)
-            t += dt
+        if stepper == "ssprk3":
+            L.ref_ssprk3(h, vp(U), 0.0, dt, steps)
+        else:
+            v = np.empty(sz[1])
+            t = 0.0
+            for _ in range(steps):
+                L.ref_velocity(h, vp(U), t, vp(v))
+                u1 = U + dt * v
+                L.ref_velocity(h, vp(u1), t + dt, vp(v))
+                u2 = 3. / 4. * U + 1. / 4. * u1 + 1. / 4. * dt * v
+                L.ref_velocity(h, vp(u2), t + dt * 0.5, vp(v))
+                U = 1. / 3. * (U + 2. * u2 + 2. * dt * v)
+                t += dt
         L.ref_destroy(h)
-        assert np.allclose(U.reshape(-1, 4)[:, 0], rho_g, rtol=1e-10, atol=1e-12), name
-        pyt[name] = dict(n=list(n), bounds=list(bounds), stencil=st, family=E2, problem=prob, scheme=scheme,
-                         icflag=1, stepper="ssprk3_py", dt=dt, steps=steps, rtol=1e-10, atol=1e-12)
-        np.save(os.path.join(GOLD, name + ".npy"), rho_g)
-    json.dump(pyt, open(os.path.join(GOLD, "py_trajectories.json"), "w"), indent=1)
+        nd = sz[0]
+        got = U.reshape(-1, nd)[:, 0] if field == "rho" else U
+        assert np.allclose(got, gold, rtol=rtol, atol=atol), name
+        gen[name] = dict(n=list(n), bounds=list(bounds), stencil=st, family=fam, problem=prob, scheme=scheme,
+                         icflag=1, stepper=stepper, dt=dt, steps=steps, field=field, rtol=rtol, atol=atol)
+        np.save(os.path.join(GOLD, name + ".npy"), gold)
+        print("gold", name)
+    json.dump(gen, open(os.path.join(GOLD, "trajectories_generated_mesh.json"), "w"), indent=1)
 
     # Crank-Nicolson + Newton + BiCGSTAB gold of the reference's implicit
     # Riemann test (first order, 20x20, dt 0.02, 30 steps, Newton tolerance 1e-5)

@@ -150,26 +150,28 @@ def test_trajectory_gold(pda, name):
             assert np.allclose(D.reshape(-1, 3)[:, 0], gold, rtol=t["rtol"], atol=t["atol"])
 
 
-PYTRAJ = json.load(open(os.path.join(GOLDEN, "gold", "py_trajectories.json")))
+GENTRAJ = json.load(open(os.path.join(GOLDEN, "gold", "trajectories_generated_mesh.json")))
 
 
-@pytest.mark.parametrize("name", sorted(PYTRAJ))
-def test_python_driver_trajectory_gold(pda, name):
-    """Golds of the reference's Python tests (cross shock 80x40, 1000 steps;
-    double Mach reflection 200x50, 500 steps, first order and WENO3) on meshes
-    from the library's generator, advanced by the device SSP-RK3.  The device
-    stepper applies Pressio's update order, the Python driver its own: both
-    are the same scheme and the gold's own tolerance (1e-10 relative, 1e-12
-    absolute) holds."""
-    t = PYTRAJ[name]
+@pytest.mark.parametrize("name", sorted(GENTRAJ))
+def test_generated_mesh_trajectory_gold(pda, name):
+    """Golds of the reference tests whose meshes the library generates here:
+    the Python tests (cross shock 80x40, 1000 steps; double Mach reflection
+    200x50, 500 steps, first order and WENO3) and the 3D Sedov symmetry runs
+    (20^3 and 20x25x28, first order and WENO3, 250 steps, whole state), all
+    advanced by the device SSP-RK3.  The device stepper applies Pressio's
+    update order and the Python driver its own: both are the same scheme and
+    the gold's own tolerance holds."""
+    t = GENTRAJ[name]
     mesh = pda.create_full_mesh(tuple(t["n"]), tuple(t["bounds"]), t["stencil"])
-    p = pda.create_problem(mesh, pda.Euler2d(t["problem"]), pda.InviscidFluxReconstruction(t["scheme"]),
-                           t["icflag"])
+    enum = (pda.Euler2d if t["family"] == 1 else pda.Euler3d)(t["problem"])
+    p = pda.create_problem(mesh, enum, pda.InviscidFluxReconstruction(t["scheme"]), t["icflag"])
     U = p.initialCondition()
     p.advance_ssprk3(U, 0.0, t["dt"], t["steps"])
-    rho = U.cpu().numpy().reshape(-1, 4)[:, 0]
+    D = U.cpu().numpy()
+    got = D.reshape(-1, p.numDofPerCell())[:, 0] if t["field"] == "rho" else D
     gold = np.load(os.path.join(GOLDEN, "gold", name + ".npy"))
-    assert np.allclose(rho, gold, rtol=t["rtol"], atol=t["atol"])
+    assert np.allclose(got, gold, rtol=t["rtol"], atol=t["atol"])
 
 
 def test_apply_jacobian_matches_spmv(pda):
@@ -286,3 +288,16 @@ def test_determinism_and_jacobian_sample_consistency_256(pda):
     sub = Jf[rows_full][:, cols_full].toarray()
     assert np.array_equal(sub, Jsm.toarray())
     assert torch.equal(Vs, V.view(-1, 4)[torch.from_numpy(gids).cuda()].reshape(-1))
+
+
+def test_sedov3d_weno5_refused_as_in_the_reference(pda):
+    """The reference's 3D Sedov ghost filler has no WENO5 layers and throws
+    at evaluation; the library refuses the evaluation the same way."""
+    torch = _torch()
+    mesh = pda.create_full_mesh((8, 8, 8), (0.0, 0.4, 0.0, 0.4, 0.0, 0.4), 7)
+    p = pda.create_problem(mesh, pda.Euler3d.SedovSymmetry, pda.InviscidFluxReconstruction.Weno5)
+    U = p.initialCondition()
+    V = p.createVelocity()
+    with pytest.raises(pda.PdaError):
+        p.velocity(U, 0.0, V)
+    torch.cuda.synchronize()

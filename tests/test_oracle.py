@@ -72,7 +72,7 @@ def test_oracle_trajectory_gold(oracle, name):
         assert np.allclose(U.reshape(-1, 3)[:, 0], gold, rtol=t["rtol"], atol=t["atol"])
 
 
-PYTRAJ = json.load(open(os.path.join(GOLDEN, "gold", "py_trajectories.json")))
+GENTRAJ = json.load(open(os.path.join(GOLDEN, "gold", "trajectories_generated_mesh.json")))
 
 
 def generated_mesh(pda, oracle, t):
@@ -80,21 +80,22 @@ def generated_mesh(pda, oracle, t):
     reference's create_full_mesh.py layout), handed to the oracle."""
     mesh = pda.create_full_mesh(tuple(t["n"]), tuple(t["bounds"]), t["stencil"])
     g, x, y, z, _, _ = mesh._arrays()
-    return oracle.mesh_from_arrays(2, t["stencil"], g, x, y, z, (mesh.dx(), mesh.dy(), mesh.dz()))
+    dim = len(t["n"])
+    return oracle.mesh_from_arrays(dim, t["stencil"], g, x, y, z, (mesh.dx(), mesh.dy(), mesh.dz()))
 
 
-@pytest.mark.parametrize("name", sorted(PYTRAJ))
-def test_oracle_python_driver_gold(pda, oracle, name):
-    """Golds of the reference's Python tests (its driver's SSP-RK3 update
-    order), with the oracle's restatement of that driver."""
-    t = PYTRAJ[name]
-    if t["n"][0] * t["n"][1] > 5000:
-        pytest.skip("the 200x50 double-Mach runs are checked on the device only (runtime)")
+@pytest.mark.parametrize("name", sorted(GENTRAJ))
+def test_oracle_generated_mesh_gold(pda, oracle, name):
+    """Golds of the reference tests whose meshes are regenerated here: the
+    Python tests (their driver's SSP-RK3 update order, ``ssprk3_py``) and the
+    3D Sedov symmetry runs (Pressio's order, whole state)."""
+    t = GENTRAJ[name]
     p = oracle.problem(generated_mesh(pda, oracle, t), t["family"], t["problem"], t["scheme"], t["icflag"])
     U = p.initial_condition()
-    p.ssprk3_py(U, 0.0, t["dt"], t["steps"])
+    (p.ssprk3_py if t["stepper"] == "ssprk3_py" else p.ssprk3)(U, 0.0, t["dt"], t["steps"])
     gold = np.load(os.path.join(GOLDEN, "gold", name + ".npy"))
-    assert np.allclose(U.reshape(-1, 4)[:, 0], gold, rtol=t["rtol"], atol=t["atol"])
+    got = U.reshape(-1, p.ndpc)[:, 0] if t["field"] == "rho" else U
+    assert np.allclose(got, gold, rtol=t["rtol"], atol=t["atol"])
 
 
 @pytest.mark.parametrize("case", sorted(MANIFEST))
