@@ -354,6 +354,14 @@ pda_status pda_lspg_decode(pda_lspg *rom, const double *d_x, double *d_y);
 pda_status pda_lspg_advance_bdf1(pda_lspg *rom, double *d_x, double dt, int64_t n_steps, int gn_iters,
                                  double tol, int use_graph, double *info);
 
+/* Gauss-Newton iteration form: fused = 1 (default) evaluates the sample-mesh
+ * velocity and the product of its Jacobian with the trial space's latent
+ * Jacobian face by face in one launch (never forming the CSR Jacobian);
+ * fused = 0 assembles the sample-mesh CSR Jacobian with pda_velocity_and_jacobian
+ * and multiplies it in a second kernel.  Same LSPG iteration; results agree
+ * to rounding. */
+pda_status pda_lspg_set_fused(pda_lspg *rom, int fused);
+
 /* Implicit steps on the device (the consumer of the Jacobian in the
  * reference's implicit tests, tests_cpp/eigen_2d_euler_riemann_implicit/
  * main.cc:31-44: Pressio's implicit stepper + Newton-Raphson + BiCGSTAB).

@@ -154,6 +154,7 @@ _SIGS = {
     "pda_advance_implicit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int64, C.c_int,
                                        C.c_double, C.c_int, C.c_double, C.c_int, C.c_void_p]),
     "pda_lspg_decode": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "pda_lspg_set_fused": (C.c_int, [C.c_void_p, C.c_int]),
     "pda_lspg_advance_bdf1": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int64, C.c_int, C.c_double,
                                         C.c_int, C.c_void_p]),
 }
@@ -785,6 +786,11 @@ class LspgRom:
                                          int(W1.shape[0]), int(W2.shape[0]), _vp(uref), _vp(scale),
                                          *[_vp(t) for t in ts], int(bool(tensor_cores)), C.byref(h)))
         return LspgRom(h, sample_problem, (s2, k, uref.numel()))
+
+    def set_fused(self, fused=True):
+        """Fused Gauss-Newton iteration (default) or the assembled sample-mesh
+        Jacobian path; the same LSPG iteration, equal to rounding."""
+        _check(lib().pda_lspg_set_fused(self._h, 1 if fused else 0))
 
     def decode(self, x):
         import torch

@@ -6,6 +6,7 @@
 #include "tiles.cuh"
 #include "batch.cuh"
 #include "jfaces.cuh"
+#include "lspg_fused.cuh"
 #include "launch.hpp"
 
 namespace pda {
@@ -97,6 +98,53 @@ void rows_vj_inner(int scheme, const RowTable &t, const MeshArgs &m, const Phys 
       k_rows_vj_inner_par<FAM, Weno5><<<div_up(t.nrows, RP::RPB), RP::THREADS, 0, s>>>(t, m, p, U, rowptr, V, J);
       break;
     }
+  }
+}
+
+int device_sms() {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+// rows per block: the fewest blocks that still cover every SM once, within
+// the shared-memory budget
+int lspg_fused_rpb(int scheme, int innerRows, int nearRows, int K) {
+  const int rows = innerRows + nearRows;
+  const int S = 2 * (scheme + 1) + 1;
+  const int bySmem = (int)(FusedPar<FAM>::kSmemLimit / FusedPar<FAM>::smem_row(S, K));
+  return std::max(1, std::min(std::min(FusedPar<FAM>::RPB_MAX, bySmem), div_up(rows, device_sms())));
+}
+
+int lspg_fused_blocks(int scheme, int innerRows, int nearRows, int K) {
+  const int rpb = lspg_fused_rpb(scheme, innerRows, nearRows, K);
+  return div_up(innerRows, rpb) + div_up(nearRows, rpb);
+}
+
+void lspg_fused_prepare() {
+  const int bytes = (int)FusedPar<FAM>::kSmemLimit;
+  cudaFuncSetAttribute(k_lspg_fused<FAM, FirstOrder>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_lspg_fused<FAM, Weno3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_lspg_fused<FAM, Weno5>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+void lspg_fused(int scheme, const RowTable &ti, const RowTable &tn, const MeshArgs &m, const Phys &p,
+                const LspgArgs &a, cudaStream_t s) {
+  const int rpb = lspg_fused_rpb(scheme, ti.nrows, tn.nrows, a.K);
+  const int nbI = div_up(ti.nrows, rpb);
+  const int nb = lspg_fused_blocks(scheme, ti.nrows, tn.nrows, a.K);
+  if (nb <= 0) return;
+  constexpr int T = FusedPar<FAM>::THREADS;
+  const size_t sm = (size_t)rpb * FusedPar<FAM>::smem_row(2 * (scheme + 1) + 1, a.K);
+  switch (scheme) {
+    case FirstOrder: k_lspg_fused<FAM, FirstOrder><<<nb, T, sm, s>>>(ti, tn, rpb, nbI, m, p, a); break;
+    case Weno3: k_lspg_fused<FAM, Weno3><<<nb, T, sm, s>>>(ti, tn, rpb, nbI, m, p, a); break;
+    default: k_lspg_fused<FAM, Weno5><<<nb, T, sm, s>>>(ti, tn, rpb, nbI, m, p, a); break;
   }
 }
 

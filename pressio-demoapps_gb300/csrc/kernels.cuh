@@ -118,6 +118,36 @@ PDA_HD void reconstruct_face_grad(double uNeg[NDPC], double uPos[NDPC],
   }
 }
 
+// One side of one dof's face reconstruction from its 2H cell values:
+// side 0 the left-biased value uNeg, side 1 the right-biased uPos (the
+// one-sided halves of reconstruct_face / reconstruct_face_grad, same
+// expressions).
+template <int SCHEME>
+PDA_HD double face_value_side(int side, const double *q) {
+  if constexpr (SCHEME == FirstOrder) {
+    return q[side];
+  } else if constexpr (SCHEME == Weno3) {
+    return side == 0 ? weno3_neg(q[0], q[1], q[2]) : weno3_pos(q[1], q[2], q[3]);
+  } else {
+    return side == 0 ? weno5_neg(q[0], q[1], q[2], q[3], q[4]) : weno5_pos(q[1], q[2], q[3], q[4], q[5]);
+  }
+}
+
+template <int SCHEME>
+PDA_HD void face_grad_side(int side, double &u, double g[2 * SchemeTraits<SCHEME>::h], const double *q) {
+  if constexpr (SCHEME == FirstOrder) {
+    u = q[side];
+    g[0] = side == 0 ? 1. : 0.;
+    g[1] = side == 0 ? 0. : 1.;
+  } else if constexpr (SCHEME == Weno3) {
+    if (side == 0) weno3_neg_grad(u, g, q[0], q[1], q[2], q[3]);
+    else weno3_pos_grad(u, g, q[0], q[1], q[2], q[3]);
+  } else {
+    if (side == 0) weno5_neg_grad(u, g, q[0], q[1], q[2], q[3], q[4], q[5]);
+    else weno5_pos_grad(u, g, q[0], q[1], q[2], q[3], q[4], q[5]);
+  }
+}
+
 template <int NDPC>
 __device__ __forceinline__ void load_cell(double q[NDPC], const double *__restrict__ U, int c,
                                           bool flip, int reflectDof) {
@@ -412,16 +442,24 @@ k_rows_vj_inner(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U,
 }
 
 // ---------------------------------------------------------------------------
-// V and J of inner rows with the faces of each row computed in parallel:
-// thread (row, face) evaluates one face (WENO value + gradient, flux, flux
-// Jacobians) into shared memory; thread (row, k) then forms dof k of V and
-// row k of the row's J block, accumulating every entry in a local array in
-// exactly the order of k_rows_vj_inner (axes, then per column dof j: left
-// face Neg / Pos over the stencil slots, then right face), and writes each
-// CSR value once.  Bit-identical to k_rows_vj_inner (WENO3 / WENO5); built
-// for sample meshes, whose few rows make the per-row serial formulation and
-// its global read-modify-write chains latency-bound.
+// V and J of the rows of a sample mesh (or of any row set), each row's work
+// spread over many threads.  GB300's FP64 units give one warp one instruction
+// per ~64 cycles, so a row set of a few hundred rows is bound by the longest
+// per-thread chain of FP64 instructions, not by the total: the work of a row
+// is split until every thread's chain is short.
+//   phase 1a  thread (side, row, face, dof): one side of the face's
+//             reconstruction (value and, for inner rows, its gradient); the
+//             side is uniform per warp, so each warp evaluates one side only
+//   phase 1b  thread (part, row, face): the face flux (part 0) or the flux
+//             Jacobians (part 1), again one part per warp
+//   phase 2   thread (row, k, j): dof k of V (j == 0) and column dof j of row
+//             k of the row's J blocks, every entry accumulated in exactly the
+//             order of the per-row kernels (k_rows_vj_inner /
+//             k_rows_vj_nearbd), then written once.
+// Bit-identical to those kernels.
 // ---------------------------------------------------------------------------
+__host__ __device__ constexpr int pad_warp(int n) { return (n + 31) / 32 * 32; }
+
 template <int FAM, int SCHEME> struct RowFace {
   static constexpr int NDPC = Fam<FAM>::ndpc, G = 2 * SchemeTraits<SCHEME>::h;
   double fl[NDPC];
@@ -432,10 +470,11 @@ template <int FAM, int SCHEME> struct RowFace {
 
 template <int FAM, int SCHEME> struct RowPar {
   static constexpr int NF = 2 * Fam<FAM>::dim, NDPC = Fam<FAM>::ndpc;
-  // few rows per block: sample meshes have few rows and GB300's FP64 units
-  // are narrow, so the rows are spread over as many SMs as possible
-  static constexpr int RPB = 4;
-  static constexpr int THREADS = RPB * NF * NDPC;  // phase 1a: one thread per (row, face, dof)
+  static constexpr int RPB = 4;                        // rows per block
+  static constexpr int SIDE = pad_warp(RPB * NF * NDPC);  // phase-1a threads per side
+  static constexpr int PART = pad_warp(RPB * NF);         // phase-1b threads per part
+  static constexpr int THREADS = 2 * SIDE;
+  static_assert(2 * PART <= THREADS, "phase 1b fits the block");
 };
 
 template <int FAM, int SCHEME>
@@ -444,36 +483,36 @@ k_rows_vj_inner_par(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U
                     double *__restrict__ V, double *__restrict__ J) {
   using F = Fam<FAM>;
   using RF = RowFace<FAM, SCHEME>;
+  using RP = RowPar<FAM, SCHEME>;
   constexpr int NDPC = F::ndpc, DIM = F::dim, H = SchemeTraits<SCHEME>::h, S = 2 * H + 1, G = 2 * H;
-  constexpr int NF = RowPar<FAM, SCHEME>::NF, RPB = RowPar<FAM, SCHEME>::RPB;
+  constexpr int NF = RP::NF, RPB = RP::RPB;
   constexpr int NB = 1 + 2 * DIM * H;  // distinct column blocks of an inner row at most
   __shared__ RF fd[RPB][NF];
   const int tid = threadIdx.x;
-  {  // phase 1a: one (face, dof) per thread: reconstruction and its gradient
-    const int rl = tid / (NF * NDPC), f = (tid / NDPC) % NF, d = tid % NDPC, ax = f >> 1, side = f & 1;
+  {  // phase 1a
+    const int side = tid / RP::SIDE, slot = tid % RP::SIDE;
+    const int rl = slot / (NF * NDPC), f = (slot / NDPC) % NF, d = slot % NDPC, ax = f >> 1, fs = f & 1;
     const int e = blockIdx.x * RPB + rl;
-    if (e < t.nrows) {
-      double q[G][1];
+    if (slot < RPB * NF * NDPC && e < t.nrows) {
+      double q[G];
       const size_t base = ((size_t)e * DIM + ax) * S;
 #pragma unroll
-      for (int s = 0; s < G; ++s) q[s][0] = __ldg(U + (size_t)t.src[base + side + s] * NDPC + d);
+      for (int s = 0; s < G; ++s) q[s] = __ldg(U + (size_t)t.src[base + fs + s] * NDPC + d);
       RF &o = fd[rl][f];
-      double uN[1], uP[1], gN[1][G], gP[1][G];
-      reconstruct_face_grad<1, SCHEME>(uN, uP, gN, gP, q);
-      o.uN[d] = uN[0];
-      o.uP[d] = uP[0];
+      double u, g[G];
+      face_grad_side<SCHEME>(side, u, g, q);
+      double *gs = side == 0 ? o.gN[d] : o.gP[d];
+      (side == 0 ? o.uN : o.uP)[d] = u;
 #pragma unroll
-      for (int s = 0; s < G; ++s) {
-        o.gN[d][s] = gN[0][s];
-        o.gP[d][s] = gP[0][s];
-      }
+      for (int s = 0; s < G; ++s) gs[s] = g[s];
     }
   }
   __syncthreads();
-  if (tid < RPB * NF) {  // phase 1b: one face per thread: flux and flux Jacobians
-    const int rl = tid / NF, f = tid % NF, ax = f >> 1;
+  {  // phase 1b
+    const int part = tid / RP::PART, slot = tid % RP::PART;
+    const int rl = slot / NF, f = slot % NF, ax = f >> 1;
     const int e = blockIdx.x * RPB + rl;
-    if (e < t.nrows) {
+    if (part < 2 && slot < RPB * NF && e < t.nrows) {
       RF &o = fd[rl][f];
       double uN[NDPC], uP[NDPC];
 #pragma unroll
@@ -481,24 +520,27 @@ k_rows_vj_inner_par(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U
         uN[d] = o.uN[d];
         uP[d] = o.uP[d];
       }
-      if (ax == 0) { F::template flux<0>(o.fl, uN, uP, p); F::template flux_jac<0>(o.JN, o.JP, uN, uP, p); }
-      if constexpr (DIM > 1) if (ax == 1) { F::template flux<1>(o.fl, uN, uP, p); F::template flux_jac<1>(o.JN, o.JP, uN, uP, p); }
-      if constexpr (DIM > 2) if (ax == 2) { F::template flux<2>(o.fl, uN, uP, p); F::template flux_jac<2>(o.JN, o.JP, uN, uP, p); }
+      if (part == 0) {
+        if (ax == 0) F::template flux<0>(o.fl, uN, uP, p);
+        if constexpr (DIM > 1) if (ax == 1) F::template flux<1>(o.fl, uN, uP, p);
+        if constexpr (DIM > 2) if (ax == 2) F::template flux<2>(o.fl, uN, uP, p);
+      } else {
+        if (ax == 0) F::template flux_jac<0>(o.JN, o.JP, uN, uP, p);
+        if constexpr (DIM > 1) if (ax == 1) F::template flux_jac<1>(o.JN, o.JP, uN, uP, p);
+        if constexpr (DIM > 2) if (ax == 2) F::template flux_jac<2>(o.JN, o.JP, uN, uP, p);
+      }
     }
   }
   __syncthreads();
-  // phase 2: thread (row, k)
-  for (int w = tid; w < RPB * NDPC; w += blockDim.x) {
-    const int rl = w / NDPC, k = w % NDPC;
+  // phase 2: thread (row, k, j)
+  for (int w = tid; w < RPB * NDPC * NDPC; w += blockDim.x) {
+    const int rl = w / (NDPC * NDPC), k = (w / NDPC) % NDPC, j = w % NDPC;
     const int e = blockIdx.x * RPB + rl;
     if (e >= t.nrows) continue;
     const int r = t.rows[e];
-    double vk = 0.;
+    double acc[NB];
 #pragma unroll
-    for (int ax = 0; ax < DIM; ++ax) vk += m.hinv[ax] * (fd[rl][2 * ax].fl[k] - fd[rl][2 * ax + 1].fl[k]);
-    double acc[NB * NDPC];
-#pragma unroll
-    for (int i = 0; i < NB * NDPC; ++i) acc[i] = 0.;
+    for (int i = 0; i < NB; ++i) acc[i] = 0.;
 #pragma unroll 1
     for (int ax = 0; ax < DIM; ++ax) {
       const double hinv = m.hinv[ax];
@@ -507,59 +549,62 @@ k_rows_vj_inner_par(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U
 #pragma unroll
       for (int s = 0; s < S; ++s) blk[s] = t.jpos[base + s] / NDPC;
       const RF &L = fd[rl][2 * ax], &R = fd[rl][2 * ax + 1];
-#pragma unroll 1
-      for (int j = 0; j < NDPC; ++j) {
-        const double ln = L.JN[k * NDPC + j], lp = L.JP[k * NDPC + j];
-        const double rn = R.JN[k * NDPC + j], rp = R.JP[k * NDPC + j];
+      const double ln = L.JN[k * NDPC + j], lp = L.JP[k * NDPC + j];
+      const double rn = R.JN[k * NDPC + j], rp = R.JP[k * NDPC + j];
 #pragma unroll
-        for (int s = 0; s < G; ++s) {
-          acc[blk[s] * NDPC + j] += ln * L.gN[j][s] * hinv;
-          acc[blk[s] * NDPC + j] += lp * L.gP[j][s] * hinv;
-        }
-#pragma unroll
-        for (int s = 0; s < G; ++s) {
-          acc[blk[s + 1] * NDPC + j] -= rn * R.gN[j][s] * hinv;
-          acc[blk[s + 1] * NDPC + j] -= rp * R.gP[j][s] * hinv;
-        }
+      for (int s = 0; s < G; ++s) {
+        acc[blk[s]] += ln * L.gN[j][s] * hinv;
+        acc[blk[s]] += lp * L.gP[j][s] * hinv;
       }
+#pragma unroll
+      for (int s = 0; s < G; ++s) {
+        acc[blk[s + 1]] -= rn * R.gN[j][s] * hinv;
+        acc[blk[s + 1]] -= rp * R.gP[j][s] * hinv;
+      }
+    }
+    double vk = 0.;
+    if (j == 0) {
+#pragma unroll
+      for (int ax = 0; ax < DIM; ++ax) vk += m.hinv[ax] * (fd[rl][2 * ax].fl[k] - fd[rl][2 * ax + 1].fl[k]);
     }
     if constexpr (FAM == Swe2d) {
       // swe_2d_prob_class.hpp:983-1012
       const int c = t.cell[e];
       const double u0 = __ldg(U + (size_t)c * 3), u1 = __ldg(U + (size_t)c * 3 + 1),
                    u2 = __ldg(U + (size_t)c * 3 + 2);
-      if (k == 1) vk -= p.coriolis * u2 / u0;
-      if (k == 2) vk += p.coriolis * u1 / u0;
+      if (j == 0 && k == 1) vk -= p.coriolis * u2 / u0;
+      if (j == 0 && k == 2) vk += p.coriolis * u1 / u0;
       const int self = t.jpos[((size_t)e * DIM + 0) * S + H] / NDPC;
-      if (k == 1) {
-        acc[self * 3 + 0] += p.coriolis * u2 / (u0 * u0);
-        acc[self * 3 + 2] += -p.coriolis / u0;
-      }
-      if (k == 2) {
-        acc[self * 3 + 1] += p.coriolis / u0;
-        acc[self * 3 + 0] += -p.coriolis * u1 / (u0 * u0);
-      }
+      if (k == 1 && j == 0) acc[self] += p.coriolis * u2 / (u0 * u0);
+      if (k == 1 && j == 2) acc[self] += -p.coriolis / u0;
+      if (k == 2 && j == 1) acc[self] += p.coriolis / u0;
+      if (k == 2 && j == 0) acc[self] += -p.coriolis * u1 / (u0 * u0);
     }
-    V[(size_t)r * NDPC + k] = vk;
+    if (j == 0) V[(size_t)r * NDPC + k] = vk;
     const int rb = rowptr[r * NDPC + k];
-    const int n = rowptr[r * NDPC + k + 1] - rb;
-    for (int i = 0; i < n && i < NB * NDPC; ++i) J[rb + i] = acc[i];
+    const int nb = (rowptr[r * NDPC + k + 1] - rb) / NDPC;
+    for (int b = 0; b < nb && b < NB; ++b) J[rb + b * NDPC + j] = acc[b];
   }
 }
 
-// Near-boundary rows with the faces of each row in parallel (thread per face:
-// the scheme's flux for V and the first-order flux Jacobians for J), then
-// thread (row, k) accumulates row k exactly as k_rows_vj_nearbd does.
+// Near-boundary rows, split the same way: phase 1a one side of the scheme's
+// face value (ghost entries through their recipes), phase 1b the face flux
+// (part 0) or the first-order flux Jacobians of the face's two cells (part 1),
+// phase 2 thread (row, k, j) accumulates exactly as k_rows_vj_nearbd does.
 template <int FAM> struct NearFace {
   static constexpr int NDPC = Fam<FAM>::ndpc;
   double fl[NDPC];
   double JN[NDPC * NDPC], JP[NDPC * NDPC];
+  double uN[NDPC], uP[NDPC];
 };
 
 template <int FAM> struct NearPar {
-  static constexpr int NF = 2 * Fam<FAM>::dim;
-  static constexpr int RPB = 4;  // spread the few near-boundary rows over many SMs
-  static constexpr int THREADS = RPB * NF;
+  static constexpr int NF = 2 * Fam<FAM>::dim, NDPC = Fam<FAM>::ndpc;
+  static constexpr int RPB = 4;
+  static constexpr int SIDE = pad_warp(RPB * NF * NDPC);
+  static constexpr int PART = pad_warp(RPB * NF);
+  static constexpr int THREADS = 2 * SIDE;
+  static_assert(2 * PART <= THREADS, "phase 1b fits the block");
 };
 
 template <int FAM, int SCHEME>
@@ -567,46 +612,68 @@ __global__ void __launch_bounds__(NearPar<FAM>::THREADS)
 k_rows_vj_nearbd_par(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U, const int *__restrict__ rowptr,
                      double *__restrict__ V, double *__restrict__ J) {
   using F = Fam<FAM>;
+  using NP = NearPar<FAM>;
   constexpr int NDPC = F::ndpc, DIM = F::dim, H = SchemeTraits<SCHEME>::h, S = 2 * H + 1, G = 2 * H;
-  constexpr int NF = NearPar<FAM>::NF, RPB = NearPar<FAM>::RPB, NB = 1 + 2 * DIM;
+  constexpr int NF = NP::NF, RPB = NP::RPB, NB = 1 + 2 * DIM;
   __shared__ NearFace<FAM> fd[RPB][NF];
   const int tid = threadIdx.x;
-  {
-    const int rl = tid / NF, f = tid % NF, ax = f >> 1, side = f & 1;
+  {  // phase 1a
+    const int side = tid / NP::SIDE, slot = tid % NP::SIDE;
+    const int rl = slot / (NF * NDPC), f = (slot / NDPC) % NF, d = slot % NDPC, ax = f >> 1, fs = f & 1;
     const int e = blockIdx.x * RPB + rl;
-    if (e < t.nrows) {
-      NearFace<FAM> &o = fd[rl][f];
-      double q[G][NDPC];
+    if (slot < RPB * NF * NDPC && e < t.nrows) {
+      double q[G];
       const size_t base = ((size_t)e * DIM + ax) * S;
 #pragma unroll
-      for (int s = 0; s < G; ++s)
-        load_entry<NDPC>(q[s], U, t.src[base + side + s], t.flip[base + side + s], m.reflect[ax], m, t.gsx, t.gsy,
-                         base + side + s);
-      double uN[NDPC], uP[NDPC];
-      reconstruct_face<NDPC, SCHEME>(uN, uP, q);
-      double q1[2][NDPC];
-      const size_t b1 = ((size_t)e * DIM + ax) * 3;
-#pragma unroll
-      for (int s = 0; s < 2; ++s)
-        load_entry<NDPC>(q1[s], U, t.src1[b1 + side + s], t.flip1[b1 + side + s], m.reflect[ax], m, t.gsx1,
-                         t.gsy1, b1 + side + s);
-      if (ax == 0) { F::template flux<0>(o.fl, uN, uP, p); F::template flux_jac<0>(o.JN, o.JP, q1[0], q1[1], p); }
-      if constexpr (DIM > 1) if (ax == 1) { F::template flux<1>(o.fl, uN, uP, p); F::template flux_jac<1>(o.JN, o.JP, q1[0], q1[1], p); }
-      if constexpr (DIM > 2) if (ax == 2) { F::template flux<2>(o.fl, uN, uP, p); F::template flux_jac<2>(o.JN, o.JP, q1[0], q1[1], p); }
+      for (int s = 0; s < G; ++s) {
+        double qe[NDPC];
+        load_entry<NDPC>(qe, U, t.src[base + fs + s], t.flip[base + fs + s], m.reflect[ax], m, t.gsx, t.gsy,
+                         base + fs + s);
+        q[s] = qe[d];
+      }
+      (side == 0 ? fd[rl][f].uN : fd[rl][f].uP)[d] = face_value_side<SCHEME>(side, q);
     }
   }
   __syncthreads();
-  for (int w = tid; w < RPB * NDPC; w += blockDim.x) {
-    const int rl = w / NDPC, k = w % NDPC;
+  {  // phase 1b
+    const int part = tid / NP::PART, slot = tid % NP::PART;
+    const int rl = slot / NF, f = slot % NF, ax = f >> 1, fs = f & 1;
+    const int e = blockIdx.x * RPB + rl;
+    if (part < 2 && slot < RPB * NF && e < t.nrows) {
+      NearFace<FAM> &o = fd[rl][f];
+      if (part == 0) {
+        double uN[NDPC], uP[NDPC];
+#pragma unroll
+        for (int d = 0; d < NDPC; ++d) {
+          uN[d] = o.uN[d];
+          uP[d] = o.uP[d];
+        }
+        if (ax == 0) F::template flux<0>(o.fl, uN, uP, p);
+        if constexpr (DIM > 1) if (ax == 1) F::template flux<1>(o.fl, uN, uP, p);
+        if constexpr (DIM > 2) if (ax == 2) F::template flux<2>(o.fl, uN, uP, p);
+      } else {
+        double q1[2][NDPC];
+        const size_t b1 = ((size_t)e * DIM + ax) * 3;
+#pragma unroll
+        for (int s = 0; s < 2; ++s)
+          load_entry<NDPC>(q1[s], U, t.src1[b1 + fs + s], t.flip1[b1 + fs + s], m.reflect[ax], m, t.gsx1, t.gsy1,
+                           b1 + fs + s);
+        if (ax == 0) F::template flux_jac<0>(o.JN, o.JP, q1[0], q1[1], p);
+        if constexpr (DIM > 1) if (ax == 1) F::template flux_jac<1>(o.JN, o.JP, q1[0], q1[1], p);
+        if constexpr (DIM > 2) if (ax == 2) F::template flux_jac<2>(o.JN, o.JP, q1[0], q1[1], p);
+      }
+    }
+  }
+  __syncthreads();
+  // phase 2: thread (row, k, j)
+  for (int w = tid; w < RPB * NDPC * NDPC; w += blockDim.x) {
+    const int rl = w / (NDPC * NDPC), k = (w / NDPC) % NDPC, j = w % NDPC;
     const int e = blockIdx.x * RPB + rl;
     if (e >= t.nrows) continue;
     const int r = t.rows[e];
-    double vk = 0.;
+    double acc[NB];
 #pragma unroll
-    for (int ax = 0; ax < DIM; ++ax) vk += m.hinv[ax] * (fd[rl][2 * ax].fl[k] - fd[rl][2 * ax + 1].fl[k]);
-    double acc[NB * NDPC];
-#pragma unroll
-    for (int i = 0; i < NB * NDPC; ++i) acc[i] = 0.;
+    for (int i = 0; i < NB; ++i) acc[i] = 0.;
 #pragma unroll 1
     for (int ax = 0; ax < DIM; ++ax) {
       const double hinv = m.hinv[ax];
@@ -615,37 +682,35 @@ k_rows_vj_nearbd_par(RowTable t, MeshArgs m, Phys p, const double *__restrict__ 
       const int bl = pl / NDPC, bc = pc / NDPC, br = pr / NDPC;
       const double *fac = t.jfac + ((size_t)e * DIM + ax) * NDPC;
       const NearFace<FAM> &L = fd[rl][2 * ax], &R = fd[rl][2 * ax + 1];
-      // JLN = L.JN, JLP = L.JP, JRN = R.JN, JRP = R.JP
-      for (int j = 0; j < NDPC; ++j) acc[bc * NDPC + j] += (L.JP[k * NDPC + j] - R.JN[k * NDPC + j]) * hinv;
-      if (pl >= 0)
-        for (int j = 0; j < NDPC; ++j) acc[bl * NDPC + j] += L.JN[k * NDPC + j] * hinv;
-      if (pr >= 0)
-        for (int j = 0; j < NDPC; ++j) acc[br * NDPC + j] += -R.JP[k * NDPC + j] * hinv;
-      if (pl < 0)
-        for (int j = 0; j < NDPC; ++j) acc[bc * NDPC + j] += (fac[j] * L.JN[k * NDPC + j]) * hinv;
-      if (pr < 0)
-        for (int j = 0; j < NDPC; ++j) acc[bc * NDPC + j] += (fac[j] * -R.JP[k * NDPC + j]) * hinv;
+      const double ln = L.JN[k * NDPC + j], lp = L.JP[k * NDPC + j];
+      const double rn = R.JN[k * NDPC + j], rp = R.JP[k * NDPC + j];
+      acc[bc] += (lp - rn) * hinv;
+      if (pl >= 0) acc[bl] += ln * hinv;
+      if (pr >= 0) acc[br] += -rp * hinv;
+      if (pl < 0) acc[bc] += (fac[j] * ln) * hinv;
+      if (pr < 0) acc[bc] += (fac[j] * -rp) * hinv;
+    }
+    double vk = 0.;
+    if (j == 0) {
+#pragma unroll
+      for (int ax = 0; ax < DIM; ++ax) vk += m.hinv[ax] * (fd[rl][2 * ax].fl[k] - fd[rl][2 * ax + 1].fl[k]);
     }
     if constexpr (FAM == Swe2d) {
       const int c = t.cell[e];
       const double u0 = __ldg(U + (size_t)c * 3), u1 = __ldg(U + (size_t)c * 3 + 1),
                    u2 = __ldg(U + (size_t)c * 3 + 2);
-      if (k == 1) vk -= p.coriolis * u2 / u0;
-      if (k == 2) vk += p.coriolis * u1 / u0;
+      if (j == 0 && k == 1) vk -= p.coriolis * u2 / u0;
+      if (j == 0 && k == 2) vk += p.coriolis * u1 / u0;
       const int self = t.jpos1[((size_t)e * DIM + 0) * 3 + 1] / 3;
-      if (k == 1) {
-        acc[self * 3 + 0] += p.coriolis * u2 / (u0 * u0);
-        acc[self * 3 + 2] += -p.coriolis / u0;
-      }
-      if (k == 2) {
-        acc[self * 3 + 1] += p.coriolis / u0;
-        acc[self * 3 + 0] += -p.coriolis * u1 / (u0 * u0);
-      }
+      if (k == 1 && j == 0) acc[self] += p.coriolis * u2 / (u0 * u0);
+      if (k == 1 && j == 2) acc[self] += -p.coriolis / u0;
+      if (k == 2 && j == 1) acc[self] += p.coriolis / u0;
+      if (k == 2 && j == 0) acc[self] += -p.coriolis * u1 / (u0 * u0);
     }
-    V[(size_t)r * NDPC + k] = vk;
+    if (j == 0) V[(size_t)r * NDPC + k] = vk;
     const int rb = rowptr[r * NDPC + k];
-    const int n = rowptr[r * NDPC + k + 1] - rb;
-    for (int i = 0; i < n && i < NB * NDPC; ++i) J[rb + i] = acc[i];
+    const int nb = (rowptr[r * NDPC + k + 1] - rb) / NDPC;
+    for (int b = 0; b < nb && b < NB; ++b) J[rb + b * NDPC + j] = acc[b];
   }
 }
 

@@ -34,6 +34,13 @@ struct Launchers {
                     double *const T[3], const int *rowptr, double *V, double *J, cudaStream_t s,
                     int *launches);
   int (*jface_components)(int scheme);
+  // one fused LSPG Gauss-Newton iteration over the inner rows ti and the
+  // near-boundary rows tn (lspg_fused.cuh); grid = lspg_fused_blocks(...)
+  void (*lspg_fused)(int scheme, const RowTable &ti, const RowTable &tn, const MeshArgs &m, const Phys &p,
+                     const LspgArgs &a, cudaStream_t s);
+  int (*lspg_fused_blocks)(int scheme, int innerRows, int nearRows, int K);
+  // raise the fused kernels' dynamic shared-memory limit (once, before any capture)
+  void (*lspg_fused_prepare)();
 };
 
 const Launchers &launchers_euler1d();

@@ -56,14 +56,15 @@ PDA_HD double cube(double x) {
 // ---------------------------------------------------------------------------
 // WENO5, one face i+1/2: uNeg from q_{i-2..i+2}, uPos from q_{i-1..i+3}.
 // ---------------------------------------------------------------------------
-PDA_HD void weno5_face(double &uNeg, double &uPos, double qim2, double qim1,
-                       double qi, double qip1, double qip2, double qip3) {
+// one side of weno5_face: uNeg (left-biased, q_{i-2..i+2})
+PDA_HD double weno5_neg(double qim2, double qim1, double qi, double qip1, double qip2) {
   constexpr double epsilon = 1e-6;
   constexpr double two = 2., three = 3., four = 4., five = 5., seven = 7.,
                    eleven = 11.;
   constexpr double oneOvfour = 1. / 4., oneOvsix = 1. / 6.,
                    oneOvten = 1. / 10., threeOvten = 3. / 10.,
                    sixOvten = 6. / 10., thirteenOvtwelve = 13. / 12.;
+  double uNeg;
   {
     const double p0 = (two * qim2 - seven * qim1 + eleven * qi) * oneOvsix;
     const double p1 = (-qim1 + five * qi + two * qip1) * oneOvsix;
@@ -83,6 +84,18 @@ PDA_HD void weno5_face(double &uNeg, double &uPos, double qim2, double qim1,
     const double w2 = alpha2 * alphaSInv;
     uNeg = w0 * p0 + w1 * p1 + w2 * p2;
   }
+  return uNeg;
+}
+
+// one side of weno5_face: uPos (right-biased, q_{i-1..i+3})
+PDA_HD double weno5_pos(double qim1, double qi, double qip1, double qip2, double qip3) {
+  constexpr double epsilon = 1e-6;
+  constexpr double two = 2., three = 3., four = 4., five = 5., seven = 7.,
+                   eleven = 11.;
+  constexpr double oneOvfour = 1. / 4., oneOvsix = 1. / 6.,
+                   oneOvten = 1. / 10., threeOvten = 3. / 10.,
+                   sixOvten = 6. / 10., thirteenOvtwelve = 13. / 12.;
+  double uPos;
   {
     const double p0 = (-qim1 + five * qi + two * qip1) * oneOvsix;
     const double p1 = (two * qi + five * qip1 - qip2) * oneOvsix;
@@ -102,13 +115,19 @@ PDA_HD void weno5_face(double &uNeg, double &uPos, double qim2, double qim1,
     const double w2 = alpha2 * alphaSInv;
     uPos = w0 * p0 + w1 * p1 + w2 * p2;
   }
+  return uPos;
+}
+
+PDA_HD void weno5_face(double &uNeg, double &uPos, double qim2, double qim1,
+                       double qi, double qip1, double qip2, double qip3) {
+  uNeg = weno5_neg(qim2, qim1, qi, qip1, qip2);
+  uPos = weno5_pos(qim1, qi, qip1, qip2, qip3);
 }
 
 // WENO5 with the gradient of the two face values with respect to the six
 // stencil values q_{i-2..i+3}: gNeg[5] == 0, gPos[0] == 0.
-PDA_HD void weno5_face_grad(double &uNeg, double &uPos, double gNeg[6],
-                            double gPos[6], double qim2, double qim1, double qi,
-                            double qip1, double qip2, double qip3) {
+// one side of weno5_face_grad: uNeg and its gradient
+PDA_HD void weno5_neg_grad(double &uNeg, double gNeg[6], double qim2, double qim1, double qi, double qip1, double qip2, double qip3) {
   constexpr double epsilon = 1e-6;
   constexpr double two = 2., three = 3., four = 4., five = 5., seven = 7.,
                    eleven = 11.;
@@ -168,6 +187,16 @@ PDA_HD void weno5_face_grad(double &uNeg, double &uPos, double gNeg[6],
     gNeg[5] = 0.;
     uNeg = w0 * p0 + w1 * p1 + w2 * p2;
   }
+}
+
+// one side of weno5_face_grad: uPos and its gradient
+PDA_HD void weno5_pos_grad(double &uPos, double gPos[6], double qim2, double qim1, double qi, double qip1, double qip2, double qip3) {
+  constexpr double epsilon = 1e-6;
+  constexpr double two = 2., three = 3., four = 4., five = 5., seven = 7.,
+                   eleven = 11.;
+  constexpr double oneOvfour = 1. / 4., oneOvsix = 1. / 6.,
+                   oneOvten = 1. / 10., threeOvten = 3. / 10.,
+                   sixOvten = 6. / 10., thirteenOvtwelve = 13. / 12.;
   {
     const double p0 = (-qim1 + five * qi + two * qip1) * oneOvsix;
     const double p1 = (two * qi + five * qip1 - qip2) * oneOvsix;
@@ -223,14 +252,22 @@ PDA_HD void weno5_face_grad(double &uNeg, double &uPos, double gNeg[6],
   }
 }
 
+PDA_HD void weno5_face_grad(double &uNeg, double &uPos, double gNeg[6],
+                            double gPos[6], double qim2, double qim1, double qi,
+                            double qip1, double qip2, double qip3) {
+  weno5_neg_grad(uNeg, gNeg, qim2, qim1, qi, qip1, qip2, qip3);
+  weno5_pos_grad(uPos, gPos, qim2, qim1, qi, qip1, qip2, qip3);
+}
+
 // ---------------------------------------------------------------------------
 // WENO3, one face i+1/2: uNeg from q_{i-1..i+1}, uPos from q_{i..i+2}.
 // ---------------------------------------------------------------------------
-PDA_HD void weno3_face(double &uNeg, double &uPos, double qim1, double qi,
-                       double qip1, double qip2) {
+// one side of weno3_face: uNeg (q_{i-1..i+1})
+PDA_HD double weno3_neg(double qim1, double qi, double qip1) {
   constexpr double epsilon = 1.e-6;
   constexpr double two = 2., three = 3.;
   constexpr double oneOvtwo = 1. / 2., oneOvthree = 1. / 3., twoOvthree = 2. / 3.;
+  double uNeg;
   {
     const double p0 = (-qim1 + three * qi) * oneOvtwo;
     const double p1 = (qi + qip1) * oneOvtwo;
@@ -243,6 +280,15 @@ PDA_HD void weno3_face(double &uNeg, double &uPos, double qim1, double qi,
     const double w1 = alpha1 * alphaSInv;
     uNeg = w0 * p0 + w1 * p1;
   }
+  return uNeg;
+}
+
+// one side of weno3_face: uPos (q_{i..i+2})
+PDA_HD double weno3_pos(double qi, double qip1, double qip2) {
+  constexpr double epsilon = 1.e-6;
+  constexpr double two = 2., three = 3.;
+  constexpr double oneOvtwo = 1. / 2., oneOvthree = 1. / 3., twoOvthree = 2. / 3.;
+  double uPos;
   {
     const double p0 = (qi + qip1) * oneOvtwo;
     const double p1 = (three * qip1 - qip2) * oneOvtwo;
@@ -255,12 +301,18 @@ PDA_HD void weno3_face(double &uNeg, double &uPos, double qim1, double qi,
     const double w1 = alpha1 * alphaSInv;
     uPos = w0 * p0 + w1 * p1;
   }
+  return uPos;
+}
+
+PDA_HD void weno3_face(double &uNeg, double &uPos, double qim1, double qi,
+                       double qip1, double qip2) {
+  uNeg = weno3_neg(qim1, qi, qip1);
+  uPos = weno3_pos(qi, qip1, qip2);
 }
 
 // WENO3 with gradients with respect to q_{i-1..i+2}: gNeg[3] == 0, gPos[0] == 0.
-PDA_HD void weno3_face_grad(double &uNeg, double &uPos, double gNeg[4],
-                            double gPos[4], double qim1, double qi, double qip1,
-                            double qip2) {
+// one side of weno3_face_grad: uNeg and its gradient
+PDA_HD void weno3_neg_grad(double &uNeg, double gNeg[4], double qim1, double qi, double qip1, double qip2) {
   constexpr double epsilon = 1e-6;
   constexpr double two = 2., three = 3.;
   constexpr double oneOvtwo = 1. / 2., oneOvthree = 1. / 3., twoOvthree = 2. / 3.;
@@ -297,6 +349,13 @@ PDA_HD void weno3_face_grad(double &uNeg, double &uPos, double gNeg[4],
     gNeg[3] = 0.;
     uNeg = w0 * p0 + w1 * p1;
   }
+}
+
+// one side of weno3_face_grad: uPos and its gradient
+PDA_HD void weno3_pos_grad(double &uPos, double gPos[4], double qim1, double qi, double qip1, double qip2) {
+  constexpr double epsilon = 1e-6;
+  constexpr double two = 2., three = 3.;
+  constexpr double oneOvtwo = 1. / 2., oneOvthree = 1. / 3., twoOvthree = 2. / 3.;
   {
     const double p0 = (qi + qip1) * oneOvtwo;
     const double p1 = (three * qip1 - qip2) * oneOvtwo;
@@ -330,6 +389,13 @@ PDA_HD void weno3_face_grad(double &uNeg, double &uPos, double gNeg[4],
     gPos[0] = 0.;
     uPos = w0 * p0 + w1 * p1;
   }
+}
+
+PDA_HD void weno3_face_grad(double &uNeg, double &uPos, double gNeg[4],
+                            double gPos[4], double qim1, double qi, double qip1,
+                            double qip2) {
+  weno3_neg_grad(uNeg, gNeg, qim1, qi, qip1, qip2);
+  weno3_pos_grad(uPos, gPos, qim1, qi, qip1, qip2);
 }
 
 // ---------------------------------------------------------------------------

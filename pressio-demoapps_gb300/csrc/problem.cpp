@@ -1135,6 +1135,15 @@ void advance(pda_problem &P, int kind, double *U, double t0, double dt, int64_t 
 
 namespace pda {
 void ensure_device_pattern(pda_problem &P) { pattern_to_device(P); }
+void ensure_row_tables(pda_problem &P) {
+  check_evaluable(P);
+  build_inner_table(P, true);
+  build_near_table(P, true);
+  pattern_to_device(P);
+  P.innerT.sync();
+  P.nearT.sync();
+  sync_recipes(P);
+}
 }  // namespace pda
 
 // ===================================================================== C ABI

@@ -181,6 +181,10 @@ struct pda_problem {
 namespace pda {
 // build the CSR pattern of the problem and copy it to the device (once)
 void ensure_device_pattern(pda_problem &P);
+// inner and near-boundary row tables with their Jacobian parts, the CSR
+// pattern and the ghost recipes on the device (allocates; call before any
+// stream capture)
+void ensure_row_tables(pda_problem &P);
 }  // namespace pda
 
 // C ABI bodies: exceptions become a status code + the thread-local message

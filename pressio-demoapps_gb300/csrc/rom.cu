@@ -33,13 +33,7 @@ namespace rom {
 
 constexpr int KMAX = 32;        // latent dimension limit
 
-struct Flags {
-  int converged;   // correction below tolerance in this step
-  int iters;       // iterations taken in this step
-  double lastCorr;  // norm of the last correction
-  double lastRes;   // residual norm at the last iterate
-  double maxRes;    // max over steps of the residual norm at the step's last iterate
-};
+using Flags = LspgFlags;
 
 // ------------------------------------------------------------ trial spaces
 template <int K>
@@ -264,10 +258,10 @@ k_lspg_rows(int ndpc, long ns, const int *__restrict__ s2st, const double *__res
 #pragma unroll
         for (int u = 0; u < 4; ++u) dv[u] = __ldg(D + (long)ci[u] * K + c);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) jd += jv[u] * dv[u];
+        for (int u = 0; u < 4; ++u) jd = fma(jv[u], dv[u], jd);
       }
-      for (; q < q1; ++q) jd += J[q] * D[(long)colidx[q] * K + c];
-      val = cf * jd + 1. * D[st * K + c];
+      for (; q < q1; ++q) jd = fma(J[q], D[(long)colidx[q] * K + c], jd);
+      val = fma(cf, jd, D[st * K + c]);
     }
   }
   sJR[rl][c] = val;
@@ -291,7 +285,7 @@ k_lspg_rows(int ndpc, long ns, const int *__restrict__ s2st, const double *__res
       b = K;
     }
     double s = 0.;
-    for (int i = 0; i < RB; ++i) s += sJR[i][a] * sJR[i][b];
+    for (int i = 0; i < RB; ++i) s = fma(sJR[i][a], sJR[i][b], s);
     partial[(long)blockIdx.x * ne + e] = s;
   }
   // the last block to finish reduces the partial sums and solves (ticket
@@ -307,29 +301,52 @@ k_lspg_rows(int ndpc, long ns, const int *__restrict__ s2st, const double *__res
   if (t == 0) *ticket = 0u;
 }
 
-// reduce the partial sums in block order, factor, solve, update (the whole
-// calling block takes part; thread 0 factors)
+// Reduce the partial sums in block order, factor, solve, update.  GB300's
+// FP64 units give one warp one instruction per ~64 cycles, so the k x k solve
+// is arranged for a short dependency chain rather than few operations: a
+// right-looking Cholesky in one warp (per column one reciprocal square root,
+// the column scaled by it, the trailing triangle updated with the pairs spread
+// over the lanes), then forward and backward substitution with one lane per
+// unknown, multiplying by the stored reciprocal diagonal.  No division.
 template <int K>
 __device__ void lspg_solve_block(int nblocks, const double *__restrict__ partial, double *__restrict__ x, double tol,
                                  Flags *f) {
-  constexpr int k = K;
+  static_assert(K <= 32, "one lane per unknown");
   __shared__ double H[K][K];
   __shared__ double g[K];
-  __shared__ double red[K + 1];
+  __shared__ double rdiag[K];
   __shared__ double rr;
+  __shared__ unsigned char pi[K * (K + 1) / 2], pl[K * (K + 1) / 2];
   constexpr int ntri = K * (K + 1) / 2, ne = ntri + K + 1;
-  const int lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
-  for (int e = threadIdx.x >> 5; e < ne; e += nwarp) {
-    // lanes take blocks lane, lane + 32, ...; then a fixed shuffle tree
+  const int lane = threadIdx.x & 31;
+  // lower-triangle pairs (i, l), i >= l, ordered by l descending: the pairs
+  // with l > j are the first (K-1-j)(K-j)/2 entries
+  for (int q = threadIdx.x; q < ntri; q += blockDim.x) {
+    int l = K - 1, rem = q;
+    while (rem >= K - l) {
+      rem -= K - l;
+      --l;
+    }
+    pi[q] = (unsigned char)(l + rem);
+    pl[q] = (unsigned char)l;
+  }
+  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+    // one thread per entry, blocks in order, loads issued four at a time
     double s = 0.;
-    for (int b = lane; b < nblocks; b += 32) s += partial[(long)b * ne + e];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane != 0) continue;
+    int b = 0;
+    for (; b + 4 <= nblocks; b += 4) {
+      const double v0 = partial[(long)b * ne + e], v1 = partial[(long)(b + 1) * ne + e],
+                   v2 = partial[(long)(b + 2) * ne + e], v3 = partial[(long)(b + 3) * ne + e];
+      s += v0;
+      s += v1;
+      s += v2;
+      s += v3;
+    }
+    for (; b < nblocks; ++b) s += partial[(long)b * ne + e];
     if (e < ntri) {
       int a = 0, rem = e;
-      while (rem >= k - a) {
-        rem -= k - a;
+      while (rem >= K - a) {
+        rem -= K - a;
         ++a;
       }
       const int b2 = a + rem;
@@ -342,55 +359,52 @@ __device__ void lspg_solve_block(int nblocks, const double *__restrict__ partial
     }
   }
   __syncthreads();
-  __shared__ int ok;
-  if (threadIdx.x == 0) ok = 1;
-  __syncthreads();
   if (threadIdx.x < 32) {
-    // Cholesky H = L L^T in place (lower triangle), one column per step, the
-    // column's rows in parallel over the warp
-    const int lane = threadIdx.x;
-    for (int j = 0; j < k; ++j) {
-      if (lane == 0) {
-        double d = H[j][j];
-        for (int p = 0; p < j; ++p) d -= H[j][p] * H[j][p];
-        if (!(d > 0.)) ok = 0;
-        else H[j][j] = sqrt(d);
+    bool ok = true;
+    for (int j = 0; j < K; ++j) {
+      const double d = H[j][j];
+      if (!(d > 0.)) {
+        ok = false;
+        break;
       }
+      const double rs = rsqrt(d);
+      if (lane == 0) rdiag[j] = rs;
+      for (int i = j + 1 + lane; i < K; i += 32) H[i][j] *= rs;
       __syncwarp();
-      if (!ok) break;
-      for (int i = j + 1 + lane; i < k; i += 32) {
-        double s = H[i][j];
-        for (int p = 0; p < j; ++p) s -= H[i][p] * H[j][p];
-        H[i][j] = s / H[j][j];
+      const int np = (K - 1 - j) * (K - j) / 2;
+      for (int q = lane; q < np; q += 32) {
+        const int i = pi[q], l = pl[q];
+        H[i][l] = fma(-H[i][j], H[l][j], H[i][l]);
       }
       __syncwarp();
     }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
+    // L z = g (lane i holds unknown i), then L^T dx = z
+    double sv = lane < K ? g[lane] : 0.;
     double corr = 0.;
     if (ok) {
-      // L L^T dx = g
-      for (int i = 0; i < k; ++i) {
-        double s = g[i];
-        for (int p = 0; p < i; ++p) s -= H[i][p] * red[p];
-        red[i] = s / H[i][i];
+      for (int i = 0; i < K; ++i) {
+        const double zi = __shfl_sync(0xffffffffu, sv, i) * rdiag[i];
+        if (lane == i) sv = zi;
+        if (lane > i && lane < K) sv = fma(-H[lane][i], zi, sv);
       }
-      for (int i = k - 1; i >= 0; --i) {
-        double s = red[i];
-        for (int p = i + 1; p < k; ++p) s -= H[p][i] * red[p];
-        red[i] = s / H[i][i];
+      for (int i = K - 1; i >= 0; --i) {
+        const double di = __shfl_sync(0xffffffffu, sv, i) * rdiag[i];
+        if (lane == i) sv = di;
+        if (lane < i) sv = fma(-H[i][lane], di, sv);
       }
-      for (int i = 0; i < k; ++i) {
-        x[i] -= red[i];
-        corr += red[i] * red[i];
-      }
+      if (lane < K) x[lane] -= sv;
+      double c2 = lane < K ? sv * sv : 0.;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+      corr = c2;
     }
-    f->iters += 1;
-    f->lastCorr = sqrt(corr);
-    f->lastRes = sqrt(rr);
-    if (!(f->lastRes <= f->maxRes)) f->maxRes = f->lastRes;
-    if (!ok || sqrt(corr) < tol) f->converged = 1;
+    if (lane == 0) {
+      f->iters += 1;
+      f->lastCorr = sqrt(corr);
+      f->lastRes = sqrt(rr);
+      if (!(f->lastRes <= f->maxRes)) f->maxRes = f->lastRes;
+      if (!ok || sqrt(corr) < tol) f->converged = 1;
+    }
   }
 }
 
@@ -418,6 +432,10 @@ struct pda_lspg {
   pda::DevBuf<unsigned> ticket;
   int nblocks = 0;
   int64_t nnz = 0;
+  // fused iteration (lspg_fused.cuh) or the assembled Jacobian path
+  // (sample-mesh V + CSR J, then k_lspg_rows)
+  bool fused = true;
+  int fusedBlocks = 0;
   cudaGraphExec_t graph = nullptr;
   double graphDt = 0;
   double *graphX = nullptr;
@@ -466,6 +484,15 @@ template <int K>
 void gn_iteration_k(pda_lspg &L, double *x, double dt, double tol, int first, cudaStream_t s) {
   Flags *f = L.flags.p;
   decode_k<K>(L, x, L.y.p, s);
+  if (L.fused) {
+    pda_problem &P = *L.P;
+    LspgArgs a{L.y.p, L.D.p, K, -dt, L.yn.p, first, L.V.p, L.partial.p, L.ticket.p, x, tol, f};
+    MeshArgs ma = P.margs;
+    ma.time = 0.0;
+    P.L->lspg_fused(P.scheme, P.innerT.t, P.nearT.t, ma, P.phys, a, s);
+    PDA_CUDA(cudaGetLastError());
+    return;
+  }
   // sample-mesh velocity and Jacobian at y (the library's own kernels); they
   // run unconditionally, cheap next to the rest once converged
   const pda_status st = pda_velocity_and_jacobian(L.P, L.y.p, 0.0, L.V.p, L.J.p);
@@ -542,10 +569,15 @@ void common_setup(pda_lspg &L, pda_problem *P, const int64_t *s2st, int k) {
   L.J.alloc((size_t)std::max<int64_t>(nnz, 1));
   L.yn.alloc((size_t)L.ns);
   L.nblocks = div_up(L.ns, rows_per_block(k));
-  L.partial.alloc((size_t)L.nblocks * (k * (k + 1) / 2 + k + 1));
+  pda::ensure_row_tables(*P);
+  P->L->lspg_fused_prepare();
+  PDA_CUDA(cudaGetLastError());
+  L.fusedBlocks = P->L->lspg_fused_blocks(P->scheme, P->innerT.t.nrows, P->nearT.t.nrows, k);
+  L.partial.alloc((size_t)std::max(L.nblocks, L.fusedBlocks + lspg_groups(L.fusedBlocks)) *
+                  (k * (k + 1) / 2 + k + 1));
   L.flags.alloc(1);
-  L.ticket.alloc(1);
-  PDA_CUDA(cudaMemset(L.ticket.p, 0, sizeof(unsigned)));
+  L.ticket.alloc((size_t)(1 + lspg_groups(L.fusedBlocks)));
+  PDA_CUDA(cudaMemset(L.ticket.p, 0, L.ticket.n * sizeof(unsigned)));
   L.xn.alloc((size_t)k);
   PDA_CUDA(cudaMemset(L.flags.p, 0, sizeof(Flags)));
   PDA_CUDA(cudaMemset(L.y.p, 0, (size_t)L.nst * sizeof(double)));
@@ -658,6 +690,17 @@ pda_status pda_lspg_decode(pda_lspg *L, const double *d_x, double *d_y) {
   pda::rom::decode(*L, d_x, d_y, s);
   PDA_CUDA(cudaGetLastError());
   PDA_CUDA(cudaStreamSynchronize(s));
+  PDA_API_END
+}
+
+pda_status pda_lspg_set_fused(pda_lspg *rom, int fused) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(rom, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  if (rom->fused != (fused != 0) && rom->graph) {
+    cudaGraphExecDestroy(rom->graph);
+    rom->graph = nullptr;
+  }
+  rom->fused = fused != 0;
   PDA_API_END
 }
 

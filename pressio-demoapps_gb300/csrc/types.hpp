@@ -89,6 +89,35 @@ constexpr int kNumTileShapes = 4;
 constexpr TileShape kTileShapes[kNumTileShapes] = {{64, 2}, {32, 4}, {128, 1}, {64, 1}};
 constexpr int kFoFacesPerTile = 128;  // first order: faces per tile (one per thread)
 
+// Per-step Gauss-Newton state of an LSPG object (device).
+struct LspgFlags {
+  int converged;    // correction below tolerance in this step
+  int iters;        // iterations taken in this step
+  double lastCorr;  // norm of the last correction
+  double lastRes;   // residual norm at the last iterate
+  double maxRes;    // max over steps of the residual norm at the step's last iterate
+};
+
+// blocks per reduction group of the fused LSPG kernel's partial sums
+constexpr int kLspgGroup = 16;
+__host__ __device__ constexpr int lspg_groups(int nblocks) { return (nblocks + kLspgGroup - 1) / kLspgGroup; }
+
+// Arguments of the fused LSPG iteration kernel (lspg_fused.cuh).
+struct LspgArgs {
+  const double *y;   // trial state at the stencil dofs
+  const double *D;   // its latent Jacobian, [stencil dofs][K]
+  int K;             // latent dimension (<= 32)
+  double cf;         // -dt (BDF1)
+  double *yn;        // y_n at the sample dofs (stored on the step's first iteration)
+  int first;
+  double *V;         // sample-mesh velocity (written)
+  double *partial;   // [blocks + groups][K(K+1)/2 + K + 1] normal-equation partial sums
+  unsigned *ticket;  // [1 + groups] last-block counters (return to 0)
+  double *x;         // latent state, updated in place
+  double tol;
+  LspgFlags *f;
+};
+
 struct BatchArgs {
   const BatchItem *items;     // device array [nItems]
   int nItems;

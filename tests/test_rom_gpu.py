@@ -182,3 +182,45 @@ def test_lspg_mlp_tensor_core_decoder_close_to_fp32(pda, oracle):
     assert torch.allclose(xa, xb, rtol=2e-2, atol=1e-3), (xa, xb)
     with pytest.raises(pda.PdaError):  # non-bf16 weights are refused in tensor-core mode
         pda.LspgRom.mlp(ps, s2st, ur, sc, W1, b1, W2, b2, W3 + 1e-4, b3, tensor_cores=True)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("family,problem,scheme,ic,params", [
+    ("Swe2d", 0, 2, 1, {"gravity": 7.0, "coriolis": -2.0, "pulseMagnitude": 0.15}),
+    ("Euler2d", 4, 1, 2, None),
+    ("Euler2d", 3, 0, 1, None),
+    ("Euler2d", 7, 2, 1, None),
+])
+def test_lspg_fused_iteration_equals_assembled_jacobian(pda, family, problem, scheme, ic, params):
+    """The fused Gauss-Newton iteration (velocity and Jf D face by face, one
+    launch) and the assembled path (CSR Jf, then Jf D) are the same LSPG
+    iteration: latent trajectories agree to 1e-10 relative, on inner and
+    near-boundary rows (Neumann mirrors, Sedov symmetry planes, cross-shock
+    inflow states) of WENO5, WENO3 and first-order problems."""
+    import torch
+    n = 20
+    bounds = (-5, 5, -5, 5) if family == "Swe2d" else ((0, 1.2, 0, 1.2) if problem == 3 else (0, 2, 0, 1))
+    full = pda.create_full_mesh((n, n), bounds, 7)
+    rng = np.random.default_rng(11)
+    gids = np.sort(rng.choice(n * n, 90, replace=False))
+    sm, st = pda.create_sample_mesh(full, gids)
+    enum = getattr(pda, family)(problem)
+    ps = pda.create_problem(sm, enum, pda.InviscidFluxReconstruction(scheme), ic, params)
+    s2st = np.searchsorted(st, gids)
+    nd = ps.numDofPerCell()
+    nst = len(st) * nd
+    pf = pda.create_problem(full, enum, pda.InviscidFluxReconstruction(scheme), ic, params)
+    u0 = pf.initialCondition().cpu().numpy().reshape(-1, nd)[st].reshape(-1)
+    k = 6
+    phi, _ = np.linalg.qr(rng.normal(0, 1, (nst, k)))
+    phi *= 0.5 * np.abs(u0)[:, None]  # relative perturbations keep pressures positive
+    x0 = rng.normal(0, 0.05, k)
+    out = []
+    for fused in (True, False):
+        rom = pda.LspgRom.affine(ps, s2st, torch.from_numpy(u0).cuda(), torch.from_numpy(phi).cuda())
+        rom.set_fused(fused)
+        x = torch.from_numpy(x0.copy()).cuda()
+        rom.advance_bdf1(x, 0.002, 3, gn_iters=4, tol=0.0, use_graph=fused)
+        out.append(x.cpu().numpy())
+    assert np.all(np.isfinite(out[0]))
+    assert np.allclose(out[0], out[1], rtol=1e-10, atol=1e-12 * np.max(np.abs(out[1]))), out
