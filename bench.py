@@ -413,7 +413,7 @@ def _rom_module():
 
 
 def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int(os.environ.get("PDA_ROM_EPOCHS", 60)),
-               batch=128, lr=1e-3, dt=0.005, rom_ratio=4, gn_iters=3):
+               batch=128, lr=1e-3, dt=0.005, rom_ratio=4, gn_iters=2):
     """Learned-manifold hyper-reduced LSPG on 2D SWE slip wall 256^2: 48
     Latin-hypercube training points (gravity, coriolis, pulse), 400 FOM
     snapshots each (SSP-RK3 dt 0.005, batched device FOM), MLP autoencoder
@@ -456,14 +456,15 @@ def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int
     checkpoints = [100, 200, 300, 400]
     rom_cps = [cp // rom_ratio for cp in checkpoints]
 
-    def run_point(p, rom_kind):
+    def run_point(p, rom_kind, gn=gn_iters, ratio=rom_ratio):
         ps = setup.problem(p, mesh=sm)
         U0 = setup.problem(p).initialCondition()
         if rom_kind == "learned":
             rom, x0, dec = learned.lspg(ps, s2st, st, tensor_cores=True), learned.encode(U0), fdec
         else:
             rom, x0, dec = R.affine_lspg(setup, phi, ps, s2st, st), (phi.T @ (U0 - setup.uref)).contiguous(), faff
-        lat, wall, maxres = R.run_rom(rom, x0, dt * rom_ratio, rom_cps, setup.stream, gn_iters=gn_iters, tol=1e-8)
+        cps = [cp // ratio for cp in checkpoints]
+        lat, wall, maxres = R.run_rom(rom, x0, dt * ratio, cps, setup.stream, gn_iters=gn, tol=1e-8)
         return lat, wall, maxres, dec
 
     # residual threshold for the FOM fallback: 5x the largest residual seen on a training point
@@ -474,6 +475,11 @@ def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int
     for p in test:
         states, fom_wall = setup.fom_trajectory(p, dt, checkpoints)
         rec = {"params": p, "fom_s": fom_wall}
+        # best the trial manifold can do: decoder(encoder(FOM state)), and the POD projection
+        rec["learned_projection_rel_l2"] = [R.rel_l2(fdec.decode(learned.encode(states[cp])), states[cp])
+                                            for cp in checkpoints]
+        rec["pod_projection_rel_l2"] = [R.rel_l2(setup.uref + phi @ (phi.T @ (states[cp] - setup.uref)), states[cp])
+                                        for cp in checkpoints]
         for kind in ("learned", "pod"):
             lat, wall, maxres, dec = run_point(p, kind)
             errs = [R.rel_l2(dec.decode(lat[cp // rom_ratio]), states[cp]) for cp in checkpoints]
@@ -497,7 +503,25 @@ def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int
         "pod_rel_l2_perturbation_final_mean": float(np.mean([q["rel_l2_perturbation"][-1] for q in P])),
         "pod_speedup": float(np.sum(fom) / np.sum([q["rom_s"] for q in P])),
         "fallbacks": int(sum(q["fallback"] for q in L)),
+        "learned_projection_rel_l2_final_mean": float(np.mean([q["learned_projection_rel_l2"][-1] for q in pts])),
+        "pod_projection_rel_l2_final_mean": float(np.mean([q["pod_projection_rel_l2"][-1] for q in pts])),
     }
+    # further (Gauss-Newton iterations : ROM step / FOM step) settings of the
+    # same trained network, e.g. PDA_ROM_VARIANTS="2:4,3:8"
+    variants = [v for v in os.environ.get("PDA_ROM_VARIANTS", "").split(",") if v]
+    if variants:
+        out["variants"] = {}
+        states_by_point = [setup.fom_trajectory(p, dt, checkpoints) for p in test]
+        for v in variants:
+            gn, ratio = (int(u) for u in v.split(":"))
+            walls, fwalls, errs = [], [], []
+            for p, (states, fw) in zip(test, states_by_point):
+                lat, wall, _, dec = run_point(p, "learned", gn, ratio)
+                walls.append(wall)
+                fwalls.append(fw)
+                errs.append(max(R.rel_l2(dec.decode(lat[cp // ratio]), states[cp]) for cp in checkpoints))
+            out["variants"][v] = {"gn_iters": gn, "dt_rom": dt * ratio, "speedup": float(sum(fwalls) / sum(walls)),
+                                  "rel_l2_state_max": float(max(errs)), "rel_l2_state_mean_of_max": float(np.mean(errs))}
     if c.orc is not None:
         # the FOM on the host cores (oracle), one point, a bounded number of steps
         import tempfile
