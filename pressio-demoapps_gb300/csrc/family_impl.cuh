@@ -16,19 +16,25 @@ namespace {
 constexpr int FAM = PDA_FAM;
 using F = Fam<FAM>;
 
+int device_sms();
+
 template <int SCHEME>
-void rows_velocity_s(const RowTable &t, const MeshArgs &m, const Phys &p, const double *U, double *V,
-                     cudaStream_t s) {
-  if (t.nrows <= 0) return;
-  k_rows_velocity<FAM, SCHEME><<<div_up(t.nrows, 128), 128, 0, s>>>(t, m, p, U, V);
+void rows_velocity_s(const RowTable &ta, const RowTable &tb, const MeshArgs &m, const Phys &p, const double *U,
+                     double *V, cudaStream_t s) {
+  const int rows = ta.nrows + tb.nrows;
+  if (rows <= 0) return;
+  // rows per block: the fewest blocks that still cover every SM once
+  const int rpb = std::max(1, std::min(VelPar<FAM>::RPB_MAX, div_up(rows, device_sms())));
+  const int nbA = div_up(ta.nrows, rpb), nb = nbA + div_up(tb.nrows, rpb);
+  k_rows_velocity_par<FAM, SCHEME><<<nb, VelPar<FAM>::THREADS, 0, s>>>(ta, tb, nbA, rpb, m, p, U, V);
 }
 
-void rows_velocity(int scheme, const RowTable &t, const MeshArgs &m, const Phys &p, const double *U,
-                   double *V, cudaStream_t s) {
+void rows_velocity(int scheme, const RowTable &ta, const RowTable &tb, const MeshArgs &m, const Phys &p,
+                   const double *U, double *V, cudaStream_t s) {
   switch (scheme) {
-    case FirstOrder: rows_velocity_s<FirstOrder>(t, m, p, U, V, s); break;
-    case Weno3: rows_velocity_s<Weno3>(t, m, p, U, V, s); break;
-    default: rows_velocity_s<Weno5>(t, m, p, U, V, s); break;
+    case FirstOrder: rows_velocity_s<FirstOrder>(ta, tb, m, p, U, V, s); break;
+    case Weno3: rows_velocity_s<Weno3>(ta, tb, m, p, U, V, s); break;
+    default: rows_velocity_s<Weno5>(ta, tb, m, p, U, V, s); break;
   }
 }
 

@@ -714,6 +714,93 @@ k_rows_vj_nearbd_par(RowTable t, MeshArgs m, Phys p, const double *__restrict__ 
   }
 }
 
+// V of one or two row sets with each row's work spread over threads (the
+// velocity-only counterpart of k_rows_vj_nearbd_par): thread (side, row, face, dof) one
+// side of the face value (ghost entries through their recipes), thread (row,
+// face) the face flux, thread (row, k) dof k of V in the order of
+// k_rows_velocity.  Bit-identical to k_rows_velocity.  Rows per block (rpb <=
+// RPB_MAX) are chosen at launch so that small row sets spread over the SMs.
+template <int FAM> struct VelPar {
+  static constexpr int NF = 2 * Fam<FAM>::dim, NDPC = Fam<FAM>::ndpc;
+  static constexpr int RPB_MAX = Fam<FAM>::dim == 3 ? 4 : 8;
+  static constexpr int SIDE = pad_warp(RPB_MAX * NF * NDPC);
+  static constexpr int THREADS = 2 * SIDE;
+};
+
+template <int FAM> struct VelFace {
+  static constexpr int NDPC = Fam<FAM>::ndpc;
+  double fl[NDPC];
+  double uN[NDPC], uP[NDPC];
+};
+
+template <int FAM, int SCHEME>
+__global__ void __launch_bounds__(VelPar<FAM>::THREADS)
+k_rows_velocity_par(RowTable ta, RowTable tb, int nbA, int rpb, MeshArgs m, Phys p, const double *__restrict__ U,
+                    double *__restrict__ V) {
+  using F = Fam<FAM>;
+  using VP = VelPar<FAM>;
+  constexpr int NDPC = F::ndpc, DIM = F::dim, H = SchemeTraits<SCHEME>::h, S = 2 * H + 1, G = 2 * H;
+  constexpr int NF = VP::NF;
+  __shared__ VelFace<FAM> fd[VP::RPB_MAX][NF];
+  // blocks [0, nbA) take the rows of table ta, the others those of tb
+  const bool first = (int)blockIdx.x < nbA;
+  const RowTable &t = first ? ta : tb;
+  const int tid = threadIdx.x, e0 = (first ? (int)blockIdx.x : (int)blockIdx.x - nbA) * rpb;
+  {  // one side of one dof's face value
+    const int side = tid / VP::SIDE, slot = tid % VP::SIDE;
+    const int rl = slot / (NF * NDPC), f = (slot / NDPC) % NF, d = slot % NDPC, ax = f >> 1, fs = f & 1;
+    const int e = e0 + rl;
+    if (slot < rpb * NF * NDPC && e < t.nrows) {
+      const size_t base = ((size_t)e * DIM + ax) * S;
+      double q[G];
+#pragma unroll
+      for (int s = 0; s < G; ++s) {
+        double qe[NDPC];
+        load_entry<NDPC>(qe, U, t.src[base + fs + s], t.flip[base + fs + s], m.reflect[ax], m, t.gsx, t.gsy,
+                         base + fs + s);
+        q[s] = qe[d];
+      }
+      (side == 0 ? fd[rl][f].uN : fd[rl][f].uP)[d] = face_value_side<SCHEME>(side, q);
+    }
+  }
+  __syncthreads();
+  if (tid < rpb * NF) {  // the face flux
+    const int rl = tid / NF, f = tid % NF, ax = f >> 1;
+    const int e = e0 + rl;
+    if (e < t.nrows) {
+      VelFace<FAM> &o = fd[rl][f];
+      double uN[NDPC], uP[NDPC];
+#pragma unroll
+      for (int d = 0; d < NDPC; ++d) {
+        uN[d] = o.uN[d];
+        uP[d] = o.uP[d];
+      }
+      if (ax == 0) F::template flux<0>(o.fl, uN, uP, p);
+      if constexpr (DIM > 1) if (ax == 1) F::template flux<1>(o.fl, uN, uP, p);
+      if constexpr (DIM > 2) if (ax == 2) F::template flux<2>(o.fl, uN, uP, p);
+    }
+  }
+  __syncthreads();
+  if (tid < rpb * NDPC) {  // dof k of the row's velocity
+    const int rl = tid / NDPC, k = tid % NDPC;
+    const int e = e0 + rl;
+    if (e < t.nrows) {
+      double vk = 0.;
+#pragma unroll
+      for (int ax = 0; ax < DIM; ++ax) vk += m.hinv[ax] * (fd[rl][2 * ax].fl[k] - fd[rl][2 * ax + 1].fl[k]);
+      if constexpr (FAM == Swe2d) {
+        // swe_2d_prob_class.hpp:983-994
+        const int c = t.cell[e];
+        const double u0 = __ldg(U + (size_t)c * 3), u1 = __ldg(U + (size_t)c * 3 + 1),
+                     u2 = __ldg(U + (size_t)c * 3 + 2);
+        if (k == 1) vk -= p.coriolis * u2 / u0;
+        if (k == 2) vk += p.coriolis * u1 / u0;
+      }
+      V[(size_t)t.rows[e] * NDPC + k] = vk;
+    }
+  }
+}
+
 // V and J for rows near a non-periodic boundary: V with the scheme's stencil
 // (ghosts folded into the table), J first order with the ghost dependence
 // folded into the diagonal block by the BC factors

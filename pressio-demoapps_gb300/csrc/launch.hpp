@@ -8,8 +8,8 @@
 namespace pda {
 
 struct Launchers {
-  // reference per-row velocity over a row table
-  void (*rows_velocity)(int scheme, const RowTable &t, const MeshArgs &m, const Phys &p,
+  // velocity of the rows of one or two row tables (tb may be empty), one launch
+  void (*rows_velocity)(int scheme, const RowTable &ta, const RowTable &tb, const MeshArgs &m, const Phys &p,
                         const double *U, double *V, cudaStream_t s);
   // structured interior: faces once per axis into F[axis], then balance into V
   // ev (may be null): dim+2 events recorded before the first face launch,

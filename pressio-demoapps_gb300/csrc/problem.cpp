@@ -706,20 +706,20 @@ void velocity(pda_problem &P, const double *U, double *V, double t, cudaEvent_t 
     int nl = 0;
     P.L->struct_velocity(P.scheme, b, ma, P.phys, U, Fb, V, P.stream, &nl, ev);
     check_launch(P, nl);
-  } else {
+  }
+  // the row tables in one launch: inner rows (when no structured box covers
+  // them) and near-boundary rows
+  RowTable none{};
+  if (!P.useStruct) {
     build_inner_table(P, false);
     P.innerT.sync();
-    if (P.innerT.t.nrows > 0) {
-      P.L->rows_velocity(P.scheme, P.innerT.t, ma, P.phys, U, V, P.stream);
-      check_launch(P);
-    }
   }
-  if (!P.structAll) {
-    P.nearT.sync();
-    if (P.nearT.t.nrows > 0) {
-      P.L->rows_velocity(P.scheme, P.nearT.t, ma, P.phys, U, V, P.stream);
-      check_launch(P);
-    }
+  if (!P.structAll) P.nearT.sync();
+  const RowTable &ta = P.useStruct ? none : P.innerT.t;
+  const RowTable &tb = P.structAll ? none : P.nearT.t;
+  if (ta.nrows + tb.nrows > 0) {
+    P.L->rows_velocity(P.scheme, ta, tb, ma, P.phys, U, V, P.stream);
+    check_launch(P);
   }
   if (ev) cudaEventRecord(ev[P.dim + 2], P.stream);
 }
@@ -1355,7 +1355,8 @@ pda_status pda_velocity_noalloc(pda_problem *p, const double *dU, double t, doub
   P.L->struct_velocity(P.scheme, P.box, ma, P.phys, dU, Fb, dV, P.stream, &nl, nullptr);
   pda::check_launch(P, nl);
   if (!P.structAll && P.nearT.t.nrows > 0) {
-    P.L->rows_velocity(P.scheme, P.nearT.t, ma, P.phys, dU, dV, P.stream);
+    pda::RowTable none{};
+    P.L->rows_velocity(P.scheme, none, P.nearT.t, ma, P.phys, dU, dV, P.stream);
     pda::check_launch(P);
   }
   PDA_API_END
