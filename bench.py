@@ -579,6 +579,9 @@ def wl_lspg_step(c, n=256, latent=12, steps=20, gn_iters=3):
     return out
 
 
+# workloads whose work is split over the ranks (every rank must run them)
+SHARDED = {"batched_swe"}
+
 WORKLOADS = {"jacobian_2d": wl_jacobian_2d, "velocity_3d": wl_velocity_3d, "jacobian_3d": wl_jacobian_3d,
              "sod_1d_ssprk3": wl_sod_1d_ssprk3, "ssprk3_3d": wl_ssprk3_3d, "batched_swe": wl_batched_swe,
              "rom_swe": wl_rom_swe, "lspg_step": wl_lspg_step}
@@ -588,7 +591,7 @@ def extra_workloads(pda, torch, stream, cpu=True, names=None):
     """Secondary configurations, one JSON object each (default: all)."""
     c = _Ctx(pda, torch, stream, cpu)
     out = {}
-    for name in names or list(WORKLOADS):
+    for name in (list(WORKLOADS) if names is None else names):
         out[name] = WORKLOADS[name](c)
         torch.cuda.empty_cache()
     return out
@@ -812,10 +815,17 @@ def main():
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pda, mesh, Uh, budget_s=args.cpu_budget)
-    if rank == 0 and not args.no_extra:
+    if not args.no_extra:
         del U, V, flush
         torch.cuda.empty_cache()
-        line["workloads"] = extra_workloads(pda, torch, stream, cpu=not args.no_cpu_baseline)
+        # workloads that shard over the ranks run on every rank, first; the
+        # others on rank 0 alone (the other ranks are done)
+        res = extra_workloads(pda, torch, stream, cpu=not args.no_cpu_baseline and rank == 0,
+                              names=[n for n in WORKLOADS if n in SHARDED])
+        if rank == 0:
+            res.update(extra_workloads(pda, torch, stream, cpu=not args.no_cpu_baseline,
+                                       names=[n for n in WORKLOADS if n not in SHARDED]))
+            line["workloads"] = res
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
