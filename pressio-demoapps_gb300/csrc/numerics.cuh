@@ -53,6 +53,18 @@ PDA_HD double cube(double x) {
   return c + (ce + e * x);
 }
 
+// x / d for a constant d with its reciprocal r = RN(1/d), correctly rounded
+// (Markstein's correction step, P. Markstein, IBM J. Res. Dev. 34(1), 1990:
+// with r within half an ulp of 1/d and q0 = RN(x r) within one ulp of x/d, the
+// remainder x - q0 d is exact in one FMA and RN(q0 + r (x - q0 d)) is the
+// correctly rounded quotient).  Three FP64 instructions instead of a full
+// division; equal to the division for results in the normal range.
+PDA_HD double div_const(double x, double d, double r) {
+  const double q0 = x * r;
+  const double e = fma(-q0, d, x);
+  return fma(e, r, q0);
+}
+
 // ---------------------------------------------------------------------------
 // WENO5, one face i+1/2: uNeg from q_{i-2..i+2}, uPos from q_{i-1..i+3}.
 // ---------------------------------------------------------------------------
@@ -148,21 +160,21 @@ PDA_HD void weno5_neg_grad(double &uNeg, double gNeg[6], double qim2, double qim
     const double B2 = thirteenOvtwelve * sq(qi - two * qip1 + qip2) +
                       oneOvfour * sq(three * qi - four * qip1 + qip2);
     double dB0[5], dB1[5], dB2[5];
-    dB0[0] = (13. * (qim2 - 2. * qim1 + qi)) / 6. + (qim2 - 4. * qim1 + 3. * qi) / 2.;
-    dB0[1] = -(13. * (qim2 - 2. * qim1 + qi)) / 3. - 2. * (qim2 - 4. * qim1 + 3. * qi);
-    dB0[2] = (13. * (qim2 - 2. * qim1 + qi)) / 6. + (3. * (qim2 - 4. * qim1 + 3. * qi)) / 2.;
+    dB0[0] = div_const(13. * (qim2 - 2. * qim1 + qi), 6., 1. / 6.) + (qim2 - 4. * qim1 + 3. * qi) / 2.;
+    dB0[1] = div_const(-(13. * (qim2 - 2. * qim1 + qi)), 3., 1. / 3.) - 2. * (qim2 - 4. * qim1 + 3. * qi);
+    dB0[2] = div_const(13. * (qim2 - 2. * qim1 + qi), 6., 1. / 6.) + (3. * (qim2 - 4. * qim1 + 3. * qi)) / 2.;
     dB0[3] = 0.;
     dB0[4] = 0.;
     dB1[0] = 0.;
-    dB1[1] = (13. * (qip1 + qim1 - 2. * qi)) / 6. + (qim1 - qip1) / 2.;
-    dB1[2] = -(13. * (qip1 + qim1 - 2. * qi)) / 3.;
-    dB1[3] = (13. * (qip1 + qim1 - 2. * qi)) / 6. - (qim1 - qip1) / 2.;
+    dB1[1] = div_const(13. * (qip1 + qim1 - 2. * qi), 6., 1. / 6.) + (qim1 - qip1) / 2.;
+    dB1[2] = div_const(-(13. * (qip1 + qim1 - 2. * qi)), 3., 1. / 3.);
+    dB1[3] = div_const(13. * (qip1 + qim1 - 2. * qi), 6., 1. / 6.) - (qim1 - qip1) / 2.;
     dB1[4] = 0.;
     dB2[0] = 0.;
     dB2[1] = 0.;
-    dB2[2] = (13. * (qip2 - 2. * qip1 + qi)) / 6. + (3. * (qip2 - 4. * qip1 + 3. * qi)) / 2.;
-    dB2[3] = -(13. * (qip2 - 2. * qip1 + qi)) / 3. - 2. * (qip2 - 4. * qip1 + 3. * qi);
-    dB2[4] = (13. * (qip2 - 2. * qip1 + qi)) / 6. + (qip2 - 4. * qip1 + 3. * qi) / 2.;
+    dB2[2] = div_const(13. * (qip2 - 2. * qip1 + qi), 6., 1. / 6.) + (3. * (qip2 - 4. * qip1 + 3. * qi)) / 2.;
+    dB2[3] = div_const(-(13. * (qip2 - 2. * qip1 + qi)), 3., 1. / 3.) - 2. * (qip2 - 4. * qip1 + 3. * qi);
+    dB2[4] = div_const(13. * (qip2 - 2. * qip1 + qi), 6., 1. / 6.) + (qip2 - 4. * qip1 + 3. * qi) / 2.;
     const double alpha0 = oneOvten / sq(epsilon + B0);
     const double alpha1 = sixOvten / sq(epsilon + B1);
     const double alpha2 = threeOvten / sq(epsilon + B2);
@@ -211,21 +223,21 @@ PDA_HD void weno5_pos_grad(double &uPos, double gPos[6], double qim2, double qim
     const double B2 = thirteenOvtwelve * sq(qip1 - two * qip2 + qip3) +
                       oneOvfour * sq(three * qip1 - four * qip2 + qip3);
     double dB0[5], dB1[5], dB2[5];
-    dB0[0] = (3. * qip1 + qim1 - 4. * qi) / 2. + (13. * (qip1 + qim1 - 2. * qi)) / 6.;
-    dB0[1] = -2. * (3. * qip1 + qim1 - 4. * qi) - (13. * (qip1 + qim1 - 2 * qi)) / 3.;
-    dB0[2] = (3. * (3. * qip1 + qim1 - 4. * qi)) / 2. + (13. * (qip1 + qim1 - 2. * qi)) / 6.;
+    dB0[0] = (3. * qip1 + qim1 - 4. * qi) / 2. + div_const(13. * (qip1 + qim1 - 2. * qi), 6., 1. / 6.);
+    dB0[1] = -2. * (3. * qip1 + qim1 - 4. * qi) - div_const(13. * (qip1 + qim1 - 2 * qi), 3., 1. / 3.);
+    dB0[2] = (3. * (3. * qip1 + qim1 - 4. * qi)) / 2. + div_const(13. * (qip1 + qim1 - 2. * qi), 6., 1. / 6.);
     dB0[3] = 0.;
     dB0[4] = 0.;
     dB1[0] = 0.;
-    dB1[1] = (13. * (qip2 - 2 * qip1 + qi)) / 6. + (qi - qip2) / 2.;
-    dB1[2] = -(13. * (qip2 - 2. * qip1 + qi)) / 3.;
-    dB1[3] = (13. * (qip2 - 2. * qip1 + qi)) / 6. - (qi - qip2) / 2.;
+    dB1[1] = div_const(13. * (qip2 - 2 * qip1 + qi), 6., 1. / 6.) + (qi - qip2) / 2.;
+    dB1[2] = div_const(-(13. * (qip2 - 2. * qip1 + qi)), 3., 1. / 3.);
+    dB1[3] = div_const(13. * (qip2 - 2. * qip1 + qi), 6., 1. / 6.) - (qi - qip2) / 2.;
     dB1[4] = 0.;
     dB2[0] = 0.;
     dB2[1] = 0.;
-    dB2[2] = (13. * (qip3 - 2. * qip2 + qip1)) / 6. + (3. * (qip3 - 4. * qip2 + 3. * qip1)) / 2.;
-    dB2[3] = -(13. * (qip3 - 2. * qip2 + qip1)) / 3. - 2. * (qip3 - 4. * qip2 + 3. * qip1);
-    dB2[4] = (13. * (qip3 - 2. * qip2 + qip1)) / 6. + (qip3 - 4. * qip2 + 3. * qip1) / 2.;
+    dB2[2] = div_const(13. * (qip3 - 2. * qip2 + qip1), 6., 1. / 6.) + (3. * (qip3 - 4. * qip2 + 3. * qip1)) / 2.;
+    dB2[3] = div_const(-(13. * (qip3 - 2. * qip2 + qip1)), 3., 1. / 3.) - 2. * (qip3 - 4. * qip2 + 3. * qip1);
+    dB2[4] = div_const(13. * (qip3 - 2. * qip2 + qip1), 6., 1. / 6.) + (qip3 - 4. * qip2 + 3. * qip1) / 2.;
     const double alpha0 = threeOvten / sq(epsilon + B0);
     const double alpha1 = sixOvten / sq(epsilon + B1);
     const double alpha2 = oneOvten / sq(epsilon + B2);
