@@ -208,6 +208,30 @@ def test_host_buffer_entry_points(pda):
     assert ok
 
 
+@pytest.mark.parametrize("shape,family,problem,scheme,ic,per", [
+    ((515, 203), "Euler2d", 4, 2, 2, False),   # Neumann mirror, uneven sides
+    ((96, 96), "Swe2d", 0, 1, 1, False),       # slip wall, WENO3
+    ((40, 36, 50), "Euler3d", 0, 2, 1, True),  # periodic
+])
+def test_host_buffer_velocity_equals_device_full_meshes(pda, shape, family, problem, scheme, ic, per):
+    """The host-buffer velocity (the C-ABI call with host vectors) on full
+    structured meshes equals the device path bit for bit, call after call."""
+    torch = _torch()
+    dim = len(shape)
+    bounds = (-1.0, 1.0) * dim if dim == 3 else (0.0, 1.0, 0.0, 1.0)
+    mesh = pda.create_full_mesh(shape, bounds, 7, (per,) * dim)
+    p = pda.create_problem(mesh, getattr(pda, family)(problem), pda.InviscidFluxReconstruction(scheme), ic)
+    U = p.initialCondition()
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    U += (torch.rand(U.shape, generator=gen, device="cuda", dtype=torch.float64) * 2 - 1) * 1e-3
+    V = p.createVelocity()
+    p.velocity(U, 0.0, V)
+    Vh = np.empty(p.totalDofSampleMesh())
+    for _ in range(2):
+        p.velocity_host(np.ascontiguousarray(U.cpu().numpy()), 0.0, Vh)
+        assert np.array_equal(Vh, V.cpu().numpy())
+
+
 # ------------------------------------------------------- full-size properties
 
 def _riemann_full(pda, n, scheme=2, noise_seed=None):
