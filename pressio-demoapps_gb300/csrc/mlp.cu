@@ -76,6 +76,26 @@ cudaError_t tc_gemm_splitk(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long 
   return cudaGetLastError();
 }
 
+cudaError_t tc_gemm_partials(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K, int splits,
+                             float *partial, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(tc::k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  int *err = nullptr;
+  cudaError_t e = cudaGetSymbolAddress((void **)&err, g_tc_err);
+  if (e != cudaSuccess) return e;
+  const int kt = (int)(K / tc::BK);
+  splits = std::max(1, std::min(splits, kt));
+  const int per = (kt + splits - 1) / splits;
+  dim3 grid((unsigned)((N + tc::BN - 1) / tc::BN), (unsigned)((M + tc::BM - 1) / tc::BM), (unsigned)splits);
+  tc::k_gemm_tn<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(A, B, M, N, K, nullptr, tc::EPI_NONE, nullptr, nullptr,
+                                                          nullptr, err, per, partial);
+  return cudaGetLastError();
+}
+
 // 1 if any tensor-core GEMM gave up waiting since the last call; clears it
 int tc_gemm_error_and_clear() {
   int h = 0;

@@ -144,15 +144,26 @@ k_decode_hidden(int h2, const float *__restrict__ W1, const float *__restrict__ 
 }
 
 // tensor-core output layer: C [nst x 16] = W3b [nst x h2] Zb^T (fp32);
-// y = uref + scale (C[., 0] + b3), D = scale C[., 1..k]
+// y = uref + scale (C[., 0] + b3), D = scale C[., 1..k], from split-K partial
+// sums Cp[split][nst][16] added in split order (the output layer is short and
+// wide: K split over the SMs hides the latency of streaming the weights)
+constexpr int kDecodeSplits = 4;
+
 template <int K>
-__global__ void k_decode_finish(long nst, const float *__restrict__ C, const float *__restrict__ b3,
-                                const double *__restrict__ uref, const double *__restrict__ scale,
-                                double *__restrict__ y, double *__restrict__ D, const Flags *f) {
+__global__ void k_decode_finish_split(long nst, int splits, const float *__restrict__ Cp, const float *__restrict__ b3,
+                                      const double *__restrict__ uref, const double *__restrict__ scale,
+                                      double *__restrict__ y, double *__restrict__ D, const Flags *f) {
   if (f->converged) return;
   const long row = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= nst) return;
-  const float *c = C + row * 16;
+  float c[K + 1];
+#pragma unroll
+  for (int j = 0; j <= K; ++j) c[j] = 0.f;
+  for (int z = 0; z < splits; ++z) {
+    const float *cz = Cp + ((long)z * nst + row) * 16;
+#pragma unroll
+    for (int j = 0; j <= K; ++j) c[j] += cz[j];
+  }
   const double s = scale[row];
   y[row] = uref[row] + s * (double)(c[0] + b3[row]);
 #pragma unroll
@@ -469,8 +480,9 @@ void decode_k(pda_lspg &L, const double *x, double *y, cudaStream_t s) {
   } else if (L.tensorCore) {
     k_decode_hidden<K, 256><<<div_up(L.h2, hidden_rows(K)), hidden_rows(K) * 4, 0, s>>>(
         L.h2, L.W1.p, L.b1.p, L.W2T.p, L.b2.p, x, L.Z.p, L.Zb.p, f);
-    PDA_CUDA(tc_gemm(L.W3b.p, L.Zb.p, L.nst, 16, L.h2, nullptr, tc::EPI_NONE, L.C.p, nullptr, nullptr, s));
-    k_decode_finish<K><<<div_up(L.nst, 256), 256, 0, s>>>(L.nst, L.C.p, L.b3.p, L.uref.p, L.scale.p, y, L.D.p, f);
+    PDA_CUDA(tc_gemm_partials(L.W3b.p, L.Zb.p, L.nst, 16, L.h2, kDecodeSplits, L.C.p, s));
+    k_decode_finish_split<K><<<div_up(L.nst, 256), 256, 0, s>>>(L.nst, std::min(kDecodeSplits, L.h2 / 64), L.C.p,
+                                                                 L.b3.p, L.uref.p, L.scale.p, y, L.D.p, f);
   } else {
     k_decode_hidden<K, 256><<<div_up(L.h2, hidden_rows(K)), hidden_rows(K) * 4, 0, s>>>(
         L.h2, L.W1.p, L.b1.p, L.W2T.p, L.b2.p, x, L.Z.p, nullptr, f);
@@ -650,7 +662,7 @@ pda_status pda_lspg_create_mlp(pda_problem *sample_problem, const int64_t *sampl
     L->tensorCore = true;
     L->W3b.alloc((size_t)L->nst * h2);
     L->Zb.alloc((size_t)16 * h2);
-    L->C.alloc((size_t)L->nst * 16);
+    L->C.alloc((size_t)pda::rom::kDecodeSplits * L->nst * 16);  // split-K partial sums
     PDA_CUDA(cudaMemset(L->Zb.p, 0, (size_t)16 * h2 * sizeof(__nv_bfloat16)));
     pda::DevBuf<int> bad;
     bad.alloc(1);
@@ -663,8 +675,7 @@ pda_status pda_lspg_create_mlp(pda_problem *sample_problem, const int64_t *sampl
     PDA_REQUIRE(hb == 0, PDA_ERR_INVALID_ARGUMENT,
                 "tensor-core decoder: output-layer weights are not bf16 values (use mode 0)");
     // one call before any capture: sets the GEMM's shared-memory attribute
-    PDA_CUDA(pda::tc_gemm(L->W3b.p, L->Zb.p, L->nst, 16, h2, nullptr, pda::tc::EPI_NONE, L->C.p, nullptr, nullptr,
-                          nullptr));
+    PDA_CUDA(pda::tc_gemm_partials(L->W3b.p, L->Zb.p, L->nst, 16, h2, pda::rom::kDecodeSplits, L->C.p, nullptr));
     PDA_CUDA(cudaDeviceSynchronize());
   } else {
     PDA_REQUIRE(mode == 0, PDA_ERR_INVALID_ARGUMENT, "mode must be 0 (fp32) or 1 (bf16 tensor cores)");

@@ -182,7 +182,7 @@ k_gemm_tn(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__
   if (!abort_flag && KT > 0) {
     const long row = m0 + warp * 32 + lane;
 #pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 16) {
+    for (int c0 = 0; c0 < BN && n0 + c0 < N; c0 += 16) {  // column groups that hold output columns
       uint32_t r[16];
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
       asm volatile(

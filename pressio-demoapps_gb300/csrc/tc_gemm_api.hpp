@@ -18,6 +18,10 @@ cudaError_t tc_gemm(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long
 cudaError_t tc_gemm_splitk(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K,
                            const float *bias, int epi, float *outF, __nv_bfloat16 *outB, float *preact, float *work,
                            long workFloats, cudaStream_t s);
+// the partial sums of A B^T over `splits` slices of K, partial[z][M][N] (raw
+// fp32, no epilogue); the caller adds them in slice order
+cudaError_t tc_gemm_partials(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K, int splits,
+                             float *partial, cudaStream_t s);
 // 1 if a GEMM gave up waiting on the tensor core since the last call (clears it)
 int tc_gemm_error_and_clear();
 
