@@ -72,7 +72,7 @@ __device__ inline double lspg_sum_rows(const double *__restrict__ a, int ne, int
 // block; warp 0 factors): right-looking Cholesky with reciprocal square
 // roots, lane-parallel substitutions
 __device__ inline void lspg_solve_rt(int K, int nparts, const double *__restrict__ partial, double *__restrict__ x,
-                                     double tol, LspgFlags *f) {
+                                     double tol, int first, LspgFlags *f) {
   __shared__ double H[kLspgKMax][kLspgKMax];
   __shared__ double g[kLspgKMax];
   __shared__ double rdiag[kLspgKMax];
@@ -149,11 +149,12 @@ __device__ inline void lspg_solve_rt(int K, int nparts, const double *__restrict
     corr = c2;
   }
   if (lane == 0) {
-    f->iters += 1;
+    // the first iteration of a step starts the step's count and flag
+    f->iters = first ? 1 : f->iters + 1;
     f->lastCorr = sqrt(corr);
     f->lastRes = sqrt(rr);
     if (!(f->lastRes <= f->maxRes)) f->maxRes = f->lastRes;
-    if (!ok || sqrt(corr) < tol) f->converged = 1;
+    f->converged = (!ok || sqrt(corr) < tol) ? 1 : 0;
   }
 }
 
@@ -175,7 +176,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 template <int FAM, int SCHEME>
 __global__ void __launch_bounds__(FusedPar<FAM>::THREADS)
 k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p, LspgArgs a) {
-  if (a.f->converged) return;
+  if (!a.first && a.f->converged) return;
   using F = Fam<FAM>;
   using FP = FusedPar<FAM>;
   using FF = FusedFace<FAM, SCHEME>;
@@ -440,7 +441,7 @@ k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p,
   __syncthreads();
   if (!last) return;
   __threadfence();
-  lspg_solve_rt(K, ng, gsum, a.x, a.tol, a.f);
+  lspg_solve_rt(K, ng, gsum, a.x, a.tol, a.first, a.f);
   if (tid == 0) *a.ticket = 0u;
 }
 

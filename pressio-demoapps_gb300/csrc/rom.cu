@@ -38,8 +38,8 @@ using Flags = LspgFlags;
 // ------------------------------------------------------------ trial spaces
 template <int K>
 __global__ void k_decode_affine(long nst, const double *__restrict__ uref, const double *__restrict__ phi,
-                                const double *__restrict__ x, double *__restrict__ y, const Flags *f) {
-  if (f->converged) return;
+                                const double *__restrict__ x, double *__restrict__ y, int first, const Flags *f) {
+  if (!first && f->converged) return;
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nst) return;
   double acc = 0.;
@@ -84,8 +84,8 @@ template <int K, int H1>
 __global__ void __launch_bounds__(hidden_rows(K) * 4)
 k_decode_hidden(int h2, const float *__restrict__ W1, const float *__restrict__ b1, const float *__restrict__ W2T,
                 const float *__restrict__ b2, const double *__restrict__ x, float *__restrict__ Z,
-                __nv_bfloat16 *__restrict__ Zb, const Flags *f) {
-  if (f->converged) return;
+                __nv_bfloat16 *__restrict__ Zb, int first, const Flags *f) {
+  if (!first && f->converged) return;
   constexpr int RPB = hidden_rows(K), PARTS = 4, ld = 1 + K;
   __shared__ float sh1[H1];
   __shared__ float sT1[H1][K];
@@ -152,18 +152,26 @@ constexpr int kDecodeSplits = 4;
 template <int K>
 __global__ void k_decode_finish_split(long nst, int splits, const float *__restrict__ Cp, const float *__restrict__ b3,
                                       const double *__restrict__ uref, const double *__restrict__ scale,
-                                      double *__restrict__ y, double *__restrict__ D, const Flags *f) {
-  if (f->converged) return;
+                                      double *__restrict__ y, double *__restrict__ D, int first, const Flags *f) {
+  if (!first && f->converged) return;
   const long row = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= nst) return;
+  // every split's row loaded before the sums (the loads in flight together)
+  float v[kDecodeSplits][K + 1];
+#pragma unroll
+  for (int z = 0; z < kDecodeSplits; ++z) {
+    const float *cz = Cp + ((long)z * nst + row) * 16;
+#pragma unroll
+    for (int j = 0; j <= K; ++j) v[z][j] = z < splits ? __ldg(cz + j) : 0.f;
+  }
   float c[K + 1];
 #pragma unroll
   for (int j = 0; j <= K; ++j) c[j] = 0.f;
-  for (int z = 0; z < splits; ++z) {
-    const float *cz = Cp + ((long)z * nst + row) * 16;
 #pragma unroll
-    for (int j = 0; j <= K; ++j) c[j] += cz[j];
-  }
+  for (int z = 0; z < kDecodeSplits; ++z)
+#pragma unroll
+    for (int j = 0; j <= K; ++j)
+      if (z < splits) c[j] += v[z][j];
   const double s = scale[row];
   y[row] = uref[row] + s * (double)(c[0] + b3[row]);
 #pragma unroll
@@ -177,8 +185,8 @@ template <int K>
 __global__ void __launch_bounds__(256)
 k_decode_out(int h2, long nst, const float *__restrict__ W3, const float *__restrict__ b3,
              const double *__restrict__ uref, const double *__restrict__ scale, const float *__restrict__ Z,
-             double *__restrict__ y, double *__restrict__ D, const Flags *f) {
-  if (f->converged) return;
+             double *__restrict__ y, double *__restrict__ D, int first, const Flags *f) {
+  if (!first && f->converged) return;
   extern __shared__ float sZ[];
   constexpr int ld = 1 + K;
   for (int i = threadIdx.x; i < h2 * ld; i += blockDim.x) sZ[i] = Z[i];
@@ -223,7 +231,7 @@ k_decode_out(int h2, long nst, const float *__restrict__ W3, const float *__rest
 
 template <int K>
 __device__ void lspg_solve_block(int nblocks, const double *__restrict__ partial, double *__restrict__ x, double tol,
-                                 Flags *f);
+                                 int first, Flags *f);
 
 // ---------------------------------------------------- LSPG residual / normal eqs
 // Block of RB sample dof rows; thread (row, c) for c < K forms JR[row][c] =
@@ -239,7 +247,7 @@ k_lspg_rows(int ndpc, long ns, const int *__restrict__ s2st, const double *__res
             const int *__restrict__ colidx, const double *__restrict__ J, double cf, double *__restrict__ yn,
             int first, double *__restrict__ partial, unsigned *__restrict__ ticket, double *__restrict__ x,
             double tol, Flags *f) {
-  if (f->converged) return;
+  if (!first && f->converged) return;
   constexpr int RB = rows_per_block(K);
   __shared__ double sJR[RB][K + 1];  // column K holds R
   const int t = threadIdx.x;
@@ -308,7 +316,7 @@ k_lspg_rows(int ndpc, long ns, const int *__restrict__ s2st, const double *__res
   __syncthreads();
   if (!last) return;
   __threadfence();
-  lspg_solve_block<K>((int)gridDim.x, partial, x, tol, f);
+  lspg_solve_block<K>((int)gridDim.x, partial, x, tol, first, f);
   if (t == 0) *ticket = 0u;
 }
 
@@ -321,7 +329,7 @@ k_lspg_rows(int ndpc, long ns, const int *__restrict__ s2st, const double *__res
 // unknown, multiplying by the stored reciprocal diagonal.  No division.
 template <int K>
 __device__ void lspg_solve_block(int nblocks, const double *__restrict__ partial, double *__restrict__ x, double tol,
-                                 Flags *f) {
+                                 int first, Flags *f) {
   static_assert(K <= 32, "one lane per unknown");
   __shared__ double H[K][K];
   __shared__ double g[K];
@@ -410,18 +418,14 @@ __device__ void lspg_solve_block(int nblocks, const double *__restrict__ partial
       corr = c2;
     }
     if (lane == 0) {
-      f->iters += 1;
+      // the first iteration of a step starts the step's count and flag
+      f->iters = first ? 1 : f->iters + 1;
       f->lastCorr = sqrt(corr);
       f->lastRes = sqrt(rr);
       if (!(f->lastRes <= f->maxRes)) f->maxRes = f->lastRes;
-      if (!ok || sqrt(corr) < tol) f->converged = 1;
+      f->converged = (!ok || sqrt(corr) < tol) ? 1 : 0;
     }
   }
-}
-
-__global__ void k_step_begin(Flags *f) {
-  f->converged = 0;
-  f->iters = 0;
 }
 
 }  // namespace rom
@@ -473,29 +477,29 @@ int decode_grid(long nst) {
 }
 
 template <int K>
-void decode_k(pda_lspg &L, const double *x, double *y, cudaStream_t s) {
+void decode_k(pda_lspg &L, const double *x, double *y, int first, cudaStream_t s) {
   Flags *f = L.flags.p;
   if (L.kind == 0) {
-    k_decode_affine<K><<<div_up(L.nst, 256), 256, 0, s>>>(L.nst, L.uref.p, L.phi.p, x, y, f);
+    k_decode_affine<K><<<div_up(L.nst, 256), 256, 0, s>>>(L.nst, L.uref.p, L.phi.p, x, y, first, f);
   } else if (L.tensorCore) {
     k_decode_hidden<K, 256><<<div_up(L.h2, hidden_rows(K)), hidden_rows(K) * 4, 0, s>>>(
-        L.h2, L.W1.p, L.b1.p, L.W2T.p, L.b2.p, x, L.Z.p, L.Zb.p, f);
+        L.h2, L.W1.p, L.b1.p, L.W2T.p, L.b2.p, x, L.Z.p, L.Zb.p, first, f);
     PDA_CUDA(tc_gemm_partials(L.W3b.p, L.Zb.p, L.nst, 16, L.h2, kDecodeSplits, L.C.p, s));
     k_decode_finish_split<K><<<div_up(L.nst, 256), 256, 0, s>>>(L.nst, std::min(kDecodeSplits, L.h2 / 64), L.C.p,
-                                                                 L.b3.p, L.uref.p, L.scale.p, y, L.D.p, f);
+                                                                 L.b3.p, L.uref.p, L.scale.p, y, L.D.p, first, f);
   } else {
     k_decode_hidden<K, 256><<<div_up(L.h2, hidden_rows(K)), hidden_rows(K) * 4, 0, s>>>(
-        L.h2, L.W1.p, L.b1.p, L.W2T.p, L.b2.p, x, L.Z.p, nullptr, f);
+        L.h2, L.W1.p, L.b1.p, L.W2T.p, L.b2.p, x, L.Z.p, nullptr, first, f);
     const int smem = L.h2 * (1 + K) * (int)sizeof(float);
     k_decode_out<K><<<decode_grid(L.nst), 256, smem, s>>>(L.h2, L.nst, L.W3.p, L.b3.p, L.uref.p, L.scale.p, L.Z.p,
-                                                            y, L.D.p, f);
+                                                            y, L.D.p, first, f);
   }
 }
 
 template <int K>
 void gn_iteration_k(pda_lspg &L, double *x, double dt, double tol, int first, cudaStream_t s) {
   Flags *f = L.flags.p;
-  decode_k<K>(L, x, L.y.p, s);
+  decode_k<K>(L, x, L.y.p, first, s);
   if (L.fused) {
     pda_problem &P = *L.P;
     LspgArgs a{L.y.p, L.D.p, K, -dt, L.yn.p, first, L.V.p, L.partial.p, L.ticket.p, x, tol, f};
@@ -540,13 +544,13 @@ void gn_iteration(pda_lspg &L, double *x, double dt, double tol, int first, cuda
 }
 
 void decode(pda_lspg &L, const double *x, double *y, cudaStream_t s) {
-#define PDA_ROM_DEC(K) decode_k<K>(L, x, y, s)
+#define PDA_ROM_DEC(K) decode_k<K>(L, x, y, 1, s)
   PDA_ROM_K_SWITCH(L.k, PDA_ROM_DEC)
 #undef PDA_ROM_DEC
 }
 
 void bdf1_step(pda_lspg &L, double *x, double dt, double tol, int iters, cudaStream_t s) {
-  k_step_begin<<<1, 1, 0, s>>>(L.flags.p);
+  // the first iteration ignores the previous step's convergence flag and resets it
   for (int it = 0; it < iters; ++it) gn_iteration(L, x, dt, tol, it == 0 ? 1 : 0, s);
   PDA_CUDA(cudaGetLastError());
 }
@@ -697,7 +701,6 @@ pda_status pda_lspg_decode(pda_lspg *L, const double *d_x, double *d_y) {
   PDA_API_BEGIN
   PDA_REQUIRE(L && d_x && d_y, PDA_ERR_INVALID_ARGUMENT, "null argument");
   cudaStream_t s = L->P->stream;
-  pda::rom::k_step_begin<<<1, 1, 0, s>>>(L->flags.p);
   pda::rom::decode(*L, d_x, d_y, s);
   PDA_CUDA(cudaGetLastError());
   PDA_CUDA(cudaStreamSynchronize(s));
