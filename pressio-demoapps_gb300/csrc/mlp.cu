@@ -17,22 +17,48 @@ namespace pda {
 
 static __device__ int g_tc_err;
 
-cudaError_t tc_gemm(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K, const float *bias,
-                    int epi, float *outF, __nv_bfloat16 *outB, float *preact, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tc::k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+// lifts the dynamic shared-memory limit of one GEMM instantiation (once)
+template <int BN_, int ST>
+static cudaError_t gemm_attr() {
+  static bool done = false;
+  if (!done) {
+    cudaError_t e = cudaFuncSetAttribute(tc::k_gemm_tn<BN_, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tc::smem_bytes(BN_, ST));
     if (e != cudaSuccess) return e;
-    attr = true;
+    done = true;
   }
+  return cudaSuccess;
+}
+
+// one launch of k_gemm_tn over all output tiles and `splits` K ranges of
+// `per` slices: the thin instantiation (N = 16 tiles, four stages) when B has
+// at most 16 rows, else 128 x 128 tiles with two stages
+static cudaError_t launch_gemm(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K,
+                               const float *bias, int epi, float *outF, __nv_bfloat16 *outB, float *preact,
+                               int splits, int per, float *partial, cudaStream_t s) {
   int *err = nullptr;
   cudaError_t e = cudaGetSymbolAddress((void **)&err, g_tc_err);
   if (e != cudaSuccess) return e;
-  dim3 grid((unsigned)((N + tc::BN - 1) / tc::BN), (unsigned)((M + tc::BM - 1) / tc::BM));
-  const int kt = (int)(K / tc::BK);
-  tc::k_gemm_tn<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(A, B, M, N, K, bias, epi, outF, outB, preact, err, kt,
-                                                          nullptr);
+  const unsigned mt = (unsigned)((M + tc::BM - 1) / tc::BM);
+  if (N <= tc::THIN_BN) {
+    e = gemm_attr<tc::THIN_BN, tc::THIN_STAGES>();
+    if (e != cudaSuccess) return e;
+    tc::k_gemm_tn<tc::THIN_BN, tc::THIN_STAGES>
+        <<<dim3(1u, mt, (unsigned)splits), tc::THREADS, tc::smem_bytes(tc::THIN_BN, tc::THIN_STAGES), s>>>(
+            A, B, M, N, K, bias, epi, outF, outB, preact, err, per, partial);
+  } else {
+    e = gemm_attr<tc::BN, tc::STAGES>();
+    if (e != cudaSuccess) return e;
+    tc::k_gemm_tn<tc::BN, tc::STAGES>
+        <<<dim3((unsigned)((N + tc::BN - 1) / tc::BN), mt, (unsigned)splits), tc::THREADS, tc::SMEM_BYTES, s>>>(
+            A, B, M, N, K, bias, epi, outF, outB, preact, err, per, partial);
+  }
   return cudaGetLastError();
+}
+
+cudaError_t tc_gemm(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K, const float *bias,
+                    int epi, float *outF, __nv_bfloat16 *outB, float *preact, cudaStream_t s) {
+  return launch_gemm(A, B, M, N, K, bias, epi, outF, outB, preact, 1, (int)(K / tc::BK), nullptr, s);
 }
 
 // Same, splitting K over `splits` CTAs per output tile when the tiles alone
@@ -49,7 +75,8 @@ cudaError_t tc_gemm_splitk(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long 
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 1;
   }
-  const long tiles = ((N + tc::BN - 1) / tc::BN) * ((M + tc::BM - 1) / tc::BM);
+  const long bn = N <= tc::THIN_BN ? tc::THIN_BN : tc::BN;
+  const long tiles = ((N + bn - 1) / bn) * ((M + tc::BM - 1) / tc::BM);
   const int kt = (int)(K / tc::BK);
   int splits = 1;
   if (tiles < 2L * sms && kt >= 32) {
@@ -57,19 +84,9 @@ cudaError_t tc_gemm_splitk(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long 
     while (splits > 1 && (long)splits * M * N > workFloats) --splits;
   }
   if (splits <= 1) return tc_gemm(A, B, M, N, K, bias, epi, outF, outB, preact, s);
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tc::k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
-  int *err = nullptr;
-  cudaError_t e = cudaGetSymbolAddress((void **)&err, g_tc_err);
-  if (e != cudaSuccess) return e;
   const int per = (kt + splits - 1) / splits;
-  dim3 grid((unsigned)((N + tc::BN - 1) / tc::BN), (unsigned)((M + tc::BM - 1) / tc::BM), (unsigned)splits);
-  tc::k_gemm_tn<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(A, B, M, N, K, nullptr, tc::EPI_NONE, nullptr, nullptr,
-                                                          nullptr, err, per, work);
+  cudaError_t e = launch_gemm(A, B, M, N, K, nullptr, tc::EPI_NONE, nullptr, nullptr, nullptr, splits, per, work, s);
+  if (e != cudaSuccess) return e;
   const long total = M * N;
   tc::k_splitk_reduce<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(M, N, splits, work, bias, epi, outF, outB,
                                                                        preact);
@@ -78,22 +95,10 @@ cudaError_t tc_gemm_splitk(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long 
 
 cudaError_t tc_gemm_partials(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K, int splits,
                              float *partial, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tc::k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
-  int *err = nullptr;
-  cudaError_t e = cudaGetSymbolAddress((void **)&err, g_tc_err);
-  if (e != cudaSuccess) return e;
   const int kt = (int)(K / tc::BK);
   splits = std::max(1, std::min(splits, kt));
   const int per = (kt + splits - 1) / splits;
-  dim3 grid((unsigned)((N + tc::BN - 1) / tc::BN), (unsigned)((M + tc::BM - 1) / tc::BM), (unsigned)splits);
-  tc::k_gemm_tn<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(A, B, M, N, K, nullptr, tc::EPI_NONE, nullptr, nullptr,
-                                                          nullptr, err, per, partial);
-  return cudaGetLastError();
+  return launch_gemm(A, B, M, N, K, nullptr, tc::EPI_NONE, nullptr, nullptr, nullptr, splits, per, partial, s);
 }
 
 // 1 if any tensor-core GEMM gave up waiting since the last call; clears it

@@ -147,7 +147,7 @@ k_decode_hidden(int h2, const float *__restrict__ W1, const float *__restrict__ 
 // y = uref + scale (C[., 0] + b3), D = scale C[., 1..k], from split-K partial
 // sums Cp[split][nst][16] added in split order (the output layer is short and
 // wide: K split over the SMs hides the latency of streaming the weights)
-constexpr int kDecodeSplits = 4;
+constexpr int kDecodeSplits = 2;
 
 template <int K>
 __global__ void k_decode_finish_split(long nst, int splits, const float *__restrict__ Cp, const float *__restrict__ b3,

@@ -4,15 +4,17 @@
 // A and B are row-major bf16 with K contiguous ("K-major" for both operands),
 // accumulation in fp32 in tensor memory.
 //
-// Structure (one CTA = 128 threads computes a 128 x 128 tile of C):
-//  * K is consumed in slices of 64; each slice of A and B (128 x 64 bf16 each)
-//    is copied global -> shared with cp.async into the canonical K-major
-//    layout without swizzle: 8 x 16-byte "core matrices", the two core
-//    matrices adjacent in K 128 bytes apart (leading byte offset) and the
-//    8-row groups 1024 bytes apart (stride byte offset);
-//  * two shared-memory stages: while the tensor core works on one slice the
-//    threads copy the next;
-//  * one elected thread issues tcgen05.mma (M = 128, N = 128, K = 16, four
+// Structure (one CTA = 128 threads computes a 128 x BN tile of C; BN = 128
+// for the autoencoder's layers, BN = 16 for the decoder's thin output layer
+// whose B holds the 1 + k latent columns):
+//  * K is consumed in slices of 64; each slice of A (128 x 64 bf16) and of B
+//    (BN x 64) is copied global -> shared with cp.async into the canonical
+//    K-major layout without swizzle: 8 x 16-byte "core matrices", the two
+//    core matrices adjacent in K 128 bytes apart (leading byte offset) and
+//    the 8-row groups 1024 bytes apart (stride byte offset);
+//  * ST shared-memory stages, ST - 1 slices in flight: while the tensor core
+//    works on one slice the threads' copies of the next ones land;
+//  * one elected thread issues tcgen05.mma (M = 128, N = BN, K = 16, four
 //    per slice) and tcgen05.commit onto the stage's mbarrier, which tells
 //    the copy threads when the stage may be overwritten;
 //  * the epilogue reads the accumulator with tcgen05.ld (warp w owns TMEM
@@ -31,9 +33,14 @@ namespace pda {
 namespace tc {
 
 constexpr int BM = 128, BN = 128, BK = 64, THREADS = 128, STAGES = 2;
-constexpr int TILE_BYTES = BM * BK * 2;                    // one operand slice
-constexpr int SMEM_BYTES = STAGES * 2 * TILE_BYTES + 1024;  // + alignment slack
-constexpr uint32_t TMEM_COLS = 128;
+constexpr int TILE_BYTES = BM * BK * 2;  // one 128-row operand slice
+// dynamic shared memory of k_gemm_tn<bn, stages> (+ 1 KB alignment slack)
+__host__ __device__ constexpr int smem_bytes(int bn, int stages) {
+  return stages * (TILE_BYTES + bn * BK * 2) + 1024;
+}
+constexpr int SMEM_BYTES = smem_bytes(BN, STAGES);
+// the decoder's output layer: N = 1 + k <= 16 columns, four stages
+constexpr int THIN_BN = 16, THIN_STAGES = 4;
 constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
@@ -82,13 +89,15 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 
 __device__ __forceinline__ float elu(float x) { return x > 0.f ? x : expm1f(x); }
 
-// copy one 128 x 64 slice (rows r0.., K columns k0..) of a row-major
+// copy one ROWS x 64 slice (rows r0.., K columns k0..) of a row-major
 // [rows x K] bf16 matrix into shared memory; rows past `rows` read as zero
+template <int ROWS>
 __device__ __forceinline__ void load_slice(uint32_t sdst, const __nv_bfloat16 *__restrict__ g, long rows, long K,
                                            long r0, long k0) {
-  // 128 rows x 8 chunks of 16 bytes; 128 threads -> 8 chunks each
+  // ROWS rows x 8 chunks of 16 bytes over 128 threads
+  static_assert((ROWS * 8) % THREADS == 0, "whole chunks per thread");
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
+  for (int i = 0; i < ROWS * 8 / THREADS; ++i) {
     const int c = threadIdx.x + i * THREADS;
     const int r = c >> 3, kc = c & 7;
     const long gr = r0 + r;
@@ -103,28 +112,37 @@ __device__ __forceinline__ void load_slice(uint32_t sdst, const __nv_bfloat16 *_
 // value before the activation.  Split K: CTA z of gridDim.z covers K slices
 // [z * kSlices, (z + 1) * kSlices) and, when `partial` is given, stores its
 // raw fp32 sums to partial[z][M][N] (no epilogue; k_splitk_reduce finishes).
+// Tiles: 128 rows of A (blockIdx.y) by BN_ rows of B (blockIdx.x).
+template <int BN_, int ST>
 __global__ void __launch_bounds__(THREADS)
 k_gemm_tn(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__ B, long M, long N, long K,
           const float *__restrict__ bias, int epi, float *__restrict__ outF, __nv_bfloat16 *__restrict__ outB,
           float *__restrict__ preact, int *__restrict__ err, int kSlices, float *__restrict__ partial) {
+  static_assert(BN_ >= 16 && BN_ <= 256 && BN_ % 16 == 0, "tcgen05 kind::f16 with M = 128: N in 16..256, step 16");
+  static_assert(ST >= 2, "at least two stages");
+  constexpr int B_BYTES = BN_ * BK * 2;
+  constexpr int STAGE_BYTES = TILE_BYTES + B_BYTES;
+  static_assert(STAGE_BYTES % 1024 == 0, "stages stay 1 KB aligned");
+  // TMEM is allocated in powers of two of at least 32 columns
+  constexpr uint32_t kTmemCols = BN_ <= 32 ? 32u : BN_ <= 64 ? 64u : BN_ <= 128 ? 128u : 256u;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  __shared__ __align__(8) uint64_t mbar[STAGES];
+  __shared__ __align__(8) uint64_t mbar[ST];
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
   // 1 KB-aligned operand area
   const uint32_t sbase = (smem_addr(smem_raw) + 1023u) & ~1023u;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long m0 = (long)blockIdx.y * BM, n0 = (long)blockIdx.x * BN;
+  const long m0 = (long)blockIdx.y * BM, n0 = (long)blockIdx.x * BN_;
 
   if (threadIdx.x == 0) {
     abort_flag = 0;
-    for (int s = 0; s < STAGES; ++s)
+    for (int s = 0; s < ST; ++s)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&mbar[s])) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(&tmem_slot)),
-                 "r"(TMEM_COLS)
+                 "r"(kTmemCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
   }
@@ -132,26 +150,43 @@ k_gemm_tn(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = tmem_slot;
-  constexpr uint32_t idesc = instr_desc(BM, BN);
+  constexpr uint32_t idesc = instr_desc(BM, BN_);
 
   const int KTall = (int)(K / BK);
   const int kBegin = (int)blockIdx.z * kSlices;
   const int KT = max(0, min(kSlices, KTall - kBegin));
-  for (int kt = 0; kt < KT; ++kt) {
-    const int st = kt & 1;
-    const uint32_t sA = sbase + (uint32_t)(st * 2 * TILE_BYTES), sB = sA + TILE_BYTES;
-    if (kt >= STAGES) {
-      // the MMAs that read this stage two slices ago must be done
-      if (!mbar_wait(smem_addr(&mbar[st]), (uint32_t)(((kt - STAGES) >> 1) & 1))) abort_flag = 1;
-      __syncthreads();
-      if (abort_flag) break;
-    }
-    load_slice(sA, A, M, K, m0, (long)(kBegin + kt) * BK);
-    load_slice(sB, B, N, K, n0, (long)(kBegin + kt) * BK);
+  // slice s lives in stage s % ST; the MMAs of slice s are the (s / ST)-th
+  // completion of that stage's mbarrier (parity (s / ST) & 1).  One cp.async
+  // group per slice: the prologue commits slices 0..ST-2, iteration kt
+  // commits slice kt + ST - 1 (an empty group past the end), so waiting until
+  // at most ST - 1 groups are pending leaves slices 0..kt complete.
+  auto stage_a = [&](int slice) { return sbase + (uint32_t)((slice % ST) * STAGE_BYTES); };
+  auto load = [&](int slice) {
+    load_slice<BM>(stage_a(slice), A, M, K, m0, (long)(kBegin + slice) * BK);
+    load_slice<BN_>(stage_a(slice) + TILE_BYTES, B, N, K, n0, (long)(kBegin + slice) * BK);
+  };
+#pragma unroll 1
+  for (int p = 0; p < ST - 1; ++p) {
+    if (p < KT) load(p);
     asm volatile("cp.async.commit_group;\n" ::: "memory");
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  }
+#pragma unroll 1
+  for (int kt = 0; kt < KT; ++kt) {
+    const int nx = kt + ST - 1;
+    if (nx < KT) {
+      if (nx >= ST) {
+        // the MMAs that read this stage (slice nx - ST) must be done
+        if (!mbar_wait(smem_addr(&mbar[nx % ST]), (uint32_t)(((nx - ST) / ST) & 1))) abort_flag = 1;
+        __syncthreads();
+        if (abort_flag) break;
+      }
+      load(nx);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(ST - 1) : "memory");
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     __syncthreads();
+    const uint32_t sA = stage_a(kt), sB = sA + TILE_BYTES;
     if (threadIdx.x == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 #pragma unroll
@@ -167,14 +202,16 @@ k_gemm_tn(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__
             : "memory");
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                       smem_addr(&mbar[st]))
+                       smem_addr(&mbar[kt % ST]))
                    : "memory");
     }
   }
+  // no copy may still be landing in shared memory when the CTA exits
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
   // wait for the last commit (it covers every earlier MMA of this thread)
   if (!abort_flag && KT > 0) {
     const int last = KT - 1;
-    if (!mbar_wait(smem_addr(&mbar[last & 1]), (uint32_t)((last >> 1) & 1))) abort_flag = 1;
+    if (!mbar_wait(smem_addr(&mbar[last % ST]), (uint32_t)((last / ST) & 1))) abort_flag = 1;
   }
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
@@ -182,7 +219,7 @@ k_gemm_tn(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__
   if (!abort_flag && KT > 0) {
     const long row = m0 + warp * 32 + lane;
 #pragma unroll 1
-    for (int c0 = 0; c0 < BN && n0 + c0 < N; c0 += 16) {  // column groups that hold output columns
+    for (int c0 = 0; c0 < BN_ && n0 + c0 < N; c0 += 16) {  // column groups that hold output columns
       uint32_t r[16];
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
       asm volatile(
@@ -219,14 +256,14 @@ k_gemm_tn(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__
     // an empty split contributes zeros
     const long row = m0 + warp * 32 + lane;
     if (row < M)
-      for (long col = n0; col < n0 + BN && col < N; ++col) partial[(long)blockIdx.z * M * N + row * N + col] = 0.f;
+      for (long col = n0; col < n0 + BN_ && col < N; ++col) partial[(long)blockIdx.z * M * N + row * N + col] = 0.f;
   }
   if (abort_flag && threadIdx.x == 0) atomicExch(err, 1);
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   if (warp == 0) {
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols) : "memory");
   }
 }
 
