@@ -65,6 +65,29 @@ PDA_HD double div_const(double x, double d, double r) {
   return fma(e, r, q0);
 }
 
+// k x + c rounded once, for k a power of two.  k x is then exact (for
+// |x| >= 2^-1020, far below any state or gradient value here), so the result
+// equals RN(RN(k x) + c), the separately rounded product and sum of the
+// reference's source, in one FP64 instruction instead of two.
+PDA_HD double fma_p2(double k, double x, double c) { return fma(k, x, c); }
+
+// The reference's WENO5 stencil expressions (impl/weno5.hpp), evaluated left
+// to right as in its source, with the power-of-two products fused:
+//   w5_curv(a, m, c)   = a - 2 m + c
+//   w5_slopeL(a, m, c) = a - 4 m + 3 c
+//   w5_slopeR(a, m, c) = 3 a - 4 m + c
+//   w5_pFarL(a, b, c)  = 2 a - 7 b + 11 c     (6 x a candidate polynomial)
+//   w5_pMidL(a, b, c)  = -a + 5 b + 2 c
+//   w5_pMidR(a, b, c)  = 2 a + 5 b - c
+//   w5_pFarR(a, b, c)  = 11 a - 7 b + 2 c
+PDA_HD double w5_curv(double a, double m, double c) { return fma_p2(-2., m, a) + c; }
+PDA_HD double w5_slopeL(double a, double m, double c) { return fma_p2(-4., m, a) + 3. * c; }
+PDA_HD double w5_slopeR(double a, double m, double c) { return fma_p2(-4., m, 3. * a) + c; }
+PDA_HD double w5_pFarL(double a, double b, double c) { return fma_p2(2., a, -(7. * b)) + 11. * c; }
+PDA_HD double w5_pMidL(double a, double b, double c) { return fma_p2(2., c, -a + 5. * b); }
+PDA_HD double w5_pMidR(double a, double b, double c) { return fma_p2(2., a, 5. * b) - c; }
+PDA_HD double w5_pFarR(double a, double b, double c) { return fma_p2(2., c, 11. * a - 7. * b); }
+
 // ---------------------------------------------------------------------------
 // WENO5, one face i+1/2: uNeg from q_{i-2..i+2}, uPos from q_{i-1..i+3}.
 // ---------------------------------------------------------------------------
@@ -78,15 +101,15 @@ PDA_HD double weno5_neg(double qim2, double qim1, double qi, double qip1, double
                    sixOvten = 6. / 10., thirteenOvtwelve = 13. / 12.;
   double uNeg;
   {
-    const double p0 = (two * qim2 - seven * qim1 + eleven * qi) * oneOvsix;
-    const double p1 = (-qim1 + five * qi + two * qip1) * oneOvsix;
-    const double p2 = (two * qi + five * qip1 - qip2) * oneOvsix;
-    const double B0 = thirteenOvtwelve * (qim2 - two * qim1 + qi) * (qim2 - two * qim1 + qi) +
-                      oneOvfour * (qim2 - four * qim1 + three * qi) * (qim2 - four * qim1 + three * qi);
-    const double B1 = thirteenOvtwelve * (qim1 - two * qi + qip1) * (qim1 - two * qi + qip1) +
-                      oneOvfour * (qim1 - qip1) * (qim1 - qip1);
-    const double B2 = thirteenOvtwelve * (qi - two * qip1 + qip2) * (qi - two * qip1 + qip2) +
-                      oneOvfour * (three * qi - four * qip1 + qip2) * (three * qi - four * qip1 + qip2);
+    const double p0 = w5_pFarL(qim2, qim1, qi) * oneOvsix;
+    const double p1 = w5_pMidL(qim1, qi, qip1) * oneOvsix;
+    const double p2 = w5_pMidR(qi, qip1, qip2) * oneOvsix;
+    const double X0 = w5_curv(qim2, qim1, qi), Y0 = w5_slopeL(qim2, qim1, qi);
+    const double X1 = w5_curv(qim1, qi, qip1), Y1 = qim1 - qip1;
+    const double X2 = w5_curv(qi, qip1, qip2), Y2 = w5_slopeR(qi, qip1, qip2);
+    const double B0 = thirteenOvtwelve * X0 * X0 + oneOvfour * Y0 * Y0;
+    const double B1 = thirteenOvtwelve * X1 * X1 + oneOvfour * Y1 * Y1;
+    const double B2 = thirteenOvtwelve * X2 * X2 + oneOvfour * Y2 * Y2;
     const double alpha0 = oneOvten / (epsilon * epsilon + 2. * epsilon * B0 + B0 * B0);
     const double alpha1 = sixOvten / (epsilon * epsilon + 2. * epsilon * B1 + B1 * B1);
     const double alpha2 = threeOvten / (epsilon * epsilon + 2. * epsilon * B2 + B2 * B2);
@@ -109,15 +132,15 @@ PDA_HD double weno5_pos(double qim1, double qi, double qip1, double qip2, double
                    sixOvten = 6. / 10., thirteenOvtwelve = 13. / 12.;
   double uPos;
   {
-    const double p0 = (-qim1 + five * qi + two * qip1) * oneOvsix;
-    const double p1 = (two * qi + five * qip1 - qip2) * oneOvsix;
-    const double p2 = (eleven * qip1 - seven * qip2 + two * qip3) * oneOvsix;
-    const double B0 = thirteenOvtwelve * (qim1 - two * qi + qip1) * (qim1 - two * qi + qip1) +
-                      oneOvfour * (qim1 - four * qi + three * qip1) * (qim1 - four * qi + three * qip1);
-    const double B1 = thirteenOvtwelve * (qi - two * qip1 + qip2) * (qi - two * qip1 + qip2) +
-                      oneOvfour * (qi - qip2) * (qi - qip2);
-    const double B2 = thirteenOvtwelve * (qip1 - two * qip2 + qip3) * (qip1 - two * qip2 + qip3) +
-                      oneOvfour * (three * qip1 - four * qip2 + qip3) * (three * qip1 - four * qip2 + qip3);
+    const double p0 = w5_pMidL(qim1, qi, qip1) * oneOvsix;
+    const double p1 = w5_pMidR(qi, qip1, qip2) * oneOvsix;
+    const double p2 = w5_pFarR(qip1, qip2, qip3) * oneOvsix;
+    const double X0 = w5_curv(qim1, qi, qip1), Y0 = w5_slopeL(qim1, qi, qip1);
+    const double X1 = w5_curv(qi, qip1, qip2), Y1 = qi - qip2;
+    const double X2 = w5_curv(qip1, qip2, qip3), Y2 = w5_slopeR(qip1, qip2, qip3);
+    const double B0 = thirteenOvtwelve * X0 * X0 + oneOvfour * Y0 * Y0;
+    const double B1 = thirteenOvtwelve * X1 * X1 + oneOvfour * Y1 * Y1;
+    const double B2 = thirteenOvtwelve * X2 * X2 + oneOvfour * Y2 * Y2;
     const double alpha0 = threeOvten / (epsilon * epsilon + 2. * epsilon * B0 + B0 * B0);
     const double alpha1 = sixOvten / (epsilon * epsilon + 2. * epsilon * B1 + B1 * B1);
     const double alpha2 = oneOvten / (epsilon * epsilon + 2. * epsilon * B2 + B2 * B2);
@@ -147,34 +170,38 @@ PDA_HD void weno5_neg_grad(double &uNeg, double gNeg[6], double qim2, double qim
                    oneOvten = 1. / 10., threeOvten = 3. / 10.,
                    sixOvten = 6. / 10., thirteenOvtwelve = 13. / 12.;
   {
-    const double p0 = (two * qim2 - seven * qim1 + eleven * qi) * oneOvsix;
-    const double p1 = (-qim1 + five * qi + two * qip1) * oneOvsix;
-    const double p2 = (two * qi + five * qip1 - qip2) * oneOvsix;
+    const double p0 = w5_pFarL(qim2, qim1, qi) * oneOvsix;
+    const double p1 = w5_pMidL(qim1, qi, qip1) * oneOvsix;
+    const double p2 = w5_pMidR(qi, qip1, qip2) * oneOvsix;
     const double dp0[5] = {1. / 3., -7. / 6., 11. / 6., 0., 0.};
     const double dp1[5] = {0., -1. / 6., 5. / 6., 1. / 3., 0.};
     const double dp2[5] = {0., 0., 1. / 3., 5. / 6., -1. / 6.};
-    const double B0 = thirteenOvtwelve * sq(qim2 - two * qim1 + qi) +
-                      oneOvfour * sq(qim2 - four * qim1 + three * qi);
-    const double B1 = thirteenOvtwelve * sq(qim1 - two * qi + qip1) +
+    const double B0 = thirteenOvtwelve * sq(w5_curv(qim2, qim1, qi)) +
+                      oneOvfour * sq(w5_slopeL(qim2, qim1, qi));
+    const double B1 = thirteenOvtwelve * sq(w5_curv(qim1, qi, qip1)) +
                       oneOvfour * sq(qim1 - qip1);
-    const double B2 = thirteenOvtwelve * sq(qi - two * qip1 + qip2) +
-                      oneOvfour * sq(three * qi - four * qip1 + qip2);
+    const double B2 = thirteenOvtwelve * sq(w5_curv(qi, qip1, qip2)) +
+                      oneOvfour * sq(w5_slopeR(qi, qip1, qip2));
+    // derivative terms (impl/weno5.hpp:294-310), the products by 2 and 1/2 fused
+    const double X0 = 13. * w5_curv(qim2, qim1, qi), Y0 = w5_slopeL(qim2, qim1, qi);
+    const double X1 = 13. * fma_p2(-2., qi, qip1 + qim1), Y1 = qim1 - qip1;
+    const double X2 = 13. * w5_curv(qip2, qip1, qi), Y2 = w5_slopeL(qip2, qip1, qi);
     double dB0[5], dB1[5], dB2[5];
-    dB0[0] = div_const(13. * (qim2 - 2. * qim1 + qi), 6., 1. / 6.) + (qim2 - 4. * qim1 + 3. * qi) / 2.;
-    dB0[1] = div_const(-(13. * (qim2 - 2. * qim1 + qi)), 3., 1. / 3.) - 2. * (qim2 - 4. * qim1 + 3. * qi);
-    dB0[2] = div_const(13. * (qim2 - 2. * qim1 + qi), 6., 1. / 6.) + (3. * (qim2 - 4. * qim1 + 3. * qi)) / 2.;
+    dB0[0] = fma_p2(0.5, Y0, div_const(X0, 6., 1. / 6.));
+    dB0[1] = fma_p2(-2., Y0, div_const(-X0, 3., 1. / 3.));
+    dB0[2] = fma_p2(0.5, 3. * Y0, div_const(X0, 6., 1. / 6.));
     dB0[3] = 0.;
     dB0[4] = 0.;
     dB1[0] = 0.;
-    dB1[1] = div_const(13. * (qip1 + qim1 - 2. * qi), 6., 1. / 6.) + (qim1 - qip1) / 2.;
-    dB1[2] = div_const(-(13. * (qip1 + qim1 - 2. * qi)), 3., 1. / 3.);
-    dB1[3] = div_const(13. * (qip1 + qim1 - 2. * qi), 6., 1. / 6.) - (qim1 - qip1) / 2.;
+    dB1[1] = fma_p2(0.5, Y1, div_const(X1, 6., 1. / 6.));
+    dB1[2] = div_const(-X1, 3., 1. / 3.);
+    dB1[3] = fma_p2(-0.5, Y1, div_const(X1, 6., 1. / 6.));
     dB1[4] = 0.;
     dB2[0] = 0.;
     dB2[1] = 0.;
-    dB2[2] = div_const(13. * (qip2 - 2. * qip1 + qi), 6., 1. / 6.) + (3. * (qip2 - 4. * qip1 + 3. * qi)) / 2.;
-    dB2[3] = div_const(-(13. * (qip2 - 2. * qip1 + qi)), 3., 1. / 3.) - 2. * (qip2 - 4. * qip1 + 3. * qi);
-    dB2[4] = div_const(13. * (qip2 - 2. * qip1 + qi), 6., 1. / 6.) + (qip2 - 4. * qip1 + 3. * qi) / 2.;
+    dB2[2] = fma_p2(0.5, 3. * Y2, div_const(X2, 6., 1. / 6.));
+    dB2[3] = fma_p2(-2., Y2, div_const(-X2, 3., 1. / 3.));
+    dB2[4] = fma_p2(0.5, Y2, div_const(X2, 6., 1. / 6.));
     const double alpha0 = oneOvten / sq(epsilon + B0);
     const double alpha1 = sixOvten / sq(epsilon + B1);
     const double alpha2 = threeOvten / sq(epsilon + B2);
@@ -210,34 +237,38 @@ PDA_HD void weno5_pos_grad(double &uPos, double gPos[6], double qim2, double qim
                    oneOvten = 1. / 10., threeOvten = 3. / 10.,
                    sixOvten = 6. / 10., thirteenOvtwelve = 13. / 12.;
   {
-    const double p0 = (-qim1 + five * qi + two * qip1) * oneOvsix;
-    const double p1 = (two * qi + five * qip1 - qip2) * oneOvsix;
-    const double p2 = (eleven * qip1 - seven * qip2 + two * qip3) * oneOvsix;
+    const double p0 = w5_pMidL(qim1, qi, qip1) * oneOvsix;
+    const double p1 = w5_pMidR(qi, qip1, qip2) * oneOvsix;
+    const double p2 = w5_pFarR(qip1, qip2, qip3) * oneOvsix;
     const double dp0[5] = {-1. / 6., 5. / 6., 1. / 3., 0., 0.};
     const double dp1[5] = {0., 1. / 3., 5. / 6., -1. / 6., 0.};
     const double dp2[5] = {0., 0., 11. / 6., -7. / 6., 1. / 3.};
-    const double B0 = thirteenOvtwelve * sq(qim1 - two * qi + qip1) +
-                      oneOvfour * sq(qim1 - four * qi + three * qip1);
-    const double B1 = thirteenOvtwelve * sq(qi - two * qip1 + qip2) +
+    const double B0 = thirteenOvtwelve * sq(w5_curv(qim1, qi, qip1)) +
+                      oneOvfour * sq(w5_slopeL(qim1, qi, qip1));
+    const double B1 = thirteenOvtwelve * sq(w5_curv(qi, qip1, qip2)) +
                       oneOvfour * sq(qi - qip2);
-    const double B2 = thirteenOvtwelve * sq(qip1 - two * qip2 + qip3) +
-                      oneOvfour * sq(three * qip1 - four * qip2 + qip3);
+    const double B2 = thirteenOvtwelve * sq(w5_curv(qip1, qip2, qip3)) +
+                      oneOvfour * sq(w5_slopeR(qip1, qip2, qip3));
+    // derivative terms (impl/weno5.hpp:385-401), the products by 2, 4 and 1/2 fused
+    const double X0 = 13. * fma_p2(-2., qi, qip1 + qim1), Y0 = fma_p2(-4., qi, 3. * qip1 + qim1);
+    const double X1 = 13. * w5_curv(qip2, qip1, qi), Y1 = qi - qip2;
+    const double X2 = 13. * w5_curv(qip3, qip2, qip1), Y2 = w5_slopeL(qip3, qip2, qip1);
     double dB0[5], dB1[5], dB2[5];
-    dB0[0] = (3. * qip1 + qim1 - 4. * qi) / 2. + div_const(13. * (qip1 + qim1 - 2. * qi), 6., 1. / 6.);
-    dB0[1] = -2. * (3. * qip1 + qim1 - 4. * qi) - div_const(13. * (qip1 + qim1 - 2 * qi), 3., 1. / 3.);
-    dB0[2] = (3. * (3. * qip1 + qim1 - 4. * qi)) / 2. + div_const(13. * (qip1 + qim1 - 2. * qi), 6., 1. / 6.);
+    dB0[0] = fma_p2(0.5, Y0, div_const(X0, 6., 1. / 6.));
+    dB0[1] = fma_p2(-2., Y0, -div_const(X0, 3., 1. / 3.));
+    dB0[2] = fma_p2(0.5, 3. * Y0, div_const(X0, 6., 1. / 6.));
     dB0[3] = 0.;
     dB0[4] = 0.;
     dB1[0] = 0.;
-    dB1[1] = div_const(13. * (qip2 - 2 * qip1 + qi), 6., 1. / 6.) + (qi - qip2) / 2.;
-    dB1[2] = div_const(-(13. * (qip2 - 2. * qip1 + qi)), 3., 1. / 3.);
-    dB1[3] = div_const(13. * (qip2 - 2. * qip1 + qi), 6., 1. / 6.) - (qi - qip2) / 2.;
+    dB1[1] = fma_p2(0.5, Y1, div_const(X1, 6., 1. / 6.));
+    dB1[2] = div_const(-X1, 3., 1. / 3.);
+    dB1[3] = fma_p2(-0.5, Y1, div_const(X1, 6., 1. / 6.));
     dB1[4] = 0.;
     dB2[0] = 0.;
     dB2[1] = 0.;
-    dB2[2] = div_const(13. * (qip3 - 2. * qip2 + qip1), 6., 1. / 6.) + (3. * (qip3 - 4. * qip2 + 3. * qip1)) / 2.;
-    dB2[3] = div_const(-(13. * (qip3 - 2. * qip2 + qip1)), 3., 1. / 3.) - 2. * (qip3 - 4. * qip2 + 3. * qip1);
-    dB2[4] = div_const(13. * (qip3 - 2. * qip2 + qip1), 6., 1. / 6.) + (qip3 - 4. * qip2 + 3. * qip1) / 2.;
+    dB2[2] = fma_p2(0.5, 3. * Y2, div_const(X2, 6., 1. / 6.));
+    dB2[3] = fma_p2(-2., Y2, div_const(-X2, 3., 1. / 3.));
+    dB2[4] = fma_p2(0.5, Y2, div_const(X2, 6., 1. / 6.));
     const double alpha0 = threeOvten / sq(epsilon + B0);
     const double alpha1 = sixOvten / sq(epsilon + B1);
     const double alpha2 = oneOvten / sq(epsilon + B2);

@@ -2,6 +2,8 @@
 //
 // The FP64 pipe bounds this path on GB300, so the kernels minimise FP64
 // operations while keeping every value bit-identical to the reference:
+//  * products by powers of two are fused into the following sum (w5_* in
+//    numerics.cuh: the product is exact, so one rounding equals two);
 //  * each face is computed once (the reference computes it from both cells);
 //  * the smoothness indicators of a cell triple (WENO5) or pair (WENO3) and
 //    the alpha terms built from them enter up to three one-sided
@@ -85,18 +87,17 @@ __device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &
   constexpr double epsilon = 1e-6;
   if constexpr (SCHEME == Weno5) {
     // center c = f0 - 2 + tx uses cells c-1, c, c+1 = sU[tx .. tx+2]
-    constexpr double two = 2., three = 3., four = 4.;
     constexpr double oneOvfour = 1. / 4., oneOvten = 1. / 10., threeOvten = 3. / 10., sixOvten = 6. / 10.,
                      thirteenOvtwelve = 13. / 12.;
     if (tx + 2 < NCELL) {
 #pragma unroll
       for (int d = 0; d < NDPC; ++d) {
         const double a = sU[ty][d][tx], m = sU[ty][d][tx + 1], c = sU[ty][d][tx + 2];
-        const double X = a - two * m + c;
+        const double X = w5_curv(a, m, c);
         const double D = thirteenOvtwelve * X * X;
-        const double YL = a - four * m + three * c;
+        const double YL = w5_slopeL(a, m, c);
         const double YC = a - c;
-        const double YR = three * a - four * m + c;
+        const double YR = w5_slopeR(a, m, c);
         const double BL = D + oneOvfour * YL * YL;
         const double BC = D + oneOvfour * YC * YC;
         const double BR = D + oneOvfour * YR * YR;
@@ -131,16 +132,16 @@ __device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &
   if (!lineOk || tx >= TW || f > b.hi[AXIS]) return;
   double uN[NDPC], uP[NDPC];
   if constexpr (SCHEME == Weno5) {
-    constexpr double two = 2., five = 5., seven = 7., eleven = 11., oneOvsix = 1. / 6.;
+    constexpr double oneOvsix = 1. / 6.;
 #pragma unroll
     for (int d = 0; d < NDPC; ++d) {
       // left cell i = f-1: cells i-2..i+3 = sU[tx .. tx+5]; centers i-1..i+2 = sA[.][tx .. tx+3]
       const double qim2 = sU[ty][d][tx], qim1 = sU[ty][d][tx + 1], qi = sU[ty][d][tx + 2];
       const double qip1 = sU[ty][d][tx + 3], qip2 = sU[ty][d][tx + 4], qip3 = sU[ty][d][tx + 5];
-      const double p0 = (two * qim2 - seven * qim1 + eleven * qi) * oneOvsix;
-      const double p1 = (-qim1 + five * qi + two * qip1) * oneOvsix;
-      const double p2 = (two * qi + five * qip1 - qip2) * oneOvsix;
-      const double p3 = (eleven * qip1 - seven * qip2 + two * qip3) * oneOvsix;
+      const double p0 = w5_pFarL(qim2, qim1, qi) * oneOvsix;
+      const double p1 = w5_pMidL(qim1, qi, qip1) * oneOvsix;
+      const double p2 = w5_pMidR(qi, qip1, qip2) * oneOvsix;
+      const double p3 = w5_pFarR(qip1, qip2, qip3) * oneOvsix;
       {
         const double a0 = sA[ty][d][0][tx], a1 = sA[ty][d][2][tx + 1], a2 = sA[ty][d][3][tx + 2];
         const double s = 1. / (a0 + a1 + a2);
