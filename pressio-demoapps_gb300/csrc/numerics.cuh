@@ -71,6 +71,11 @@ PDA_HD double div_const(double x, double d, double r) {
 // reference's source, in one FP64 instruction instead of two.
 PDA_HD double fma_p2(double k, double x, double c) { return fma(k, x, c); }
 
+// x + k w for a tabulated constant k: a zero k makes the product exact (a
+// signed zero, or NaN for an infinite or NaN w, exactly as RN(k w)), so one
+// rounding; otherwise the two separate roundings of the source
+PDA_HD double add_table_prod(double x, double k, double w) { return k == 0. ? fma(k, w, x) : x + k * w; }
+
 // The reference's WENO5 stencil expressions (impl/weno5.hpp), evaluated left
 // to right as in its source, with the power-of-two products fused:
 //   w5_curv(a, m, c)   = a - 2 m + c
@@ -218,9 +223,9 @@ PDA_HD void weno5_neg_grad(double &uNeg, double gNeg[6], double qim2, double qim
       const double da1 = c1 * dB1[i];
       const double da2 = c2 * dB2[i];
       const double daS = cS * (da0 + da1 + da2);
-      double g = (da0 * alphaSInv + daS * alpha0) * p0 + dp0[i] * w0;
-      g += (da1 * alphaSInv + daS * alpha1) * p1 + dp1[i] * w1;
-      g += (da2 * alphaSInv + daS * alpha2) * p2 + dp2[i] * w2;
+      double g = add_table_prod((da0 * alphaSInv + daS * alpha0) * p0, dp0[i], w0);
+      g += add_table_prod((da1 * alphaSInv + daS * alpha1) * p1, dp1[i], w1);
+      g += add_table_prod((da2 * alphaSInv + daS * alpha2) * p2, dp2[i], w2);
       gNeg[i] = g;
     }
     gNeg[5] = 0.;
@@ -285,9 +290,9 @@ PDA_HD void weno5_pos_grad(double &uPos, double gPos[6], double qim2, double qim
       const double da1 = c1 * dB1[i];
       const double da2 = c2 * dB2[i];
       const double daS = cS * (da0 + da1 + da2);
-      double g = (da0 * alphaSInv + daS * alpha0) * p0 + dp0[i] * w0;
-      g += (da1 * alphaSInv + daS * alpha1) * p1 + dp1[i] * w1;
-      g += (da2 * alphaSInv + daS * alpha2) * p2 + dp2[i] * w2;
+      double g = add_table_prod((da0 * alphaSInv + daS * alpha0) * p0, dp0[i], w0);
+      g += add_table_prod((da1 * alphaSInv + daS * alpha1) * p1, dp1[i], w1);
+      g += add_table_prod((da2 * alphaSInv + daS * alpha2) * p2, dp2[i], w2);
       gPos[i + 1] = g;
     }
     gPos[0] = 0.;
@@ -616,10 +621,10 @@ PDA_HD void euler3_flux_jac(double JL[9], double JR[9], const double qL[3],
   const double VVRoeR = uR * u;
   const double uRelRoe = u / sqrt(VMagSqrRoe);
   double gL[3], gR[3];
-  gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe + half * gm1 / a * (half * (VMagSqrRoe + VVRoeL) + half * (HL - H) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
+  gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe + half * gm1 / a * (fma_p2(half, VMagSqrRoe + VVRoeL, half * (HL - H)) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
   gL[1] = one / (rL + r) * (uRelRoe - half * (gm1 * (u + gm1 * uL)) / (a));
   gL[2] = half / (rL + r) * gamma * gm1 / (a);
-  gR[0] = one / (rR + r) * (-half * (uR + u) * uRelRoe + half * gm1 / a * (half * (VMagSqrRoe + VVRoeR) + half * (HR - H) - aR * aR / gm1 + half * (gamma - two) * VMagSqrR));
+  gR[0] = one / (rR + r) * (-half * (uR + u) * uRelRoe + half * gm1 / a * (fma_p2(half, VMagSqrRoe + VVRoeR, half * (HR - H)) - aR * aR / gm1 + half * (gamma - two) * VMagSqrR));
   gR[1] = one / (rR + r) * (uRelRoe - half * (gm1 * (u + gm1 * uR)) / (a));
   gR[2] = half / (rR + r) * gamma * gm1 / (a);
   JL[0] = 0;
@@ -632,7 +637,7 @@ PDA_HD void euler3_flux_jac(double JL[9], double JR[9], const double qL[3],
   JL[7] = half * (HL - gm1 * uL * uL);
   JL[8] = half * gamma * uL;
   for (int i = 0; i < 3; i++) {
-    JL[i * 3 + i] += half * smax;
+    JL[i * 3 + i] = fma_p2(half, smax, JL[i * 3 + i]);
     for (int j = 0; j < 3; j++) JL[i * 3 + j] += half * gL[j] * (qL[i] - qR[i]);
   }
   JR[0] = 0;
@@ -645,7 +650,7 @@ PDA_HD void euler3_flux_jac(double JL[9], double JR[9], const double qL[3],
   JR[7] = half * (HR - gm1 * uR * uR);
   JR[8] = half * gamma * uR;
   for (int i = 0; i < 3; i++) {
-    JR[i * 3 + i] -= half * smax;
+    JR[i * 3 + i] = fma_p2(-half, smax, JR[i * 3 + i]);
     for (int j = 0; j < 3; j++) JR[i * 3 + j] += half * gR[j] * (qL[i] - qR[i]);
   }
 }
@@ -686,11 +691,11 @@ PDA_HD void euler4_flux_jac(double JL[16], double JR[16], const double qL[4],
   const double uRelRoe = u / sqrt(VMagSqrRoe);
   const double vRelRoe = v / sqrt(VMagSqrRoe);
   double gL[4], gR[4];
-  gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe - half * (vL + v) * vRelRoe + half * gm1 / a * (half * (VMagSqrRoe + VVRoeL) + half * (HL - H) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
+  gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe - half * (vL + v) * vRelRoe + half * gm1 / a * (fma_p2(half, VMagSqrRoe + VVRoeL, half * (HL - H)) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
   gL[1] = one / (rL + r) * (uRelRoe - half * (gm1 * (u + gm1 * uL)) / (a));
   gL[2] = one / (rL + r) * (vRelRoe - half * (gm1 * (v + gm1 * vL)) / (a));
   gL[3] = half / (rL + r) * gamma * gm1 / (a);
-  gR[0] = one / (rR + r) * (-half * (uR + u) * uRelRoe - half * (vR + v) * vRelRoe + half * gm1 / a * (half * (VMagSqrRoe + VVRoeR) + half * (HR - H) - aR * aR / gm1 + half * (gamma - two) * VMagSqrR));
+  gR[0] = one / (rR + r) * (-half * (uR + u) * uRelRoe - half * (vR + v) * vRelRoe + half * gm1 / a * (fma_p2(half, VMagSqrRoe + VVRoeR, half * (HR - H)) - aR * aR / gm1 + half * (gamma - two) * VMagSqrR));
   gR[1] = one / (rR + r) * (uRelRoe - half * (gm1 * (u + gm1 * uR)) / (a));
   gR[2] = one / (rR + r) * (vRelRoe - half * (gm1 * (v + gm1 * vR)) / (a));
   gR[3] = half / (rR + r) * gamma * gm1 / (a);
@@ -712,7 +717,7 @@ PDA_HD void euler4_flux_jac(double JL[16], double JR[16], const double qL[4],
   JL[14] = half * (HL * n[1] - gm1 * vL * unL);
   JL[15] = half * gamma * unL;
   for (int i = 0; i < 4; i++) {
-    JL[i * 4 + i] += half * smax;
+    JL[i * 4 + i] = fma_p2(half, smax, JL[i * 4 + i]);
     for (int j = 0; j < 4; j++) JL[i * 4 + j] += half * gL[j] * (qL[i] - qR[i]);
   }
   // right
@@ -733,7 +738,7 @@ PDA_HD void euler4_flux_jac(double JL[16], double JR[16], const double qL[4],
   JR[14] = half * (HR * n[1] - gm1 * vR * unR);
   JR[15] = half * gamma * unR;
   for (int i = 0; i < 4; i++) {
-    JR[i * 4 + i] -= half * smax;
+    JR[i * 4 + i] = fma_p2(-half, smax, JR[i * 4 + i]);
     for (int j = 0; j < 4; j++) JR[i * 4 + j] += half * gR[j] * (qL[i] - qR[i]);
   }
 }
@@ -778,12 +783,12 @@ PDA_HD void euler5_flux_jac(double JL[25], double JR[25], const double qL[5],
   const double vRelRoe = v / sqrt(VMagSqrRoe);
   const double wRelRoe = w / sqrt(VMagSqrRoe);
   double gL[5], gR[5];
-  gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe - half * (vL + v) * vRelRoe - half * (wL + w) * wRelRoe + half * gm1 / a * (half * (VMagSqrRoe + VVRoeL) + half * (HL - H) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
+  gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe - half * (vL + v) * vRelRoe - half * (wL + w) * wRelRoe + half * gm1 / a * (fma_p2(half, VMagSqrRoe + VVRoeL, half * (HL - H)) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
   gL[1] = one / (rL + r) * (uRelRoe - half * (gm1 * (u + gm1 * uL)) / (a));
   gL[2] = one / (rL + r) * (vRelRoe - half * (gm1 * (v + gm1 * vL)) / (a));
   gL[3] = one / (rL + r) * (wRelRoe - half * (gm1 * (w + gm1 * wL)) / (a));
   gL[4] = half / (rL + r) * gamma * gm1 / (a);
-  gR[0] = one / (rR + r) * (-half * (uR + u) * uRelRoe - half * (vR + v) * vRelRoe - half * (wR + w) * wRelRoe + half * gm1 / a * (half * (VMagSqrRoe + VVRoeR) + half * (HR - H) - aR * aR / gm1 + half * (gamma - two) * VMagSqrR));
+  gR[0] = one / (rR + r) * (-half * (uR + u) * uRelRoe - half * (vR + v) * vRelRoe - half * (wR + w) * wRelRoe + half * gm1 / a * (fma_p2(half, VMagSqrRoe + VVRoeR, half * (HR - H)) - aR * aR / gm1 + half * (gamma - two) * VMagSqrR));
   gR[1] = one / (rR + r) * (uRelRoe - half * (gm1 * (u + gm1 * uR)) / (a));
   gR[2] = one / (rR + r) * (vRelRoe - half * (gm1 * (v + gm1 * vR)) / (a));
   gR[3] = one / (rR + r) * (wRelRoe - half * (gm1 * (w + gm1 * wR)) / (a));
@@ -817,13 +822,13 @@ PDA_HD void euler5_flux_jac(double JL[25], double JR[25], const double qL[5],
   J[24] = half * gamma * unX;
   PDA_FILL_J5(JL, uL, vL, wL, unL, HL, VMagSqrL)
   for (int i = 0; i < 5; i++) {
-    JL[i * 5 + i] += half * smax;
+    JL[i * 5 + i] = fma_p2(half, smax, JL[i * 5 + i]);
     for (int j = 0; j < 5; j++) JL[i * 5 + j] += half * gL[j] * (qL[i] - qR[i]);
   }
   PDA_FILL_J5(JR, uR, vR, wR, unR, HR, VMagSqrR)
 #undef PDA_FILL_J5
   for (int i = 0; i < 5; i++) {
-    JR[i * 5 + i] -= half * smax;
+    JR[i * 5 + i] = fma_p2(-half, smax, JR[i * 5 + i]);
     for (int j = 0; j < 5; j++) JR[i * 5 + j] += half * gR[j] * (qL[i] - qR[i]);
   }
 }
