@@ -432,7 +432,8 @@ def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int
     pda, torch = c.pda, c.torch
     out = {"config": "swe_slipwall_256^2_weno5_learned_lspg_bdf1_latent12", "train_points": n_train,
            "snapshots_per_point": n_snap, "test_points": n_test, "latent": latent, "epochs": epochs,
-           "dt_fom": dt, "dt_rom": dt * rom_ratio, "gn_iters_max": gn_iters}
+           "dt_fom": dt, "dt_rom": dt * rom_ratio, "gn_iters_max": gn_iters,
+           "gauss_newton": "residual, normal equations and solve fp64; Jacobian terms fp32 (inexact step)"}
     setup = R.SweSetup(pda, n)
     train = R.latin_hypercube(n_train, seed=5)
     test = R.uniform_points(n_test, seed=6)
@@ -570,9 +571,13 @@ def wl_lspg_step(c, n=256, latent=12, steps=20, gn_iters=3):
     out = {"config": "lspg_bdf1_swe256_sample1pct", "sample_cells": int(len(gids)), "stencil_cells": int(len(st)),
            "gn_iters": gn_iters, "steps_timed": steps}
     learned.dec = tuple(t.to(torch.bfloat16).float() if t.dim() == 2 else t for t in learned.dec)
-    for kind, rom in (("affine", R.affine_lspg(setup, phi, ps, s2st, st)),
-                      ("mlp_fp32", learned.lspg(ps, s2st, st, tensor_cores=False)),
-                      ("mlp_tensor_cores", learned.lspg(ps, s2st, st, tensor_cores=True))):
+    # the first three with the exact (double) Jacobian, the last two with its
+    # terms in single precision (the ROM's default: an inexact Gauss-Newton step)
+    for kind, rom in (("affine", R.affine_lspg(setup, phi, ps, s2st, st, jacobian_bits=64)),
+                      ("mlp_fp32", learned.lspg(ps, s2st, st, tensor_cores=False, jacobian_bits=64)),
+                      ("mlp_tensor_cores", learned.lspg(ps, s2st, st, tensor_cores=True, jacobian_bits=64)),
+                      ("affine_jac32", R.affine_lspg(setup, phi, ps, s2st, st, jacobian_bits=32)),
+                      ("mlp_tensor_cores_jac32", learned.lspg(ps, s2st, st, tensor_cores=True, jacobian_bits=32))):
         x = torch.zeros(latent, dtype=torch.float64, device="cuda")
         rom.advance_bdf1(x, 0.02, 2, gn_iters, 0.0)  # capture + warm-up; tol 0: every iteration runs
         setup.stream.synchronize()

@@ -362,6 +362,15 @@ pda_status pda_lspg_advance_bdf1(pda_lspg *rom, double *d_x, double dt, int64_t 
  * to rounding. */
 pda_status pda_lspg_set_fused(pda_lspg *rom, int fused);
 
+/* Precision of the Jacobian terms in the fused iteration: 64 (default) the
+ * exact Jacobian of the sample-mesh residual in double; 32 the reconstruction
+ * gradients, flux Jacobians and the Jacobian-times-basis product in single
+ * precision, an inexact Gauss-Newton step (relative perturbation ~1e-7 of
+ * the step) on the same double-precision velocity, residual, normal
+ * equations and solve.  No counterpart in the reference (which has no ROM);
+ * the assembled form (fused = 0) is always double. */
+pda_status pda_lspg_set_jacobian_precision(pda_lspg *rom, int bits);
+
 /* Implicit steps on the device (the consumer of the Jacobian in the
  * reference's implicit tests, tests_cpp/eigen_2d_euler_riemann_implicit/
  * main.cc:31-44: Pressio's implicit stepper + Newton-Raphson + BiCGSTAB).

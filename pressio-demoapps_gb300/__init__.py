@@ -155,6 +155,7 @@ _SIGS = {
                                        C.c_double, C.c_int, C.c_double, C.c_int, C.c_void_p]),
     "pda_lspg_decode": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "pda_lspg_set_fused": (C.c_int, [C.c_void_p, C.c_int]),
+    "pda_lspg_set_jacobian_precision": (C.c_int, [C.c_void_p, C.c_int]),
     "pda_lspg_advance_bdf1": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int64, C.c_int, C.c_double,
                                         C.c_int, C.c_void_p]),
 }
@@ -791,6 +792,12 @@ class LspgRom:
         """Fused Gauss-Newton iteration (default) or the assembled sample-mesh
         Jacobian path; the same LSPG iteration, equal to rounding."""
         _check(lib().pda_lspg_set_fused(self._h, 1 if fused else 0))
+
+    def set_jacobian_precision(self, bits=64):
+        """64 (default): the exact Jacobian of the sample-mesh residual; 32: its
+        terms in single precision (an inexact Gauss-Newton step on the same
+        double-precision residual and normal equations; fused form only)."""
+        _check(lib().pda_lspg_set_jacobian_precision(self._h, int(bits)))
 
     def decode(self, x):
         import torch

@@ -132,11 +132,17 @@ int lspg_fused_blocks(int scheme, int innerRows, int nearRows, int K) {
   return div_up(innerRows, rpb) + div_up(nearRows, rpb);
 }
 
-void lspg_fused_prepare() {
+template <typename JT>
+void lspg_fused_prepare_t() {
   const int bytes = (int)FusedPar<FAM>::kSmemLimit;
-  cudaFuncSetAttribute(k_lspg_fused<FAM, FirstOrder>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  cudaFuncSetAttribute(k_lspg_fused<FAM, Weno3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  cudaFuncSetAttribute(k_lspg_fused<FAM, Weno5>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_lspg_fused<FAM, FirstOrder, JT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_lspg_fused<FAM, Weno3, JT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_lspg_fused<FAM, Weno5, JT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+void lspg_fused_prepare() {
+  lspg_fused_prepare_t<double>();
+  lspg_fused_prepare_t<float>();
 }
 
 void lspg_fused(int scheme, const RowTable &ti, const RowTable &tn, const MeshArgs &m, const Phys &p,
@@ -147,10 +153,18 @@ void lspg_fused(int scheme, const RowTable &ti, const RowTable &tn, const MeshAr
   if (nb <= 0) return;
   constexpr int T = FusedPar<FAM>::THREADS;
   const size_t sm = (size_t)rpb * FusedPar<FAM>::smem_row(2 * (scheme + 1) + 1, a.K);
+  if (a.jac32) {
+    switch (scheme) {
+      case FirstOrder: k_lspg_fused<FAM, FirstOrder, float><<<nb, T, sm, s>>>(ti, tn, rpb, nbI, m, p, a); break;
+      case Weno3: k_lspg_fused<FAM, Weno3, float><<<nb, T, sm, s>>>(ti, tn, rpb, nbI, m, p, a); break;
+      default: k_lspg_fused<FAM, Weno5, float><<<nb, T, sm, s>>>(ti, tn, rpb, nbI, m, p, a); break;
+    }
+    return;
+  }
   switch (scheme) {
-    case FirstOrder: k_lspg_fused<FAM, FirstOrder><<<nb, T, sm, s>>>(ti, tn, rpb, nbI, m, p, a); break;
-    case Weno3: k_lspg_fused<FAM, Weno3><<<nb, T, sm, s>>>(ti, tn, rpb, nbI, m, p, a); break;
-    default: k_lspg_fused<FAM, Weno5><<<nb, T, sm, s>>>(ti, tn, rpb, nbI, m, p, a); break;
+    case FirstOrder: k_lspg_fused<FAM, FirstOrder, double><<<nb, T, sm, s>>>(ti, tn, rpb, nbI, m, p, a); break;
+    case Weno3: k_lspg_fused<FAM, Weno3, double><<<nb, T, sm, s>>>(ti, tn, rpb, nbI, m, p, a); break;
+    default: k_lspg_fused<FAM, Weno5, double><<<nb, T, sm, s>>>(ti, tn, rpb, nbI, m, p, a); break;
   }
 }
 

@@ -31,10 +31,9 @@ template <> struct Fam<Euler1d> {
   static PDA_HD void flux(double F[3], const double qL[3], const double qR[3], const Phys &p) {
     euler3_flux(F, qL, qR, p.gamma);
   }
-  template <int AXIS>
-  static PDA_HD void flux_jac(double JL[9], double JR[9], const double qL[3], const double qR[3],
-                              const Phys &p) {
-    euler3_flux_jac(JL, JR, qL, qR, p.gamma);
+  template <int AXIS, typename T>
+  static PDA_HD void flux_jac(T JL[9], T JR[9], const T qL[3], const T qR[3], const Phys &p) {
+    euler3_flux_jac(JL, JR, qL, qR, (T)p.gamma);
   }
 };
 template <> struct Fam<Euler2d> {
@@ -43,10 +42,9 @@ template <> struct Fam<Euler2d> {
   static PDA_HD void flux(double F[4], const double qL[4], const double qR[4], const Phys &p) {
     euler4_flux<AXIS>(F, qL, qR, p.gamma);
   }
-  template <int AXIS>
-  static PDA_HD void flux_jac(double JL[16], double JR[16], const double qL[4], const double qR[4],
-                              const Phys &p) {
-    euler4_flux_jac<AXIS>(JL, JR, qL, qR, p.gamma);
+  template <int AXIS, typename T>
+  static PDA_HD void flux_jac(T JL[16], T JR[16], const T qL[4], const T qR[4], const Phys &p) {
+    euler4_flux_jac<AXIS>(JL, JR, qL, qR, (T)p.gamma);
   }
 };
 template <> struct Fam<Euler3d> {
@@ -55,10 +53,9 @@ template <> struct Fam<Euler3d> {
   static PDA_HD void flux(double F[5], const double qL[5], const double qR[5], const Phys &p) {
     euler5_flux<AXIS>(F, qL, qR, p.gamma);
   }
-  template <int AXIS>
-  static PDA_HD void flux_jac(double JL[25], double JR[25], const double qL[5], const double qR[5],
-                              const Phys &p) {
-    euler5_flux_jac<AXIS>(JL, JR, qL, qR, p.gamma);
+  template <int AXIS, typename T>
+  static PDA_HD void flux_jac(T JL[25], T JR[25], const T qL[5], const T qR[5], const Phys &p) {
+    euler5_flux_jac<AXIS>(JL, JR, qL, qR, (T)p.gamma);
   }
 };
 template <> struct Fam<Swe2d> {
@@ -67,10 +64,9 @@ template <> struct Fam<Swe2d> {
   static PDA_HD void flux(double F[3], const double qL[3], const double qR[3], const Phys &p) {
     swe_flux<AXIS>(F, qL, qR, p.gravity);
   }
-  template <int AXIS>
-  static PDA_HD void flux_jac(double JL[9], double JR[9], const double qL[3], const double qR[3],
-                              const Phys &p) {
-    swe_flux_jac<AXIS>(JL, JR, qL, qR, p.gravity);
+  template <int AXIS, typename T>
+  static PDA_HD void flux_jac(T JL[9], T JR[9], const T qL[3], const T qR[3], const Phys &p) {
+    swe_flux_jac<AXIS>(JL, JR, qL, qR, (T)p.gravity);
   }
 };
 
@@ -133,12 +129,12 @@ PDA_HD double face_value_side(int side, const double *q) {
   }
 }
 
-template <int SCHEME>
-PDA_HD void face_grad_side(int side, double &u, double g[2 * SchemeTraits<SCHEME>::h], const double *q) {
+template <int SCHEME, typename T>
+PDA_HD void face_grad_side(int side, T &u, T g[2 * SchemeTraits<SCHEME>::h], const T *q) {
   if constexpr (SCHEME == FirstOrder) {
     u = q[side];
-    g[0] = side == 0 ? 1. : 0.;
-    g[1] = side == 0 ? 0. : 1.;
+    g[0] = side == 0 ? T(1) : T(0);
+    g[1] = side == 0 ? T(0) : T(1);
   } else if constexpr (SCHEME == Weno3) {
     if (side == 0) weno3_neg_grad(u, g, q[0], q[1], q[2], q[3]);
     else weno3_pos_grad(u, g, q[0], q[1], q[2], q[3]);

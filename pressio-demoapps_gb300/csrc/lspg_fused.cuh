@@ -158,12 +158,14 @@ __device__ inline void lspg_solve_rt(int K, int nparts, const double *__restrict
   }
 }
 
-template <int FAM, int SCHEME> struct FusedFace {
+// one face of a block's rows: the flux and face values in double, the
+// Jacobian terms in JT (double, or float for the inexact Gauss-Newton step)
+template <int FAM, int SCHEME, typename JT> struct FusedFace {
   static constexpr int NDPC = Fam<FAM>::ndpc, G = 2 * SchemeTraits<SCHEME>::h;
   double fl[NDPC];
-  double JN[NDPC * NDPC], JP[NDPC * NDPC];
-  double gN[NDPC][G], gP[NDPC][G];
   double uN[NDPC], uP[NDPC];
+  JT JN[NDPC * NDPC], JP[NDPC * NDPC];
+  JT gN[NDPC][G], gP[NDPC][G];
 };
 
 // 16-byte global -> shared copy that does not hold up the issuing warp
@@ -173,13 +175,17 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-template <int FAM, int SCHEME>
+// JT: the scalar type of the Jacobian terms (double: the exact Jacobian of
+// the sample-mesh residual; float: an approximate one, on GB300's far wider
+// FP32 units, for an inexact Gauss-Newton step on the same double residual)
+template <int FAM, int SCHEME, typename JT>
 __global__ void __launch_bounds__(FusedPar<FAM>::THREADS)
 k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p, LspgArgs a) {
   if (!a.first && a.f->converged) return;
   using F = Fam<FAM>;
   using FP = FusedPar<FAM>;
-  using FF = FusedFace<FAM, SCHEME>;
+  using FF = FusedFace<FAM, SCHEME, JT>;
+  constexpr bool kExact = sizeof(JT) == sizeof(double);
   constexpr int NDPC = F::ndpc, DIM = F::dim, H = SchemeTraits<SCHEME>::h, S = 2 * H + 1, G = 2 * H;
   constexpr int NF = FP::NF;
   __shared__ FF fd[FP::RPB_MAX][NF];
@@ -219,10 +225,18 @@ k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p,
       if (inner) {
 #pragma unroll
         for (int s = 0; s < G; ++s) q[s] = __ldg(a.y + (size_t)t.src[base + fs + s] * NDPC + d);
-        double u, gg[G];
-        face_grad_side<SCHEME>(side, u, gg, q);
-        double *gs = side == 0 ? o.gN[d] : o.gP[d];
-        (side == 0 ? o.uN : o.uP)[d] = u;
+        JT u, gg[G];
+        if constexpr (kExact) {
+          face_grad_side<SCHEME>(side, u, gg, q);
+        } else {
+          // the value in double (it enters V and R); the gradient in float
+          JT qf[G];
+#pragma unroll
+          for (int s = 0; s < G; ++s) qf[s] = (JT)q[s];
+          face_grad_side<SCHEME>(side, u, gg, qf);
+        }
+        JT *gs = side == 0 ? o.gN[d] : o.gP[d];
+        (side == 0 ? o.uN : o.uP)[d] = kExact ? (double)u : face_value_side<SCHEME>(side, q);
 #pragma unroll
         for (int s = 0; s < G; ++s) gs[s] = gg[s];
       } else {
@@ -292,10 +306,15 @@ k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p,
             for (int d = 0; d < NDPC; ++d) (s == 0 ? uN : uP)[d] = qe[d];
           }
         }
-        double JN[NDPC * NDPC], JP[NDPC * NDPC];
-        if (ax == 0) F::template flux_jac<0>(JN, JP, uN, uP, p);
-        if constexpr (DIM > 1) if (ax == 1) F::template flux_jac<1>(JN, JP, uN, uP, p);
-        if constexpr (DIM > 2) if (ax == 2) F::template flux_jac<2>(JN, JP, uN, uP, p);
+        JT JN[NDPC * NDPC], JP[NDPC * NDPC], vN[NDPC], vP[NDPC];
+#pragma unroll
+        for (int d = 0; d < NDPC; ++d) {
+          vN[d] = (JT)uN[d];
+          vP[d] = (JT)uP[d];
+        }
+        if (ax == 0) F::template flux_jac<0>(JN, JP, vN, vP, p);
+        if constexpr (DIM > 1) if (ax == 1) F::template flux_jac<1>(JN, JP, vN, vP, p);
+        if constexpr (DIM > 2) if (ax == 2) F::template flux_jac<2>(JN, JP, vN, vP, p);
         // one of the two per warp (the part is warp-uniform): the other's
         // arithmetic is dead and dropped
         if (part == 1) {
@@ -316,19 +335,19 @@ k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p,
     if (e >= t.nrows) continue;
     const FF &o = fd[rl][f];
     const double *Dax = sD + ((size_t)rl * DIM + ax) * S * CB;  // staged D of this axis' positions
-    double dN[NDPC], dP[NDPC];
+    JT dN[NDPC], dP[NDPC];
     if (inner) {
 #pragma unroll
       for (int d = 0; d < NDPC; ++d) {
-        dN[d] = 0.;
-        dP[d] = 0.;
+        dN[d] = JT(0);
+        dP[d] = JT(0);
       }
 #pragma unroll
       for (int s = 0; s < G; ++s) {
         const double *Ds = Dax + (size_t)(fs + s) * CB;
 #pragma unroll
         for (int d = 0; d < NDPC; ++d) {
-          const double dv = Ds[d * K + c];
+          const JT dv = (JT)Ds[d * K + c];
           dN[d] = fma(o.gN[d][s], dv, dN[d]);
           dP[d] = fma(o.gP[d][s], dv, dP[d]);
         }
@@ -344,19 +363,19 @@ k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p,
 #pragma unroll
         for (int d = 0; d < NDPC; ++d) {
           const double dv = Ds[d * K + c];
-          (s == 0 ? dN : dP)[d] = ghost ? fac[d] * dv : dv;
+          (s == 0 ? dN : dP)[d] = (JT)(ghost ? fac[d] * dv : dv);
         }
       }
     }
 #pragma unroll
     for (int k = 0; k < NDPC; ++k) {
-      double acc = 0.;
+      JT acc = JT(0);
 #pragma unroll
       for (int d = 0; d < NDPC; ++d) {
         acc = fma(o.JN[k * NDPC + d], dN[d], acc);
         acc = fma(o.JP[k * NDPC + d], dP[d], acc);
       }
-      ctb[(((size_t)rl * NF + f) * NDPC + k) * K + c] = acc;
+      ctb[(((size_t)rl * NF + f) * NDPC + k) * K + c] = (double)acc;
     }
   }
   __syncthreads();

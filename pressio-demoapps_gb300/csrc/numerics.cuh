@@ -9,6 +9,11 @@
 // double-precision result.  The few places that cannot be bit-identical are
 // marked "deviation" and are within the stated parity tolerance.
 //
+// The gradient and flux-Jacobian functions are templates on the scalar type:
+// T = double is the reference's arithmetic (every literal is a T, so the
+// double instantiation is the same expression tree); T = float serves the
+// reduced-order model's approximate Jacobians.
+//
 // Reference (pressio-demoapps, include/pressiodemoapps/...):
 //   impl/weno5.hpp:56-178   weno5           -> weno5_face
 //   impl/weno5.hpp:180-434  weno5WithGrad   -> weno5_face_grad
@@ -38,7 +43,7 @@ template <> struct SchemeTraits<FirstOrder> { static constexpr int h = 1; };
 template <> struct SchemeTraits<Weno3> { static constexpr int h = 2; };
 template <> struct SchemeTraits<Weno5> { static constexpr int h = 3; };
 
-PDA_HD double sq(double x) { return x * x; }
+template <typename T> PDA_HD T sq(T x) { return x * x; }
 // x^3 for the reference's std::pow(x, 3.) (glibc pow, correctly rounded in
 // all but pathological near-midpoint cases).  Computed with Dekker's exact
 // two-product: x*x = p + e and p*x = c + ce exactly, so x^3 = c + ce + e*x
@@ -65,16 +70,23 @@ PDA_HD double div_const(double x, double d, double r) {
   return fma(e, r, q0);
 }
 
+// Single precision, for the approximate (inexact Gauss-Newton) Jacobians of
+// the reduced-order model: no exact-rounding constructions are needed there.
+PDA_HD float cube(float x) { return x * x * x; }
+PDA_HD float div_const(float x, float, float r) { return x * r; }
+
 // k x + c rounded once, for k a power of two.  k x is then exact (for
 // |x| >= 2^-1020, far below any state or gradient value here), so the result
 // equals RN(RN(k x) + c), the separately rounded product and sum of the
 // reference's source, in one FP64 instruction instead of two.
-PDA_HD double fma_p2(double k, double x, double c) { return fma(k, x, c); }
+template <typename T>
+PDA_HD T fma_p2(T k, T x, T c) { return fma(k, x, c); }
 
 // x + k w for a tabulated constant k: a zero k makes the product exact (a
 // signed zero, or NaN for an infinite or NaN w, exactly as RN(k w)), so one
 // rounding; otherwise the two separate roundings of the source
-PDA_HD double add_table_prod(double x, double k, double w) { return k == 0. ? fma(k, w, x) : x + k * w; }
+template <typename T>
+PDA_HD T add_table_prod(T x, T k, T w) { return k == T(0.) ? fma(k, w, x) : x + k * w; }
 
 // The reference's WENO5 stencil expressions (impl/weno5.hpp), evaluated left
 // to right as in its source, with the power-of-two products fused:
@@ -85,13 +97,20 @@ PDA_HD double add_table_prod(double x, double k, double w) { return k == 0. ? fm
 //   w5_pMidL(a, b, c)  = -a + 5 b + 2 c
 //   w5_pMidR(a, b, c)  = 2 a + 5 b - c
 //   w5_pFarR(a, b, c)  = 11 a - 7 b + 2 c
-PDA_HD double w5_curv(double a, double m, double c) { return fma_p2(-2., m, a) + c; }
-PDA_HD double w5_slopeL(double a, double m, double c) { return fma_p2(-4., m, a) + 3. * c; }
-PDA_HD double w5_slopeR(double a, double m, double c) { return fma_p2(-4., m, 3. * a) + c; }
-PDA_HD double w5_pFarL(double a, double b, double c) { return fma_p2(2., a, -(7. * b)) + 11. * c; }
-PDA_HD double w5_pMidL(double a, double b, double c) { return fma_p2(2., c, -a + 5. * b); }
-PDA_HD double w5_pMidR(double a, double b, double c) { return fma_p2(2., a, 5. * b) - c; }
-PDA_HD double w5_pFarR(double a, double b, double c) { return fma_p2(2., c, 11. * a - 7. * b); }
+template <typename T>
+PDA_HD T w5_curv(T a, T m, T c) { return fma_p2(-T(2.), m, a) + c; }
+template <typename T>
+PDA_HD T w5_slopeL(T a, T m, T c) { return fma_p2(-T(4.), m, a) + T(3.) * c; }
+template <typename T>
+PDA_HD T w5_slopeR(T a, T m, T c) { return fma_p2(-T(4.), m, T(3.) * a) + c; }
+template <typename T>
+PDA_HD T w5_pFarL(T a, T b, T c) { return fma_p2(T(2.), a, -(T(7.) * b)) + T(11.) * c; }
+template <typename T>
+PDA_HD T w5_pMidL(T a, T b, T c) { return fma_p2(T(2.), c, -a + T(5.) * b); }
+template <typename T>
+PDA_HD T w5_pMidR(T a, T b, T c) { return fma_p2(T(2.), a, T(5.) * b) - c; }
+template <typename T>
+PDA_HD T w5_pFarR(T a, T b, T c) { return fma_p2(T(2.), c, T(11.) * a - T(7.) * b); }
 
 // ---------------------------------------------------------------------------
 // WENO5, one face i+1/2: uNeg from q_{i-2..i+2}, uPos from q_{i-1..i+3}.
@@ -167,135 +186,137 @@ PDA_HD void weno5_face(double &uNeg, double &uPos, double qim2, double qim1,
 // WENO5 with the gradient of the two face values with respect to the six
 // stencil values q_{i-2..i+3}: gNeg[5] == 0, gPos[0] == 0.
 // one side of weno5_face_grad: uNeg and its gradient
-PDA_HD void weno5_neg_grad(double &uNeg, double gNeg[6], double qim2, double qim1, double qi, double qip1, double qip2, double qip3) {
-  constexpr double epsilon = 1e-6;
-  constexpr double two = 2., three = 3., four = 4., five = 5., seven = 7.,
-                   eleven = 11.;
-  constexpr double oneOvfour = 1. / 4., oneOvsix = 1. / 6.,
-                   oneOvten = 1. / 10., threeOvten = 3. / 10.,
-                   sixOvten = 6. / 10., thirteenOvtwelve = 13. / 12.;
+template <typename T>
+PDA_HD void weno5_neg_grad(T &uNeg, T gNeg[6], T qim2, T qim1, T qi, T qip1, T qip2, T qip3) {
+  constexpr T epsilon = T(1e-6);
+  constexpr T two = T(2.), three = T(3.), four = T(4.), five = T(5.), seven = T(7.),
+                   eleven = T(11.);
+  constexpr T oneOvfour = T(1.) / T(4.), oneOvsix = T(1.) / T(6.),
+                   oneOvten = T(1.) / T(10.), threeOvten = T(3.) / T(10.),
+                   sixOvten = T(6.) / T(10.), thirteenOvtwelve = T(13.) / T(12.);
   {
-    const double p0 = w5_pFarL(qim2, qim1, qi) * oneOvsix;
-    const double p1 = w5_pMidL(qim1, qi, qip1) * oneOvsix;
-    const double p2 = w5_pMidR(qi, qip1, qip2) * oneOvsix;
-    const double dp0[5] = {1. / 3., -7. / 6., 11. / 6., 0., 0.};
-    const double dp1[5] = {0., -1. / 6., 5. / 6., 1. / 3., 0.};
-    const double dp2[5] = {0., 0., 1. / 3., 5. / 6., -1. / 6.};
-    const double B0 = thirteenOvtwelve * sq(w5_curv(qim2, qim1, qi)) +
+    const T p0 = w5_pFarL(qim2, qim1, qi) * oneOvsix;
+    const T p1 = w5_pMidL(qim1, qi, qip1) * oneOvsix;
+    const T p2 = w5_pMidR(qi, qip1, qip2) * oneOvsix;
+    const T dp0[5] = {T(1.) / T(3.), -T(7.) / T(6.), T(11.) / T(6.), T(0.), T(0.)};
+    const T dp1[5] = {T(0.), -T(1.) / T(6.), T(5.) / T(6.), T(1.) / T(3.), T(0.)};
+    const T dp2[5] = {T(0.), T(0.), T(1.) / T(3.), T(5.) / T(6.), -T(1.) / T(6.)};
+    const T B0 = thirteenOvtwelve * sq(w5_curv(qim2, qim1, qi)) +
                       oneOvfour * sq(w5_slopeL(qim2, qim1, qi));
-    const double B1 = thirteenOvtwelve * sq(w5_curv(qim1, qi, qip1)) +
+    const T B1 = thirteenOvtwelve * sq(w5_curv(qim1, qi, qip1)) +
                       oneOvfour * sq(qim1 - qip1);
-    const double B2 = thirteenOvtwelve * sq(w5_curv(qi, qip1, qip2)) +
+    const T B2 = thirteenOvtwelve * sq(w5_curv(qi, qip1, qip2)) +
                       oneOvfour * sq(w5_slopeR(qi, qip1, qip2));
     // derivative terms (impl/weno5.hpp:294-310), the products by 2 and 1/2 fused
-    const double X0 = 13. * w5_curv(qim2, qim1, qi), Y0 = w5_slopeL(qim2, qim1, qi);
-    const double X1 = 13. * fma_p2(-2., qi, qip1 + qim1), Y1 = qim1 - qip1;
-    const double X2 = 13. * w5_curv(qip2, qip1, qi), Y2 = w5_slopeL(qip2, qip1, qi);
-    double dB0[5], dB1[5], dB2[5];
-    dB0[0] = fma_p2(0.5, Y0, div_const(X0, 6., 1. / 6.));
-    dB0[1] = fma_p2(-2., Y0, div_const(-X0, 3., 1. / 3.));
-    dB0[2] = fma_p2(0.5, 3. * Y0, div_const(X0, 6., 1. / 6.));
-    dB0[3] = 0.;
-    dB0[4] = 0.;
-    dB1[0] = 0.;
-    dB1[1] = fma_p2(0.5, Y1, div_const(X1, 6., 1. / 6.));
-    dB1[2] = div_const(-X1, 3., 1. / 3.);
-    dB1[3] = fma_p2(-0.5, Y1, div_const(X1, 6., 1. / 6.));
-    dB1[4] = 0.;
-    dB2[0] = 0.;
-    dB2[1] = 0.;
-    dB2[2] = fma_p2(0.5, 3. * Y2, div_const(X2, 6., 1. / 6.));
-    dB2[3] = fma_p2(-2., Y2, div_const(-X2, 3., 1. / 3.));
-    dB2[4] = fma_p2(0.5, Y2, div_const(X2, 6., 1. / 6.));
-    const double alpha0 = oneOvten / sq(epsilon + B0);
-    const double alpha1 = sixOvten / sq(epsilon + B1);
-    const double alpha2 = threeOvten / sq(epsilon + B2);
-    const double alphaSInv = 1. / (alpha0 + alpha1 + alpha2);
-    const double c0 = -1. / (5. * cube(B0 + epsilon));
-    const double c1 = -6. / (5. * cube(B1 + epsilon));
-    const double c2 = -3. / (5. * cube(B2 + epsilon));
-    const double cS = -1. / sq(alpha2 + alpha1 + alpha0);
-    const double w0 = alpha0 * alphaSInv;
-    const double w1 = alpha1 * alphaSInv;
-    const double w2 = alpha2 * alphaSInv;
+    const T X0 = T(13.) * w5_curv(qim2, qim1, qi), Y0 = w5_slopeL(qim2, qim1, qi);
+    const T X1 = T(13.) * fma_p2(-T(2.), qi, qip1 + qim1), Y1 = qim1 - qip1;
+    const T X2 = T(13.) * w5_curv(qip2, qip1, qi), Y2 = w5_slopeL(qip2, qip1, qi);
+    T dB0[5], dB1[5], dB2[5];
+    dB0[0] = fma_p2(T(0.5), Y0, div_const(X0, T(6.), T(1.) / T(6.)));
+    dB0[1] = fma_p2(-T(2.), Y0, div_const(-X0, T(3.), T(1.) / T(3.)));
+    dB0[2] = fma_p2(T(0.5), T(3.) * Y0, div_const(X0, T(6.), T(1.) / T(6.)));
+    dB0[3] = T(0.);
+    dB0[4] = T(0.);
+    dB1[0] = T(0.);
+    dB1[1] = fma_p2(T(0.5), Y1, div_const(X1, T(6.), T(1.) / T(6.)));
+    dB1[2] = div_const(-X1, T(3.), T(1.) / T(3.));
+    dB1[3] = fma_p2(-T(0.5), Y1, div_const(X1, T(6.), T(1.) / T(6.)));
+    dB1[4] = T(0.);
+    dB2[0] = T(0.);
+    dB2[1] = T(0.);
+    dB2[2] = fma_p2(T(0.5), T(3.) * Y2, div_const(X2, T(6.), T(1.) / T(6.)));
+    dB2[3] = fma_p2(-T(2.), Y2, div_const(-X2, T(3.), T(1.) / T(3.)));
+    dB2[4] = fma_p2(T(0.5), Y2, div_const(X2, T(6.), T(1.) / T(6.)));
+    const T alpha0 = oneOvten / sq(epsilon + B0);
+    const T alpha1 = sixOvten / sq(epsilon + B1);
+    const T alpha2 = threeOvten / sq(epsilon + B2);
+    const T alphaSInv = T(1.) / (alpha0 + alpha1 + alpha2);
+    const T c0 = -T(1.) / (T(5.) * cube(B0 + epsilon));
+    const T c1 = -T(6.) / (T(5.) * cube(B1 + epsilon));
+    const T c2 = -T(3.) / (T(5.) * cube(B2 + epsilon));
+    const T cS = -T(1.) / sq(alpha2 + alpha1 + alpha0);
+    const T w0 = alpha0 * alphaSInv;
+    const T w1 = alpha1 * alphaSInv;
+    const T w2 = alpha2 * alphaSInv;
     for (int i = 0; i < 5; i++) {
-      const double da0 = c0 * dB0[i];
-      const double da1 = c1 * dB1[i];
-      const double da2 = c2 * dB2[i];
-      const double daS = cS * (da0 + da1 + da2);
-      double g = add_table_prod((da0 * alphaSInv + daS * alpha0) * p0, dp0[i], w0);
+      const T da0 = c0 * dB0[i];
+      const T da1 = c1 * dB1[i];
+      const T da2 = c2 * dB2[i];
+      const T daS = cS * (da0 + da1 + da2);
+      T g = add_table_prod((da0 * alphaSInv + daS * alpha0) * p0, dp0[i], w0);
       g += add_table_prod((da1 * alphaSInv + daS * alpha1) * p1, dp1[i], w1);
       g += add_table_prod((da2 * alphaSInv + daS * alpha2) * p2, dp2[i], w2);
       gNeg[i] = g;
     }
-    gNeg[5] = 0.;
+    gNeg[5] = T(0.);
     uNeg = w0 * p0 + w1 * p1 + w2 * p2;
   }
 }
 
 // one side of weno5_face_grad: uPos and its gradient
-PDA_HD void weno5_pos_grad(double &uPos, double gPos[6], double qim2, double qim1, double qi, double qip1, double qip2, double qip3) {
-  constexpr double epsilon = 1e-6;
-  constexpr double two = 2., three = 3., four = 4., five = 5., seven = 7.,
-                   eleven = 11.;
-  constexpr double oneOvfour = 1. / 4., oneOvsix = 1. / 6.,
-                   oneOvten = 1. / 10., threeOvten = 3. / 10.,
-                   sixOvten = 6. / 10., thirteenOvtwelve = 13. / 12.;
+template <typename T>
+PDA_HD void weno5_pos_grad(T &uPos, T gPos[6], T qim2, T qim1, T qi, T qip1, T qip2, T qip3) {
+  constexpr T epsilon = T(1e-6);
+  constexpr T two = T(2.), three = T(3.), four = T(4.), five = T(5.), seven = T(7.),
+                   eleven = T(11.);
+  constexpr T oneOvfour = T(1.) / T(4.), oneOvsix = T(1.) / T(6.),
+                   oneOvten = T(1.) / T(10.), threeOvten = T(3.) / T(10.),
+                   sixOvten = T(6.) / T(10.), thirteenOvtwelve = T(13.) / T(12.);
   {
-    const double p0 = w5_pMidL(qim1, qi, qip1) * oneOvsix;
-    const double p1 = w5_pMidR(qi, qip1, qip2) * oneOvsix;
-    const double p2 = w5_pFarR(qip1, qip2, qip3) * oneOvsix;
-    const double dp0[5] = {-1. / 6., 5. / 6., 1. / 3., 0., 0.};
-    const double dp1[5] = {0., 1. / 3., 5. / 6., -1. / 6., 0.};
-    const double dp2[5] = {0., 0., 11. / 6., -7. / 6., 1. / 3.};
-    const double B0 = thirteenOvtwelve * sq(w5_curv(qim1, qi, qip1)) +
+    const T p0 = w5_pMidL(qim1, qi, qip1) * oneOvsix;
+    const T p1 = w5_pMidR(qi, qip1, qip2) * oneOvsix;
+    const T p2 = w5_pFarR(qip1, qip2, qip3) * oneOvsix;
+    const T dp0[5] = {-T(1.) / T(6.), T(5.) / T(6.), T(1.) / T(3.), T(0.), T(0.)};
+    const T dp1[5] = {T(0.), T(1.) / T(3.), T(5.) / T(6.), -T(1.) / T(6.), T(0.)};
+    const T dp2[5] = {T(0.), T(0.), T(11.) / T(6.), -T(7.) / T(6.), T(1.) / T(3.)};
+    const T B0 = thirteenOvtwelve * sq(w5_curv(qim1, qi, qip1)) +
                       oneOvfour * sq(w5_slopeL(qim1, qi, qip1));
-    const double B1 = thirteenOvtwelve * sq(w5_curv(qi, qip1, qip2)) +
+    const T B1 = thirteenOvtwelve * sq(w5_curv(qi, qip1, qip2)) +
                       oneOvfour * sq(qi - qip2);
-    const double B2 = thirteenOvtwelve * sq(w5_curv(qip1, qip2, qip3)) +
+    const T B2 = thirteenOvtwelve * sq(w5_curv(qip1, qip2, qip3)) +
                       oneOvfour * sq(w5_slopeR(qip1, qip2, qip3));
     // derivative terms (impl/weno5.hpp:385-401), the products by 2, 4 and 1/2 fused
-    const double X0 = 13. * fma_p2(-2., qi, qip1 + qim1), Y0 = fma_p2(-4., qi, 3. * qip1 + qim1);
-    const double X1 = 13. * w5_curv(qip2, qip1, qi), Y1 = qi - qip2;
-    const double X2 = 13. * w5_curv(qip3, qip2, qip1), Y2 = w5_slopeL(qip3, qip2, qip1);
-    double dB0[5], dB1[5], dB2[5];
-    dB0[0] = fma_p2(0.5, Y0, div_const(X0, 6., 1. / 6.));
-    dB0[1] = fma_p2(-2., Y0, -div_const(X0, 3., 1. / 3.));
-    dB0[2] = fma_p2(0.5, 3. * Y0, div_const(X0, 6., 1. / 6.));
-    dB0[3] = 0.;
-    dB0[4] = 0.;
-    dB1[0] = 0.;
-    dB1[1] = fma_p2(0.5, Y1, div_const(X1, 6., 1. / 6.));
-    dB1[2] = div_const(-X1, 3., 1. / 3.);
-    dB1[3] = fma_p2(-0.5, Y1, div_const(X1, 6., 1. / 6.));
-    dB1[4] = 0.;
-    dB2[0] = 0.;
-    dB2[1] = 0.;
-    dB2[2] = fma_p2(0.5, 3. * Y2, div_const(X2, 6., 1. / 6.));
-    dB2[3] = fma_p2(-2., Y2, div_const(-X2, 3., 1. / 3.));
-    dB2[4] = fma_p2(0.5, Y2, div_const(X2, 6., 1. / 6.));
-    const double alpha0 = threeOvten / sq(epsilon + B0);
-    const double alpha1 = sixOvten / sq(epsilon + B1);
-    const double alpha2 = oneOvten / sq(epsilon + B2);
-    const double alphaSInv = 1. / (alpha0 + alpha1 + alpha2);
-    const double c0 = -3. / (5. * cube(B0 + epsilon));
-    const double c1 = -6. / (5. * cube(B1 + epsilon));
-    const double c2 = -1. / (5. * cube(B2 + epsilon));
-    const double cS = -1. / sq(alpha2 + alpha1 + alpha0);
-    const double w0 = alpha0 * alphaSInv;
-    const double w1 = alpha1 * alphaSInv;
-    const double w2 = alpha2 * alphaSInv;
+    const T X0 = T(13.) * fma_p2(-T(2.), qi, qip1 + qim1), Y0 = fma_p2(-T(4.), qi, T(3.) * qip1 + qim1);
+    const T X1 = T(13.) * w5_curv(qip2, qip1, qi), Y1 = qi - qip2;
+    const T X2 = T(13.) * w5_curv(qip3, qip2, qip1), Y2 = w5_slopeL(qip3, qip2, qip1);
+    T dB0[5], dB1[5], dB2[5];
+    dB0[0] = fma_p2(T(0.5), Y0, div_const(X0, T(6.), T(1.) / T(6.)));
+    dB0[1] = fma_p2(-T(2.), Y0, -div_const(X0, T(3.), T(1.) / T(3.)));
+    dB0[2] = fma_p2(T(0.5), T(3.) * Y0, div_const(X0, T(6.), T(1.) / T(6.)));
+    dB0[3] = T(0.);
+    dB0[4] = T(0.);
+    dB1[0] = T(0.);
+    dB1[1] = fma_p2(T(0.5), Y1, div_const(X1, T(6.), T(1.) / T(6.)));
+    dB1[2] = div_const(-X1, T(3.), T(1.) / T(3.));
+    dB1[3] = fma_p2(-T(0.5), Y1, div_const(X1, T(6.), T(1.) / T(6.)));
+    dB1[4] = T(0.);
+    dB2[0] = T(0.);
+    dB2[1] = T(0.);
+    dB2[2] = fma_p2(T(0.5), T(3.) * Y2, div_const(X2, T(6.), T(1.) / T(6.)));
+    dB2[3] = fma_p2(-T(2.), Y2, div_const(-X2, T(3.), T(1.) / T(3.)));
+    dB2[4] = fma_p2(T(0.5), Y2, div_const(X2, T(6.), T(1.) / T(6.)));
+    const T alpha0 = threeOvten / sq(epsilon + B0);
+    const T alpha1 = sixOvten / sq(epsilon + B1);
+    const T alpha2 = oneOvten / sq(epsilon + B2);
+    const T alphaSInv = T(1.) / (alpha0 + alpha1 + alpha2);
+    const T c0 = -T(3.) / (T(5.) * cube(B0 + epsilon));
+    const T c1 = -T(6.) / (T(5.) * cube(B1 + epsilon));
+    const T c2 = -T(1.) / (T(5.) * cube(B2 + epsilon));
+    const T cS = -T(1.) / sq(alpha2 + alpha1 + alpha0);
+    const T w0 = alpha0 * alphaSInv;
+    const T w1 = alpha1 * alphaSInv;
+    const T w2 = alpha2 * alphaSInv;
     for (int i = 0; i < 5; i++) {
-      const double da0 = c0 * dB0[i];
-      const double da1 = c1 * dB1[i];
-      const double da2 = c2 * dB2[i];
-      const double daS = cS * (da0 + da1 + da2);
-      double g = add_table_prod((da0 * alphaSInv + daS * alpha0) * p0, dp0[i], w0);
+      const T da0 = c0 * dB0[i];
+      const T da1 = c1 * dB1[i];
+      const T da2 = c2 * dB2[i];
+      const T daS = cS * (da0 + da1 + da2);
+      T g = add_table_prod((da0 * alphaSInv + daS * alpha0) * p0, dp0[i], w0);
       g += add_table_prod((da1 * alphaSInv + daS * alpha1) * p1, dp1[i], w1);
       g += add_table_prod((da2 * alphaSInv + daS * alpha2) * p2, dp2[i], w2);
       gPos[i + 1] = g;
     }
-    gPos[0] = 0.;
+    gPos[0] = T(0.);
     uPos = w0 * p0 + w1 * p1 + w2 * p2;
   }
 }
@@ -360,81 +381,83 @@ PDA_HD void weno3_face(double &uNeg, double &uPos, double qim1, double qi,
 
 // WENO3 with gradients with respect to q_{i-1..i+2}: gNeg[3] == 0, gPos[0] == 0.
 // one side of weno3_face_grad: uNeg and its gradient
-PDA_HD void weno3_neg_grad(double &uNeg, double gNeg[4], double qim1, double qi, double qip1, double qip2) {
-  constexpr double epsilon = 1e-6;
-  constexpr double two = 2., three = 3.;
-  constexpr double oneOvtwo = 1. / 2., oneOvthree = 1. / 3., twoOvthree = 2. / 3.;
+template <typename T>
+PDA_HD void weno3_neg_grad(T &uNeg, T gNeg[4], T qim1, T qi, T qip1, T qip2) {
+  constexpr T epsilon = T(1e-6);
+  constexpr T two = T(2.), three = T(3.);
+  constexpr T oneOvtwo = T(1.) / T(2.), oneOvthree = T(1.) / T(3.), twoOvthree = T(2.) / T(3.);
   {
-    const double p0 = (-qim1 + three * qi) * oneOvtwo;
-    const double p1 = (qi + qip1) * oneOvtwo;
-    const double dp0[3] = {-1. / 2., 3. / 2., 0.};
-    const double dp1[3] = {0., 1. / 2., 1. / 2.};
-    const double B0 = (qim1 - qi) * (qim1 - qi);
-    const double B1 = (qi - qip1) * (qi - qip1);
-    const double alpha0 = oneOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
-    const double alpha1 = twoOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
-    const double alphaSInv = 1. / (alpha0 + alpha1);
-    const double e0 = sq(qim1 - qi) + epsilon;  // pow(pow(qim1-qi,2.)+eps, .)
-    const double e1 = sq(qi - qip1) + epsilon;
-    const double A = 2. / (3. * sq(e1)) + 1. / (3. * sq(e0));
-    double da0[3], da1[3], daS[3];
-    da0[0] = -4. * (qim1 - qi) / (3. * cube(e0));
-    da0[1] = 4. * (qim1 - qi) / (3. * cube(e0));
-    da0[2] = 0.;
-    da1[0] = 0.;
-    da1[1] = -8. * (qi - qip1) / (3. * cube(e1));
-    da1[2] = 8. * (qi - qip1) / (3. * cube(e1));
-    daS[0] = (4. * (qim1 - qi)) / (3. * cube(e0) * sq(A));
-    daS[1] = -((4. * (qim1 - qi)) / (3. * cube(e0)) - (8. * (qi - qip1)) / (3. * cube(e1))) / sq(A);
-    daS[2] = -(8. * (qi - qip1)) / (3. * sq(A) * cube(e1));
-    const double w0 = alpha0 * alphaSInv;
-    const double w1 = alpha1 * alphaSInv;
+    const T p0 = (-qim1 + three * qi) * oneOvtwo;
+    const T p1 = (qi + qip1) * oneOvtwo;
+    const T dp0[3] = {-T(1.) / T(2.), T(3.) / T(2.), T(0.)};
+    const T dp1[3] = {T(0.), T(1.) / T(2.), T(1.) / T(2.)};
+    const T B0 = (qim1 - qi) * (qim1 - qi);
+    const T B1 = (qi - qip1) * (qi - qip1);
+    const T alpha0 = oneOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
+    const T alpha1 = twoOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
+    const T alphaSInv = T(1.) / (alpha0 + alpha1);
+    const T e0 = sq(qim1 - qi) + epsilon;  // pow(pow(qim1-qi,2.)+eps, .)
+    const T e1 = sq(qi - qip1) + epsilon;
+    const T A = T(2.) / (T(3.) * sq(e1)) + T(1.) / (T(3.) * sq(e0));
+    T da0[3], da1[3], daS[3];
+    da0[0] = -T(4.) * (qim1 - qi) / (T(3.) * cube(e0));
+    da0[1] = T(4.) * (qim1 - qi) / (T(3.) * cube(e0));
+    da0[2] = T(0.);
+    da1[0] = T(0.);
+    da1[1] = -T(8.) * (qi - qip1) / (T(3.) * cube(e1));
+    da1[2] = T(8.) * (qi - qip1) / (T(3.) * cube(e1));
+    daS[0] = (T(4.) * (qim1 - qi)) / (T(3.) * cube(e0) * sq(A));
+    daS[1] = -((T(4.) * (qim1 - qi)) / (T(3.) * cube(e0)) - (T(8.) * (qi - qip1)) / (T(3.) * cube(e1))) / sq(A);
+    daS[2] = -(T(8.) * (qi - qip1)) / (T(3.) * sq(A) * cube(e1));
+    const T w0 = alpha0 * alphaSInv;
+    const T w1 = alpha1 * alphaSInv;
     for (int i = 0; i < 3; i++) {
-      double g = (da0[i] * alphaSInv + daS[i] * alpha0) * p0 + dp0[i] * w0;
+      T g = (da0[i] * alphaSInv + daS[i] * alpha0) * p0 + dp0[i] * w0;
       g += (da1[i] * alphaSInv + daS[i] * alpha1) * p1 + dp1[i] * w1;
       gNeg[i] = g;
     }
-    gNeg[3] = 0.;
+    gNeg[3] = T(0.);
     uNeg = w0 * p0 + w1 * p1;
   }
 }
 
 // one side of weno3_face_grad: uPos and its gradient
-PDA_HD void weno3_pos_grad(double &uPos, double gPos[4], double qim1, double qi, double qip1, double qip2) {
-  constexpr double epsilon = 1e-6;
-  constexpr double two = 2., three = 3.;
-  constexpr double oneOvtwo = 1. / 2., oneOvthree = 1. / 3., twoOvthree = 2. / 3.;
+template <typename T>
+PDA_HD void weno3_pos_grad(T &uPos, T gPos[4], T qim1, T qi, T qip1, T qip2) {
+  constexpr T epsilon = T(1e-6);
+  constexpr T two = T(2.), three = T(3.);
+  constexpr T oneOvtwo = T(1.) / T(2.), oneOvthree = T(1.) / T(3.), twoOvthree = T(2.) / T(3.);
   {
-    const double p0 = (qi + qip1) * oneOvtwo;
-    const double p1 = (three * qip1 - qip2) * oneOvtwo;
-    const double B0 = (qi - qip1) * (qi - qip1);
-    const double B1 = (qip1 - qip2) * (qip1 - qip2);
-    const double alpha0 = twoOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
-    const double alpha1 = oneOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
-    const double alphaSInv = 1. / (alpha0 + alpha1);
-    const double w0 = alpha0 * alphaSInv;
-    const double w1 = alpha1 * alphaSInv;
-    const double dp0[3] = {1. / 2., 1 / 2., 0.};
-    const double dp1[3] = {0., 3. / 2., -1. / 2.};
-    const double e0 = sq(qi - qip1) + epsilon;
-    const double e1 = sq(qip1 - qip2) + epsilon;
-    const double A = 1. / (3. * sq(e1)) + 2. / (3. * sq(e0));
-    double da0[3], da1[3], daS[3];
-    da0[0] = -8. * (qi - qip1) / (3. * cube(e0));
-    da0[1] = 8. * (qi - qip1) / (3. * cube(e0));
-    da0[2] = 0.;
-    da1[0] = 0.;
-    da1[1] = -4. * (qip1 - qip2) / (3. * cube(e1));
-    da1[2] = 4. * (qip1 - qip2) / (3. * cube(e1));
-    daS[0] = 8. * (qi - qip1) / (3. * cube(e0) * sq(A));
-    daS[1] = -(8. * (qi - qip1) / (3 * cube(e0)) - 4. * (qip1 - qip2) / (3. * cube(e1))) / sq(A);
-    daS[2] = -4. * (qip1 - qip2) / (3. * sq(A) * cube(e1));
+    const T p0 = (qi + qip1) * oneOvtwo;
+    const T p1 = (three * qip1 - qip2) * oneOvtwo;
+    const T B0 = (qi - qip1) * (qi - qip1);
+    const T B1 = (qip1 - qip2) * (qip1 - qip2);
+    const T alpha0 = twoOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
+    const T alpha1 = oneOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
+    const T alphaSInv = T(1.) / (alpha0 + alpha1);
+    const T w0 = alpha0 * alphaSInv;
+    const T w1 = alpha1 * alphaSInv;
+    const T dp0[3] = {T(1.) / T(2.), 1 / T(2.), T(0.)};
+    const T dp1[3] = {T(0.), T(3.) / T(2.), -T(1.) / T(2.)};
+    const T e0 = sq(qi - qip1) + epsilon;
+    const T e1 = sq(qip1 - qip2) + epsilon;
+    const T A = T(1.) / (T(3.) * sq(e1)) + T(2.) / (T(3.) * sq(e0));
+    T da0[3], da1[3], daS[3];
+    da0[0] = -T(8.) * (qi - qip1) / (T(3.) * cube(e0));
+    da0[1] = T(8.) * (qi - qip1) / (T(3.) * cube(e0));
+    da0[2] = T(0.);
+    da1[0] = T(0.);
+    da1[1] = -T(4.) * (qip1 - qip2) / (T(3.) * cube(e1));
+    da1[2] = T(4.) * (qip1 - qip2) / (T(3.) * cube(e1));
+    daS[0] = T(8.) * (qi - qip1) / (T(3.) * cube(e0) * sq(A));
+    daS[1] = -(T(8.) * (qi - qip1) / (3 * cube(e0)) - T(4.) * (qip1 - qip2) / (T(3.) * cube(e1))) / sq(A);
+    daS[2] = -T(4.) * (qip1 - qip2) / (T(3.) * sq(A) * cube(e1));
     for (int i = 0; i < 3; i++) {
-      double g = (da0[i] * alphaSInv + daS[i] * alpha0) * p0 + dp0[i] * w0;
+      T g = (da0[i] * alphaSInv + daS[i] * alpha0) * p0 + dp0[i] * w0;
       g += (da1[i] * alphaSInv + daS[i] * alpha1) * p1 + dp1[i] * w1;
       gPos[i + 1] = g;
     }
-    gPos[0] = 0.;
+    gPos[0] = T(0.);
     uPos = w0 * p0 + w1 * p1;
   }
 }
@@ -593,34 +616,35 @@ PDA_HD void swe_flux(double F[3], const double qL[3], const double qR[3],
 // Analytic Rusanov flux Jacobians JL = dF/dqL, JR = dF/dqR (row-major n x n).
 // These keep the reference's generic normal vector n.
 // ---------------------------------------------------------------------------
-PDA_HD void euler3_flux_jac(double JL[9], double JR[9], const double qL[3],
-                            const double qR[3], double gamma) {
-  constexpr double one = 1., two = 2., three = 3., half = 1. / 2.;
-  constexpr double es = 1.e-30;
-  const double gm1 = gamma - one;
-  const double rL = qL[0];
-  const double uL = qL[1] / (rL + es);
-  const double pL = gm1 * (qL[2] - half * rL * (uL * uL));
-  const double HL = (qL[2] + pL) / rL;
-  const double aL = sqrt(gm1 * (HL - half * (uL * uL)));
-  const double rR = qR[0];
-  const double uR = qR[1] / (rR + es);
-  const double pR = gm1 * (qR[2] - half * rR * (uR * uR));
-  const double HR = (qR[2] + pR) / rR;
-  const double aR = sqrt(gm1 * (HR - half * (uR * uR)));
-  const double r = sqrt(rR * rL);
-  const double RT = sqrt(rR / (rL));
-  const double u = (uL + RT * uR) / (one + RT);
-  const double H = (HL + RT * HR) / (one + RT);
-  const double a = sqrt(gm1 * (H - half * (u * u)));
-  const double smax = fabs(u) + a;
-  const double VMagSqrRoe = u * u + es;
-  const double VMagSqrL = uL * uL;
-  const double VVRoeL = uL * u;
-  const double VMagSqrR = uR * uR;
-  const double VVRoeR = uR * u;
-  const double uRelRoe = u / sqrt(VMagSqrRoe);
-  double gL[3], gR[3];
+template <typename T>
+PDA_HD void euler3_flux_jac(T JL[9], T JR[9], const T qL[3],
+                            const T qR[3], T gamma) {
+  constexpr T one = T(1.), two = T(2.), three = T(3.), half = T(1.) / T(2.);
+  constexpr T es = T(1.e-30);
+  const T gm1 = gamma - one;
+  const T rL = qL[0];
+  const T uL = qL[1] / (rL + es);
+  const T pL = gm1 * (qL[2] - half * rL * (uL * uL));
+  const T HL = (qL[2] + pL) / rL;
+  const T aL = sqrt(gm1 * (HL - half * (uL * uL)));
+  const T rR = qR[0];
+  const T uR = qR[1] / (rR + es);
+  const T pR = gm1 * (qR[2] - half * rR * (uR * uR));
+  const T HR = (qR[2] + pR) / rR;
+  const T aR = sqrt(gm1 * (HR - half * (uR * uR)));
+  const T r = sqrt(rR * rL);
+  const T RT = sqrt(rR / (rL));
+  const T u = (uL + RT * uR) / (one + RT);
+  const T H = (HL + RT * HR) / (one + RT);
+  const T a = sqrt(gm1 * (H - half * (u * u)));
+  const T smax = fabs(u) + a;
+  const T VMagSqrRoe = u * u + es;
+  const T VMagSqrL = uL * uL;
+  const T VVRoeL = uL * u;
+  const T VMagSqrR = uR * uR;
+  const T VVRoeR = uR * u;
+  const T uRelRoe = u / sqrt(VMagSqrRoe);
+  T gL[3], gR[3];
   gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe + half * gm1 / a * (fma_p2(half, VMagSqrRoe + VVRoeL, half * (HL - H)) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
   gL[1] = one / (rL + r) * (uRelRoe - half * (gm1 * (u + gm1 * uL)) / (a));
   gL[2] = half / (rL + r) * gamma * gm1 / (a);
@@ -655,42 +679,42 @@ PDA_HD void euler3_flux_jac(double JL[9], double JR[9], const double qL[3],
   }
 }
 
-template <int AXIS>
-PDA_HD void euler4_flux_jac(double JL[16], double JR[16], const double qL[4],
-                            const double qR[4], double gamma) {
-  constexpr double one = 1., two = 2., half = 1. / 2.;
-  constexpr double es = 1.e-30;
-  const double n[2] = {AXIS == 0 ? 1. : 0., AXIS == 1 ? 1. : 0.};
-  const double gm1 = gamma - one;
-  const double rL = qL[0];
-  const double uL = qL[1] / (rL + es);
-  const double vL = qL[2] / (rL + es);
-  const double unL = uL * n[0] + vL * n[1];
-  const double pL = gm1 * (qL[3] - half * rL * (uL * uL + vL * vL));
-  const double HL = (qL[3] + pL) / rL;
-  const double aL = sqrt(gm1 * (HL - half * (uL * uL + vL * vL)));
-  const double rR = qR[0];
-  const double uR = qR[1] / (rR + es);
-  const double vR = qR[2] / (rR + es);
-  const double unR = uR * n[0] + vR * n[1];
-  const double pR = gm1 * (qR[3] - half * rR * (uR * uR + vR * vR));
-  const double HR = (qR[3] + pR) / rR;
-  const double aR = sqrt(gm1 * (HR - half * (uR * uR + vR * vR)));
-  const double r = sqrt(rR * rL);
-  const double RT = sqrt(rR / (rL));
-  const double u = (uL + RT * uR) / (one + RT);
-  const double v = (vL + RT * vR) / (one + RT);
-  const double H = (HL + RT * HR) / (one + RT);
-  const double a = sqrt(gm1 * (H - half * (u * u + v * v)));
-  const double smax = sqrt(u * u + v * v) + a;
-  const double VMagSqrRoe = u * u + v * v + es;
-  const double VMagSqrL = uL * uL + vL * vL;
-  const double VVRoeL = uL * u + vL * v;
-  const double VMagSqrR = uR * uR + vR * vR;
-  const double VVRoeR = uR * u + vR * v;
-  const double uRelRoe = u / sqrt(VMagSqrRoe);
-  const double vRelRoe = v / sqrt(VMagSqrRoe);
-  double gL[4], gR[4];
+template <int AXIS, typename T>
+PDA_HD void euler4_flux_jac(T JL[16], T JR[16], const T qL[4],
+                            const T qR[4], T gamma) {
+  constexpr T one = T(1.), two = T(2.), half = T(1.) / T(2.);
+  constexpr T es = T(1.e-30);
+  const T n[2] = {AXIS == 0 ? T(1.) : T(0.), AXIS == 1 ? T(1.) : T(0.)};
+  const T gm1 = gamma - one;
+  const T rL = qL[0];
+  const T uL = qL[1] / (rL + es);
+  const T vL = qL[2] / (rL + es);
+  const T unL = uL * n[0] + vL * n[1];
+  const T pL = gm1 * (qL[3] - half * rL * (uL * uL + vL * vL));
+  const T HL = (qL[3] + pL) / rL;
+  const T aL = sqrt(gm1 * (HL - half * (uL * uL + vL * vL)));
+  const T rR = qR[0];
+  const T uR = qR[1] / (rR + es);
+  const T vR = qR[2] / (rR + es);
+  const T unR = uR * n[0] + vR * n[1];
+  const T pR = gm1 * (qR[3] - half * rR * (uR * uR + vR * vR));
+  const T HR = (qR[3] + pR) / rR;
+  const T aR = sqrt(gm1 * (HR - half * (uR * uR + vR * vR)));
+  const T r = sqrt(rR * rL);
+  const T RT = sqrt(rR / (rL));
+  const T u = (uL + RT * uR) / (one + RT);
+  const T v = (vL + RT * vR) / (one + RT);
+  const T H = (HL + RT * HR) / (one + RT);
+  const T a = sqrt(gm1 * (H - half * (u * u + v * v)));
+  const T smax = sqrt(u * u + v * v) + a;
+  const T VMagSqrRoe = u * u + v * v + es;
+  const T VMagSqrL = uL * uL + vL * vL;
+  const T VVRoeL = uL * u + vL * v;
+  const T VMagSqrR = uR * uR + vR * vR;
+  const T VVRoeR = uR * u + vR * v;
+  const T uRelRoe = u / sqrt(VMagSqrRoe);
+  const T vRelRoe = v / sqrt(VMagSqrRoe);
+  T gL[4], gR[4];
   gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe - half * (vL + v) * vRelRoe + half * gm1 / a * (fma_p2(half, VMagSqrRoe + VVRoeL, half * (HL - H)) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
   gL[1] = one / (rL + r) * (uRelRoe - half * (gm1 * (u + gm1 * uL)) / (a));
   gL[2] = one / (rL + r) * (vRelRoe - half * (gm1 * (v + gm1 * vL)) / (a));
@@ -743,46 +767,46 @@ PDA_HD void euler4_flux_jac(double JL[16], double JR[16], const double qL[4],
   }
 }
 
-template <int AXIS>
-PDA_HD void euler5_flux_jac(double JL[25], double JR[25], const double qL[5],
-                            const double qR[5], double gamma) {
-  constexpr double one = 1., two = 2., half = 1. / 2.;
-  constexpr double es = 1.e-30;
-  const double n[3] = {AXIS == 0 ? 1. : 0., AXIS == 1 ? 1. : 0., AXIS == 2 ? 1. : 0.};
-  const double gm1 = gamma - one;
-  const double rL = qL[0];
-  const double uL = qL[1] / (rL + es);
-  const double vL = qL[2] / (rL + es);
-  const double wL = qL[3] / (rL + es);
-  const double unL = uL * n[0] + vL * n[1] + wL * n[2];
-  const double pL = gm1 * (qL[4] - half * rL * (uL * uL + vL * vL + wL * wL));
-  const double HL = (qL[4] + pL) / rL;
-  const double aL = sqrt(gm1 * (HL - half * (uL * uL + vL * vL + wL * wL)));
-  const double rR = qR[0];
-  const double uR = qR[1] / (rR + es);
-  const double vR = qR[2] / (rR + es);
-  const double wR = qR[3] / (rR + es);
-  const double unR = uR * n[0] + vR * n[1] + wR * n[2];
-  const double pR = gm1 * (qR[4] - half * rR * (uR * uR + vR * vR + wR * wR));
-  const double HR = (qR[4] + pR) / rR;
-  const double aR = sqrt(gm1 * (HR - half * (uR * uR + vR * vR + wR * wR)));
-  const double r = sqrt(rR * rL);
-  const double RT = sqrt(rR / (rL));
-  const double u = (uL + RT * uR) / (one + RT);
-  const double v = (vL + RT * vR) / (one + RT);
-  const double w = (wL + RT * wR) / (one + RT);
-  const double H = (HL + RT * HR) / (one + RT);
-  const double a = sqrt(gm1 * (H - half * (u * u + v * v + w * w)));
-  const double smax = sqrt(u * u + v * v + w * w) + a;
-  const double VMagSqrRoe = u * u + v * v + w * w + es;
-  const double VMagSqrL = uL * uL + vL * vL + wL * wL;
-  const double VVRoeL = uL * u + vL * v + wL * w;
-  const double VMagSqrR = uR * uR + vR * vR + wR * wR;
-  const double VVRoeR = uR * u + vR * v + wR * w;
-  const double uRelRoe = u / sqrt(VMagSqrRoe);
-  const double vRelRoe = v / sqrt(VMagSqrRoe);
-  const double wRelRoe = w / sqrt(VMagSqrRoe);
-  double gL[5], gR[5];
+template <int AXIS, typename T>
+PDA_HD void euler5_flux_jac(T JL[25], T JR[25], const T qL[5],
+                            const T qR[5], T gamma) {
+  constexpr T one = T(1.), two = T(2.), half = T(1.) / T(2.);
+  constexpr T es = T(1.e-30);
+  const T n[3] = {AXIS == 0 ? T(1.) : T(0.), AXIS == 1 ? T(1.) : T(0.), AXIS == 2 ? T(1.) : T(0.)};
+  const T gm1 = gamma - one;
+  const T rL = qL[0];
+  const T uL = qL[1] / (rL + es);
+  const T vL = qL[2] / (rL + es);
+  const T wL = qL[3] / (rL + es);
+  const T unL = uL * n[0] + vL * n[1] + wL * n[2];
+  const T pL = gm1 * (qL[4] - half * rL * (uL * uL + vL * vL + wL * wL));
+  const T HL = (qL[4] + pL) / rL;
+  const T aL = sqrt(gm1 * (HL - half * (uL * uL + vL * vL + wL * wL)));
+  const T rR = qR[0];
+  const T uR = qR[1] / (rR + es);
+  const T vR = qR[2] / (rR + es);
+  const T wR = qR[3] / (rR + es);
+  const T unR = uR * n[0] + vR * n[1] + wR * n[2];
+  const T pR = gm1 * (qR[4] - half * rR * (uR * uR + vR * vR + wR * wR));
+  const T HR = (qR[4] + pR) / rR;
+  const T aR = sqrt(gm1 * (HR - half * (uR * uR + vR * vR + wR * wR)));
+  const T r = sqrt(rR * rL);
+  const T RT = sqrt(rR / (rL));
+  const T u = (uL + RT * uR) / (one + RT);
+  const T v = (vL + RT * vR) / (one + RT);
+  const T w = (wL + RT * wR) / (one + RT);
+  const T H = (HL + RT * HR) / (one + RT);
+  const T a = sqrt(gm1 * (H - half * (u * u + v * v + w * w)));
+  const T smax = sqrt(u * u + v * v + w * w) + a;
+  const T VMagSqrRoe = u * u + v * v + w * w + es;
+  const T VMagSqrL = uL * uL + vL * vL + wL * wL;
+  const T VVRoeL = uL * u + vL * v + wL * w;
+  const T VMagSqrR = uR * uR + vR * vR + wR * wR;
+  const T VVRoeR = uR * u + vR * v + wR * w;
+  const T uRelRoe = u / sqrt(VMagSqrRoe);
+  const T vRelRoe = v / sqrt(VMagSqrRoe);
+  const T wRelRoe = w / sqrt(VMagSqrRoe);
+  T gL[5], gR[5];
   gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe - half * (vL + v) * vRelRoe - half * (wL + w) * wRelRoe + half * gm1 / a * (fma_p2(half, VMagSqrRoe + VVRoeL, half * (HL - H)) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
   gL[1] = one / (rL + r) * (uRelRoe - half * (gm1 * (u + gm1 * uL)) / (a));
   gL[2] = one / (rL + r) * (vRelRoe - half * (gm1 * (v + gm1 * vL)) / (a));
@@ -835,57 +859,57 @@ PDA_HD void euler5_flux_jac(double JL[25], double JR[25], const double qL[5],
 
 // Shallow-water Rusanov flux Jacobian (generic normal).  deviation: pow(x,0.5)
 // -> sqrt(x); pow(2,3/2) is the correctly rounded constant 2*sqrt(2).
-template <int AXIS>
-PDA_HD void swe_flux_jac(double JL[9], double JR[9], const double qL[3],
-                         const double qR[3], double g) {
-  constexpr double es = 1.e-30;
-  const double n[2] = {AXIS == 0 ? 1. : 0., AXIS == 1 ? 1. : 0.};
-  const double hL = qL[0];
-  const double uL = qL[1] / (hL + es);
-  const double vL = qL[2] / (hL + es);
-  const double unL = uL * n[0] + vL * n[1];
-  const double hR = qR[0];
-  const double uR = qR[1] / (hR + es);
-  const double vR = qR[2] / (hR + es);
-  const double unR = uR * n[0] + vR * n[1];
-  const double hm = 0.5 * (hL + hR);
-  const double hL_sqrt = sqrt(hL);
-  const double hR_sqrt = sqrt(hR);
-  const double um = (unL * hL_sqrt + unR * hR_sqrt) / (hL_sqrt + hR_sqrt + es);
-  const double smax = fabs(um) + fabs(sqrt(g * hm));
-  const double termL = (n[0] * qL[1] + n[1] * qL[2]) / sq(qL[0]);
-  const double termR = (n[0] * qR[1] + n[1] * qR[2]) / sq(qR[0]);
-  const double hsqrt_un = hL_sqrt * unL + hR_sqrt * unR + es;
-  const double two_pow_1p5 = 2. * sqrt(2.);
-  double dL[3], dR[3];
-  dL[0] = -fabs(hsqrt_un) / (2. * hL_sqrt * sq(hL_sqrt + hR_sqrt)) +
-          (0.5 * unL / hL_sqrt - hL_sqrt * termL) * hsqrt_un / ((hL_sqrt + hR_sqrt) * fabs(hsqrt_un)) +
+template <int AXIS, typename T>
+PDA_HD void swe_flux_jac(T JL[9], T JR[9], const T qL[3],
+                         const T qR[3], T g) {
+  constexpr T es = T(1.e-30);
+  const T n[2] = {AXIS == 0 ? T(1.) : T(0.), AXIS == 1 ? T(1.) : T(0.)};
+  const T hL = qL[0];
+  const T uL = qL[1] / (hL + es);
+  const T vL = qL[2] / (hL + es);
+  const T unL = uL * n[0] + vL * n[1];
+  const T hR = qR[0];
+  const T uR = qR[1] / (hR + es);
+  const T vR = qR[2] / (hR + es);
+  const T unR = uR * n[0] + vR * n[1];
+  const T hm = T(0.5) * (hL + hR);
+  const T hL_sqrt = sqrt(hL);
+  const T hR_sqrt = sqrt(hR);
+  const T um = (unL * hL_sqrt + unR * hR_sqrt) / (hL_sqrt + hR_sqrt + es);
+  const T smax = fabs(um) + fabs(sqrt(g * hm));
+  const T termL = (n[0] * qL[1] + n[1] * qL[2]) / sq(qL[0]);
+  const T termR = (n[0] * qR[1] + n[1] * qR[2]) / sq(qR[0]);
+  const T hsqrt_un = hL_sqrt * unL + hR_sqrt * unR + es;
+  const T two_pow_1p5 = T(2.) * sqrt(T(2.));
+  T dL[3], dR[3];
+  dL[0] = -fabs(hsqrt_un) / (T(2.) * hL_sqrt * sq(hL_sqrt + hR_sqrt)) +
+          (T(0.5) * unL / hL_sqrt - hL_sqrt * termL) * hsqrt_un / ((hL_sqrt + hR_sqrt) * fabs(hsqrt_un)) +
           g / (two_pow_1p5 * sqrt(g * (hL + hR)));
   dL[1] = n[0] * hsqrt_un / (hL_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
   dL[2] = n[1] * hsqrt_un / (hL_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
-  dR[0] = -fabs(hsqrt_un) / (2. * hR_sqrt * sq(hL_sqrt + hR_sqrt)) +
-          (0.5 * unR / hR_sqrt - hR_sqrt * termR) * hsqrt_un / ((hL_sqrt + hR_sqrt) * fabs(hsqrt_un)) +
+  dR[0] = -fabs(hsqrt_un) / (T(2.) * hR_sqrt * sq(hL_sqrt + hR_sqrt)) +
+          (T(0.5) * unR / hR_sqrt - hR_sqrt * termR) * hsqrt_un / ((hL_sqrt + hR_sqrt) * fabs(hsqrt_un)) +
           g / (two_pow_1p5 * sqrt(g * (hL + hR)));
   dR[1] = n[0] * hsqrt_un / (hR_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
   dR[2] = n[1] * hsqrt_un / (hR_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
-  JL[0] = -0.5 * dL[0] * (qR[0] - qL[0]) + 0.5 * (n[0] * uL + n[1] * vL - qL[0] * termL) + 0.5 * smax;
-  JL[1] = 0.5 * n[0] - 0.5 * dL[1] * (qR[0] - qL[0]);
-  JL[2] = 0.5 * n[1] - 0.5 * dL[2] * (qR[0] - qL[0]);
-  JL[3] = 0.5 * (g * n[0] * qL[0] - qL[1] * termL) - 0.5 * dL[0] * (qR[1] - qL[1]);
-  JL[4] = n[0] * uL + 0.5 * n[1] * vL + 0.5 * smax - 0.5 * dL[1] * (qR[1] - qL[1]);
-  JL[5] = 0.5 * n[1] * uL - 0.5 * dL[2] * (qR[1] - qL[1]);
-  JL[6] = 0.5 * (g * n[1] * qL[0] - qL[2] * termL) - 0.5 * dL[0] * (qR[2] - qL[2]);
-  JL[7] = 0.5 * n[0] * vL - 0.5 * dL[1] * (qR[2] - qL[2]);
-  JL[8] = n[1] * vL + 0.5 * n[0] * uL + 0.5 * smax - 0.5 * dL[2] * (qR[2] - qL[2]);
-  JR[0] = -0.5 * dR[0] * (qR[0] - qL[0]) + 0.5 * (n[0] * uR + n[1] * vR - qR[0] * termR) - 0.5 * smax;
-  JR[1] = 0.5 * n[0] - 0.5 * dR[1] * (qR[0] - qL[0]);
-  JR[2] = 0.5 * n[1] - 0.5 * dR[2] * (qR[0] - qL[0]);
-  JR[3] = 0.5 * (g * n[0] * qR[0] - qR[1] * termR) - 0.5 * dR[0] * (qR[1] - qL[1]);
-  JR[4] = n[0] * uR + 0.5 * n[1] * vR - 0.5 * smax - 0.5 * dR[1] * (qR[1] - qL[1]);
-  JR[5] = 0.5 * n[1] * uR - 0.5 * dR[2] * (qR[1] - qL[1]);
-  JR[6] = 0.5 * (g * n[1] * qR[0] - qR[2] * termR) - 0.5 * dR[0] * (qR[2] - qL[2]);
-  JR[7] = 0.5 * n[0] * vR - 0.5 * dR[1] * (qR[2] - qL[2]);
-  JR[8] = n[1] * vR + 0.5 * n[0] * uR - 0.5 * smax - 0.5 * dR[2] * (qR[2] - qL[2]);
+  JL[0] = -T(0.5) * dL[0] * (qR[0] - qL[0]) + T(0.5) * (n[0] * uL + n[1] * vL - qL[0] * termL) + T(0.5) * smax;
+  JL[1] = T(0.5) * n[0] - T(0.5) * dL[1] * (qR[0] - qL[0]);
+  JL[2] = T(0.5) * n[1] - T(0.5) * dL[2] * (qR[0] - qL[0]);
+  JL[3] = T(0.5) * (g * n[0] * qL[0] - qL[1] * termL) - T(0.5) * dL[0] * (qR[1] - qL[1]);
+  JL[4] = n[0] * uL + T(0.5) * n[1] * vL + T(0.5) * smax - T(0.5) * dL[1] * (qR[1] - qL[1]);
+  JL[5] = T(0.5) * n[1] * uL - T(0.5) * dL[2] * (qR[1] - qL[1]);
+  JL[6] = T(0.5) * (g * n[1] * qL[0] - qL[2] * termL) - T(0.5) * dL[0] * (qR[2] - qL[2]);
+  JL[7] = T(0.5) * n[0] * vL - T(0.5) * dL[1] * (qR[2] - qL[2]);
+  JL[8] = n[1] * vL + T(0.5) * n[0] * uL + T(0.5) * smax - T(0.5) * dL[2] * (qR[2] - qL[2]);
+  JR[0] = -T(0.5) * dR[0] * (qR[0] - qL[0]) + T(0.5) * (n[0] * uR + n[1] * vR - qR[0] * termR) - T(0.5) * smax;
+  JR[1] = T(0.5) * n[0] - T(0.5) * dR[1] * (qR[0] - qL[0]);
+  JR[2] = T(0.5) * n[1] - T(0.5) * dR[2] * (qR[0] - qL[0]);
+  JR[3] = T(0.5) * (g * n[0] * qR[0] - qR[1] * termR) - T(0.5) * dR[0] * (qR[1] - qL[1]);
+  JR[4] = n[0] * uR + T(0.5) * n[1] * vR - T(0.5) * smax - T(0.5) * dR[1] * (qR[1] - qL[1]);
+  JR[5] = T(0.5) * n[1] * uR - T(0.5) * dR[2] * (qR[1] - qL[1]);
+  JR[6] = T(0.5) * (g * n[1] * qR[0] - qR[2] * termR) - T(0.5) * dR[0] * (qR[2] - qL[2]);
+  JR[7] = T(0.5) * n[0] * vR - T(0.5) * dR[1] * (qR[2] - qL[2]);
+  JR[8] = n[1] * vR + T(0.5) * n[0] * uR - T(0.5) * smax - T(0.5) * dR[2] * (qR[2] - qL[2]);
 }
 
 }  // namespace pda

@@ -450,6 +450,7 @@ struct pda_lspg {
   // fused iteration (lspg_fused.cuh) or the assembled Jacobian path
   // (sample-mesh V + CSR J, then k_lspg_rows)
   bool fused = true;
+  bool jac32 = false;  // fused form: single-precision Jacobian terms
   int fusedBlocks = 0;
   cudaGraphExec_t graph = nullptr;
   double graphDt = 0;
@@ -502,7 +503,7 @@ void gn_iteration_k(pda_lspg &L, double *x, double dt, double tol, int first, cu
   decode_k<K>(L, x, L.y.p, first, s);
   if (L.fused) {
     pda_problem &P = *L.P;
-    LspgArgs a{L.y.p, L.D.p, K, -dt, L.yn.p, first, L.V.p, L.partial.p, L.ticket.p, x, tol, f};
+    LspgArgs a{L.y.p, L.D.p, K, -dt, L.yn.p, first, L.V.p, L.partial.p, L.ticket.p, x, tol, f, L.jac32 ? 1 : 0};
     MeshArgs ma = P.margs;
     ma.time = 0.0;
     P.L->lspg_fused(P.scheme, P.innerT.t, P.nearT.t, ma, P.phys, a, s);
@@ -715,6 +716,17 @@ pda_status pda_lspg_set_fused(pda_lspg *rom, int fused) {
     rom->graph = nullptr;
   }
   rom->fused = fused != 0;
+  PDA_API_END
+}
+
+pda_status pda_lspg_set_jacobian_precision(pda_lspg *rom, int bits) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(rom && (bits == 32 || bits == 64), PDA_ERR_INVALID_ARGUMENT, "bits must be 32 or 64");
+  if (rom->jac32 != (bits == 32) && rom->graph) {
+    cudaGraphExecDestroy(rom->graph);
+    rom->graph = nullptr;
+  }
+  rom->jac32 = bits == 32;
   PDA_API_END
 }
 

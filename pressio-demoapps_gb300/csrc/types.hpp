@@ -116,6 +116,9 @@ struct LspgArgs {
   double *x;         // latent state, updated in place
   double tol;
   LspgFlags *f;
+  int jac32;         // 1: reconstruction gradients, flux Jacobians and Jf D in
+                     // single precision (an inexact Gauss-Newton step; V, R, the
+                     // normal equations and the solve stay double)
 };
 
 struct BatchArgs {

@@ -166,16 +166,20 @@ class LearnedRom:
         _, Z = self.ae.reconstruct(x.contiguous())
         return Z[0].double().contiguous()
 
-    def lspg(self, problem, s2st, stencil_gids, tensor_cores=True):
+    def lspg(self, problem, s2st, stencil_gids, tensor_cores=True, jacobian_bits=32):
         """tensor_cores: the decoder's output layer as a bf16 tcgen05 GEMM (the
-        numerics the network was trained with); False: fp32 on CUDA cores."""
+        numerics the network was trained with); False: fp32 on CUDA cores.
+        jacobian_bits: 32 forms the Gauss-Newton Jacobian terms in single
+        precision (the residual and normal equations stay double), 64 exactly."""
         rows = stencil_rows(stencil_gids)
         import torch
         r = torch.from_numpy(rows).cuda()
         W1, b1, W2, b2, W3, b3 = self.dec
-        return self.setup.pda.LspgRom.mlp(problem, s2st, self.setup.uref[r].contiguous(),
-                                          self.scale[r].contiguous(), W1, b1, W2, b2, W3[r].contiguous(),
-                                          b3[r].contiguous(), tensor_cores=tensor_cores)
+        rom = self.setup.pda.LspgRom.mlp(problem, s2st, self.setup.uref[r].contiguous(),
+                                         self.scale[r].contiguous(), W1, b1, W2, b2, W3[r].contiguous(),
+                                         b3[r].contiguous(), tensor_cores=tensor_cores)
+        rom.set_jacobian_precision(jacobian_bits)
+        return rom
 
     def full_decoder(self):
         """The decoder on every row (error evaluation), through a full-mesh LSPG object."""
@@ -186,10 +190,12 @@ class LearnedRom:
         return s.pda.LspgRom.mlp(p, ident, s.uref, self.scale, W1, b1, W2, b2, W3, b3), p
 
 
-def affine_lspg(setup, phi, problem, s2st, stencil_gids):
+def affine_lspg(setup, phi, problem, s2st, stencil_gids, jacobian_bits=32):
     import torch
     r = torch.from_numpy(stencil_rows(stencil_gids)).cuda()
-    return setup.pda.LspgRom.affine(problem, s2st, setup.uref[r].contiguous(), phi[r].contiguous())
+    rom = setup.pda.LspgRom.affine(problem, s2st, setup.uref[r].contiguous(), phi[r].contiguous())
+    rom.set_jacobian_precision(jacobian_bits)
+    return rom
 
 
 def rel_l2(a, b, ref=None):
