@@ -58,39 +58,30 @@ __global__ void k_to_bf16_exact(const float *__restrict__ in, __nv_bfloat16 *__r
   if (__bfloat162float(b) != in[i]) *bad = 1;
 }
 
-// out[c][r] = in[r][c], R x C floats (set-up only)
-__global__ void k_transpose_f32(const float *__restrict__ in, float *__restrict__ out, long R, long C) {
-  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= R * C) return;
-  const long r = i / C, c = i % C;
-  out[c * R + r] = in[i];
-}
-
 __device__ __forceinline__ float elu_f(float a) { return a > 0.f ? a : expm1f(a); }
 __device__ __forceinline__ float delu_f(float a) { return a > 0.f ? 1.f : expf(a); }
 
 // hidden layers: every block recomputes layer 1 (h1 x k, tiny) in shared
-// memory, then its slice of layer 2: h2[r] and T2[r][c] = elu'(a2_r) (W2 T1)_rc
-// with T1 = diag(elu'(a1)) W1.  Output Z[r][0] = h2, Z[r][1 + c] = T2.
-// W2T is W2 transposed ([h1 x h2]).  Block = 64 output rows x 4 threads;
-// thread (row, q) sums j in [q H1/4, (q+1) H1/4), the four partial sums are
-// added in q order.  Every block recomputes layer 1 (h1 x k, tiny).  Output
-// Z[r][0] = h2, Z[r][1 + c] = T2 (fp32), and when Zb is given the same
-// values as bf16 rows [1 + k (padded to 16)][h2] for the tensor-core output
-// layer (B operand, K-major).
-__host__ __device__ constexpr int hidden_rows(int K) { return K <= 16 ? 64 : 16; }
+// memory, then layer 2 for its rows, one warp per row: h2[r] and
+// T2[r][c] = elu'(a2_r) (W2 T1)_rc with T1 = diag(elu'(a1)) W1.  The lanes
+// split the layer-1 width (coalesced reads of W2's row r), their 1 + k partial
+// sums are added by a butterfly of shuffles.  Output Z[r][0] = h2,
+// Z[r][1 + c] = T2 (fp32), and when Zb is given the same values as bf16 rows
+// [1 + k (padded to 16)][h2] for the tensor-core output layer (B operand,
+// K-major).
+constexpr int kHiddenWarps = 8;
 
 template <int K, int H1>
-__global__ void __launch_bounds__(hidden_rows(K) * 4)
-k_decode_hidden(int h2, const float *__restrict__ W1, const float *__restrict__ b1, const float *__restrict__ W2T,
+__global__ void __launch_bounds__(kHiddenWarps * 32)
+k_decode_hidden(int h2, const float *__restrict__ W1, const float *__restrict__ b1, const float *__restrict__ W2,
                 const float *__restrict__ b2, const double *__restrict__ x, float *__restrict__ Z,
                 __nv_bfloat16 *__restrict__ Zb, int first, const Flags *f) {
   if (!first && f->converged) return;
-  constexpr int RPB = hidden_rows(K), PARTS = 4, ld = 1 + K;
+  static_assert(H1 % 32 == 0, "layer-1 width a multiple of the warp");
+  constexpr int ld = 1 + K;
   __shared__ float sh1[H1];
-  __shared__ float sT1[H1][K];
+  __shared__ float sT1[H1][K + 1];  // odd row length: lanes j, j+1 hit different banks
   __shared__ float sx[K];
-  __shared__ float sp[PARTS][RPB][ld];
   if (threadIdx.x < K) sx[threadIdx.x] = (float)x[threadIdx.x];
   __syncthreads();
   for (int r = threadIdx.x; r < H1; r += blockDim.x) {
@@ -103,43 +94,38 @@ k_decode_hidden(int h2, const float *__restrict__ W1, const float *__restrict__ 
     for (int c = 0; c < K; ++c) sT1[r][c] = d * W1[r * K + c];
   }
   __syncthreads();
-  const int rl = threadIdx.x % RPB, q = threadIdx.x / RPB;
-  const int r = blockIdx.x * RPB + rl;
+  const int lane = threadIdx.x & 31;
+  const int r = blockIdx.x * kHiddenWarps + (threadIdx.x >> 5);
+  if (r >= h2) return;
+  const float *__restrict__ w = W2 + (long)r * H1;
+  float wv[H1 / 32];
+#pragma unroll
+  for (int i = 0; i < H1 / 32; ++i) wv[i] = __ldg(w + lane + 32 * i);  // all loads in flight together
   float acc[ld];
 #pragma unroll
   for (int c = 0; c < ld; ++c) acc[c] = 0.f;
-  if (r < h2) {
-    const int j0 = q * (H1 / PARTS);
-#pragma unroll 8
-    for (int j = j0; j < j0 + H1 / PARTS; ++j) {
-      const float wj = __ldg(W2T + (long)j * h2 + r);
-      acc[0] += wj * sh1[j];
 #pragma unroll
-      for (int c = 0; c < K; ++c) acc[1 + c] += wj * sT1[j][c];
-    }
+  for (int i = 0; i < H1 / 32; ++i) {
+    const int j = lane + 32 * i;
+    acc[0] += wv[i] * sh1[j];
+#pragma unroll
+    for (int c = 0; c < K; ++c) acc[1 + c] += wv[i] * sT1[j][c];
   }
 #pragma unroll
-  for (int c = 0; c < ld; ++c) sp[q][rl][c] = acc[c];
-  __syncthreads();
-  if (q != 0 || r >= h2) return;
-  float a = b2[r];
-  float t[K];
+  for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
-  for (int c = 0; c < K; ++c) t[c] = 0.f;
-  for (int qq = 0; qq < PARTS; ++qq) {
-    a += sp[qq][rl][0];
-#pragma unroll
-    for (int c = 0; c < K; ++c) t[c] += sp[qq][rl][1 + c];
-  }
+    for (int c = 0; c < ld; ++c) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+  if (lane != 0) return;
+  const float a = b2[r] + acc[0];
   const float d = delu_f(a);
   const float h = elu_f(a);
   Z[(long)r * ld] = h;
 #pragma unroll
-  for (int c = 0; c < K; ++c) Z[(long)r * ld + 1 + c] = d * t[c];
+  for (int c = 0; c < K; ++c) Z[(long)r * ld + 1 + c] = d * acc[1 + c];
   if (Zb) {
     Zb[r] = __float2bfloat16_rn(h);
 #pragma unroll
-    for (int c = 0; c < K; ++c) Zb[(long)(1 + c) * h2 + r] = __float2bfloat16_rn(d * t[c]);
+    for (int c = 0; c < K; ++c) Zb[(long)(1 + c) * h2 + r] = __float2bfloat16_rn(d * acc[1 + c]);
   }
 }
 
@@ -439,7 +425,7 @@ struct pda_lspg {
   long nst = 0, ns = 0, nSampleCells = 0;
   pda::DevBuf<int> s2st;
   pda::DevBuf<double> uref, phi, scale;
-  pda::DevBuf<float> W1, b1, W2, W2T, b2, W3, b3, Z, C;
+  pda::DevBuf<float> W1, b1, W2, b2, W3, b3, Z, C;
   bool tensorCore = false;
   pda::DevBuf<__nv_bfloat16> W3b, Zb;
   pda::DevBuf<double> y, D, V, J, yn, partial, xn;
@@ -483,14 +469,14 @@ void decode_k(pda_lspg &L, const double *x, double *y, int first, cudaStream_t s
   if (L.kind == 0) {
     k_decode_affine<K><<<div_up(L.nst, 256), 256, 0, s>>>(L.nst, L.uref.p, L.phi.p, x, y, first, f);
   } else if (L.tensorCore) {
-    k_decode_hidden<K, 256><<<div_up(L.h2, hidden_rows(K)), hidden_rows(K) * 4, 0, s>>>(
-        L.h2, L.W1.p, L.b1.p, L.W2T.p, L.b2.p, x, L.Z.p, L.Zb.p, first, f);
+    k_decode_hidden<K, 256><<<div_up(L.h2, kHiddenWarps), kHiddenWarps * 32, 0, s>>>(
+        L.h2, L.W1.p, L.b1.p, L.W2.p, L.b2.p, x, L.Z.p, L.Zb.p, first, f);
     PDA_CUDA(tc_gemm_partials(L.W3b.p, L.Zb.p, L.nst, 16, L.h2, kDecodeSplits, L.C.p, s));
     k_decode_finish_split<K><<<div_up(L.nst, 256), 256, 0, s>>>(L.nst, std::min(kDecodeSplits, L.h2 / 64), L.C.p,
                                                                  L.b3.p, L.uref.p, L.scale.p, y, L.D.p, first, f);
   } else {
-    k_decode_hidden<K, 256><<<div_up(L.h2, hidden_rows(K)), hidden_rows(K) * 4, 0, s>>>(
-        L.h2, L.W1.p, L.b1.p, L.W2T.p, L.b2.p, x, L.Z.p, nullptr, first, f);
+    k_decode_hidden<K, 256><<<div_up(L.h2, kHiddenWarps), kHiddenWarps * 32, 0, s>>>(
+        L.h2, L.W1.p, L.b1.p, L.W2.p, L.b2.p, x, L.Z.p, nullptr, first, f);
     const int smem = L.h2 * (1 + K) * (int)sizeof(float);
     k_decode_out<K><<<decode_grid(L.nst), 256, smem, s>>>(L.h2, L.nst, L.W3.p, L.b3.p, L.uref.p, L.scale.p, L.Z.p,
                                                             y, L.D.p, first, f);
@@ -652,8 +638,6 @@ pda_status pda_lspg_create_mlp(pda_problem *sample_problem, const int64_t *sampl
   pda::rom::upload_dev(L->W1, d_W1, (size_t)h1 * k);
   pda::rom::upload_dev(L->b1, d_b1, (size_t)h1);
   pda::rom::upload_dev(L->W2, d_W2, (size_t)h2 * h1);
-  L->W2T.alloc((size_t)h2 * h1);
-  pda::rom::k_transpose_f32<<<pda::div_up((long)h2 * h1, 256), 256>>>(L->W2.p, L->W2T.p, h2, h1);
   PDA_CUDA(cudaGetLastError());
   PDA_CUDA(cudaDeviceSynchronize());
   pda::rom::upload_dev(L->b2, d_b2, (size_t)h2);
