@@ -35,6 +35,17 @@ template <> struct Fam<Euler1d> {
   static PDA_HD void flux_jac(T JL[9], T JR[9], const T qL[3], const T qR[3], const Phys &p) {
     euler3_flux_jac(JL, JR, qL, qR, (T)p.gamma);
   }
+  // the flux in two halves (one face state, then the combination); bit-identical to flux
+  using Side = FluxSide<3>;
+  template <int AXIS>
+  static PDA_HD void flux_side(Side &o, const double q[3], const Phys &p) {
+    euler3_side(o, q, p.gamma);
+  }
+  template <int AXIS>
+  static PDA_HD void flux_combine(double F[3], const double qL[3], const double qR[3], const Side &L,
+                                  const Side &R, const Phys &p) {
+    euler3_combine(F, qL, qR, L, R, p.gamma);
+  }
 };
 template <> struct Fam<Euler2d> {
   static constexpr int dim = 2, ndpc = 4;
@@ -45,6 +56,17 @@ template <> struct Fam<Euler2d> {
   template <int AXIS, typename T>
   static PDA_HD void flux_jac(T JL[16], T JR[16], const T qL[4], const T qR[4], const Phys &p) {
     euler4_flux_jac<AXIS>(JL, JR, qL, qR, (T)p.gamma);
+  }
+  // the flux in two halves (one face state, then the combination); bit-identical to flux
+  using Side = FluxSide<4>;
+  template <int AXIS>
+  static PDA_HD void flux_side(Side &o, const double q[4], const Phys &p) {
+    euler4_side<AXIS>(o, q, p.gamma);
+  }
+  template <int AXIS>
+  static PDA_HD void flux_combine(double F[4], const double qL[4], const double qR[4], const Side &L,
+                                  const Side &R, const Phys &p) {
+    euler4_combine<AXIS>(F, qL, qR, L, R, p.gamma);
   }
 };
 template <> struct Fam<Euler3d> {
@@ -57,6 +79,17 @@ template <> struct Fam<Euler3d> {
   static PDA_HD void flux_jac(T JL[25], T JR[25], const T qL[5], const T qR[5], const Phys &p) {
     euler5_flux_jac<AXIS>(JL, JR, qL, qR, (T)p.gamma);
   }
+  // the flux in two halves (one face state, then the combination); bit-identical to flux
+  using Side = FluxSide<5>;
+  template <int AXIS>
+  static PDA_HD void flux_side(Side &o, const double q[5], const Phys &p) {
+    euler5_side<AXIS>(o, q, p.gamma);
+  }
+  template <int AXIS>
+  static PDA_HD void flux_combine(double F[5], const double qL[5], const double qR[5], const Side &L,
+                                  const Side &R, const Phys &p) {
+    euler5_combine<AXIS>(F, qL, qR, L, R, p.gamma);
+  }
 };
 template <> struct Fam<Swe2d> {
   static constexpr int dim = 2, ndpc = 3;
@@ -67,6 +100,17 @@ template <> struct Fam<Swe2d> {
   template <int AXIS, typename T>
   static PDA_HD void flux_jac(T JL[9], T JR[9], const T qL[3], const T qR[3], const Phys &p) {
     swe_flux_jac<AXIS>(JL, JR, qL, qR, (T)p.gravity);
+  }
+  // the flux in two halves (one face state, then the combination); bit-identical to flux
+  using Side = FluxSide<3>;
+  template <int AXIS>
+  static PDA_HD void flux_side(Side &o, const double q[3], const Phys &p) {
+    swe_side<AXIS>(o, q, p.gravity);
+  }
+  template <int AXIS>
+  static PDA_HD void flux_combine(double F[3], const double qL[3], const double qR[3], const Side &L,
+                                  const Side &R, const Phys &p) {
+    swe_combine<AXIS>(F, qL, qR, L, R, p.gravity);
   }
 };
 

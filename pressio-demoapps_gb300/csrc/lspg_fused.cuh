@@ -37,7 +37,8 @@ template <int FAM> struct FusedPar {
   static constexpr int SIDE = pad_warp(RPB_MAX * NF * NDPC);
   static constexpr int PART = pad_warp(RPB_MAX * NF);
   static constexpr int THREADS = 2 * SIDE;
-  static_assert(3 * PART <= THREADS, "phase B fits the block");
+  static_assert(4 * PART <= THREADS, "phase B fits the block");
+  static_assert(RPB_MAX * NF <= PART && RPB_MAX <= PART, "a warp covers the block's faces and rows");
   static constexpr size_t kSmemLimit = 160 * 1024;  // dynamic shared memory per block
   // dynamic shared memory per row: staged D of the row's stencil cells, the
   // per-face J D columns and the row's JR rows
@@ -70,22 +71,25 @@ __device__ inline double lspg_sum_rows(const double *__restrict__ a, int ne, int
 
 // reduce the group sums in group order, factor, solve, update (the calling
 // block; warp 0 factors): right-looking Cholesky with reciprocal square
-// roots, lane-parallel substitutions
+// roots of the matrix [H g; g^T .] augmented by the right-hand side, so that
+// its last row becomes z = L^-1 g in the trailing updates (no separate
+// forward substitution), then a lane-parallel back substitution
 __device__ inline void lspg_solve_rt(int K, int nparts, const double *__restrict__ partial, double *__restrict__ x,
                                      double tol, int first, LspgFlags *f) {
-  __shared__ double H[kLspgKMax][kLspgKMax];
-  __shared__ double g[kLspgKMax];
+  constexpr int KA = kLspgKMax + 1;  // augmented order
+  __shared__ double H[KA][KA];
   __shared__ double rdiag[kLspgKMax];
   __shared__ double rr;
-  __shared__ unsigned char pi[kLspgKMax * (kLspgKMax + 1) / 2], pl[kLspgKMax * (kLspgKMax + 1) / 2];
-  const int ntri = K * (K + 1) / 2, ne = ntri + K + 1;
+  __shared__ unsigned char pi[KA * (KA + 1) / 2], pl[KA * (KA + 1) / 2];
+  const int ntri = K * (K + 1) / 2, ne = ntri + K + 1, Ka = K + 1;
   const int lane = threadIdx.x & 31;
-  // lower-triangle pairs (i, l), i >= l, ordered by l descending: the pairs
-  // with l > j are the first (K-1-j)(K-j)/2 entries
-  for (int q = threadIdx.x; q < ntri; q += blockDim.x) {
-    int l = K - 1, rem = q;
-    while (rem >= K - l) {
-      rem -= K - l;
+  // lower-triangle pairs (i, l), i >= l, of the augmented order, by l
+  // descending: the pairs with l > j are the first (Ka-1-j)(Ka-j)/2 entries
+  const int ntriA = Ka * (Ka + 1) / 2;
+  for (int q = threadIdx.x; q < ntriA; q += blockDim.x) {
+    int l = Ka - 1, rem = q;
+    while (rem >= Ka - l) {
+      rem -= Ka - l;
       --l;
     }
     pi[q] = (unsigned char)(l + rem);
@@ -103,7 +107,7 @@ __device__ inline void lspg_solve_rt(int K, int nparts, const double *__restrict
       H[a][b2] = s;
       H[b2][a] = s;
     } else if (e < ntri + K) {
-      g[e - ntri] = s;
+      H[K][e - ntri] = s;  // the right-hand side as the augmented row
     } else {
       rr = s;
     }
@@ -113,30 +117,27 @@ __device__ inline void lspg_solve_rt(int K, int nparts, const double *__restrict
   bool ok = true;
   for (int j = 0; j < K; ++j) {
     const double d = H[j][j];
-    if (!(d > 0.)) {
+    // positive and finite, tested on the bits (no FP64 instruction)
+    const long long db = __double_as_longlong(d);
+    if (!(db > 0 && db < 0x7FF0000000000000LL)) {
       ok = false;
       break;
     }
     const double rs = rsqrt(d);
     if (lane == 0) rdiag[j] = rs;
-    for (int i = j + 1 + lane; i < K; i += 32) H[i][j] *= rs;
+    for (int i = j + 1 + lane; i <= K; i += 32) H[i][j] *= rs;
     __syncwarp();
-    // trailing lower triangle, its pairs spread over the lanes
-    const int np = (K - 1 - j) * (K - j) / 2;
+    // trailing lower triangle (the augmented row included), its pairs spread over the lanes
+    const int np = (Ka - 1 - j) * (Ka - j) / 2;
     for (int q = lane; q < np; q += 32) {
       const int row = pi[q], col = pl[q];
       H[row][col] = fma(-H[row][j], H[col][j], H[row][col]);
     }
     __syncwarp();
   }
-  double sv = lane < K ? g[lane] : 0.;
+  double sv = lane < K ? H[K][lane] : 0.;  // z = L^-1 g
   double corr = 0.;
   if (ok) {
-    for (int i = 0; i < K; ++i) {
-      const double zi = __shfl_sync(0xffffffffu, sv, i) * rdiag[i];
-      if (lane == i) sv = zi;
-      if (lane > i && lane < K) sv = fma(-H[lane][i], zi, sv);
-    }
     for (int i = K - 1; i >= 0; --i) {
       const double di = __shfl_sync(0xffffffffu, sv, i) * rdiag[i];
       if (lane == i) sv = di;
@@ -192,6 +193,7 @@ k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p,
   __shared__ double sY[FP::RPB_MAX][NDPC];    // state at the row's cell
   __shared__ double sSrc[FP::RPB_MAX][NDPC];  // source-term velocity (shallow water: Coriolis)
   __shared__ double sSJ[FP::RPB_MAX][NDPC * NDPC];  // its Jacobian
+  __shared__ typename F::Side sSide[FP::RPB_MAX][NF][2];  // the two face states' halves of the flux
   extern __shared__ double dyn[];
   const int tid = threadIdx.x, K = a.K, RD = rpb * NDPC, CB = NDPC * K;  // CB: D doubles per cell
   double *sD = dyn;                                  // [rpb][DIM][S][NDPC][K] staged D of stencil cells
@@ -253,47 +255,75 @@ k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p,
   }
   cp_async_wait_all();
   __syncthreads();
-  {  // phase B: (part, row, face): the face flux (part 0), JN (part 1) or JP (part 2);
-     // thread (part 0, row, face 0) also forms the row's source term and its Jacobian
+  // GB300 issues one FP64 warp instruction per ~64 cycles per sub-partition
+  // whatever the number of active lanes, so a stage costs its longest
+  // per-warp FP64 instruction stream.  With single-precision Jacobian terms
+  // phase B runs in two stages so that no warp evaluates a whole flux: B1 the
+  // two face states' halves of the flux (warps 0 / 1) beside JN / JP (warps
+  // 2 / 3), B2 their combination (warp 0) beside the row's source term (warp
+  // 1).  With double-precision Jacobian terms the flux Jacobians are the
+  // longest streams, so one stage: warp 0 the whole flux, warp 1 the source.
+  auto row_state_and_source = [&](int rl) {
+    const int e = e0 + rl;
+    if (rl >= rpb || e >= t.nrows) return;
+    const int cell = t.cell[e];
+    double y[NDPC];
+#pragma unroll
+    for (int d = 0; d < NDPC; ++d) y[d] = __ldg(a.y + (size_t)cell * NDPC + d);
+#pragma unroll
+    for (int d = 0; d < NDPC; ++d) {
+      sY[rl][d] = y[d];
+      sSrc[rl][d] = 0.;
+    }
+#pragma unroll
+    for (int i = 0; i < NDPC * NDPC; ++i) sSJ[rl][i] = 0.;
+    if constexpr (FAM == Swe2d) {
+      // Coriolis source (swe_2d_prob_class.hpp:983-1012) and its Jacobian
+      const double u0 = y[0], u1 = y[1], u2 = y[2];
+      sSrc[rl][1] = -(p.coriolis * u2 / u0);
+      sSrc[rl][2] = p.coriolis * u1 / u0;
+      sSJ[rl][1 * 3 + 0] = p.coriolis * u2 / (u0 * u0);
+      sSJ[rl][1 * 3 + 2] = -p.coriolis / u0;
+      sSJ[rl][2 * 3 + 1] = p.coriolis / u0;
+      sSJ[rl][2 * 3 + 0] = -p.coriolis * u1 / (u0 * u0);
+    }
+  };
+  auto combine = [&](int rl, int f) {
+    FF &o = fd[rl][f];
+    const int ax = f >> 1;
+    const typename F::Side &L = sSide[rl][f][0], &R = sSide[rl][f][1];
+    if (ax == 0) F::template flux_combine<0>(o.fl, o.uN, o.uP, L, R, p);
+    if constexpr (DIM > 1) if (ax == 1) F::template flux_combine<1>(o.fl, o.uN, o.uP, L, R, p);
+    if constexpr (DIM > 2) if (ax == 2) F::template flux_combine<2>(o.fl, o.uN, o.uP, L, R, p);
+  };
+  {  // phase B1: (part, row, face): parts 0 / 1 the left / right face state's
+     // half of the flux (exact Jacobian: part 0 both halves and the flux,
+     // part 1 the rows' sources), parts 2 / 3 JN / JP
     const int part = tid / FP::PART, slot = tid % FP::PART;
     const int rl = slot / NF, f = slot % NF, ax = f >> 1, fs = f & 1;
     const int e = e0 + rl;
-    if (part < 3 && slot < rpb * NF && e < t.nrows) {
+    if (kExact && part == 1) {
+      row_state_and_source(slot);
+    } else if (part < 4 && slot < rpb * NF && e < t.nrows) {
       FF &o = fd[rl][f];
-      double uN[NDPC], uP[NDPC];
+      if (part < 2) {
 #pragma unroll
-      for (int d = 0; d < NDPC; ++d) {
-        uN[d] = o.uN[d];
-        uP[d] = o.uP[d];
-      }
-      if (part == 0) {
-        if (ax == 0) F::template flux<0>(o.fl, uN, uP, p);
-        if constexpr (DIM > 1) if (ax == 1) F::template flux<1>(o.fl, uN, uP, p);
-        if constexpr (DIM > 2) if (ax == 2) F::template flux<2>(o.fl, uN, uP, p);
-        if (f == 0) {
-          const int cell = t.cell[e];
-          double y[NDPC];
-#pragma unroll
-          for (int d = 0; d < NDPC; ++d) y[d] = __ldg(a.y + (size_t)cell * NDPC + d);
-#pragma unroll
-          for (int d = 0; d < NDPC; ++d) {
-            sY[rl][d] = y[d];
-            sSrc[rl][d] = 0.;
-          }
-#pragma unroll
-          for (int i = 0; i < NDPC * NDPC; ++i) sSJ[rl][i] = 0.;
-          if constexpr (FAM == Swe2d) {
-            // Coriolis source (swe_2d_prob_class.hpp:983-1012) and its Jacobian
-            const double u0 = y[0], u1 = y[1], u2 = y[2];
-            sSrc[rl][1] = -(p.coriolis * u2 / u0);
-            sSrc[rl][2] = p.coriolis * u1 / u0;
-            sSJ[rl][1 * 3 + 0] = p.coriolis * u2 / (u0 * u0);
-            sSJ[rl][1 * 3 + 2] = -p.coriolis / u0;
-            sSJ[rl][2 * 3 + 1] = p.coriolis / u0;
-            sSJ[rl][2 * 3 + 0] = -p.coriolis * u1 / (u0 * u0);
-          }
+        for (int sd = 0; sd < (kExact ? 2 : 1); ++sd) {
+          const int side = kExact ? sd : part;
+          const double *q = side == 0 ? o.uN : o.uP;
+          typename F::Side &so = sSide[rl][f][side];
+          if (ax == 0) F::template flux_side<0>(so, q, p);
+          if constexpr (DIM > 1) if (ax == 1) F::template flux_side<1>(so, q, p);
+          if constexpr (DIM > 2) if (ax == 2) F::template flux_side<2>(so, q, p);
         }
+        if (kExact) combine(rl, f);
       } else {
+        double uN[NDPC], uP[NDPC];
+#pragma unroll
+        for (int d = 0; d < NDPC; ++d) {
+          uN[d] = o.uN[d];
+          uP[d] = o.uP[d];
+        }
         if (!inner) {
           // first-order Jacobian at the face's two cells (ghosts through their recipes)
           const size_t b1 = ((size_t)e * DIM + ax) * 3;
@@ -317,7 +347,7 @@ k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p,
         if constexpr (DIM > 2) if (ax == 2) F::template flux_jac<2>(JN, JP, vN, vP, p);
         // one of the two per warp (the part is warp-uniform): the other's
         // arithmetic is dead and dropped
-        if (part == 1) {
+        if (part == 2) {
 #pragma unroll
           for (int i = 0; i < NDPC * NDPC; ++i) o.JN[i] = JN[i];
         } else {
@@ -328,6 +358,16 @@ k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p,
     }
   }
   __syncthreads();
+  if constexpr (!kExact) {  // phase B2: warp 0 (row, face) the flux from its two halves; warp 1
+                            // (row) the row's state and its source term with its Jacobian
+    if (tid < FP::PART) {
+      const int rl = tid / NF, f = tid % NF;
+      if (tid < rpb * NF && e0 + rl < t.nrows) combine(rl, f);
+    } else if (tid < 2 * FP::PART) {
+      row_state_and_source(tid - FP::PART);
+    }
+    __syncthreads();
+  }
   // phase C: (row, face, column c): the face's (JN dU_N + JP dU_P) D column
   for (int w = tid; w < rpb * NF * K; w += blockDim.x) {
     const int rl = w / (NF * K), f = (w / K) % NF, c = w % K, ax = f >> 1, fs = f & 1;

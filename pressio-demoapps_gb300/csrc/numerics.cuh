@@ -613,6 +613,139 @@ PDA_HD void swe_flux(double F[3], const double qL[3], const double qR[3],
 }
 
 // ---------------------------------------------------------------------------
+// The Rusanov fluxes above in two halves: flux_side (the quantities of one
+// face state: its velocities, enthalpy or sqrt(h), and physical flux) and
+// flux_combine (the Roe / wave-speed average and the Rusanov sum).
+// combine(side(qL), side(qR)) evaluates every expression of the *_flux
+// function above unchanged, so it is bit-identical; the halves let a kernel
+// compute the two states of a face on different warps.
+// ---------------------------------------------------------------------------
+template <int N> struct FluxSide {
+  double F[N];  // the state's physical flux along the axis
+  double u, v, w, H;  // Euler: velocities and total enthalpy; shallow water: u = normal velocity, H = sqrt(h)
+};
+
+PDA_HD void euler3_side(FluxSide<3> &o, const double q[3], double gamma) {
+  constexpr double half = 1. / 2.;
+  constexpr double es = 1.e-30;
+  const double r = q[0];
+  const double u = q[1] / (r + es);
+  const double p = (gamma - 1) * (q[2] - half * r * (u * u));
+  const double H = (q[2] + p) / r;
+  o.F[0] = r * u;
+  o.F[1] = r * u * u + p;
+  o.F[2] = r * u * H;
+  o.u = u;
+  o.H = H;
+}
+PDA_HD void euler3_combine(double F[3], const double qL[3], const double qR[3], const FluxSide<3> &L,
+                           const FluxSide<3> &R, double gamma) {
+  constexpr double half = 1. / 2.;
+  const double RT = sqrt(qR[0] / (qL[0]));
+  const double u = (L.u + RT * R.u) / (1. + RT);
+  const double H = (L.H + RT * R.H) / (1. + RT);
+  const double a = sqrt((gamma - 1.) * (H - half * (u * u)));
+  const double smax = fabs(u) + a;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) F[d] = half * (L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
+}
+
+template <int AXIS>
+PDA_HD void euler4_side(FluxSide<4> &o, const double q[4], double gamma) {
+  constexpr double half = 1. / 2.;
+  constexpr double es = 1.e-30;
+  const double r = q[0];
+  const double u = q[1] / (r + es);
+  const double v = q[2] / (r + es);
+  const double un = AXIS == 0 ? u : v;
+  const double p = (gamma - 1) * (q[3] - half * r * (u * u + v * v));
+  const double H = (q[3] + p) / r;
+  o.F[0] = r * un;
+  o.F[1] = AXIS == 0 ? r * un * u + p : r * un * u;
+  o.F[2] = AXIS == 1 ? r * un * v + p : r * un * v;
+  o.F[3] = r * un * H;
+  o.u = u;
+  o.v = v;
+  o.H = H;
+}
+template <int AXIS>
+PDA_HD void euler4_combine(double F[4], const double qL[4], const double qR[4], const FluxSide<4> &L,
+                           const FluxSide<4> &R, double gamma) {
+  constexpr double half = 1. / 2.;
+  const double RT = sqrt(qR[0] / (qL[0]));
+  const double u = (L.u + RT * R.u) / (1. + RT);
+  const double v = (L.v + RT * R.v) / (1. + RT);
+  const double H = (L.H + RT * R.H) / (1. + RT);
+  const double a = sqrt((gamma - 1.) * (H - half * (u * u + v * v)));
+  const double smax = sqrt(u * u + v * v) + a;
+#pragma unroll
+  for (int d = 0; d < 4; ++d) F[d] = half * (L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
+}
+
+template <int AXIS>
+PDA_HD void euler5_side(FluxSide<5> &o, const double q[5], double gamma) {
+  constexpr double half = 1. / 2.;
+  constexpr double es = 1.e-30;
+  const double r = q[0];
+  const double u = q[1] / (r + es);
+  const double v = q[2] / (r + es);
+  const double w = q[3] / (r + es);
+  const double un = AXIS == 0 ? u : (AXIS == 1 ? v : w);
+  const double p = (gamma - 1) * (q[4] - half * r * (u * u + v * v + w * w));
+  const double H = (q[4] + p) / r;
+  o.F[0] = r * un;
+  o.F[1] = AXIS == 0 ? r * un * u + p : r * un * u;
+  o.F[2] = AXIS == 1 ? r * un * v + p : r * un * v;
+  o.F[3] = AXIS == 2 ? r * un * w + p : r * un * w;
+  o.F[4] = r * un * H;
+  o.u = u;
+  o.v = v;
+  o.w = w;
+  o.H = H;
+}
+template <int AXIS>
+PDA_HD void euler5_combine(double F[5], const double qL[5], const double qR[5], const FluxSide<5> &L,
+                           const FluxSide<5> &R, double gamma) {
+  constexpr double half = 1. / 2.;
+  const double RT = sqrt(qR[0] / (qL[0]));
+  const double u = (L.u + RT * R.u) / (1. + RT);
+  const double v = (L.v + RT * R.v) / (1. + RT);
+  const double w = (L.w + RT * R.w) / (1. + RT);
+  const double H = (L.H + RT * R.H) / (1. + RT);
+  const double a = sqrt((gamma - 1.) * (H - half * (u * u + v * v + w * w)));
+  const double smax = sqrt(u * u + v * v + w * w) + a;
+#pragma unroll
+  for (int d = 0; d < 5; ++d) F[d] = half * (L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
+}
+
+template <int AXIS>
+PDA_HD void swe_side(FluxSide<3> &o, const double q[3], double gravity) {
+  constexpr double es = 1.e-30;
+  const double h = q[0];
+  const double u = q[1] / (h + es);
+  const double v = q[2] / (h + es);
+  const double un = AXIS == 0 ? u : v;
+  const double p = 0.5 * gravity * h * h;
+  o.F[0] = h * un;
+  o.F[1] = AXIS == 0 ? h * un * u + p : h * un * u;
+  o.F[2] = AXIS == 1 ? h * un * v + p : h * un * v;
+  o.u = un;
+  o.H = sqrt(h);
+}
+template <int AXIS>
+PDA_HD void swe_combine(double F[3], const double qL[3], const double qR[3], const FluxSide<3> &L,
+                        const FluxSide<3> &R, double gravity) {
+  constexpr double half = 1. / 2.;
+  constexpr double es = 1.e-30;
+  const double hm = 0.5 * (qL[0] + qR[0]);
+  const double um = (L.u * L.H + R.u * R.H) / (L.H + R.H + es);
+  const double sg = sqrt(gravity * hm);
+  const double smax = sqrt(um * um) + sqrt(sg * sg);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) F[d] = half * (L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
+}
+
+// ---------------------------------------------------------------------------
 // Analytic Rusanov flux Jacobians JL = dF/dqL, JR = dF/dqR (row-major n x n).
 // These keep the reference's generic normal vector n.
 // ---------------------------------------------------------------------------

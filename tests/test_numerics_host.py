@@ -80,6 +80,8 @@ def test_flux_and_flux_jacobian_bitwise(oracle, host_numerics, family, axes, nd,
     fo, fh = oracle.L.orc_point_flux, host_numerics.pdn_point_flux
     for fn in (fo, fh):
         fn.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
+    fs = host_numerics.pdn_point_flux_split
+    fs.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]
     for _ in range(5000):
         qL, qR = rng.uniform(-1, 1, nd), rng.uniform(-1, 1, nd)
         qL[0], qR[0] = rng.uniform(0.2, 2.0), rng.uniform(0.2, 2.0)
@@ -94,6 +96,10 @@ def test_flux_and_flux_jacobian_bitwise(oracle, host_numerics, family, axes, nd,
             fh(family, ax, vp(qL), vp(qR), param, vp(F2), vp(J[2]), vp(J[3]))
             # the axis-specialised flux differs at most in the sign of an exact zero
             assert np.array_equal(F1, F2)
+            # the flux in two halves (face states on separate threads) is the same flux
+            F3 = np.empty(nd)
+            fs(family, ax, vp(qL), vp(qR), param, vp(F3))
+            assert np.array_equal(F3, F2)
             # shallow-water Jacobians use sqrt for glibc's pow(h, 0.5): 1-ulp differences
             for a, b in ((J[0], J[2]), (J[1], J[3])):
                 assert np.allclose(a, b, rtol=1e-13, atol=1e-15 * np.abs(a).max())
