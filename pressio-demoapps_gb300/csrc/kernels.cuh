@@ -765,6 +765,8 @@ template <int FAM> struct VelPar {
   static constexpr int RPB_MAX = Fam<FAM>::dim == 3 ? 4 : 8;
   static constexpr int SIDE = pad_warp(RPB_MAX * NF * NDPC);
   static constexpr int THREADS = 2 * SIDE;
+  static constexpr int PART = pad_warp(RPB_MAX * NF);  // one warp: the block's faces
+  static_assert(2 * PART <= THREADS, "the two face-state halves fit the block");
 };
 
 template <int FAM> struct VelFace {
@@ -782,6 +784,7 @@ k_rows_velocity_par(RowTable ta, RowTable tb, int nbA, int rpb, MeshArgs m, Phys
   constexpr int NDPC = F::ndpc, DIM = F::dim, H = SchemeTraits<SCHEME>::h, S = 2 * H + 1, G = 2 * H;
   constexpr int NF = VP::NF;
   __shared__ VelFace<FAM> fd[VP::RPB_MAX][NF];
+  __shared__ typename F::Side sSide[VP::RPB_MAX][NF][2];  // the two face states' halves of each flux
   // blocks [0, nbA) take the rows of table ta, the others those of tb
   const bool first = (int)blockIdx.x < nbA;
   const RowTable &t = first ? ta : tb;
@@ -804,20 +807,29 @@ k_rows_velocity_par(RowTable ta, RowTable tb, int nbA, int rpb, MeshArgs m, Phys
     }
   }
   __syncthreads();
-  if (tid < rpb * NF) {  // the face flux
+  // the face flux in two halves, so that no warp evaluates a whole flux (a
+  // stage costs its longest per-warp FP64 instruction stream): warps 0 / 1
+  // the left / right face state's quantities, then warp 0 their combination
+  {
+    const int part = tid / VP::PART, slot = tid % VP::PART;
+    const int rl = slot / NF, f = slot % NF, ax = f >> 1;
+    if (part < 2 && slot < rpb * NF && e0 + rl < t.nrows) {
+      const double *q = part == 0 ? fd[rl][f].uN : fd[rl][f].uP;
+      typename F::Side &so = sSide[rl][f][part];
+      if (ax == 0) F::template flux_side<0>(so, q, p);
+      if constexpr (DIM > 1) if (ax == 1) F::template flux_side<1>(so, q, p);
+      if constexpr (DIM > 2) if (ax == 2) F::template flux_side<2>(so, q, p);
+    }
+  }
+  __syncthreads();
+  if (tid < rpb * NF) {
     const int rl = tid / NF, f = tid % NF, ax = f >> 1;
-    const int e = e0 + rl;
-    if (e < t.nrows) {
+    if (e0 + rl < t.nrows) {
       VelFace<FAM> &o = fd[rl][f];
-      double uN[NDPC], uP[NDPC];
-#pragma unroll
-      for (int d = 0; d < NDPC; ++d) {
-        uN[d] = o.uN[d];
-        uP[d] = o.uP[d];
-      }
-      if (ax == 0) F::template flux<0>(o.fl, uN, uP, p);
-      if constexpr (DIM > 1) if (ax == 1) F::template flux<1>(o.fl, uN, uP, p);
-      if constexpr (DIM > 2) if (ax == 2) F::template flux<2>(o.fl, uN, uP, p);
+      const typename F::Side &L = sSide[rl][f][0], &R = sSide[rl][f][1];
+      if (ax == 0) F::template flux_combine<0>(o.fl, o.uN, o.uP, L, R, p);
+      if constexpr (DIM > 1) if (ax == 1) F::template flux_combine<1>(o.fl, o.uN, o.uP, L, R, p);
+      if constexpr (DIM > 2) if (ax == 2) F::template flux_combine<2>(o.fl, o.uN, o.uP, L, R, p);
     }
   }
   __syncthreads();
