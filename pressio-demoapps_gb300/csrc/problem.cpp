@@ -985,11 +985,18 @@ void create_problem(pda_problem &P, const Mesh &m, int family, int probEn, int s
       }
       cells *= (long)(b.hi[a] - b.lo[a]);
     }
-    if (mirror && cells == (long)m.sampleMeshSize) {
+    // Small 1D meshes take the per-row kernels for every row: the face pass
+    // puts a whole face (every dof's reconstructions and the flux) on one
+    // thread, and below about 60 faces per SM its blocks cannot fill the GPU,
+    // so a call costs one long per-warp FP64 instruction stream (GB300 issues
+    // one FP64 warp instruction per ~64 cycles per sub-partition); the row
+    // kernel spreads a row's work over warps.
+    const bool smallLine = P.dim == 1 && (long)m.sampleMeshSize < kRowsOnlyCells1D;
+    if (!smallLine && mirror && cells == (long)m.sampleMeshSize) {
       P.box = b;
       P.useStruct = true;
       P.structAll = true;
-    } else if (!mirror && cells == (long)m.inner.size()) {
+    } else if (!smallLine && !mirror && cells == (long)m.inner.size()) {
       P.box = b;
       P.useStruct = true;
     }
@@ -1323,9 +1330,18 @@ pda_status pda_velocity_noalloc(pda_problem *p, const double *dU, double t, doub
   pda::check_evaluable(P);
   pda::MeshArgs ma = P.margs;
   ma.time = t;
-  PDA_REQUIRE(P.useStruct, PDA_ERR_UNSUPPORTED,
-              "pda_velocity_noalloc: only full meshes evaluated by the structured face pass are supported "
-              "(sample meshes have no face scratch: use pda_velocity)");
+  if (!P.useStruct) {
+    // every row through the row kernel (small 1D full meshes): no face
+    // scratch, only the two row tables, uploaded by the first pda_velocity call
+    PDA_REQUIRE(P.mesh->structured && P.innerBuiltV && !P.innerT.dirty && !P.nearT.dirty &&
+                    (P.recipes.empty() || P.d_recipes.p),
+                PDA_ERR_UNSUPPORTED,
+                "pda_velocity_noalloc: full meshes only, and the row tables of this problem are not on the device "
+                "yet; one pda_velocity call on the problem uploads them");
+    P.L->rows_velocity(P.scheme, P.innerT.t, P.nearT.t, ma, P.phys, dU, dV, P.stream);
+    pda::check_launch(P);
+    return PDA_OK;
+  }
   // the near-boundary row table is uploaded by the first pda_velocity call;
   // uploading it here would allocate
   const bool nearResident =

@@ -188,6 +188,12 @@ void ensure_row_tables(pda_problem &P);
 }  // namespace pda
 
 // C ABI bodies: exceptions become a status code + the thread-local message
+// 1D full meshes below this many cells evaluate every row with the per-row
+// kernel: the face pass takes 61 faces per block, so below ~61 x 152 cells its
+// grid does not cover GB300's SMs and a call costs one whole-face FP64
+// instruction stream per warp
+constexpr long kRowsOnlyCells1D = 8192;
+
 #define PDA_API_BEGIN try {
 #define PDA_API_END                                   \
   return PDA_OK;                                      \

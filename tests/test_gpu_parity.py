@@ -270,6 +270,35 @@ def test_sample_mesh_rows_equal_full_mesh_rows_1024(pda, scheme):
     assert torch.equal(Vs, ref)
 
 
+@pytest.mark.parametrize("scheme", [0, 1, 2])
+def test_sample_mesh_rows_equal_full_mesh_faces_1d(pda, scheme):
+    """1D full meshes below 8192 cells take the per-row kernel for every row
+    (the face pass would leave most SMs idle); at 20,000 cells the Sod mesh
+    takes the structured face pass, so its velocity at sampled cells must
+    equal the sample mesh's (per-row kernel) bit for bit, boundary rows
+    included."""
+    torch = _torch()
+    n = 20000
+    mesh = pda.create_full_mesh((n,), (-0.5, 0.5), 7, (False,))
+    p = pda.create_problem(mesh, pda.Euler1d.Sod, pda.InviscidFluxReconstruction(scheme))
+    U = p.initialCondition()
+    gen = torch.Generator(device="cuda").manual_seed(17)
+    U += (torch.rand(U.shape, generator=gen, device="cuda", dtype=torch.float64) * 2 - 1) * 1e-3
+    V = p.createVelocity()
+    p.velocity(U, 0.0, V)
+    assert torch.isfinite(V).all()
+    rng = np.random.default_rng(9)
+    gids = np.unique(np.concatenate([rng.choice(n, 500, replace=False), np.arange(0, 8), np.arange(n - 8, n),
+                                     np.arange(n // 2 - 4, n // 2 + 4)]))
+    sm, stencil_gids = pda.create_sample_mesh(mesh, gids)
+    ps = pda.create_problem(sm, pda.Euler1d.Sod, pda.InviscidFluxReconstruction(scheme))
+    Us = U.view(-1, 3)[torch.from_numpy(stencil_gids).cuda()].reshape(-1).contiguous()
+    Vs = ps.createVelocity()
+    ps.velocity(Us, 0.0, Vs)
+    ref = V.view(-1, 3)[torch.from_numpy(gids).cuda()].reshape(-1)
+    assert torch.equal(Vs, ref)
+
+
 def test_periodic_translation_invariance_512(pda):
     torch = _torch()
     mesh = pda.create_full_mesh((512, 512), (-1.0, 1.0, -1.0, 1.0), 7, (True, True))
