@@ -2,6 +2,8 @@
 // PDA_FAM defined to the family enum value.
 #pragma once
 
+#include <type_traits>
+
 #include "kernels.cuh"
 #include "tiles.cuh"
 #include "batch.cuh"
@@ -17,6 +19,8 @@ constexpr int FAM = PDA_FAM;
 using F = Fam<FAM>;
 
 int device_sms();
+// whether this family has the given axis
+constexpr bool F_dim_ok(int axis) { return axis < Fam<PDA_FAM>::dim; }
 
 template <int SCHEME>
 void rows_velocity_s(const RowTable &ta, const RowTable &tb, const MeshArgs &m, const Phys &p, const double *U,
@@ -86,6 +90,28 @@ void struct_velocity(int scheme, const Box &b, const MeshArgs &m, const Phys &p,
     case Weno3: struct_velocity_s<Weno3>(b, m, p, U, Fb, V, s, launches, ev); break;
     default: struct_velocity_s<Weno5>(b, m, p, U, Fb, V, s, launches, ev); break;
   }
+}
+
+void struct_faces(int scheme, int axis, const Box &b, const Phys &p, const double *U, double *F, cudaStream_t s) {
+  int nl = 0;
+  auto go = [&](auto sch) {
+    constexpr int SC = decltype(sch)::value;
+    if (axis == 0) faces_s<SC, 0>(b, p, U, F, s, &nl, nullptr);
+    if constexpr (F_dim_ok(1)) if (axis == 1) faces_s<SC, 1>(b, p, U, F, s, &nl, nullptr);
+    if constexpr (F_dim_ok(2)) if (axis == 2) faces_s<SC, 2>(b, p, U, F, s, &nl, nullptr);
+  };
+  switch (scheme) {
+    case FirstOrder: go(std::integral_constant<int, FirstOrder>{}); break;
+    case Weno3: go(std::integral_constant<int, Weno3>{}); break;
+    default: go(std::integral_constant<int, Weno5>{}); break;
+  }
+}
+
+void struct_balance(const Box &b, const MeshArgs &m, const Phys &p, const double *U, const double *const F[3],
+                    double *V, cudaStream_t s) {
+  long nc = 1;
+  for (int a = 0; a < 3; ++a) nc *= (long)(b.hi[a] - b.lo[a]);
+  if (nc > 0) k_struct_balance<FAM><<<div_up(nc, 256), 256, 0, s>>>(b, m, p, U, F[0], F[1], F[2], V);
 }
 
 void rows_vj_inner(int scheme, const RowTable &t, const MeshArgs &m, const Phys &p, const double *U,

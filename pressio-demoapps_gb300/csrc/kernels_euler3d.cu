@@ -5,6 +5,7 @@
 namespace pda {
 const Launchers &launchers_euler3d() {
   static const Launchers L = {fam_impl::rows_velocity, fam_impl::struct_velocity,
+                              fam_impl::struct_faces, fam_impl::struct_balance,
                               fam_impl::rows_vj_inner, fam_impl::rows_vj_nearbd,
                               fam_impl::batch_faces, fam_impl::batch_balance,
                               fam_impl::batch_num_shapes, fam_impl::struct_vj,

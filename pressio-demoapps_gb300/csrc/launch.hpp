@@ -17,6 +17,13 @@ struct Launchers {
   void (*struct_velocity)(int scheme, const Box &b, const MeshArgs &m, const Phys &p,
                           const double *U, double *const F[3], double *V, cudaStream_t s,
                           int *launches, cudaEvent_t *ev);
+  // the pieces of struct_velocity over a sub-box (bands of the host-buffer
+  // path): faces normal to `axis` into F (the face array of that box), and
+  // the balance of the box's cells from F[axis] (offset to the box) into V
+  void (*struct_faces)(int scheme, int axis, const Box &b, const Phys &p, const double *U, double *F,
+                       cudaStream_t s);
+  void (*struct_balance)(const Box &b, const MeshArgs &m, const Phys &p, const double *U,
+                         const double *const F[3], double *V, cudaStream_t s);
   // V and J for inner rows / near-boundary rows
   void (*rows_vj_inner)(int scheme, const RowTable &t, const MeshArgs &m, const Phys &p,
                         const double *U, const int *rowptr, double *V, double *J, cudaStream_t s);

@@ -1378,9 +1378,97 @@ pda_status pda_velocity_noalloc(pda_problem *p, const double *dU, double t, doub
   PDA_API_END
 }
 
+namespace pda {
+// pda_velocity_host for 2D meshes that one structured box covers: two row
+// bands whose copies overlap the other band's kernels.  The copy stream moves
+// band 0's rows, then band 1's; each band's x faces start on its own compute
+// stream as soon as its rows are on the device (x faces read no other row),
+// its y faces once both bands are (y faces [0, r] for band 0, [r + 1, n] for
+// band 1), its balance after its own faces (band 1 also after band 0's y
+// faces: it reads face r), and its velocity rows go back as soon as its
+// balance is done.  Band 0 runs on a high-priority stream, so it finishes
+// first while band 1's blocks fill its tails: band 1's rows come in under band
+// 0's x faces and band 0's velocity goes out under band 1's kernels.  The same
+// kernels on sub-boxes: V equals pda_velocity's bit for bit.  Returns false
+// when the mesh does not qualify.
+bool velocity_host_banded(pda_problem &P, const double *hU, double t, double *hV) {
+  if (!(P.useStruct && P.structAll && P.dim == 2 && P.box.n[1] >= 64 && P.dofsSample == P.dofsStencil))
+    return false;
+  check_evaluable(P);
+  sync_recipes(P);
+  if (!P.hostCopy) {
+    int least = 0, greatest = 0;
+    PDA_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    PDA_CUDA(cudaStreamCreateWithPriority(&P.hostFirst, cudaStreamNonBlocking, greatest));
+    PDA_CUDA(cudaStreamCreateWithPriority(&P.hostCompute, cudaStreamNonBlocking, least));
+    PDA_CUDA(cudaStreamCreateWithFlags(&P.hostCopy, cudaStreamNonBlocking));
+    for (cudaEvent_t &e : P.hostEv) PDA_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  const Box &B = P.box;
+  const int nx = B.n[0], ny = B.n[1], nd = P.ndpc;
+  const int r[3] = {0, ny / 2, ny};
+  const size_t rowDofs = (size_t)nx * nd;
+  P.d_U.alloc(P.dofsStencil);
+  P.d_V.alloc(P.dofsSample);
+  P.F[0].alloc((size_t)(nx + 1) * ny * nd);
+  P.F[1].alloc((size_t)nx * (ny + 1) * nd);
+  double *U = P.d_U.p, *V = P.d_V.p, *Fx = P.F[0].p, *Fy = P.F[1].p;
+  MeshArgs ma = P.margs;
+  ma.time = t;
+  cudaStream_t cs[2] = {P.hostFirst, P.hostCompute}, sc = P.hostCopy;
+  cudaEvent_t *ev = P.hostEv;  // 0 start, 1-2 band rows in, 3-4 y faces, 5-6 balance, 7 copies out, 8 spare
+  // after whatever the problem's stream holds
+  PDA_CUDA(cudaEventRecord(ev[0], P.stream));
+  PDA_CUDA(cudaStreamWaitEvent(sc, ev[0], 0));
+  PDA_CUDA(cudaStreamWaitEvent(cs[0], ev[0], 0));
+  PDA_CUDA(cudaStreamWaitEvent(cs[1], ev[0], 0));
+  for (int b = 0; b < 2; ++b) {
+    PDA_CUDA(cudaMemcpyAsync(U + r[b] * rowDofs, hU + r[b] * rowDofs, (size_t)(r[b + 1] - r[b]) * rowDofs * 8,
+                             cudaMemcpyHostToDevice, sc));
+    PDA_CUDA(cudaEventRecord(ev[1 + b], sc));
+  }
+  for (int b = 0; b < 2; ++b) {
+    PDA_CUDA(cudaStreamWaitEvent(cs[b], ev[1 + b], 0));
+    Box xb = B;
+    xb.lo[1] = r[b];
+    xb.hi[1] = r[b + 1];
+    P.L->struct_faces(P.scheme, 0, xb, P.phys, U, Fx + (size_t)(nx + 1) * r[b] * nd, cs[b]);
+  }
+  for (int b = 0; b < 2; ++b) {
+    PDA_CUDA(cudaStreamWaitEvent(cs[b], ev[2 - b], 0));  // the other band's rows
+    Box yb = B;
+    yb.lo[1] = b == 0 ? 0 : r[1] + 1;
+    yb.hi[1] = b == 0 ? r[1] : ny;
+    P.L->struct_faces(P.scheme, 1, yb, P.phys, U, Fy + (size_t)nx * yb.lo[1] * nd, cs[b]);
+    PDA_CUDA(cudaEventRecord(ev[3 + b], cs[b]));
+  }
+  for (int b = 0; b < 2; ++b) {
+    if (b == 1) PDA_CUDA(cudaStreamWaitEvent(cs[1], ev[3], 0));  // face r, from band 0's y faces
+    Box bb = B;
+    bb.lo[1] = r[b];
+    bb.hi[1] = r[b + 1];
+    const double *Fb[3] = {Fx + (size_t)(nx + 1) * r[b] * nd, Fy + (size_t)nx * r[b] * nd, nullptr};
+    P.L->struct_balance(bb, ma, P.phys, U, Fb, V, cs[b]);
+    PDA_CUDA(cudaEventRecord(ev[5 + b], cs[b]));
+  }
+  for (int b = 0; b < 2; ++b) {
+    PDA_CUDA(cudaStreamWaitEvent(sc, ev[5 + b], 0));
+    PDA_CUDA(cudaMemcpyAsync(hV + r[b] * rowDofs, V + r[b] * rowDofs, (size_t)(r[b + 1] - r[b]) * rowDofs * 8,
+                             cudaMemcpyDeviceToHost, sc));
+  }
+  PDA_CUDA(cudaEventRecord(ev[7], sc));
+  PDA_CUDA(cudaStreamWaitEvent(P.stream, ev[7], 0));  // later work on the problem's stream follows
+  P.launches += 6;
+  PDA_CUDA(cudaStreamSynchronize(sc));  // the last copy follows every kernel of both bands
+  PDA_CUDA(cudaGetLastError());
+  return true;
+}
+}  // namespace pda
+
 pda_status pda_velocity_host(pda_problem *p, const double *hU, double t, double *hV) {
   PDA_API_BEGIN
   PDA_REQUIRE(p && hU && hV, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  if (pda::velocity_host_banded(*p, hU, t, hV)) return PDA_OK;
   p->d_U.alloc(p->dofsStencil);
   p->d_V.alloc(p->dofsSample);
   PDA_CUDA(cudaMemcpyAsync(p->d_U.p, hU, p->dofsStencil * sizeof(double), cudaMemcpyHostToDevice, p->stream));

@@ -136,6 +136,10 @@ struct pda_problem {
   // second stream + events: inner and near-boundary row kernels run side by side
   cudaStream_t side = nullptr;
   cudaEvent_t evFork = nullptr, evJoin = nullptr;
+  // host-buffer velocity in row bands: two compute streams (the first band's
+  // at high priority), a copy stream and their events (created on first use)
+  cudaStream_t hostFirst = nullptr, hostCompute = nullptr, hostCopy = nullptr;
+  cudaEvent_t hostEv[9] = {};
   int ndpc = 0, dim = 0, h = 0;
   int64_t dofsSample = 0, dofsStencil = 0;
   int bc = pda::BC_NONE;
@@ -175,6 +179,11 @@ struct pda_problem {
     if (side) cudaStreamDestroy(side);
     if (evFork) cudaEventDestroy(evFork);
     if (evJoin) cudaEventDestroy(evJoin);
+    if (hostFirst) cudaStreamDestroy(hostFirst);
+    if (hostCompute) cudaStreamDestroy(hostCompute);
+    if (hostCopy) cudaStreamDestroy(hostCopy);
+    for (cudaEvent_t e : hostEv)
+      if (e) cudaEventDestroy(e);
   }
 };
 
