@@ -93,12 +93,35 @@ cudaError_t tc_gemm_splitk(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long 
   return cudaGetLastError();
 }
 
-cudaError_t tc_gemm_partials(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K, int splits,
-                             float *partial, cudaStream_t s) {
+cudaError_t tc_block_operand(const __nv_bfloat16 *W, long M, long K, int rowsPerSlice, __nv_bfloat16 *Wb,
+                             cudaStream_t s) {
+  if (K % tc::BK != 0 || (rowsPerSlice != tc::BM && !(rowsPerSlice == tc::THIN_BN && M <= tc::THIN_BN)))
+    return cudaErrorInvalidValue;
+  const long n = (M + rowsPerSlice - 1) / rowsPerSlice * (K / tc::BK) * rowsPerSlice * (tc::BK / 8);
+  tc::k_block_operand<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(W, M, K, rowsPerSlice, Wb);
+  return cudaGetLastError();
+}
+
+cudaError_t tc_gemm_thin_blocked(const __nv_bfloat16 *Ablk, const __nv_bfloat16 *Bblk, long M, long K, int splits,
+                                 float *partial, cudaStream_t s) {
+  constexpr int ST = tc::THIN_STAGES;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(tc::k_gemm_thin_blocked<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tc::blocked_smem_bytes(ST));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  int *err = nullptr;
+  cudaError_t e = cudaGetSymbolAddress((void **)&err, g_tc_err);
+  if (e != cudaSuccess) return e;
   const int kt = (int)(K / tc::BK);
   splits = std::max(1, std::min(splits, kt));
   const int per = (kt + splits - 1) / splits;
-  return launch_gemm(A, B, M, N, K, nullptr, tc::EPI_NONE, nullptr, nullptr, nullptr, splits, per, partial, s);
+  dim3 grid((unsigned)((M + tc::BM - 1) / tc::BM), (unsigned)splits);
+  tc::k_gemm_thin_blocked<ST><<<grid, tc::THREADS, tc::blocked_smem_bytes(ST), s>>>(Ablk, Bblk, M, kt, per, partial,
+                                                                                    err);
+  return cudaGetLastError();
 }
 
 // 1 if any tensor-core GEMM gave up waiting since the last call; clears it

@@ -67,8 +67,8 @@ __device__ __forceinline__ float delu_f(float a) { return a > 0.f ? 1.f : expf(a
 // split the layer-1 width (coalesced reads of W2's row r), their 1 + k partial
 // sums are added by a butterfly of shuffles.  Output Z[r][0] = h2,
 // Z[r][1 + c] = T2 (fp32), and when Zb is given the same values as bf16 rows
-// [1 + k (padded to 16)][h2] for the tensor-core output layer (B operand,
-// K-major).
+// [1 + k (padded to 16)][h2] for the tensor-core output layer (its B operand,
+// in the blocked slice layout of tc_gemm_thin_blocked).
 constexpr int kHiddenWarps = 8;
 
 template <int K, int H1>
@@ -122,14 +122,15 @@ k_decode_hidden(int h2, const float *__restrict__ W1, const float *__restrict__ 
   Z[(long)r * ld] = h;
 #pragma unroll
   for (int c = 0; c < K; ++c) Z[(long)r * ld + 1 + c] = d * acc[1 + c];
-  if (Zb) {
-    Zb[r] = __float2bfloat16_rn(h);
+  if (Zb) {  // B operand of the output layer, blocked as tc_gemm_thin_blocked reads it
+    Zb[tc::thin_b_index(0, r)] = __float2bfloat16_rn(h);
 #pragma unroll
-    for (int c = 0; c < K; ++c) Zb[(long)(1 + c) * h2 + r] = __float2bfloat16_rn(d * acc[1 + c]);
+    for (int c = 0; c < K; ++c) Zb[tc::thin_b_index(1 + c, r)] = __float2bfloat16_rn(d * acc[1 + c]);
   }
 }
 
-// tensor-core output layer: C [nst x 16] = W3b [nst x h2] Zb^T (fp32);
+// tensor-core output layer: C [nst x 16] = W3b [nst x h2] Zb^T (fp32), both
+// operands in the blocked slice layout (one bulk copy per 64-column slice);
 // y = uref + scale (C[., 0] + b3), D = scale C[., 1..k], from split-K partial
 // sums Cp[split][nst][16] added in split order (the output layer is short and
 // wide: K split over the SMs hides the latency of streaming the weights)
@@ -471,7 +472,7 @@ void decode_k(pda_lspg &L, const double *x, double *y, int first, cudaStream_t s
   } else if (L.tensorCore) {
     k_decode_hidden<K, 256><<<div_up(L.h2, kHiddenWarps), kHiddenWarps * 32, 0, s>>>(
         L.h2, L.W1.p, L.b1.p, L.W2.p, L.b2.p, x, L.Z.p, L.Zb.p, first, f);
-    PDA_CUDA(tc_gemm_partials(L.W3b.p, L.Zb.p, L.nst, 16, L.h2, kDecodeSplits, L.C.p, s));
+    PDA_CUDA(tc_gemm_thin_blocked(L.W3b.p, L.Zb.p, L.nst, L.h2, kDecodeSplits, L.C.p, s));
     k_decode_finish_split<K><<<div_up(L.nst, 256), 256, 0, s>>>(L.nst, std::min(kDecodeSplits, L.h2 / 64), L.C.p,
                                                                  L.b3.p, L.uref.p, L.scale.p, y, L.D.p, first, f);
   } else {
@@ -649,22 +650,27 @@ pda_status pda_lspg_create_mlp(pda_problem *sample_problem, const int64_t *sampl
     PDA_REQUIRE(h2 % 64 == 0 && k + 1 <= 16, PDA_ERR_UNSUPPORTED,
                 "tensor-core decoder: hidden width a multiple of 64 and latent at most 15");
     L->tensorCore = true;
-    L->W3b.alloc((size_t)L->nst * h2);
+    // the weights in bf16, then blocked by 128-row tiles and 64-column slices
+    // (rows past nst zero) so that each slice the GEMM reads is one block
+    pda::DevBuf<__nv_bfloat16> w3rows;
+    w3rows.alloc((size_t)L->nst * h2);
+    L->W3b.alloc((size_t)pda::div_up(L->nst, 128) * 128 * h2);
     L->Zb.alloc((size_t)16 * h2);
     L->C.alloc((size_t)pda::rom::kDecodeSplits * L->nst * 16);  // split-K partial sums
     PDA_CUDA(cudaMemset(L->Zb.p, 0, (size_t)16 * h2 * sizeof(__nv_bfloat16)));
     pda::DevBuf<int> bad;
     bad.alloc(1);
     PDA_CUDA(cudaMemset(bad.p, 0, sizeof(int)));
-    pda::rom::k_to_bf16_exact<<<pda::div_up(L->nst * (long)h2, 256), 256>>>(L->W3.p, L->W3b.p, L->nst * (long)h2,
+    pda::rom::k_to_bf16_exact<<<pda::div_up(L->nst * (long)h2, 256), 256>>>(L->W3.p, w3rows.p, L->nst * (long)h2,
                                                                              bad.p);
     PDA_CUDA(cudaGetLastError());
     int hb = 0;
     PDA_CUDA(cudaMemcpy(&hb, bad.p, sizeof(int), cudaMemcpyDeviceToHost));
     PDA_REQUIRE(hb == 0, PDA_ERR_INVALID_ARGUMENT,
                 "tensor-core decoder: output-layer weights are not bf16 values (use mode 0)");
+    PDA_CUDA(pda::tc_block_operand(w3rows.p, L->nst, h2, 128, L->W3b.p, nullptr));
     // one call before any capture: sets the GEMM's shared-memory attribute
-    PDA_CUDA(pda::tc_gemm_partials(L->W3b.p, L->Zb.p, L->nst, 16, h2, pda::rom::kDecodeSplits, L->C.p, nullptr));
+    PDA_CUDA(pda::tc_gemm_thin_blocked(L->W3b.p, L->Zb.p, L->nst, h2, pda::rom::kDecodeSplits, L->C.p, nullptr));
     PDA_CUDA(cudaDeviceSynchronize());
   } else {
     PDA_REQUIRE(mode == 0, PDA_ERR_INVALID_ARGUMENT, "mode must be 0 (fp32) or 1 (bf16 tensor cores)");

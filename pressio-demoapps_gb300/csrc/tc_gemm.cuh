@@ -47,11 +47,6 @@ __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-// byte offset of element (r, k) of a 128 x 64 bf16 slice in the canonical
-// K-major no-swizzle layout
-__device__ __forceinline__ uint32_t slice_offset(int r, int k) {
-  return (uint32_t)((((r >> 3) << 3) + (k >> 3)) << 7) + (uint32_t)((r & 7) << 4) + (uint32_t)((k & 7) << 1);
-}
 
 // shared-memory matrix descriptor: start, leading / stride byte offsets (in
 // 16-byte units), descriptor version 1, no swizzle
@@ -265,6 +260,175 @@ k_gemm_tn(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols) : "memory");
   }
+}
+
+// ---------------------------------------------------------------------------
+// Thin GEMM on pre-blocked operands, for a constant wide operand streamed
+// once per call (the ROM decoder's output layer, N = 16):
+//   partial[z][M][16] = sum over the K slices of split z of A B^T,
+// A blocked as Ablk[tile][slice] = the 128 x 64 bf16 slice of rows
+// 128 tile.. in the canonical K-major no-swizzle layout (16 KB, rows past M
+// zero) and B as Bblk[slice] = its 16 x 64 slice in the same layout (2 KB).
+// Each slice is then one contiguous block: thread 0 moves it with one bulk
+// copy (cp.async.bulk, the Tensor Memory Accelerator), counted on the stage's
+// `full` mbarrier by its bytes, issues the MMAs once it lands and commits them
+// to the stage's `empty` mbarrier, which frees the stage for slice kt + ST.
+// A CTA's slices are consecutive blocks (one sequential stream per CTA).
+// Every wait is bounded; on expiry the CTA flags the error, waits (bounded)
+// for the copies it issued and returns.
+// ---------------------------------------------------------------------------
+constexpr int BLK_A_BYTES = BM * BK * 2, BLK_B_BYTES = THIN_BN * BK * 2;
+__host__ __device__ constexpr int blocked_smem_bytes(int stages) {
+  return stages * (BLK_A_BYTES + BLK_B_BYTES) + 1024;
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+template <int ST>
+__global__ void __launch_bounds__(THREADS)
+k_gemm_thin_blocked(const __nv_bfloat16 *__restrict__ Ablk, const __nv_bfloat16 *__restrict__ Bblk, long M, int KT,
+                    int kSlices, float *__restrict__ partial, int *__restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t full[ST], empty[ST];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  constexpr int STAGE = BLK_A_BYTES + BLK_B_BYTES;
+  constexpr uint32_t kTmemCols = 32;
+  const uint32_t sbase = (smem_addr(smem_raw) + 1023u) & ~1023u;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long m0 = (long)blockIdx.x * BM;
+  const int kBegin = (int)blockIdx.y * kSlices;
+  const int KTc = max(0, min(kSlices, KT - kBegin));
+  if (threadIdx.x == 0) {
+    abort_flag = 0;
+    for (int s = 0; s < ST; ++s) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&full[s])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&empty[s])) : "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(&tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  constexpr uint32_t idesc = instr_desc(BM, THIN_BN);
+  const uint8_t *Ab = reinterpret_cast<const uint8_t *>(Ablk) + ((long)blockIdx.x * KT + kBegin) * BLK_A_BYTES;
+  const uint8_t *Bb = reinterpret_cast<const uint8_t *>(Bblk) + (long)kBegin * BLK_B_BYTES;
+  if (threadIdx.x == 0) {
+    int issued = 0;  // slices whose copies were issued
+    auto issue = [&](int slice) {
+      const int st = slice % ST;
+      const uint32_t sA = sbase + (uint32_t)(st * STAGE);
+      mbar_expect_tx(smem_addr(&full[st]), (uint32_t)STAGE);
+      bulk_g2s(sA, Ab + (long)slice * BLK_A_BYTES, BLK_A_BYTES, smem_addr(&full[st]));
+      bulk_g2s(sA + BLK_A_BYTES, Bb + (long)slice * BLK_B_BYTES, BLK_B_BYTES, smem_addr(&full[st]));
+      issued = slice + 1;
+    };
+    for (int p = 0; p < ST && p < KTc; ++p) issue(p);
+    bool ok = true;
+    for (int kt = 0; kt < KTc && ok; ++kt) {
+      const int st = kt % ST;
+      const uint32_t par = (uint32_t)((kt / ST) & 1);
+      if (!mbar_wait(smem_addr(&full[st]), par)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const uint32_t sA = sbase + (uint32_t)(st * STAGE), sB = sA + BLK_A_BYTES;
+#pragma unroll
+      for (int s = 0; s < BK / 16; ++s) {
+        const uint64_t ad = smem_desc(sA + (uint32_t)(s * 256), 128u, 1024u);
+        const uint64_t bd = smem_desc(sB + (uint32_t)(s * 256), 128u, 1024u);
+        const uint32_t acc = (kt > 0 || s > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                       smem_addr(&empty[st]))
+                   : "memory");
+      const int nx = kt + ST;
+      if (nx < KTc) {
+        // the stage is free once this slice's MMAs are done
+        if (!mbar_wait(smem_addr(&empty[st]), par)) {
+          ok = false;
+          break;
+        }
+        issue(nx);
+      }
+    }
+    if (ok && KTc > 0) {
+      const int last = KTc - 1;
+      if (!mbar_wait(smem_addr(&empty[last % ST]), (uint32_t)((last / ST) & 1))) ok = false;
+    }
+    if (!ok) {
+      abort_flag = 1;
+      // let the copies already issued land before the CTA's shared memory is released
+      for (int sl = max(0, issued - ST); sl < issued; ++sl) mbar_wait(smem_addr(&full[sl % ST]), (uint32_t)((sl / ST) & 1));
+    }
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  if (!abort_flag) {
+    const long row = m0 + warp * 32 + lane;
+    uint32_t r[16];
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+    if (row < M) {
+      float *pp = partial + ((long)blockIdx.y * M + row) * THIN_BN;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) pp[j] = KTc > 0 ? __uint_as_float(r[j]) : 0.f;
+    }
+  } else if (threadIdx.x == 0) {
+    atomicExch(err, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols) : "memory");
+  }
+}
+
+// row-major [M x K] bf16 -> the blocked layout of k_gemm_thin_blocked's A
+// (rows = 128-row tiles, zero past M; `rowsPerSlice` 128 for A, 16 for B
+// with M <= 16): one 16-byte chunk per thread
+__global__ void k_block_operand(const __nv_bfloat16 *__restrict__ W, long M, long K, int rowsPerSlice,
+                                __nv_bfloat16 *__restrict__ Wb) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long KT = K / BK, tiles = (M + rowsPerSlice - 1) / rowsPerSlice;
+  const int chunks = rowsPerSlice * (BK / 8);
+  if (i >= tiles * KT * chunks) return;
+  const long blk = i / chunks;
+  const int c = (int)(i % chunks);
+  const long t = blk / KT, sl = blk % KT;
+  const int r = c >> 3, kc = c & 7;
+  const long row = t * rowsPerSlice + r;
+  uint4 v = make_uint4(0u, 0u, 0u, 0u);
+  if (row < M) v = *reinterpret_cast<const uint4 *>(W + row * K + sl * BK + kc * 8);
+  *reinterpret_cast<uint4 *>(reinterpret_cast<uint8_t *>(Wb) + blk * (long)rowsPerSlice * BK * 2 +
+                             slice_offset(r, kc * 8)) = v;
 }
 
 // sum the split-K partials in split order, then the epilogue of k_gemm_tn
