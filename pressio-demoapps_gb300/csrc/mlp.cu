@@ -30,9 +30,8 @@ static cudaError_t gemm_attr() {
   return cudaSuccess;
 }
 
-// one launch of k_gemm_tn over all output tiles and `splits` K ranges of
-// `per` slices: the thin instantiation (N = 16 tiles, four stages) when B has
-// at most 16 rows, else 128 x 128 tiles with two stages
+// one launch of k_gemm_tn (128 x 128 tiles, two stages) over all output
+// tiles and `splits` K ranges of `per` slices
 static cudaError_t launch_gemm(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K,
                                const float *bias, int epi, float *outF, __nv_bfloat16 *outB, float *preact,
                                int splits, int per, float *partial, cudaStream_t s) {
@@ -40,19 +39,11 @@ static cudaError_t launch_gemm(const __nv_bfloat16 *A, const __nv_bfloat16 *B, l
   cudaError_t e = cudaGetSymbolAddress((void **)&err, g_tc_err);
   if (e != cudaSuccess) return e;
   const unsigned mt = (unsigned)((M + tc::BM - 1) / tc::BM);
-  if (N <= tc::THIN_BN) {
-    e = gemm_attr<tc::THIN_BN, tc::THIN_STAGES>();
-    if (e != cudaSuccess) return e;
-    tc::k_gemm_tn<tc::THIN_BN, tc::THIN_STAGES>
-        <<<dim3(1u, mt, (unsigned)splits), tc::THREADS, tc::smem_bytes(tc::THIN_BN, tc::THIN_STAGES), s>>>(
-            A, B, M, N, K, bias, epi, outF, outB, preact, err, per, partial);
-  } else {
-    e = gemm_attr<tc::BN, tc::STAGES>();
-    if (e != cudaSuccess) return e;
-    tc::k_gemm_tn<tc::BN, tc::STAGES>
-        <<<dim3((unsigned)((N + tc::BN - 1) / tc::BN), mt, (unsigned)splits), tc::THREADS, tc::SMEM_BYTES, s>>>(
-            A, B, M, N, K, bias, epi, outF, outB, preact, err, per, partial);
-  }
+  e = gemm_attr<tc::BN, tc::STAGES>();
+  if (e != cudaSuccess) return e;
+  tc::k_gemm_tn<tc::BN, tc::STAGES>
+      <<<dim3((unsigned)((N + tc::BN - 1) / tc::BN), mt, (unsigned)splits), tc::THREADS, tc::SMEM_BYTES, s>>>(
+          A, B, M, N, K, bias, epi, outF, outB, preact, err, per, partial);
   return cudaGetLastError();
 }
 
@@ -75,8 +66,7 @@ cudaError_t tc_gemm_splitk(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long 
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 1;
   }
-  const long bn = N <= tc::THIN_BN ? tc::THIN_BN : tc::BN;
-  const long tiles = ((N + bn - 1) / bn) * ((M + tc::BM - 1) / tc::BM);
+  const long tiles = ((N + tc::BN - 1) / tc::BN) * ((M + tc::BM - 1) / tc::BM);
   const int kt = (int)(K / tc::BK);
   int splits = 1;
   if (tiles < 2L * sms && kt >= 32) {
@@ -88,8 +78,8 @@ cudaError_t tc_gemm_splitk(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long 
   cudaError_t e = launch_gemm(A, B, M, N, K, nullptr, tc::EPI_NONE, nullptr, nullptr, nullptr, splits, per, work, s);
   if (e != cudaSuccess) return e;
   const long total = M * N;
-  tc::k_splitk_reduce<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(M, N, splits, work, bias, epi, outF, outB,
-                                                                       preact);
+  tc::k_splitk_reduce<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(M, N, splits, work, N, bias, epi, outF,
+                                                                       outB, preact);
   return cudaGetLastError();
 }
 
@@ -124,6 +114,38 @@ cudaError_t tc_gemm_thin_blocked(const __nv_bfloat16 *Ablk, const __nv_bfloat16 
   return cudaGetLastError();
 }
 
+// B with at most 16 rows: both operands blocked into scratch, the thin
+// blocked GEMM (K split over the SMs when the row tiles are few and K long),
+// then the split reduction with the epilogue
+static cudaError_t tc_gemm_thin(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K,
+                                const float *bias, int epi, float *outF, __nv_bfloat16 *outB, float *preact,
+                                cudaStream_t s) {
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long tiles = (M + tc::BM - 1) / tc::BM, kt = K / tc::BK;
+  int splits = 1;
+  if (tiles < 2L * sms && kt >= 32) splits = (int)std::min<long>((2L * sms + tiles - 1) / tiles, kt / 16);
+  __nv_bfloat16 *Ablk = nullptr, *Bblk = nullptr;
+  float *part = nullptr;
+  cudaError_t e = cudaMalloc((void **)&Ablk, (size_t)tiles * tc::BM * K * sizeof(__nv_bfloat16));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&Bblk, (size_t)tc::THIN_BN * K * sizeof(__nv_bfloat16));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&part, (size_t)splits * M * tc::THIN_BN * sizeof(float));
+  if (e == cudaSuccess) e = tc_block_operand(A, M, K, tc::BM, Ablk, s);
+  if (e == cudaSuccess) e = tc_block_operand(B, N, K, tc::THIN_BN, Bblk, s);
+  if (e == cudaSuccess) e = tc_gemm_thin_blocked(Ablk, Bblk, M, K, splits, part, s);
+  if (e == cudaSuccess) {
+    tc::k_splitk_reduce<<<(unsigned)((M * N + 255) / 256), 256, 0, s>>>(M, N, splits, part, tc::THIN_BN, bias, epi,
+                                                                          outF, outB, preact);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(Ablk);
+  cudaFree(Bblk);
+  cudaFree(part);
+  return e;
+}
+
 // 1 if any tensor-core GEMM gave up waiting since the last call; clears it
 int tc_gemm_error_and_clear() {
   int h = 0;
@@ -146,6 +168,19 @@ pda_status pda_tc_gemm_bf16(const void *d_A, const void *d_B, int64_t M, int64_t
     return PDA_ERR_INVALID_ARGUMENT;
   }
   cudaStream_t s = (cudaStream_t)stream;
+  if (N <= pda::tc::THIN_BN) {
+    const cudaError_t e = pda::tc_gemm_thin((const __nv_bfloat16 *)d_A, (const __nv_bfloat16 *)d_B, M, N, K, d_bias,
+                                            epilogue, d_outF, (__nv_bfloat16 *)d_outB, d_preact, s);
+    if (e != cudaSuccess) {
+      pda::set_last_error(std::string("pda_tc_gemm_bf16: ") + cudaGetErrorString(e));
+      return PDA_ERR_CUDA;
+    }
+    if (pda::tc_gemm_error_and_clear() != 0) {
+      pda::set_last_error("pda_tc_gemm_bf16: a tensor-core wait timed out");
+      return PDA_ERR_CUDA;
+    }
+    return PDA_OK;
+  }
   // split-K scratch for shapes with few output tiles and a long K
   float *work = nullptr;
   const long workFloats = 32L * M * N;

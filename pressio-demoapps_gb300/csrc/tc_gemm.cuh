@@ -431,15 +431,17 @@ __global__ void k_block_operand(const __nv_bfloat16 *__restrict__ W, long M, lon
                              slice_offset(r, kc * 8)) = v;
 }
 
-// sum the split-K partials in split order, then the epilogue of k_gemm_tn
-__global__ void k_splitk_reduce(long M, long N, int splits, const float *__restrict__ partial,
+// sum the split-K partials in split order, then the epilogue of k_gemm_tn;
+// partial[z][M][ldp] (ldp >= N: 16 for the thin blocked GEMM)
+__global__ void k_splitk_reduce(long M, long N, int splits, const float *__restrict__ partial, long ldp,
                                 const float *__restrict__ bias, int epi, float *__restrict__ outF,
                                 __nv_bfloat16 *__restrict__ outB, float *__restrict__ preact) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= M * N) return;
+  const long row = i / N, col = i % N;
   float v = 0.f;
-  for (int z = 0; z < splits; ++z) v += partial[(long)z * M * N + i];
-  if (epi != EPI_NONE) v += bias[i % N];
+  for (int z = 0; z < splits; ++z) v += partial[((long)z * M + row) * ldp + col];
+  if (epi != EPI_NONE) v += bias[col];
   if (preact) preact[i] = v;
   if (epi == EPI_BIAS_ELU) v = elu(v);
   if (outF) outF[i] = v;

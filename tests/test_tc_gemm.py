@@ -10,7 +10,8 @@ import pytest
 
 SHAPES = [(128, 128, 64), (256, 384, 128), (200, 130, 192), (256, 1024, 4096), (384, 256, 1024),
           (128, 256, 16384), (200, 100, 8192),  # the last two take the split-K path
-          # N <= 16: the thin tiles (the ROM decoder's output layer, 1 + k columns); the last two split K
+          # N <= 16: the thin blocked GEMM of the ROM decoder's output layer (operands blocked by
+          # 64-column slices, one bulk copy per slice); the last two split K
           (96, 12, 64), (1000, 13, 1024), (23916, 13, 1024), (300, 16, 4096), (2000, 1, 2048)]
 
 
