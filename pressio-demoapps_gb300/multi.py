@@ -4,7 +4,7 @@ ranks and the host-side reductions of the timing and metrics.
 The path has no exchange step: batched instances (different parameters and
 meshes) are independent, so rank r advances its share of the instances on
 its own GPU and only scalars cross ranks (the slowest rank's time, summed
-work counts).  A single large mesh is replicated, not split, in this build.
+work counts).  A single large mesh is replicated on every rank, not split.
 """
 from __future__ import annotations
 
