@@ -127,16 +127,30 @@ def build_workload(pda, torch, stream):
     return mesh, prob, U
 
 
-def cpu_baseline(pda, mesh, U, budget_s=10.0, threads=0):
-    """The oracle (C restatement of the reference algorithm) on the host cores."""
+def oracle_workload(threads=0):
+    """The headline workload built by the oracle alone: the mesh from
+    oracle/mesh_gen.py (the reference's mesh-script layout), the initial
+    condition from the oracle's restatement of riemann2dIC2 and the same
+    seeded noise; nothing from the library."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import mesh_gen
     import oracle_py
     orc = oracle_py.load()
     used = orc.set_threads(threads if threads > 0 else (os.cpu_count() or 1))
-    g, x, y, z, _, _ = mesh._arrays()
-    om = orc.mesh_from_arrays(2, 7, g, x, y, z, (mesh.dx(), mesh.dy(), 0.0))
-    op = orc.problem(om, 1, 4, 2, 2)
-    op.velocity(U)  # warm-up
+    mg = mesh_gen.full_mesh((N_CELLS_SIDE, N_CELLS_SIDE), (0.0, 1.0, 0.0, 1.0), 7, orc=orc)
+    op = orc.problem(mg.oracle_mesh(orc), 1, 4, 2, 2)
+    U0 = op.initial_condition()
+    rng = np.random.default_rng(20261203)
+    return orc, op, U0 + rng.uniform(-1e-3, 1e-3, U0.shape), used
+
+
+def cpu_baseline(U, V_gpu, budget_s=10.0, threads=0):
+    """The oracle (C restatement of the reference algorithm) on the host
+    cores: all threads for the reported value, one thread beside it, and the
+    oracle's velocity compared with the GPU's (the line's parity field)."""
+    orc, op, Uo, used = oracle_workload(threads)
+    assert np.array_equal(U, Uo), "the library's and the oracle's workloads differ"
+    Vo = op.velocity(U)  # warm-up, and the parity reference
     times = []
     t_end = time.perf_counter() + budget_s
     while time.perf_counter() < t_end or len(times) < 2:
@@ -145,33 +159,35 @@ def cpu_baseline(pda, mesh, U, budget_s=10.0, threads=0):
         times.append(time.perf_counter() - t0)
     cells = N_CELLS_SIDE * N_CELLS_SIDE
     med = statistics.median(times)
+    orc.set_threads(1)
+    t0 = time.perf_counter()
+    op.velocity(U)
+    one = time.perf_counter() - t0
+    orc.set_threads(used)
     import platform
-    return {"value": cells / med / 1e9, "unit": "Gcell/s", "cores": used, "kind": "port",
+    diff = np.abs(V_gpu - Vo)
+    scale = np.maximum(np.abs(Vo), 1e-3 * np.max(np.abs(Vo.reshape(-1, NDPC)), axis=0)[None, :].repeat(
+        Vo.size // NDPC, axis=0).reshape(-1))
+    parity = {"reference": "oracle (C restatement, bit-identical to the reference on the golden cases)",
+              "bitwise": bool(np.array_equal(V_gpu, Vo)), "max_abs": float(diff.max()),
+              "max_rel": float(np.max(diff / scale)), "rule": "per cell, floor 1e-3 x field max"}
+    base = {"value": cells / med / 1e9, "unit": "Gcell/s", "cores": used, "kind": "port",
             "sample": f"{len(times)} velocity() calls of the same 1024^2 Riemann WENO5 workload on {used} "
                       f"threads of {platform.machine()} ({os.cpu_count()} logical CPUs); median "
-                      f"{med * 1e3:.1f} ms/call"}
+                      f"{med * 1e3:.1f} ms/call",
+            "single_thread": {"value": cells / one / 1e9, "unit": "Gcell/s", "cores": 1,
+                              "sample": f"one call on 1 thread, {one * 1e3:.0f} ms"}}
+    return base, parity
 
 
 def run_reference(args):
+    """The reference's CPU algorithm (the oracle port; the reference C++ is
+    header-only and not on the GPU host) on all host cores, mesh and initial
+    condition from the oracle itself: no library code on this path."""
     rank, world, _ = rank_info()
     if rank != 0:
         return 0
-    import importlib
-    ge = importlib.import_module("__graft_entry__")
-    pda = ge.package()
-    mesh = pda.create_full_mesh((N_CELLS_SIDE, N_CELLS_SIDE), (0.0, 1.0, 0.0, 1.0), 7)
-    # host-only calls: the initial condition and the mesh arrays need no GPU
-    prob = pda.create_problem(mesh, pda.Euler2d.Riemann, pda.InviscidFluxReconstruction.Weno5, 2, stream=0)
-    U0 = prob.initialConditionHost()
-    rng = np.random.default_rng(20261203)
-    U = U0 + rng.uniform(-1e-3, 1e-3, U0.shape)
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import oracle_py
-    orc = oracle_py.load()
-    used = orc.set_threads(os.cpu_count() or 1)
-    g, x, y, z, _, _ = mesh._arrays()
-    om = orc.mesh_from_arrays(2, 7, g, x, y, z, (mesh.dx(), mesh.dy(), 0.0))
-    op = orc.problem(om, 1, 4, 2, 2)
+    orc, op, U, used = oracle_workload()
     for _ in range(args.warmup):
         op.velocity(U)
     ts = []
@@ -190,8 +206,9 @@ def run_reference(args):
             "config": workload_config(),
             "cpu_baseline": {"value": value, "unit": "Gcell/s", "cores": used, "kind": "port",
                              "sample": f"{args.steps} full 1024^2 velocity() calls on {used} threads of "
-                                       f"{platform.machine()}; reference C++ not compiled on the GPU host "
-                                       f"(C restatement timed, bit-identical results)"},
+                                       f"{platform.machine()}; the oracle's C restatement, bit-identical to "
+                                       f"the reference (header-only C++, no checkout on the GPU host); mesh "
+                                       f"and initial condition built by the oracle"},
             "e2e": {"value": value, "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -824,7 +841,7 @@ def main():
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(pda, mesh, Uh, budget_s=args.cpu_budget)
+        line["cpu_baseline"], line["parity"] = cpu_baseline(Uh, V.cpu().numpy(), budget_s=args.cpu_budget)
     if not args.no_extra:
         del U, V, flush
         torch.cuda.empty_cache()

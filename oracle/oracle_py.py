@@ -48,6 +48,7 @@ def load():
         L.orc_weno5.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_weno3.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_set_cube_mode.argtypes = [C.c_int]
+        L.orc_round14.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
         L.orc_set_threads.restype = C.c_int
         L.orc_set_threads.argtypes = [C.c_int]
         _L = L
@@ -150,6 +151,13 @@ class Oracle:
     def set_cube_mode(self, correctly_rounded):
         """0: x^3 by pow (the reference); 1: correctly rounded (the library)."""
         self.L.orc_set_cube_mode(int(bool(correctly_rounded)))
+
+    def round14(self, v):
+        """strtod(sprintf("%.14f", v)) element-wise: a mesh-script coordinate as read back."""
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        out = np.empty_like(v)
+        self.L.orc_round14(_vp(v), _vp(out), v.size)
+        return out
 
     def set_threads(self, n):
         return self.L.orc_set_threads(n)

@@ -1474,6 +1474,18 @@ int orc_set_threads(int n) {
 #endif
 }
 
+/* The value the reference's mesh reader gets for a coordinate the mesh
+ * scripts wrote with "%.14f" (meshing_scripts/create_full_mesh.py), element
+ * by element: printf then strtod, both correctly rounded. */
+void orc_round14(const double *in, double *out, int64_t n) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    char buf[64];
+    snprintf(buf, sizeof buf, "%.14f", in[i]);
+    out[i] = strtod(buf, NULL);
+  }
+}
+
 /* ------------------------------------------------ point-wise test exports */
 void orc_weno5_face_grad(const double q[6], double u[2], double gN[6], double gP[6]) {
   weno5_grad_impl(&u[0], &u[1], gN, gP, q[0], q[1], q[2], q[3], q[4], q[5]);

@@ -45,6 +45,8 @@ void orc_point_flux(int family, int ax, const double *qL, const double *qR, doub
                     double *JL, double *JR);
 /* 0: pow(x, 3.) as the reference (default); 1: correctly rounded x^3 */
 void orc_set_cube_mode(int correctly_rounded);
+/* out[i] = strtod(sprintf("%.14f", in[i])): mesh-script coordinates as read back */
+void orc_round14(const double *in, double *out, int64_t n);
 /* OpenMP threads for the CPU baseline (<= 0: all). Returns the count used. */
 int orc_set_threads(int n);
 

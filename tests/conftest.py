@@ -109,15 +109,16 @@ def j_close(got, ref, rowptr, rtol=1e-12, floor_frac=1e-3):
     if not np.array_equal(np.isnan(got), np.isnan(ref)):
         return False, float("inf")
     got, ref = np.nan_to_num(got, nan=0.0), np.nan_to_num(ref, nan=0.0)
-    rows = len(rowptr) - 1
-    rmax = np.zeros(rows)
+    if len(ref) == 0:
+        return True, 0.0
+    rowptr = np.asarray(rowptr, dtype=np.int64)
+    counts = np.diff(rowptr)
     absr = np.abs(ref)
-    for r in range(rows):
-        a, b = rowptr[r], rowptr[r + 1]
-        if b > a:
-            rmax[r] = absr[a:b].max()
-    rowof = np.repeat(np.arange(rows), np.diff(rowptr))
-    tol = rtol * np.maximum(absr, floor_frac * rmax[rowof])
+    rmax = np.zeros(len(counts))
+    nz = counts > 0
+    rmax[nz] = np.maximum.reduceat(absr, rowptr[:-1][nz])
+    tol = rtol * np.maximum(absr, floor_frac * np.repeat(rmax, counts))
     tol = np.maximum(tol, 1e-300)
-    bad = np.abs(got - ref) > tol
-    return (not bad.any()), float(np.max(np.abs(got - ref) / tol * rtol)) if len(ref) else 0.0
+    err = np.abs(got - ref)
+    bad = err > tol
+    return (not bad.any()), float(np.max(err / tol * rtol))

@@ -1,7 +1,7 @@
 """Generate the golden fixtures under tests/golden/ from the reference.
 
-Runs only where the reference checkout exists (it reads REF, default
-/root/reference).  It
+Runs only where a reference checkout exists; its location comes from the
+environment variable PDA_REFERENCE (required).  It
   1. runs the reference's own mesh scripts (meshing_scripts/create_full_mesh.py,
      create_sample_mesh.py) into tests/golden/meshes/<name>/,
   2. evaluates the reference itself through oracle/_ref/libpdaref.so (built by
@@ -13,7 +13,7 @@ Runs only where the reference checkout exists (it reads REF, default
      tests/golden/gold/, checking on the way that the reference shim
      reproduces them.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  PDA_REFERENCE=<checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -29,7 +29,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("PDA_REFERENCE", "/root/reference")
+REF = os.environ.get("PDA_REFERENCE", "")
 MESHES = os.path.join(HERE, "meshes")
 CASES = os.path.join(HERE, "cases")
 GOLD = os.path.join(HERE, "gold")
@@ -460,6 +460,8 @@ def make_gold(ref: Ref):
 
 
 def main():
+    if not REF or not os.path.isdir(os.path.join(REF, "include", "pressiodemoapps")):
+        sys.exit("set PDA_REFERENCE to a pressio-demoapps checkout")
     make_meshes()
     ref = Ref()
     manifest = make_cases(ref)

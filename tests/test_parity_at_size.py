@@ -1,0 +1,211 @@
+"""GPU parity at the benchmark workloads' own sizes, against the oracle.
+
+The golden suite pins the device path to the reference on small meshes.
+Here the device path meets the oracle (the C restatement, itself pinned bit
+for bit to the reference) on the configurations the benchmark times, so the
+tiled face kernels run with many tiles per line, halo chunks and all, and
+the CSR assembly runs at full size:
+
+* 2D Euler four-quadrant Riemann (IC2), 1024 x 1024, WENO5: velocity on the
+  initial condition and on IC + seeded U[-1e-3, 1e-3] noise bit for bit;
+  CSR row pointers and column indices bit for bit, values bit for bit
+  against the oracle with the correctly rounded x^3 and within 1e-12 of the
+  row scale against the oracle's pow(x, 3.) (the reference's arithmetic);
+* 1D Sod, 1000 cells, WENO5, SSP-RK3 dt = 1e-4 for the full 2000 steps:
+  final state bit for bit;
+* 3D Euler smooth periodic, WENO5: velocity at 256^3 (IC + noise) bit for
+  bit; CSR Jacobian at 96^3 bit for bit (correctly rounded cube);
+* batched 2D shallow-water slip wall: one instance of every mesh size the
+  512-instance batch draws (n = 64, 96, ..., 512, with that draw's
+  parameters), batched velocity and one batched SSP-RK3 step against the
+  oracle per instance, within 1e-13 per cell (the shallow-water flux takes
+  sqrt(h) for the reference's pow(h, 0.5)).
+
+Meshes for the oracle come from oracle/mesh_gen.py (a restatement of the
+reference's mesh scripts), not from the library.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ORACLE_DIR, j_close, v_close
+
+pytestmark = pytest.mark.gpu
+
+SEED = 20261203
+
+
+def _torch():
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need CUDA"
+    return torch
+
+
+def _mesh_gen():
+    sys.path.insert(0, ORACLE_DIR)
+    import mesh_gen
+    return mesh_gen
+
+
+@pytest.fixture(scope="module")
+def orc_all(oracle):
+    oracle.set_threads(os.cpu_count() or 1)
+    return oracle
+
+
+def _pair(pda, orc, n, bounds, stencil, periodic, family_enum, fam, prob, scheme, ic, params=None):
+    """The library problem and the oracle problem of one configuration."""
+    mg = _mesh_gen().full_mesh(n, bounds, stencil, periodic, orc=orc)
+    mesh = pda.create_full_mesh(n, bounds, stencil, periodic)
+    g, x, y, z, _, _ = mesh._arrays()
+    # the two generators agree, so both sides see the same mesh
+    assert np.array_equal(g, mg.graph) and np.array_equal(x, mg.x) and np.array_equal(y, mg.y)
+    p = pda.create_problem(mesh, family_enum, pda.InviscidFluxReconstruction(scheme), ic, params)
+    op = orc.problem(mg.oracle_mesh(orc), fam, prob, scheme, ic, params)
+    return mesh, p, op
+
+
+@pytest.fixture(scope="module")
+def riemann1024(pda, orc_all):
+    mesh, p, op = _pair(pda, orc_all, (1024, 1024), (0.0, 1.0, 0.0, 1.0), 7, (False, False),
+                        pda.Euler2d.Riemann, 1, 4, 2, 2)
+    U0 = op.initial_condition()
+    rng = np.random.default_rng(SEED)
+    U1 = U0 + rng.uniform(-1e-3, 1e-3, U0.shape)
+    return mesh, p, op, U0, U1
+
+
+def test_riemann_1024_initial_condition_and_velocity_bitwise(riemann1024):
+    torch = _torch()
+    mesh, p, op, U0, U1 = riemann1024
+    assert np.array_equal(p.initialCondition().cpu().numpy(), U0)
+    for U in (U0, U1):
+        V = p.createVelocity()
+        p.velocity(torch.from_numpy(U).cuda(), 0.0, V)
+        got, want = V.cpu().numpy(), op.velocity(U)
+        assert np.array_equal(got, want), f"{np.sum(got != want)} of {got.size} velocity entries differ"
+
+
+def test_riemann_1024_jacobian(riemann1024, orc_all):
+    torch = _torch()
+    mesh, p, op, U0, U1 = riemann1024
+    J = p.createJacobian()
+    V = p.createVelocity()
+    p.rightHandSideAndJacobian(torch.from_numpy(U1).cuda(), 0.0, V, J)
+    jv = J.values.cpu().numpy()
+    rp, ci = J.rowptr.cpu().numpy(), J.colidx.cpu().numpy()
+    del J
+    orc_all.set_cube_mode(1)
+    try:
+        Vo, rpo, cio, jo = op.velocity_and_jacobian(U1)
+    finally:
+        orc_all.set_cube_mode(0)
+    assert np.array_equal(rp, rpo) and np.array_equal(ci, cio)
+    del cio
+    assert np.array_equal(V.cpu().numpy(), Vo)
+    assert np.array_equal(jv, jo), f"{np.sum(jv != jo)} of {jv.size} Jacobian values differ"
+    del jo
+    _, _, _, jr = op.velocity_and_jacobian(U1)  # pow(x, 3.): the reference's arithmetic
+    ok, worst = j_close(jv, jr, rp, rtol=1e-12, floor_frac=1.0)
+    assert ok, f"worst {worst:.3e} of the row scale"
+
+
+def test_sod_1000_cells_2000_steps_bitwise(pda, orc_all):
+    torch = _torch()
+    mesh, p, op = _pair(pda, orc_all, (1000,), (-0.5, 0.5), 7, (False,), pda.Euler1d.Sod, 0, 1, 2, 1)
+    U = p.initialCondition()
+    Uo = op.initial_condition()
+    assert np.array_equal(U.cpu().numpy(), Uo)
+    V = p.createVelocity()
+    p.velocity(U, 0.0, V)
+    assert np.array_equal(V.cpu().numpy(), op.velocity(Uo))
+    p.advance_ssprk3(U, 0.0, 1e-4, 2000)
+    op.ssprk3(Uo, 0.0, 1e-4, 2000)
+    got = U.cpu().numpy()
+    assert np.array_equal(got, Uo), f"max |diff| {np.max(np.abs(got - Uo)):.3e}"
+    p.velocity(U, 0.2, V)
+    assert np.array_equal(V.cpu().numpy(), op.velocity(Uo, 0.2))
+    torch.cuda.synchronize()
+
+
+def test_euler3d_weno5_velocity_256_bitwise(pda, orc_all):
+    torch = _torch()
+    b = (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0)
+    mesh, p, op = _pair(pda, orc_all, (256, 256, 256), b, 7, (True, True, True), pda.Euler3d.PeriodicSmooth,
+                        2, 0, 2, 1)
+    U0 = op.initial_condition()
+    assert np.array_equal(p.initialCondition().cpu().numpy(), U0)
+    rng = np.random.default_rng(SEED)
+    U1 = U0 + rng.uniform(-1e-3, 1e-3, U0.shape)
+    V = p.createVelocity()
+    p.velocity(torch.from_numpy(U1).cuda(), 0.0, V)
+    got, want = V.cpu().numpy(), op.velocity(U1)
+    assert np.array_equal(got, want), f"{np.sum(got != want)} of {got.size} velocity entries differ"
+
+
+def test_euler3d_weno5_jacobian_96(pda, orc_all):
+    torch = _torch()
+    b = (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0)
+    mesh, p, op = _pair(pda, orc_all, (96, 96, 96), b, 7, (True, True, True), pda.Euler3d.PeriodicSmooth,
+                        2, 0, 2, 1)
+    rng = np.random.default_rng(SEED + 1)
+    U1 = op.initial_condition() + rng.uniform(-1e-3, 1e-3, p.totalDofStencilMesh())
+    J = p.createJacobian()
+    V = p.createVelocity()
+    p.rightHandSideAndJacobian(torch.from_numpy(U1).cuda(), 0.0, V, J)
+    jv = J.values.cpu().numpy()
+    rp, ci = J.rowptr.cpu().numpy(), J.colidx.cpu().numpy()
+    del J
+    orc_all.set_cube_mode(1)
+    try:
+        Vo, rpo, cio, jo = op.velocity_and_jacobian(U1)
+    finally:
+        orc_all.set_cube_mode(0)
+    assert np.array_equal(rp, rpo) and np.array_equal(ci, cio)
+    del ci, cio
+    assert np.array_equal(V.cpu().numpy(), Vo)
+    assert np.array_equal(jv, jo), f"{np.sum(jv != jo)} of {jv.size} Jacobian values differ"
+
+
+def _batch_draw(n_inst=512):
+    """The 512-instance batch's draw (sizes and parameters, seeded)."""
+    brng = np.random.default_rng(512)
+    ns = brng.choice(np.arange(64, 513, 32), size=n_inst)
+    grav = brng.uniform(5.0, 10.0, n_inst)
+    cor = brng.uniform(-4.0, -1.0, n_inst)
+    amp = brng.uniform(0.05, 0.2, n_inst)
+    return ns, grav, cor, amp
+
+
+def test_batched_swe_one_instance_per_size(pda, orc_all):
+    torch = _torch()
+    ns, grav, cor, amp = _batch_draw()
+    first = [int(np.flatnonzero(ns == n)[0]) for n in sorted(set(ns.tolist()))]
+    assert len(first) == 15
+    probs, oprobs = [], []
+    for i in first:
+        n = int(ns[i])
+        prm = {"gravity": float(grav[i]), "coriolis": float(cor[i]), "pulseMagnitude": float(amp[i])}
+        _, p, op = _pair(pda, orc_all, (n, n), (-5.0, 5.0, -5.0, 5.0), 7, (False, False), pda.Swe2d.SlipWall,
+                         3, 0, 2, 1, prm)
+        probs.append(p)
+        oprobs.append(op)
+    B = pda.create_batch(probs)
+    U = B.initialCondition()
+    V = torch.empty_like(U)
+    B.velocity(U, 0.0, V)
+    for k, op in enumerate(oprobs):
+        Uo = op.initial_condition()
+        assert np.array_equal(B.instance(U, k).cpu().numpy(), Uo)
+        ok, worst = v_close(B.instance(V, k).cpu().numpy(), op.velocity(Uo), 3)
+        assert ok, f"n = {int(ns[first[k]])}: velocity worst {worst:.3e}"
+    B.advance_ssprk3(U, 0.0, 0.005, 1)
+    for k, op in enumerate(oprobs):
+        Uo = op.initial_condition()
+        op.ssprk3(Uo, 0.0, 0.005, 1)
+        ok, worst = v_close(B.instance(U, k).cpu().numpy(), Uo, 3)
+        assert ok, f"n = {int(ns[first[k]])}: state after one step worst {worst:.3e}"
