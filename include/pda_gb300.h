@@ -350,9 +350,19 @@ pda_status pda_lspg_decode(pda_lspg *rom, const double *d_x, double *d_y);
  * gn_iters Gauss-Newton iterations per step (stopping early once the
  * correction norm is below tol); use_graph != 0 replays one captured step.
  * info (may be NULL) receives {last correction norm, iterations of the last
- * step, residual norm at the last iterate, max over steps of that norm}. */
+ * step, residual norm at the last iterate, max of that norm over the
+ * iterates of this call's steps}. */
 pda_status pda_lspg_advance_bdf1(pda_lspg *rom, double *d_x, double dt, int64_t n_steps, int gn_iters,
                                  double tol, int use_graph, double *info);
+/* The same with the backward-difference order chosen: order 1 (BDF1) or 2
+ * (BDF2: R = y_n+1 - 4/3 y_n + 1/3 y_n-1 - 2/3 dt f(y_n+1)).  first_step is
+ * the 1-based index, within the trajectory, of the first step this call
+ * takes; as in Pressio's BDF2 LSPG (rom/impl/lspg_unsteady_rj_policy_hypred.hpp:
+ * 124-134) step 1 is a BDF1 step, and each step's first Gauss-Newton iteration
+ * moves the stored y_n to y_n-1, so consecutive calls continue one
+ * trajectory when first_step continues its numbering. */
+pda_status pda_lspg_advance(pda_lspg *rom, double *d_x, double dt, int64_t n_steps, int gn_iters, double tol,
+                            int order, int64_t first_step, int use_graph, double *info);
 
 /* Gauss-Newton iteration form: fused = 1 (default) evaluates the sample-mesh
  * velocity and the product of its Jacobian with the trial space's latent
@@ -400,6 +410,16 @@ pda_status pda_profile_velocity(pda_problem *p, const double *d_U, double *d_V, 
 
 /* Measured FP64 FMA throughput of the current device (FLOP/s, FMA = 2). */
 pda_status pda_measure_fp64_peak(double *flops_per_s);
+
+/* Self-check of the integer-pipe division and square root the kernels use
+ * for every FP64 division and square root: on (SMs x 2048 threads) x
+ * per_thread seeded operand sets of the given mode (0 normal-range
+ * operands, 1 divisor mantissas near the ends of [1, 2), 2 near-exact
+ * quotients and roots, 3 arbitrary bit patterns), compares each result with
+ * the FP64 pipe's IEEE division and square root bit for bit.  counts receives
+ * {operand sets, division mismatches, square-root mismatches}.  No
+ * counterpart in the reference (whose divisions are the CPU's). */
+pda_status pda_check_divsqrt(int mode, uint64_t seed, int64_t per_thread, int64_t counts[3]);
 
 #ifdef __cplusplus
 }

@@ -1,14 +1,15 @@
 """Test infrastructure only (the oracle): numpy restatement of hyper-reduced
-LSPG with BDF1 and Gauss-Newton, the algorithm of Pressio's
+LSPG with BDF1 / BDF2 and Gauss-Newton, the algorithm of Pressio's
 LspgUnsteadyResidualJacobianPolicyHypRed
 (tests_cpp/pressio/include/pressio/rom/impl/lspg_unsteady_rj_policy_hypred.hpp:
-180-264; BDF1 constants c_np1 = 1, c_n = -1, c_f = -1 from
-ode/ode_constants.hpp:61-63), over the C oracle's sample-mesh velocity and
-Jacobian.  Imported by tests/ only.
+100-264; constants from ode/ode_constants.hpp:57-73: BDF1 c_n = -1, c_f = -1;
+BDF2 c_n = -4/3, c_nm1 = 1/3, c_f = -2/3, whose first step is a BDF1 step),
+over the C oracle's sample-mesh velocity and Jacobian.  Imported by tests/
+only.
 
 Per step n -> n+1 and iteration, with y(x) the trial state on the stencil mesh
 and D = dy/dx:
-    R  = cf V(y) + (y - y_n)|sample,        cf = -dt
+    R  = cf V(y) + (y + c_n y_n [+ c_nm1 y_nm1])|sample,   cf = c_f dt
     JR = cf Jf(y) D + D|sample
     (JR^T JR) dx = JR^T R,   x <- x - dx   (stop when |dx| < tol)
 """
@@ -50,22 +51,31 @@ def mlp_decoder(uref, scale, W1, b1, W2, b2, W3, b3):
     return dec
 
 
-def lspg_bdf1(problem, s2st, decoder, x0, dt, n_steps, iters=5, tol=1e-10):
+def lspg_bdf(problem, s2st, decoder, x0, dt, n_steps, order=1, iters=5, tol=1e-10):
     """problem: oracle Problem on the sample mesh; returns (x, [x per step])."""
     sd = sample_dofs(s2st, problem.ndpc)
     x = np.array(x0, dtype=np.float64)
     traj = []
-    for _ in range(n_steps):
+    ynm1 = None
+    for step in range(1, n_steps + 1):
         yn = decoder(x)[0][sd]
+        two = order == 2 and step > 1
+        cf, cn, cnm1 = ((-1. * (2. / 3.) * dt, -1. * (4. / 3.), 1. / 3.) if two else (-1. * dt, -1., 0.))
         for _ in range(iters):
             y, D = decoder(x)
             V, rp, ci, jv = problem.velocity_and_jacobian(y)
             J = sp.csr_matrix((jv, ci, rp), shape=(len(rp) - 1, len(y)))
-            R = -dt * V + (y[sd] - yn)
-            JR = -dt * (J @ D) + D[sd]
+            helper = 1. * y[sd] + cn * yn + cnm1 * ynm1 if two else 1. * y[sd] + cn * yn
+            R = cf * V + helper
+            JR = cf * (J @ D) + D[sd]
             dx = np.linalg.solve(JR.T @ JR, JR.T @ R)
             x = x - dx
             if np.linalg.norm(dx) < tol:
                 break
+        ynm1 = yn
         traj.append(x.copy())
     return x, traj
+
+
+def lspg_bdf1(problem, s2st, decoder, x0, dt, n_steps, iters=5, tol=1e-10):
+    return lspg_bdf(problem, s2st, decoder, x0, dt, n_steps, 1, iters, tol)

@@ -119,6 +119,7 @@ _SIGS = {
     "pda_profile_velocity": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                        C.POINTER(C.c_double)]),
     "pda_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
+    "pda_check_divsqrt": (C.c_int, [C.c_int, C.c_uint64, C.c_int64, C.c_void_p]),
     "pda_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_void_p, C.POINTER(C.c_void_p)]),
     "pda_batch_free": (None, [C.c_void_p]),
     "pda_batch_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int64),
@@ -158,6 +159,8 @@ _SIGS = {
     "pda_lspg_set_jacobian_precision": (C.c_int, [C.c_void_p, C.c_int]),
     "pda_lspg_advance_bdf1": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int64, C.c_int, C.c_double,
                                         C.c_int, C.c_void_p]),
+    "pda_lspg_advance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int64, C.c_int, C.c_double,
+                                   C.c_int, C.c_int64, C.c_int, C.c_void_p]),
 }
 
 
@@ -537,6 +540,16 @@ def measure_fp64_peak():
     return v.value
 
 
+def check_divsqrt(mode, seed=1, per_thread=4096):
+    """Bit-for-bit comparison of the kernels' integer-pipe division and square
+    root with the FP64 pipe's IEEE operations on seeded operands; returns
+    (operand sets, division mismatches, square-root mismatches)."""
+    import numpy as np
+    c = np.zeros(3, dtype=np.int64)
+    _check(lib().pda_check_divsqrt(int(mode), int(seed), int(per_thread), c.ctypes.data_as(C.c_void_p)))
+    return tuple(int(v) for v in c)
+
+
 def _stream_handle(stream):
     if stream is None:
         try:
@@ -806,9 +819,16 @@ class LspgRom:
         return y
 
     def advance_bdf1(self, x, dt, n_steps, gn_iters=5, tol=1e-10, use_graph=True):
+        return self.advance(x, dt, n_steps, gn_iters, tol, order=1, first_step=1, use_graph=use_graph)
+
+    def advance(self, x, dt, n_steps, gn_iters=5, tol=1e-10, order=1, first_step=1, use_graph=True):
+        """n_steps BDF1 (order 1) or BDF2 (order 2) LSPG steps; first_step is
+        the 1-based index of the first of them in the trajectory (BDF2 takes
+        step 1 with BDF1, as Pressio does)."""
         import numpy as np
         info = np.zeros(4)
-        _check(lib().pda_lspg_advance_bdf1(self._h, _vp(x), float(dt), int(n_steps), int(gn_iters), float(tol),
-                                           int(bool(use_graph)), info.ctypes.data_as(C.c_void_p)))
+        _check(lib().pda_lspg_advance(self._h, _vp(x), float(dt), int(n_steps), int(gn_iters), float(tol),
+                                      int(order), int(first_step), int(bool(use_graph)),
+                                      info.ctypes.data_as(C.c_void_p)))
         return {"last_correction": info[0], "iters_last_step": int(info[1]), "residual": info[2],
                 "max_residual": info[3]}

@@ -61,6 +61,8 @@ void launch_axpby_stage(int kind, double *out, const double *a, const double *b,
                         long n, cudaStream_t s);
 // FP64 FMA throughput probe: returns FLOP/s measured with CUDA events
 double measure_fp64_fma_rate(int blocks, int threads, int iters, cudaStream_t s);
+// counts = {operand sets, division mismatches, square-root mismatches}
+void check_divsqrt(int mode, uint64_t seed, long per_thread, long long counts[3], cudaStream_t s);
 void launch_csr_spmm(long rows, const int *rowptr, const int *colidx, const double *vals,
                      const double *B, long ldb, int ncols, double *R, long ldr, cudaStream_t s);
 

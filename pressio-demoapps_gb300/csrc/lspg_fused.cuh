@@ -447,8 +447,13 @@ k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p,
         const int r = t.rows[e];
         a.V[(size_t)r * NDPC + k] = vk;
         const double ynp1 = sY[rl][k];
-        if (a.first) a.yn[(size_t)r * NDPC + k] = ynp1;
-        const double helper = 1. * ynp1 + (-1.) * a.yn[(size_t)r * NDPC + k];
+        const size_t q = (size_t)r * NDPC + k;
+        if (a.first) {
+          a.ynm1[q] = a.yn[q];
+          a.yn[q] = ynp1;
+        }
+        // Pressio's ops::update(helper, 0, y_n+1, 1, y_n, cn[, y_n-1, cnm1])
+        const double helper = a.bdf2 ? 1. * ynp1 + a.cn * a.yn[q] + a.cnm1 * a.ynm1[q] : 1. * ynp1 + a.cn * a.yn[q];
         val = a.cf * vk + 1. * helper;
       }
     }

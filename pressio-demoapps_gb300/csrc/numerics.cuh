@@ -27,6 +27,8 @@
 
 #include <math.h>
 
+#include "fp64_intpipe.cuh"
+
 #if defined(__CUDACC__)
 #define PDA_HD __host__ __device__ __forceinline__
 #else
@@ -42,6 +44,37 @@ template <int S> struct SchemeTraits;
 template <> struct SchemeTraits<FirstOrder> { static constexpr int h = 1; };
 template <> struct SchemeTraits<Weno3> { static constexpr int h = 2; };
 template <> struct SchemeTraits<Weno5> { static constexpr int h = 3; };
+
+// Division and square root of runtime operands.  Device code computes them
+// on the integer pipe (fp64_intpipe.cuh): the IEEE round-to-nearest results,
+// bit for bit, without occupying GB300's FP64 pipe (one warp instruction per
+// ~64 cycles per SM sub-partition), which is left to the multiplications and
+// additions.  INL = true expands them in place (the residual's face kernels);
+// otherwise they are calls.  Host code uses the operators.  Compiling with
+// -DPDA_FP64_PIPE_DIVSQRT selects the FP64-pipe operations on the device too
+// (the same results), for comparison.
+template <bool INL = false>
+PDA_HD double div_rn(double a, double b) {
+#if defined(__CUDA_ARCH__) && !defined(PDA_FP64_PIPE_DIVSQRT)
+  if constexpr (INL) return ip::div(a, b);
+  else return ip::div_call(a, b);
+#else
+  return a / b;
+#endif
+}
+template <bool INL = false>
+PDA_HD double sqrt_rn(double x) {
+#if defined(__CUDA_ARCH__) && !defined(PDA_FP64_PIPE_DIVSQRT)
+  if constexpr (INL) return ip::sqrt(x);
+  else return ip::sqrt_call(x);
+#else
+  return sqrt(x);
+#endif
+}
+template <bool INL = false>
+PDA_HD float div_rn(float a, float b) { return a / b; }
+template <bool INL = false>
+PDA_HD float sqrt_rn(float x) { return sqrtf(x); }
 
 template <typename T> PDA_HD T sq(T x) { return x * x; }
 // x^3 for the reference's std::pow(x, 3.) (glibc pow, correctly rounded in
@@ -134,10 +167,10 @@ PDA_HD double weno5_neg(double qim2, double qim1, double qi, double qip1, double
     const double B0 = thirteenOvtwelve * X0 * X0 + oneOvfour * Y0 * Y0;
     const double B1 = thirteenOvtwelve * X1 * X1 + oneOvfour * Y1 * Y1;
     const double B2 = thirteenOvtwelve * X2 * X2 + oneOvfour * Y2 * Y2;
-    const double alpha0 = oneOvten / (epsilon * epsilon + 2. * epsilon * B0 + B0 * B0);
-    const double alpha1 = sixOvten / (epsilon * epsilon + 2. * epsilon * B1 + B1 * B1);
-    const double alpha2 = threeOvten / (epsilon * epsilon + 2. * epsilon * B2 + B2 * B2);
-    const double alphaSInv = 1. / (alpha0 + alpha1 + alpha2);
+    const double alpha0 = div_rn(oneOvten, (epsilon * epsilon + 2. * epsilon * B0 + B0 * B0));
+    const double alpha1 = div_rn(sixOvten, (epsilon * epsilon + 2. * epsilon * B1 + B1 * B1));
+    const double alpha2 = div_rn(threeOvten, (epsilon * epsilon + 2. * epsilon * B2 + B2 * B2));
+    const double alphaSInv = div_rn(1., (alpha0 + alpha1 + alpha2));
     const double w0 = alpha0 * alphaSInv;
     const double w1 = alpha1 * alphaSInv;
     const double w2 = alpha2 * alphaSInv;
@@ -165,10 +198,10 @@ PDA_HD double weno5_pos(double qim1, double qi, double qip1, double qip2, double
     const double B0 = thirteenOvtwelve * X0 * X0 + oneOvfour * Y0 * Y0;
     const double B1 = thirteenOvtwelve * X1 * X1 + oneOvfour * Y1 * Y1;
     const double B2 = thirteenOvtwelve * X2 * X2 + oneOvfour * Y2 * Y2;
-    const double alpha0 = threeOvten / (epsilon * epsilon + 2. * epsilon * B0 + B0 * B0);
-    const double alpha1 = sixOvten / (epsilon * epsilon + 2. * epsilon * B1 + B1 * B1);
-    const double alpha2 = oneOvten / (epsilon * epsilon + 2. * epsilon * B2 + B2 * B2);
-    const double alphaSInv = 1. / (alpha0 + alpha1 + alpha2);
+    const double alpha0 = div_rn(threeOvten, (epsilon * epsilon + 2. * epsilon * B0 + B0 * B0));
+    const double alpha1 = div_rn(sixOvten, (epsilon * epsilon + 2. * epsilon * B1 + B1 * B1));
+    const double alpha2 = div_rn(oneOvten, (epsilon * epsilon + 2. * epsilon * B2 + B2 * B2));
+    const double alphaSInv = div_rn(1., (alpha0 + alpha1 + alpha2));
     const double w0 = alpha0 * alphaSInv;
     const double w1 = alpha1 * alphaSInv;
     const double w2 = alpha2 * alphaSInv;
@@ -227,14 +260,14 @@ PDA_HD void weno5_neg_grad(T &uNeg, T gNeg[6], T qim2, T qim1, T qi, T qip1, T q
     dB2[2] = fma_p2(T(0.5), T(3.) * Y2, div_const(X2, T(6.), T(1.) / T(6.)));
     dB2[3] = fma_p2(-T(2.), Y2, div_const(-X2, T(3.), T(1.) / T(3.)));
     dB2[4] = fma_p2(T(0.5), Y2, div_const(X2, T(6.), T(1.) / T(6.)));
-    const T alpha0 = oneOvten / sq(epsilon + B0);
-    const T alpha1 = sixOvten / sq(epsilon + B1);
-    const T alpha2 = threeOvten / sq(epsilon + B2);
-    const T alphaSInv = T(1.) / (alpha0 + alpha1 + alpha2);
-    const T c0 = -T(1.) / (T(5.) * cube(B0 + epsilon));
-    const T c1 = -T(6.) / (T(5.) * cube(B1 + epsilon));
-    const T c2 = -T(3.) / (T(5.) * cube(B2 + epsilon));
-    const T cS = -T(1.) / sq(alpha2 + alpha1 + alpha0);
+    const T alpha0 = div_rn(oneOvten, sq(epsilon + B0));
+    const T alpha1 = div_rn(sixOvten, sq(epsilon + B1));
+    const T alpha2 = div_rn(threeOvten, sq(epsilon + B2));
+    const T alphaSInv = div_rn(T(1.), (alpha0 + alpha1 + alpha2));
+    const T c0 = div_rn(-T(1.), (T(5.) * cube(B0 + epsilon)));
+    const T c1 = div_rn(-T(6.), (T(5.) * cube(B1 + epsilon)));
+    const T c2 = div_rn(-T(3.), (T(5.) * cube(B2 + epsilon)));
+    const T cS = div_rn(-T(1.), sq(alpha2 + alpha1 + alpha0));
     const T w0 = alpha0 * alphaSInv;
     const T w1 = alpha1 * alphaSInv;
     const T w2 = alpha2 * alphaSInv;
@@ -295,14 +328,14 @@ PDA_HD void weno5_pos_grad(T &uPos, T gPos[6], T qim2, T qim1, T qi, T qip1, T q
     dB2[2] = fma_p2(T(0.5), T(3.) * Y2, div_const(X2, T(6.), T(1.) / T(6.)));
     dB2[3] = fma_p2(-T(2.), Y2, div_const(-X2, T(3.), T(1.) / T(3.)));
     dB2[4] = fma_p2(T(0.5), Y2, div_const(X2, T(6.), T(1.) / T(6.)));
-    const T alpha0 = threeOvten / sq(epsilon + B0);
-    const T alpha1 = sixOvten / sq(epsilon + B1);
-    const T alpha2 = oneOvten / sq(epsilon + B2);
-    const T alphaSInv = T(1.) / (alpha0 + alpha1 + alpha2);
-    const T c0 = -T(3.) / (T(5.) * cube(B0 + epsilon));
-    const T c1 = -T(6.) / (T(5.) * cube(B1 + epsilon));
-    const T c2 = -T(1.) / (T(5.) * cube(B2 + epsilon));
-    const T cS = -T(1.) / sq(alpha2 + alpha1 + alpha0);
+    const T alpha0 = div_rn(threeOvten, sq(epsilon + B0));
+    const T alpha1 = div_rn(sixOvten, sq(epsilon + B1));
+    const T alpha2 = div_rn(oneOvten, sq(epsilon + B2));
+    const T alphaSInv = div_rn(T(1.), (alpha0 + alpha1 + alpha2));
+    const T c0 = div_rn(-T(3.), (T(5.) * cube(B0 + epsilon)));
+    const T c1 = div_rn(-T(6.), (T(5.) * cube(B1 + epsilon)));
+    const T c2 = div_rn(-T(1.), (T(5.) * cube(B2 + epsilon)));
+    const T cS = div_rn(-T(1.), sq(alpha2 + alpha1 + alpha0));
     const T w0 = alpha0 * alphaSInv;
     const T w1 = alpha1 * alphaSInv;
     const T w2 = alpha2 * alphaSInv;
@@ -342,9 +375,9 @@ PDA_HD double weno3_neg(double qim1, double qi, double qip1) {
     const double p1 = (qi + qip1) * oneOvtwo;
     const double B0 = (qim1 - qi) * (qim1 - qi);
     const double B1 = (qi - qip1) * (qi - qip1);
-    const double alpha0 = oneOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
-    const double alpha1 = twoOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
-    const double alphaSInv = 1. / (alpha0 + alpha1);
+    const double alpha0 = div_rn(oneOvthree, (epsilon * epsilon + two * epsilon * B0 + B0 * B0));
+    const double alpha1 = div_rn(twoOvthree, (epsilon * epsilon + two * epsilon * B1 + B1 * B1));
+    const double alphaSInv = div_rn(1., (alpha0 + alpha1));
     const double w0 = alpha0 * alphaSInv;
     const double w1 = alpha1 * alphaSInv;
     uNeg = w0 * p0 + w1 * p1;
@@ -363,9 +396,9 @@ PDA_HD double weno3_pos(double qi, double qip1, double qip2) {
     const double p1 = (three * qip1 - qip2) * oneOvtwo;
     const double B0 = (qi - qip1) * (qi - qip1);
     const double B1 = (qip1 - qip2) * (qip1 - qip2);
-    const double alpha0 = twoOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
-    const double alpha1 = oneOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
-    const double alphaSInv = 1. / (alpha0 + alpha1);
+    const double alpha0 = div_rn(twoOvthree, (epsilon * epsilon + two * epsilon * B0 + B0 * B0));
+    const double alpha1 = div_rn(oneOvthree, (epsilon * epsilon + two * epsilon * B1 + B1 * B1));
+    const double alphaSInv = div_rn(1., (alpha0 + alpha1));
     const double w0 = alpha0 * alphaSInv;
     const double w1 = alpha1 * alphaSInv;
     uPos = w0 * p0 + w1 * p1;
@@ -393,22 +426,22 @@ PDA_HD void weno3_neg_grad(T &uNeg, T gNeg[4], T qim1, T qi, T qip1, T qip2) {
     const T dp1[3] = {T(0.), T(1.) / T(2.), T(1.) / T(2.)};
     const T B0 = (qim1 - qi) * (qim1 - qi);
     const T B1 = (qi - qip1) * (qi - qip1);
-    const T alpha0 = oneOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
-    const T alpha1 = twoOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
-    const T alphaSInv = T(1.) / (alpha0 + alpha1);
+    const T alpha0 = div_rn(oneOvthree, (epsilon * epsilon + two * epsilon * B0 + B0 * B0));
+    const T alpha1 = div_rn(twoOvthree, (epsilon * epsilon + two * epsilon * B1 + B1 * B1));
+    const T alphaSInv = div_rn(T(1.), (alpha0 + alpha1));
     const T e0 = sq(qim1 - qi) + epsilon;  // pow(pow(qim1-qi,2.)+eps, .)
     const T e1 = sq(qi - qip1) + epsilon;
-    const T A = T(2.) / (T(3.) * sq(e1)) + T(1.) / (T(3.) * sq(e0));
+    const T A = div_rn(T(2.), (T(3.) * sq(e1))) + div_rn(T(1.), (T(3.) * sq(e0)));
     T da0[3], da1[3], daS[3];
-    da0[0] = -T(4.) * (qim1 - qi) / (T(3.) * cube(e0));
-    da0[1] = T(4.) * (qim1 - qi) / (T(3.) * cube(e0));
+    da0[0] = div_rn(-T(4.) * (qim1 - qi), (T(3.) * cube(e0)));
+    da0[1] = div_rn(T(4.) * (qim1 - qi), (T(3.) * cube(e0)));
     da0[2] = T(0.);
     da1[0] = T(0.);
-    da1[1] = -T(8.) * (qi - qip1) / (T(3.) * cube(e1));
-    da1[2] = T(8.) * (qi - qip1) / (T(3.) * cube(e1));
-    daS[0] = (T(4.) * (qim1 - qi)) / (T(3.) * cube(e0) * sq(A));
-    daS[1] = -((T(4.) * (qim1 - qi)) / (T(3.) * cube(e0)) - (T(8.) * (qi - qip1)) / (T(3.) * cube(e1))) / sq(A);
-    daS[2] = -(T(8.) * (qi - qip1)) / (T(3.) * sq(A) * cube(e1));
+    da1[1] = div_rn(-T(8.) * (qi - qip1), (T(3.) * cube(e1)));
+    da1[2] = div_rn(T(8.) * (qi - qip1), (T(3.) * cube(e1)));
+    daS[0] = div_rn((T(4.) * (qim1 - qi)), (T(3.) * cube(e0) * sq(A)));
+    daS[1] = div_rn(-(div_rn((T(4.) * (qim1 - qi)), (T(3.) * cube(e0))) - div_rn((T(8.) * (qi - qip1)), (T(3.) * cube(e1)))), sq(A));
+    daS[2] = div_rn(-(T(8.) * (qi - qip1)), (T(3.) * sq(A) * cube(e1)));
     const T w0 = alpha0 * alphaSInv;
     const T w1 = alpha1 * alphaSInv;
     for (int i = 0; i < 3; i++) {
@@ -432,26 +465,26 @@ PDA_HD void weno3_pos_grad(T &uPos, T gPos[4], T qim1, T qi, T qip1, T qip2) {
     const T p1 = (three * qip1 - qip2) * oneOvtwo;
     const T B0 = (qi - qip1) * (qi - qip1);
     const T B1 = (qip1 - qip2) * (qip1 - qip2);
-    const T alpha0 = twoOvthree / (epsilon * epsilon + two * epsilon * B0 + B0 * B0);
-    const T alpha1 = oneOvthree / (epsilon * epsilon + two * epsilon * B1 + B1 * B1);
-    const T alphaSInv = T(1.) / (alpha0 + alpha1);
+    const T alpha0 = div_rn(twoOvthree, (epsilon * epsilon + two * epsilon * B0 + B0 * B0));
+    const T alpha1 = div_rn(oneOvthree, (epsilon * epsilon + two * epsilon * B1 + B1 * B1));
+    const T alphaSInv = div_rn(T(1.), (alpha0 + alpha1));
     const T w0 = alpha0 * alphaSInv;
     const T w1 = alpha1 * alphaSInv;
     const T dp0[3] = {T(1.) / T(2.), 1 / T(2.), T(0.)};
     const T dp1[3] = {T(0.), T(3.) / T(2.), -T(1.) / T(2.)};
     const T e0 = sq(qi - qip1) + epsilon;
     const T e1 = sq(qip1 - qip2) + epsilon;
-    const T A = T(1.) / (T(3.) * sq(e1)) + T(2.) / (T(3.) * sq(e0));
+    const T A = div_rn(T(1.), (T(3.) * sq(e1))) + div_rn(T(2.), (T(3.) * sq(e0)));
     T da0[3], da1[3], daS[3];
-    da0[0] = -T(8.) * (qi - qip1) / (T(3.) * cube(e0));
-    da0[1] = T(8.) * (qi - qip1) / (T(3.) * cube(e0));
+    da0[0] = div_rn(-T(8.) * (qi - qip1), (T(3.) * cube(e0)));
+    da0[1] = div_rn(T(8.) * (qi - qip1), (T(3.) * cube(e0)));
     da0[2] = T(0.);
     da1[0] = T(0.);
-    da1[1] = -T(4.) * (qip1 - qip2) / (T(3.) * cube(e1));
-    da1[2] = T(4.) * (qip1 - qip2) / (T(3.) * cube(e1));
-    daS[0] = T(8.) * (qi - qip1) / (T(3.) * cube(e0) * sq(A));
-    daS[1] = -(T(8.) * (qi - qip1) / (3 * cube(e0)) - T(4.) * (qip1 - qip2) / (T(3.) * cube(e1))) / sq(A);
-    daS[2] = -T(4.) * (qip1 - qip2) / (T(3.) * sq(A) * cube(e1));
+    da1[1] = div_rn(-T(4.) * (qip1 - qip2), (T(3.) * cube(e1)));
+    da1[2] = div_rn(T(4.) * (qip1 - qip2), (T(3.) * cube(e1)));
+    daS[0] = div_rn(T(8.) * (qi - qip1), (T(3.) * cube(e0) * sq(A)));
+    daS[1] = div_rn(-(div_rn(T(8.) * (qi - qip1), (3 * cube(e0))) - div_rn(T(4.) * (qip1 - qip2), (T(3.) * cube(e1)))), sq(A));
+    daS[2] = div_rn(-T(4.) * (qip1 - qip2), (T(3.) * sq(A) * cube(e1)));
     for (int i = 0; i < 3; i++) {
       T g = (da0[i] * alphaSInv + daS[i] * alpha0) * p0 + dp0[i] * w0;
       g += (da1[i] * alphaSInv + daS[i] * alpha1) * p1 + dp1[i] * w1;
@@ -474,79 +507,80 @@ PDA_HD void weno3_face_grad(double &uNeg, double &uPos, double gNeg[4],
 // the face normal (axis-aligned unit vectors); products with 0 and 1 are
 // elided, which changes no value other than the sign of an exact zero.
 // ---------------------------------------------------------------------------
+template <bool INL = false>
 PDA_HD void euler3_flux(double F[3], const double qL[3], const double qR[3],
                         double gamma) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double rL = qL[0];
-  const double uL = qL[1] / (rL + es);
+  const double uL = div_rn<INL>(qL[1], (rL + es));
   const double pL = (gamma - 1) * (qL[2] - half * rL * (uL * uL));
-  const double HL = (qL[2] + pL) / rL;
+  const double HL = div_rn<INL>((qL[2] + pL), rL);
   const double FL0 = rL * uL, FL1 = rL * uL * uL + pL, FL2 = rL * uL * HL;
   const double rR = qR[0];
-  const double uR = qR[1] / (rR + es);
+  const double uR = div_rn<INL>(qR[1], (rR + es));
   const double pR = (gamma - 1) * (qR[2] - half * rR * (uR * uR));
-  const double HR = (qR[2] + pR) / rR;
+  const double HR = div_rn<INL>((qR[2] + pR), rR);
   const double FR0 = rR * uR, FR1 = rR * uR * uR + pR, FR2 = rR * uR * HR;
-  const double RT = sqrt(rR / (rL));
-  const double u = (uL + RT * uR) / (1. + RT);
-  const double H = (HL + RT * HR) / (1. + RT);
-  const double a = sqrt((gamma - 1.) * (H - half * (u * u)));
+  const double RT = sqrt_rn<INL>(div_rn<INL>(rR, (rL)));
+  const double u = div_rn<INL>((uL + RT * uR), (1. + RT));
+  const double H = div_rn<INL>((HL + RT * HR), (1. + RT));
+  const double a = sqrt_rn<INL>((gamma - 1.) * (H - half * (u * u)));
   const double smax = fabs(u) + a;
   F[0] = half * (FL0 + FR0 + smax * (qL[0] - qR[0]));
   F[1] = half * (FL1 + FR1 + smax * (qL[1] - qR[1]));
   F[2] = half * (FL2 + FR2 + smax * (qL[2] - qR[2]));
 }
 
-template <int AXIS>
+template <int AXIS, bool INL = false>
 PDA_HD void euler4_flux(double F[4], const double qL[4], const double qR[4],
                         double gamma) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double rL = qL[0];
-  const double uL = qL[1] / (rL + es);
-  const double vL = qL[2] / (rL + es);
+  const double uL = div_rn<INL>(qL[1], (rL + es));
+  const double vL = div_rn<INL>(qL[2], (rL + es));
   const double unL = AXIS == 0 ? uL : vL;
   const double pL = (gamma - 1) * (qL[3] - half * rL * (uL * uL + vL * vL));
-  const double HL = (qL[3] + pL) / rL;
+  const double HL = div_rn<INL>((qL[3] + pL), rL);
   double FL[4];
   FL[0] = rL * unL;
   FL[1] = AXIS == 0 ? rL * unL * uL + pL : rL * unL * uL;
   FL[2] = AXIS == 1 ? rL * unL * vL + pL : rL * unL * vL;
   FL[3] = rL * unL * HL;
   const double rR = qR[0];
-  const double uR = qR[1] / (rR + es);
-  const double vR = qR[2] / (rR + es);
+  const double uR = div_rn<INL>(qR[1], (rR + es));
+  const double vR = div_rn<INL>(qR[2], (rR + es));
   const double unR = AXIS == 0 ? uR : vR;
   const double pR = (gamma - 1) * (qR[3] - half * rR * (uR * uR + vR * vR));
-  const double HR = (qR[3] + pR) / rR;
+  const double HR = div_rn<INL>((qR[3] + pR), rR);
   double FR[4];
   FR[0] = rR * unR;
   FR[1] = AXIS == 0 ? rR * unR * uR + pR : rR * unR * uR;
   FR[2] = AXIS == 1 ? rR * unR * vR + pR : rR * unR * vR;
   FR[3] = rR * unR * HR;
-  const double RT = sqrt(rR / (rL));
-  const double u = (uL + RT * uR) / (1. + RT);
-  const double v = (vL + RT * vR) / (1. + RT);
-  const double H = (HL + RT * HR) / (1. + RT);
-  const double a = sqrt((gamma - 1.) * (H - half * (u * u + v * v)));
-  const double smax = sqrt(u * u + v * v) + a;
+  const double RT = sqrt_rn<INL>(div_rn<INL>(rR, (rL)));
+  const double u = div_rn<INL>((uL + RT * uR), (1. + RT));
+  const double v = div_rn<INL>((vL + RT * vR), (1. + RT));
+  const double H = div_rn<INL>((HL + RT * HR), (1. + RT));
+  const double a = sqrt_rn<INL>((gamma - 1.) * (H - half * (u * u + v * v)));
+  const double smax = sqrt_rn<INL>(u * u + v * v) + a;
 #pragma unroll
   for (int d = 0; d < 4; ++d) F[d] = half * (FL[d] + FR[d] + smax * (qL[d] - qR[d]));
 }
 
-template <int AXIS>
+template <int AXIS, bool INL = false>
 PDA_HD void euler5_flux(double F[5], const double qL[5], const double qR[5],
                         double gamma) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double rL = qL[0];
-  const double uL = qL[1] / (rL + es);
-  const double vL = qL[2] / (rL + es);
-  const double wL = qL[3] / (rL + es);
+  const double uL = div_rn<INL>(qL[1], (rL + es));
+  const double vL = div_rn<INL>(qL[2], (rL + es));
+  const double wL = div_rn<INL>(qL[3], (rL + es));
   const double unL = AXIS == 0 ? uL : (AXIS == 1 ? vL : wL);
   const double pL = (gamma - 1) * (qL[4] - half * rL * (uL * uL + vL * vL + wL * wL));
-  const double HL = (qL[4] + pL) / rL;
+  const double HL = div_rn<INL>((qL[4] + pL), rL);
   double FL[5];
   FL[0] = rL * unL;
   FL[1] = AXIS == 0 ? rL * unL * uL + pL : rL * unL * uL;
@@ -554,25 +588,25 @@ PDA_HD void euler5_flux(double F[5], const double qL[5], const double qR[5],
   FL[3] = AXIS == 2 ? rL * unL * wL + pL : rL * unL * wL;
   FL[4] = rL * unL * HL;
   const double rR = qR[0];
-  const double uR = qR[1] / (rR + es);
-  const double vR = qR[2] / (rR + es);
-  const double wR = qR[3] / (rR + es);
+  const double uR = div_rn<INL>(qR[1], (rR + es));
+  const double vR = div_rn<INL>(qR[2], (rR + es));
+  const double wR = div_rn<INL>(qR[3], (rR + es));
   const double unR = AXIS == 0 ? uR : (AXIS == 1 ? vR : wR);
   const double pR = (gamma - 1) * (qR[4] - half * rR * (uR * uR + vR * vR + wR * wR));
-  const double HR = (qR[4] + pR) / rR;
+  const double HR = div_rn<INL>((qR[4] + pR), rR);
   double FR[5];
   FR[0] = rR * unR;
   FR[1] = AXIS == 0 ? rR * unR * uR + pR : rR * unR * uR;
   FR[2] = AXIS == 1 ? rR * unR * vR + pR : rR * unR * vR;
   FR[3] = AXIS == 2 ? rR * unR * wR + pR : rR * unR * wR;
   FR[4] = rR * unR * HR;
-  const double RT = sqrt(rR / (rL));
-  const double u = (uL + RT * uR) / (1. + RT);
-  const double v = (vL + RT * vR) / (1. + RT);
-  const double w = (wL + RT * wR) / (1. + RT);
-  const double H = (HL + RT * HR) / (1. + RT);
-  const double a = sqrt((gamma - 1.) * (H - half * (u * u + v * v + w * w)));
-  const double smax = sqrt(u * u + v * v + w * w) + a;
+  const double RT = sqrt_rn<INL>(div_rn<INL>(rR, (rL)));
+  const double u = div_rn<INL>((uL + RT * uR), (1. + RT));
+  const double v = div_rn<INL>((vL + RT * vR), (1. + RT));
+  const double w = div_rn<INL>((wL + RT * wR), (1. + RT));
+  const double H = div_rn<INL>((HL + RT * HR), (1. + RT));
+  const double a = sqrt_rn<INL>((gamma - 1.) * (H - half * (u * u + v * v + w * w)));
+  const double smax = sqrt_rn<INL>(u * u + v * v + w * w) + a;
 #pragma unroll
   for (int d = 0; d < 5; ++d) F[d] = half * (FL[d] + FR[d] + smax * (qL[d] - qR[d]));
 }
@@ -580,14 +614,14 @@ PDA_HD void euler5_flux(double F[5], const double qL[5], const double qR[5],
 // Shallow-water Rusanov flux.  deviation: the reference's std::pow(h, 0.5) is
 // evaluated as sqrt(h) (correctly rounded; glibc pow agrees except in rare
 // near-midpoint cases, a 1-ulp difference).
-template <int AXIS>
+template <int AXIS, bool INL = false>
 PDA_HD void swe_flux(double F[3], const double qL[3], const double qR[3],
                      double gravity) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double hL = qL[0];
-  const double uL = qL[1] / (hL + es);
-  const double vL = qL[2] / (hL + es);
+  const double uL = div_rn<INL>(qL[1], (hL + es));
+  const double vL = div_rn<INL>(qL[2], (hL + es));
   const double unL = AXIS == 0 ? uL : vL;
   const double pL = 0.5 * gravity * hL * hL;
   double FL[3];
@@ -595,8 +629,8 @@ PDA_HD void swe_flux(double F[3], const double qL[3], const double qR[3],
   FL[1] = AXIS == 0 ? hL * unL * uL + pL : hL * unL * uL;
   FL[2] = AXIS == 1 ? hL * unL * vL + pL : hL * unL * vL;
   const double hR = qR[0];
-  const double uR = qR[1] / (hR + es);
-  const double vR = qR[2] / (hR + es);
+  const double uR = div_rn<INL>(qR[1], (hR + es));
+  const double vR = div_rn<INL>(qR[2], (hR + es));
   const double unR = AXIS == 0 ? uR : vR;
   const double pR = 0.5 * gravity * hR * hR;
   double FR[3];
@@ -604,10 +638,10 @@ PDA_HD void swe_flux(double F[3], const double qL[3], const double qR[3],
   FR[1] = AXIS == 0 ? hR * unR * uR + pR : hR * unR * uR;
   FR[2] = AXIS == 1 ? hR * unR * vR + pR : hR * unR * vR;
   const double hm = 0.5 * (hL + hR);
-  const double sL = sqrt(hL), sR = sqrt(hR);
-  const double um = (unL * sL + unR * sR) / (sL + sR + es);
-  const double sg = sqrt(gravity * hm);
-  const double smax = sqrt(um * um) + sqrt(sg * sg);
+  const double sL = sqrt_rn<INL>(hL), sR = sqrt_rn<INL>(hR);
+  const double um = div_rn<INL>((unL * sL + unR * sR), (sL + sR + es));
+  const double sg = sqrt_rn<INL>(gravity * hm);
+  const double smax = sqrt_rn<INL>(um * um) + sqrt_rn<INL>(sg * sg);
 #pragma unroll
   for (int d = 0; d < 3; ++d) F[d] = half * (FL[d] + FR[d] + smax * (qL[d] - qR[d]));
 }
@@ -629,9 +663,9 @@ PDA_HD void euler3_side(FluxSide<3> &o, const double q[3], double gamma) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double r = q[0];
-  const double u = q[1] / (r + es);
+  const double u = div_rn(q[1], (r + es));
   const double p = (gamma - 1) * (q[2] - half * r * (u * u));
-  const double H = (q[2] + p) / r;
+  const double H = div_rn((q[2] + p), r);
   o.F[0] = r * u;
   o.F[1] = r * u * u + p;
   o.F[2] = r * u * H;
@@ -641,10 +675,10 @@ PDA_HD void euler3_side(FluxSide<3> &o, const double q[3], double gamma) {
 PDA_HD void euler3_combine(double F[3], const double qL[3], const double qR[3], const FluxSide<3> &L,
                            const FluxSide<3> &R, double gamma) {
   constexpr double half = 1. / 2.;
-  const double RT = sqrt(qR[0] / (qL[0]));
-  const double u = (L.u + RT * R.u) / (1. + RT);
-  const double H = (L.H + RT * R.H) / (1. + RT);
-  const double a = sqrt((gamma - 1.) * (H - half * (u * u)));
+  const double RT = sqrt_rn(div_rn(qR[0], (qL[0])));
+  const double u = div_rn((L.u + RT * R.u), (1. + RT));
+  const double H = div_rn((L.H + RT * R.H), (1. + RT));
+  const double a = sqrt_rn((gamma - 1.) * (H - half * (u * u)));
   const double smax = fabs(u) + a;
 #pragma unroll
   for (int d = 0; d < 3; ++d) F[d] = half * (L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
@@ -655,11 +689,11 @@ PDA_HD void euler4_side(FluxSide<4> &o, const double q[4], double gamma) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double r = q[0];
-  const double u = q[1] / (r + es);
-  const double v = q[2] / (r + es);
+  const double u = div_rn(q[1], (r + es));
+  const double v = div_rn(q[2], (r + es));
   const double un = AXIS == 0 ? u : v;
   const double p = (gamma - 1) * (q[3] - half * r * (u * u + v * v));
-  const double H = (q[3] + p) / r;
+  const double H = div_rn((q[3] + p), r);
   o.F[0] = r * un;
   o.F[1] = AXIS == 0 ? r * un * u + p : r * un * u;
   o.F[2] = AXIS == 1 ? r * un * v + p : r * un * v;
@@ -672,12 +706,12 @@ template <int AXIS>
 PDA_HD void euler4_combine(double F[4], const double qL[4], const double qR[4], const FluxSide<4> &L,
                            const FluxSide<4> &R, double gamma) {
   constexpr double half = 1. / 2.;
-  const double RT = sqrt(qR[0] / (qL[0]));
-  const double u = (L.u + RT * R.u) / (1. + RT);
-  const double v = (L.v + RT * R.v) / (1. + RT);
-  const double H = (L.H + RT * R.H) / (1. + RT);
-  const double a = sqrt((gamma - 1.) * (H - half * (u * u + v * v)));
-  const double smax = sqrt(u * u + v * v) + a;
+  const double RT = sqrt_rn(div_rn(qR[0], (qL[0])));
+  const double u = div_rn((L.u + RT * R.u), (1. + RT));
+  const double v = div_rn((L.v + RT * R.v), (1. + RT));
+  const double H = div_rn((L.H + RT * R.H), (1. + RT));
+  const double a = sqrt_rn((gamma - 1.) * (H - half * (u * u + v * v)));
+  const double smax = sqrt_rn(u * u + v * v) + a;
 #pragma unroll
   for (int d = 0; d < 4; ++d) F[d] = half * (L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
 }
@@ -687,12 +721,12 @@ PDA_HD void euler5_side(FluxSide<5> &o, const double q[5], double gamma) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double r = q[0];
-  const double u = q[1] / (r + es);
-  const double v = q[2] / (r + es);
-  const double w = q[3] / (r + es);
+  const double u = div_rn(q[1], (r + es));
+  const double v = div_rn(q[2], (r + es));
+  const double w = div_rn(q[3], (r + es));
   const double un = AXIS == 0 ? u : (AXIS == 1 ? v : w);
   const double p = (gamma - 1) * (q[4] - half * r * (u * u + v * v + w * w));
-  const double H = (q[4] + p) / r;
+  const double H = div_rn((q[4] + p), r);
   o.F[0] = r * un;
   o.F[1] = AXIS == 0 ? r * un * u + p : r * un * u;
   o.F[2] = AXIS == 1 ? r * un * v + p : r * un * v;
@@ -707,13 +741,13 @@ template <int AXIS>
 PDA_HD void euler5_combine(double F[5], const double qL[5], const double qR[5], const FluxSide<5> &L,
                            const FluxSide<5> &R, double gamma) {
   constexpr double half = 1. / 2.;
-  const double RT = sqrt(qR[0] / (qL[0]));
-  const double u = (L.u + RT * R.u) / (1. + RT);
-  const double v = (L.v + RT * R.v) / (1. + RT);
-  const double w = (L.w + RT * R.w) / (1. + RT);
-  const double H = (L.H + RT * R.H) / (1. + RT);
-  const double a = sqrt((gamma - 1.) * (H - half * (u * u + v * v + w * w)));
-  const double smax = sqrt(u * u + v * v + w * w) + a;
+  const double RT = sqrt_rn(div_rn(qR[0], (qL[0])));
+  const double u = div_rn((L.u + RT * R.u), (1. + RT));
+  const double v = div_rn((L.v + RT * R.v), (1. + RT));
+  const double w = div_rn((L.w + RT * R.w), (1. + RT));
+  const double H = div_rn((L.H + RT * R.H), (1. + RT));
+  const double a = sqrt_rn((gamma - 1.) * (H - half * (u * u + v * v + w * w)));
+  const double smax = sqrt_rn(u * u + v * v + w * w) + a;
 #pragma unroll
   for (int d = 0; d < 5; ++d) F[d] = half * (L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
 }
@@ -722,15 +756,15 @@ template <int AXIS>
 PDA_HD void swe_side(FluxSide<3> &o, const double q[3], double gravity) {
   constexpr double es = 1.e-30;
   const double h = q[0];
-  const double u = q[1] / (h + es);
-  const double v = q[2] / (h + es);
+  const double u = div_rn(q[1], (h + es));
+  const double v = div_rn(q[2], (h + es));
   const double un = AXIS == 0 ? u : v;
   const double p = 0.5 * gravity * h * h;
   o.F[0] = h * un;
   o.F[1] = AXIS == 0 ? h * un * u + p : h * un * u;
   o.F[2] = AXIS == 1 ? h * un * v + p : h * un * v;
   o.u = un;
-  o.H = sqrt(h);
+  o.H = sqrt_rn(h);
 }
 template <int AXIS>
 PDA_HD void swe_combine(double F[3], const double qL[3], const double qR[3], const FluxSide<3> &L,
@@ -738,9 +772,9 @@ PDA_HD void swe_combine(double F[3], const double qL[3], const double qR[3], con
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double hm = 0.5 * (qL[0] + qR[0]);
-  const double um = (L.u * L.H + R.u * R.H) / (L.H + R.H + es);
-  const double sg = sqrt(gravity * hm);
-  const double smax = sqrt(um * um) + sqrt(sg * sg);
+  const double um = div_rn((L.u * L.H + R.u * R.H), (L.H + R.H + es));
+  const double sg = sqrt_rn(gravity * hm);
+  const double smax = sqrt_rn(um * um) + sqrt_rn(sg * sg);
 #pragma unroll
   for (int d = 0; d < 3; ++d) F[d] = half * (L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
 }
@@ -756,34 +790,34 @@ PDA_HD void euler3_flux_jac(T JL[9], T JR[9], const T qL[3],
   constexpr T es = T(1.e-30);
   const T gm1 = gamma - one;
   const T rL = qL[0];
-  const T uL = qL[1] / (rL + es);
+  const T uL = div_rn(qL[1], (rL + es));
   const T pL = gm1 * (qL[2] - half * rL * (uL * uL));
-  const T HL = (qL[2] + pL) / rL;
-  const T aL = sqrt(gm1 * (HL - half * (uL * uL)));
+  const T HL = div_rn((qL[2] + pL), rL);
+  const T aL = sqrt_rn(gm1 * (HL - half * (uL * uL)));
   const T rR = qR[0];
-  const T uR = qR[1] / (rR + es);
+  const T uR = div_rn(qR[1], (rR + es));
   const T pR = gm1 * (qR[2] - half * rR * (uR * uR));
-  const T HR = (qR[2] + pR) / rR;
-  const T aR = sqrt(gm1 * (HR - half * (uR * uR)));
-  const T r = sqrt(rR * rL);
-  const T RT = sqrt(rR / (rL));
-  const T u = (uL + RT * uR) / (one + RT);
-  const T H = (HL + RT * HR) / (one + RT);
-  const T a = sqrt(gm1 * (H - half * (u * u)));
+  const T HR = div_rn((qR[2] + pR), rR);
+  const T aR = sqrt_rn(gm1 * (HR - half * (uR * uR)));
+  const T r = sqrt_rn(rR * rL);
+  const T RT = sqrt_rn(div_rn(rR, (rL)));
+  const T u = div_rn((uL + RT * uR), (one + RT));
+  const T H = div_rn((HL + RT * HR), (one + RT));
+  const T a = sqrt_rn(gm1 * (H - half * (u * u)));
   const T smax = fabs(u) + a;
   const T VMagSqrRoe = u * u + es;
   const T VMagSqrL = uL * uL;
   const T VVRoeL = uL * u;
   const T VMagSqrR = uR * uR;
   const T VVRoeR = uR * u;
-  const T uRelRoe = u / sqrt(VMagSqrRoe);
+  const T uRelRoe = div_rn(u, sqrt_rn(VMagSqrRoe));
   T gL[3], gR[3];
-  gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe + half * gm1 / a * (fma_p2(half, VMagSqrRoe + VVRoeL, half * (HL - H)) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
-  gL[1] = one / (rL + r) * (uRelRoe - half * (gm1 * (u + gm1 * uL)) / (a));
-  gL[2] = half / (rL + r) * gamma * gm1 / (a);
-  gR[0] = one / (rR + r) * (-half * (uR + u) * uRelRoe + half * gm1 / a * (fma_p2(half, VMagSqrRoe + VVRoeR, half * (HR - H)) - aR * aR / gm1 + half * (gamma - two) * VMagSqrR));
-  gR[1] = one / (rR + r) * (uRelRoe - half * (gm1 * (u + gm1 * uR)) / (a));
-  gR[2] = half / (rR + r) * gamma * gm1 / (a);
+  gL[0] = div_rn(one, (rL + r)) * (-half * (uL + u) * uRelRoe + div_rn(half * gm1, a) * (fma_p2(half, VMagSqrRoe + VVRoeL, half * (HL - H)) - div_rn(aL * aL, gm1) + half * (gamma - two) * VMagSqrL));
+  gL[1] = div_rn(one, (rL + r)) * (uRelRoe - div_rn(half * (gm1 * (u + gm1 * uL)), (a)));
+  gL[2] = div_rn(div_rn(half, (rL + r)) * gamma * gm1, (a));
+  gR[0] = div_rn(one, (rR + r)) * (-half * (uR + u) * uRelRoe + div_rn(half * gm1, a) * (fma_p2(half, VMagSqrRoe + VVRoeR, half * (HR - H)) - div_rn(aR * aR, gm1) + half * (gamma - two) * VMagSqrR));
+  gR[1] = div_rn(one, (rR + r)) * (uRelRoe - div_rn(half * (gm1 * (u + gm1 * uR)), (a)));
+  gR[2] = div_rn(div_rn(half, (rR + r)) * gamma * gm1, (a));
   JL[0] = 0;
   JL[1] = half;
   JL[2] = 0;
@@ -820,42 +854,42 @@ PDA_HD void euler4_flux_jac(T JL[16], T JR[16], const T qL[4],
   const T n[2] = {AXIS == 0 ? T(1.) : T(0.), AXIS == 1 ? T(1.) : T(0.)};
   const T gm1 = gamma - one;
   const T rL = qL[0];
-  const T uL = qL[1] / (rL + es);
-  const T vL = qL[2] / (rL + es);
+  const T uL = div_rn(qL[1], (rL + es));
+  const T vL = div_rn(qL[2], (rL + es));
   const T unL = uL * n[0] + vL * n[1];
   const T pL = gm1 * (qL[3] - half * rL * (uL * uL + vL * vL));
-  const T HL = (qL[3] + pL) / rL;
-  const T aL = sqrt(gm1 * (HL - half * (uL * uL + vL * vL)));
+  const T HL = div_rn((qL[3] + pL), rL);
+  const T aL = sqrt_rn(gm1 * (HL - half * (uL * uL + vL * vL)));
   const T rR = qR[0];
-  const T uR = qR[1] / (rR + es);
-  const T vR = qR[2] / (rR + es);
+  const T uR = div_rn(qR[1], (rR + es));
+  const T vR = div_rn(qR[2], (rR + es));
   const T unR = uR * n[0] + vR * n[1];
   const T pR = gm1 * (qR[3] - half * rR * (uR * uR + vR * vR));
-  const T HR = (qR[3] + pR) / rR;
-  const T aR = sqrt(gm1 * (HR - half * (uR * uR + vR * vR)));
-  const T r = sqrt(rR * rL);
-  const T RT = sqrt(rR / (rL));
-  const T u = (uL + RT * uR) / (one + RT);
-  const T v = (vL + RT * vR) / (one + RT);
-  const T H = (HL + RT * HR) / (one + RT);
-  const T a = sqrt(gm1 * (H - half * (u * u + v * v)));
-  const T smax = sqrt(u * u + v * v) + a;
+  const T HR = div_rn((qR[3] + pR), rR);
+  const T aR = sqrt_rn(gm1 * (HR - half * (uR * uR + vR * vR)));
+  const T r = sqrt_rn(rR * rL);
+  const T RT = sqrt_rn(div_rn(rR, (rL)));
+  const T u = div_rn((uL + RT * uR), (one + RT));
+  const T v = div_rn((vL + RT * vR), (one + RT));
+  const T H = div_rn((HL + RT * HR), (one + RT));
+  const T a = sqrt_rn(gm1 * (H - half * (u * u + v * v)));
+  const T smax = sqrt_rn(u * u + v * v) + a;
   const T VMagSqrRoe = u * u + v * v + es;
   const T VMagSqrL = uL * uL + vL * vL;
   const T VVRoeL = uL * u + vL * v;
   const T VMagSqrR = uR * uR + vR * vR;
   const T VVRoeR = uR * u + vR * v;
-  const T uRelRoe = u / sqrt(VMagSqrRoe);
-  const T vRelRoe = v / sqrt(VMagSqrRoe);
+  const T uRelRoe = div_rn(u, sqrt_rn(VMagSqrRoe));
+  const T vRelRoe = div_rn(v, sqrt_rn(VMagSqrRoe));
   T gL[4], gR[4];
-  gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe - half * (vL + v) * vRelRoe + half * gm1 / a * (fma_p2(half, VMagSqrRoe + VVRoeL, half * (HL - H)) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
-  gL[1] = one / (rL + r) * (uRelRoe - half * (gm1 * (u + gm1 * uL)) / (a));
-  gL[2] = one / (rL + r) * (vRelRoe - half * (gm1 * (v + gm1 * vL)) / (a));
-  gL[3] = half / (rL + r) * gamma * gm1 / (a);
-  gR[0] = one / (rR + r) * (-half * (uR + u) * uRelRoe - half * (vR + v) * vRelRoe + half * gm1 / a * (fma_p2(half, VMagSqrRoe + VVRoeR, half * (HR - H)) - aR * aR / gm1 + half * (gamma - two) * VMagSqrR));
-  gR[1] = one / (rR + r) * (uRelRoe - half * (gm1 * (u + gm1 * uR)) / (a));
-  gR[2] = one / (rR + r) * (vRelRoe - half * (gm1 * (v + gm1 * vR)) / (a));
-  gR[3] = half / (rR + r) * gamma * gm1 / (a);
+  gL[0] = div_rn(one, (rL + r)) * (-half * (uL + u) * uRelRoe - half * (vL + v) * vRelRoe + div_rn(half * gm1, a) * (fma_p2(half, VMagSqrRoe + VVRoeL, half * (HL - H)) - div_rn(aL * aL, gm1) + half * (gamma - two) * VMagSqrL));
+  gL[1] = div_rn(one, (rL + r)) * (uRelRoe - div_rn(half * (gm1 * (u + gm1 * uL)), (a)));
+  gL[2] = div_rn(one, (rL + r)) * (vRelRoe - div_rn(half * (gm1 * (v + gm1 * vL)), (a)));
+  gL[3] = div_rn(div_rn(half, (rL + r)) * gamma * gm1, (a));
+  gR[0] = div_rn(one, (rR + r)) * (-half * (uR + u) * uRelRoe - half * (vR + v) * vRelRoe + div_rn(half * gm1, a) * (fma_p2(half, VMagSqrRoe + VVRoeR, half * (HR - H)) - div_rn(aR * aR, gm1) + half * (gamma - two) * VMagSqrR));
+  gR[1] = div_rn(one, (rR + r)) * (uRelRoe - div_rn(half * (gm1 * (u + gm1 * uR)), (a)));
+  gR[2] = div_rn(one, (rR + r)) * (vRelRoe - div_rn(half * (gm1 * (v + gm1 * vR)), (a)));
+  gR[3] = div_rn(div_rn(half, (rR + r)) * gamma * gm1, (a));
   // left
   JL[0] = 0;
   JL[1] = half * n[0];
@@ -908,48 +942,48 @@ PDA_HD void euler5_flux_jac(T JL[25], T JR[25], const T qL[5],
   const T n[3] = {AXIS == 0 ? T(1.) : T(0.), AXIS == 1 ? T(1.) : T(0.), AXIS == 2 ? T(1.) : T(0.)};
   const T gm1 = gamma - one;
   const T rL = qL[0];
-  const T uL = qL[1] / (rL + es);
-  const T vL = qL[2] / (rL + es);
-  const T wL = qL[3] / (rL + es);
+  const T uL = div_rn(qL[1], (rL + es));
+  const T vL = div_rn(qL[2], (rL + es));
+  const T wL = div_rn(qL[3], (rL + es));
   const T unL = uL * n[0] + vL * n[1] + wL * n[2];
   const T pL = gm1 * (qL[4] - half * rL * (uL * uL + vL * vL + wL * wL));
-  const T HL = (qL[4] + pL) / rL;
-  const T aL = sqrt(gm1 * (HL - half * (uL * uL + vL * vL + wL * wL)));
+  const T HL = div_rn((qL[4] + pL), rL);
+  const T aL = sqrt_rn(gm1 * (HL - half * (uL * uL + vL * vL + wL * wL)));
   const T rR = qR[0];
-  const T uR = qR[1] / (rR + es);
-  const T vR = qR[2] / (rR + es);
-  const T wR = qR[3] / (rR + es);
+  const T uR = div_rn(qR[1], (rR + es));
+  const T vR = div_rn(qR[2], (rR + es));
+  const T wR = div_rn(qR[3], (rR + es));
   const T unR = uR * n[0] + vR * n[1] + wR * n[2];
   const T pR = gm1 * (qR[4] - half * rR * (uR * uR + vR * vR + wR * wR));
-  const T HR = (qR[4] + pR) / rR;
-  const T aR = sqrt(gm1 * (HR - half * (uR * uR + vR * vR + wR * wR)));
-  const T r = sqrt(rR * rL);
-  const T RT = sqrt(rR / (rL));
-  const T u = (uL + RT * uR) / (one + RT);
-  const T v = (vL + RT * vR) / (one + RT);
-  const T w = (wL + RT * wR) / (one + RT);
-  const T H = (HL + RT * HR) / (one + RT);
-  const T a = sqrt(gm1 * (H - half * (u * u + v * v + w * w)));
-  const T smax = sqrt(u * u + v * v + w * w) + a;
+  const T HR = div_rn((qR[4] + pR), rR);
+  const T aR = sqrt_rn(gm1 * (HR - half * (uR * uR + vR * vR + wR * wR)));
+  const T r = sqrt_rn(rR * rL);
+  const T RT = sqrt_rn(div_rn(rR, (rL)));
+  const T u = div_rn((uL + RT * uR), (one + RT));
+  const T v = div_rn((vL + RT * vR), (one + RT));
+  const T w = div_rn((wL + RT * wR), (one + RT));
+  const T H = div_rn((HL + RT * HR), (one + RT));
+  const T a = sqrt_rn(gm1 * (H - half * (u * u + v * v + w * w)));
+  const T smax = sqrt_rn(u * u + v * v + w * w) + a;
   const T VMagSqrRoe = u * u + v * v + w * w + es;
   const T VMagSqrL = uL * uL + vL * vL + wL * wL;
   const T VVRoeL = uL * u + vL * v + wL * w;
   const T VMagSqrR = uR * uR + vR * vR + wR * wR;
   const T VVRoeR = uR * u + vR * v + wR * w;
-  const T uRelRoe = u / sqrt(VMagSqrRoe);
-  const T vRelRoe = v / sqrt(VMagSqrRoe);
-  const T wRelRoe = w / sqrt(VMagSqrRoe);
+  const T uRelRoe = div_rn(u, sqrt_rn(VMagSqrRoe));
+  const T vRelRoe = div_rn(v, sqrt_rn(VMagSqrRoe));
+  const T wRelRoe = div_rn(w, sqrt_rn(VMagSqrRoe));
   T gL[5], gR[5];
-  gL[0] = one / (rL + r) * (-half * (uL + u) * uRelRoe - half * (vL + v) * vRelRoe - half * (wL + w) * wRelRoe + half * gm1 / a * (fma_p2(half, VMagSqrRoe + VVRoeL, half * (HL - H)) - aL * aL / gm1 + half * (gamma - two) * VMagSqrL));
-  gL[1] = one / (rL + r) * (uRelRoe - half * (gm1 * (u + gm1 * uL)) / (a));
-  gL[2] = one / (rL + r) * (vRelRoe - half * (gm1 * (v + gm1 * vL)) / (a));
-  gL[3] = one / (rL + r) * (wRelRoe - half * (gm1 * (w + gm1 * wL)) / (a));
-  gL[4] = half / (rL + r) * gamma * gm1 / (a);
-  gR[0] = one / (rR + r) * (-half * (uR + u) * uRelRoe - half * (vR + v) * vRelRoe - half * (wR + w) * wRelRoe + half * gm1 / a * (fma_p2(half, VMagSqrRoe + VVRoeR, half * (HR - H)) - aR * aR / gm1 + half * (gamma - two) * VMagSqrR));
-  gR[1] = one / (rR + r) * (uRelRoe - half * (gm1 * (u + gm1 * uR)) / (a));
-  gR[2] = one / (rR + r) * (vRelRoe - half * (gm1 * (v + gm1 * vR)) / (a));
-  gR[3] = one / (rR + r) * (wRelRoe - half * (gm1 * (w + gm1 * wR)) / (a));
-  gR[4] = half / (rR + r) * gamma * gm1 / (a);
+  gL[0] = div_rn(one, (rL + r)) * (-half * (uL + u) * uRelRoe - half * (vL + v) * vRelRoe - half * (wL + w) * wRelRoe + div_rn(half * gm1, a) * (fma_p2(half, VMagSqrRoe + VVRoeL, half * (HL - H)) - div_rn(aL * aL, gm1) + half * (gamma - two) * VMagSqrL));
+  gL[1] = div_rn(one, (rL + r)) * (uRelRoe - div_rn(half * (gm1 * (u + gm1 * uL)), (a)));
+  gL[2] = div_rn(one, (rL + r)) * (vRelRoe - div_rn(half * (gm1 * (v + gm1 * vL)), (a)));
+  gL[3] = div_rn(one, (rL + r)) * (wRelRoe - div_rn(half * (gm1 * (w + gm1 * wL)), (a)));
+  gL[4] = div_rn(div_rn(half, (rL + r)) * gamma * gm1, (a));
+  gR[0] = div_rn(one, (rR + r)) * (-half * (uR + u) * uRelRoe - half * (vR + v) * vRelRoe - half * (wR + w) * wRelRoe + div_rn(half * gm1, a) * (fma_p2(half, VMagSqrRoe + VVRoeR, half * (HR - H)) - div_rn(aR * aR, gm1) + half * (gamma - two) * VMagSqrR));
+  gR[1] = div_rn(one, (rR + r)) * (uRelRoe - div_rn(half * (gm1 * (u + gm1 * uR)), (a)));
+  gR[2] = div_rn(one, (rR + r)) * (vRelRoe - div_rn(half * (gm1 * (v + gm1 * vR)), (a)));
+  gR[3] = div_rn(one, (rR + r)) * (wRelRoe - div_rn(half * (gm1 * (w + gm1 * wR)), (a)));
+  gR[4] = div_rn(div_rn(half, (rR + r)) * gamma * gm1, (a));
   // left and right use the same template; X = L or R
 #define PDA_FILL_J5(J, uX, vX, wX, unX, HX, VMagSqrX)                 \
   J[0] = 0;                                                           \
@@ -998,33 +1032,33 @@ PDA_HD void swe_flux_jac(T JL[9], T JR[9], const T qL[3],
   constexpr T es = T(1.e-30);
   const T n[2] = {AXIS == 0 ? T(1.) : T(0.), AXIS == 1 ? T(1.) : T(0.)};
   const T hL = qL[0];
-  const T uL = qL[1] / (hL + es);
-  const T vL = qL[2] / (hL + es);
+  const T uL = div_rn(qL[1], (hL + es));
+  const T vL = div_rn(qL[2], (hL + es));
   const T unL = uL * n[0] + vL * n[1];
   const T hR = qR[0];
-  const T uR = qR[1] / (hR + es);
-  const T vR = qR[2] / (hR + es);
+  const T uR = div_rn(qR[1], (hR + es));
+  const T vR = div_rn(qR[2], (hR + es));
   const T unR = uR * n[0] + vR * n[1];
   const T hm = T(0.5) * (hL + hR);
-  const T hL_sqrt = sqrt(hL);
-  const T hR_sqrt = sqrt(hR);
-  const T um = (unL * hL_sqrt + unR * hR_sqrt) / (hL_sqrt + hR_sqrt + es);
-  const T smax = fabs(um) + fabs(sqrt(g * hm));
-  const T termL = (n[0] * qL[1] + n[1] * qL[2]) / sq(qL[0]);
-  const T termR = (n[0] * qR[1] + n[1] * qR[2]) / sq(qR[0]);
+  const T hL_sqrt = sqrt_rn(hL);
+  const T hR_sqrt = sqrt_rn(hR);
+  const T um = div_rn((unL * hL_sqrt + unR * hR_sqrt), (hL_sqrt + hR_sqrt + es));
+  const T smax = fabs(um) + fabs(sqrt_rn(g * hm));
+  const T termL = div_rn((n[0] * qL[1] + n[1] * qL[2]), sq(qL[0]));
+  const T termR = div_rn((n[0] * qR[1] + n[1] * qR[2]), sq(qR[0]));
   const T hsqrt_un = hL_sqrt * unL + hR_sqrt * unR + es;
   const T two_pow_1p5 = T(2.) * sqrt(T(2.));
   T dL[3], dR[3];
-  dL[0] = -fabs(hsqrt_un) / (T(2.) * hL_sqrt * sq(hL_sqrt + hR_sqrt)) +
-          (T(0.5) * unL / hL_sqrt - hL_sqrt * termL) * hsqrt_un / ((hL_sqrt + hR_sqrt) * fabs(hsqrt_un)) +
-          g / (two_pow_1p5 * sqrt(g * (hL + hR)));
-  dL[1] = n[0] * hsqrt_un / (hL_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
-  dL[2] = n[1] * hsqrt_un / (hL_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
-  dR[0] = -fabs(hsqrt_un) / (T(2.) * hR_sqrt * sq(hL_sqrt + hR_sqrt)) +
-          (T(0.5) * unR / hR_sqrt - hR_sqrt * termR) * hsqrt_un / ((hL_sqrt + hR_sqrt) * fabs(hsqrt_un)) +
-          g / (two_pow_1p5 * sqrt(g * (hL + hR)));
-  dR[1] = n[0] * hsqrt_un / (hR_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
-  dR[2] = n[1] * hsqrt_un / (hR_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un));
+  dL[0] = div_rn(-fabs(hsqrt_un), (T(2.) * hL_sqrt * sq(hL_sqrt + hR_sqrt))) +
+          div_rn((div_rn(T(0.5) * unL, hL_sqrt) - hL_sqrt * termL) * hsqrt_un, ((hL_sqrt + hR_sqrt) * fabs(hsqrt_un))) +
+          div_rn(g, (two_pow_1p5 * sqrt_rn(g * (hL + hR))));
+  dL[1] = div_rn(n[0] * hsqrt_un, (hL_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un)));
+  dL[2] = div_rn(n[1] * hsqrt_un, (hL_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un)));
+  dR[0] = div_rn(-fabs(hsqrt_un), (T(2.) * hR_sqrt * sq(hL_sqrt + hR_sqrt))) +
+          div_rn((div_rn(T(0.5) * unR, hR_sqrt) - hR_sqrt * termR) * hsqrt_un, ((hL_sqrt + hR_sqrt) * fabs(hsqrt_un))) +
+          div_rn(g, (two_pow_1p5 * sqrt_rn(g * (hL + hR))));
+  dR[1] = div_rn(n[0] * hsqrt_un, (hR_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un)));
+  dR[2] = div_rn(n[1] * hsqrt_un, (hR_sqrt * (hL_sqrt + hR_sqrt) * fabs(hsqrt_un)));
   JL[0] = -T(0.5) * dL[0] * (qR[0] - qL[0]) + T(0.5) * (n[0] * uL + n[1] * vL - qL[0] * termL) + T(0.5) * smax;
   JL[1] = T(0.5) * n[0] - T(0.5) * dL[1] * (qR[0] - qL[0]);
   JL[2] = T(0.5) * n[1] - T(0.5) * dL[2] * (qR[0] - qL[0]);

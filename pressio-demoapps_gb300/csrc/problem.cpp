@@ -1607,4 +1607,14 @@ pda_status pda_measure_fp64_peak(double *flops_per_s) {
   PDA_API_END
 }
 
+pda_status pda_check_divsqrt(int mode, uint64_t seed, int64_t per_thread, int64_t counts[3]) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(counts && mode >= 0 && mode <= 3 && per_thread > 0, PDA_ERR_INVALID_ARGUMENT, "invalid argument");
+  long long c[3] = {0, 0, 0};
+  pda::check_divsqrt(mode, seed, (long)per_thread, c, nullptr);
+  PDA_CUDA(cudaGetLastError());
+  for (int k = 0; k < 3; ++k) counts[k] = (int64_t)c[k];
+  PDA_API_END
+}
+
 }  // extern "C"

@@ -1,4 +1,4 @@
-// Hyper-reduced LSPG (BDF1, Gauss-Newton with FP64 normal equations) on the
+// Hyper-reduced LSPG (BDF1 / BDF2, Gauss-Newton with FP64 normal equations) on the
 // device, over a sample-mesh problem, with an affine trial space
 // (y = u_ref + Phi x) or a nonlinear manifold given by an MLP decoder
 // (y = u_ref + scale * dec(x), dec = W3 elu(W2 elu(W1 x + b1) + b2) + b3
@@ -6,11 +6,11 @@
 //
 // Per time step n -> n+1 and Gauss-Newton iteration (Pressio's
 // LspgUnsteadyResidualJacobianPolicyHypRed, lspg_unsteady_rj_policy_hypred.hpp:
-// 180-264, with the BDF1 constants c_np1 = 1, c_n = -1, c_f = -1 of
-// ode_constants.hpp:61-63):
+// 180-264, with the constants of ode_constants.hpp:57-73: BDF1 c_n = -1,
+// c_f = -1; BDF2 c_n = -4/3, c_n-1 = 1/3, c_f = -2/3, its first step BDF1):
 //   y      = trial state at the current latent x (stencil rows), D = dy/dx
 //   V, Jf  = sample-mesh velocity and Jacobian at y (the library's kernels)
-//   R      = cf V + (y - y_n)|sample                 cf = -dt
+//   R      = cf V + (y + c_n y_n [+ c_n-1 y_n-1])|sample     cf = c_f dt
 //   JR     = cf (Jf D) + D|sample
 //   (JR^T JR) dx = JR^T R,  x <- x - dx               (FP64, Cholesky)
 // Each kernel reads a per-step "converged" flag and returns at once after the
@@ -233,7 +233,7 @@ k_lspg_rows(int ndpc, long ns, const int *__restrict__ s2st, const double *__res
             const double *__restrict__ D, const double *__restrict__ V, const int *__restrict__ rowptr,
             const int *__restrict__ colidx, const double *__restrict__ J, double cf, double *__restrict__ yn,
             int first, double *__restrict__ partial, unsigned *__restrict__ ticket, double *__restrict__ x,
-            double tol, Flags *f) {
+            double tol, Flags *f, double cn, double cnm1, double *__restrict__ ynm1, int bdf2) {
   if (!first && f->converged) return;
   constexpr int RB = rows_per_block(K);
   __shared__ double sJR[RB][K + 1];  // column K holds R
@@ -245,8 +245,11 @@ k_lspg_rows(int ndpc, long ns, const int *__restrict__ s2st, const double *__res
     const long st = (long)s2st[r / ndpc] * ndpc + r % ndpc;  // stencil dof of this sample dof
     if (c == K) {
       const double ynp1 = y[st];
-      if (first) yn[r] = ynp1;  // first iteration of a step: y_n = y(x_n)
-      const double helper = 1. * ynp1 + (-1.) * yn[r];
+      if (first) {  // first iteration of a step: y_n-1 = y_n, y_n = y(x_n)
+        ynm1[r] = yn[r];
+        yn[r] = ynp1;
+      }
+      const double helper = bdf2 ? 1. * ynp1 + cn * yn[r] + cnm1 * ynm1[r] : 1. * ynp1 + cn * yn[r];
       val = cf * V[r] + 1. * helper;
     } else {
       double jd = 0.;
@@ -429,7 +432,7 @@ struct pda_lspg {
   pda::DevBuf<float> W1, b1, W2, b2, W3, b3, Z, C;
   bool tensorCore = false;
   pda::DevBuf<__nv_bfloat16> W3b, Zb;
-  pda::DevBuf<double> y, D, V, J, yn, partial, xn;
+  pda::DevBuf<double> y, D, V, J, yn, ynm1, partial, xn;
   pda::DevBuf<pda::rom::Flags> flags;
   pda::DevBuf<unsigned> ticket;
   int nblocks = 0;
@@ -439,14 +442,23 @@ struct pda_lspg {
   bool fused = true;
   bool jac32 = false;  // fused form: single-precision Jacobian terms
   int fusedBlocks = 0;
-  cudaGraphExec_t graph = nullptr;
-  double graphDt = 0;
-  double *graphX = nullptr;
-  int graphIters = 0;
-  double graphTol = 0;
-  ~pda_lspg() {
-    if (graph) cudaGraphExecDestroy(graph);
+  // one captured step per backward-difference formula: [0] BDF1 (also the
+  // first step of a BDF2 trajectory), [1] BDF2
+  struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    double dt = 0;
+    double *x = nullptr;
+    int iters = 0;
+    double tol = 0;
+  } graph[2];
+  void drop_graphs() {
+    for (auto &g : graph)
+      if (g.exec) {
+        cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+      }
   }
+  ~pda_lspg() { drop_graphs(); }
 };
 
 namespace pda {
@@ -484,13 +496,29 @@ void decode_k(pda_lspg &L, const double *x, double *y, int first, cudaStream_t s
   }
 }
 
+// the backward-difference scheme of one step: BDF1 (c_n = -1, c_f = -1) or
+// BDF2 (c_n = -4/3, c_n-1 = 1/3, c_f = -2/3), ode_constants.hpp:57-73
+struct Bdf {
+  double cf, cn, cnm1;
+  int two;
+};
+inline Bdf bdf_coeffs(int order, double dt) {
+  constexpr double one = 1., two = 2., three = 3., four = 4.;
+  if (order == 2) return Bdf{-1. * (two / three) * dt, -1. * (four / three), one / three, 1};
+  return Bdf{-1. * dt, -1., 0., 0};
+}
+
 template <int K>
-void gn_iteration_k(pda_lspg &L, double *x, double dt, double tol, int first, cudaStream_t s) {
+void gn_iteration_k(pda_lspg &L, double *x, const Bdf &b, double tol, int first, cudaStream_t s) {
   Flags *f = L.flags.p;
   decode_k<K>(L, x, L.y.p, first, s);
   if (L.fused) {
     pda_problem &P = *L.P;
-    LspgArgs a{L.y.p, L.D.p, K, -dt, L.yn.p, first, L.V.p, L.partial.p, L.ticket.p, x, tol, f, L.jac32 ? 1 : 0};
+    LspgArgs a{L.y.p, L.D.p, K, b.cf, L.yn.p, first, L.V.p, L.partial.p, L.ticket.p, x, tol, f, L.jac32 ? 1 : 0};
+    a.cn = b.cn;
+    a.cnm1 = b.cnm1;
+    a.ynm1 = L.ynm1.p;
+    a.bdf2 = b.two;
     MeshArgs ma = P.margs;
     ma.time = 0.0;
     P.L->lspg_fused(P.scheme, P.innerT.t, P.nearT.t, ma, P.phys, a, s);
@@ -502,8 +530,9 @@ void gn_iteration_k(pda_lspg &L, double *x, double dt, double tol, int first, cu
   const pda_status st = pda_velocity_and_jacobian(L.P, L.y.p, 0.0, L.V.p, L.J.p);
   if (st != PDA_OK) throw Error(st, pda_last_error());
   k_lspg_rows<K><<<L.nblocks, rows_per_block(K) * (K + 1), 0, s>>>(L.ndpc, L.ns, L.s2st.p, L.y.p, L.D.p, L.V.p,
-                                                      L.P->d_rowptr.p, L.P->d_colidx.p, L.J.p, -dt, L.yn.p, first,
-                                                      L.partial.p, L.ticket.p, x, tol, f);
+                                                      L.P->d_rowptr.p, L.P->d_colidx.p, L.J.p, b.cf, L.yn.p, first,
+                                                      L.partial.p, L.ticket.p, x, tol, f, b.cn, b.cnm1, L.ynm1.p,
+                                                      b.two);
 }
 
 #define PDA_ROM_K_SWITCH(k, CALL) \
@@ -525,8 +554,8 @@ bool k_supported(int k) {
   return k == 2 || k == 4 || k == 6 || k == 8 || k == 10 || k == 12 || k == 16 || k == 20 || k == 24 || k == 32;
 }
 
-void gn_iteration(pda_lspg &L, double *x, double dt, double tol, int first, cudaStream_t s) {
-#define PDA_ROM_GN(K) gn_iteration_k<K>(L, x, dt, tol, first, s)
+void gn_iteration(pda_lspg &L, double *x, const Bdf &b, double tol, int first, cudaStream_t s) {
+#define PDA_ROM_GN(K) gn_iteration_k<K>(L, x, b, tol, first, s)
   PDA_ROM_K_SWITCH(L.k, PDA_ROM_GN)
 #undef PDA_ROM_GN
 }
@@ -537,9 +566,9 @@ void decode(pda_lspg &L, const double *x, double *y, cudaStream_t s) {
 #undef PDA_ROM_DEC
 }
 
-void bdf1_step(pda_lspg &L, double *x, double dt, double tol, int iters, cudaStream_t s) {
+void bdf_step(pda_lspg &L, double *x, const Bdf &b, double tol, int iters, cudaStream_t s) {
   // the first iteration ignores the previous step's convergence flag and resets it
-  for (int it = 0; it < iters; ++it) gn_iteration(L, x, dt, tol, it == 0 ? 1 : 0, s);
+  for (int it = 0; it < iters; ++it) gn_iteration(L, x, b, tol, it == 0 ? 1 : 0, s);
   PDA_CUDA(cudaGetLastError());
 }
 
@@ -572,6 +601,7 @@ void common_setup(pda_lspg &L, pda_problem *P, const int64_t *s2st, int k) {
   L.V.alloc((size_t)L.ns);
   L.J.alloc((size_t)std::max<int64_t>(nnz, 1));
   L.yn.alloc((size_t)L.ns);
+  L.ynm1.alloc((size_t)L.ns);
   L.nblocks = div_up(L.ns, rows_per_block(k));
   pda::ensure_row_tables(*P);
   P->L->lspg_fused_prepare();
@@ -701,10 +731,7 @@ pda_status pda_lspg_decode(pda_lspg *L, const double *d_x, double *d_y) {
 pda_status pda_lspg_set_fused(pda_lspg *rom, int fused) {
   PDA_API_BEGIN
   PDA_REQUIRE(rom, PDA_ERR_INVALID_ARGUMENT, "null argument");
-  if (rom->fused != (fused != 0) && rom->graph) {
-    cudaGraphExecDestroy(rom->graph);
-    rom->graph = nullptr;
-  }
+  if (rom->fused != (fused != 0)) rom->drop_graphs();
   rom->fused = fused != 0;
   PDA_API_END
 }
@@ -712,45 +739,52 @@ pda_status pda_lspg_set_fused(pda_lspg *rom, int fused) {
 pda_status pda_lspg_set_jacobian_precision(pda_lspg *rom, int bits) {
   PDA_API_BEGIN
   PDA_REQUIRE(rom && (bits == 32 || bits == 64), PDA_ERR_INVALID_ARGUMENT, "bits must be 32 or 64");
-  if (rom->jac32 != (bits == 32) && rom->graph) {
-    cudaGraphExecDestroy(rom->graph);
-    rom->graph = nullptr;
-  }
+  if (rom->jac32 != (bits == 32)) rom->drop_graphs();
   rom->jac32 = bits == 32;
   PDA_API_END
 }
 
-pda_status pda_lspg_advance_bdf1(pda_lspg *L, double *d_x, double dt, int64_t n_steps, int gn_iters, double tol,
-                                 int use_graph, double *info) {
+pda_status pda_lspg_advance(pda_lspg *L, double *d_x, double dt, int64_t n_steps, int gn_iters, double tol,
+                            int order, int64_t first_step, int use_graph, double *info) {
   PDA_API_BEGIN
   PDA_REQUIRE(L && d_x && n_steps >= 0 && gn_iters >= 1, PDA_ERR_INVALID_ARGUMENT, "invalid argument");
+  PDA_REQUIRE(order == 1 || order == 2, PDA_ERR_INVALID_ARGUMENT, "order must be 1 (BDF1) or 2 (BDF2)");
+  PDA_REQUIRE(first_step >= 1, PDA_ERR_INVALID_ARGUMENT, "steps are numbered from 1");
   cudaStream_t s = L->P->stream;
-  if (!use_graph || s == nullptr) {
-    for (int64_t n = 0; n < n_steps; ++n) pda::rom::bdf1_step(*L, d_x, dt, tol, gn_iters, s);
-  } else {
-    if (L->graph && (L->graphDt != dt || L->graphX != d_x || L->graphIters != gn_iters || L->graphTol != tol)) {
-      cudaGraphExecDestroy(L->graph);
-      L->graph = nullptr;
+  // info[3] covers this call's steps
+  PDA_CUDA(cudaMemsetAsync(&L->flags.p->maxRes, 0, sizeof(double), s));
+  for (int64_t n = 0; n < n_steps; ++n) {
+    // Pressio's BDF2 LSPG takes its first step with BDF1 (lspg_unsteady_rj_policy_hypred.hpp:124-134)
+    const int slot = (order == 2 && first_step + n > 1) ? 1 : 0;
+    const pda::rom::Bdf b = pda::rom::bdf_coeffs(slot == 1 ? 2 : 1, dt);
+    if (!use_graph || s == nullptr) {
+      pda::rom::bdf_step(*L, d_x, b, tol, gn_iters, s);
+      continue;
     }
-    if (!L->graph) {
+    auto &G = L->graph[slot];
+    if (G.exec && (G.dt != dt || G.x != d_x || G.iters != gn_iters || G.tol != tol)) {
+      cudaGraphExecDestroy(G.exec);
+      G.exec = nullptr;
+    }
+    if (!G.exec) {
       PDA_CUDA(cudaStreamSynchronize(s));
       cudaGraph_t g;
       PDA_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       try {
-        pda::rom::bdf1_step(*L, d_x, dt, tol, gn_iters, s);
+        pda::rom::bdf_step(*L, d_x, b, tol, gn_iters, s);
       } catch (...) {
         cudaStreamEndCapture(s, &g);
         throw;
       }
       PDA_CUDA(cudaStreamEndCapture(s, &g));
-      PDA_CUDA(cudaGraphInstantiate(&L->graph, g, 0));
+      PDA_CUDA(cudaGraphInstantiate(&G.exec, g, 0));
       cudaGraphDestroy(g);
-      L->graphDt = dt;
-      L->graphX = d_x;
-      L->graphIters = gn_iters;
-      L->graphTol = tol;
+      G.dt = dt;
+      G.x = d_x;
+      G.iters = gn_iters;
+      G.tol = tol;
     }
-    for (int64_t n = 0; n < n_steps; ++n) PDA_CUDA(cudaGraphLaunch(L->graph, s));
+    PDA_CUDA(cudaGraphLaunch(G.exec, s));
   }
   if (info) {
     pda::rom::Flags hf;
@@ -762,6 +796,11 @@ pda_status pda_lspg_advance_bdf1(pda_lspg *L, double *d_x, double dt, int64_t n_
     info[3] = hf.maxRes;
   }
   PDA_API_END
+}
+
+pda_status pda_lspg_advance_bdf1(pda_lspg *L, double *d_x, double dt, int64_t n_steps, int gn_iters, double tol,
+                                 int use_graph, double *info) {
+  return pda_lspg_advance(L, d_x, dt, n_steps, gn_iters, tol, 1, 1, use_graph, info);
 }
 
 }  // extern "C"

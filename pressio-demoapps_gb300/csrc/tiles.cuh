@@ -104,11 +104,11 @@ __device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &
         const double dL = epsilon * epsilon + 2. * epsilon * BL + BL * BL;
         const double dC = epsilon * epsilon + 2. * epsilon * BC + BC * BC;
         const double dR = epsilon * epsilon + 2. * epsilon * BR + BR * BR;
-        sA[ty][d][0][tx] = oneOvten / dL;    // uNeg alpha0 of face c+1+1/2
-        sA[ty][d][1][tx] = threeOvten / dL;  // uPos alpha0 of face c+1/2
-        sA[ty][d][2][tx] = sixOvten / dC;    // uNeg alpha1 of face c+1/2, uPos alpha1 of face c-1/2
-        sA[ty][d][3][tx] = threeOvten / dR;  // uNeg alpha2 of face c-1/2
-        sA[ty][d][4][tx] = oneOvten / dR;    // uPos alpha2 of face c-2+1/2
+        sA[ty][d][0][tx] = div_rn<true>(oneOvten, dL);    // uNeg alpha0 of face c+1+1/2
+        sA[ty][d][1][tx] = div_rn<true>(threeOvten, dL);  // uPos alpha0 of face c+1/2
+        sA[ty][d][2][tx] = div_rn<true>(sixOvten, dC);    // uNeg alpha1 of face c+1/2, uPos alpha1 of face c-1/2
+        sA[ty][d][3][tx] = div_rn<true>(threeOvten, dR);  // uNeg alpha2 of face c-1/2
+        sA[ty][d][4][tx] = div_rn<true>(oneOvten, dR);    // uPos alpha2 of face c-2+1/2
       }
     }
   } else {
@@ -120,8 +120,8 @@ __device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &
         const double a = sU[ty][d][tx], c = sU[ty][d][tx + 1];
         const double B = (a - c) * (a - c);
         const double den = epsilon * epsilon + two * epsilon * B + B * B;
-        sA[ty][d][0][tx] = oneOvthree / den;
-        sA[ty][d][1][tx] = twoOvthree / den;
+        sA[ty][d][0][tx] = div_rn<true>(oneOvthree, den);
+        sA[ty][d][1][tx] = div_rn<true>(twoOvthree, den);
       }
     }
   }
@@ -144,12 +144,12 @@ __device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &
       const double p3 = w5_pFarR(qip1, qip2, qip3) * oneOvsix;
       {
         const double a0 = sA[ty][d][0][tx], a1 = sA[ty][d][2][tx + 1], a2 = sA[ty][d][3][tx + 2];
-        const double s = 1. / (a0 + a1 + a2);
+        const double s = div_rn<true>(1., (a0 + a1 + a2));
         uN[d] = (a0 * s) * p0 + (a1 * s) * p1 + (a2 * s) * p2;
       }
       {
         const double a0 = sA[ty][d][1][tx + 1], a1 = sA[ty][d][2][tx + 2], a2 = sA[ty][d][4][tx + 3];
-        const double s = 1. / (a0 + a1 + a2);
+        const double s = div_rn<true>(1., (a0 + a1 + a2));
         uP[d] = (a0 * s) * p1 + (a1 * s) * p2 + (a2 * s) * p3;
       }
     }
@@ -165,18 +165,18 @@ __device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &
       const double p2 = (three * qip1 - qip2) * oneOvtwo;
       {
         const double a0 = sA[ty][d][0][tx], a1 = sA[ty][d][1][tx + 1];
-        const double s = 1. / (a0 + a1);
+        const double s = div_rn<true>(1., (a0 + a1));
         uN[d] = (a0 * s) * p0 + (a1 * s) * p1;
       }
       {
         const double a0 = sA[ty][d][1][tx + 1], a1 = sA[ty][d][0][tx + 2];
-        const double s = 1. / (a0 + a1);
+        const double s = div_rn<true>(1., (a0 + a1));
         uP[d] = (a0 * s) * p1 + (a1 * s) * p2;
       }
     }
   }
   double fl[NDPC];
-  F::template flux<AXIS>(fl, uN, uP, p);
+  F::template flux<AXIS, true>(fl, uN, uP, p);
   // output layout of k_struct_faces: face axis index fastest within its line
   // ordering [A2][A1][face] for AXIS=0, [k][face][i] for AXIS=1, [face][j][i] for AXIS=2
   const int fi = f - b.lo[AXIS];

@@ -119,6 +119,13 @@ struct LspgArgs {
   int jac32;         // 1: reconstruction gradients, flux Jacobians and Jf D in
                      // single precision (an inexact Gauss-Newton step; V, R, the
                      // normal equations and the solve stay double)
+  // backward-difference history: R = cf V + (y + cn y_n [+ cnm1 y_n-1]) with
+  // BDF1 (cf, cn) = (-dt, -1), BDF2 (cf, cn, cnm1) = (-2/3 dt, -4/3, 1/3); the
+  // first iteration of a step moves y_n to y_n-1 (ynm1) and stores y(x_n)
+  double cn;
+  double cnm1;
+  double *ynm1;
+  int bdf2;
 };
 
 struct BatchArgs {

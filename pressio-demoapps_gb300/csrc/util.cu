@@ -1,4 +1,7 @@
-// Element-wise stepper updates and the CSR sparse x dense product.
+// Element-wise stepper updates, the CSR sparse x dense product, the FP64
+// throughput probe and the self-check of the integer-pipe division and
+// square root.
+#include "fp64_intpipe.cuh"
 #include "launch.hpp"
 
 namespace pda {
@@ -56,7 +59,77 @@ __global__ void k_fp64_fma(double *out, int iters, double a, double b) {
   if (s == 123.456) out[threadIdx.x] = s;  // keeps the chains alive
 }
 
+__device__ __forceinline__ uint64_t splitmix64(uint64_t &s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// Operand sets for the comparison of ip::div / ip::sqrt with the FP64 pipe's
+// IEEE operations.  mode 0: random mantissas, exponents within 2^-40..2^40
+// (quotients and roots of the normal range); 1: divisors with mantissas
+// within 1024 units of 1 and of 2 - 2^-52 (the ends of the reciprocal's
+// range); 2: near-exact quotients and roots (rounding midpoints and exact
+// results: a = b q or x = q^2 with short q, moved by up to two units);
+// 3: arbitrary bit patterns (zeros, subnormals, infinities, NaNs included).
+__global__ void k_check_divsqrt(int mode, uint64_t seed, long per_thread, unsigned long long *bad) {
+  uint64_t st = seed ^ ((uint64_t)(blockIdx.x * blockDim.x + threadIdx.x) * 0x632BE59BD9B4E019ull);
+  unsigned long long nd = 0, ns = 0;
+  constexpr uint64_t M = 0x000FFFFFFFFFFFFFull;
+  for (long k = 0; k < per_thread; ++k) {
+    const uint64_t r1 = splitmix64(st), r2 = splitmix64(st), r3 = splitmix64(st);
+    uint64_t ua, ub, ux;
+    if (mode == 0) {
+      ua = (r1 & M) | ((uint64_t)(1023 + (int)(r3 % 81) - 40) << 52) | (r3 & (1ull << 63));
+      ub = (r2 & M) | ((uint64_t)(1023 + (int)((r3 >> 8) % 81) - 40) << 52) | ((r3 << 1) & (1ull << 63));
+      ux = (r2 & M) | ((uint64_t)(1023 - 60 + (int)((r1 >> 52) % 121)) << 52);
+    } else if (mode == 1) {
+      const uint64_t m = (r2 & 1) ? (M - (r2 >> 1) % 1024) : ((r2 >> 1) % 1024);
+      ua = (r1 & M) | (1023ull << 52);
+      ub = m | ((uint64_t)(1000 + (r3 % 40)) << 52);
+      ux = m | ((uint64_t)(1000 + (r3 % 41)) << 52);
+    } else if (mode == 2) {
+      const double b = __longlong_as_double((long long)((r2 & M & ~0xFFFFFFull) | (1023ull << 52)));
+      const double q = __longlong_as_double((long long)((r1 & M & ~0xFFFFFFFull) | (1023ull << 52)));
+      ua = (uint64_t)__double_as_longlong(b * q) + (r3 & 1 ? ((r3 >> 1) % 5) - 2 : 0);
+      ub = (uint64_t)__double_as_longlong(b);
+      ux = (uint64_t)__double_as_longlong(q * q) + ((r3 >> 8) % 5) - 2;
+    } else {
+      ua = r1;
+      ub = r2;
+      ux = r3;
+    }
+    const double a = __longlong_as_double((long long)ua), b = __longlong_as_double((long long)ub);
+    const double x = __longlong_as_double((long long)ux);
+    const double hd = a / b, gd = ip::div(a, b);
+    const double hs = sqrt(x), gs = ip::sqrt(x);
+    nd += !(__double_as_longlong(hd) == __double_as_longlong(gd) || (hd != hd && gd != gd));
+    ns += !(__double_as_longlong(hs) == __double_as_longlong(gs) || (hs != hs && gs != gs));
+  }
+  atomicAdd(bad, nd);
+  atomicAdd(bad + 1, ns);
+}
+
 }  // namespace
+
+void check_divsqrt(int mode, uint64_t seed, long per_thread, long long counts[3], cudaStream_t s) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  unsigned long long *bad = nullptr;
+  cudaMalloc((void **)&bad, 2 * sizeof(unsigned long long));
+  cudaMemsetAsync(bad, 0, 2 * sizeof(unsigned long long), s);
+  const int blocks = (sms > 0 ? sms : 1) * 8, threads = 256;
+  k_check_divsqrt<<<blocks, threads, 0, s>>>(mode, seed, per_thread, bad);
+  unsigned long long h[2] = {0, 0};
+  cudaMemcpyAsync(h, bad, sizeof(h), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  cudaFree(bad);
+  counts[0] = (long long)blocks * threads * per_thread;
+  counts[1] = (long long)h[0];
+  counts[2] = (long long)h[1];
+}
 
 double measure_fp64_fma_rate(int blocks, int threads, int iters, cudaStream_t s) {
   double *out = nullptr;

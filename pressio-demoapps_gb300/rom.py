@@ -10,7 +10,8 @@ decoder evaluated only at the stencil-mesh rows.  Torch holds device buffers
 and does the offline bookkeeping (slicing, normalisation, the POD basis of
 the affine baseline); every residual, Jacobian, GEMM and solve runs in the
 library's kernels.  The reference (pressio-demoapps) has no ROM; the LSPG
-algorithm is Pressio's (rom/impl/lspg_unsteady_rj_policy_hypred.hpp).
+algorithm is Pressio's (rom/impl/lspg_unsteady_rj_policy_hypred.hpp), with
+BDF1 or BDF2.  The full-order model is the ROM's fallback (FallbackRun).
 """
 from __future__ import annotations
 
@@ -205,22 +206,75 @@ def rel_l2(a, b, ref=None):
     return num / max(den, 1e-300)
 
 
-def run_rom(rom, x0, dt, checkpoints_steps, stream, gn_iters=5, tol=1e-9):
-    """Advance the latent through the checkpoints (step counts of size dt);
-    returns {step: latent}, wall seconds, max residual norm."""
+def run_rom(rom, x0, dt, checkpoints_steps, stream, gn_iters=5, tol=1e-9, order=1):
+    """Advance the latent through the checkpoints (step counts of size dt)
+    with BDF1 (order 1) or BDF2 (order 2); returns {step: latent}, wall
+    seconds, max residual norm.  The step graphs are captured on the buffer
+    the timed run uses, so no capture or instantiation is timed."""
+    import torch
     x = x0.clone()
-    rom.advance_bdf1(x, dt, 1, gn_iters, tol)  # capture the step graph
-    x = x0.clone()
+    rom.advance(x, dt, 1, gn_iters, tol, order=order, first_step=1)  # capture the first step's graph
+    if order == 2:
+        rom.advance(x, dt, 1, gn_iters, tol, order=2, first_step=2)  # and the BDF2 step's
+    with torch.cuda.stream(stream):
+        x.copy_(x0)
     stream.synchronize()
     out, done, wall, maxres = {}, 0, 0.0, 0.0
     for c in sorted(checkpoints_steps):
         t0 = time.perf_counter()
-        info = rom.advance_bdf1(x, dt, c - done, gn_iters, tol)
+        info = rom.advance(x, dt, c - done, gn_iters, tol, order=order, first_step=done + 1)
         wall += time.perf_counter() - t0
         maxres = max(maxres, info["max_residual"])
         done = c
         out[c] = x.clone()
     return out, wall, maxres
+
+
+class FallbackRun:
+    """A ROM trajectory whose steps fall back to the full-order model.
+
+    The ROM advances checkpoint by checkpoint; when the largest Gauss-Newton
+    residual norm of a stretch exceeds `threshold`, that stretch is dropped,
+    the latent state at its start is decoded to the full state and the GPU FOM
+    (SSP-RK3 at the FOM step) advances from there to the end.  `states` holds
+    the full state at every checkpoint (decoded where the ROM produced it),
+    `fallback_at` the FOM step count where the FOM took over (None if never)."""
+
+    def __init__(self, setup, params, rom, decoder, x0, dt_fom, ratio, checkpoints, threshold, gn_iters=1,
+                 tol=1e-9, order=1):
+        import torch
+        self.states, self.fallback_at = {}, None
+        x = x0.clone()
+        rom.advance(x, dt_fom * ratio, 1, gn_iters, tol, order=order, first_step=1)
+        if order == 2:
+            rom.advance(x, dt_fom * ratio, 1, gn_iters, tol, order=2, first_step=2)
+        with torch.cuda.stream(setup.stream):
+            x.copy_(x0)
+        fom = setup.problem(params)
+        U = fom.initialCondition()
+        fom.advance_ssprk3(U, 0.0, dt_fom, 1)  # capture the FOM step graph on U
+        setup.stream.synchronize()
+        wall, done = 0.0, 0
+        for c in sorted(checkpoints):
+            t0 = time.perf_counter()
+            if self.fallback_at is None:
+                with torch.cuda.stream(setup.stream):
+                    start = x.clone()
+                info = rom.advance(x, dt_fom * ratio, (c - done) // ratio, gn_iters, tol, order=order,
+                                   first_step=done // ratio + 1)
+                if info["max_residual"] > threshold:
+                    self.fallback_at = done
+                    y = decoder.decode(start)
+                    with torch.cuda.stream(setup.stream):
+                        U.copy_(y)
+                    fom.advance_ssprk3(U, done * dt_fom, dt_fom, c - done)
+            else:
+                fom.advance_ssprk3(U, done * dt_fom, dt_fom, c - done)
+            setup.stream.synchronize()
+            wall += time.perf_counter() - t0
+            self.states[c] = U.clone() if self.fallback_at is not None else decoder.decode(x)
+            done = c
+        self.wall = wall
 
 
 def timed(fn):

@@ -1,7 +1,7 @@
 """Pins the LSPG oracle (oracle/lspg_oracle.py): every step it returns is a
 stationary point of ||R(x)||^2 (the Gauss-Newton normal equations hold at the
 returned latent) and equals the minimiser found by scipy's Levenberg-Marquardt
-on the same BDF1 residual."""
+on the same BDF1 or BDF2 residual."""
 from __future__ import annotations
 
 import os
@@ -56,3 +56,37 @@ def test_lspg_oracle_steps_are_least_squares_minimisers(pda, oracle):
     assert np.linalg.norm(JR.T @ R) <= 1e-9 * np.linalg.norm(JR) * max(np.linalg.norm(R), 1e-300)
     ref = least_squares(resid, x0, jac=jac, method="lm", xtol=1e-15, ftol=1e-15, gtol=1e-15)
     assert np.allclose(x1, ref.x, rtol=1e-8, atol=1e-11)
+
+
+def test_lspg_oracle_bdf2_steps_are_least_squares_minimisers(pda, oracle):
+    """BDF2 (Pressio's hyper-reduced policy: step 1 is BDF1, then
+    R = -2/3 dt V(y) + (y - 4/3 y_n + 1/3 y_n-1))."""
+    from scipy.optimize import least_squares
+    po, s2st, uref, phi, _ = _setup(pda, oracle, seed=3)
+    dec = lspg_oracle.affine_decoder(uref, phi)
+    x0 = np.array([0.1, -0.05, 0.02, 0.03])
+    dt = 0.01
+    _, traj = lspg_oracle.lspg_bdf(po, s2st, dec, x0, dt, 3, order=2, iters=25, tol=1e-13)
+    sd = lspg_oracle.sample_dofs(s2st, 3)
+    # step 1 is the BDF1 step
+    x1b, _ = lspg_oracle.lspg_bdf1(po, s2st, dec, x0, dt, 1, iters=25, tol=1e-13)
+    assert np.array_equal(traj[0], x1b)
+    for n in (1, 2):
+        yn = dec(traj[n - 1])[0][sd]
+        ynm1 = dec(traj[n - 2] if n >= 2 else x0)[0][sd]
+
+        def resid(x):
+            y, _ = dec(x)
+            return -(2. / 3.) * dt * po.velocity(y) + (y[sd] - (4. / 3.) * yn + (1. / 3.) * ynm1)
+
+        def jac(x):
+            y, D = dec(x)
+            _, rp, ci, jv = po.velocity_and_jacobian(y)
+            J = sp.csr_matrix((jv, ci, rp), shape=(len(rp) - 1, len(y)))
+            return -(2. / 3.) * dt * (J @ D) + D[sd]
+
+        xs = traj[n]
+        R, JR = resid(xs), jac(xs)
+        assert np.linalg.norm(JR.T @ R) <= 1e-9 * np.linalg.norm(JR) * max(np.linalg.norm(R), 1e-300)
+        ref = least_squares(resid, traj[n - 1], jac=jac, method="lm", xtol=1e-15, ftol=1e-15, gtol=1e-15)
+        assert np.allclose(xs, ref.x, rtol=1e-8, atol=1e-11)
