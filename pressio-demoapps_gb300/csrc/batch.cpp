@@ -30,7 +30,7 @@ struct pda_batch {
   pda::DevBuf<pda::BatchItem> d_items;
   pda::DevBuf<long> d_tileStart[3], d_blockStart;
   pda::BatchArgs args{};
-  pda::DevBuf<double> F, aux, r0;
+  pda::DevBuf<double> F, aux;
   cudaGraphExec_t graph = nullptr;
   double graphDt = 0;
   double *graphU = nullptr;
@@ -97,29 +97,32 @@ void batch_velocity(pda_batch &B, const double *U, double *V) {
 }
 
 void batch_buffers(pda_batch &B) {
-  if (B.r0.p && B.aux.p) return;
+  if (B.aux.p) return;
   B.aux.alloc((size_t)B.totalDofs);
-  B.r0.alloc((size_t)B.totalDofs);
   // entries between instances are never written by the kernels: keep them 0
-  PDA_CUDA(cudaMemsetAsync(B.r0.p, 0, (size_t)B.totalDofs * sizeof(double), B.stream));
   PDA_CUDA(cudaMemsetAsync(B.aux.p, 0, (size_t)B.totalDofs * sizeof(double), B.stream));
 }
 
 // One SSP-RK3 step, the single-problem stage formulas over the packed vector
-// (ode_explicit_stepper_without_mass_matrix.hpp:230-282).
+// (ode_explicit_stepper_without_mass_matrix.hpp:230-282): per stage the face
+// passes, then the balance fused with the stage update (no velocity buffer).
+void batch_faces_all(pda_batch &B, const double *U) {
+  for (int a = 0; a < B.dim; ++a) {
+    B.probs[0]->L->batch_faces(B.scheme, a, B.shape[a], B.args, U, B.F.p, B.stream);
+    ++B.launches;
+  }
+}
+
 void batch_ssprk3_step(pda_batch &B, double *U, double dt) {
-  const long n = (long)B.totalDofs;
-  double *r0 = B.r0.p, *aux = B.aux.p;
-  batch_velocity(B, U, r0);
-  launch_axpby_stage(0, aux, U, r0, nullptr, 0., dt, 0., 0., nullptr, nullptr, n, B.stream);
-  batch_velocity(B, aux, r0);
-  const double fourInv = 1. / 4., threeOvFour = 3. / 4.;
-  launch_axpby_stage(1, aux, U, r0, nullptr, fourInv, threeOvFour, fourInv * dt, 0., nullptr, nullptr, n,
-                     B.stream);
-  batch_velocity(B, aux, r0);
-  const double oneOvThree = 1. / 3., twoOvThree = 2. / 3.;
-  launch_axpby_stage(1, U, aux, r0, nullptr, oneOvThree, twoOvThree, twoOvThree * dt, 0., nullptr, nullptr, n,
-                     B.stream);
+  double *aux = B.aux.p;
+  const pda::Launchers &L = *B.probs[0]->L;
+  const double fourInv = 1. / 4., threeOvFour = 3. / 4., oneOvThree = 1. / 3., twoOvThree = 2. / 3.;
+  batch_faces_all(B, U);  // u_1 = u_n + dt rhs(u_n)
+  L.batch_balance_stage(B.args, U, B.F.p, aux, U, 0, 0., dt, 0., B.stream);
+  batch_faces_all(B, aux);  // u_2 = 3/4 u_n + 1/4 u_1 + 1/4 dt rhs(u_1)
+  L.batch_balance_stage(B.args, aux, B.F.p, aux, U, 1, fourInv, threeOvFour, fourInv * dt, B.stream);
+  batch_faces_all(B, aux);  // u_n+1 = 1/3 u_n + 2/3 u_2 + 2/3 dt rhs(u_2)
+  L.batch_balance_stage(B.args, aux, B.F.p, U, aux, 1, oneOvThree, twoOvThree, twoOvThree * dt, B.stream);
   B.launches += 3;
   PDA_CUDA(cudaGetLastError());
 }

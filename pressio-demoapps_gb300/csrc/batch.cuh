@@ -77,4 +77,36 @@ k_batch_balance(BatchArgs a, const double *__restrict__ U, const double *__restr
   }
 }
 
+// The balance of every instance fused with an SSP-RK3 stage update: the
+// velocity r of the cell (state Us) goes straight into
+//   kind 0: out = x + cb r
+//   kind 1: out = ca out + cb x + cc r
+// (the stage formulas of the unfused update kernels, same association), so
+// the stage needs no velocity buffer and no separate update pass.  Each
+// thread reads its own cell's state before writing, so out may be Us.
+template <int FAM>
+__global__ void __launch_bounds__(kBalanceBlock)
+k_batch_balance_stage(BatchArgs a, const double *Us, const double *__restrict__ F, double *out,
+                      const double *x, int kind, double ca, double cb, double cc) {
+  constexpr int NDPC = Fam<FAM>::ndpc;
+  for (long blk = blockIdx.x; blk < a.totalBlocks; blk += gridDim.x) {
+    const int it = batch_find(a.blockStart, a.nItems, blk);
+    const BatchItem &bi = a.items[it];
+    const Box b = bi.b;
+    const MeshArgs m = bi.m;
+    const Phys p = bi.p;
+    const long t = (blk - a.blockStart[it]) * kBalanceBlock + threadIdx.x;
+    double v[NDPC];
+    long cell;
+    if (!balance_values<FAM>(b, m, p, Us + bi.uOff, F + bi.fOff[0], F + bi.fOff[1], F + bi.fOff[2], t, v, cell))
+      continue;
+    const long q0 = bi.uOff + cell * NDPC;
+#pragma unroll
+    for (int d = 0; d < NDPC; ++d) {
+      const long q = q0 + d;
+      out[q] = kind == 0 ? x[q] + cb * v[d] : ca * out[q] + cb * x[q] + cc * v[d];
+    }
+  }
+}
+
 }  // namespace pda

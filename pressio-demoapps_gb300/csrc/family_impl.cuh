@@ -279,36 +279,45 @@ void batch_balance(const BatchArgs &a, const double *U, const double *Fo, double
   if (g > 0) k<<<(unsigned)g, kBalanceBlock, 0, s>>>(a, U, Fo, V);
 }
 
+void batch_balance_stage(const BatchArgs &a, const double *Us, const double *Fo, double *out, const double *x,
+                         int kind, double ca, double cb, double cc, cudaStream_t s) {
+  auto k = k_batch_balance_stage<FAM>;
+  const long g = persistent_grid(k, kBalanceBlock, a.totalBlocks);
+  if (g > 0) k<<<(unsigned)g, kBalanceBlock, 0, s>>>(a, Us, Fo, out, x, kind, ca, cb, cc);
+}
+
 int batch_num_shapes() { return F::dim == 2 ? kNumTileShapes : 1; }
 
 
 // ----------------------------------------------------- Jacobian, faces once
+template <int SCHEME, int AXIS>
+void struct_vj_axis(const Box &b, const MeshArgs &m, const Phys &p, const double *U, const int *rowptr,
+                    double *V, double *J, cudaStream_t s) {
+  constexpr int LANES = 64;
+  using Cfg = JTileCfg<FAM, SCHEME, LANES>;
+  constexpr int A1 = AXIS == 0 ? 1 : 0, A2 = AXIS == 2 ? 1 : 2;
+  const long lines = (long)(b.hi[A1] - b.lo[A1]) * (b.hi[A2] - b.lo[A2]);
+  const int nfa = b.hi[AXIS] - b.lo[AXIS] + 1;
+  dim3 grid((unsigned)lines, (unsigned)div_up(nfa, Cfg::TW));
+  k_jtile<FAM, SCHEME, AXIS, LANES><<<grid, LANES, 0, s>>>(b, m, p, U, rowptr, V, J);
+}
+
 template <int SCHEME>
-void struct_vj_s(const Box &b, const MeshArgs &m, const Phys &p, const double *U, double *const T[3],
-                 const int *rowptr, double *V, double *J, cudaStream_t s, int *launches) {
+void struct_vj_s(const Box &b, const MeshArgs &m, const Phys &p, const double *U, const int *rowptr, double *V,
+                 double *J, cudaStream_t s, int *launches) {
   long nc = 1;
   for (int a = 0; a < 3; ++a) nc *= (long)(b.hi[a] - b.lo[a]);
   if (nc <= 0) return;
-  auto nfaces = [&](int ax) {
-    long nf = 1;
-    for (int a = 0; a < 3; ++a) nf *= (long)(b.hi[a] - b.lo[a] + (a == ax ? 1 : 0));
-    return nf;
-  };
-  k_jfaces<FAM, SCHEME, 0><<<div_up(nfaces(0), 128), 128, 0, s>>>(b, p, m.hinv[0], U, T[0]);
-  if constexpr (F::dim > 1) k_jfaces<FAM, SCHEME, 1><<<div_up(nfaces(1), 128), 128, 0, s>>>(b, p, m.hinv[1], U, T[1]);
-  if constexpr (F::dim > 2) k_jfaces<FAM, SCHEME, 2><<<div_up(nfaces(2), 128), 128, 0, s>>>(b, p, m.hinv[2], U, T[2]);
-  k_jassemble<FAM, SCHEME><<<div_up(nc, 128), 128, 0, s>>>(b, m, p, U, T[0], T[1], T[2], rowptr, V, J);
-  *launches += F::dim + 1;
+  struct_vj_axis<SCHEME, 0>(b, m, p, U, rowptr, V, J, s);
+  if constexpr (F::dim > 1) struct_vj_axis<SCHEME, 1>(b, m, p, U, rowptr, V, J, s);
+  if constexpr (F::dim > 2) struct_vj_axis<SCHEME, 2>(b, m, p, U, rowptr, V, J, s);
+  *launches += F::dim;
 }
 
-void struct_vj(int scheme, const Box &b, const MeshArgs &m, const Phys &p, const double *U, double *const T[3],
-               const int *rowptr, double *V, double *J, cudaStream_t s, int *launches) {
-  if (scheme == Weno3) struct_vj_s<Weno3>(b, m, p, U, T, rowptr, V, J, s, launches);
-  else if (scheme == Weno5) struct_vj_s<Weno5>(b, m, p, U, T, rowptr, V, J, s, launches);
-}
-
-int jface_components(int scheme) {
-  return scheme == Weno3 ? JFaceLayout<FAM, Weno3>::NCOMP : (scheme == Weno5 ? JFaceLayout<FAM, Weno5>::NCOMP : 0);
+void struct_vj(int scheme, const Box &b, const MeshArgs &m, const Phys &p, const double *U, const int *rowptr,
+               double *V, double *J, cudaStream_t s, int *launches) {
+  if (scheme == Weno3) struct_vj_s<Weno3>(b, m, p, U, rowptr, V, J, s, launches);
+  else if (scheme == Weno5) struct_vj_s<Weno5>(b, m, p, U, rowptr, V, J, s, launches);
 }
 
 }  // namespace

@@ -337,19 +337,18 @@ k_struct_faces(Box b, Phys p, const double *__restrict__ U, double *__restrict__
 // V for every box cell from the face fluxes, in the reference's axis order
 // (x, then y, then z, then the shallow-water Coriolis source).
 template <int FAM>
-__device__ __forceinline__ void balance_cell(const Box &b, const MeshArgs &m, const Phys &p,
-                                             const double *__restrict__ U, const double *__restrict__ Fx,
-                                             const double *__restrict__ Fy, const double *__restrict__ Fz,
-                                             double *__restrict__ V, long t) {
+__device__ __forceinline__ bool balance_values(const Box &b, const MeshArgs &m, const Phys &p,
+                                               const double *__restrict__ U, const double *__restrict__ Fx,
+                                               const double *__restrict__ Fy, const double *__restrict__ Fz,
+                                               long t, double v[], long &cell) {
   using F = Fam<FAM>;
   constexpr int NDPC = F::ndpc, DIM = F::dim;
   const int nb[3] = {b.hi[0] - b.lo[0], b.hi[1] - b.lo[1], b.hi[2] - b.lo[2]};
   const long total = (long)nb[0] * nb[1] * nb[2];
-  if (t >= total) return;
+  if (t >= total) return false;
   const int i = (int)(t % nb[0]);
   const int j = (int)((t / nb[0]) % nb[1]);
   const int k = (int)(t / ((long)nb[0] * nb[1]));
-  double v[NDPC];
 #pragma unroll
   for (int d = 0; d < NDPC; ++d) v[d] = 0.;
   {
@@ -369,12 +368,24 @@ __device__ __forceinline__ void balance_cell(const Box &b, const MeshArgs &m, co
 #pragma unroll
     for (int d = 0; d < NDPC; ++d) v[d] += m.hinv[2] * (Fz[f0 + d] - Fz[f1 + d]);
   }
-  const long cell = (i + b.lo[0]) + (long)b.n[0] * ((j + b.lo[1]) + (long)b.n[1] * (k + b.lo[2]));
+  cell = (i + b.lo[0]) + (long)b.n[0] * ((j + b.lo[1]) + (long)b.n[1] * (k + b.lo[2]));
   if constexpr (FAM == Swe2d) {
     const double u0 = __ldg(U + cell * 3), u1 = __ldg(U + cell * 3 + 1), u2 = __ldg(U + cell * 3 + 2);
     v[1] -= p.coriolis * u2 / u0;
     v[2] += p.coriolis * u1 / u0;
   }
+  return true;
+}
+
+template <int FAM>
+__device__ __forceinline__ void balance_cell(const Box &b, const MeshArgs &m, const Phys &p,
+                                             const double *__restrict__ U, const double *__restrict__ Fx,
+                                             const double *__restrict__ Fy, const double *__restrict__ Fz,
+                                             double *__restrict__ V, long t) {
+  constexpr int NDPC = Fam<FAM>::ndpc;
+  double v[NDPC];
+  long cell;
+  if (!balance_values<FAM>(b, m, p, U, Fx, Fy, Fz, t, v, cell)) return;
 #pragma unroll
   for (int d = 0; d < NDPC; ++d) V[cell * NDPC + d] = v[d];
 }

@@ -34,13 +34,14 @@ struct Launchers {
   void (*batch_faces)(int scheme, int axis, int shape, const BatchArgs &a, const double *U, double *F,
                       cudaStream_t s);
   void (*batch_balance)(const BatchArgs &a, const double *U, const double *F, double *V, cudaStream_t s);
+  // the balance fused with an SSP-RK3 stage update (k_batch_balance_stage)
+  void (*batch_balance_stage)(const BatchArgs &a, const double *Us, const double *F, double *out,
+                              const double *x, int kind, double ca, double cb, double cc, cudaStream_t s);
   int (*batch_num_shapes)();  // tile shapes compiled for this family
-  // V + J of the inner box with faces computed once (WENO3 / WENO5):
-  // T[axis] holds jface_components(scheme) doubles per face of that axis
+  // V + J of the inner box with faces computed once (WENO3 / WENO5), one
+  // launch per axis (jfaces.cuh)
   void (*struct_vj)(int scheme, const Box &b, const MeshArgs &m, const Phys &p, const double *U,
-                    double *const T[3], const int *rowptr, double *V, double *J, cudaStream_t s,
-                    int *launches);
-  int (*jface_components)(int scheme);
+                    const int *rowptr, double *V, double *J, cudaStream_t s, int *launches);
   // one fused LSPG Gauss-Newton iteration over the inner rows ti and the
   // near-boundary rows tn (lspg_fused.cuh); grid = lspg_fused_blocks(...)
   void (*lspg_fused)(int scheme, const RowTable &ti, const RowTable &tn, const MeshArgs &m, const Phys &p,

@@ -733,16 +733,8 @@ void velocity_and_jacobian(pda_problem &P, const double *U, double *V, double *J
     build_near_table(P, true);
     pattern_to_device(P);
     P.nearT.sync();
-    const long nc = P.L->jface_components(P.scheme);
-    double *T[3] = {nullptr, nullptr, nullptr};
-    for (int a = 0; a < P.dim; ++a) {
-      long nf = 1;
-      for (int c = 0; c < 3; ++c) nf *= (long)(P.jbox.hi[c] - P.jbox.lo[c] + (c == a ? 1 : 0));
-      P.JT[a].alloc((size_t)(nf * nc));
-      T[a] = P.JT[a].p;
-    }
     int nl = 0;
-    P.L->struct_vj(P.scheme, P.jbox, ma, P.phys, U, T, P.d_rowptr.p, V, J, P.stream, &nl);
+    P.L->struct_vj(P.scheme, P.jbox, ma, P.phys, U, P.d_rowptr.p, V, J, P.stream, &nl);
     check_launch(P, nl);
     if (P.nearT.t.nrows > 0) {
       P.L->rows_vj_nearbd(P.scheme, P.nearT.t, ma, P.phys, U, P.d_rowptr.p, V, J, P.stream);

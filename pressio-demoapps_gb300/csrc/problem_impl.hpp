@@ -155,7 +155,7 @@ struct pda_problem {
   // Jacobian, faces once on the inner box (jfaces.cuh)
   bool jStruct = false;
   pda::Box jbox{};
-  pda::DevBuf<double> JT[3];
+
   pda::Table nearT;   // near-boundary rows: V stencil (+ J first-order tables)
   pda::Table innerT;  // inner rows (sample meshes for V; every mesh for V+J)
   bool innerBuiltV = false, innerBuiltJ = false, nearBuiltJ = false;

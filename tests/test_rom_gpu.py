@@ -273,3 +273,130 @@ def test_lspg_single_precision_jacobian_is_an_inexact_gauss_newton_step(pda, fam
     assert not np.array_equal(out[1], out[0])  # the single-precision kernel ran
     with pytest.raises(pda.PdaError):
         rom.set_jacobian_precision(16)
+
+
+@pytest.mark.gpu
+def test_lspg_bdf2_matches_oracle_fused_assembled_graph_and_chunks(pda, oracle):
+    """BDF2 LSPG (Pressio's hyper-reduced policy: step 1 with BDF1, then
+    R = -2/3 dt V + (y - 4/3 y_n + 1/3 y_n-1)) against the numpy oracle:
+    fused and assembled iterations, eager and graph replay, one call and the
+    same steps split over calls that continue the step numbering."""
+    import torch
+    import lspg_oracle
+    full, sm, st, ps, po, om, s2st, rng = _sample_problem(pda, oracle, seed=4)
+    nst = len(st) * 3
+    k = 6
+    uref = np.zeros(nst)
+    uref[0::3] = 1.0
+    phi, _ = np.linalg.qr(rng.normal(0, 1, (nst, k)))
+    phi *= 0.3
+    x0 = np.array([0.1, -0.05, 0.02, 0.0, 0.01, -0.02])
+    dt, steps = 0.01, 5
+    xr, _ = lspg_oracle.lspg_bdf(po, s2st, lspg_oracle.affine_decoder(uref, phi), x0, dt, steps, order=2, iters=8,
+                                 tol=1e-12)
+    x1, _ = lspg_oracle.lspg_bdf1(po, s2st, lspg_oracle.affine_decoder(uref, phi), x0, dt, steps, iters=8,
+                                  tol=1e-12)
+    assert not np.allclose(xr, x1, rtol=1e-6)  # the second-order steps differ from BDF1's
+    res = []
+    for fused in (True, False):
+        for graph in (False, True):
+            rom = pda.LspgRom.affine(ps, s2st, torch.from_numpy(uref).cuda(), torch.from_numpy(phi).cuda())
+            rom.set_fused(fused)
+            x = torch.from_numpy(x0).cuda()
+            rom.advance(x, dt, steps, gn_iters=8, tol=1e-12, order=2, first_step=1, use_graph=graph)
+            res.append(x.cpu().numpy())
+            assert np.allclose(res[-1], xr, rtol=1e-8, atol=1e-12), (fused, graph, res[-1], xr)
+            # the same trajectory in three calls
+            x = torch.from_numpy(x0).cuda()
+            rom.advance(x, dt, 1, gn_iters=8, tol=1e-12, order=2, first_step=1, use_graph=graph)
+            rom.advance(x, dt, 3, gn_iters=8, tol=1e-12, order=2, first_step=2, use_graph=graph)
+            rom.advance(x, dt, 1, gn_iters=8, tol=1e-12, order=2, first_step=5, use_graph=graph)
+            assert np.array_equal(x.cpu().numpy(), res[-1])
+    assert np.array_equal(res[0], res[1]) and np.array_equal(res[2], res[3])
+
+
+def _small_swe_rom(pda, n=24, k=6, seed=0):
+    """A small slip-wall shallow-water ROM setup: full problem, sample mesh
+    (30 % of the cells + WENO5 stencils), a POD basis of FOM snapshots, the
+    sample LSPG and the full-mesh decoder of the same basis."""
+    import torch
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("pda_gb300_rom", os.path.join(
+        os.path.dirname(ORACLE), "pressio-demoapps_gb300", "rom.py"))
+    R = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(R)
+    setup = R.SweSetup(pda, n)
+    params = {"gravity": 7.5, "coriolis": -2.5, "pulseMagnitude": 0.15}
+    dt = 0.01
+    S = setup.snapshots([params], dt, 40)
+    phi = R.pod_basis(S, setup.uref, k)
+    sm, gids, st, s2st = setup.sample_mesh(0.3, seed=seed)
+    ps = setup.problem(params, mesh=sm)
+    rom = R.affine_lspg(setup, phi, ps, s2st, st, jacobian_bits=64)
+    fp = setup.problem(params)
+    dec = pda.LspgRom.affine(fp, np.arange(n * n), setup.uref, phi)
+    U0 = fp.initialCondition()
+    x0 = (phi.T @ (U0 - setup.uref)).contiguous()
+    return R, setup, params, dt, rom, dec, x0
+
+
+@pytest.mark.gpu
+def test_rom_falls_back_to_the_fom(pda):
+    """FallbackRun: with a residual threshold of 0 the first stretch's
+    residual exceeds it, so the FOM takes over from the decoded initial
+    latent and every checkpoint equals the FOM advanced from that state; with
+    an infinite threshold the ROM runs to the end and matches run_rom."""
+    import torch
+    R, setup, params, dt, rom, dec, x0 = _small_swe_rom(pda)
+    ratio, cps = 2, [4, 8, 12]
+    fb = R.FallbackRun(setup, params, rom, dec, x0, dt, ratio, cps, threshold=0.0, gn_iters=2, order=2)
+    assert fb.fallback_at == 0
+    fom = setup.problem(params)
+    U = dec.decode(x0)
+    done = 0
+    for c in cps:
+        fom.advance_ssprk3(U, done * dt, dt, c - done)
+        done = c
+        setup.stream.synchronize()
+        assert torch.equal(fb.states[c], U), c
+    nofb = R.FallbackRun(setup, params, rom, dec, x0, dt, ratio, cps, threshold=float("inf"), gn_iters=2, order=2)
+    assert nofb.fallback_at is None
+    lat, _, _ = R.run_rom(rom, x0, dt * ratio, [c // ratio for c in cps], setup.stream, gn_iters=2, order=2)
+    for c in cps:
+        assert torch.equal(nofb.states[c], dec.decode(lat[c // ratio])), c
+
+
+@pytest.mark.gpu
+def test_learned_manifold_beats_linear_subspace(pda):
+    """What the trained network gains over the method without it, at a
+    reduced size (24 x 24 slip-wall shallow water, 6 training points x 60
+    snapshots, latent 4): the autoencoder trained by the library's tcgen05
+    kernels represents held-out FOM states (decoder(encoder(u))) more closely
+    than the POD subspace of the same dimension built from the same
+    snapshots."""
+    import torch
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("pda_gb300_rom", os.path.join(
+        os.path.dirname(ORACLE), "pressio-demoapps_gb300", "rom.py"))
+    R = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(R)
+    n, k, dt = 24, 4, 0.01
+    setup = R.SweSetup(pda, n)
+    train = R.latin_hypercube(6, seed=3)
+    S = setup.snapshots(train, dt, 60)
+    scale = setup.normalization(S)
+    X = setup.training_data(S, scale)
+    phi = R.pod_basis(S, setup.uref, k)
+    ae = pda.AutoEncoder(setup.N, k, 256, 256, seed=1, stream=setup.stream)
+    R.train_schedule(ae, X, 200, batch=64, lr=2e-3, seed=2)
+    learned = R.LearnedRom(setup, ae, scale)
+    fdec, _ = learned.full_decoder()
+    test = R.uniform_points(2, seed=9)
+    e_ae, e_pod = [], []
+    for p in test:
+        states, _ = setup.fom_trajectory(p, dt, [20, 40, 60])
+        for c in (20, 40, 60):
+            u = states[c]
+            e_ae.append(R.rel_l2(fdec.decode(learned.encode(u)), u, setup.uref))
+            e_pod.append(R.rel_l2(setup.uref + phi @ (phi.T @ (u - setup.uref)), u, setup.uref))
+    assert max(e_ae) < 0.5 and np.mean(e_ae) < 0.7 * np.mean(e_pod), (e_ae, e_pod)
