@@ -258,11 +258,12 @@ class _Ctx:
 
 
 def wl_jacobian_2d(c):
-    """2D Euler Riemann WENO5 Jacobian (V + CSR J), 1024^2"""
+    """2D Euler Riemann WENO5 Jacobian (V + CSR J), 1024^2 (PDA_JAC_N overrides
+    the size for profiling runs)"""
     pda, torch, stream, orc, threads, rng = c.pda, c.torch, c.stream, c.orc, c.threads, c.rng
     cpu = orc is not None
     oracle_problem = c.oracle_problem
-    n = 1024
+    n = int(os.environ.get("PDA_JAC_N", 1024))
     mesh = pda.create_full_mesh((n, n), (0.0, 1.0, 0.0, 1.0), 7)
     prob = pda.create_problem(mesh, pda.Euler2d.Riemann, pda.InviscidFluxReconstruction.Weno5, 2, stream=stream)
     Uh = prob.initialConditionHost() + rng.uniform(-1e-3, 1e-3, 4 * n * n)
@@ -272,7 +273,7 @@ def wl_jacobian_2d(c):
         J = prob.createJacobian()
     ms = _time_gpu(torch, stream, lambda: prob.rightHandSideAndJacobian(U, 0.0, V, J), 5)
     nnz = J.nonZeros()
-    w = {"config": "euler2d_riemann_ic2_weno5_jacobian_1024x1024", "ms_per_call": ms, "nnz": nnz,
+    w = {"config": f"euler2d_riemann_ic2_weno5_jacobian_{n}x{n}", "ms_per_call": ms, "nnz": nnz,
          "value": nnz / (ms * 1e-3) / 1e9, "unit": "Gnnz/s (V + CSR J per call)",
          "gcell_per_s": n * n / (ms * 1e-3) / 1e9}
     del U, V, J, prob
@@ -435,21 +436,24 @@ def _rom_module():
 
 
 def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int(os.environ.get("PDA_ROM_EPOCHS", 60)),
-               batch=128, lr=1e-3, dt=0.005, rom_ratio=4, gn_iters=1):
+               batch=128, lr=1e-3, dt=0.005, rom_ratio=int(os.environ.get("PDA_ROM_RATIO", 4)), gn_iters=1,
+               order=int(os.environ.get("PDA_ROM_ORDER", 2))):
     """Learned-manifold hyper-reduced LSPG on 2D SWE slip wall 256^2: 48
     Latin-hypercube training points (gravity, coriolis, pulse), 400 FOM
     snapshots each (SSP-RK3 dt 0.005, batched device FOM), MLP autoencoder
     latent 12, hidden 256 / 1024, ELU, full-width output, trained on the device
     (BF16 tcgen05 GEMMs, fp32 accumulation, Adam); sample mesh 1 % of the cells
-    (fixed seed) + WENO5 stencils; LSPG BDF1 with Gauss-Newton (FP64 normal
-    equations) on 8 held-out points; wall time and relative L2 error against
-    the single-point GPU FOM, and the same for POD-LSPG with the same latent
-    size (the method without the learned part)."""
+    (fixed seed) + WENO5 stencils; LSPG with BDF2 (first step BDF1) and
+    Gauss-Newton (FP64 normal equations) on 8 held-out points, the FOM as the
+    fallback whenever a stretch's Gauss-Newton residual exceeds a threshold;
+    wall time and relative L2 error against the single-point GPU FOM, and the
+    same for POD-LSPG with the same latent size (the method without the
+    learned part)."""
     R = _rom_module()
     pda, torch = c.pda, c.torch
-    out = {"config": "swe_slipwall_256^2_weno5_learned_lspg_bdf1_latent12", "train_points": n_train,
+    out = {"config": f"swe_slipwall_256^2_weno5_learned_lspg_bdf{order}_latent12", "train_points": n_train,
            "snapshots_per_point": n_snap, "test_points": n_test, "latent": latent, "epochs": epochs,
-           "dt_fom": dt, "dt_rom": dt * rom_ratio, "gn_iters_max": gn_iters,
+           "dt_fom": dt, "dt_rom": dt * rom_ratio, "gn_iters_max": gn_iters, "bdf_order": order,
            "gauss_newton": "residual, normal equations and solve fp64; Jacobian terms fp32 (inexact step)"}
     setup = R.SweSetup(pda, n)
     train = R.latin_hypercube(n_train, seed=5)
@@ -477,21 +481,23 @@ def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int
     fp_aff = setup.problem({"gravity": 9.8, "coriolis": -3.0, "pulseMagnitude": 0.125})
     faff = pda.LspgRom.affine(fp_aff, np.arange(n * n), setup.uref, phi)
     checkpoints = [100, 200, 300, 400]
-    rom_cps = [cp // rom_ratio for cp in checkpoints]
 
-    def run_point(p, rom_kind, gn=gn_iters, ratio=rom_ratio):
+    def make_rom(p, kind):
         ps = setup.problem(p, mesh=sm)
         U0 = setup.problem(p).initialCondition()
-        if rom_kind == "learned":
-            rom, x0, dec = learned.lspg(ps, s2st, st, tensor_cores=True), learned.encode(U0), fdec
-        else:
-            rom, x0, dec = R.affine_lspg(setup, phi, ps, s2st, st), (phi.T @ (U0 - setup.uref)).contiguous(), faff
-        cps = [cp // ratio for cp in checkpoints]
-        lat, wall, maxres = R.run_rom(rom, x0, dt * ratio, cps, setup.stream, gn_iters=gn, tol=1e-8)
-        return lat, wall, maxres, dec
+        if kind == "learned":
+            return learned.lspg(ps, s2st, st, tensor_cores=True), learned.encode(U0), fdec
+        return R.affine_lspg(setup, phi, ps, s2st, st), (phi.T @ (U0 - setup.uref)).contiguous(), faff
 
-    # residual threshold for the FOM fallback: 5x the largest residual seen on a training point
-    _, _, res_train, _ = run_point(train[0], "learned")
+    def run_point(p, kind, threshold, gn=gn_iters, ratio=rom_ratio, ordr=order):
+        rom, x0, dec = make_rom(p, kind)
+        return R.FallbackRun(setup, p, rom, dec, x0, dt, ratio, checkpoints, threshold, gn_iters=gn, order=ordr)
+
+    # residual threshold for the FOM fallback: 5x the largest Gauss-Newton
+    # residual norm seen over a training point's trajectory
+    rom0, x00, _ = make_rom(train[0], "learned")
+    _, _, res_train = R.run_rom(rom0, x00, dt * rom_ratio, [cp // rom_ratio for cp in checkpoints], setup.stream,
+                                gn_iters=gn_iters, order=order)
     threshold = 5.0 * res_train
     out["fallback_residual_threshold"] = threshold
     pts = []
@@ -504,12 +510,11 @@ def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int
         rec["pod_projection_rel_l2"] = [R.rel_l2(setup.uref + phi @ (phi.T @ (states[cp] - setup.uref)), states[cp])
                                         for cp in checkpoints]
         for kind in ("learned", "pod"):
-            lat, wall, maxres, dec = run_point(p, kind)
-            errs = [R.rel_l2(dec.decode(lat[cp // rom_ratio]), states[cp]) for cp in checkpoints]
-            errp = [R.rel_l2(dec.decode(lat[cp // rom_ratio]), states[cp], setup.uref) for cp in checkpoints]
-            rec[kind] = {"rom_s": wall, "speedup": fom_wall / wall, "rel_l2_state": errs,
-                         "rel_l2_perturbation": errp, "max_residual": maxres}
-        rec["learned"]["fallback"] = bool(rec["learned"]["max_residual"] > threshold)
+            run = run_point(p, kind, threshold if kind == "learned" else float("inf"))
+            errs = [R.rel_l2(run.states[cp], states[cp]) for cp in checkpoints]
+            errp = [R.rel_l2(run.states[cp], states[cp], setup.uref) for cp in checkpoints]
+            rec[kind] = {"rom_s": run.wall, "speedup": fom_wall / run.wall, "rel_l2_state": errs,
+                         "rel_l2_perturbation": errp, "fallback_at_step": run.fallback_at}
         pts.append(rec)
     out["points"] = pts
     L = [q["learned"] for q in pts]
@@ -518,32 +523,37 @@ def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int
     out["summary"] = {
         "fom_s_per_point": float(np.mean(fom)),
         "rom_s_per_point": float(np.mean([q["rom_s"] for q in L])),
+        "rom_s_per_point_median": float(np.median([q["rom_s"] for q in L])),
+        "rom_s_points": [float(q["rom_s"]) for q in L],
         "speedup": float(np.sum(fom) / np.sum([q["rom_s"] for q in L])),
+        "speedup_median": float(np.median([q["speedup"] for q in L])),
         "rel_l2_state_final_mean": float(np.mean([q["rel_l2_state"][-1] for q in L])),
         "rel_l2_state_max": float(np.max([max(q["rel_l2_state"]) for q in L])),
         "rel_l2_perturbation_final_mean": float(np.mean([q["rel_l2_perturbation"][-1] for q in L])),
         "pod_rel_l2_state_final_mean": float(np.mean([q["rel_l2_state"][-1] for q in P])),
+        "pod_rel_l2_state_max": float(np.max([max(q["rel_l2_state"]) for q in P])),
         "pod_rel_l2_perturbation_final_mean": float(np.mean([q["rel_l2_perturbation"][-1] for q in P])),
         "pod_speedup": float(np.sum(fom) / np.sum([q["rom_s"] for q in P])),
-        "fallbacks": int(sum(q["fallback"] for q in L)),
+        "fallbacks": int(sum(q["fallback_at_step"] is not None for q in L)),
         "learned_projection_rel_l2_final_mean": float(np.mean([q["learned_projection_rel_l2"][-1] for q in pts])),
         "pod_projection_rel_l2_final_mean": float(np.mean([q["pod_projection_rel_l2"][-1] for q in pts])),
     }
-    # further (Gauss-Newton iterations : ROM step / FOM step) settings of the
-    # same trained network: the speed / accuracy trade-off of BDF1's step size
-    variants = [v for v in os.environ.get("PDA_ROM_VARIANTS", "2:4,1:2,1:1").split(",") if v]
+    # further (order : Gauss-Newton iterations : ROM step / FOM step) settings
+    # of the same trained network: the speed / accuracy trade-off of the step
+    variants = [v for v in os.environ.get("PDA_ROM_VARIANTS", "1:1:4,2:1:8,2:1:2").split(",") if v]
     if variants:
         out["variants"] = {}
         states_by_point = [setup.fom_trajectory(p, dt, checkpoints) for p in test]
         for v in variants:
-            gn, ratio = (int(u) for u in v.split(":"))
+            ordr, gn, ratio = (int(u) for u in v.split(":"))
             walls, fwalls, errs = [], [], []
             for p, (states, fw) in zip(test, states_by_point):
-                lat, wall, _, dec = run_point(p, "learned", gn, ratio)
-                walls.append(wall)
+                run = run_point(p, "learned", float("inf"), gn, ratio, ordr)
+                walls.append(run.wall)
                 fwalls.append(fw)
-                errs.append(max(R.rel_l2(dec.decode(lat[cp // ratio]), states[cp]) for cp in checkpoints))
-            out["variants"][v] = {"gn_iters": gn, "dt_rom": dt * ratio, "speedup": float(sum(fwalls) / sum(walls)),
+                errs.append(max(R.rel_l2(run.states[cp], states[cp]) for cp in checkpoints))
+            out["variants"][v] = {"bdf_order": ordr, "gn_iters": gn, "dt_rom": dt * ratio,
+                                  "speedup": float(sum(fwalls) / sum(walls)),
                                   "rel_l2_state_max": float(max(errs)), "rel_l2_state_mean_of_max": float(np.mean(errs))}
     if c.orc is not None:
         # the FOM on the host cores (oracle), one point, a bounded number of steps
