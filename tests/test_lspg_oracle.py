@@ -90,3 +90,30 @@ def test_lspg_oracle_bdf2_steps_are_least_squares_minimisers(pda, oracle):
         assert np.linalg.norm(JR.T @ R) <= 1e-9 * np.linalg.norm(JR) * max(np.linalg.norm(R), 1e-300)
         ref = least_squares(resid, traj[n - 1], jac=jac, method="lm", xtol=1e-15, ftol=1e-15, gtol=1e-15)
         assert np.allclose(xs, ref.x, rtol=1e-8, atol=1e-11)
+
+
+LSPG_GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "lspg")
+
+
+def _lspg_gold_cases():
+    return sorted(f[:-4] for f in os.listdir(LSPG_GOLD) if f.endswith(".npz"))
+
+
+@pytest.mark.parametrize("name", _lspg_gold_cases())
+def test_lspg_oracle_matches_pressio_golds(oracle, name):
+    """The oracle's latent trajectories equal those of the reference's own
+    hyper-reduced LSPG (vendored Pressio over the reference's slip-wall
+    shallow-water problem on a reference-made sample mesh;
+    tests/golden/make_lspg_golden.py), BDF1 and BDF2, with the same number of
+    Gauss-Newton updates per step, to 1e-9 relative (the normal equations are
+    solved by Householder QR there, by LU here)."""
+    g = dict(np.load(os.path.join(LSPG_GOLD, name + ".npz")))
+    gr, co, pu = (float(v) for v in g["params"])
+    om = oracle.mesh_load(os.path.join(os.path.dirname(LSPG_GOLD), "meshes", "s2d_s7_20"))
+    po = oracle.problem(om, 3, 0, 2, 1, {"gravity": gr, "coriolis": co, "pulseMagnitude": pu})
+    dec = lspg_oracle.affine_decoder(g["uref"], g["phi"])
+    _, traj = lspg_oracle.lspg_bdf(po, g["s2st"], dec, g["x0"], float(g["dt"]), int(g["steps"]), order=int(g["order"]),
+                                   iters=int(g["updates"]), tol=0.0)
+    traj = np.array(traj)
+    scale = np.max(np.abs(g["traj"]))
+    assert np.allclose(traj, g["traj"], rtol=1e-9, atol=1e-11 * scale), np.max(np.abs(traj - g["traj"])) / scale
