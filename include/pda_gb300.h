@@ -186,8 +186,8 @@ pda_status pda_velocity_host(pda_problem *p, const double *h_U, double t, double
 
 /* Allocation-free variant of pda_velocity (no counterpart in the reference).
  * For callers that may not allocate device memory while evaluating the
- * right-hand side: code inside a stream capture it owns, fixed-budget
- * real-time loops, hosts whose pool allocator forbids library allocations.
+ * right-hand side: fixed-budget real-time loops whose memory is set aside at
+ * start-up, hosts whose pool allocator forbids library allocations.
  * pda_velocity allocates its face-flux buffers on a problem's first call;
  * this entry point puts them in one static device array of
  * PDA_NOALLOC_SCRATCH_DOUBLES doubles (32 MiB) inside the library instead
@@ -201,7 +201,9 @@ pda_status pda_velocity_host(pda_problem *p, const double *h_U, double t, double
  *    then PDA_ERR_UNSUPPORTED.
  *  - The first call on each device looks up the array's device address
  *    (this may load the module that holds it); make that first call before
- *    any stream capture or allocation-free section begins.
+ *    any stream capture or allocation-free section begins.  The address is
+ *    kept per device for the process; like every problem handle it does not
+ *    survive cudaDeviceReset.
  *  - Nothing in the array needs to start at zero.  The array is shared by all
  *    problems of the process on a device: calls that overlap in time (other
  *    streams or threads without ordering between them) race on it. */
@@ -294,7 +296,10 @@ int64_t pda_batch_launch_count(const pda_batch *b);
  * 2 bias + ELU), A and B row-major bf16 (uint16 storage), K a multiple of 64.
  * Outputs (any may be NULL, not both of d_outF / d_outB): fp32 and / or bf16
  * row-major [M x N], d_preact = fp32 value before the activation.
- * Synchronous on `stream` (cudaStream_t, NULL = legacy default). */
+ * Synchronous on `stream` (cudaStream_t, NULL = legacy default).  Shapes
+ * with N <= 16 take the thin blocked kernel and allocate scratch for both
+ * operands' blocked copies and the split partial sums on every call (the
+ * reduced-order model's decoder keeps its operands pre-blocked instead). */
 pda_status pda_tc_gemm_bf16(const void *d_A, const void *d_B, int64_t M, int64_t N, int64_t K,
                             const float *d_bias, int epilogue, float *d_outF, void *d_outB,
                             float *d_preact, void *stream);

@@ -95,12 +95,17 @@ cudaError_t tc_block_operand(const __nv_bfloat16 *W, long M, long K, int rowsPer
 cudaError_t tc_gemm_thin_blocked(const __nv_bfloat16 *Ablk, const __nv_bfloat16 *Bblk, long M, long K, int splits,
                                  float *partial, cudaStream_t s) {
   constexpr int ST = tc::THIN_STAGES;
-  static bool attr = false;
-  if (!attr) {
+  // the larger dynamic shared memory is a per-device function attribute
+  constexpr int kMaxDev = 64;
+  static bool attr[kMaxDev] = {};
+  int dev = 0;
+  cudaError_t ed = cudaGetDevice(&dev);
+  if (ed != cudaSuccess) return ed;
+  if (dev < 0 || dev >= kMaxDev || !attr[dev]) {
     cudaError_t e = cudaFuncSetAttribute(tc::k_gemm_thin_blocked<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          tc::blocked_smem_bytes(ST));
     if (e != cudaSuccess) return e;
-    attr = true;
+    if (dev >= 0 && dev < kMaxDev) attr[dev] = true;
   }
   int *err = nullptr;
   cudaError_t e = cudaGetSymbolAddress((void **)&err, g_tc_err);

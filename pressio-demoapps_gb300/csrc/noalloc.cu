@@ -2,11 +2,9 @@
 // allocation-free velocity entry point (pda_velocity_noalloc).
 //
 // Who needs it: callers that may not allocate device memory while they
-// evaluate the right-hand side -- code running between the capture calls of
-// a CUDA stream capture they own (cudaMalloc is not a capturable operation),
-// real-time or embedded loops whose memory budget is fixed at start-up, and
-// hosts with their own pool allocators that forbid a library allocating
-// behind their back.  The regular entry point allocates its face buffers on
+// evaluate the right-hand side -- real-time or embedded loops whose memory
+// budget is fixed at start-up, and hosts with their own pool allocators that
+// forbid a library allocating behind their back.  The regular entry point allocates its face buffers on
 // the first call of each problem (and grows them on demand), which none of
 // those callers can accept.
 //
@@ -34,7 +32,9 @@ double *g_addr[kMaxCachedDevices] = {};
 
 // Device address of the scratch array on the current device.  The symbol is
 // looked up once per device (this first lookup may load the module that
-// holds the array) and cached afterwards.
+// holds the array) and cached for the process: like every problem handle,
+// the cached address does not survive cudaDeviceReset.  Devices beyond the
+// cache's 64 entries look the symbol up on every call (it allocates nothing).
 cudaError_t noalloc_face_scratch(double **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
