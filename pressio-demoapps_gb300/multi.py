@@ -23,6 +23,30 @@ def shard_by_cost(costs, world):
     return [sorted(s) for s in shards]
 
 
+def gather_instances(mine, arrays, n_instances):
+    """Reassemble per-instance results computed on the ranks: rank r passes
+    its shard `mine` (instance indices) and the matching host arrays; every
+    rank receives the list of all n_instances arrays in global instance
+    order.  Each instance must be owned by exactly one rank."""
+    import torch.distributed as dist
+    local = list(zip((int(i) for i in mine), arrays))
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        parts = [None] * dist.get_world_size()
+        dist.all_gather_object(parts, local)
+    else:
+        parts = [local]
+    out = [None] * n_instances
+    for part in parts:
+        for i, a in part:
+            if out[i] is not None:
+                raise ValueError(f"instance {i} owned by more than one rank")
+            out[i] = a
+    missing = [i for i, a in enumerate(out) if a is None]
+    if missing:
+        raise ValueError(f"instances without an owner: {missing[:8]}")
+    return out
+
+
 def max_over_ranks(value, device=None):
     """The largest value over all ranks (a step's time is the slowest rank's)."""
     import torch
