@@ -191,7 +191,7 @@ __device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &
 
 // grid: x = line groups of NR lines, y = face chunks of TW faces
 template <int FAM, int SCHEME, int AXIS, int NR, int LANES = 64>
-__global__ void __launch_bounds__(LANES *NR, 8)
+__global__ void __launch_bounds__(LANES *NR)
 k_faces_tile(Box b, Phys p, const double *__restrict__ U, double *__restrict__ Fout) {
   __shared__ FaceTileSmem<FAM, SCHEME, NR, LANES> sm;
   face_tile<FAM, SCHEME, AXIS, NR, LANES>(sm, b, p, U, Fout, (long)blockIdx.x, (int)blockIdx.y);
