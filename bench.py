@@ -616,12 +616,40 @@ def wl_lspg_step(c, n=256, latent=12, steps=20, gn_iters=3):
     return out
 
 
+def wl_ae_step(c, n=3 * 256 * 256, latent=12, ha=1024, hb=256, batch=128, steps=24):
+    """One Adam step of the ROM's autoencoder (n = 196,608 outputs = 256^2
+    shallow-water cells x 3, latent 12, hidden 1024 / 256, batch 128) on seeded
+    random bf16 rows: forward and backward tcgen05 GEMMs, ELU, MSE, Adam.  Time
+    per step next to the HBM floor of the Adam pass (fp32 weight, m, v and
+    gradient read, weight, m and v written, bf16 copy written: 30 B per
+    parameter)."""
+    pda, torch = c.pda, c.torch
+    g = torch.Generator(device="cuda").manual_seed(0)
+    X = (torch.rand(batch * steps, n, generator=g, device="cuda") * 2 - 1).to(torch.bfloat16)
+    ae = pda.AutoEncoder(n, latent, ha, hb, seed=1, stream=c.stream)
+    ae.train(X[: batch * 4], batch=batch, epochs=1, lr=1e-3, seed=0)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ae.train(X, batch=batch, epochs=1, lr=1e-3, seed=1)
+    torch.cuda.synchronize()
+    ms = 1e3 * (time.perf_counter() - t0) / steps
+    params = sum(i * o + o for i, o in zip((n, ha, hb, latent, hb, ha), (ha, hb, latent, hb, ha, n)))
+    hbm, src = measured_peaks()
+    floor_ms = params * 30 / (hbm * 1e9) * 1e3
+    out = {"config": "autoencoder_adam_step_n196608_latent12_hidden1024_256_batch128", "ms_per_step": ms,
+           "parameters": params, "adam_bytes_per_step": params * 30, "adam_hbm_floor_ms": floor_ms,
+           "adam_floor_fraction_of_step": floor_ms / ms, "peak_source": src,
+           "note": "host clock around whole epochs of the library's training loop (one loss read back per call)"}
+    del X, ae
+    return out
+
+
 # workloads whose work is split over the ranks (every rank must run them)
 SHARDED = {"batched_swe"}
 
 WORKLOADS = {"jacobian_2d": wl_jacobian_2d, "velocity_3d": wl_velocity_3d, "jacobian_3d": wl_jacobian_3d,
              "sod_1d_ssprk3": wl_sod_1d_ssprk3, "ssprk3_3d": wl_ssprk3_3d, "batched_swe": wl_batched_swe,
-             "rom_swe": wl_rom_swe, "lspg_step": wl_lspg_step}
+             "rom_swe": wl_rom_swe, "lspg_step": wl_lspg_step, "ae_step": wl_ae_step}
 
 
 def extra_workloads(pda, torch, stream, cpu=True, names=None):
