@@ -482,15 +482,16 @@ def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int
     faff = pda.LspgRom.affine(fp_aff, np.arange(n * n), setup.uref, phi)
     checkpoints = [100, 200, 300, 400]
 
-    def make_rom(p, kind):
-        ps = setup.problem(p, mesh=sm)
+    def make_rom(p, kind, sample=(sm, st, s2st)):
+        smesh, stc, s2 = sample
+        ps = setup.problem(p, mesh=smesh)
         U0 = setup.problem(p).initialCondition()
         if kind == "learned":
-            return learned.lspg(ps, s2st, st, tensor_cores=True), learned.encode(U0), fdec
-        return R.affine_lspg(setup, phi, ps, s2st, st), (phi.T @ (U0 - setup.uref)).contiguous(), faff
+            return learned.lspg(ps, s2, stc, tensor_cores=True), learned.encode(U0), fdec
+        return R.affine_lspg(setup, phi, ps, s2, stc), (phi.T @ (U0 - setup.uref)).contiguous(), faff
 
-    def run_point(p, kind, threshold, gn=gn_iters, ratio=rom_ratio, ordr=order):
-        rom, x0, dec = make_rom(p, kind)
+    def run_point(p, kind, threshold, gn=gn_iters, ratio=rom_ratio, ordr=order, sample=(sm, st, s2st)):
+        rom, x0, dec = make_rom(p, kind, sample)
         return R.FallbackRun(setup, p, rom, dec, x0, dt, ratio, checkpoints, threshold, gn_iters=gn, order=ordr)
 
     # residual threshold for the FOM fallback: 5x the largest Gauss-Newton
@@ -538,21 +539,30 @@ def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int
         "learned_projection_rel_l2_final_mean": float(np.mean([q["learned_projection_rel_l2"][-1] for q in pts])),
         "pod_projection_rel_l2_final_mean": float(np.mean([q["pod_projection_rel_l2"][-1] for q in pts])),
     }
-    # further (order : Gauss-Newton iterations : ROM step / FOM step) settings
-    # of the same trained network: the speed / accuracy trade-off of the step
-    variants = [v for v in os.environ.get("PDA_ROM_VARIANTS", "1:1:4,2:1:8,2:1:2").split(",") if v]
+    # further (order : Gauss-Newton iterations : ROM step / FOM step [: sample
+    # fraction]) settings of the same trained network: the speed / accuracy
+    # trade-off of the step and of the sample mesh
+    variants = [v for v in os.environ.get("PDA_ROM_VARIANTS", "1:1:4,2:1:8,2:1:2,2:1:4:0.03").split(",") if v]
     if variants:
         out["variants"] = {}
         states_by_point = [setup.fom_trajectory(p, dt, checkpoints) for p in test]
         for v in variants:
-            ordr, gn, ratio = (int(u) for u in v.split(":"))
+            f = v.split(":")
+            ordr, gn, ratio = (int(u) for u in f[:3])
+            frac = float(f[3]) if len(f) > 3 else 0.01
+            if frac != 0.01:
+                sm_v, gids_v, st_v, s2st_v = setup.sample_mesh(frac, seed=7)
+                sample = (sm_v, st_v, s2st_v)
+            else:
+                sample = (sm, st, s2st)
             walls, fwalls, errs = [], [], []
             for p, (states, fw) in zip(test, states_by_point):
-                run = run_point(p, "learned", float("inf"), gn, ratio, ordr)
+                run = run_point(p, "learned", float("inf"), gn, ratio, ordr, sample)
                 walls.append(run.wall)
                 fwalls.append(fw)
                 errs.append(max(R.rel_l2(run.states[cp], states[cp]) for cp in checkpoints))
-            out["variants"][v] = {"bdf_order": ordr, "gn_iters": gn, "dt_rom": dt * ratio,
+            out["variants"][v] = {"bdf_order": ordr, "gn_iters": gn, "dt_rom": dt * ratio, "sample_fraction": frac,
+                                  "sample_cells": int(len(sample[2])),
                                   "speedup": float(sum(fwalls) / sum(walls)),
                                   "rel_l2_state_max": float(max(errs)), "rel_l2_state_mean_of_max": float(np.mean(errs))}
     if c.orc is not None:
@@ -619,28 +629,38 @@ def wl_lspg_step(c, n=256, latent=12, steps=20, gn_iters=3):
 def wl_ae_step(c, n=3 * 256 * 256, latent=12, ha=1024, hb=256, batch=128, steps=24):
     """One Adam step of the ROM's autoencoder (n = 196,608 outputs = 256^2
     shallow-water cells x 3, latent 12, hidden 1024 / 256, batch 128) on seeded
-    random bf16 rows: forward and backward tcgen05 GEMMs, ELU, MSE, Adam.  Time
-    per step next to the HBM floor of the Adam pass (fp32 weight, m, v and
-    gradient read, weight, m and v written, bf16 copy written: 30 B per
-    parameter)."""
+    random bf16 rows: forward and backward tcgen05 GEMMs, ELU, squared error,
+    Adam; with Adam fused into the weight-gradient GEMMs (the library's
+    default) and as a separate pass.  HBM floor of a step: every weight once
+    through the schedule -- bf16 copy read by the forward GEMM (2 B), fp32
+    weight and moments read and written (24 B), bf16 copy written (2 B), and
+    for the layers whose input gradient is needed the bf16 transpose read and
+    written (4 B): 28 or 32 B per weight."""
     pda, torch = c.pda, c.torch
+    n = int(os.environ.get("PDA_AE_N", n))  # smaller outputs for profiling captures
+    steps = int(os.environ.get("PDA_AE_STEPS", steps))
     g = torch.Generator(device="cuda").manual_seed(0)
     X = (torch.rand(batch * steps, n, generator=g, device="cuda") * 2 - 1).to(torch.bfloat16)
-    ae = pda.AutoEncoder(n, latent, ha, hb, seed=1, stream=c.stream)
-    ae.train(X[: batch * 4], batch=batch, epochs=1, lr=1e-3, seed=0)  # warm-up
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    ae.train(X, batch=batch, epochs=1, lr=1e-3, seed=1)
-    torch.cuda.synchronize()
-    ms = 1e3 * (time.perf_counter() - t0) / steps
-    params = sum(i * o + o for i, o in zip((n, ha, hb, latent, hb, ha), (ha, hb, latent, hb, ha, n)))
+    shapes = list(zip((n, ha, hb, latent, hb, ha), (ha, hb, latent, hb, ha, n)))
+    params = sum(i * o + o for i, o in shapes)
+    floor_bytes = sum(i * o * (28 if l == 0 else 32) for l, (i, o) in enumerate(shapes))
     hbm, src = measured_peaks()
-    floor_ms = params * 30 / (hbm * 1e9) * 1e3
-    out = {"config": "autoencoder_adam_step_n196608_latent12_hidden1024_256_batch128", "ms_per_step": ms,
-           "parameters": params, "adam_bytes_per_step": params * 30, "adam_hbm_floor_ms": floor_ms,
-           "adam_floor_fraction_of_step": floor_ms / ms, "peak_source": src,
-           "note": "host clock around whole epochs of the library's training loop (one loss read back per call)"}
-    del X, ae
+    floor_ms = floor_bytes / (hbm * 1e9) * 1e3
+    out = {"config": f"autoencoder_adam_step_n{n}_latent12_hidden1024_256_batch128", "parameters": params,
+           "hbm_floor_bytes_per_step": floor_bytes, "hbm_floor_ms": floor_ms, "peak_source": src,
+           "note": "host clock around whole epochs of the library's training loop (one loss read back per step)"}
+    for fused in (True, False):
+        ae = pda.AutoEncoder(n, latent, ha, hb, seed=1, stream=c.stream)
+        ae.set_fused(fused)
+        ae.train(X[: batch * 4], batch=batch, epochs=1, lr=1e-3, seed=0)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ae.train(X, batch=batch, epochs=1, lr=1e-3, seed=1)
+        torch.cuda.synchronize()
+        ms = 1e3 * (time.perf_counter() - t0) / steps
+        out["fused_adam" if fused else "separate_adam"] = {"ms_per_step": ms, "hbm_floor_fraction": floor_ms / ms}
+        del ae
+    del X
     return out
 
 

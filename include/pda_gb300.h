@@ -318,6 +318,11 @@ void pda_ae_free(pda_ae *ae);
  * batch loss (may be NULL); batch a multiple of 64 */
 pda_status pda_ae_train(pda_ae *ae, const void *d_data, int64_t ns, int batch, int epochs, double lr,
                         uint64_t seed, double *losses);
+/* fused = 1 (default): each Adam step runs inside the epilogues of the
+ * weight-gradient GEMMs, so the fp32 weight gradients are never stored;
+ * fused = 0: gradients are stored, then a separate optimizer pass.  Both give
+ * the same weights bit for bit. */
+pda_status pda_ae_set_fused(pda_ae *ae, int fused);
 /* Y = decoder(encoder(X)) (fp32 [rows x n]); Z (may be NULL) = latent [rows x latent] */
 pda_status pda_ae_reconstruct(pda_ae *ae, const void *d_X, int64_t rows, float *d_Y, float *d_Z);
 /* loss and all parameter gradients of one batch, no update (gradient checks);

@@ -142,6 +142,7 @@ _SIGS = {
     "pda_ae_free": (None, [C.c_void_p]),
     "pda_ae_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_double, C.c_uint64,
                                C.c_void_p]),
+    "pda_ae_set_fused": (C.c_int, [C.c_void_p, C.c_int]),
     "pda_ae_reconstruct": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "pda_ae_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_void_p]),
     "pda_ae_layer": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -723,6 +724,11 @@ class AutoEncoder:
         _check(lib().pda_ae_train(self._h, _vp(data), data.shape[0], int(batch), int(epochs), float(lr), int(seed),
                                   losses.ctypes.data_as(C.c_void_p)))
         return losses[:epochs]
+
+    def set_fused(self, fused=True):
+        """Adam inside the weight-gradient GEMM epilogues (default) or as a
+        separate pass over stored gradients; the weights agree bit for bit."""
+        _check(lib().pda_ae_set_fused(self._h, 1 if fused else 0))
 
     def reconstruct(self, X):
         import torch

@@ -4,7 +4,10 @@ Every translation unit is compiled by nvcc in parallel, then linked into
 ``pressio-demoapps_gb300/lib/libpda_gb300.so`` (in-tree).  Floating-point
 contraction is disabled on device (``-fmad=false``) and host
 (``-ffp-contract=off``) so that results reproduce the reference's
-double-precision operation order bit for bit.
+double-precision operation order bit for bit.  The reduced-order-model units
+(LSPG, GEMM launchers, autoencoder) owe the reference no bitwise parity and
+are built with contraction on (``-fmad=true``); their tests bound them by
+tolerances.
 
 Usage: ``python pressio-demoapps_gb300/build_lib.py [--force] [--ptxas-verbose]``
 """
@@ -52,8 +55,13 @@ def lib_path() -> str:
     return os.path.join(LIBDIR, LIBNAME)
 
 
-def _flags(ptxas_verbose: bool) -> list[str]:
-    f = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "--expt-relaxed-constexpr",
+# translation units without a bitwise-parity obligation: FMA contraction on
+CONTRACTED = {"rom.cu", "mlp.cu", "ae.cu"}
+
+
+def _flags(ptxas_verbose: bool, src: str = "") -> list[str]:
+    fmad = "-fmad=true" if src in CONTRACTED else "-fmad=false"
+    f = ["-O3", "-std=c++17", "-lineinfo", fmad, "--expt-relaxed-constexpr",
          "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I" + CSRC]
     if ptxas_verbose:
         f += ["-Xptxas", "-v"]
@@ -73,7 +81,6 @@ def build(force: bool = False, ptxas_verbose: bool = False, jobs: int | None = N
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".hpp", ".h"))]
     headers.append(os.path.join(os.path.dirname(HERE), "include", "pda_gb300.h"))
     cc = nvcc()
-    flags = _flags(ptxas_verbose)
     objs = []
     cmds = []
     for src in SOURCES:
@@ -81,7 +88,7 @@ def build(force: bool = False, ptxas_verbose: bool = False, jobs: int | None = N
         obj = os.path.join(BUILDDIR, src + ".o")
         objs.append(obj)
         if force or _needs_build(obj, [sp] + headers):
-            cmds.append([cc, *flags, "-c", sp, "-o", obj])
+            cmds.append([cc, *_flags(ptxas_verbose, src), "-c", sp, "-o", obj])
 
     def run(cmd):
         p = subprocess.run(cmd, capture_output=True, text=True)

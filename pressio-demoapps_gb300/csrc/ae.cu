@@ -9,6 +9,12 @@
 // in bf16 for the next GEMM and in fp32 before the activation for the
 // backward pass.  Loss: mean squared reconstruction error.
 //
+// One training step is a single pass over the weights: the output layer's
+// GEMM epilogue forms the error gradient (and its transpose) without storing
+// the reconstruction, and each weight-gradient GEMM's epilogue applies Adam
+// to its tile and writes the refreshed bf16 copies, so the fp32 gradients of
+// the weights never reach memory.
+//
 // Every product of the forward and backward pass is C = A B^T with both
 // operands K-major:
 //   forward   H_l   = act(H_{l-1} W_l^T + b_l)
@@ -85,25 +91,6 @@ __global__ void k_gather_rows(const bf16 *__restrict__ data, const int64_t *__re
   reinterpret_cast<uint4 *>(X + r * n)[c] = reinterpret_cast<const uint4 *>(data + idx[r] * n)[c];
 }
 
-// dY = 2 (Y - X) / (rows n), bf16; per-block partial sums of (Y - X)^2
-__global__ void k_mse(const float *__restrict__ Y, const bf16 *__restrict__ X, long total, float gscale,
-                      bf16 *__restrict__ dY, double *__restrict__ partial) {
-  __shared__ double red[256];
-  double acc = 0.;
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-    const float d = Y[i] - __bfloat162float(X[i]);
-    acc += (double)d * d;
-    dY[i] = __float2bfloat16_rn(gscale * d);
-  }
-  red[threadIdx.x] = acc;
-  __syncthreads();
-  for (int o = 128; o > 0; o >>= 1) {
-    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
-}
-
 // dA = dH * elu'(pre) -> bf16 (pre is the value before the ELU)
 __global__ void k_elu_back(const float *__restrict__ dH, const float *__restrict__ pre, bf16 *__restrict__ dA,
                            long n) {
@@ -113,33 +100,55 @@ __global__ void k_elu_back(const float *__restrict__ dH, const float *__restrict
   dA[i] = __float2bfloat16_rn(dH[i] * (a > 0.f ? 1.f : expf(a)));
 }
 
-// column sums of a bf16 [rows x cols] matrix (bias gradients), fixed order
-__global__ void k_colsum(const bf16 *__restrict__ d, long rows, long cols, float *__restrict__ out) {
+// column sums of a bf16 [rows x cols] matrix (bias gradients), fixed order;
+// with `b` given, also the Adam update of the bias b (moments mb, vb) on the
+// first `realCols` entries
+__global__ void k_colsum(const bf16 *__restrict__ d, long rows, long cols, float *__restrict__ out,
+                         float *__restrict__ b, float *__restrict__ mb, float *__restrict__ vb, long realCols,
+                         AdamCoef coef) {
   const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= cols) return;
   float s = 0.f;
   for (long r = 0; r < rows; ++r) s += __bfloat162float(d[r * cols + c]);
   out[c] = s;
+  if (b && c < realCols) b[c] = adam_update(b[c], mb[c], vb[c], s, coef);
 }
 
-// Adam (Kingma & Ba): m = b1 m + (1 - b1) g, v = b2 v + (1 - b2) g^2,
-// w -= lr * (m / (1 - b1^t)) / (sqrt(v / (1 - b2^t)) + eps); bf16 copy of w.
-// Entries outside the first `cols` columns of each row (latent padding) stay 0.
+// row sums of a bf16 [rows x cols] matrix, one warp per row (lane l adds
+// columns l, l + 32, ... in order, then a fixed butterfly over the lanes):
+// the bias gradient from a transposed error gradient; Adam on b as in
+// k_colsum.  Launch rows * 32 threads.
+__global__ void k_rowsum(const bf16 *__restrict__ d, long rows, long cols, float *__restrict__ out,
+                         float *__restrict__ b, float *__restrict__ mb, float *__restrict__ vb, long realRows,
+                         AdamCoef coef) {
+  const long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= rows) return;  // whole warps
+  float s = 0.f;
+  for (long c = lane; c < cols; c += 32) s += __bfloat162float(d[r * cols + c]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    out[r] = s;
+    if (b && r < realRows) b[r] = adam_update(b[r], mb[r], vb[r], s, coef);
+  }
+}
+
+// Adam on a [n / ld x ld] parameter block with gradient g, refreshing the
+// bf16 copy wb when given; entries outside the first `cols` columns of each
+// row (latent padding) stay 0.
 __global__ void k_adam(float *__restrict__ w, float *__restrict__ m, float *__restrict__ v,
-                       const float *__restrict__ g, bf16 *__restrict__ wb, long n, long ld, long cols, float lr,
-                       float b1, float b2, float c1, float c2, float eps) {
+                       const float *__restrict__ g, bf16 *__restrict__ wb, long n, long ld, long cols, AdamCoef coef) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   if (i % ld >= cols) {
     if (wb) wb[i] = __float2bfloat16_rn(0.f);
     return;
   }
-  const float gi = g[i];
-  const float mi = b1 * m[i] + (1.f - b1) * gi;
-  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  float mi = m[i], vi = v[i];
+  const float wi = adam_update(w[i], mi, vi, g[i], coef);
   m[i] = mi;
   v[i] = vi;
-  const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
   w[i] = wi;
   if (wb) wb[i] = __float2bfloat16_rn(wi);
 }
@@ -170,8 +179,12 @@ struct Layer {
   long inReal = 0, outReal = 0;
   bool elu = false;
   Buf<float> W, b, mW, vW, mb, vb, gW, gb;
-  Buf<bf16> Wb, WbT;  // [out x in], [in x out]
+  Buf<bf16> Wb, WbT;  // [out x in], [in x out]: row-major, or blocked operands
   bool needT = false;
+  // the wide layers (first and last) keep their bf16 copies in the blocked
+  // operand layout for the bulk-copy GEMM (their forward and input-gradient
+  // products have K = n or N = n)
+  bool blk = false;
 };
 
 }  // namespace ae
@@ -184,13 +197,19 @@ struct pda_ae {
   pda::ae::Layer L[6];
   int batch = 0;
   // activations for one batch
-  pda::ae::Buf<pda::ae::bf16> X, XT, Hb[6], HbT[6], dA, dAT, dYb;
+  pda::ae::Buf<pda::ae::bf16> X, XT, Hb[6], HbT[6], dA, dAT;
+  // blocked operands of the wide layers' GEMMs: the batch, layer 4's output,
+  // the output error gradient (rows padded to 128 and zero)
+  pda::ae::Buf<pda::ae::bf16> Xblk, H4blk, dYblk;
   pda::ae::Buf<float> pre[6], Y, dH;
   pda::ae::Buf<float> work;
   pda::ae::Buf<double> lossPart;
   pda::ae::Buf<int64_t> idx;
   long workFloats = 0;
   int64_t step = 0;
+  // Adam fused into the weight-gradient GEMMs' epilogues (false: the
+  // gradients are stored and a separate optimizer pass follows)
+  bool fusedAdam = true;
 };
 
 namespace pda {
@@ -209,8 +228,20 @@ void transpose(const bf16 *in, bf16 *out, long R, long C, cudaStream_t s) {
 }
 
 void refresh_bf16(Layer &l, cudaStream_t s) {
+  if (l.blk) {
+    check(tc_to_bf16_blocked(l.W.p, l.out, l.in, 0, l.Wb.p, s), "bf16 blocked copy");
+    if (l.needT) check(tc_to_bf16_blocked(l.W.p, l.out, l.in, 1, l.WbT.p, s), "bf16 blocked transpose");
+    return;
+  }
   k_to_bf16<<<g1(l.out * l.in), 256, 0, s>>>(l.W.p, l.Wb.p, l.out * l.in);
   if (l.needT) transpose(l.Wb.p, l.WbT.p, l.out, l.in, s);
+}
+
+inline long pad128(long r) { return (r + 127) / 128 * 128; }
+
+void alloc_zero(Buf<bf16> &b, size_t n, cudaStream_t s) {
+  b.alloc(n);
+  check(cudaMemsetAsync(b.p, 0, n * sizeof(bf16), s), "memset");
 }
 
 void ensure_batch(pda_ae &A, int B) {
@@ -225,7 +256,9 @@ void ensure_batch(pda_ae &A, int B) {
     A.pre[l].alloc((size_t)B * A.L[l].out);
   }
   A.Y.alloc((size_t)B * n);
-  A.dYb.alloc((size_t)B * n);
+  alloc_zero(A.Xblk, (size_t)pad128(B) * n, A.s);
+  alloc_zero(A.H4blk, (size_t)pad128(B) * A.L[4].out, A.s);
+  alloc_zero(A.dYblk, (size_t)pad128(B) * n, A.s);
   long maxOut = 0;
   for (auto &l : A.L) maxOut = std::max(maxOut, std::max(l.out, l.in));
   A.dA.alloc((size_t)B * std::max(maxOut, n));
@@ -233,7 +266,7 @@ void ensure_batch(pda_ae &A, int B) {
   A.dH.alloc((size_t)B * maxOut);
   A.workFloats = 64L * B * std::max<long>(A.ha, 1024);
   A.work.alloc((size_t)A.workFloats);
-  A.lossPart.alloc(1024);
+  A.lossPart.alloc((size_t)std::max<long>(1024, ((n + 127) / 128) * ((B + 127) / 128)));
   A.idx.alloc((size_t)B);
 }
 
@@ -242,13 +275,41 @@ void gemm(pda_ae &A, const bf16 *a, const bf16 *b, long M, long N, long K, const
   check(tc_gemm_splitk(a, b, M, N, K, bias, epi, outF, outB, pre, A.work.p, A.workFloats, A.s), "tc gemm");
 }
 
-// forward of a batch already in A.X; returns nothing, fills Hb/pre/Y
-void forward(pda_ae &A, int B) {
+// forward of a batch already in A.X: fills Hb / pre; the output layer either
+// writes Y (train = false) or, in training, the reconstruction error's
+// gradient dY (blocked in A.dYblk, and its transpose in A.dAT) and per-CTA
+// sums of squares (A.lossPart, `parts` of them) without storing Y
+void forward(pda_ae &A, int B, bool train, long *parts = nullptr) {
   const bf16 *in = A.X.p;
   for (int l = 0; l < 6; ++l) {
     Layer &ly = A.L[l];
-    if (l == 5) {
-      gemm(A, in, ly.Wb.p, B, ly.out, ly.in, ly.b.p, tc::EPI_BIAS, A.Y.p, nullptr, nullptr);
+    if (l == 0) {
+      // K = n: both operands blocked, K split over the SMs
+      check(tc_block_operand(A.X.p, B, A.n, 128, A.Xblk.p, A.s), "block X");
+      check(tc_gemm_blocked(A.Xblk.p, ly.Wb.p, B, ly.out, ly.in, ly.b.p, tc::EPI_BIAS_ELU, nullptr, A.Hb[0].p,
+                            A.pre[0].p, nullptr, A.work.p, A.workFloats, A.s),
+            "tc gemm (first layer)");
+      in = A.Hb[0].p;
+    } else if (l == 5) {
+      // N = n: layer 4's output blocked against the blocked weights
+      check(tc_block_operand(in, B, ly.in, 128, A.H4blk.p, A.s), "block H4");
+      if (train) {
+        tc::MseEpi me;
+        me.X = A.X.p;
+        me.dY = A.dYblk.p;
+        me.blocked = true;
+        me.dYT = A.dAT.p;
+        me.gscale = 2.f / (float)((long)B * A.n);
+        me.partial = A.lossPart.p;
+        check(tc_gemm_blocked(A.H4blk.p, ly.Wb.p, B, ly.out, ly.in, ly.b.p, tc::EPI_BIAS, nullptr, nullptr, nullptr,
+                              &me, nullptr, 0, A.s),
+              "tc gemm (output layer, squared error)");
+        if (parts) *parts = ((ly.out + 127) / 128) * ((B + 127) / 128);  // one per 128 x 128 output tile
+      } else {
+        check(tc_gemm_blocked(A.H4blk.p, ly.Wb.p, B, ly.out, ly.in, ly.b.p, tc::EPI_BIAS, A.Y.p, nullptr, nullptr,
+                              nullptr, nullptr, 0, A.s),
+              "tc gemm (output layer)");
+      }
     } else {
       gemm(A, in, ly.Wb.p, B, ly.out, ly.in, ly.b.p, ly.elu ? tc::EPI_BIAS_ELU : tc::EPI_BIAS, nullptr, A.Hb[l].p,
            A.pre[l].p);
@@ -257,60 +318,84 @@ void forward(pda_ae &A, int B) {
   }
 }
 
+
 // gradients of the mean squared error of the batch in A.X; returns the loss
-// (sum of squares / (B n)) on the host
-double backward(pda_ae &A, int B) {
-  const long n = A.n;
-  const long total = (long)B * n;
-  const float gscale = 2.f / (float)total;
-  const int nb = 1024;
-  k_mse<<<nb, 256, 0, A.s>>>(A.Y.p, A.X.p, total, gscale, A.dYb.p, A.lossPart.p);
-  // layer 5 (output): dA5 = dY
-  const bf16 *dAcur = A.dYb.p;
+// (sum of squares / (B n)) on the host.  With `coef`, each layer's weights
+// and bias take their Adam step as soon as their gradients exist (fused into
+// the weight-gradient GEMM and the bias column sums); the layer's input
+// gradient is formed first, from the weights before the step.
+double forward_backward(pda_ae &A, int B, const AdamCoef *coef) {
+  long parts = 0;
+  forward(A, B, true, &parts);
+  // layer 5 (output): dA5 = dY (blocked), its transpose already in A.dAT
+  const bf16 *dAcur = A.dYblk.p;
   for (int l = 5; l >= 0; --l) {
     Layer &ly = A.L[l];
     const bf16 *hin = l == 0 ? A.X.p : A.Hb[l - 1].p;
     const long inW = ly.in, outW = ly.out;
-    // dW = dA^T H_in: A = dA^T [out x B], B = H_in^T [in x B]
-    transpose(dAcur, A.dAT.p, B, outW, A.s);
+    if (l < 5) transpose(dAcur, A.dAT.p, B, outW, A.s);
     bf16 *hinT = (l == 0) ? A.XT.p : A.HbT[l - 1].p;
     transpose(hin, hinT, B, inW, A.s);
-    gemm(A, A.dAT.p, hinT, outW, inW, B, nullptr, tc::EPI_NONE, ly.gW.p, nullptr, nullptr);
-    k_colsum<<<g1(outW), 256, 0, A.s>>>(dAcur, B, outW, ly.gb.p);
-    if (l == 0) break;
+    const AdamCoef c0{};
+    if (l == 5)  // bias gradient from the transposed error gradient [n x B]
+      k_rowsum<<<g1(outW * 32), 256, 0, A.s>>>(A.dAT.p, outW, B, ly.gb.p, coef ? ly.b.p : nullptr, ly.mb.p,
+                                               ly.vb.p, ly.outReal, coef ? *coef : c0);
+    else
+      k_colsum<<<g1(outW), 256, 0, A.s>>>(dAcur, B, outW, ly.gb.p, coef ? ly.b.p : nullptr, ly.mb.p, ly.vb.p,
+                                          ly.outReal, coef ? *coef : c0);
     // dH_in = dA W: B operand = W^T [in x out]
-    gemm(A, dAcur, ly.WbT.p, B, inW, outW, nullptr, tc::EPI_NONE, A.dH.p, nullptr, nullptr);
+    if (l == 5)
+      check(tc_gemm_blocked(A.dYblk.p, ly.WbT.p, B, inW, outW, nullptr, tc::EPI_NONE, A.dH.p, nullptr, nullptr,
+                            nullptr, A.work.p, A.workFloats, A.s),
+            "tc gemm (output layer, input gradient)");
+    else if (l > 0)
+      gemm(A, dAcur, ly.WbT.p, B, inW, outW, nullptr, tc::EPI_NONE, A.dH.p, nullptr, nullptr);
+    // dW = dA^T H_in: A = dA^T [out x B], B = H_in^T [in x B]
+    if (coef) {
+      tc::AdamEpi ad;
+      ad.W = ly.W.p;
+      ad.m = ly.mW.p;
+      ad.v = ly.vW.p;
+      ad.Wb = ly.Wb.p;
+      ad.WbT = ly.needT ? ly.WbT.p : nullptr;
+      ad.cols = ly.inReal;
+      ad.coef = *coef;
+      ad.blocked = ly.blk;
+      check(tc_gemm_adam(A.dAT.p, hinT, outW, inW, B, ad, A.s), "tc gemm (weight gradient, Adam)");
+    } else {
+      gemm(A, A.dAT.p, hinT, outW, inW, B, nullptr, tc::EPI_NONE, ly.gW.p, nullptr, nullptr);
+    }
+    if (l == 0) break;
     Layer &prev = A.L[l - 1];
+    // dA of the layer below overwrites A.dA only after its last use above
     if (prev.elu) {
       k_elu_back<<<g1((long)B * inW), 256, 0, A.s>>>(A.dH.p, A.pre[l - 1].p, A.dA.p, (long)B * inW);
     } else {
       k_to_bf16<<<g1((long)B * inW), 256, 0, A.s>>>(A.dH.p, A.dA.p, (long)B * inW);
     }
-    // the next iteration reads dA while writing dAT / HbT only
     dAcur = A.dA.p;
-    // copy dA to a separate buffer so the next layer's transpose does not alias
-    // (dA and dAT are distinct; dAcur stays valid until overwritten by k_elu_back
-    // of the following layer, after its last use)
   }
-  std::vector<double> h(nb);
-  check(cudaMemcpyAsync(h.data(), A.lossPart.p, nb * sizeof(double), cudaMemcpyDeviceToHost, A.s), "loss copy");
+  std::vector<double> h((size_t)parts);
+  check(cudaMemcpyAsync(h.data(), A.lossPart.p, parts * sizeof(double), cudaMemcpyDeviceToHost, A.s), "loss copy");
   check(cudaStreamSynchronize(A.s), "sync");
   double sum = 0.;
   for (double v : h) sum += v;
-  return sum / (double)total;
+  return sum / ((double)B * A.n);
 }
 
-void adam_step(pda_ae &A, float lr) {
-  A.step += 1;
-  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-  const float c1 = 1.f - std::pow(b1, (float)A.step), c2 = 1.f - std::pow(b2, (float)A.step);
+// the optimizer pass over stored gradients (the unfused schedule)
+void adam_step(pda_ae &A, const AdamCoef &coef) {
   for (auto &ly : A.L) {
     const long nw = ly.out * ly.in;
-    k_adam<<<g1(nw), 256, 0, A.s>>>(ly.W.p, ly.mW.p, ly.vW.p, ly.gW.p, ly.Wb.p, nw, ly.in, ly.inReal, lr, b1, b2,
-                                    c1, c2, eps);
-    k_adam<<<g1(ly.out), 256, 0, A.s>>>(ly.b.p, ly.mb.p, ly.vb.p, ly.gb.p, nullptr, ly.out, ly.out, ly.outReal, lr,
-                                        b1, b2, c1, c2, eps);
-    if (ly.needT) transpose(ly.Wb.p, ly.WbT.p, ly.out, ly.in, A.s);
+    k_adam<<<g1(nw), 256, 0, A.s>>>(ly.W.p, ly.mW.p, ly.vW.p, ly.gW.p, ly.blk ? nullptr : ly.Wb.p, nw, ly.in,
+                                    ly.inReal, coef);
+    k_adam<<<g1(ly.out), 256, 0, A.s>>>(ly.b.p, ly.mb.p, ly.vb.p, ly.gb.p, nullptr, ly.out, ly.out, ly.outReal,
+                                        coef);
+    if (ly.blk) {
+      refresh_bf16(ly, A.s);
+    } else if (ly.needT) {
+      transpose(ly.Wb.p, ly.WbT.p, ly.out, ly.in, A.s);
+    }
   }
 }
 
@@ -338,6 +423,7 @@ void create(pda_ae &A, long n, int k, int ha, int hb, uint64_t seed, void *strea
     ly.outReal = outsR[l];
     ly.elu = elus[l];
     ly.needT = l > 0;  // dH_in of layer 0 (the data) is never needed
+    ly.blk = l == 0 || l == 5;
     const long nw = ly.out * ly.in;
     ly.W.alloc(nw);
     ly.mW.alloc(nw);
@@ -347,8 +433,13 @@ void create(pda_ae &A, long n, int k, int ha, int hb, uint64_t seed, void *strea
     ly.mb.alloc(ly.out);
     ly.vb.alloc(ly.out);
     ly.gb.alloc(ly.out);
-    ly.Wb.alloc(nw);
-    if (ly.needT) ly.WbT.alloc(nw);
+    if (ly.blk) {  // blocked operands: rows padded to 128 and zero
+      alloc_zero(ly.Wb, (size_t)pad128(ly.out) * ly.in, A.s);
+      if (ly.needT) alloc_zero(ly.WbT, (size_t)pad128(ly.in) * ly.out, A.s);
+    } else {
+      ly.Wb.alloc(nw);
+      if (ly.needT) ly.WbT.alloc(nw);
+    }
     // Glorot uniform on the real fan-in / fan-out; padding rows / columns 0
     const float a = std::sqrt(6.f / (float)(ly.inReal + ly.outReal));
     k_init_uniform<<<g1(nw), 256, 0, A.s>>>(ly.W.p, ly.out, ly.in, ly.inReal, a, seed + 7919ull * (l + 1));
@@ -406,15 +497,27 @@ pda_status pda_ae_train(pda_ae *A, const void *d_data, int64_t ns, int batch, in
       PDA_CUDA(cudaMemcpyAsync(A->idx.p, perm.data() + b0, batch * sizeof(int64_t), cudaMemcpyHostToDevice, A->s));
       pda::ae::k_gather_rows<<<pda::ae::g1((long)batch * (A->n / 8)), 256, 0, A->s>>>(data, A->idx.p, A->n, batch,
                                                                                        A->X.p);
-      pda::ae::forward(*A, batch);
-      acc += pda::ae::backward(*A, batch);
-      pda::ae::adam_step(*A, (float)lr);
+      A->step += 1;
+      const pda::AdamCoef coef = pda::adam_coef((float)lr, (long)A->step);
+      if (A->fusedAdam) {
+        acc += pda::ae::forward_backward(*A, batch, &coef);
+      } else {
+        acc += pda::ae::forward_backward(*A, batch, nullptr);
+        pda::ae::adam_step(*A, coef);
+      }
       ++nbat;
     }
     if (losses) losses[e] = acc / std::max(nbat, 1);
   }
   PDA_CUDA(cudaStreamSynchronize(A->s));
   PDA_REQUIRE(pda::tc_gemm_error_and_clear() == 0, PDA_ERR_CUDA, "autoencoder: a tensor-core wait timed out");
+  PDA_API_END
+}
+
+pda_status pda_ae_set_fused(pda_ae *A, int fused) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(A, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  A->fusedAdam = fused != 0;
   PDA_API_END
 }
 
@@ -428,7 +531,7 @@ pda_status pda_ae_reconstruct(pda_ae *A, const void *d_X, int64_t rows, float *d
     PDA_CUDA(cudaMemsetAsync(A->X.p, 0, (size_t)B * A->n * sizeof(pda::ae::bf16), A->s));
     PDA_CUDA(cudaMemcpyAsync(A->X.p, (const pda::ae::bf16 *)d_X + r0 * A->n, nr * A->n * sizeof(pda::ae::bf16),
                              cudaMemcpyDeviceToDevice, A->s));
-    pda::ae::forward(*A, B);
+    pda::ae::forward(*A, B, false);
     PDA_CUDA(cudaMemcpyAsync(d_Y + r0 * A->n, A->Y.p, nr * A->n * sizeof(float), cudaMemcpyDeviceToDevice, A->s));
     if (d_Z) {
       // latent = layer 2 output (pre-activation, linear layer), first k columns
@@ -448,8 +551,7 @@ pda_status pda_ae_gradients(pda_ae *A, const void *d_X, int batch, double *loss,
   PDA_REQUIRE(A && d_X && batch > 0 && batch % 64 == 0, PDA_ERR_INVALID_ARGUMENT, "invalid argument");
   pda::ae::ensure_batch(*A, batch);
   PDA_CUDA(cudaMemcpyAsync(A->X.p, d_X, (size_t)batch * A->n * sizeof(pda::ae::bf16), cudaMemcpyDeviceToDevice, A->s));
-  pda::ae::forward(*A, batch);
-  const double l = pda::ae::backward(*A, batch);
+  const double l = pda::ae::forward_backward(*A, batch, nullptr);
   if (loss) *loss = l;
   if (d_grads) {
     size_t off = 0;

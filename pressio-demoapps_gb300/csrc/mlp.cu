@@ -17,34 +17,80 @@ namespace pda {
 
 static __device__ int g_tc_err;
 
-// lifts the dynamic shared-memory limit of one GEMM instantiation (once)
-template <int BN_, int ST>
+// lifts the dynamic shared-memory limit of one GEMM instantiation to what
+// its largest epilogue needs (a per-device function attribute, set once per
+// device)
+template <int BN_, int ST, int NT = tc::THREADS>
 static cudaError_t gemm_attr() {
-  static bool done = false;
-  if (!done) {
-    cudaError_t e = cudaFuncSetAttribute(tc::k_gemm_tn<BN_, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         tc::smem_bytes(BN_, ST));
+  constexpr int kMaxDev = 64;
+  static bool done[kMaxDev] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDev || !done[dev]) {
+    const int bytes = tc::smem_bytes(BN_, ST) > tc::adam_smem_bytes(BN_, ST) ? tc::smem_bytes(BN_, ST)
+                                                                              : tc::adam_smem_bytes(BN_, ST);
+    e = cudaFuncSetAttribute(tc::k_gemm_tn<BN_, ST, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
-    done = true;
+    if (dev >= 0 && dev < kMaxDev) done[dev] = true;
   }
   return cudaSuccess;
 }
 
-// one launch of k_gemm_tn (128 x 128 tiles, two stages) over all output
-// tiles and `splits` K ranges of `per` slices
+// one launch of k_gemm_tn (128 x 128 tiles) over all output tiles and
+// `splits` K ranges of `per` slices; split-K launches (two CTAs per SM) keep
+// two slices in flight per CTA (three stages), the others one (two stages,
+// three CTAs per SM)
 static cudaError_t launch_gemm(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K,
                                const float *bias, int epi, float *outF, __nv_bfloat16 *outB, float *preact,
-                               int splits, int per, float *partial, cudaStream_t s) {
+                               int splits, int per, float *partial, cudaStream_t s,
+                               const tc::AdamEpi &adam = tc::AdamEpi{}, const tc::MseEpi &mse = tc::MseEpi{}) {
   int *err = nullptr;
   cudaError_t e = cudaGetSymbolAddress((void **)&err, g_tc_err);
   if (e != cudaSuccess) return e;
-  const unsigned mt = (unsigned)((M + tc::BM - 1) / tc::BM);
-  e = gemm_attr<tc::BN, tc::STAGES>();
-  if (e != cudaSuccess) return e;
-  tc::k_gemm_tn<tc::BN, tc::STAGES>
-      <<<dim3((unsigned)((N + tc::BN - 1) / tc::BN), mt, (unsigned)splits), tc::THREADS, tc::SMEM_BYTES, s>>>(
-          A, B, M, N, K, bias, epi, outF, outB, preact, err, per, partial);
+  const dim3 grid((unsigned)((N + tc::BN - 1) / tc::BN), (unsigned)((M + tc::BM - 1) / tc::BM), (unsigned)splits);
+  if (splits > 1) {
+    constexpr int ST = 3;
+    e = gemm_attr<tc::BN, ST>();
+    if (e != cudaSuccess) return e;
+    tc::k_gemm_tn<tc::BN, ST><<<grid, tc::THREADS, tc::smem_bytes(tc::BN, ST), s>>>(
+        A, B, M, N, K, bias, epi, outF, outB, preact, err, per, partial, adam, mse);
+  } else if (adam.W) {
+    // the Adam epilogue runs eight warps: twice the rows in flight and half
+    // the dependent optimizer arithmetic per warp
+    constexpr int ST = tc::STAGES, NT = 2 * tc::THREADS;
+    e = gemm_attr<tc::BN, ST, NT>();
+    if (e != cudaSuccess) return e;
+    tc::k_gemm_tn<tc::BN, ST, NT><<<grid, NT, tc::adam_smem_bytes(tc::BN, ST), s>>>(
+        A, B, M, N, K, bias, epi, outF, outB, preact, err, per, partial, adam, mse);
+  } else {
+    constexpr int ST = tc::STAGES;
+    e = gemm_attr<tc::BN, ST>();
+    if (e != cudaSuccess) return e;
+    tc::k_gemm_tn<tc::BN, ST><<<grid, tc::THREADS, tc::smem_bytes(tc::BN, ST), s>>>(
+        A, B, M, N, K, bias, epi, outF, outB, preact, err, per, partial, adam, mse);
+  }
   return cudaGetLastError();
+}
+
+cudaError_t tc_gemm_adam(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K,
+                         const tc::AdamEpi &adam, cudaStream_t s) {
+  const auto misaligned = [](const void *p) { return ((uintptr_t)p & 15u) != 0; };
+  if (K % tc::BK != 0 || N % 4 != 0 || M % 2 != 0 || !adam.W || !adam.m || !adam.v || !adam.Wb ||
+      misaligned(adam.W) || misaligned(adam.m) || misaligned(adam.v) || ((uintptr_t)adam.Wb & 7u) != 0 ||
+      ((uintptr_t)adam.WbT & 3u) != 0)
+    return cudaErrorInvalidValue;
+  return launch_gemm(A, B, M, N, K, nullptr, tc::EPI_NONE, nullptr, nullptr, nullptr, 1, (int)(K / tc::BK), nullptr,
+                     s, adam, tc::MseEpi{});
+}
+
+cudaError_t tc_gemm_mse(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K, const float *bias,
+                        const tc::MseEpi &mse, cudaStream_t s) {
+  if (K % tc::BK != 0 || N % 16 != 0 || !bias || !mse.X || !mse.dY || !mse.dYT || !mse.partial ||
+      ((uintptr_t)mse.X & 15u) != 0 || ((uintptr_t)mse.dY & 15u) != 0)
+    return cudaErrorInvalidValue;
+  return launch_gemm(A, B, M, N, K, bias, tc::EPI_BIAS, nullptr, nullptr, nullptr, 1, (int)(K / tc::BK), nullptr, s,
+                     tc::AdamEpi{}, mse);
 }
 
 cudaError_t tc_gemm(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K, const float *bias,
@@ -80,6 +126,62 @@ cudaError_t tc_gemm_splitk(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long 
   const long total = M * N;
   tc::k_splitk_reduce<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(M, N, splits, work, N, bias, epi, outF,
                                                                        outB, preact);
+  return cudaGetLastError();
+}
+
+// blocked-operand GEMM: three stages (two slices in flight per CTA, two CTAs
+// per SM)
+cudaError_t tc_gemm_blocked(const __nv_bfloat16 *Ablk, const __nv_bfloat16 *Bblk, long M, long N, long K,
+                            const float *bias, int epi, float *outF, __nv_bfloat16 *outB, float *preact,
+                            const tc::MseEpi *mse, float *work, long workFloats, cudaStream_t s) {
+  constexpr int ST = 3;
+  if (K % tc::BK != 0 || (mse && (N % 16 != 0 || !bias || !mse->X || !mse->dY || !mse->dYT || !mse->partial)))
+    return cudaErrorInvalidValue;
+  constexpr int kMaxDev = 64;
+  static bool attr[kMaxDev] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDev || !attr[dev]) {
+    e = cudaFuncSetAttribute(tc::k_gemm_blocked<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             tc::blocked_gemm_smem_bytes(ST));
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < kMaxDev) attr[dev] = true;
+  }
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms <= 0) sms = 1;
+  int *err = nullptr;
+  e = cudaGetSymbolAddress((void **)&err, g_tc_err);
+  if (e != cudaSuccess) return e;
+  const long tiles = ((N + tc::BN - 1) / tc::BN) * ((M + tc::BM - 1) / tc::BM);
+  const int kt = (int)(K / tc::BK);
+  int splits = 1;
+  if (!mse && work && tiles < 2L * sms && kt >= 32) {
+    splits = (int)std::min<long>((2L * sms + tiles - 1) / tiles, kt / 16);
+    while (splits > 1 && (long)splits * M * N > workFloats) --splits;
+  }
+  const int per = (kt + splits - 1) / splits;
+  const dim3 grid((unsigned)((N + tc::BN - 1) / tc::BN), (unsigned)((M + tc::BM - 1) / tc::BM), (unsigned)splits);
+  const tc::MseEpi me = mse ? *mse : tc::MseEpi{};
+  if (splits == 1) {
+    tc::k_gemm_blocked<ST><<<grid, tc::THREADS, tc::blocked_gemm_smem_bytes(ST), s>>>(
+        Ablk, Bblk, M, N, kt, per, bias, epi, outF, outB, preact, err, nullptr, me);
+    return cudaGetLastError();
+  }
+  tc::k_gemm_blocked<ST><<<grid, tc::THREADS, tc::blocked_gemm_smem_bytes(ST), s>>>(
+      Ablk, Bblk, M, N, kt, per, nullptr, tc::EPI_NONE, nullptr, nullptr, nullptr, err, work, me);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  tc::k_splitk_reduce<<<(unsigned)((M * N + 255) / 256), 256, 0, s>>>(M, N, splits, work, N, bias, epi, outF, outB,
+                                                                       preact);
+  return cudaGetLastError();
+}
+
+cudaError_t tc_to_bf16_blocked(const float *W, long R, long C, int trans, __nv_bfloat16 *out, cudaStream_t s) {
+  if (R % 64 != 0 || C % 64 != 0) return cudaErrorInvalidValue;
+  const long n = R * C / 8;
+  tc::k_to_bf16_blocked<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(W, R, C, trans, out);
   return cudaGetLastError();
 }
 

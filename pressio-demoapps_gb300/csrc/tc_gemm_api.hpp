@@ -7,15 +7,49 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include "adam.cuh"
+
 namespace pda {
 namespace tc {
 enum Epilogue : int { EPI_NONE = 0, EPI_BIAS = 1, EPI_BIAS_ELU = 2 };
+
+// Epilogue of a weight-gradient product C = dW [M x N]: the Adam update of
+// the fp32 weights W (moments m, v) and the refresh of their bf16 copy Wb
+// [M x N] and, when WbT is given, of its transpose [N x M].  Columns at or
+// past `cols` are padding: W, m and v stay, both bf16 copies get 0.
+struct AdamEpi {
+  float *W = nullptr, *m = nullptr, *v = nullptr;
+  __nv_bfloat16 *Wb = nullptr, *WbT = nullptr;
+  long cols = 0;
+  AdamCoef coef{};
+  // bf16 copies in the blocked operand layout (Wb with N / 64 slices, WbT
+  // with M / 64) instead of row-major
+  bool blocked = false;
+};
+// Epilogue of the output layer's product in training: Y = C + bias is the
+// reconstruction of X [M x N] (bf16); writes dY = bf16(gscale (Y - X)) as
+// [M x N] and as its transpose dYT [N x M], and one double per CTA, the sum of
+// (Y - X)^2 over its tile, to partial[blockIdx.y * gridDim.x + blockIdx.x].
+struct MseEpi {
+  const __nv_bfloat16 *X = nullptr;
+  __nv_bfloat16 *dY = nullptr, *dYT = nullptr;
+  float gscale = 0.f;
+  double *partial = nullptr;
+  // dY in the blocked operand layout with N / 64 slices instead of row-major
+  bool blocked = false;
+};
 
 // byte offset of element (r, k) of a 64-column bf16 operand slice in the
 // canonical K-major no-swizzle layout of tcgen05: 8 x 16-byte core matrices,
 // the two adjacent in K 128 bytes apart, the 8-row groups 1024 bytes apart
 __host__ __device__ inline uint32_t slice_offset(int r, int k) {
   return (uint32_t)((((r >> 3) << 3) + (k >> 3)) << 7) + (uint32_t)((r & 7) << 4) + (uint32_t)((k & 7) << 1);
+}
+// element index of (r, k) of an operand of `kt` 64-column slices in the
+// blocked layout of k_gemm_blocked: 128 x 64 blocks (16 KB) stored
+// [r / 128][k / 64], each in the canonical layout of slice_offset
+__host__ __device__ inline long blocked_index(long r, long k, long kt) {
+  return ((((r >> 7) * kt) + (k >> 6)) << 13) + (long)(slice_offset((int)(r & 127), (int)(k & 63)) >> 1);
 }
 // element index of (r, k) of a 16-row operand in the blocked layout of
 // tc_gemm_thin_blocked's B: one 2 KB slice per 64 columns
@@ -32,6 +66,26 @@ cudaError_t tc_gemm(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long
 cudaError_t tc_gemm_splitk(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K,
                            const float *bias, int epi, float *outF, __nv_bfloat16 *outB, float *preact, float *work,
                            long workFloats, cudaStream_t s);
+// C = A B^T is the gradient of a weight matrix [M x N]; the epilogue applies
+// Adam to it (no split K; N a multiple of 4, M even, 16-byte aligned W, m, v)
+cudaError_t tc_gemm_adam(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K,
+                         const tc::AdamEpi &adam, cudaStream_t s);
+// C = A B^T + bias is a reconstruction of X; the epilogue writes the squared
+// error's gradient and per-CTA sums of squares (no split K; N a multiple of
+// 16); `partial` holds ceil(M / 128) * ceil(N / 128) doubles
+cudaError_t tc_gemm_mse(const __nv_bfloat16 *A, const __nv_bfloat16 *B, long M, long N, long K, const float *bias,
+                        const tc::MseEpi &mse, cudaStream_t s);
+// C = A B^T (+ bias, ELU) with both operands in the blocked layout
+// (blocked_index; rows past M or N zero), one bulk copy per 16 KB slice, K
+// split over CTAs into `work` when the output tiles are few; mse (optional)
+// as in tc_gemm_mse
+cudaError_t tc_gemm_blocked(const __nv_bfloat16 *Ablk, const __nv_bfloat16 *Bblk, long M, long N, long K,
+                            const float *bias, int epi, float *outF, __nv_bfloat16 *outB, float *preact,
+                            const tc::MseEpi *mse, float *work, long workFloats, cudaStream_t s);
+// fp32 [R x C] -> bf16 in the blocked layout, as the operand [R x C]
+// (trans = 0, C / 64 slices) or as its transpose [C x R] (trans = 1, R / 64
+// slices); rows past the operand's end are left alone
+cudaError_t tc_to_bf16_blocked(const float *W, long R, long C, int trans, __nv_bfloat16 *out, cudaStream_t s);
 // a row-major [M x K] bf16 operand in the blocked layout of
 // tc_gemm_thin_blocked: rowsPerSlice = 128 for A ([tiles][K / 64] slices of
 // 128 x 64, rows past M zero), 16 for B (M <= 16); K a multiple of 64

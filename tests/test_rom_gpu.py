@@ -28,10 +28,12 @@ def _bf16(torch, a):
 
 
 @pytest.mark.gpu
-def test_autoencoder_gradients_match_oracle(pda):
+@pytest.mark.parametrize("n", [192, 4096])
+def test_autoencoder_gradients_match_oracle(pda, n):
+    """n = 4096: the wide layers' blocked-operand GEMMs split K over CTAs."""
     import torch
     import mlp_oracle
-    n, k, ha, hb, B = 192, 4, 128, 64, 64
+    k, ha, hb, B = 4, 128, 64, 64
     ae = pda.AutoEncoder(n, k, ha, hb, seed=3)
     rng = np.random.default_rng(5)
     X = rng.normal(0, 0.5, (B, n))
@@ -76,6 +78,31 @@ def test_autoencoder_training_reduces_loss(pda):
     err = np.linalg.norm(Y.cpu().numpy() - X[:200]) / np.linalg.norm(X[:200])
     assert err < 0.2, err
     assert Z.shape == (200, k)
+
+
+@pytest.mark.gpu
+def test_autoencoder_fused_adam_equals_separate_pass(pda):
+    """Adam inside the weight-gradient GEMM epilogues (with the bf16 copy and
+    transpose refreshed there) and Adam as a separate pass over stored
+    gradients give the same weights, biases and losses bit for bit; the
+    latent padding stays zero."""
+    import torch
+    n, k, ha, hb = 384, 5, 256, 128
+    rng = np.random.default_rng(7)
+    X = _bf16(torch, np.tanh(rng.normal(0, 0.7, (512, 3)) @ rng.normal(0, 1, (3, n))))
+    out = []
+    for fused in (True, False):
+        ae = pda.AutoEncoder(n, k, ha, hb, seed=4)
+        ae.set_fused(fused)
+        losses = ae.train(X, batch=128, epochs=3, lr=3e-3, seed=9)
+        out.append((losses, [tuple(t.cpu().numpy() for t in ae.layer(l)) for l in range(6)]))
+    (la, wa), (lb, wb) = out
+    assert np.array_equal(la, lb), (la, lb)
+    for l in range(6):
+        assert np.array_equal(wa[l][0], wb[l][0]) and np.array_equal(wa[l][1], wb[l][1]), l
+    assert np.all(wa[2][0][k:] == 0) and np.all(wa[2][1][k:] == 0)  # encoder output rows past the latent
+    assert np.all(wa[3][0][:, k:] == 0)  # decoder input columns past the latent
+    assert la[-1] < la[0]
 
 
 def _sample_problem(pda, oracle, n=24, frac=0.3, seed=0):
