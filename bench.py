@@ -273,9 +273,13 @@ def wl_jacobian_2d(c):
         J = prob.createJacobian()
     ms = _time_gpu(torch, stream, lambda: prob.rightHandSideAndJacobian(U, 0.0, V, J), 5)
     nnz = J.nonZeros()
+    with torch.cuda.stream(stream):
+        U.copy_(torch.from_numpy(prob.initialConditionHost()))
+    ms_ic = _time_gpu(torch, stream, lambda: prob.rightHandSideAndJacobian(U, 0.0, V, J), 5)
     w = {"config": f"euler2d_riemann_ic2_weno5_jacobian_{n}x{n}", "ms_per_call": ms, "nnz": nnz,
          "value": nnz / (ms * 1e-3) / 1e9, "unit": "Gnnz/s (V + CSR J per call)",
-         "gcell_per_s": n * n / (ms * 1e-3) / 1e9}
+         "gcell_per_s": n * n / (ms * 1e-3) / 1e9,
+         "on_initial_condition": {"ms_per_call": ms_ic, "value": nnz / (ms_ic * 1e-3) / 1e9}}
     del U, V, J, prob
     torch.cuda.empty_cache()
     if cpu:
@@ -287,6 +291,44 @@ def wl_jacobian_2d(c):
         med, k = _cpu_rate(lambda: op.velocity_and_jacobian(U2), 5.0)
         w["cpu_baseline"] = {"value": op.nnz / med / 1e9, "unit": "Gnnz/s", "cores": threads, "kind": "port",
                              "sample": f"{k} V+J calls at 256^2 (same problem/scheme), median {med*1e3:.1f} ms"}
+        U2ic = p2.initialConditionHost()
+        med, k = _cpu_rate(lambda: op.velocity_and_jacobian(U2ic), 2.0)
+        w["cpu_baseline"]["on_initial_condition"] = {"value": op.nnz / med / 1e9, "sample": f"{k} calls at 256^2"}
+    return w
+
+
+def wl_jacobian_swe(c, n=1024, ns=256):
+    """2D shallow water, slip walls, WENO5, V + CSR J at 1024^2 (the reference's
+    default parameters: gravity 9.8, Coriolis -3, pulse 0.125).  The CPU leg
+    runs one thread: the reference's threaded near-boundary Jacobian loop of
+    this problem races on a shared member, so its J is timed serially."""
+    pda, torch, stream, orc, rng = c.pda, c.torch, c.stream, c.orc, c.rng
+    params = {"gravity": 9.8, "coriolis": -3.0, "pulseMagnitude": 0.125}
+    mesh = pda.create_full_mesh((n, n), (-5.0, 5.0, -5.0, 5.0), 7)
+    prob = pda.create_problem(mesh, pda.Swe2d.SlipWall, pda.InviscidFluxReconstruction.Weno5, 1, params,
+                              stream=stream)
+    Uh = prob.initialConditionHost() + rng.uniform(-1e-3, 1e-3, 3 * n * n)
+    with torch.cuda.stream(stream):
+        U = torch.from_numpy(Uh).cuda()
+        V = prob.createVelocity()
+        J = prob.createJacobian()
+    ms = _time_gpu(torch, stream, lambda: prob.rightHandSideAndJacobian(U, 0.0, V, J), 5)
+    nnz = J.nonZeros()
+    w = {"config": f"swe2d_slipwall_weno5_jacobian_{n}x{n}", "ms_per_call": ms, "nnz": nnz,
+         "value": nnz / (ms * 1e-3) / 1e9, "unit": "Gnnz/s (V + CSR J per call)"}
+    del U, V, J, prob
+    torch.cuda.empty_cache()
+    if orc is not None:
+        m2 = pda.create_full_mesh((ns, ns), (-5.0, 5.0, -5.0, 5.0), 7)
+        g, x, y, z, _, _ = m2._arrays()
+        om = orc.mesh_from_arrays(2, 7, g, x, y, z, (m2.dx(), m2.dy(), m2.dz()))
+        op = orc.problem(om, 3, 0, 2, 1, params)
+        U2 = op.initial_condition() + rng.uniform(-1e-3, 1e-3, 3 * ns * ns)
+        used = orc.set_threads(1)
+        med, k = _cpu_rate(lambda: op.velocity_and_jacobian(U2), 3.0)
+        orc.set_threads(c.threads)
+        w["cpu_baseline"] = {"value": op.nnz / med / 1e9, "unit": "Gnnz/s", "cores": used, "kind": "port",
+                             "sample": f"{k} V+J calls at {ns}^2 on 1 thread, median {med*1e3:.0f} ms"}
     return w
 
 
@@ -305,7 +347,11 @@ def wl_velocity_3d(c):
     prof = prob.profile_velocity(U, V, reps=3)
     w = {"config": "euler3d_smooth_periodic_weno5_velocity_256^3", "ms_per_call": ms,
          "value": n ** 3 / (ms * 1e-3) / 1e9, "unit": "Gcell/s", "kernel_ms": prof}
-    del U, V, prob
+    # WENO3, the reference's own 3D scheme (its 3D path has no WENO5)
+    p3 = pda.create_problem(mesh, pda.Euler3d.PeriodicSmooth, pda.InviscidFluxReconstruction.Weno3, stream=stream)
+    ms3 = _time_gpu(torch, stream, lambda: p3.velocity(U, 0.0, V), 5)
+    w["weno3"] = {"ms_per_call": ms3, "value": n ** 3 / (ms3 * 1e-3) / 1e9, "unit": "Gcell/s"}
+    del U, V, prob, p3
     torch.cuda.empty_cache()
     if cpu:
         ns = 64
@@ -315,6 +361,10 @@ def wl_velocity_3d(c):
         med, k = _cpu_rate(lambda: op.velocity(U3), 5.0)
         w["cpu_baseline"] = {"value": ns ** 3 / med / 1e9, "unit": "Gcell/s", "cores": threads, "kind": "port",
                              "sample": f"{k} velocity calls at 64^3 (same problem/scheme), median {med*1e3:.1f} ms"}
+        om3, op3 = oracle_problem(m3, 2, 0, 1, 1, 3, 7)
+        med, k = _cpu_rate(lambda: op3.velocity(U3), 2.0)
+        w["weno3"]["cpu_baseline"] = {"value": ns ** 3 / med / 1e9, "unit": "Gcell/s", "cores": threads,
+                                      "kind": "port", "sample": f"{k} WENO3 velocity calls at 64^3"}
     return w
 
 
@@ -667,7 +717,8 @@ def wl_ae_step(c, n=3 * 256 * 256, latent=12, ha=1024, hb=256, batch=128, steps=
 # workloads whose work is split over the ranks (every rank must run them)
 SHARDED = {"batched_swe"}
 
-WORKLOADS = {"jacobian_2d": wl_jacobian_2d, "velocity_3d": wl_velocity_3d, "jacobian_3d": wl_jacobian_3d,
+WORKLOADS = {"jacobian_2d": wl_jacobian_2d, "jacobian_swe": wl_jacobian_swe, "velocity_3d": wl_velocity_3d,
+             "jacobian_3d": wl_jacobian_3d,
              "sod_1d_ssprk3": wl_sod_1d_ssprk3, "ssprk3_3d": wl_ssprk3_3d, "batched_swe": wl_batched_swe,
              "rom_swe": wl_rom_swe, "lspg_step": wl_lspg_step, "ae_step": wl_ae_step}
 
