@@ -485,7 +485,7 @@ def _rom_module():
     return mod
 
 
-def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int(os.environ.get("PDA_ROM_EPOCHS", 60)),
+def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int(os.environ.get("PDA_ROM_EPOCHS", 150)),
                batch=128, lr=1e-3, dt=0.005, rom_ratio=int(os.environ.get("PDA_ROM_RATIO", 4)), gn_iters=1,
                order=int(os.environ.get("PDA_ROM_ORDER", 2))):
     """Learned-manifold hyper-reduced LSPG on 2D SWE slip wall 256^2: 48
