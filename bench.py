@@ -369,11 +369,12 @@ def wl_velocity_3d(c):
 
 
 def wl_jacobian_3d(c):
-    """3D Euler WENO5 Jacobian, 96^3"""
+    """3D Euler WENO5 Jacobian, 96^3 (PDA_JAC3_N overrides the size for
+    profiling runs)"""
     pda, torch, stream, orc, threads, rng = c.pda, c.torch, c.stream, c.orc, c.threads, c.rng
     cpu = orc is not None
     oracle_problem = c.oracle_problem
-    n = 96
+    n = int(os.environ.get("PDA_JAC3_N", 96))
     mesh = pda.create_full_mesh((n, n, n), (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0), 7, (True, True, True))
     prob = pda.create_problem(mesh, pda.Euler3d.PeriodicSmooth, pda.InviscidFluxReconstruction.Weno5, stream=stream)
     with torch.cuda.stream(stream):
@@ -382,7 +383,7 @@ def wl_jacobian_3d(c):
         J = prob.createJacobian()
     ms = _time_gpu(torch, stream, lambda: prob.rightHandSideAndJacobian(U, 0.0, V, J), 3)
     nnz = J.nonZeros()
-    w = {"config": "euler3d_smooth_periodic_weno5_jacobian_96^3", "ms_per_call": ms, "nnz": nnz,
+    w = {"config": f"euler3d_smooth_periodic_weno5_jacobian_{n}^3", "ms_per_call": ms, "nnz": nnz,
          "value": nnz / (ms * 1e-3) / 1e9, "unit": "Gnnz/s (V + CSR J per call)"}
     del U, V, J, prob
     torch.cuda.empty_cache()

@@ -45,8 +45,17 @@ template <int FAM, int SCHEME, int LANES> struct JTileSmem {
 
 // grid: x = lines of the box along AXIS (first other axis fastest), y = face
 // chunks of TW faces
+// Resident blocks per SM the register allocation must allow.  The kernel is
+// FP64-bound with few warps (one face per thread holds its gradients and flux
+// Jacobians); measured at 1024^2 / 96^3, capping registers for 8 blocks of 64
+// threads (2D) or 6 (3D) beats the uncapped allocation by 4-6 % / 3 %, the
+// few spills included.
+template <int DIM> struct JTileMinBlocks {
+  static constexpr int value = DIM == 3 ? 6 : 8;
+};
+
 template <int FAM, int SCHEME, int AXIS, int LANES>
-__global__ void __launch_bounds__(LANES)
+__global__ void __launch_bounds__(LANES, JTileMinBlocks<Fam<FAM>::dim>::value)
 k_jtile(Box b, MeshArgs m, Phys p, const double *__restrict__ U, const int *__restrict__ rowptr,
         double *__restrict__ V, double *__restrict__ J) {
   using F = Fam<FAM>;

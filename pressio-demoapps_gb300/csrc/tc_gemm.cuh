@@ -17,8 +17,14 @@
 //  * one elected thread issues tcgen05.mma (M = 128, N = BN, K = 16, four
 //    per slice) and tcgen05.commit onto the stage's mbarrier, which tells
 //    the copy threads when the stage may be overwritten;
-//  * the epilogue reads the accumulator with tcgen05.ld (warp w owns TMEM
-//    lanes 32w..32w+31 = tile rows), adds the bias, applies ELU and stores.
+//  * the epilogue (tile_epilogue) reads the accumulator with tcgen05.ld
+//    (warp w owns TMEM lanes 32 (w % 4).. = tile rows) and either adds the
+//    bias, applies ELU and stores, or stores split-K partial sums, or forms
+//    the output layer's squared-error gradient, or (CTAs of eight warps)
+//    applies Adam to the weights whose gradient the tile is.
+// Three kernels share that epilogue: k_gemm_tn (row-major operands),
+// k_gemm_blocked (both operands pre-blocked, one bulk copy per slice, for
+// long K) and, with its own epilogue, k_gemm_thin_blocked (N = 16).
 // Every wait on an mbarrier is bounded by a clock budget; on expiry the CTA
 // sets an error flag, skips the remaining work, frees its TMEM and returns.
 #pragma once
