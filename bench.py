@@ -487,7 +487,7 @@ def _rom_module():
 
 
 def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int(os.environ.get("PDA_ROM_EPOCHS", 150)),
-               batch=128, lr=1e-3, dt=0.005, rom_ratio=int(os.environ.get("PDA_ROM_RATIO", 4)), gn_iters=1,
+               batch=128, lr=1e-3, dt=0.005, rom_ratio=int(os.environ.get("PDA_ROM_RATIO", 5)), gn_iters=1,
                order=int(os.environ.get("PDA_ROM_ORDER", 2))):
     """Learned-manifold hyper-reduced LSPG on 2D SWE slip wall 256^2: 48
     Latin-hypercube training points (gravity, coriolis, pulse), 400 FOM
@@ -593,7 +593,8 @@ def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int
     # further (order : Gauss-Newton iterations : ROM step / FOM step [: sample
     # fraction]) settings of the same trained network: the speed / accuracy
     # trade-off of the step and of the sample mesh
-    variants = [v for v in os.environ.get("PDA_ROM_VARIANTS", "1:1:4,2:1:8,2:1:2,2:1:4:0.03").split(",") if v]
+    variants = [v for v in os.environ.get("PDA_ROM_VARIANTS", "1:1:5,2:1:2,2:1:4,2:2:5,2:1:10,2:1:5:0.03").split(",")
+                if v]
     if variants:
         out["variants"] = {}
         states_by_point = [setup.fom_trajectory(p, dt, checkpoints) for p in test]
@@ -601,6 +602,9 @@ def wl_rom_swe(c, n=256, n_train=48, n_snap=400, n_test=8, latent=12, epochs=int
             f = v.split(":")
             ordr, gn, ratio = (int(u) for u in f[:3])
             frac = float(f[3]) if len(f) > 3 else 0.01
+            if any(cp % ratio for cp in checkpoints):
+                out["variants"][v] = {"skipped": f"checkpoints {checkpoints} are not multiples of {ratio}"}
+                continue
             if frac != 0.01:
                 sm_v, gids_v, st_v, s2st_v = setup.sample_mesh(frac, seed=7)
                 sample = (sm_v, st_v, s2st_v)

@@ -243,6 +243,8 @@ class FallbackRun:
     def __init__(self, setup, params, rom, decoder, x0, dt_fom, ratio, checkpoints, threshold, gn_iters=1,
                  tol=1e-9, order=1):
         import torch
+        if any(c % ratio for c in checkpoints):
+            raise ValueError(f"every checkpoint must be a multiple of the ROM step ratio {ratio}: {checkpoints}")
         self.states, self.fallback_at = {}, None
         x = x0.clone()
         rom.advance(x, dt_fom * ratio, 1, gn_iters, tol, order=order, first_step=1)
