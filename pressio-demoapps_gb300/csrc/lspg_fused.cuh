@@ -1,11 +1,12 @@
-// One Gauss-Newton iteration of hyper-reduced LSPG (BDF1) in one launch:
-// sample-mesh velocity V, the product Jf D of the sample-mesh Jacobian with
-// the trial space's latent Jacobian D formed face by face (never assembling
-// Jf), the LSPG residual R = cf V + (y - y_n) and JR = cf Jf D + D at the
-// sample dofs, the block partial sums of JR^T JR, JR^T R and R^T R, and, in
-// the last block to finish, their reduction, the k x k Cholesky solve and
-// the latent update (Pressio's LspgUnsteadyResidualJacobianPolicyHypRed,
-// lspg_unsteady_rj_policy_hypred.hpp:180-264, with BDF1).
+// One Gauss-Newton iteration of hyper-reduced LSPG (BDF1 or BDF2) in one
+// launch: sample-mesh velocity V, the product Jf D of the sample-mesh
+// Jacobian with the trial space's latent Jacobian D formed face by face
+// (never assembling Jf), the LSPG residual R = cf V + (y + cn y_n [+ cnm1
+// y_n-1]) and JR = cf Jf D + D at the sample dofs, the block partial sums of
+// JR^T JR, JR^T R and R^T R, and, in the last block to finish, their
+// reduction, the k x k Cholesky solve and the latent update (Pressio's
+// LspgUnsteadyResidualJacobianPolicyHypRed,
+// lspg_unsteady_rj_policy_hypred.hpp:180-264).
 //
 // Jf D row by row: Jf's row is the sum over the row's faces of
 // +-h^-1 (JN dU/dq + JP dU/dq) with dU/dq the reconstruction gradients, so
