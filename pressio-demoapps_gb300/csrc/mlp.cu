@@ -191,30 +191,57 @@ cudaError_t tc_block_operand(const __nv_bfloat16 *W, long M, long K, int rowsPer
   return cudaGetLastError();
 }
 
-cudaError_t tc_gemm_thin_blocked(const __nv_bfloat16 *Ablk, const __nv_bfloat16 *Bblk, long M, long K, int splits,
-                                 float *partial, cudaStream_t s) {
-  constexpr int ST = tc::THIN_STAGES;
-  // the larger dynamic shared memory is a per-device function attribute
+// the larger dynamic shared memory of the thin GEMM is a per-device function
+// attribute, set once per device
+template <int ST>
+static cudaError_t thin_attr() {
   constexpr int kMaxDev = 64;
   static bool attr[kMaxDev] = {};
   int dev = 0;
-  cudaError_t ed = cudaGetDevice(&dev);
-  if (ed != cudaSuccess) return ed;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDev || !attr[dev]) {
-    cudaError_t e = cudaFuncSetAttribute(tc::k_gemm_thin_blocked<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         tc::blocked_smem_bytes(ST));
+    e = cudaFuncSetAttribute(tc::k_gemm_thin_blocked<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             tc::blocked_smem_bytes(ST));
     if (e != cudaSuccess) return e;
     if (dev >= 0 && dev < kMaxDev) attr[dev] = true;
   }
+  return cudaSuccess;
+}
+
+cudaError_t tc_gemm_thin_blocked(const __nv_bfloat16 *Ablk, const __nv_bfloat16 *Bblk, long M, long K, int splits,
+                                 float *partial, cudaStream_t s) {
+  constexpr int ST = tc::THIN_STAGES;
+  cudaError_t e = thin_attr<ST>();
+  if (e != cudaSuccess) return e;
   int *err = nullptr;
-  cudaError_t e = cudaGetSymbolAddress((void **)&err, g_tc_err);
+  e = cudaGetSymbolAddress((void **)&err, g_tc_err);
   if (e != cudaSuccess) return e;
   const int kt = (int)(K / tc::BK);
   splits = std::max(1, std::min(splits, kt));
   const int per = (kt + splits - 1) / splits;
   dim3 grid((unsigned)((M + tc::BM - 1) / tc::BM), (unsigned)splits);
   tc::k_gemm_thin_blocked<ST><<<grid, tc::THREADS, tc::blocked_smem_bytes(ST), s>>>(Ablk, Bblk, M, kt, per, partial,
-                                                                                    err);
+                                                                                    err, tc::ThinDecode{});
+  return cudaGetLastError();
+}
+
+cudaError_t tc_gemm_thin_prepare() { return thin_attr<tc::THIN_STAGES>(); }
+
+cudaError_t tc_gemm_thin_decode(const __nv_bfloat16 *Ablk, const __nv_bfloat16 *Bblk, long M, long K,
+                                const tc::ThinDecode &dec, cudaStream_t s) {
+  constexpr int ST = tc::THIN_STAGES;
+  if (!dec.y || !dec.D || !dec.b3 || !dec.uref || !dec.scale || dec.K < 1 || dec.K > 15 || K % tc::BK != 0)
+    return cudaErrorInvalidValue;
+  cudaError_t e = thin_attr<ST>();
+  if (e != cudaSuccess) return e;
+  int *err = nullptr;
+  e = cudaGetSymbolAddress((void **)&err, g_tc_err);
+  if (e != cudaSuccess) return e;
+  const int kt = (int)(K / tc::BK);
+  dim3 grid((unsigned)((M + tc::BM - 1) / tc::BM), 1u);
+  tc::k_gemm_thin_blocked<ST><<<grid, tc::THREADS, tc::blocked_smem_bytes(ST), s>>>(Ablk, Bblk, M, kt, kt, nullptr,
+                                                                                    err, dec);
   return cudaGetLastError();
 }
 

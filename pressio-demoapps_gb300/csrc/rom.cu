@@ -129,41 +129,10 @@ k_decode_hidden(int h2, const float *__restrict__ W1, const float *__restrict__ 
   }
 }
 
-// tensor-core output layer: C [nst x 16] = W3b [nst x h2] Zb^T (fp32), both
-// operands in the blocked slice layout (one bulk copy per 64-column slice);
-// y = uref + scale (C[., 0] + b3), D = scale C[., 1..k], from split-K partial
-// sums Cp[split][nst][16] added in split order (the output layer is short and
-// wide: K split over the SMs hides the latency of streaming the weights)
-constexpr int kDecodeSplits = 2;
-
-template <int K>
-__global__ void k_decode_finish_split(long nst, int splits, const float *__restrict__ Cp, const float *__restrict__ b3,
-                                      const double *__restrict__ uref, const double *__restrict__ scale,
-                                      double *__restrict__ y, double *__restrict__ D, int first, const Flags *f) {
-  if (!first && f->converged) return;
-  const long row = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= nst) return;
-  // every split's row loaded before the sums (the loads in flight together)
-  float v[kDecodeSplits][K + 1];
-#pragma unroll
-  for (int z = 0; z < kDecodeSplits; ++z) {
-    const float *cz = Cp + ((long)z * nst + row) * 16;
-#pragma unroll
-    for (int j = 0; j <= K; ++j) v[z][j] = z < splits ? __ldg(cz + j) : 0.f;
-  }
-  float c[K + 1];
-#pragma unroll
-  for (int j = 0; j <= K; ++j) c[j] = 0.f;
-#pragma unroll
-  for (int z = 0; z < kDecodeSplits; ++z)
-#pragma unroll
-    for (int j = 0; j <= K; ++j)
-      if (z < splits) c[j] += v[z][j];
-  const double s = scale[row];
-  y[row] = uref[row] + s * (double)(c[0] + b3[row]);
-#pragma unroll
-  for (int j = 0; j < K; ++j) D[row * K + j] = s * (double)c[1 + j];
-}
+// tensor-core output layer: [y-part | D-part] [nst x 16] = W3b [nst x h2]
+// Zb^T (fp32), both operands in the blocked slice layout (one bulk copy per
+// 64-column slice), finished in the GEMM's epilogue: y = uref + scale (C[., 0]
+// + b3), D = scale C[., 1..k] (tc_gemm_thin_decode).
 
 // output layer at the stencil rows: one warp per row (lanes over the hidden
 // width, 8 weights in flight per lane), the [h2 | T2] block staged in shared
@@ -429,7 +398,7 @@ struct pda_lspg {
   long nst = 0, ns = 0, nSampleCells = 0;
   pda::DevBuf<int> s2st;
   pda::DevBuf<double> uref, phi, scale;
-  pda::DevBuf<float> W1, b1, W2, b2, W3, b3, Z, C;
+  pda::DevBuf<float> W1, b1, W2, b2, W3, b3, Z;
   bool tensorCore = false;
   pda::DevBuf<__nv_bfloat16> W3b, Zb;
   pda::DevBuf<double> y, D, V, J, yn, ynm1, partial, xn;
@@ -481,9 +450,14 @@ void decode_k(pda_lspg &L, const double *x, double *y, int first, cudaStream_t s
   } else if (L.tensorCore) {
     k_decode_hidden<K, 256><<<div_up(L.h2, kHiddenWarps), kHiddenWarps * 32, 0, s>>>(
         L.h2, L.W1.p, L.b1.p, L.W2.p, L.b2.p, x, L.Z.p, L.Zb.p, first, f);
-    PDA_CUDA(tc_gemm_thin_blocked(L.W3b.p, L.Zb.p, L.nst, L.h2, kDecodeSplits, L.C.p, s));
-    k_decode_finish_split<K><<<div_up(L.nst, 256), 256, 0, s>>>(L.nst, std::min(kDecodeSplits, L.h2 / 64), L.C.p,
-                                                                 L.b3.p, L.uref.p, L.scale.p, y, L.D.p, first, f);
+    tc::ThinDecode dec;
+    dec.b3 = L.b3.p;
+    dec.uref = L.uref.p;
+    dec.scale = L.scale.p;
+    dec.y = y;
+    dec.D = L.D.p;
+    dec.K = K;
+    PDA_CUDA(tc_gemm_thin_decode(L.W3b.p, L.Zb.p, L.nst, L.h2, dec, s));
   } else {
     k_decode_hidden<K, 256><<<div_up(L.h2, kHiddenWarps), kHiddenWarps * 32, 0, s>>>(
         L.h2, L.W1.p, L.b1.p, L.W2.p, L.b2.p, x, L.Z.p, nullptr, first, f);
@@ -683,7 +657,6 @@ pda_status pda_lspg_create_mlp(pda_problem *sample_problem, const int64_t *sampl
     w3rows.alloc((size_t)L->nst * h2);
     L->W3b.alloc((size_t)pda::div_up(L->nst, 128) * 128 * h2);
     L->Zb.alloc((size_t)16 * h2);
-    L->C.alloc((size_t)pda::rom::kDecodeSplits * L->nst * 16);  // split-K partial sums
     PDA_CUDA(cudaMemset(L->Zb.p, 0, (size_t)16 * h2 * sizeof(__nv_bfloat16)));
     pda::DevBuf<int> bad;
     bad.alloc(1);
@@ -696,8 +669,8 @@ pda_status pda_lspg_create_mlp(pda_problem *sample_problem, const int64_t *sampl
     PDA_REQUIRE(hb == 0, PDA_ERR_INVALID_ARGUMENT,
                 "tensor-core decoder: output-layer weights are not bf16 values (use mode 0)");
     PDA_CUDA(pda::tc_block_operand(w3rows.p, L->nst, h2, 128, L->W3b.p, nullptr));
-    // one call before any capture: sets the GEMM's shared-memory attribute
-    PDA_CUDA(pda::tc_gemm_thin_blocked(L->W3b.p, L->Zb.p, L->nst, h2, pda::rom::kDecodeSplits, L->C.p, nullptr));
+    // before any capture: the GEMM's shared-memory attribute
+    PDA_CUDA(pda::tc_gemm_thin_prepare());
     PDA_CUDA(cudaDeviceSynchronize());
   } else {
     PDA_REQUIRE(mode == 0, PDA_ERR_INVALID_ARGUMENT, "mode must be 0 (fp32) or 1 (bf16 tensor cores)");

@@ -493,7 +493,7 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
 template <int ST>
 __global__ void __launch_bounds__(THREADS)
 k_gemm_thin_blocked(const __nv_bfloat16 *__restrict__ Ablk, const __nv_bfloat16 *__restrict__ Bblk, long M, int KT,
-                    int kSlices, float *__restrict__ partial, int *__restrict__ err) {
+                    int kSlices, float *__restrict__ partial, int *__restrict__ err, const ThinDecode dec) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full[ST], empty[ST];
   __shared__ uint32_t tmem_slot;
@@ -594,7 +594,14 @@ k_gemm_thin_blocked(const __nv_bfloat16 *__restrict__ Ablk, const __nv_bfloat16 
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-    if (row < M) {
+    if (row < M && dec.y) {
+      // the decoder's output row (one K split: KTc covers all of K)
+      const double sc = dec.scale[row];
+      dec.y[row] = dec.uref[row] + sc * (double)(__uint_as_float(r[0]) + dec.b3[row]);
+#pragma unroll
+      for (int j = 0; j < 15; ++j)
+        if (j < dec.K) dec.D[row * dec.K + j] = sc * (double)__uint_as_float(r[1 + j]);
+    } else if (row < M) {
       float *pp = partial + ((long)blockIdx.y * M + row) * THIN_BN;
 #pragma unroll
       for (int j = 0; j < 16; ++j) pp[j] = KTc > 0 ? __uint_as_float(r[j]) : 0.f;

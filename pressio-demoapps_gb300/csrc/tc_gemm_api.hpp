@@ -38,6 +38,15 @@ struct MseEpi {
   // dY in the blocked operand layout with N / 64 slices instead of row-major
   bool blocked = false;
 };
+// Epilogue of the thin GEMM as the ROM decoder's output layer (one K split):
+// row r of C = [c0, c1..cK] (the layer's output and its latent derivatives)
+// becomes y[r] = uref[r] + scale[r] (c0 + b3[r]) and D[r][j] = scale[r] c(1+j).
+struct ThinDecode {
+  const float *b3 = nullptr;
+  const double *uref = nullptr, *scale = nullptr;
+  double *y = nullptr, *D = nullptr;
+  int K = 0;  // latent columns, at most 15
+};
 
 // byte offset of element (r, k) of a 64-column bf16 operand slice in the
 // canonical K-major no-swizzle layout of tcgen05: 8 x 16-byte core matrices,
@@ -95,6 +104,13 @@ cudaError_t tc_block_operand(const __nv_bfloat16 *W, long M, long K, int rowsPer
 // of K, A and B in the blocked layout (one bulk copy per slice)
 cudaError_t tc_gemm_thin_blocked(const __nv_bfloat16 *Ablk, const __nv_bfloat16 *Bblk, long M, long K, int splits,
                                  float *partial, cudaStream_t s);
+// sets the thin GEMM's shared-memory attribute on the current device (call
+// before capturing a launch of it into a graph)
+cudaError_t tc_gemm_thin_prepare();
+// the same product over the whole K in one pass per row tile, finished in
+// the epilogue as the decoder's output (ThinDecode)
+cudaError_t tc_gemm_thin_decode(const __nv_bfloat16 *Ablk, const __nv_bfloat16 *Bblk, long M, long K,
+                                const tc::ThinDecode &dec, cudaStream_t s);
 // 1 if a GEMM gave up waiting on the tensor core since the last call (clears it)
 int tc_gemm_error_and_clear();
 
