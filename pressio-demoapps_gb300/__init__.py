@@ -120,6 +120,7 @@ _SIGS = {
                                        C.POINTER(C.c_double)]),
     "pda_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double)]),
     "pda_check_divsqrt": (C.c_int, [C.c_int, C.c_uint64, C.c_int64, C.c_void_p]),
+    "pda_check_products": (C.c_int, [C.c_int, C.c_uint64, C.c_int64, C.c_void_p]),
     "pda_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_void_p, C.POINTER(C.c_void_p)]),
     "pda_batch_free": (None, [C.c_void_p]),
     "pda_batch_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int64),
@@ -548,6 +549,17 @@ def check_divsqrt(mode, seed=1, per_thread=4096):
     import numpy as np
     c = np.zeros(3, dtype=np.int64)
     _check(lib().pda_check_divsqrt(int(mode), int(seed), int(per_thread), c.ctypes.data_as(C.c_void_p)))
+    return tuple(int(v) for v in c)
+
+
+def check_products(mode, seed=1, per_thread=4096):
+    """Bit-for-bit comparison of the kernels' integer-pipe exact products
+    (3x, 5x, 7x, 11x, 13x; x/2, x/4; x + 1e-30) with the FP64 pipe's
+    operations on seeded operands; returns (operands, small-integer product
+    mismatches, power-of-two mismatches, guard mismatches)."""
+    import numpy as np
+    c = np.zeros(4, dtype=np.int64)
+    _check(lib().pda_check_products(int(mode), int(seed), int(per_thread), c.ctypes.data_as(C.c_void_p)))
     return tuple(int(v) for v in c)
 
 

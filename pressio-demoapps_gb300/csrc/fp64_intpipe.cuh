@@ -33,6 +33,10 @@
 // quotient then costs one 64x64 high product, one 128-bit product and a few
 // integer operations (quot).
 //
+// The same file holds the integer forms of the exact products (small integers,
+// powers of two) and of the density guard r + 1e-30; they are described
+// beside their code.
+//
 // The square root follows the same pattern: for normal x > 0 with 53-bit
 // mantissa MX and unbiased exponent E, N = MX * 2^(52 + (E & 1)) lies in
 // [2^104, 2^106) and sqrt(x) = sqrt(N) * 2^(floor(E / 2) - 52).  The integer
@@ -218,6 +222,70 @@ __device__ __forceinline__ double sqrt(double x) {
 // costs a few integer and move instructions, which do not touch the FP64 pipe.
 static __device__ __noinline__ double div_call(double a, double b) { return div(a, b); }
 static __device__ __noinline__ double sqrt_call(double x) { return sqrt(x); }
+
+// ---------------------------------------------------------------------------
+// Exact-by-construction products and sums on the integer pipe.
+//
+// The WENO and Rusanov expressions multiply by small integers (3, 5, 7, 11),
+// by 1/2 and 1/4, and add 1e-30 to a density.  Each of these has an IEEE
+// round-to-nearest result that integer arithmetic forms cheaply from the bit
+// pattern, so they leave the FP64 pipe to the general products and sums:
+//   * RN(K x), K a small integer: the 53-bit mantissa times K fits 57 bits;
+//     it is shifted back to 53 bits with round to nearest, ties to even
+//     (adding half a unit minus one, plus the kept part's last bit, before
+//     the shift), and a carry into bit 53 moves into the exponent field by
+//     adding the mantissa (implicit bit included) to the exponent minus one;
+//   * x * 2^-S is exact while the result stays normal: S is subtracted from
+//     the exponent field;
+//   * RN(r + 1e-30) = r whenever 1e-30 is below half a unit in the last place
+//     of r: for |r| >= 2^-44 the nearest neighbour of r lies at least 2^-97
+//     (about 6.3e-30) away on either side.
+// Operands outside these fast paths (zeros aside: zero, subnormal, huge,
+// infinite or NaN) take the ordinary FP64 operation out of line, so every
+// result is the IEEE one bit for bit.
+static __device__ __noinline__ double mul_call(double a, double b) { return a * b; }
+static __device__ __noinline__ double add_call(double a, double b) { return a + b; }
+
+// RN(K x) for an integer constant 2 < K < 16 that is not a power of two
+template <int K>
+__device__ __forceinline__ double mul_small(double x) {
+  static_assert(K > 2 && K < 16 && (K & (K - 1)) != 0, "K: a small integer that is not a power of two");
+  constexpr int KB = K >= 8 ? 3 : (K >= 4 ? 2 : 1);  // floor(log2 K)
+  const uint64_t ux = (uint64_t)__double_as_longlong(x);
+  const uint32_t ex = (uint32_t)(ux >> 52) & 0x7FFu;
+  // fast path: normal x with K x (rounded) below 2^1023 * 2: ex in [1, 0x7F9]
+  if (ex - 1u >= 0x7F9u) {
+    if ((ux << 1) == 0) return x;  // K * (+-0) = +-0
+    return mul_call(x, (double)K);
+  }
+  // P = m K in [2^(52+KB), 2^(54+KB)); s = KB or KB + 1 puts P >> s in [2^52, 2^53)
+  const uint64_t P = ((ux & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull) * (uint64_t)K;
+  const int s = (P >> (53 + KB)) != 0 ? KB + 1 : KB;
+  const uint64_t q = (P + ((1ull << (s - 1)) - 1ull) + ((P >> s) & 1ull)) >> s;  // in [2^52, 2^53]
+  return __longlong_as_double(
+      (long long)((ux & 0x8000000000000000ull) + ((uint64_t)(ex + (uint32_t)s - 1u) << 52) + q));
+}
+
+// x * 2^-S (S = 1, 2): exact for a normal result
+template <int S>
+__device__ __forceinline__ double mul_pow2_neg(double x) {
+  static_assert(S >= 1 && S <= 8, "S");
+  const uint64_t ux = (uint64_t)__double_as_longlong(x);
+  const uint32_t ex = (uint32_t)(ux >> 52) & 0x7FFu;
+  // fast path: ex in [S + 1, 0x7FE]
+  if (ex - (uint32_t)(S + 1) >= (uint32_t)(0x7FF - (S + 1))) {
+    if ((ux << 1) == 0) return x;  // +-0 * 2^-S = +-0
+    return mul_call(x, 1.0 / (double)(1 << S));
+  }
+  return __longlong_as_double((long long)(ux - ((uint64_t)S << 52)));
+}
+
+// RN(r + 1e-30)
+__device__ __forceinline__ double add_1em30(double r) {
+  const uint32_t ex = (uint32_t)((uint64_t)__double_as_longlong(r) >> 52) & 0x7FFu;
+  if (ex - 979u < 0x7FFu - 979u) return r;  // 2^-44 <= |r| < infinity
+  return add_call(r, 1.e-30);
+}
 
 #endif  // __CUDACC__
 

@@ -87,7 +87,7 @@ __device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &
   constexpr double epsilon = 1e-6;
   if constexpr (SCHEME == Weno5) {
     // center c = f0 - 2 + tx uses cells c-1, c, c+1 = sU[tx .. tx+2]
-    constexpr double oneOvfour = 1. / 4., oneOvten = 1. / 10., threeOvten = 3. / 10., sixOvten = 6. / 10.,
+    constexpr double oneOvten = 1. / 10., threeOvten = 3. / 10., sixOvten = 6. / 10.,
                      thirteenOvtwelve = 13. / 12.;
     if (tx + 2 < NCELL) {
 #pragma unroll
@@ -98,9 +98,9 @@ __device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &
         const double YL = w5_slopeL(a, m, c);
         const double YC = a - c;
         const double YR = w5_slopeR(a, m, c);
-        const double BL = D + oneOvfour * YL * YL;
-        const double BC = D + oneOvfour * YC * YC;
-        const double BR = D + oneOvfour * YR * YR;
+        const double BL = D + quarter_of(YL) * YL;
+        const double BC = D + quarter_of(YC) * YC;
+        const double BR = D + quarter_of(YR) * YR;
         const double dL = epsilon * epsilon + 2. * epsilon * BL + BL * BL;
         const double dC = epsilon * epsilon + 2. * epsilon * BC + BC * BC;
         const double dR = epsilon * epsilon + 2. * epsilon * BR + BR * BR;
@@ -154,15 +154,15 @@ __device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &
       }
     }
   } else {
-    constexpr double three = 3., oneOvtwo = 1. / 2.;
+    // p0 = (-q_{i-1} + 3 q_i) / 2, p1 = (q_i + q_{i+1}) / 2, p2 = (3 q_{i+1} - q_{i+2}) / 2
 #pragma unroll
     for (int d = 0; d < NDPC; ++d) {
       // left cell i = f-1: cells i-1..i+2 = sU[tx .. tx+3]; pairs i-1, i, i+1 = sA[.][tx .. tx+2]
       const double qim1 = sU[ty][d][tx], qi = sU[ty][d][tx + 1], qip1 = sU[ty][d][tx + 2],
                    qip2 = sU[ty][d][tx + 3];
-      const double p0 = (-qim1 + three * qi) * oneOvtwo;
-      const double p1 = (qi + qip1) * oneOvtwo;
-      const double p2 = (three * qip1 - qip2) * oneOvtwo;
+      const double p0 = half_of(-qim1 + mul_k<3>(qi));
+      const double p1 = half_of(qi + qip1);
+      const double p2 = half_of(mul_k<3>(qip1) - qip2);
       {
         const double a0 = sA[ty][d][0][tx], a1 = sA[ty][d][1][tx + 1];
         const double s = div_rn<true>(1., (a0 + a1));

@@ -1,6 +1,6 @@
 // Element-wise stepper updates, the CSR sparse x dense product, the FP64
-// throughput probe and the self-check of the integer-pipe division and
-// square root.
+// throughput probe and the self-checks of the integer-pipe division, square
+// root and exact products.
 #include "fp64_intpipe.cuh"
 #include "launch.hpp"
 
@@ -111,6 +111,54 @@ __global__ void k_check_divsqrt(int mode, uint64_t seed, long per_thread, unsign
   atomicAdd(bad + 1, ns);
 }
 
+// Operand sets for the comparison of the integer-pipe exact products
+// (ip::mul_small<K>, ip::mul_pow2_neg<S>, ip::add_1em30) with the FP64
+// pipe's operations.  mode 0: random mantissas, exponents within 2^-60..2^60;
+// 1: exponents at the edges of the fast paths (subnormal results of the
+// halvings, near-overflow products, the 2^-44 bound of the density guard)
+// and short mantissas (exact products and rounding ties); 2: mantissas
+// within 64 units of 1 and of 2 - 2^-52; 3: arbitrary bit patterns (zeros,
+// subnormals, infinities, NaNs included).
+__device__ __forceinline__ bool same_bits(double a, double b) {
+  return __double_as_longlong(a) == __double_as_longlong(b) || (a != a && b != b);
+}
+
+__global__ void k_check_products(int mode, uint64_t seed, long per_thread, unsigned long long *bad) {
+  uint64_t st = seed ^ ((uint64_t)(blockIdx.x * blockDim.x + threadIdx.x) * 0x9E6C63D0676A9A99ull);
+  unsigned long long nk = 0, np = 0, ne = 0;
+  constexpr uint64_t M = 0x000FFFFFFFFFFFFFull;
+  for (long k = 0; k < per_thread; ++k) {
+    const uint64_t r1 = splitmix64(st), r2 = splitmix64(st);
+    uint64_t ux;
+    if (mode == 0) {
+      ux = (r1 & M) | ((uint64_t)(1023 - 60 + (int)(r2 % 121)) << 52) | (r2 & (1ull << 63));
+    } else if (mode == 1) {
+      static const int edges[] = {0, 1, 2, 3, 4, 0x7F5, 0x7F6, 0x7F7, 0x7F8, 0x7F9, 0x7FA, 0x7FB, 0x7FE, 0x7FF,
+                                  975, 976, 977, 978, 979, 980, 981, 1023};
+      const int e = edges[(r2 >> 8) % (sizeof(edges) / sizeof(edges[0]))];
+      const uint64_t m = (r2 & 1) ? (r1 & M & ~((1ull << 40) - 1)) : (r1 & M);
+      ux = m | ((uint64_t)e << 52) | (r2 & (1ull << 63));
+    } else if (mode == 2) {
+      const uint64_t m = (r2 & 1) ? (M - (r2 >> 1) % 64) : ((r2 >> 1) % 64);
+      ux = m | ((uint64_t)(1000 + (r1 % 48)) << 52) | (r1 & (1ull << 63));
+    } else {
+      ux = r1;
+    }
+    const double x = __longlong_as_double((long long)ux);
+    nk += !same_bits(x * 3., ip::mul_small<3>(x));
+    nk += !same_bits(x * 5., ip::mul_small<5>(x));
+    nk += !same_bits(x * 7., ip::mul_small<7>(x));
+    nk += !same_bits(x * 11., ip::mul_small<11>(x));
+    nk += !same_bits(x * 13., ip::mul_small<13>(x));
+    np += !same_bits(x * 0.5, ip::mul_pow2_neg<1>(x));
+    np += !same_bits(x * 0.25, ip::mul_pow2_neg<2>(x));
+    ne += !same_bits(x + 1.e-30, ip::add_1em30(x));
+  }
+  atomicAdd(bad, nk);
+  atomicAdd(bad + 1, np);
+  atomicAdd(bad + 2, ne);
+}
+
 }  // namespace
 
 void check_divsqrt(int mode, uint64_t seed, long per_thread, long long counts[3], cudaStream_t s) {
@@ -129,6 +177,25 @@ void check_divsqrt(int mode, uint64_t seed, long per_thread, long long counts[3]
   counts[0] = (long long)blocks * threads * per_thread;
   counts[1] = (long long)h[0];
   counts[2] = (long long)h[1];
+}
+
+void check_products(int mode, uint64_t seed, long per_thread, long long counts[4], cudaStream_t s) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  unsigned long long *bad = nullptr;
+  cudaMalloc((void **)&bad, 3 * sizeof(unsigned long long));
+  cudaMemsetAsync(bad, 0, 3 * sizeof(unsigned long long), s);
+  const int blocks = (sms > 0 ? sms : 1) * 8, threads = 256;
+  k_check_products<<<blocks, threads, 0, s>>>(mode, seed, per_thread, bad);
+  unsigned long long h[3] = {0, 0, 0};
+  cudaMemcpyAsync(h, bad, sizeof(h), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  cudaFree(bad);
+  counts[0] = (long long)blocks * threads * per_thread;
+  counts[1] = (long long)h[0];
+  counts[2] = (long long)h[1];
+  counts[3] = (long long)h[2];
 }
 
 double measure_fp64_fma_rate(int blocks, int threads, int iters, cudaStream_t s) {
