@@ -431,16 +431,17 @@ pda_status pda_measure_fp64_peak(double *flops_per_s);
  * counterpart in the reference (whose divisions are the CPU's). */
 pda_status pda_check_divsqrt(int mode, uint64_t seed, int64_t per_thread, int64_t counts[3]);
 
-/* Self-check of the integer-pipe forms of the exact products the kernels use
- * (K x for K = 3, 5, 7, 11, 13; x / 2 and x / 4; the density guard
- * x + 1e-30): on (SMs x 2048 threads) x per_thread seeded operands of the
- * given mode (0 normal range, 1 exponents at the edges of the fast paths and
- * short mantissas, 2 mantissas near the ends of [1, 2), 3 arbitrary bit
- * patterns), compares each result with the FP64 pipe's operation bit for
- * bit.  counts receives {operands, small-integer product mismatches,
- * power-of-two mismatches, guard mismatches}.  No counterpart in the
- * reference. */
-pda_status pda_check_products(int mode, uint64_t seed, int64_t per_thread, int64_t counts[4]);
+/* Self-check of the integer-pipe forms of the products by constants the
+ * kernels use (K x for K = 3, 5, 7, 11, 13; x / 2 and x / 4; x c for
+ * literals c such as 1/6, 13/12, 2e-6) and of the density guard x + 1e-30:
+ * on (SMs x 2048 threads) x per_thread seeded operands of the given mode
+ * (0 normal range, 1 exponents at the edges of the fast paths and short
+ * mantissas, 2 mantissas near the ends of [1, 2), 3 arbitrary bit patterns),
+ * compares each result with the FP64 pipe's operation bit for bit.  counts
+ * receives {operands, small-integer product mismatches, power-of-two
+ * mismatches, guard mismatches, constant product mismatches}.  No
+ * counterpart in the reference. */
+pda_status pda_check_products(int mode, uint64_t seed, int64_t per_thread, int64_t counts[5]);
 
 #ifdef __cplusplus
 }

@@ -553,12 +553,14 @@ def check_divsqrt(mode, seed=1, per_thread=4096):
 
 
 def check_products(mode, seed=1, per_thread=4096):
-    """Bit-for-bit comparison of the kernels' integer-pipe exact products
-    (3x, 5x, 7x, 11x, 13x; x/2, x/4; x + 1e-30) with the FP64 pipe's
-    operations on seeded operands; returns (operands, small-integer product
-    mismatches, power-of-two mismatches, guard mismatches)."""
+    """Bit-for-bit comparison of the kernels' integer-pipe products by
+    constants (3x, 5x, 7x, 11x, 13x; x/2, x/4; x c for literals c) and
+    density guard (x + 1e-30) with the FP64 pipe's operations on seeded
+    operands; returns (operands, small-integer product mismatches,
+    power-of-two mismatches, guard mismatches, constant product
+    mismatches)."""
     import numpy as np
-    c = np.zeros(4, dtype=np.int64)
+    c = np.zeros(5, dtype=np.int64)
     _check(lib().pda_check_products(int(mode), int(seed), int(per_thread), c.ctypes.data_as(C.c_void_p)))
     return tuple(int(v) for v in c)
 

@@ -52,15 +52,16 @@ void faces_s(const Box &b, const Phys &p, const double *U, double *Fo, cudaStrea
       k_struct_faces<FAM, SCHEME, AXIS><<<div_up(nf, 128), 128, 0, s>>>(b, p, U, Fo);
     } else {
       // tiled kernel: lines of the other two axes in grid x, face chunks in grid y
-      constexpr int NR = 2;
-      using Cfg = TileCfg<SCHEME>;
+      // 64 x 2 threads: measured against 128 x 1, 128 x 2 and 32 x 4
+      constexpr int NR = 2, LANES = 64;
+      using Cfg = TileCfg<SCHEME, LANES>;
       long lines = 1;
       for (int a = 0; a < 3; ++a)
         if (a != AXIS) lines *= (long)(b.hi[a] - b.lo[a]);
       const int nfa = b.hi[AXIS] - b.lo[AXIS] + 1;
       dim3 grid(div_up(lines, NR), div_up(nfa, Cfg::TW));
       dim3 block(Cfg::LANES, NR);
-      k_faces_tile<FAM, SCHEME, AXIS, NR><<<grid, block, 0, s>>>(b, p, U, Fo);
+      k_faces_tile<FAM, SCHEME, AXIS, NR, LANES><<<grid, block, 0, s>>>(b, p, U, Fo);
     }
     ++*launches;
   }

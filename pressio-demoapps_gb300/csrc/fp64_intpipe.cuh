@@ -33,9 +33,9 @@
 // quotient then costs one 64x64 high product, one 128-bit product and a few
 // integer operations (quot).
 //
-// The same file holds the integer forms of the exact products (small integers,
-// powers of two) and of the density guard r + 1e-30; they are described
-// beside their code.
+// The same file holds the integer forms of the correctly rounded products by
+// constants (small integers, powers of two, literals such as 1/6) and of the
+// density guard r + 1e-30; they are described beside their code.
 //
 // The square root follows the same pattern: for normal x > 0 with 53-bit
 // mantissa MX and unbiased exponent E, N = MX * 2^(52 + (E & 1)) lies in
@@ -50,6 +50,18 @@
 #include <stdint.h>
 
 namespace pda {
+
+// several quotients by one divisor (the divisor's reciprocal formed once)
+struct Quot2 {
+  double q0, q1;
+};
+struct Quot3 {
+  double q0, q1, q2;
+};
+struct Quot4 {
+  double q0, q1, q2, q3;
+};
+
 namespace ip {
 
 #if defined(__CUDACC__)
@@ -155,6 +167,18 @@ __device__ __forceinline__ double quot(double a, const Den &D) {
 }
 
 __device__ __forceinline__ double div(double a, double b) { return quot(a, den_prep(b)); }
+__device__ __forceinline__ Quot2 div2(double a0, double a1, double b) {
+  const Den D = den_prep(b);
+  return {quot(a0, D), quot(a1, D)};
+}
+__device__ __forceinline__ Quot3 div3(double a0, double a1, double a2, double b) {
+  const Den D = den_prep(b);
+  return {quot(a0, D), quot(a1, D), quot(a2, D)};
+}
+__device__ __forceinline__ Quot4 div4(double a0, double a1, double a2, double a3, double b) {
+  const Den D = den_prep(b);
+  return {quot(a0, D), quot(a1, D), quot(a2, D), quot(a3, D)};
+}
 
 __device__ __forceinline__ float rsqrt_seed_f32(float x) {
   float r;
@@ -222,14 +246,28 @@ __device__ __forceinline__ double sqrt(double x) {
 // costs a few integer and move instructions, which do not touch the FP64 pipe.
 static __device__ __noinline__ double div_call(double a, double b) { return div(a, b); }
 static __device__ __noinline__ double sqrt_call(double x) { return sqrt(x); }
+// Several quotients by one divisor, out of line: one division call per
+// quotient.  A call that returns one double keeps its result in registers;
+// sharing the reciprocal through a call that returns two or more quotients
+// (or stores them) measured slower in the face kernels, and so did forming
+// the reciprocal out of line with the quotients in place (more code).
+__device__ __forceinline__ Quot2 div2_call(double a0, double a1, double b) { return {div_call(a0, b), div_call(a1, b)}; }
+__device__ __forceinline__ Quot3 div3_call(double a0, double a1, double a2, double b) {
+  return {div_call(a0, b), div_call(a1, b), div_call(a2, b)};
+}
+__device__ __forceinline__ Quot4 div4_call(double a0, double a1, double a2, double a3, double b) {
+  return {div_call(a0, b), div_call(a1, b), div_call(a2, b), div_call(a3, b)};
+}
 
 // ---------------------------------------------------------------------------
 // Exact-by-construction products and sums on the integer pipe.
 //
 // The WENO and Rusanov expressions multiply by small integers (3, 5, 7, 11),
-// by 1/2 and 1/4, and add 1e-30 to a density.  Each of these has an IEEE
-// round-to-nearest result that integer arithmetic forms cheaply from the bit
-// pattern, so they leave the FP64 pipe to the general products and sums:
+// by 1/2 and 1/4, by constants (1/6, 13/12, 2e-6), and add 1e-30 to a
+// density.  Each of these has an IEEE round-to-nearest result that integer
+// arithmetic forms from the bit pattern at a fraction of an FP64
+// instruction's cost on GB300, so they leave the FP64 pipe to the products
+// and sums of two variables:
 //   * RN(K x), K a small integer: the 53-bit mantissa times K fits 57 bits;
 //     it is shifted back to 53 bits with round to nearest, ties to even
 //     (adding half a unit minus one, plus the kept part's last bit, before
@@ -264,6 +302,38 @@ __device__ __forceinline__ double mul_small(double x) {
   const uint64_t q = (P + ((1ull << (s - 1)) - 1ull) + ((P >> s) & 1ull)) >> s;  // in [2^52, 2^53]
   return __longlong_as_double(
       (long long)((ux & 0x8000000000000000ull) + ((uint64_t)(ex + (uint32_t)s - 1u) << 52) + q));
+}
+
+// RN(x c) for a positive normal constant c (a literal: its mantissa and
+// exponent fold at compile time).  With 53-bit mantissas MX, MC, the product
+// P = MX MC lies in [2^104, 2^106); a = MX 2^11 and b = MC 2^11 give
+// hi = floor(a b / 2^64) = floor(P / 2^42) exactly, the low word a b mod 2^64
+// is zero exactly when P mod 2^42 is, so the 53 kept bits, the bits below
+// them and the sticky bit are all known: round to nearest, ties to even.
+__device__ __forceinline__ double mul_const(double x, const double c) {
+  const uint64_t uc = (uint64_t)__double_as_longlong(c);
+  const int ec = (int)((uc >> 52) & 0x7FF);
+  const uint64_t b = ((uc & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull) << 11;
+  const uint64_t ux = (uint64_t)__double_as_longlong(x);
+  const int ex = (int)((ux >> 52) & 0x7FF);
+  const int er = ex + ec - 1023;  // biased exponent of the result when P < 2^105
+  // fast path: x normal and the result normal and finite: er in [1, 0x7FC]
+  if (ex == 0 || ex == 0x7FF || er < 1 || er > 0x7FC) {
+    if ((ux << 1) == 0) return x;  // +-0 * c = +-0 for c > 0
+    return mul_call(x, c);
+  }
+  const uint64_t a = ((ux & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull) << 11;
+  const uint64_t hi = __umul64hi(a, b);  // in [2^62, 2^64)
+  const uint64_t lo = a * b;
+  const int top = (int)(hi >> 63);  // P >= 2^105
+  const int sh = 10 + top;
+  const uint64_t m = hi >> sh;                      // the 53 kept bits
+  const uint64_t rest = hi & ((1ull << sh) - 1ull);  // the bits of hi below them
+  const uint64_t half = 1ull << (sh - 1);
+  const bool up = rest > half || (rest == half && (lo != 0 || (m & 1ull)));
+  const uint64_t q = m + (up ? 1ull : 0ull);  // in [2^52, 2^53]
+  return __longlong_as_double(
+      (long long)((ux & 0x8000000000000000ull) + ((uint64_t)(er + top - 1) << 52) + q));
 }
 
 // x * 2^-S (S = 1, 2): exact for a normal result

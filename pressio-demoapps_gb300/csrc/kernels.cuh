@@ -27,9 +27,9 @@ namespace pda {
 template <int FAM> struct Fam;
 template <> struct Fam<Euler1d> {
   static constexpr int dim = 1, ndpc = 3;
-  template <int AXIS, bool INL = false>
+  template <int AXIS, bool INL = false, bool IP = false>
   static PDA_HD void flux(double F[3], const double qL[3], const double qR[3], const Phys &p) {
-    euler3_flux<INL>(F, qL, qR, p.gamma);
+    euler3_flux<INL, IP>(F, qL, qR, p.gamma);
   }
   template <int AXIS, typename T>
   static PDA_HD void flux_jac(T JL[9], T JR[9], const T qL[3], const T qR[3], const Phys &p) {
@@ -49,9 +49,9 @@ template <> struct Fam<Euler1d> {
 };
 template <> struct Fam<Euler2d> {
   static constexpr int dim = 2, ndpc = 4;
-  template <int AXIS, bool INL = false>
+  template <int AXIS, bool INL = false, bool IP = false>
   static PDA_HD void flux(double F[4], const double qL[4], const double qR[4], const Phys &p) {
-    euler4_flux<AXIS, INL>(F, qL, qR, p.gamma);
+    euler4_flux<AXIS, INL, IP>(F, qL, qR, p.gamma);
   }
   template <int AXIS, typename T>
   static PDA_HD void flux_jac(T JL[16], T JR[16], const T qL[4], const T qR[4], const Phys &p) {
@@ -71,9 +71,9 @@ template <> struct Fam<Euler2d> {
 };
 template <> struct Fam<Euler3d> {
   static constexpr int dim = 3, ndpc = 5;
-  template <int AXIS, bool INL = false>
+  template <int AXIS, bool INL = false, bool IP = false>
   static PDA_HD void flux(double F[5], const double qL[5], const double qR[5], const Phys &p) {
-    euler5_flux<AXIS, INL>(F, qL, qR, p.gamma);
+    euler5_flux<AXIS, INL, IP>(F, qL, qR, p.gamma);
   }
   template <int AXIS, typename T>
   static PDA_HD void flux_jac(T JL[25], T JR[25], const T qL[5], const T qR[5], const Phys &p) {
@@ -93,9 +93,9 @@ template <> struct Fam<Euler3d> {
 };
 template <> struct Fam<Swe2d> {
   static constexpr int dim = 2, ndpc = 3;
-  template <int AXIS, bool INL = false>
+  template <int AXIS, bool INL = false, bool IP = false>
   static PDA_HD void flux(double F[3], const double qL[3], const double qR[3], const Phys &p) {
-    swe_flux<AXIS, INL>(F, qL, qR, p.gravity);
+    swe_flux<AXIS, INL, IP>(F, qL, qR, p.gravity);
   }
   template <int AXIS, typename T>
   static PDA_HD void flux_jac(T JL[9], T JR[9], const T qL[3], const T qR[3], const Phys &p) {

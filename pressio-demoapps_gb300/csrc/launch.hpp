@@ -64,7 +64,7 @@ void launch_axpby_stage(int kind, double *out, const double *a, const double *b,
 double measure_fp64_fma_rate(int blocks, int threads, int iters, cudaStream_t s);
 // counts = {operand sets, division mismatches, square-root mismatches}
 void check_divsqrt(int mode, uint64_t seed, long per_thread, long long counts[3], cudaStream_t s);
-void check_products(int mode, uint64_t seed, long per_thread, long long counts[4], cudaStream_t s);
+void check_products(int mode, uint64_t seed, long per_thread, long long counts[5], cudaStream_t s);
 void launch_csr_spmm(long rows, const int *rowptr, const int *colidx, const double *vals,
                      const double *B, long ldb, int ncols, double *R, long ldr, cudaStream_t s);
 

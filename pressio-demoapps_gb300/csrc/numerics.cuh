@@ -71,13 +71,42 @@ PDA_HD double sqrt_rn(double x) {
   return sqrt(x);
 #endif
 }
+// Several quotients by one divisor: the same IEEE quotients as div_rn, with
+// the divisor's reciprocal formed once on the device.
+template <bool INL = false>
+PDA_HD Quot2 div2_rn(double a0, double a1, double b) {
+#if defined(__CUDA_ARCH__) && !defined(PDA_FP64_PIPE_DIVSQRT)
+  if constexpr (INL) return ip::div2(a0, a1, b);
+  else return ip::div2_call(a0, a1, b);
+#else
+  return {a0 / b, a1 / b};
+#endif
+}
+template <bool INL = false>
+PDA_HD Quot3 div3_rn(double a0, double a1, double a2, double b) {
+#if defined(__CUDA_ARCH__) && !defined(PDA_FP64_PIPE_DIVSQRT)
+  if constexpr (INL) return ip::div3(a0, a1, a2, b);
+  else return ip::div3_call(a0, a1, a2, b);
+#else
+  return {a0 / b, a1 / b, a2 / b};
+#endif
+}
+template <bool INL = false>
+PDA_HD Quot4 div4_rn(double a0, double a1, double a2, double a3, double b) {
+#if defined(__CUDA_ARCH__) && !defined(PDA_FP64_PIPE_DIVSQRT)
+  if constexpr (INL) return ip::div4(a0, a1, a2, a3, b);
+  else return ip::div4_call(a0, a1, a2, a3, b);
+#else
+  return {a0 / b, a1 / b, a2 / b, a3 / b};
+#endif
+}
 template <bool INL = false>
 PDA_HD float div_rn(float a, float b) { return a / b; }
 template <bool INL = false>
 PDA_HD float sqrt_rn(float x) { return sqrtf(x); }
 
-// The reference's products by small integers (K x), by 1/2 and 1/4, and its
-// density guard r + 1e-30.  Device code forms the double results on the
+// The reference's products by small integers (K x), by 1/2 and 1/4, by
+// constants, and its density guard r + 1e-30.  Device code forms the double results on the
 // integer pipe (fp64_intpipe.cuh: the IEEE round-to-nearest values, bit for
 // bit); host code and single precision use the operators.
 template <int K, typename T>
@@ -101,6 +130,14 @@ PDA_HD T quarter_of(T x) {
 #endif
   return T(1. / 4.) * x;
 }
+// RN(c x) for a positive literal constant c (1/6, 13/12, 2e-6)
+PDA_HD double mul_c(double x, double c) {
+#if defined(__CUDA_ARCH__) && !defined(PDA_FP64_PIPE_DIVSQRT)
+  return ip::mul_const(x, c);
+#else
+  return c * x;
+#endif
+}
 PDA_HD double plus_es(double r) {
 #if defined(__CUDA_ARCH__) && !defined(PDA_FP64_PIPE_DIVSQRT)
   return ip::add_1em30(r);
@@ -108,6 +145,26 @@ PDA_HD double plus_es(double r) {
   return r + 1.e-30;
 #endif
 }
+// Selectable forms of the above: IP = true forms the exact products on the
+// integer pipe (the tile kernels of the residual, where that pays); IP = false
+// keeps the FP64 operations (row, Jacobian and reduced-order kernels, where
+// the extra integer code measured slower).  Both give the same bits.
+template <bool IP, int K, typename T>
+PDA_HD T kx(T x) {
+  if constexpr (IP) return mul_k<K>(x);
+  else return T(K) * x;
+}
+template <bool IP, typename T>
+PDA_HD T halfx(T x) {
+  if constexpr (IP) return half_of(x);
+  else return T(1. / 2.) * x;
+}
+template <bool IP>
+PDA_HD double esx(double r) {
+  if constexpr (IP) return plus_es(r);
+  else return r + 1.e-30;
+}
+
 
 template <typename T> PDA_HD T sq(T x) { return x * x; }
 // x^3 for the reference's std::pow(x, 3.) (glibc pow, correctly rounded in
@@ -163,20 +220,20 @@ PDA_HD T add_table_prod(T x, T k, T w) { return k == T(0.) ? fma(k, w, x) : x + 
 //   w5_pMidL(a, b, c)  = -a + 5 b + 2 c
 //   w5_pMidR(a, b, c)  = 2 a + 5 b - c
 //   w5_pFarR(a, b, c)  = 11 a - 7 b + 2 c
-template <typename T>
+template <bool IP = false, typename T>
 PDA_HD T w5_curv(T a, T m, T c) { return fma_p2(-T(2.), m, a) + c; }
-template <typename T>
-PDA_HD T w5_slopeL(T a, T m, T c) { return fma_p2(-T(4.), m, a) + mul_k<3>(c); }
-template <typename T>
-PDA_HD T w5_slopeR(T a, T m, T c) { return fma_p2(-T(4.), m, mul_k<3>(a)) + c; }
-template <typename T>
-PDA_HD T w5_pFarL(T a, T b, T c) { return fma_p2(T(2.), a, -mul_k<7>(b)) + mul_k<11>(c); }
-template <typename T>
-PDA_HD T w5_pMidL(T a, T b, T c) { return fma_p2(T(2.), c, -a + mul_k<5>(b)); }
-template <typename T>
-PDA_HD T w5_pMidR(T a, T b, T c) { return fma_p2(T(2.), a, mul_k<5>(b)) - c; }
-template <typename T>
-PDA_HD T w5_pFarR(T a, T b, T c) { return fma_p2(T(2.), c, mul_k<11>(a) - mul_k<7>(b)); }
+template <bool IP = false, typename T>
+PDA_HD T w5_slopeL(T a, T m, T c) { return fma_p2(-T(4.), m, a) + kx<IP, 3>(c); }
+template <bool IP = false, typename T>
+PDA_HD T w5_slopeR(T a, T m, T c) { return fma_p2(-T(4.), m, kx<IP, 3>(a)) + c; }
+template <bool IP = false, typename T>
+PDA_HD T w5_pFarL(T a, T b, T c) { return fma_p2(T(2.), a, -kx<IP, 7>(b)) + kx<IP, 11>(c); }
+template <bool IP = false, typename T>
+PDA_HD T w5_pMidL(T a, T b, T c) { return fma_p2(T(2.), c, -a + kx<IP, 5>(b)); }
+template <bool IP = false, typename T>
+PDA_HD T w5_pMidR(T a, T b, T c) { return fma_p2(T(2.), a, kx<IP, 5>(b)) - c; }
+template <bool IP = false, typename T>
+PDA_HD T w5_pFarR(T a, T b, T c) { return fma_p2(T(2.), c, kx<IP, 11>(a) - kx<IP, 7>(b)); }
 
 // ---------------------------------------------------------------------------
 // WENO5, one face i+1/2: uNeg from q_{i-2..i+2}, uPos from q_{i-1..i+3}.
@@ -197,9 +254,9 @@ PDA_HD double weno5_neg(double qim2, double qim1, double qi, double qip1, double
     const double X0 = w5_curv(qim2, qim1, qi), Y0 = w5_slopeL(qim2, qim1, qi);
     const double X1 = w5_curv(qim1, qi, qip1), Y1 = qim1 - qip1;
     const double X2 = w5_curv(qi, qip1, qip2), Y2 = w5_slopeR(qi, qip1, qip2);
-    const double B0 = thirteenOvtwelve * X0 * X0 + quarter_of(Y0) * Y0;
-    const double B1 = thirteenOvtwelve * X1 * X1 + quarter_of(Y1) * Y1;
-    const double B2 = thirteenOvtwelve * X2 * X2 + quarter_of(Y2) * Y2;
+    const double B0 = thirteenOvtwelve * X0 * X0 + oneOvfour * Y0 * Y0;
+    const double B1 = thirteenOvtwelve * X1 * X1 + oneOvfour * Y1 * Y1;
+    const double B2 = thirteenOvtwelve * X2 * X2 + oneOvfour * Y2 * Y2;
     const double alpha0 = div_rn(oneOvten, (epsilon * epsilon + 2. * epsilon * B0 + B0 * B0));
     const double alpha1 = div_rn(sixOvten, (epsilon * epsilon + 2. * epsilon * B1 + B1 * B1));
     const double alpha2 = div_rn(threeOvten, (epsilon * epsilon + 2. * epsilon * B2 + B2 * B2));
@@ -228,9 +285,9 @@ PDA_HD double weno5_pos(double qim1, double qi, double qip1, double qip2, double
     const double X0 = w5_curv(qim1, qi, qip1), Y0 = w5_slopeL(qim1, qi, qip1);
     const double X1 = w5_curv(qi, qip1, qip2), Y1 = qi - qip2;
     const double X2 = w5_curv(qip1, qip2, qip3), Y2 = w5_slopeR(qip1, qip2, qip3);
-    const double B0 = thirteenOvtwelve * X0 * X0 + quarter_of(Y0) * Y0;
-    const double B1 = thirteenOvtwelve * X1 * X1 + quarter_of(Y1) * Y1;
-    const double B2 = thirteenOvtwelve * X2 * X2 + quarter_of(Y2) * Y2;
+    const double B0 = thirteenOvtwelve * X0 * X0 + oneOvfour * Y0 * Y0;
+    const double B1 = thirteenOvtwelve * X1 * X1 + oneOvfour * Y1 * Y1;
+    const double B2 = thirteenOvtwelve * X2 * X2 + oneOvfour * Y2 * Y2;
     const double alpha0 = div_rn(threeOvten, (epsilon * epsilon + 2. * epsilon * B0 + B0 * B0));
     const double alpha1 = div_rn(sixOvten, (epsilon * epsilon + 2. * epsilon * B1 + B1 * B1));
     const double alpha2 = div_rn(oneOvten, (epsilon * epsilon + 2. * epsilon * B2 + B2 * B2));
@@ -268,11 +325,11 @@ PDA_HD void weno5_neg_grad(T &uNeg, T gNeg[6], T qim2, T qim1, T qi, T qip1, T q
     const T dp1[5] = {T(0.), -T(1.) / T(6.), T(5.) / T(6.), T(1.) / T(3.), T(0.)};
     const T dp2[5] = {T(0.), T(0.), T(1.) / T(3.), T(5.) / T(6.), -T(1.) / T(6.)};
     const T B0 = thirteenOvtwelve * sq(w5_curv(qim2, qim1, qi)) +
-                      quarter_of(sq(w5_slopeL(qim2, qim1, qi)));
+                      oneOvfour * sq(w5_slopeL(qim2, qim1, qi));
     const T B1 = thirteenOvtwelve * sq(w5_curv(qim1, qi, qip1)) +
-                      quarter_of(sq(qim1 - qip1));
+                      oneOvfour * sq(qim1 - qip1);
     const T B2 = thirteenOvtwelve * sq(w5_curv(qi, qip1, qip2)) +
-                      quarter_of(sq(w5_slopeR(qi, qip1, qip2)));
+                      oneOvfour * sq(w5_slopeR(qi, qip1, qip2));
     // derivative terms (impl/weno5.hpp:294-310), the products by 2 and 1/2 fused
     const T X0 = T(13.) * w5_curv(qim2, qim1, qi), Y0 = w5_slopeL(qim2, qim1, qi);
     const T X1 = T(13.) * fma_p2(-T(2.), qi, qip1 + qim1), Y1 = qim1 - qip1;
@@ -336,11 +393,11 @@ PDA_HD void weno5_pos_grad(T &uPos, T gPos[6], T qim2, T qim1, T qi, T qip1, T q
     const T dp1[5] = {T(0.), T(1.) / T(3.), T(5.) / T(6.), -T(1.) / T(6.), T(0.)};
     const T dp2[5] = {T(0.), T(0.), T(11.) / T(6.), -T(7.) / T(6.), T(1.) / T(3.)};
     const T B0 = thirteenOvtwelve * sq(w5_curv(qim1, qi, qip1)) +
-                      quarter_of(sq(w5_slopeL(qim1, qi, qip1)));
+                      oneOvfour * sq(w5_slopeL(qim1, qi, qip1));
     const T B1 = thirteenOvtwelve * sq(w5_curv(qi, qip1, qip2)) +
-                      quarter_of(sq(qi - qip2));
+                      oneOvfour * sq(qi - qip2);
     const T B2 = thirteenOvtwelve * sq(w5_curv(qip1, qip2, qip3)) +
-                      quarter_of(sq(w5_slopeR(qip1, qip2, qip3)));
+                      oneOvfour * sq(w5_slopeR(qip1, qip2, qip3));
     // derivative terms (impl/weno5.hpp:385-401), the products by 2, 4 and 1/2 fused
     const T X0 = T(13.) * fma_p2(-T(2.), qi, qip1 + qim1), Y0 = fma_p2(-T(4.), qi, T(3.) * qip1 + qim1);
     const T X1 = T(13.) * w5_curv(qip2, qip1, qi), Y1 = qi - qip2;
@@ -404,8 +461,8 @@ PDA_HD double weno3_neg(double qim1, double qi, double qip1) {
   constexpr double oneOvtwo = 1. / 2., oneOvthree = 1. / 3., twoOvthree = 2. / 3.;
   double uNeg;
   {
-    const double p0 = half_of(-qim1 + mul_k<3>(qi));
-    const double p1 = half_of(qi + qip1);
+    const double p0 = (-qim1 + three * qi) * oneOvtwo;
+    const double p1 = (qi + qip1) * oneOvtwo;
     const double B0 = (qim1 - qi) * (qim1 - qi);
     const double B1 = (qi - qip1) * (qi - qip1);
     const double alpha0 = div_rn(oneOvthree, (epsilon * epsilon + two * epsilon * B0 + B0 * B0));
@@ -425,8 +482,8 @@ PDA_HD double weno3_pos(double qi, double qip1, double qip2) {
   constexpr double oneOvtwo = 1. / 2., oneOvthree = 1. / 3., twoOvthree = 2. / 3.;
   double uPos;
   {
-    const double p0 = half_of(qi + qip1);
-    const double p1 = half_of(mul_k<3>(qip1) - qip2);
+    const double p0 = (qi + qip1) * oneOvtwo;
+    const double p1 = (three * qip1 - qip2) * oneOvtwo;
     const double B0 = (qi - qip1) * (qi - qip1);
     const double B1 = (qip1 - qip2) * (qip1 - qip2);
     const double alpha0 = div_rn(twoOvthree, (epsilon * epsilon + two * epsilon * B0 + B0 * B0));
@@ -453,8 +510,8 @@ PDA_HD void weno3_neg_grad(T &uNeg, T gNeg[4], T qim1, T qi, T qip1, T qip2) {
   constexpr T two = T(2.), three = T(3.);
   constexpr T oneOvtwo = T(1.) / T(2.), oneOvthree = T(1.) / T(3.), twoOvthree = T(2.) / T(3.);
   {
-    const T p0 = half_of(-qim1 + mul_k<3>(qi));
-    const T p1 = half_of(qi + qip1);
+    const T p0 = (-qim1 + three * qi) * oneOvtwo;
+    const T p1 = (qi + qip1) * oneOvtwo;
     const T dp0[3] = {-T(1.) / T(2.), T(3.) / T(2.), T(0.)};
     const T dp1[3] = {T(0.), T(1.) / T(2.), T(1.) / T(2.)};
     const T B0 = (qim1 - qi) * (qim1 - qi);
@@ -494,8 +551,8 @@ PDA_HD void weno3_pos_grad(T &uPos, T gPos[4], T qim1, T qi, T qip1, T qip2) {
   constexpr T two = T(2.), three = T(3.);
   constexpr T oneOvtwo = T(1.) / T(2.), oneOvthree = T(1.) / T(3.), twoOvthree = T(2.) / T(3.);
   {
-    const T p0 = half_of(qi + qip1);
-    const T p1 = half_of(mul_k<3>(qip1) - qip2);
+    const T p0 = (qi + qip1) * oneOvtwo;
+    const T p1 = (three * qip1 - qip2) * oneOvtwo;
     const T B0 = (qi - qip1) * (qi - qip1);
     const T B1 = (qip1 - qip2) * (qip1 - qip2);
     const T alpha0 = div_rn(twoOvthree, (epsilon * epsilon + two * epsilon * B0 + B0 * B0));
@@ -540,80 +597,81 @@ PDA_HD void weno3_face_grad(double &uNeg, double &uPos, double gNeg[4],
 // the face normal (axis-aligned unit vectors); products with 0 and 1 are
 // elided, which changes no value other than the sign of an exact zero.
 // ---------------------------------------------------------------------------
-template <bool INL = false>
+template <bool INL = false, bool IP = false>
 PDA_HD void euler3_flux(double F[3], const double qL[3], const double qR[3],
                         double gamma) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double rL = qL[0];
-  const double uL = div_rn<INL>(qL[1], plus_es(rL));
-  const double pL = (gamma - 1) * (qL[2] - half_of(rL) * (uL * uL));
-  const double HL = div_rn<INL>((qL[2] + pL), rL);
+  const double uL = div_rn<INL>(qL[1], esx<IP>(rL));
+  const double pL = (gamma - 1) * (qL[2] - halfx<IP>(rL) * (uL * uL));
+  const Quot2 hl = div2_rn<INL>((qL[2] + pL), qR[0], rL);  // HL and rR / rL
+  const double HL = hl.q0;
   const double FL0 = rL * uL, FL1 = rL * uL * uL + pL, FL2 = rL * uL * HL;
   const double rR = qR[0];
-  const double uR = div_rn<INL>(qR[1], plus_es(rR));
-  const double pR = (gamma - 1) * (qR[2] - half_of(rR) * (uR * uR));
+  const double uR = div_rn<INL>(qR[1], esx<IP>(rR));
+  const double pR = (gamma - 1) * (qR[2] - halfx<IP>(rR) * (uR * uR));
   const double HR = div_rn<INL>((qR[2] + pR), rR);
   const double FR0 = rR * uR, FR1 = rR * uR * uR + pR, FR2 = rR * uR * HR;
-  const double RT = sqrt_rn<INL>(div_rn<INL>(rR, (rL)));
-  const double u = div_rn<INL>((uL + RT * uR), (1. + RT));
-  const double H = div_rn<INL>((HL + RT * HR), (1. + RT));
-  const double a = sqrt_rn<INL>((gamma - 1.) * (H - half_of(u * u)));
+  const double RT = sqrt_rn<INL>(hl.q1);
+  const Quot2 roe = div2_rn<INL>((uL + RT * uR), (HL + RT * HR), (1. + RT));
+  const double u = roe.q0, H = roe.q1;
+  const double a = sqrt_rn<INL>((gamma - 1.) * (H - halfx<IP>(u * u)));
   const double smax = fabs(u) + a;
-  F[0] = half_of(FL0 + FR0 + smax * (qL[0] - qR[0]));
-  F[1] = half_of(FL1 + FR1 + smax * (qL[1] - qR[1]));
-  F[2] = half_of(FL2 + FR2 + smax * (qL[2] - qR[2]));
+  F[0] = halfx<IP>(FL0 + FR0 + smax * (qL[0] - qR[0]));
+  F[1] = halfx<IP>(FL1 + FR1 + smax * (qL[1] - qR[1]));
+  F[2] = halfx<IP>(FL2 + FR2 + smax * (qL[2] - qR[2]));
 }
 
-template <int AXIS, bool INL = false>
+template <int AXIS, bool INL = false, bool IP = false>
 PDA_HD void euler4_flux(double F[4], const double qL[4], const double qR[4],
                         double gamma) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double rL = qL[0];
-  const double uL = div_rn<INL>(qL[1], plus_es(rL));
-  const double vL = div_rn<INL>(qL[2], plus_es(rL));
+  const Quot2 vl = div2_rn<INL>(qL[1], qL[2], esx<IP>(rL));
+  const double uL = vl.q0, vL = vl.q1;
   const double unL = AXIS == 0 ? uL : vL;
-  const double pL = (gamma - 1) * (qL[3] - half_of(rL) * (uL * uL + vL * vL));
-  const double HL = div_rn<INL>((qL[3] + pL), rL);
+  const double pL = (gamma - 1) * (qL[3] - halfx<IP>(rL) * (uL * uL + vL * vL));
+  const Quot2 hl = div2_rn<INL>((qL[3] + pL), qR[0], rL);  // HL and rR / rL
+  const double HL = hl.q0;
   double FL[4];
   FL[0] = rL * unL;
   FL[1] = AXIS == 0 ? rL * unL * uL + pL : rL * unL * uL;
   FL[2] = AXIS == 1 ? rL * unL * vL + pL : rL * unL * vL;
   FL[3] = rL * unL * HL;
   const double rR = qR[0];
-  const double uR = div_rn<INL>(qR[1], plus_es(rR));
-  const double vR = div_rn<INL>(qR[2], plus_es(rR));
+  const Quot2 vr = div2_rn<INL>(qR[1], qR[2], esx<IP>(rR));
+  const double uR = vr.q0, vR = vr.q1;
   const double unR = AXIS == 0 ? uR : vR;
-  const double pR = (gamma - 1) * (qR[3] - half_of(rR) * (uR * uR + vR * vR));
+  const double pR = (gamma - 1) * (qR[3] - halfx<IP>(rR) * (uR * uR + vR * vR));
   const double HR = div_rn<INL>((qR[3] + pR), rR);
   double FR[4];
   FR[0] = rR * unR;
   FR[1] = AXIS == 0 ? rR * unR * uR + pR : rR * unR * uR;
   FR[2] = AXIS == 1 ? rR * unR * vR + pR : rR * unR * vR;
   FR[3] = rR * unR * HR;
-  const double RT = sqrt_rn<INL>(div_rn<INL>(rR, (rL)));
-  const double u = div_rn<INL>((uL + RT * uR), (1. + RT));
-  const double v = div_rn<INL>((vL + RT * vR), (1. + RT));
-  const double H = div_rn<INL>((HL + RT * HR), (1. + RT));
-  const double a = sqrt_rn<INL>((gamma - 1.) * (H - half_of(u * u + v * v)));
+  const double RT = sqrt_rn<INL>(hl.q1);
+  const Quot3 roe = div3_rn<INL>((uL + RT * uR), (vL + RT * vR), (HL + RT * HR), (1. + RT));
+  const double u = roe.q0, v = roe.q1, H = roe.q2;
+  const double a = sqrt_rn<INL>((gamma - 1.) * (H - halfx<IP>(u * u + v * v)));
   const double smax = sqrt_rn<INL>(u * u + v * v) + a;
 #pragma unroll
-  for (int d = 0; d < 4; ++d) F[d] = half_of(FL[d] + FR[d] + smax * (qL[d] - qR[d]));
+  for (int d = 0; d < 4; ++d) F[d] = halfx<IP>(FL[d] + FR[d] + smax * (qL[d] - qR[d]));
 }
 
-template <int AXIS, bool INL = false>
+template <int AXIS, bool INL = false, bool IP = false>
 PDA_HD void euler5_flux(double F[5], const double qL[5], const double qR[5],
                         double gamma) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double rL = qL[0];
-  const double uL = div_rn<INL>(qL[1], plus_es(rL));
-  const double vL = div_rn<INL>(qL[2], plus_es(rL));
-  const double wL = div_rn<INL>(qL[3], plus_es(rL));
+  const Quot3 vl = div3_rn<INL>(qL[1], qL[2], qL[3], esx<IP>(rL));
+  const double uL = vl.q0, vL = vl.q1, wL = vl.q2;
   const double unL = AXIS == 0 ? uL : (AXIS == 1 ? vL : wL);
-  const double pL = (gamma - 1) * (qL[4] - half_of(rL) * (uL * uL + vL * vL + wL * wL));
-  const double HL = div_rn<INL>((qL[4] + pL), rL);
+  const double pL = (gamma - 1) * (qL[4] - halfx<IP>(rL) * (uL * uL + vL * vL + wL * wL));
+  const Quot2 hl = div2_rn<INL>((qL[4] + pL), qR[0], rL);  // HL and rR / rL
+  const double HL = hl.q0;
   double FL[5];
   FL[0] = rL * unL;
   FL[1] = AXIS == 0 ? rL * unL * uL + pL : rL * unL * uL;
@@ -621,11 +679,10 @@ PDA_HD void euler5_flux(double F[5], const double qL[5], const double qR[5],
   FL[3] = AXIS == 2 ? rL * unL * wL + pL : rL * unL * wL;
   FL[4] = rL * unL * HL;
   const double rR = qR[0];
-  const double uR = div_rn<INL>(qR[1], plus_es(rR));
-  const double vR = div_rn<INL>(qR[2], plus_es(rR));
-  const double wR = div_rn<INL>(qR[3], plus_es(rR));
+  const Quot3 vr = div3_rn<INL>(qR[1], qR[2], qR[3], esx<IP>(rR));
+  const double uR = vr.q0, vR = vr.q1, wR = vr.q2;
   const double unR = AXIS == 0 ? uR : (AXIS == 1 ? vR : wR);
-  const double pR = (gamma - 1) * (qR[4] - half_of(rR) * (uR * uR + vR * vR + wR * wR));
+  const double pR = (gamma - 1) * (qR[4] - halfx<IP>(rR) * (uR * uR + vR * vR + wR * wR));
   const double HR = div_rn<INL>((qR[4] + pR), rR);
   double FR[5];
   FR[0] = rR * unR;
@@ -633,50 +690,48 @@ PDA_HD void euler5_flux(double F[5], const double qL[5], const double qR[5],
   FR[2] = AXIS == 1 ? rR * unR * vR + pR : rR * unR * vR;
   FR[3] = AXIS == 2 ? rR * unR * wR + pR : rR * unR * wR;
   FR[4] = rR * unR * HR;
-  const double RT = sqrt_rn<INL>(div_rn<INL>(rR, (rL)));
-  const double u = div_rn<INL>((uL + RT * uR), (1. + RT));
-  const double v = div_rn<INL>((vL + RT * vR), (1. + RT));
-  const double w = div_rn<INL>((wL + RT * wR), (1. + RT));
-  const double H = div_rn<INL>((HL + RT * HR), (1. + RT));
-  const double a = sqrt_rn<INL>((gamma - 1.) * (H - half_of(u * u + v * v + w * w)));
+  const double RT = sqrt_rn<INL>(hl.q1);
+  const Quot4 roe = div4_rn<INL>((uL + RT * uR), (vL + RT * vR), (wL + RT * wR), (HL + RT * HR), (1. + RT));
+  const double u = roe.q0, v = roe.q1, w = roe.q2, H = roe.q3;
+  const double a = sqrt_rn<INL>((gamma - 1.) * (H - halfx<IP>(u * u + v * v + w * w)));
   const double smax = sqrt_rn<INL>(u * u + v * v + w * w) + a;
 #pragma unroll
-  for (int d = 0; d < 5; ++d) F[d] = half_of(FL[d] + FR[d] + smax * (qL[d] - qR[d]));
+  for (int d = 0; d < 5; ++d) F[d] = halfx<IP>(FL[d] + FR[d] + smax * (qL[d] - qR[d]));
 }
 
 // Shallow-water Rusanov flux.  deviation: the reference's std::pow(h, 0.5) is
 // evaluated as sqrt(h) (correctly rounded; glibc pow agrees except in rare
 // near-midpoint cases, a 1-ulp difference).
-template <int AXIS, bool INL = false>
+template <int AXIS, bool INL = false, bool IP = false>
 PDA_HD void swe_flux(double F[3], const double qL[3], const double qR[3],
                      double gravity) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double hL = qL[0];
-  const double uL = div_rn<INL>(qL[1], plus_es(hL));
-  const double vL = div_rn<INL>(qL[2], plus_es(hL));
+  const Quot2 vl = div2_rn<INL>(qL[1], qL[2], esx<IP>(hL));
+  const double uL = vl.q0, vL = vl.q1;
   const double unL = AXIS == 0 ? uL : vL;
-  const double pL = half_of(gravity) * hL * hL;
+  const double pL = halfx<IP>(gravity) * hL * hL;
   double FL[3];
   FL[0] = hL * unL;
   FL[1] = AXIS == 0 ? hL * unL * uL + pL : hL * unL * uL;
   FL[2] = AXIS == 1 ? hL * unL * vL + pL : hL * unL * vL;
   const double hR = qR[0];
-  const double uR = div_rn<INL>(qR[1], plus_es(hR));
-  const double vR = div_rn<INL>(qR[2], plus_es(hR));
+  const Quot2 vr = div2_rn<INL>(qR[1], qR[2], esx<IP>(hR));
+  const double uR = vr.q0, vR = vr.q1;
   const double unR = AXIS == 0 ? uR : vR;
-  const double pR = half_of(gravity) * hR * hR;
+  const double pR = halfx<IP>(gravity) * hR * hR;
   double FR[3];
   FR[0] = hR * unR;
   FR[1] = AXIS == 0 ? hR * unR * uR + pR : hR * unR * uR;
   FR[2] = AXIS == 1 ? hR * unR * vR + pR : hR * unR * vR;
-  const double hm = half_of(hL + hR);
+  const double hm = halfx<IP>(hL + hR);
   const double sL = sqrt_rn<INL>(hL), sR = sqrt_rn<INL>(hR);
-  const double um = div_rn<INL>((unL * sL + unR * sR), plus_es(sL + sR));
+  const double um = div_rn<INL>((unL * sL + unR * sR), esx<IP>(sL + sR));
   const double sg = sqrt_rn<INL>(gravity * hm);
   const double smax = sqrt_rn<INL>(um * um) + sqrt_rn<INL>(sg * sg);
 #pragma unroll
-  for (int d = 0; d < 3; ++d) F[d] = half_of(FL[d] + FR[d] + smax * (qL[d] - qR[d]));
+  for (int d = 0; d < 3; ++d) F[d] = halfx<IP>(FL[d] + FR[d] + smax * (qL[d] - qR[d]));
 }
 
 // ---------------------------------------------------------------------------
@@ -696,8 +751,8 @@ PDA_HD void euler3_side(FluxSide<3> &o, const double q[3], double gamma) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double r = q[0];
-  const double u = div_rn(q[1], plus_es(r));
-  const double p = (gamma - 1) * (q[2] - half_of(r) * (u * u));
+  const double u = div_rn(q[1], (r + es));
+  const double p = (gamma - 1) * (q[2] - half * r * (u * u));
   const double H = div_rn((q[2] + p), r);
   o.F[0] = r * u;
   o.F[1] = r * u * u + p;
@@ -711,10 +766,10 @@ PDA_HD void euler3_combine(double F[3], const double qL[3], const double qR[3], 
   const double RT = sqrt_rn(div_rn(qR[0], (qL[0])));
   const double u = div_rn((L.u + RT * R.u), (1. + RT));
   const double H = div_rn((L.H + RT * R.H), (1. + RT));
-  const double a = sqrt_rn((gamma - 1.) * (H - half_of(u * u)));
+  const double a = sqrt_rn((gamma - 1.) * (H - half * (u * u)));
   const double smax = fabs(u) + a;
 #pragma unroll
-  for (int d = 0; d < 3; ++d) F[d] = half_of(L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
+  for (int d = 0; d < 3; ++d) F[d] = half * (L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
 }
 
 template <int AXIS>
@@ -722,10 +777,10 @@ PDA_HD void euler4_side(FluxSide<4> &o, const double q[4], double gamma) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double r = q[0];
-  const double u = div_rn(q[1], plus_es(r));
-  const double v = div_rn(q[2], plus_es(r));
+  const double u = div_rn(q[1], (r + es));
+  const double v = div_rn(q[2], (r + es));
   const double un = AXIS == 0 ? u : v;
-  const double p = (gamma - 1) * (q[3] - half_of(r) * (u * u + v * v));
+  const double p = (gamma - 1) * (q[3] - half * r * (u * u + v * v));
   const double H = div_rn((q[3] + p), r);
   o.F[0] = r * un;
   o.F[1] = AXIS == 0 ? r * un * u + p : r * un * u;
@@ -743,10 +798,10 @@ PDA_HD void euler4_combine(double F[4], const double qL[4], const double qR[4], 
   const double u = div_rn((L.u + RT * R.u), (1. + RT));
   const double v = div_rn((L.v + RT * R.v), (1. + RT));
   const double H = div_rn((L.H + RT * R.H), (1. + RT));
-  const double a = sqrt_rn((gamma - 1.) * (H - half_of(u * u + v * v)));
+  const double a = sqrt_rn((gamma - 1.) * (H - half * (u * u + v * v)));
   const double smax = sqrt_rn(u * u + v * v) + a;
 #pragma unroll
-  for (int d = 0; d < 4; ++d) F[d] = half_of(L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
+  for (int d = 0; d < 4; ++d) F[d] = half * (L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
 }
 
 template <int AXIS>
@@ -754,11 +809,11 @@ PDA_HD void euler5_side(FluxSide<5> &o, const double q[5], double gamma) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double r = q[0];
-  const double u = div_rn(q[1], plus_es(r));
-  const double v = div_rn(q[2], plus_es(r));
-  const double w = div_rn(q[3], plus_es(r));
+  const double u = div_rn(q[1], (r + es));
+  const double v = div_rn(q[2], (r + es));
+  const double w = div_rn(q[3], (r + es));
   const double un = AXIS == 0 ? u : (AXIS == 1 ? v : w);
-  const double p = (gamma - 1) * (q[4] - half_of(r) * (u * u + v * v + w * w));
+  const double p = (gamma - 1) * (q[4] - half * r * (u * u + v * v + w * w));
   const double H = div_rn((q[4] + p), r);
   o.F[0] = r * un;
   o.F[1] = AXIS == 0 ? r * un * u + p : r * un * u;
@@ -779,20 +834,20 @@ PDA_HD void euler5_combine(double F[5], const double qL[5], const double qR[5], 
   const double v = div_rn((L.v + RT * R.v), (1. + RT));
   const double w = div_rn((L.w + RT * R.w), (1. + RT));
   const double H = div_rn((L.H + RT * R.H), (1. + RT));
-  const double a = sqrt_rn((gamma - 1.) * (H - half_of(u * u + v * v + w * w)));
+  const double a = sqrt_rn((gamma - 1.) * (H - half * (u * u + v * v + w * w)));
   const double smax = sqrt_rn(u * u + v * v + w * w) + a;
 #pragma unroll
-  for (int d = 0; d < 5; ++d) F[d] = half_of(L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
+  for (int d = 0; d < 5; ++d) F[d] = half * (L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
 }
 
 template <int AXIS>
 PDA_HD void swe_side(FluxSide<3> &o, const double q[3], double gravity) {
   constexpr double es = 1.e-30;
   const double h = q[0];
-  const double u = div_rn(q[1], plus_es(h));
-  const double v = div_rn(q[2], plus_es(h));
+  const double u = div_rn(q[1], (h + es));
+  const double v = div_rn(q[2], (h + es));
   const double un = AXIS == 0 ? u : v;
-  const double p = half_of(gravity) * h * h;
+  const double p = 0.5 * gravity * h * h;
   o.F[0] = h * un;
   o.F[1] = AXIS == 0 ? h * un * u + p : h * un * u;
   o.F[2] = AXIS == 1 ? h * un * v + p : h * un * v;
@@ -804,12 +859,12 @@ PDA_HD void swe_combine(double F[3], const double qL[3], const double qR[3], con
                         const FluxSide<3> &R, double gravity) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
-  const double hm = half_of(qL[0] + qR[0]);
-  const double um = div_rn((L.u * L.H + R.u * R.H), plus_es(L.H + R.H));
+  const double hm = 0.5 * (qL[0] + qR[0]);
+  const double um = div_rn((L.u * L.H + R.u * R.H), (L.H + R.H + es));
   const double sg = sqrt_rn(gravity * hm);
   const double smax = sqrt_rn(um * um) + sqrt_rn(sg * sg);
 #pragma unroll
-  for (int d = 0; d < 3; ++d) F[d] = half_of(L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
+  for (int d = 0; d < 3; ++d) F[d] = half * (L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
 }
 
 // ---------------------------------------------------------------------------

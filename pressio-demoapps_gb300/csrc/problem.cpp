@@ -1609,13 +1609,13 @@ pda_status pda_check_divsqrt(int mode, uint64_t seed, int64_t per_thread, int64_
   PDA_API_END
 }
 
-pda_status pda_check_products(int mode, uint64_t seed, int64_t per_thread, int64_t counts[4]) {
+pda_status pda_check_products(int mode, uint64_t seed, int64_t per_thread, int64_t counts[5]) {
   PDA_API_BEGIN
   PDA_REQUIRE(counts && mode >= 0 && mode <= 3 && per_thread > 0, PDA_ERR_INVALID_ARGUMENT, "invalid argument");
-  long long c[4] = {0, 0, 0, 0};
+  long long c[5] = {0, 0, 0, 0, 0};
   pda::check_products(mode, seed, (long)per_thread, c, nullptr);
   PDA_CUDA(cudaGetLastError());
-  for (int k = 0; k < 4; ++k) counts[k] = (int64_t)c[k];
+  for (int k = 0; k < 5; ++k) counts[k] = (int64_t)c[k];
   PDA_API_END
 }
 

@@ -10,6 +10,15 @@
 //    reconstructions of neighbouring faces with identical expression trees
 //    (impl/weno5.hpp:112-178, impl/weno3.hpp:82-131), so they are computed
 //    once per cell into shared memory and reused;
+//  * the reference's products by small integers, 1/2, 1/4 and constants and
+//    its divisions and square roots run on the integer pipe
+//    (fp64_intpipe.cuh), bit for bit;
+//  * the code stays small enough for the instruction cache: the per-dof
+//    loops of the cell and face phases are not unrolled (face states kept in
+//    registers by predicated moves) and every division and square root is
+//    an out-of-line call.  Fully unrolled with inline divisions the kernel
+//    is a straight line of about 10^4 instructions per thread, and
+//    instruction-fetch stalls were its largest stall reason;
 //  * boundary faces of the mirror-type boundary conditions (2D Neumann and
 //    slip wall, whose ghost layers are exact mirror images,
 //    euler_2d_ghost_filler_neumann.hpp:101-276,
@@ -25,6 +34,14 @@
 #include "kernels.cuh"
 
 namespace pda {
+
+// v[d] = x for a runtime d, with v kept in registers (predicated moves)
+template <int N>
+__device__ __forceinline__ void set_dof(double (&v)[N], int d, double x) {
+#pragma unroll
+  for (int k = 0; k < N; ++k)
+    if (k == d) v[k] = x;
+}
 
 template <int SCHEME, int LANES_ = 64> struct TileCfg;
 template <int LANES_> struct TileCfg<Weno5, LANES_> {
@@ -90,38 +107,40 @@ __device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &
     constexpr double oneOvten = 1. / 10., threeOvten = 3. / 10., sixOvten = 6. / 10.,
                      thirteenOvtwelve = 13. / 12.;
     if (tx + 2 < NCELL) {
-#pragma unroll
+#pragma unroll 1
       for (int d = 0; d < NDPC; ++d) {
         const double a = sU[ty][d][tx], m = sU[ty][d][tx + 1], c = sU[ty][d][tx + 2];
-        const double X = w5_curv(a, m, c);
-        const double D = thirteenOvtwelve * X * X;
-        const double YL = w5_slopeL(a, m, c);
+        const double X = w5_curv<true>(a, m, c);
+        const double D = mul_c(X, thirteenOvtwelve) * X;
+        const double YL = w5_slopeL<true>(a, m, c);
         const double YC = a - c;
-        const double YR = w5_slopeR(a, m, c);
+        const double YR = w5_slopeR<true>(a, m, c);
         const double BL = D + quarter_of(YL) * YL;
         const double BC = D + quarter_of(YC) * YC;
         const double BR = D + quarter_of(YR) * YR;
-        const double dL = epsilon * epsilon + 2. * epsilon * BL + BL * BL;
-        const double dC = epsilon * epsilon + 2. * epsilon * BC + BC * BC;
-        const double dR = epsilon * epsilon + 2. * epsilon * BR + BR * BR;
-        sA[ty][d][0][tx] = div_rn<true>(oneOvten, dL);    // uNeg alpha0 of face c+1+1/2
-        sA[ty][d][1][tx] = div_rn<true>(threeOvten, dL);  // uPos alpha0 of face c+1/2
-        sA[ty][d][2][tx] = div_rn<true>(sixOvten, dC);    // uNeg alpha1 of face c+1/2, uPos alpha1 of face c-1/2
-        sA[ty][d][3][tx] = div_rn<true>(threeOvten, dR);  // uNeg alpha2 of face c-1/2
-        sA[ty][d][4][tx] = div_rn<true>(oneOvten, dR);    // uPos alpha2 of face c-2+1/2
+        const double dL = epsilon * epsilon + mul_c(BL, 2. * epsilon) + BL * BL;
+        const double dC = epsilon * epsilon + mul_c(BC, 2. * epsilon) + BC * BC;
+        const double dR = epsilon * epsilon + mul_c(BR, 2. * epsilon) + BR * BR;
+        const Quot2 aL = div2_rn(oneOvten, threeOvten, dL);
+        const Quot2 aR = div2_rn(threeOvten, oneOvten, dR);
+        sA[ty][d][0][tx] = aL.q0;                 // uNeg alpha0 of face c+1+1/2
+        sA[ty][d][1][tx] = aL.q1;                 // uPos alpha0 of face c+1/2
+        sA[ty][d][2][tx] = div_rn(sixOvten, dC);  // uNeg alpha1 of face c+1/2, uPos alpha1 of face c-1/2
+        sA[ty][d][3][tx] = aR.q0;                 // uNeg alpha2 of face c-1/2
+        sA[ty][d][4][tx] = aR.q1;                 // uPos alpha2 of face c-2+1/2
       }
     }
   } else {
     // pair k = (f0 - 2 + tx, f0 - 1 + tx) uses cells sU[tx], sU[tx+1]
     constexpr double two = 2., oneOvthree = 1. / 3., twoOvthree = 2. / 3.;
     if (tx + 1 < NCELL) {
-#pragma unroll
+#pragma unroll 1
       for (int d = 0; d < NDPC; ++d) {
         const double a = sU[ty][d][tx], c = sU[ty][d][tx + 1];
         const double B = (a - c) * (a - c);
-        const double den = epsilon * epsilon + two * epsilon * B + B * B;
-        sA[ty][d][0][tx] = div_rn<true>(oneOvthree, den);
-        sA[ty][d][1][tx] = div_rn<true>(twoOvthree, den);
+        const double den = epsilon * epsilon + mul_c(B, two * epsilon) + B * B;
+        sA[ty][d][0][tx] = div_rn(oneOvthree, den);
+        sA[ty][d][1][tx] = div_rn(twoOvthree, den);
       }
     }
   }
@@ -133,29 +152,29 @@ __device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &
   double uN[NDPC], uP[NDPC];
   if constexpr (SCHEME == Weno5) {
     constexpr double oneOvsix = 1. / 6.;
-#pragma unroll
+#pragma unroll 1
     for (int d = 0; d < NDPC; ++d) {
       // left cell i = f-1: cells i-2..i+3 = sU[tx .. tx+5]; centers i-1..i+2 = sA[.][tx .. tx+3]
       const double qim2 = sU[ty][d][tx], qim1 = sU[ty][d][tx + 1], qi = sU[ty][d][tx + 2];
       const double qip1 = sU[ty][d][tx + 3], qip2 = sU[ty][d][tx + 4], qip3 = sU[ty][d][tx + 5];
-      const double p0 = w5_pFarL(qim2, qim1, qi) * oneOvsix;
-      const double p1 = w5_pMidL(qim1, qi, qip1) * oneOvsix;
-      const double p2 = w5_pMidR(qi, qip1, qip2) * oneOvsix;
-      const double p3 = w5_pFarR(qip1, qip2, qip3) * oneOvsix;
+      const double p0 = mul_c(w5_pFarL<true>(qim2, qim1, qi), oneOvsix);
+      const double p1 = mul_c(w5_pMidL<true>(qim1, qi, qip1), oneOvsix);
+      const double p2 = mul_c(w5_pMidR<true>(qi, qip1, qip2), oneOvsix);
+      const double p3 = mul_c(w5_pFarR<true>(qip1, qip2, qip3), oneOvsix);
       {
         const double a0 = sA[ty][d][0][tx], a1 = sA[ty][d][2][tx + 1], a2 = sA[ty][d][3][tx + 2];
-        const double s = div_rn<true>(1., (a0 + a1 + a2));
-        uN[d] = (a0 * s) * p0 + (a1 * s) * p1 + (a2 * s) * p2;
+        const double s = div_rn(1., (a0 + a1 + a2));
+        set_dof(uN, d, (a0 * s) * p0 + (a1 * s) * p1 + (a2 * s) * p2);
       }
       {
         const double a0 = sA[ty][d][1][tx + 1], a1 = sA[ty][d][2][tx + 2], a2 = sA[ty][d][4][tx + 3];
-        const double s = div_rn<true>(1., (a0 + a1 + a2));
-        uP[d] = (a0 * s) * p1 + (a1 * s) * p2 + (a2 * s) * p3;
+        const double s = div_rn(1., (a0 + a1 + a2));
+        set_dof(uP, d, (a0 * s) * p1 + (a1 * s) * p2 + (a2 * s) * p3);
       }
     }
   } else {
     // p0 = (-q_{i-1} + 3 q_i) / 2, p1 = (q_i + q_{i+1}) / 2, p2 = (3 q_{i+1} - q_{i+2}) / 2
-#pragma unroll
+#pragma unroll 1
     for (int d = 0; d < NDPC; ++d) {
       // left cell i = f-1: cells i-1..i+2 = sU[tx .. tx+3]; pairs i-1, i, i+1 = sA[.][tx .. tx+2]
       const double qim1 = sU[ty][d][tx], qi = sU[ty][d][tx + 1], qip1 = sU[ty][d][tx + 2],
@@ -165,18 +184,18 @@ __device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &
       const double p2 = half_of(mul_k<3>(qip1) - qip2);
       {
         const double a0 = sA[ty][d][0][tx], a1 = sA[ty][d][1][tx + 1];
-        const double s = div_rn<true>(1., (a0 + a1));
-        uN[d] = (a0 * s) * p0 + (a1 * s) * p1;
+        const double s = div_rn(1., (a0 + a1));
+        set_dof(uN, d, (a0 * s) * p0 + (a1 * s) * p1);
       }
       {
         const double a0 = sA[ty][d][1][tx + 1], a1 = sA[ty][d][0][tx + 2];
-        const double s = div_rn<true>(1., (a0 + a1));
-        uP[d] = (a0 * s) * p1 + (a1 * s) * p2;
+        const double s = div_rn(1., (a0 + a1));
+        set_dof(uP, d, (a0 * s) * p1 + (a1 * s) * p2);
       }
     }
   }
   double fl[NDPC];
-  F::template flux<AXIS, true>(fl, uN, uP, p);
+  F::template flux<AXIS, false, true>(fl, uN, uP, p);
   // output layout of k_struct_faces: face axis index fastest within its line
   // ordering [A2][A1][face] for AXIS=0, [k][face][i] for AXIS=1, [face][j][i] for AXIS=2
   const int fi = f - b.lo[AXIS];

@@ -111,8 +111,9 @@ __global__ void k_check_divsqrt(int mode, uint64_t seed, long per_thread, unsign
   atomicAdd(bad + 1, ns);
 }
 
-// Operand sets for the comparison of the integer-pipe exact products
-// (ip::mul_small<K>, ip::mul_pow2_neg<S>, ip::add_1em30) with the FP64
+// Operand sets for the comparison of the integer-pipe products by constants
+// (ip::mul_small<K>, ip::mul_pow2_neg<S>, ip::mul_const) and of
+// ip::add_1em30 with the FP64
 // pipe's operations.  mode 0: random mantissas, exponents within 2^-60..2^60;
 // 1: exponents at the edges of the fast paths (subnormal results of the
 // halvings, near-overflow products, the 2^-44 bound of the density guard)
@@ -125,7 +126,7 @@ __device__ __forceinline__ bool same_bits(double a, double b) {
 
 __global__ void k_check_products(int mode, uint64_t seed, long per_thread, unsigned long long *bad) {
   uint64_t st = seed ^ ((uint64_t)(blockIdx.x * blockDim.x + threadIdx.x) * 0x9E6C63D0676A9A99ull);
-  unsigned long long nk = 0, np = 0, ne = 0;
+  unsigned long long nk = 0, np = 0, ne = 0, nc = 0;
   constexpr uint64_t M = 0x000FFFFFFFFFFFFFull;
   for (long k = 0; k < per_thread; ++k) {
     const uint64_t r1 = splitmix64(st), r2 = splitmix64(st);
@@ -153,10 +154,18 @@ __global__ void k_check_products(int mode, uint64_t seed, long per_thread, unsig
     np += !same_bits(x * 0.5, ip::mul_pow2_neg<1>(x));
     np += !same_bits(x * 0.25, ip::mul_pow2_neg<2>(x));
     ne += !same_bits(x + 1.e-30, ip::add_1em30(x));
+    nc += !same_bits(x * (1. / 6.), ip::mul_const(x, 1. / 6.));
+    nc += !same_bits(x * (13. / 12.), ip::mul_const(x, 13. / 12.));
+    nc += !same_bits(x * (2. * 1e-6), ip::mul_const(x, 2. * 1e-6));
+    nc += !same_bits(x * 0.1, ip::mul_const(x, 0.1));
+    nc += !same_bits(x * 1.4, ip::mul_const(x, 1.4));
+    nc += !same_bits(x * 1e300, ip::mul_const(x, 1e300));
+    nc += !same_bits(x * 1e-300, ip::mul_const(x, 1e-300));
   }
   atomicAdd(bad, nk);
   atomicAdd(bad + 1, np);
   atomicAdd(bad + 2, ne);
+  atomicAdd(bad + 3, nc);
 }
 
 }  // namespace
@@ -179,16 +188,16 @@ void check_divsqrt(int mode, uint64_t seed, long per_thread, long long counts[3]
   counts[2] = (long long)h[1];
 }
 
-void check_products(int mode, uint64_t seed, long per_thread, long long counts[4], cudaStream_t s) {
+void check_products(int mode, uint64_t seed, long per_thread, long long counts[5], cudaStream_t s) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   unsigned long long *bad = nullptr;
-  cudaMalloc((void **)&bad, 3 * sizeof(unsigned long long));
-  cudaMemsetAsync(bad, 0, 3 * sizeof(unsigned long long), s);
+  cudaMalloc((void **)&bad, 4 * sizeof(unsigned long long));
+  cudaMemsetAsync(bad, 0, 4 * sizeof(unsigned long long), s);
   const int blocks = (sms > 0 ? sms : 1) * 8, threads = 256;
   k_check_products<<<blocks, threads, 0, s>>>(mode, seed, per_thread, bad);
-  unsigned long long h[3] = {0, 0, 0};
+  unsigned long long h[4] = {0, 0, 0, 0};
   cudaMemcpyAsync(h, bad, sizeof(h), cudaMemcpyDeviceToHost, s);
   cudaStreamSynchronize(s);
   cudaFree(bad);
@@ -196,6 +205,7 @@ void check_products(int mode, uint64_t seed, long per_thread, long long counts[4
   counts[1] = (long long)h[0];
   counts[2] = (long long)h[1];
   counts[3] = (long long)h[2];
+  counts[4] = (long long)h[3];
 }
 
 double measure_fp64_fma_rate(int blocks, int threads, int iters, cudaStream_t s) {
