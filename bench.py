@@ -38,9 +38,14 @@ BYTES_PER_CELL = 16 * NDPC  # read U once + write V once (FP64)
 # + 10 divisions + 3 square roots; two faces per cell plus the 24-flop
 # balance; a division or square root counts as one operation).
 # DRAM bytes (read + write) per cell of one face launch, measured by ncu on
-# k_faces_tile at 2048^2 (x-axis launch: 135.4 MB read + 85.4 MB written);
+# k_faces_tile at 2048^2 (x-axis launch: 134.3 MB read + 91.2 MB written);
 # traffic grows in proportion to the cells, so it scales to other sizes
-FACE_TRAFFIC_BYTES_PER_CELL = (135.4e6 + 85.4e6) / 2048 ** 2
+FACE_TRAFFIC_BYTES_PER_CELL = (134.31e6 + 91.17e6) / 2048 ** 2
+# FP64 instructions the face kernel executes per face (ncu thread-instruction
+# counters dadd + dmul + dfma of the same capture, 268.3 per face): the work
+# the FP64 pipe actually does, after the divisions, square roots and
+# products by constants moved to the integer pipe
+FP64_INST_PER_FACE = 268.3
 FLOPS_PER_CELL = 2 * (4 * 2 * (71 + 4) + 65 + 10 + 3) + 24
 L2_FLUSH_BYTES = 256 << 20
 
@@ -923,6 +928,7 @@ def main():
     fp64_peak = pda.measure_fp64_peak()  # FLOP/s with an FMA counted as 2
     fp64_inst_peak = fp64_peak / 2.0      # FP64 instructions per second (DFMA/DMUL/DADD)
     ops_face_launch = cells * (FLOPS_PER_CELL - 24) / 2
+    fp64_inst_face_launch = FP64_INST_PER_FACE * (N_CELLS_SIDE + 1) * N_CELLS_SIDE
     ops_ach = ops_face_launch / (face_ms * 1e-3)
     step_ops = cells * FLOPS_PER_CELL / (ms * 1e-3)
 
@@ -946,9 +952,15 @@ def main():
                               "frac": ops_ach / fp64_inst_peak, "peak_tflops_fma2": fp64_peak / 1e12,
                               "peak_source": "measured DFMA probe (pda_measure_fp64_peak)",
                               "note": "algorithmic FP64 ops (add/mul/div/sqrt = 1) per second of the face kernel "
-                                      "against the FP64 instruction issue rate; divisions and square roots "
-                                      "execute several instructions each, so the pipe is busier than frac "
-                                      "(ncu: 86 % FP64 pipe busy, profiles/)",
+                                      "against the FP64 instruction issue rate; divisions, square roots and "
+                                      "products by constants run on the integer pipe, so frac exceeds 1; "
+                                      "pipe_frac is the FP64 pipe's own occupancy",
+                              "inst_per_face": FP64_INST_PER_FACE,
+                              "pipe_achieved_ginst_per_s": fp64_inst_face_launch / (face_ms * 1e-3) / 1e9,
+                              "pipe_frac": fp64_inst_face_launch / (face_ms * 1e-3) / fp64_inst_peak,
+                              "pipe_source": "ncu dadd + dmul + dfma thread-instruction counters of k_faces_tile "
+                                             "(profiles/k_faces_tile_riemann2d_weno5_2048.md) x faces per launch "
+                                             "/ live CUDA-event time",
                               "step_achieved_gops": step_ops / 1e9,
                               "algorithmic_ops_per_cell": FLOPS_PER_CELL},
                      "kernel_ms": prof},
