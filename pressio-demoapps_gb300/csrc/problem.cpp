@@ -1371,34 +1371,45 @@ pda_status pda_velocity_noalloc(pda_problem *p, const double *dU, double t, doub
 }
 
 namespace pda {
-// pda_velocity_host for 2D meshes that one structured box covers: two row
-// bands whose copies overlap the other band's kernels.  The copy stream moves
-// band 0's rows, then band 1's; each band's x faces start on its own compute
-// stream as soon as its rows are on the device (x faces read no other row),
-// its y faces once both bands are (y faces [0, r] for band 0, [r + 1, n] for
-// band 1), its balance after its own faces (band 1 also after band 0's y
-// faces: it reads face r), and its velocity rows go back as soon as its
-// balance is done.  Band 0 runs on a high-priority stream, so it finishes
-// first while band 1's blocks fill its tails: band 1's rows come in under band
-// 0's x faces and band 0's velocity goes out under band 1's kernels.  The same
-// kernels on sub-boxes: V equals pda_velocity's bit for bit.  Returns false
-// when the mesh does not qualify.
+// pda_velocity_host for 2D meshes that one structured box covers: kHostBands
+// row bands whose copies overlap the other bands' kernels.  The copy stream
+// moves the bands' rows in order; each band's x faces start on its own
+// compute stream as soon as its rows are on the device (x faces read no
+// other row), its y faces once the next band's rows are in too (band b
+// computes y faces [r_b + 1, r_b+1], band 0 from face 0), its balance after
+// its own faces and the previous band's y faces (it reads face r_b), and its
+// velocity rows go back as soon as its balance is done.  Earlier bands run
+// at higher stream priority, so they finish first while later bands' blocks
+// fill their tails.  The first band's copy in and the last band's copy out
+// cannot overlap any kernel; more bands shorten them.  The same kernels on
+// sub-boxes: V equals pda_velocity's bit for bit.
+//
+// Repeated calls with the same pinned buffers and time replay the whole
+// sequence (copies, kernels, cross-stream events) as one CUDA graph, captured
+// on the second consecutive call with the same arguments and device buffers;
+// pageable host buffers (not capturable) and changing arguments take the
+// direct path.  Returns false when the mesh does not qualify.
 bool velocity_host_banded(pda_problem &P, const double *hU, double t, double *hV) {
-  if (!(P.useStruct && P.structAll && P.dim == 2 && P.box.n[1] >= 64 && P.dofsSample == P.dofsStencil))
+  constexpr int NB = kHostBands;
+  if (!(P.useStruct && P.structAll && P.dim == 2 && P.box.n[1] >= 16 * NB && P.dofsSample == P.dofsStencil))
     return false;
   check_evaluable(P);
   sync_recipes(P);
   if (!P.hostCopy) {
     int least = 0, greatest = 0;
     PDA_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-    PDA_CUDA(cudaStreamCreateWithPriority(&P.hostFirst, cudaStreamNonBlocking, greatest));
-    PDA_CUDA(cudaStreamCreateWithPriority(&P.hostCompute, cudaStreamNonBlocking, least));
+    for (int b = 0; b < NB; ++b) {
+      // priorities run from greatest (numerically lowest) to least
+      const int prio = greatest + b > least ? least : greatest + b;
+      PDA_CUDA(cudaStreamCreateWithPriority(&P.hostBand[b], cudaStreamNonBlocking, prio));
+    }
     PDA_CUDA(cudaStreamCreateWithFlags(&P.hostCopy, cudaStreamNonBlocking));
     for (cudaEvent_t &e : P.hostEv) PDA_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
   const Box &B = P.box;
   const int nx = B.n[0], ny = B.n[1], nd = P.ndpc;
-  const int r[3] = {0, ny / 2, ny};
+  int r[NB + 1];
+  for (int b = 0; b <= NB; ++b) r[b] = (int)((long)ny * b / NB);
   const size_t rowDofs = (size_t)nx * nd;
   P.d_U.alloc(P.dofsStencil);
   P.d_V.alloc(P.dofsSample);
@@ -1407,51 +1418,115 @@ bool velocity_host_banded(pda_problem &P, const double *hU, double t, double *hV
   double *U = P.d_U.p, *V = P.d_V.p, *Fx = P.F[0].p, *Fy = P.F[1].p;
   MeshArgs ma = P.margs;
   ma.time = t;
-  cudaStream_t cs[2] = {P.hostFirst, P.hostCompute}, sc = P.hostCopy;
-  cudaEvent_t *ev = P.hostEv;  // 0 start, 1-2 band rows in, 3-4 y faces, 5-6 balance, 7 copies out, 8 spare
-  // after whatever the problem's stream holds
-  PDA_CUDA(cudaEventRecord(ev[0], P.stream));
-  PDA_CUDA(cudaStreamWaitEvent(sc, ev[0], 0));
-  PDA_CUDA(cudaStreamWaitEvent(cs[0], ev[0], 0));
-  PDA_CUDA(cudaStreamWaitEvent(cs[1], ev[0], 0));
-  for (int b = 0; b < 2; ++b) {
+  const HostGraphKey key{hU, hV, t, U, V, Fx, Fy};
+  bool pinned = false;
+  {
+    cudaPointerAttributes au{}, av{};
+    if (cudaPointerGetAttributes(&au, hU) == cudaSuccess && cudaPointerGetAttributes(&av, hV) == cudaSuccess)
+      pinned = au.type == cudaMemoryTypeHost && av.type == cudaMemoryTypeHost;
+    cudaGetLastError();  // a pageable pointer may leave an error behind on older drivers
+  }
+  constexpr int nLaunch = 3 * NB;
+  // events: start, rows in [NB], y faces [NB], balance [NB], copies out, graph order
+  cudaEvent_t *ev = P.hostEv;
+  cudaEvent_t evStart = ev[0], *evIn = ev + 1, *evY = ev + 1 + NB, *evBal = ev + 1 + 2 * NB;
+  cudaEvent_t evOut = ev[1 + 3 * NB], evOrder = ev[2 + 3 * NB];
+  cudaStream_t *cs = P.hostBand, sc = P.hostCopy;
+  // the graph runs on the first band's stream, after whatever the problem's
+  // stream holds; later work on the problem's stream follows it
+  auto launch_graph = [&]() {
+    PDA_CUDA(cudaEventRecord(evOrder, P.stream));
+    PDA_CUDA(cudaStreamWaitEvent(cs[0], evOrder, 0));
+    PDA_CUDA(cudaGraphLaunch(P.hostGraph, cs[0]));
+    PDA_CUDA(cudaEventRecord(evOrder, cs[0]));
+    PDA_CUDA(cudaStreamWaitEvent(P.stream, evOrder, 0));
+    PDA_CUDA(cudaStreamSynchronize(cs[0]));
+  };
+  if (pinned && P.hostGraph && P.hostGraphKey == key) {
+    launch_graph();
+    P.launches += nLaunch;
+    return true;
+  }
+  const bool capture = pinned && P.hostLastKey == key;
+  P.hostLastKey = key;
+  // ends an open capture if an error leaves this function early
+  struct CaptureGuard {
+    cudaStream_t s;
+    bool open;
+    ~CaptureGuard() {
+      if (!open) return;
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+    }
+  } guard{cs[0], false};
+  if (capture) {
+    PDA_CUDA(cudaStreamBeginCapture(cs[0], cudaStreamCaptureModeThreadLocal));
+    guard.open = true;
+  }
+  // the sequence starts and ends on `so`: the problem's stream when run
+  // directly, the first band's stream (the capture origin) when captured
+  const cudaStream_t so = capture ? cs[0] : P.stream;
+  PDA_CUDA(cudaEventRecord(evStart, so));
+  PDA_CUDA(cudaStreamWaitEvent(sc, evStart, 0));
+  for (int b = 0; b < NB; ++b) PDA_CUDA(cudaStreamWaitEvent(cs[b], evStart, 0));
+  for (int b = 0; b < NB; ++b) {
     PDA_CUDA(cudaMemcpyAsync(U + r[b] * rowDofs, hU + r[b] * rowDofs, (size_t)(r[b + 1] - r[b]) * rowDofs * 8,
                              cudaMemcpyHostToDevice, sc));
-    PDA_CUDA(cudaEventRecord(ev[1 + b], sc));
+    PDA_CUDA(cudaEventRecord(evIn[b], sc));
   }
-  for (int b = 0; b < 2; ++b) {
-    PDA_CUDA(cudaStreamWaitEvent(cs[b], ev[1 + b], 0));
+  for (int b = 0; b < NB; ++b) {
+    PDA_CUDA(cudaStreamWaitEvent(cs[b], evIn[b], 0));
     Box xb = B;
     xb.lo[1] = r[b];
     xb.hi[1] = r[b + 1];
     P.L->struct_faces(P.scheme, 0, xb, P.phys, U, Fx + (size_t)(nx + 1) * r[b] * nd, cs[b]);
   }
-  for (int b = 0; b < 2; ++b) {
-    PDA_CUDA(cudaStreamWaitEvent(cs[b], ev[2 - b], 0));  // the other band's rows
+  for (int b = 0; b < NB; ++b) {
+    // the next band's rows (the copy stream is in order: earlier rows too)
+    PDA_CUDA(cudaStreamWaitEvent(cs[b], evIn[b + 1 < NB ? b + 1 : b], 0));
     Box yb = B;
-    yb.lo[1] = b == 0 ? 0 : r[1] + 1;
-    yb.hi[1] = b == 0 ? r[1] : ny;
+    yb.lo[1] = b == 0 ? 0 : r[b] + 1;
+    yb.hi[1] = r[b + 1];
     P.L->struct_faces(P.scheme, 1, yb, P.phys, U, Fy + (size_t)nx * yb.lo[1] * nd, cs[b]);
-    PDA_CUDA(cudaEventRecord(ev[3 + b], cs[b]));
+    PDA_CUDA(cudaEventRecord(evY[b], cs[b]));
   }
-  for (int b = 0; b < 2; ++b) {
-    if (b == 1) PDA_CUDA(cudaStreamWaitEvent(cs[1], ev[3], 0));  // face r, from band 0's y faces
+  for (int b = 0; b < NB; ++b) {
+    if (b > 0) PDA_CUDA(cudaStreamWaitEvent(cs[b], evY[b - 1], 0));  // face r_b, from the previous band
     Box bb = B;
     bb.lo[1] = r[b];
     bb.hi[1] = r[b + 1];
     const double *Fb[3] = {Fx + (size_t)(nx + 1) * r[b] * nd, Fy + (size_t)nx * r[b] * nd, nullptr};
     P.L->struct_balance(bb, ma, P.phys, U, Fb, V, cs[b]);
-    PDA_CUDA(cudaEventRecord(ev[5 + b], cs[b]));
+    PDA_CUDA(cudaEventRecord(evBal[b], cs[b]));
   }
-  for (int b = 0; b < 2; ++b) {
-    PDA_CUDA(cudaStreamWaitEvent(sc, ev[5 + b], 0));
+  for (int b = 0; b < NB; ++b) {
+    PDA_CUDA(cudaStreamWaitEvent(sc, evBal[b], 0));
     PDA_CUDA(cudaMemcpyAsync(hV + r[b] * rowDofs, V + r[b] * rowDofs, (size_t)(r[b + 1] - r[b]) * rowDofs * 8,
                              cudaMemcpyDeviceToHost, sc));
   }
-  PDA_CUDA(cudaEventRecord(ev[7], sc));
-  PDA_CUDA(cudaStreamWaitEvent(P.stream, ev[7], 0));  // later work on the problem's stream follows
-  P.launches += 6;
-  PDA_CUDA(cudaStreamSynchronize(sc));  // the last copy follows every kernel of both bands
+  PDA_CUDA(cudaEventRecord(evOut, sc));
+  // every band stream's last work is awaited by the copy stream, which `so`
+  // awaits: the fork joins back (as a capture requires), and later work on
+  // `so` follows
+  PDA_CUDA(cudaStreamWaitEvent(so, evOut, 0));
+  P.launches += nLaunch;
+  if (capture) {
+    cudaGraph_t g = nullptr;
+    guard.open = false;
+    PDA_CUDA(cudaStreamEndCapture(cs[0], &g));
+    if (P.hostGraph) {
+      cudaGraphExecDestroy(P.hostGraph);
+      P.hostGraph = nullptr;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&P.hostGraph, g, 0);
+    cudaGraphDestroy(g);
+    PDA_CUDA(ie);
+    P.hostGraphKey = key;
+    launch_graph();
+  } else {
+    PDA_CUDA(cudaStreamSynchronize(P.stream));  // the last copy follows every kernel of every band
+  }
   PDA_CUDA(cudaGetLastError());
   return true;
 }

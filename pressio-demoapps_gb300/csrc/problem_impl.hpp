@@ -122,6 +122,25 @@ enum BcKind {
 
 }  // namespace pda
 
+namespace pda {
+// row bands of the host-buffer velocity (velocity_host_banded); measured at
+// 1024^2 with the copies at about 300 GB/s: 2, 3, 4, 6, 8 bands gave 1.565,
+// 1.556, 1.584, 1.535, 1.701 ms per call
+constexpr int kHostBands = 6;
+// the arguments and device buffers a captured host-buffer velocity graph is
+// bound to
+struct HostGraphKey {
+  const double *hU = nullptr;
+  const double *hV = nullptr;
+  double t = 0;
+  const double *U = nullptr, *V = nullptr, *Fx = nullptr, *Fy = nullptr;
+  bool operator==(const HostGraphKey &o) const {
+    return hU != nullptr && hU == o.hU && hV == o.hV && t == o.t && U == o.U && V == o.V && Fx == o.Fx &&
+           Fy == o.Fy;
+  }
+};
+}  // namespace pda
+
 struct pda_mesh {
   pda::Mesh m;
 };
@@ -136,10 +155,15 @@ struct pda_problem {
   // second stream + events: inner and near-boundary row kernels run side by side
   cudaStream_t side = nullptr;
   cudaEvent_t evFork = nullptr, evJoin = nullptr;
-  // host-buffer velocity in row bands: two compute streams (the first band's
-  // at high priority), a copy stream and their events (created on first use)
-  cudaStream_t hostFirst = nullptr, hostCompute = nullptr, hostCopy = nullptr;
-  cudaEvent_t hostEv[9] = {};
+  // host-buffer velocity in row bands: one compute stream per band (earlier
+  // bands at higher priority), a copy stream and their events (created on
+  // first use)
+  cudaStream_t hostBand[pda::kHostBands] = {}, hostCopy = nullptr;
+  cudaEvent_t hostEv[3 * pda::kHostBands + 3] = {};
+  // the host-buffer velocity as one graph, for repeated calls with the same
+  // arguments (velocity_host_banded)
+  cudaGraphExec_t hostGraph = nullptr;
+  pda::HostGraphKey hostGraphKey{}, hostLastKey{};
   int ndpc = 0, dim = 0, h = 0;
   int64_t dofsSample = 0, dofsStencil = 0;
   int bc = pda::BC_NONE;
@@ -176,11 +200,12 @@ struct pda_problem {
   int64_t launches = 0;
   ~pda_problem() {
     if (stepGraph) cudaGraphExecDestroy(stepGraph);
+    if (hostGraph) cudaGraphExecDestroy(hostGraph);
     if (side) cudaStreamDestroy(side);
     if (evFork) cudaEventDestroy(evFork);
     if (evJoin) cudaEventDestroy(evJoin);
-    if (hostFirst) cudaStreamDestroy(hostFirst);
-    if (hostCompute) cudaStreamDestroy(hostCompute);
+    for (cudaStream_t h : hostBand)
+      if (h) cudaStreamDestroy(h);
     if (hostCopy) cudaStreamDestroy(hostCopy);
     for (cudaEvent_t e : hostEv)
       if (e) cudaEventDestroy(e);
