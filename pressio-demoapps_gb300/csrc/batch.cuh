@@ -4,11 +4,13 @@
 // Work is cut into tiles (the single-problem tile of tiles.cuh: NR lines x
 // TW faces of one instance), numbered instance by instance; per-instance
 // prefix sums of tile counts let each block find its instance by binary
-// search.  The kernels are persistent: a grid of (resident blocks per SM x
-// SMs) loops over all tiles of all instances, so small instances no longer
-// leave most of the GPU idle and one launch replaces one per instance.  Each
-// tile runs exactly the single-problem code, so every instance's residual is
-// bit-identical to evaluating that problem alone.
+// search.  One launch per phase covers all instances: the face kernels run
+// one block per tile of every instance, the first-order faces and the
+// balance passes are persistent (a grid of resident blocks per SM x SMs loops
+// over the work), so small instances no longer leave most of the GPU idle
+// and one launch replaces one per instance.  Each tile runs exactly the
+// single-problem code, so every instance's residual is bit-identical to
+// evaluating that problem alone.
 #pragma once
 
 #include "kernels.cuh"
@@ -28,22 +30,24 @@ __device__ __forceinline__ int batch_find(const long *__restrict__ start, int n,
   return lo;
 }
 
+// One block per tile of any instance (grid = all tiles of the axis), with
+// registers capped for 32 resident warps per SM.  Measured on 512 shallow-
+// water instances: 169 ms per SSP-RK3 step, against 193 ms for a persistent
+// loop over the tiles (its loop state raised the registers from 74 to 80: 6
+// blocks per SM) and 178 ms for one block per tile without the cap.
 template <int FAM, int SCHEME, int AXIS, int NR, int LANES>
-__global__ void __launch_bounds__(LANES *NR)
+__global__ void __launch_bounds__(LANES *NR, 1024 / (LANES * NR))
 k_batch_faces_tile(BatchArgs a, const double *__restrict__ U, double *__restrict__ F) {
   __shared__ FaceTileSmem<FAM, SCHEME, NR, LANES> sm;
-  const long total = a.totalTiles[AXIS];
-  for (long t = blockIdx.x; t < total; t += gridDim.x) {
-    const int it = batch_find(a.tileStart[AXIS], a.nItems, t);
-    const BatchItem &bi = a.items[it];
-    const Box b = bi.b;
-    const Phys p = bi.p;
-    const long local = t - a.tileStart[AXIS][it];
-    const long g = bi.groups[AXIS];
-    face_tile<FAM, SCHEME, AXIS, NR, LANES>(sm, b, p, U + bi.uOff, F + bi.fOff[AXIS], local % g,
-                                            (int)(local / g));
-    __syncthreads();  // the next tile reuses the shared buffers
-  }
+  const long t = blockIdx.x;
+  const int it = batch_find(a.tileStart[AXIS], a.nItems, t);
+  const BatchItem &bi = a.items[it];
+  const Box b = bi.b;
+  const Phys p = bi.p;
+  const long local = t - a.tileStart[AXIS][it];
+  const long g = bi.groups[AXIS];
+  face_tile<FAM, SCHEME, AXIS, NR, LANES>(sm, b, p, U + bi.uOff, F + bi.fOff[AXIS], local % g,
+                                          (int)(local / g));
 }
 
 // first order: one face per thread, kFoFacesPerTile faces per tile

@@ -229,7 +229,7 @@ long persistent_grid(K kernel, int threads, long work) {
 template <int SCHEME, int AXIS, int NR, int LANES>
 void batch_tile_launch(const BatchArgs &a, const double *U, double *Fo, cudaStream_t s) {
   auto k = k_batch_faces_tile<FAM, SCHEME, AXIS, NR, LANES>;
-  const long g = persistent_grid(k, LANES * NR, a.totalTiles[AXIS]);
+  const long g = a.totalTiles[AXIS];  // one block per tile
   if (g > 0) k<<<(unsigned)g, dim3(LANES, NR), 0, s>>>(a, U, Fo);
 }
 
