@@ -261,8 +261,8 @@ k_rows_velocity(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U, do
     const int c = t.cell[e];
     const double u0 = __ldg(U + (size_t)c * 3), u1 = __ldg(U + (size_t)c * 3 + 1),
                  u2 = __ldg(U + (size_t)c * 3 + 2);
-    v[1] -= p.coriolis * u2 / u0;
-    v[2] += p.coriolis * u1 / u0;
+    v[1] -= div_rn(p.coriolis * u2, u0);
+    v[2] += div_rn(p.coriolis * u1, u0);
   }
 #pragma unroll
   for (int d = 0; d < NDPC; ++d) V[(size_t)r * NDPC + d] = v[d];
@@ -371,8 +371,8 @@ __device__ __forceinline__ bool balance_values(const Box &b, const MeshArgs &m, 
   cell = (i + b.lo[0]) + (long)b.n[0] * ((j + b.lo[1]) + (long)b.n[1] * (k + b.lo[2]));
   if constexpr (FAM == Swe2d) {
     const double u0 = __ldg(U + cell * 3), u1 = __ldg(U + cell * 3 + 1), u2 = __ldg(U + cell * 3 + 2);
-    v[1] -= p.coriolis * u2 / u0;
-    v[2] += p.coriolis * u1 / u0;
+    v[1] -= div_rn(p.coriolis * u2, u0);
+    v[2] += div_rn(p.coriolis * u1, u0);
   }
   return true;
 }
@@ -479,14 +479,14 @@ k_rows_vj_inner(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U,
     const int c = t.cell[e];
     const double u0 = __ldg(U + (size_t)c * 3), u1 = __ldg(U + (size_t)c * 3 + 1),
                  u2 = __ldg(U + (size_t)c * 3 + 2);
-    v[1] -= p.coriolis * u2 / u0;
-    v[2] += p.coriolis * u1 / u0;
+    v[1] -= div_rn(p.coriolis * u2, u0);
+    v[2] += div_rn(p.coriolis * u1, u0);
     const int self = t.jpos[((size_t)e * DIM + 0) * S + H];
     const int rb1 = rowptr[r * 3 + 1], rb2 = rowptr[r * 3 + 2];
-    J[rb1 + self + 0] += p.coriolis * u2 / (u0 * u0);
-    J[rb1 + self + 2] += -p.coriolis / u0;
-    J[rb2 + self + 1] += p.coriolis / u0;
-    J[rb2 + self + 0] += -p.coriolis * u1 / (u0 * u0);
+    J[rb1 + self + 0] += div_rn(p.coriolis * u2, (u0 * u0));
+    J[rb1 + self + 2] += div_rn(-p.coriolis, u0);
+    J[rb2 + self + 1] += div_rn(p.coriolis, u0);
+    J[rb2 + self + 0] += div_rn(-p.coriolis * u1, (u0 * u0));
   }
 #pragma unroll
   for (int d = 0; d < NDPC; ++d) V[(size_t)r * NDPC + d] = v[d];
@@ -623,13 +623,13 @@ k_rows_vj_inner_par(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U
       const int c = t.cell[e];
       const double u0 = __ldg(U + (size_t)c * 3), u1 = __ldg(U + (size_t)c * 3 + 1),
                    u2 = __ldg(U + (size_t)c * 3 + 2);
-      if (j == 0 && k == 1) vk -= p.coriolis * u2 / u0;
-      if (j == 0 && k == 2) vk += p.coriolis * u1 / u0;
+      if (j == 0 && k == 1) vk -= div_rn(p.coriolis * u2, u0);
+      if (j == 0 && k == 2) vk += div_rn(p.coriolis * u1, u0);
       const int self = t.jpos[((size_t)e * DIM + 0) * S + H] / NDPC;
-      if (k == 1 && j == 0) acc[self] += p.coriolis * u2 / (u0 * u0);
-      if (k == 1 && j == 2) acc[self] += -p.coriolis / u0;
-      if (k == 2 && j == 1) acc[self] += p.coriolis / u0;
-      if (k == 2 && j == 0) acc[self] += -p.coriolis * u1 / (u0 * u0);
+      if (k == 1 && j == 0) acc[self] += div_rn(p.coriolis * u2, (u0 * u0));
+      if (k == 1 && j == 2) acc[self] += div_rn(-p.coriolis, u0);
+      if (k == 2 && j == 1) acc[self] += div_rn(p.coriolis, u0);
+      if (k == 2 && j == 0) acc[self] += div_rn(-p.coriolis * u1, (u0 * u0));
     }
     if (j == 0) V[(size_t)r * NDPC + k] = vk;
     const int rb = rowptr[r * NDPC + k];
@@ -750,13 +750,13 @@ k_rows_vj_nearbd_par(RowTable t, MeshArgs m, Phys p, const double *__restrict__ 
       const int c = t.cell[e];
       const double u0 = __ldg(U + (size_t)c * 3), u1 = __ldg(U + (size_t)c * 3 + 1),
                    u2 = __ldg(U + (size_t)c * 3 + 2);
-      if (j == 0 && k == 1) vk -= p.coriolis * u2 / u0;
-      if (j == 0 && k == 2) vk += p.coriolis * u1 / u0;
+      if (j == 0 && k == 1) vk -= div_rn(p.coriolis * u2, u0);
+      if (j == 0 && k == 2) vk += div_rn(p.coriolis * u1, u0);
       const int self = t.jpos1[((size_t)e * DIM + 0) * 3 + 1] / 3;
-      if (k == 1 && j == 0) acc[self] += p.coriolis * u2 / (u0 * u0);
-      if (k == 1 && j == 2) acc[self] += -p.coriolis / u0;
-      if (k == 2 && j == 1) acc[self] += p.coriolis / u0;
-      if (k == 2 && j == 0) acc[self] += -p.coriolis * u1 / (u0 * u0);
+      if (k == 1 && j == 0) acc[self] += div_rn(p.coriolis * u2, (u0 * u0));
+      if (k == 1 && j == 2) acc[self] += div_rn(-p.coriolis, u0);
+      if (k == 2 && j == 1) acc[self] += div_rn(p.coriolis, u0);
+      if (k == 2 && j == 0) acc[self] += div_rn(-p.coriolis * u1, (u0 * u0));
     }
     if (j == 0) V[(size_t)r * NDPC + k] = vk;
     const int rb = rowptr[r * NDPC + k];
@@ -856,8 +856,8 @@ k_rows_velocity_par(RowTable ta, RowTable tb, int nbA, int rpb, MeshArgs m, Phys
         const int c = t.cell[e];
         const double u0 = __ldg(U + (size_t)c * 3), u1 = __ldg(U + (size_t)c * 3 + 1),
                      u2 = __ldg(U + (size_t)c * 3 + 2);
-        if (k == 1) vk -= p.coriolis * u2 / u0;
-        if (k == 2) vk += p.coriolis * u1 / u0;
+        if (k == 1) vk -= div_rn(p.coriolis * u2, u0);
+        if (k == 2) vk += div_rn(p.coriolis * u1, u0);
       }
       V[(size_t)t.rows[e] * NDPC + k] = vk;
     }
@@ -945,13 +945,13 @@ k_rows_vj_nearbd(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U,
     const int c = t.cell[e];
     const double u0 = __ldg(U + (size_t)c * 3), u1 = __ldg(U + (size_t)c * 3 + 1),
                  u2 = __ldg(U + (size_t)c * 3 + 2);
-    v[1] -= p.coriolis * u2 / u0;
-    v[2] += p.coriolis * u1 / u0;
+    v[1] -= div_rn(p.coriolis * u2, u0);
+    v[2] += div_rn(p.coriolis * u1, u0);
     const int self = t.jpos1[((size_t)e * DIM + 0) * 3 + 1] / 3;
-    acc[(self * 3 + 1) * 3 + 0] += p.coriolis * u2 / (u0 * u0);
-    acc[(self * 3 + 1) * 3 + 2] += -p.coriolis / u0;
-    acc[(self * 3 + 2) * 3 + 1] += p.coriolis / u0;
-    acc[(self * 3 + 2) * 3 + 0] += -p.coriolis * u1 / (u0 * u0);
+    acc[(self * 3 + 1) * 3 + 0] += div_rn(p.coriolis * u2, (u0 * u0));
+    acc[(self * 3 + 1) * 3 + 2] += div_rn(-p.coriolis, u0);
+    acc[(self * 3 + 2) * 3 + 1] += div_rn(p.coriolis, u0);
+    acc[(self * 3 + 2) * 3 + 0] += div_rn(-p.coriolis * u1, (u0 * u0));
   }
 #pragma unroll
   for (int d = 0; d < NDPC; ++d) V[(size_t)r * NDPC + d] = v[d];
