@@ -208,9 +208,11 @@ __device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &
   for (int d = 0; d < NDPC; ++d) Fout[o * NDPC + d] = fl[d];
 }
 
-// grid: x = line groups of NR lines, y = face chunks of TW faces
+// grid: x = line groups of NR lines, y = face chunks of TW faces; registers
+// capped for 32 resident warps per SM (0.634 against 0.638 ms per 1024^2
+// face pass at the uncapped 68 registers)
 template <int FAM, int SCHEME, int AXIS, int NR, int LANES = 64>
-__global__ void __launch_bounds__(LANES *NR)
+__global__ void __launch_bounds__(LANES *NR, 1024 / (LANES * NR))
 k_faces_tile(Box b, Phys p, const double *__restrict__ U, double *__restrict__ Fout) {
   __shared__ FaceTileSmem<FAM, SCHEME, NR, LANES> sm;
   face_tile<FAM, SCHEME, AXIS, NR, LANES>(sm, b, p, U, Fout, (long)blockIdx.x, (int)blockIdx.y);
