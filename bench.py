@@ -38,14 +38,14 @@ BYTES_PER_CELL = 16 * NDPC  # read U once + write V once (FP64)
 # + 10 divisions + 3 square roots; two faces per cell plus the 24-flop
 # balance; a division or square root counts as one operation).
 # DRAM bytes (read + write) per cell of one face launch, measured by ncu on
-# k_faces_tile at 2048^2 (x-axis launch: 134.3 MB read + 91.2 MB written);
+# k_faces_tile at 2048^2 (x-axis launch: 135.3 MB read + 96.3 MB written);
 # traffic grows in proportion to the cells, so it scales to other sizes
-FACE_TRAFFIC_BYTES_PER_CELL = (134.31e6 + 91.17e6) / 2048 ** 2
+FACE_TRAFFIC_BYTES_PER_CELL = (135.32e6 + 96.27e6) / 2048 ** 2
 # FP64 instructions the face kernel executes per face (ncu thread-instruction
-# counters dadd + dmul + dfma of the same capture, 268.3 per face): the work
+# counters dadd + dmul + dfma of the same capture, 270.7 per face): the work
 # the FP64 pipe actually does, after the divisions, square roots and
 # products by constants moved to the integer pipe
-FP64_INST_PER_FACE = 268.3
+FP64_INST_PER_FACE = 270.7
 FLOPS_PER_CELL = 2 * (4 * 2 * (71 + 4) + 65 + 10 + 3) + 24
 L2_FLUSH_BYTES = 256 << 20
 

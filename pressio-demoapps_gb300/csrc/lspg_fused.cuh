@@ -281,12 +281,13 @@ k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p,
     if constexpr (FAM == Swe2d) {
       // Coriolis source (swe_2d_prob_class.hpp:983-1012) and its Jacobian
       const double u0 = y[0], u1 = y[1], u2 = y[2];
-      sSrc[rl][1] = -(p.coriolis * u2 / u0);
-      sSrc[rl][2] = p.coriolis * u1 / u0;
-      sSJ[rl][1 * 3 + 0] = p.coriolis * u2 / (u0 * u0);
-      sSJ[rl][1 * 3 + 2] = -p.coriolis / u0;
-      sSJ[rl][2 * 3 + 1] = p.coriolis / u0;
-      sSJ[rl][2 * 3 + 0] = -p.coriolis * u1 / (u0 * u0);
+      // (divisions on the integer pipe, the IEEE quotients)
+      sSrc[rl][1] = -div_rn(p.coriolis * u2, u0);
+      sSrc[rl][2] = div_rn(p.coriolis * u1, u0);
+      sSJ[rl][1 * 3 + 0] = div_rn(p.coriolis * u2, (u0 * u0));
+      sSJ[rl][1 * 3 + 2] = div_rn(-p.coriolis, u0);
+      sSJ[rl][2 * 3 + 1] = div_rn(p.coriolis, u0);
+      sSJ[rl][2 * 3 + 0] = div_rn(-p.coriolis * u1, (u0 * u0));
     }
   };
   auto combine = [&](int rl, int f) {
