@@ -80,6 +80,8 @@ _SIGS = {
     "pda_mesh_create_sample": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.c_int64,
                                          C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]),
     "pda_mesh_write": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "pda_mesh_write_binary": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "pda_mesh_load_binary": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
     "pda_mesh_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int64),
                                 C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "pda_mesh_arrays": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -298,10 +300,21 @@ class CellCenteredUniformMesh:
     def write(self, directory):
         _check(lib().pda_mesh_write(self._h, os.fsencode(directory)))
 
+    def write_binary(self, path):
+        """Write the mesh as one binary file (load_mesh_binary reads it)."""
+        _check(lib().pda_mesh_write_binary(self._h, os.fsencode(str(path))))
+
 
 def load_cellcentered_uniform_mesh(directory) -> CellCenteredUniformMesh:
     h = C.c_void_p()
     _check(lib().pda_mesh_load(os.fsencode(str(directory)), C.byref(h)))
+    return CellCenteredUniformMesh(h)
+
+
+def load_mesh_binary(path) -> CellCenteredUniformMesh:
+    """Load a mesh written by CellCenteredUniformMesh.write_binary."""
+    h = C.c_void_p()
+    _check(lib().pda_mesh_load_binary(os.fsencode(str(path)), C.byref(h)))
     return CellCenteredUniformMesh(h)
 
 

@@ -57,6 +57,8 @@ double round14(double v);
 Mesh mesh_generate_full(const int n[3], const double bounds[6], int stencil, const int periodic[3]);
 Mesh mesh_load(const std::string &dir);
 void mesh_write(const Mesh &m, const std::string &dir);
+void mesh_write_binary(const Mesh &m, const std::string &path);
+Mesh mesh_load_binary(const std::string &path);
 Mesh mesh_sample(const Mesh &full, const std::vector<int64_t> &gids, std::vector<int64_t> *stencilGids);
 void mesh_detect_structure(Mesh &m, const int nInfo[3], bool haveN);
 

@@ -1,4 +1,5 @@
-// Mesh files, native full-mesh and sample-mesh generators, and the
+// Mesh files (the reference's text format and a binary format of this
+// library), native full-mesh and sample-mesh generators, and the
 // inner/near-boundary row classification.
 //
 // The generators reproduce the connectivity rules of the reference's
@@ -10,6 +11,7 @@
 // than the stencil) is kept as in the scripts because it defines the format.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -429,6 +431,172 @@ void mesh_write(const Mesh &m, const std::string &dir) {
     }
     std::fclose(f);
   }
+}
+
+// ----------------------------------------------------------- binary files
+// One little-endian file: a fixed header, the graph (int32, row-major), the
+// x and y coordinates (and z in 3D) as doubles, then a 64-bit checksum of
+// every byte before it.  The header carries what info.dat carries plus the
+// structured-mesh descriptor, so loading needs no graph comparison.
+namespace {
+constexpr char kBinMagic[8] = {'P', 'D', 'A', 'M', 'E', 'S', 'H', '1'};
+constexpr uint32_t kBinByteOrder = 0x01020304u;
+
+struct BinHeader {
+  char magic[8];
+  uint32_t byteOrder;
+  uint32_t headerBytes;
+  int32_t dim, stencil, ncols, structured;
+  int64_t stencilMeshSize, sampleMeshSize;
+  double dx[3];
+  double bounds[6];
+  int32_t hasBounds, reserved;
+  int32_t n[3], periodic[3];
+};
+static_assert(sizeof(BinHeader) % 8 == 0, "header keeps the arrays 8-byte aligned");
+
+// 64-bit multiply-xorshift over 8-byte words (a tail shorter than 8 bytes is
+// zero-padded): detects truncation and corruption, not tampering
+struct Checksum {
+  uint64_t h = 0x9E3779B97F4A7C15ull;
+  void add(const void *data, size_t bytes) {
+    const unsigned char *c = static_cast<const unsigned char *>(data);
+    size_t k = 0;
+    for (; k + 8 <= bytes; k += 8) {
+      uint64_t w;
+      std::memcpy(&w, c + k, 8);
+      word(w);
+    }
+    if (k < bytes) {
+      uint64_t w = 0;
+      std::memcpy(&w, c + k, bytes - k);
+      word(w);
+    }
+  }
+  void word(uint64_t w) {
+    h ^= w + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+    h *= 0xFF51AFD7ED558CCDull;
+    h ^= h >> 33;
+  }
+};
+
+size_t graph_bytes(const Mesh &m) { return (size_t)m.sampleMeshSize * m.ncols * sizeof(int32_t); }
+size_t pad8(size_t b) { return (b + 7) / 8 * 8; }
+}  // namespace
+
+void mesh_write_binary(const Mesh &m, const std::string &path) {
+  BinHeader h;
+  std::memset(&h, 0, sizeof h);
+  std::memcpy(h.magic, kBinMagic, 8);
+  h.byteOrder = kBinByteOrder;
+  h.headerBytes = sizeof(BinHeader);
+  h.dim = m.dim;
+  h.stencil = m.stencil;
+  h.ncols = m.ncols;
+  h.structured = m.structured ? 1 : 0;
+  h.stencilMeshSize = m.stencilMeshSize;
+  h.sampleMeshSize = m.sampleMeshSize;
+  for (int a = 0; a < 3; ++a) {
+    h.dx[a] = m.dx[a];
+    h.n[a] = m.n[a];
+    h.periodic[a] = m.periodic[a];
+  }
+  for (int k = 0; k < 6; ++k) h.bounds[k] = m.bounds[k];
+  h.hasBounds = m.hasBounds ? 1 : 0;
+  std::FILE *f = std::fopen(path.c_str(), "wb");
+  PDA_REQUIRE(f, PDA_ERR_IO, "cannot write " + path);
+  Checksum cs;
+  bool ok = true;
+  auto put = [&](const void *p, size_t bytes) {
+    if (bytes == 0 || !ok) return;
+    ok = std::fwrite(p, 1, bytes, f) == bytes;
+    cs.add(p, bytes);
+  };
+  put(&h, sizeof h);
+  put(m.graph.data(), graph_bytes(m));
+  const char zeros[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  put(zeros, pad8(graph_bytes(m)) - graph_bytes(m));
+  const size_t nc = (size_t)m.stencilMeshSize * sizeof(double);
+  put(m.x.data(), nc);
+  put(m.y.data(), nc);
+  if (m.dim == 3) put(m.z.data(), nc);
+  const uint64_t sum = cs.h;
+  if (ok) ok = std::fwrite(&sum, 1, 8, f) == 8;
+  ok = (std::fclose(f) == 0) && ok;
+  PDA_REQUIRE(ok, PDA_ERR_IO, "write failed: " + path);
+}
+
+Mesh mesh_load_binary(const std::string &path) {
+  std::FILE *f = std::fopen(path.c_str(), "rb");
+  PDA_REQUIRE(f, PDA_ERR_IO, "file not found " + path);
+  struct Closer {
+    std::FILE *f;
+    ~Closer() { std::fclose(f); }
+  } closer{f};
+  std::fseek(f, 0, SEEK_END);
+  const long long fileBytes = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  BinHeader h;
+  PDA_REQUIRE(fileBytes >= (long long)sizeof h && std::fread(&h, 1, sizeof h, f) == sizeof h, PDA_ERR_IO,
+              path + ": not a binary mesh file (too short)");
+  PDA_REQUIRE(std::memcmp(h.magic, kBinMagic, 8) == 0, PDA_ERR_IO, path + ": not a binary mesh file");
+  PDA_REQUIRE(h.byteOrder == kBinByteOrder, PDA_ERR_IO, path + ": written with another byte order");
+  PDA_REQUIRE(h.headerBytes == sizeof h, PDA_ERR_IO, path + ": unsupported binary mesh version");
+  PDA_REQUIRE(h.dim >= 1 && h.dim <= 3, PDA_ERR_IO, path + ": invalid dim");
+  PDA_REQUIRE(h.stencil == 3 || h.stencil == 5 || h.stencil == 7, PDA_ERR_IO, path + ": invalid stencil size");
+  PDA_REQUIRE(h.ncols == 1 + (h.stencil - 1) * h.dim, PDA_ERR_IO, path + ": invalid graph width");
+  PDA_REQUIRE(h.sampleMeshSize > 0 && h.stencilMeshSize > 0 && h.sampleMeshSize <= h.stencilMeshSize &&
+                  h.stencilMeshSize < (int64_t)1 << 31,
+              PDA_ERR_IO, path + ": invalid mesh sizes");
+  Mesh m;
+  m.dim = h.dim;
+  m.stencil = h.stencil;
+  m.ncols = h.ncols;
+  m.sampleMeshSize = h.sampleMeshSize;
+  m.stencilMeshSize = h.stencilMeshSize;
+  const size_t gb = graph_bytes(m), nc = (size_t)m.stencilMeshSize * sizeof(double);
+  const size_t expect = sizeof h + pad8(gb) + nc * (m.dim == 3 ? 3 : 2) + 8;
+  PDA_REQUIRE((size_t)fileBytes == expect, PDA_ERR_IO, path + ": truncated or oversized binary mesh file");
+  Checksum cs;
+  cs.add(&h, sizeof h);
+  auto get = [&](void *p, size_t bytes) {
+    if (bytes == 0) return;
+    PDA_REQUIRE(std::fread(p, 1, bytes, f) == bytes, PDA_ERR_IO, path + ": read failed");
+    cs.add(p, bytes);
+  };
+  m.graph.resize((size_t)m.sampleMeshSize * m.ncols);
+  get(m.graph.data(), gb);
+  char pad[8];
+  get(pad, pad8(gb) - gb);
+  m.x.resize(m.stencilMeshSize);
+  m.y.resize(m.stencilMeshSize);
+  m.z.assign(m.stencilMeshSize, 0.0);
+  get(m.x.data(), nc);
+  get(m.y.data(), nc);
+  if (m.dim == 3) get(m.z.data(), nc);
+  uint64_t sum = 0;
+  PDA_REQUIRE(std::fread(&sum, 1, 8, f) == 8, PDA_ERR_IO, path + ": read failed");
+  PDA_REQUIRE(sum == cs.h, PDA_ERR_IO, path + ": checksum mismatch (corrupt binary mesh file)");
+  for (int64_t r = 0; r < m.sampleMeshSize; ++r)
+    for (int c = 0; c < m.ncols; ++c) {
+      const int32_t v = m.g(r, c);
+      PDA_REQUIRE(v >= -1 && v < m.stencilMeshSize && (c > 0 ? true : v >= 0), PDA_ERR_IO,
+                  path + ": cell id out of range");
+    }
+  for (int a = 0; a < 3; ++a) {
+    m.dx[a] = h.dx[a];
+    m.dxInv[a] = a < m.dim ? 1.0 / h.dx[a] : 0.0;
+    m.n[a] = h.n[a];
+    m.periodic[a] = h.periodic[a];
+  }
+  for (int k = 0; k < 6; ++k) m.bounds[k] = h.bounds[k];
+  m.hasBounds = h.hasBounds != 0;
+  m.classify();
+  m.structured = h.structured != 0;
+  if (m.structured)
+    PDA_REQUIRE(m.sampleMeshSize == m.stencilMeshSize && (int64_t)m.n[0] * m.n[1] * m.n[2] == m.sampleMeshSize,
+                PDA_ERR_IO, path + ": inconsistent structured-mesh descriptor");
+  return m;
 }
 
 // create_sample_mesh.py:54-137

@@ -1192,6 +1192,22 @@ pda_status pda_mesh_write(const pda_mesh *m, const char *dir) {
   PDA_API_END
 }
 
+pda_status pda_mesh_write_binary(const pda_mesh *m, const char *path) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(m && path, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  pda::mesh_write_binary(m->m, path);
+  PDA_API_END
+}
+
+pda_status pda_mesh_load_binary(const char *path, pda_mesh **out) {
+  PDA_API_BEGIN
+  PDA_REQUIRE(path && out, PDA_ERR_INVALID_ARGUMENT, "null argument");
+  std::unique_ptr<pda_mesh> m(new pda_mesh);
+  m->m = pda::mesh_load_binary(path);
+  *out = m.release();
+  PDA_API_END
+}
+
 pda_status pda_mesh_info(const pda_mesh *mm, int dims[3], int64_t sizes[4], double dx[3], double dxinv[3],
                          int flags[2]) {
   PDA_API_BEGIN

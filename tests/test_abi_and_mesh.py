@@ -160,3 +160,93 @@ def test_parameters_and_errors(pda):
         bad.initialConditionHost()
     with pytest.raises(pda.PdaError):  # PeriodicSmooth needs a fully periodic mesh
         pda.create_problem(e2, pda.Euler2d.PeriodicSmooth, pda.InviscidFluxReconstruction.Weno5, stream=0)
+
+
+def _mesh_equal(a, b):
+    assert (a.dimensionality(), a.stencilSize(), a.sampleMeshSize(), a.stencilMeshSize()) == \
+        (b.dimensionality(), b.stencilSize(), b.sampleMeshSize(), b.stencilMeshSize())
+    assert a.isStructured() == b.isStructured() and a.isFullyPeriodic() == b.isFullyPeriodic()
+    assert a.dx() == b.dx() and a.dxInv() == b.dxInv()
+    for u, v in zip(a._arrays(), b._arrays()):
+        assert u.dtype == v.dtype and np.array_equal(u, v)
+
+
+@pytest.mark.parametrize("n,bounds,st,per", [
+    ((40,), (-0.5, 0.5), 7, (False,)),
+    ((24, 18), (0.0, 1.0, 0.0, 2.0), 5, (False, True)),
+    ((12, 10, 8), (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0), 7, (True, True, True)),
+    ((9, 11, 6), (0.0, 1.0, 0.0, 1.0, 0.0, 1.0), 3, (False, False, False)),
+])
+def test_binary_mesh_round_trip(pda, tmp_path, n, bounds, st, per):
+    """The library's binary mesh file gives back the mesh written, bit for
+    bit: graph, coordinates, spacing, row classification and the structured
+    descriptor (1D, 2D and 3D; periodic and bounded axes)."""
+    m = pda.create_full_mesh(n, bounds, st, per)
+    f = tmp_path / "mesh.bin"
+    m.write_binary(f)
+    _mesh_equal(pda.load_mesh_binary(f), m)
+
+
+@pytest.mark.parametrize("name", ["m2d_s7_20", "s2d_s7_10", "m2d_s7_16_per"])
+def test_binary_mesh_equals_text_mesh(pda, tmp_path, name):
+    """A mesh read from the reference's text files (full, sample and periodic)
+    and saved in the binary format loads back identical."""
+    m = pda.load_cellcentered_uniform_mesh(mesh_dir(name))
+    f = tmp_path / "mesh.bin"
+    m.write_binary(f)
+    _mesh_equal(pda.load_mesh_binary(f), m)
+
+
+def test_binary_mesh_sample_round_trip(pda, tmp_path):
+    full = pda.create_full_mesh((30, 20), (0.0, 1.0, 0.0, 1.0), 7)
+    sm, _ = pda.create_sample_mesh(full, np.arange(0, 600, 7, dtype=np.int64))
+    f = tmp_path / "sample.bin"
+    sm.write_binary(f)
+    _mesh_equal(pda.load_mesh_binary(f), sm)
+
+
+def test_binary_mesh_rejects_bad_files(pda, tmp_path):
+    """Missing, truncated, corrupt and foreign files are PDA_ERR_IO, never a
+    crash or a silently wrong mesh."""
+    m = pda.create_full_mesh((16, 16), (0.0, 1.0, 0.0, 1.0), 5)
+    good = tmp_path / "good.bin"
+    m.write_binary(good)
+    data = good.read_bytes()
+    cases = {
+        "missing": None,
+        "truncated": data[:-9],
+        "extended": data + b"\0" * 8,
+        "flipped": data[:300] + bytes([data[300] ^ 0x10]) + data[301:],
+        "magic": b"XDAMESH1" + data[8:],
+        "text": b"dim 2\n",
+    }
+    for name, blob in cases.items():
+        f = tmp_path / (name + ".bin")
+        if blob is not None:
+            f.write_bytes(blob)
+        with pytest.raises(pda.PdaError) as e:
+            pda.load_mesh_binary(f)
+        assert e.value.code == -2, name
+
+
+@pytest.mark.gpu
+def test_problem_on_binary_mesh_equals_text_mesh(pda, tmp_path):
+    """A problem built on the binary-loaded mesh evaluates the same velocity
+    and Jacobian as on the text-loaded mesh, bit for bit."""
+    import torch
+    m = MANIFEST["riemann_w5"]
+    g = golden_case("riemann_w5")
+    text = pda.load_cellcentered_uniform_mesh(mesh_dir(m["mesh"]))
+    f = tmp_path / "mesh.bin"
+    text.write_binary(f)
+    binm = pda.load_mesh_binary(f)
+    out = []
+    for mesh in (text, binm):
+        p = create_case_problem(pda, m, mesh)
+        U = torch.from_numpy(g["U1"]).cuda()
+        V = p.createVelocity()
+        J = p.createJacobian()
+        p.rightHandSideAndJacobian(U, 0.0, V, J)
+        torch.cuda.synchronize()
+        out.append((V.cpu().numpy(), J.values.cpu().numpy()))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
