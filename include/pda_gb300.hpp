@@ -52,6 +52,8 @@ class Mesh {
   int stencilSize() const { return info().first[1]; }
   int64_t stencilMeshSize() const { return info().second[0]; }
   int64_t sampleMeshSize() const { return info().second[1]; }
+  // the library's one-file binary format (load_mesh_binary reads it back)
+  void write_binary(const std::string &path) const { check(pda_mesh_write_binary(h_.get(), path.c_str())); }
 
  private:
   std::pair<std::vector<int>, std::vector<int64_t>> info() const {
@@ -66,6 +68,12 @@ class Mesh {
 inline Mesh load_cellcentered_uniform_mesh(const std::string &dir) {
   pda_mesh *m = nullptr;
   check(pda_mesh_load(dir.c_str(), &m));
+  return Mesh(m);
+}
+
+inline Mesh load_mesh_binary(const std::string &path) {
+  pda_mesh *m = nullptr;
+  check(pda_mesh_load_binary(path.c_str(), &m));
   return Mesh(m);
 }
 
