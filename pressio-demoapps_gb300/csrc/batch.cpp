@@ -6,8 +6,8 @@
 // instances loops over problem objects, one velocity call (and, on a GPU,
 // several kernel launches) per instance and stage.  Here the instances'
 // states are packed into one vector and each phase of the residual is one
-// persistent launch over all of them (batch.cuh), with per-instance boxes,
-// mesh spacings and physical parameters read from a device table.
+// launch over all of them (batch.cuh), with per-instance boxes, mesh
+// spacings and physical parameters read from a device table.
 #include <algorithm>
 #include <cstring>
 #include <memory>
