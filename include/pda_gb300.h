@@ -425,7 +425,8 @@ int64_t pda_problem_launch_count(const pda_problem *p);
 /* Evaluate the velocity reps times with CUDA events between the kernels of
  * the structured path; ms[5] receives the mean device time of the face
  * kernels along x, y, z, the balance kernel and the near-boundary row
- * kernel (0 where absent). */
+ * kernel (0 where absent).  The kernels run one after another here;
+ * pda_velocity runs the face passes of different axes side by side. */
 pda_status pda_profile_velocity(pda_problem *p, const double *d_U, double *d_V, int reps,
                                 double ms[5]);
 

@@ -704,8 +704,32 @@ void velocity(pda_problem &P, const double *U, double *V, double t, cudaEvent_t 
       Fb[a] = P.F[a].p;
     }
     int nl = 0;
-    P.L->struct_velocity(P.scheme, b, ma, P.phys, U, Fb, V, P.stream, &nl, ev);
-    check_launch(P, nl);
+    if (!ev && P.dim >= 2) {
+      // the face passes of different axes are independent (separate face
+      // arrays): the y faces run on the side stream beside the x (and z)
+      // faces, so each pass's last, partly filled wave overlaps the other's
+      // (1024^2 Riemann WENO5: 1.302 ms per velocity against 1.319 ms with
+      // the passes in sequence).  The profiling path (ev) keeps the
+      // sequence, one pass at a time.
+      if (!P.side) {
+        PDA_CUDA(cudaStreamCreateWithFlags(&P.side, cudaStreamNonBlocking));
+        PDA_CUDA(cudaEventCreateWithFlags(&P.evFork, cudaEventDisableTiming));
+        PDA_CUDA(cudaEventCreateWithFlags(&P.evJoin, cudaEventDisableTiming));
+      }
+      PDA_CUDA(cudaEventRecord(P.evFork, P.stream));
+      PDA_CUDA(cudaStreamWaitEvent(P.side, P.evFork, 0));
+      P.L->struct_faces(P.scheme, 0, b, P.phys, U, Fb[0], P.stream);
+      P.L->struct_faces(P.scheme, 1, b, P.phys, U, Fb[1], P.side);
+      if (P.dim == 3) P.L->struct_faces(P.scheme, 2, b, P.phys, U, Fb[2], P.stream);
+      PDA_CUDA(cudaEventRecord(P.evJoin, P.side));
+      PDA_CUDA(cudaStreamWaitEvent(P.stream, P.evJoin, 0));
+      const double *Fc[3] = {Fb[0], Fb[1], Fb[2]};
+      P.L->struct_balance(b, ma, P.phys, U, Fc, V, P.stream);
+      check_launch(P, P.dim + 1);
+    } else {
+      P.L->struct_velocity(P.scheme, b, ma, P.phys, U, Fb, V, P.stream, &nl, ev);
+      check_launch(P, nl);
+    }
   }
   // the row tables in one launch: inner rows (when no structured box covers
   // them) and near-boundary rows
