@@ -49,8 +49,9 @@ template <> struct SchemeTraits<Weno5> { static constexpr int h = 3; };
 // on the integer pipe (fp64_intpipe.cuh): the IEEE round-to-nearest results,
 // bit for bit, without occupying GB300's FP64 pipe (one warp instruction per
 // ~64 cycles per SM sub-partition), which is left to the multiplications and
-// additions.  INL = true expands them in place (the residual's face kernels);
-// otherwise they are calls.  Host code uses the operators.  Compiling with
+// additions.  INL = true expands them in place; otherwise (every kernel of
+// the library) they are calls: inlined, the face kernels outgrew the
+// instruction cache and ran slower.  Host code uses the operators.  Compiling with
 // -DPDA_FP64_PIPE_DIVSQRT selects the FP64-pipe operations on the device too
 // (the same results), for comparison.
 template <bool INL = false>
