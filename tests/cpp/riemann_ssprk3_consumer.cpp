@@ -1,6 +1,7 @@
 // A C++ consumer of the library through include/pda_gb300.hpp, following the
 // flow of the reference test tests_cpp/eigen_2d_euler_riemann_explicit/main.cc:
-// load a mesh, create_problem(Euler2d::Riemann, scheme, icFlag 2), take the
+// load a mesh (here also written to and read back from the library's binary
+// mesh file), create_problem(Euler2d::Riemann, scheme, icFlag 2), take the
 // initial condition, advance SSP-RK3 with dt = 0.01 for 0.6 / dt steps.
 //
 // Two drivers over the same problem object:
@@ -47,7 +48,12 @@ int main(int argc, char **argv) {
     return 2;
   }
   namespace pda = pda_gb300;
-  const auto mesh = pda::load_cellcentered_uniform_mesh(argv[1]);
+  // the reference's text mesh, passed through the library's binary mesh
+  // file (written next to the outputs, then loaded back)
+  const auto textMesh = pda::load_cellcentered_uniform_mesh(argv[1]);
+  const std::string binPath = std::string(argv[5]) + ".mesh.bin";
+  textMesh.write_binary(binPath);
+  const auto mesh = pda::load_mesh_binary(binPath);
   const auto order = static_cast<pda::InviscidFluxReconstruction>(std::atoi(argv[2]));
   const double dt = std::atof(argv[3]);
   const long nsteps = std::atol(argv[4]);
