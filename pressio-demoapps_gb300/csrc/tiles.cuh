@@ -208,11 +208,22 @@ __device__ __forceinline__ void face_tile(FaceTileSmem<FAM, SCHEME, NR, LANES> &
   for (int d = 0; d < NDPC; ++d) Fout[o * NDPC + d] = fl[d];
 }
 
-// grid: x = line groups of NR lines, y = face chunks of TW faces; registers
-// capped for 32 resident warps per SM (0.634 against 0.638 ms per 1024^2
-// face pass at the uncapped 68 registers)
+// Resident blocks per SM the register allocation must allow: 32 warps per SM,
+// or fewer where the tile's shared memory admits fewer blocks (3D: 7), so the
+// cap never forces spills that buy no occupancy.  2D Euler, 1024^2: 0.634
+// against 0.638 ms per face pass at the uncapped 68 registers.
+template <int FAM, int SCHEME, int NR, int LANES>
+struct FaceTileMinBlocks {
+  static constexpr int kSmemPerSM = 228 * 1024, kReservedPerBlock = 1024;
+  static constexpr int bySmem =
+      kSmemPerSM / ((int)sizeof(FaceTileSmem<FAM, SCHEME, NR, LANES>) + kReservedPerBlock);
+  static constexpr int byWarps = 1024 / (LANES * NR);
+  static constexpr int value = bySmem < byWarps ? (bySmem > 0 ? bySmem : 1) : byWarps;
+};
+
+// grid: x = line groups of NR lines, y = face chunks of TW faces
 template <int FAM, int SCHEME, int AXIS, int NR, int LANES = 64>
-__global__ void __launch_bounds__(LANES *NR, 1024 / (LANES * NR))
+__global__ void __launch_bounds__(LANES *NR, (FaceTileMinBlocks<FAM, SCHEME, NR, LANES>::value))
 k_faces_tile(Box b, Phys p, const double *__restrict__ U, double *__restrict__ Fout) {
   __shared__ FaceTileSmem<FAM, SCHEME, NR, LANES> sm;
   face_tile<FAM, SCHEME, AXIS, NR, LANES>(sm, b, p, U, Fout, (long)blockIdx.x, (int)blockIdx.y);
