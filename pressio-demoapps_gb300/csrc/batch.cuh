@@ -31,12 +31,13 @@ __device__ __forceinline__ int batch_find(const long *__restrict__ start, int n,
 }
 
 // One block per tile of any instance (grid = all tiles of the axis), with
-// registers capped for 32 resident warps per SM.  Measured on 512 shallow-
-// water instances: 169 ms per SSP-RK3 step, against 193 ms for a persistent
-// loop over the tiles (its loop state raised the registers from 74 to 80: 6
-// blocks per SM) and 178 ms for one block per tile without the cap.
+// registers capped for 32 resident warps per SM (fewer where the tile's
+// shared memory admits fewer blocks, FaceTileMinBlocks).  Measured on 512
+// shallow-water instances: 169 ms per SSP-RK3 step, against 193 ms for a
+// persistent loop over the tiles (its loop state raised the registers from
+// 74 to 80: 6 blocks per SM) and 178 ms for one block per tile without the cap.
 template <int FAM, int SCHEME, int AXIS, int NR, int LANES>
-__global__ void __launch_bounds__(LANES *NR, 1024 / (LANES * NR))
+__global__ void __launch_bounds__(LANES *NR, (FaceTileMinBlocks<FAM, SCHEME, NR, LANES>::value))
 k_batch_faces_tile(BatchArgs a, const double *__restrict__ U, double *__restrict__ F) {
   __shared__ FaceTileSmem<FAM, SCHEME, NR, LANES> sm;
   const long t = blockIdx.x;
