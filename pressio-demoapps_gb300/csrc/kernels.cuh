@@ -41,6 +41,7 @@ template <> struct Fam<Euler1d> {
   static PDA_HD void flux_side(Side &o, const double q[3], const Phys &p) {
     euler3_side(o, q, p.gamma);
   }
+  static PDA_HD void flux_side_ax(Side &o, const double q[3], const Phys &p, int) { euler3_side(o, q, p.gamma); }
   template <int AXIS>
   static PDA_HD void flux_combine(double F[3], const double qL[3], const double qR[3], const Side &L,
                                   const Side &R, const Phys &p) {
@@ -62,6 +63,9 @@ template <> struct Fam<Euler2d> {
   template <int AXIS>
   static PDA_HD void flux_side(Side &o, const double q[4], const Phys &p) {
     euler4_side<AXIS>(o, q, p.gamma);
+  }
+  static PDA_HD void flux_side_ax(Side &o, const double q[4], const Phys &p, int ax) {
+    euler4_side_ax(o, q, p.gamma, ax);
   }
   template <int AXIS>
   static PDA_HD void flux_combine(double F[4], const double qL[4], const double qR[4], const Side &L,
@@ -85,6 +89,9 @@ template <> struct Fam<Euler3d> {
   static PDA_HD void flux_side(Side &o, const double q[5], const Phys &p) {
     euler5_side<AXIS>(o, q, p.gamma);
   }
+  static PDA_HD void flux_side_ax(Side &o, const double q[5], const Phys &p, int ax) {
+    euler5_side_ax(o, q, p.gamma, ax);
+  }
   template <int AXIS>
   static PDA_HD void flux_combine(double F[5], const double qL[5], const double qR[5], const Side &L,
                                   const Side &R, const Phys &p) {
@@ -106,6 +113,9 @@ template <> struct Fam<Swe2d> {
   template <int AXIS>
   static PDA_HD void flux_side(Side &o, const double q[3], const Phys &p) {
     swe_side<AXIS>(o, q, p.gravity);
+  }
+  static PDA_HD void flux_side_ax(Side &o, const double q[3], const Phys &p, int ax) {
+    swe_side_ax(o, q, p.gravity, ax);
   }
   template <int AXIS>
   static PDA_HD void flux_combine(double F[3], const double qL[3], const double qR[3], const Side &L,
@@ -827,20 +837,16 @@ k_rows_velocity_par(RowTable ta, RowTable tb, int nbA, int rpb, MeshArgs m, Phys
     if (part < 2 && slot < rpb * NF && e0 + rl < t.nrows) {
       const double *q = part == 0 ? fd[rl][f].uN : fd[rl][f].uP;
       typename F::Side &so = sSide[rl][f][part];
-      if (ax == 0) F::template flux_side<0>(so, q, p);
-      if constexpr (DIM > 1) if (ax == 1) F::template flux_side<1>(so, q, p);
-      if constexpr (DIM > 2) if (ax == 2) F::template flux_side<2>(so, q, p);
+      F::flux_side_ax(so, q, p, ax);  // one stream for all axes of the warp
     }
   }
   __syncthreads();
   if (tid < rpb * NF) {
-    const int rl = tid / NF, f = tid % NF, ax = f >> 1;
+    const int rl = tid / NF, f = tid % NF;
     if (e0 + rl < t.nrows) {
       VelFace<FAM> &o = fd[rl][f];
       const typename F::Side &L = sSide[rl][f][0], &R = sSide[rl][f][1];
-      if (ax == 0) F::template flux_combine<0>(o.fl, o.uN, o.uP, L, R, p);
-      if constexpr (DIM > 1) if (ax == 1) F::template flux_combine<1>(o.fl, o.uN, o.uP, L, R, p);
-      if constexpr (DIM > 2) if (ax == 2) F::template flux_combine<2>(o.fl, o.uN, o.uP, L, R, p);
+      F::template flux_combine<0>(o.fl, o.uN, o.uP, L, R, p);  // the combination does not depend on the axis
     }
   }
   __syncthreads();

@@ -292,11 +292,8 @@ k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p,
   };
   auto combine = [&](int rl, int f) {
     FF &o = fd[rl][f];
-    const int ax = f >> 1;
     const typename F::Side &L = sSide[rl][f][0], &R = sSide[rl][f][1];
-    if (ax == 0) F::template flux_combine<0>(o.fl, o.uN, o.uP, L, R, p);
-    if constexpr (DIM > 1) if (ax == 1) F::template flux_combine<1>(o.fl, o.uN, o.uP, L, R, p);
-    if constexpr (DIM > 2) if (ax == 2) F::template flux_combine<2>(o.fl, o.uN, o.uP, L, R, p);
+    F::template flux_combine<0>(o.fl, o.uN, o.uP, L, R, p);  // the combination does not depend on the axis
   };
   {  // phase B1: (part, row, face): parts 0 / 1 the left / right face state's
      // half of the flux (exact Jacobian: part 0 both halves and the flux,
@@ -314,9 +311,7 @@ k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p,
           const int side = kExact ? sd : part;
           const double *q = side == 0 ? o.uN : o.uP;
           typename F::Side &so = sSide[rl][f][side];
-          if (ax == 0) F::template flux_side<0>(so, q, p);
-          if constexpr (DIM > 1) if (ax == 1) F::template flux_side<1>(so, q, p);
-          if constexpr (DIM > 2) if (ax == 2) F::template flux_side<2>(so, q, p);
+          F::flux_side_ax(so, q, p, ax);  // one stream for all axes of the warp
         }
         if (kExact) combine(rl, f);
       } else {

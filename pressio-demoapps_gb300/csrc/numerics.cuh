@@ -738,7 +738,11 @@ PDA_HD void swe_flux(double F[3], const double qL[3], const double qR[3],
 // ---------------------------------------------------------------------------
 // The Rusanov fluxes above in two halves: flux_side (the quantities of one
 // face state: its velocities, enthalpy or sqrt(h), and physical flux) and
-// flux_combine (the Roe / wave-speed average and the Rusanov sum).
+// flux_combine (the Roe / wave-speed average and the Rusanov sum).  The side
+// takes the face normal as a runtime axis (*_side_ax; the templated form
+// passes its constant), so threads of one warp that hold faces of different
+// axes run one instruction stream; the combination does not depend on the
+// axis at all.
 // combine(side(qL), side(qR)) evaluates every expression of the *_flux
 // function above unchanged, so it is bit-identical; the halves let a kernel
 // compute the two states of a face on different warps.
@@ -773,23 +777,26 @@ PDA_HD void euler3_combine(double F[3], const double qL[3], const double qR[3], 
   for (int d = 0; d < 3; ++d) F[d] = half * (L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
 }
 
-template <int AXIS>
-PDA_HD void euler4_side(FluxSide<4> &o, const double q[4], double gamma) {
+PDA_HD void euler4_side_ax(FluxSide<4> &o, const double q[4], double gamma, int ax) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double r = q[0];
   const double u = div_rn(q[1], (r + es));
   const double v = div_rn(q[2], (r + es));
-  const double un = AXIS == 0 ? u : v;
+  const double un = ax == 0 ? u : v;
   const double p = (gamma - 1) * (q[3] - half * r * (u * u + v * v));
   const double H = div_rn((q[3] + p), r);
   o.F[0] = r * un;
-  o.F[1] = AXIS == 0 ? r * un * u + p : r * un * u;
-  o.F[2] = AXIS == 1 ? r * un * v + p : r * un * v;
+  o.F[1] = ax == 0 ? r * un * u + p : r * un * u;
+  o.F[2] = ax == 1 ? r * un * v + p : r * un * v;
   o.F[3] = r * un * H;
   o.u = u;
   o.v = v;
   o.H = H;
+}
+template <int AXIS>
+PDA_HD void euler4_side(FluxSide<4> &o, const double q[4], double gamma) {
+  euler4_side_ax(o, q, gamma, AXIS);
 }
 template <int AXIS>
 PDA_HD void euler4_combine(double F[4], const double qL[4], const double qR[4], const FluxSide<4> &L,
@@ -805,26 +812,29 @@ PDA_HD void euler4_combine(double F[4], const double qL[4], const double qR[4], 
   for (int d = 0; d < 4; ++d) F[d] = half * (L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
 }
 
-template <int AXIS>
-PDA_HD void euler5_side(FluxSide<5> &o, const double q[5], double gamma) {
+PDA_HD void euler5_side_ax(FluxSide<5> &o, const double q[5], double gamma, int ax) {
   constexpr double half = 1. / 2.;
   constexpr double es = 1.e-30;
   const double r = q[0];
   const double u = div_rn(q[1], (r + es));
   const double v = div_rn(q[2], (r + es));
   const double w = div_rn(q[3], (r + es));
-  const double un = AXIS == 0 ? u : (AXIS == 1 ? v : w);
+  const double un = ax == 0 ? u : (ax == 1 ? v : w);
   const double p = (gamma - 1) * (q[4] - half * r * (u * u + v * v + w * w));
   const double H = div_rn((q[4] + p), r);
   o.F[0] = r * un;
-  o.F[1] = AXIS == 0 ? r * un * u + p : r * un * u;
-  o.F[2] = AXIS == 1 ? r * un * v + p : r * un * v;
-  o.F[3] = AXIS == 2 ? r * un * w + p : r * un * w;
+  o.F[1] = ax == 0 ? r * un * u + p : r * un * u;
+  o.F[2] = ax == 1 ? r * un * v + p : r * un * v;
+  o.F[3] = ax == 2 ? r * un * w + p : r * un * w;
   o.F[4] = r * un * H;
   o.u = u;
   o.v = v;
   o.w = w;
   o.H = H;
+}
+template <int AXIS>
+PDA_HD void euler5_side(FluxSide<5> &o, const double q[5], double gamma) {
+  euler5_side_ax(o, q, gamma, AXIS);
 }
 template <int AXIS>
 PDA_HD void euler5_combine(double F[5], const double qL[5], const double qR[5], const FluxSide<5> &L,
@@ -841,19 +851,22 @@ PDA_HD void euler5_combine(double F[5], const double qL[5], const double qR[5], 
   for (int d = 0; d < 5; ++d) F[d] = half * (L.F[d] + R.F[d] + smax * (qL[d] - qR[d]));
 }
 
-template <int AXIS>
-PDA_HD void swe_side(FluxSide<3> &o, const double q[3], double gravity) {
+PDA_HD void swe_side_ax(FluxSide<3> &o, const double q[3], double gravity, int ax) {
   constexpr double es = 1.e-30;
   const double h = q[0];
   const double u = div_rn(q[1], (h + es));
   const double v = div_rn(q[2], (h + es));
-  const double un = AXIS == 0 ? u : v;
+  const double un = ax == 0 ? u : v;
   const double p = 0.5 * gravity * h * h;
   o.F[0] = h * un;
-  o.F[1] = AXIS == 0 ? h * un * u + p : h * un * u;
-  o.F[2] = AXIS == 1 ? h * un * v + p : h * un * v;
+  o.F[1] = ax == 0 ? h * un * u + p : h * un * u;
+  o.F[2] = ax == 1 ? h * un * v + p : h * un * v;
   o.u = un;
   o.H = sqrt_rn(h);
+}
+template <int AXIS>
+PDA_HD void swe_side(FluxSide<3> &o, const double q[3], double gravity) {
+  swe_side_ax(o, q, gravity, AXIS);
 }
 template <int AXIS>
 PDA_HD void swe_combine(double F[3], const double qL[3], const double qR[3], const FluxSide<3> &L,
