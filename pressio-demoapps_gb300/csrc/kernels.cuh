@@ -35,6 +35,10 @@ template <> struct Fam<Euler1d> {
   static PDA_HD void flux_jac(T JL[9], T JR[9], const T qL[3], const T qR[3], const Phys &p) {
     euler3_flux_jac(JL, JR, qL, qR, (T)p.gamma);
   }
+  template <typename T>
+  static PDA_HD void flux_jac_ax(T JL[9], T JR[9], const T qL[3], const T qR[3], const Phys &p, int) {
+    euler3_flux_jac(JL, JR, qL, qR, (T)p.gamma);
+  }
   // the flux in two halves (one face state, then the combination); bit-identical to flux
   using Side = FluxSide<3>;
   template <int AXIS>
@@ -57,6 +61,10 @@ template <> struct Fam<Euler2d> {
   template <int AXIS, typename T>
   static PDA_HD void flux_jac(T JL[16], T JR[16], const T qL[4], const T qR[4], const Phys &p) {
     euler4_flux_jac<AXIS>(JL, JR, qL, qR, (T)p.gamma);
+  }
+  template <typename T>
+  static PDA_HD void flux_jac_ax(T JL[16], T JR[16], const T qL[4], const T qR[4], const Phys &p, int ax) {
+    euler4_flux_jac_ax(JL, JR, qL, qR, (T)p.gamma, ax);
   }
   // the flux in two halves (one face state, then the combination); bit-identical to flux
   using Side = FluxSide<4>;
@@ -83,6 +91,10 @@ template <> struct Fam<Euler3d> {
   static PDA_HD void flux_jac(T JL[25], T JR[25], const T qL[5], const T qR[5], const Phys &p) {
     euler5_flux_jac<AXIS>(JL, JR, qL, qR, (T)p.gamma);
   }
+  template <typename T>
+  static PDA_HD void flux_jac_ax(T JL[25], T JR[25], const T qL[5], const T qR[5], const Phys &p, int ax) {
+    euler5_flux_jac_ax(JL, JR, qL, qR, (T)p.gamma, ax);
+  }
   // the flux in two halves (one face state, then the combination); bit-identical to flux
   using Side = FluxSide<5>;
   template <int AXIS>
@@ -107,6 +119,10 @@ template <> struct Fam<Swe2d> {
   template <int AXIS, typename T>
   static PDA_HD void flux_jac(T JL[9], T JR[9], const T qL[3], const T qR[3], const Phys &p) {
     swe_flux_jac<AXIS>(JL, JR, qL, qR, (T)p.gravity);
+  }
+  template <typename T>
+  static PDA_HD void flux_jac_ax(T JL[9], T JR[9], const T qL[3], const T qR[3], const Phys &p, int ax) {
+    swe_flux_jac_ax(JL, JR, qL, qR, (T)p.gravity, ax);
   }
   // the flux in two halves (one face state, then the combination); bit-identical to flux
   using Side = FluxSide<3>;
@@ -586,9 +602,7 @@ k_rows_vj_inner_par(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U
         if constexpr (DIM > 1) if (ax == 1) F::template flux<1>(o.fl, uN, uP, p);
         if constexpr (DIM > 2) if (ax == 2) F::template flux<2>(o.fl, uN, uP, p);
       } else {
-        if (ax == 0) F::template flux_jac<0>(o.JN, o.JP, uN, uP, p);
-        if constexpr (DIM > 1) if (ax == 1) F::template flux_jac<1>(o.JN, o.JP, uN, uP, p);
-        if constexpr (DIM > 2) if (ax == 2) F::template flux_jac<2>(o.JN, o.JP, uN, uP, p);
+        F::flux_jac_ax(o.JN, o.JP, uN, uP, p, ax);  // one stream for all axes of the warp
       }
     }
   }
@@ -719,9 +733,7 @@ k_rows_vj_nearbd_par(RowTable t, MeshArgs m, Phys p, const double *__restrict__ 
         for (int s = 0; s < 2; ++s)
           load_entry<NDPC>(q1[s], U, t.src1[b1 + fs + s], t.flip1[b1 + fs + s], m.reflect[ax], m, t.gsx1, t.gsy1,
                            b1 + fs + s);
-        if (ax == 0) F::template flux_jac<0>(o.JN, o.JP, q1[0], q1[1], p);
-        if constexpr (DIM > 1) if (ax == 1) F::template flux_jac<1>(o.JN, o.JP, q1[0], q1[1], p);
-        if constexpr (DIM > 2) if (ax == 2) F::template flux_jac<2>(o.JN, o.JP, q1[0], q1[1], p);
+        F::flux_jac_ax(o.JN, o.JP, q1[0], q1[1], p, ax);  // one stream for all axes of the warp
       }
     }
   }

@@ -339,9 +339,7 @@ k_lspg_fused(RowTable ti, RowTable tn, int rpb, int nbInner, MeshArgs m, Phys p,
           vN[d] = (JT)uN[d];
           vP[d] = (JT)uP[d];
         }
-        if (ax == 0) F::template flux_jac<0>(JN, JP, vN, vP, p);
-        if constexpr (DIM > 1) if (ax == 1) F::template flux_jac<1>(JN, JP, vN, vP, p);
-        if constexpr (DIM > 2) if (ax == 2) F::template flux_jac<2>(JN, JP, vN, vP, p);
+        F::flux_jac_ax(JN, JP, vN, vP, p, ax);  // one stream for all axes of the warp
         // one of the two per warp (the part is warp-uniform): the other's
         // arithmetic is dead and dropped
         if (part == 2) {

@@ -883,7 +883,9 @@ PDA_HD void swe_combine(double F[3], const double qL[3], const double qR[3], con
 
 // ---------------------------------------------------------------------------
 // Analytic Rusanov flux Jacobians JL = dF/dqL, JR = dF/dqR (row-major n x n).
-// These keep the reference's generic normal vector n.
+// These keep the reference's generic normal vector n, built from a runtime
+// axis (*_flux_jac_ax; the templated form passes its constant), so threads
+// of one warp that hold faces of different axes run one instruction stream.
 // ---------------------------------------------------------------------------
 template <typename T>
 PDA_HD void euler3_flux_jac(T JL[9], T JR[9], const T qL[3],
@@ -948,12 +950,12 @@ PDA_HD void euler3_flux_jac(T JL[9], T JR[9], const T qL[3],
   }
 }
 
-template <int AXIS, typename T>
-PDA_HD void euler4_flux_jac(T JL[16], T JR[16], const T qL[4],
-                            const T qR[4], T gamma) {
+template <typename T>
+PDA_HD void euler4_flux_jac_ax(T JL[16], T JR[16], const T qL[4],
+                            const T qR[4], T gamma, int ax) {
   constexpr T one = T(1.), two = T(2.), half = T(1.) / T(2.);
   constexpr T es = T(1.e-30);
-  const T n[2] = {AXIS == 0 ? T(1.) : T(0.), AXIS == 1 ? T(1.) : T(0.)};
+  const T n[2] = {ax == 0 ? T(1.) : T(0.), ax == 1 ? T(1.) : T(0.)};
   const T gm1 = gamma - one;
   const T rL = qL[0];
   const T uL = div_rn(qL[1], (rL + es));
@@ -1035,13 +1037,18 @@ PDA_HD void euler4_flux_jac(T JL[16], T JR[16], const T qL[4],
     for (int j = 0; j < 4; j++) JR[i * 4 + j] += half * gR[j] * (qL[i] - qR[i]);
   }
 }
-
 template <int AXIS, typename T>
-PDA_HD void euler5_flux_jac(T JL[25], T JR[25], const T qL[5],
-                            const T qR[5], T gamma) {
+PDA_HD void euler4_flux_jac(T JL[16], T JR[16], const T qL[4],
+                            const T qR[4], T gamma) {
+  euler4_flux_jac_ax(JL, JR, qL, qR, gamma, AXIS);
+}
+
+template <typename T>
+PDA_HD void euler5_flux_jac_ax(T JL[25], T JR[25], const T qL[5],
+                            const T qR[5], T gamma, int ax) {
   constexpr T one = T(1.), two = T(2.), half = T(1.) / T(2.);
   constexpr T es = T(1.e-30);
-  const T n[3] = {AXIS == 0 ? T(1.) : T(0.), AXIS == 1 ? T(1.) : T(0.), AXIS == 2 ? T(1.) : T(0.)};
+  const T n[3] = {ax == 0 ? T(1.) : T(0.), ax == 1 ? T(1.) : T(0.), ax == 2 ? T(1.) : T(0.)};
   const T gm1 = gamma - one;
   const T rL = qL[0];
   const T uL = div_rn(qL[1], (rL + es));
@@ -1125,14 +1132,19 @@ PDA_HD void euler5_flux_jac(T JL[25], T JR[25], const T qL[5],
     for (int j = 0; j < 5; j++) JR[i * 5 + j] += half * gR[j] * (qL[i] - qR[i]);
   }
 }
+template <int AXIS, typename T>
+PDA_HD void euler5_flux_jac(T JL[25], T JR[25], const T qL[5],
+                            const T qR[5], T gamma) {
+  euler5_flux_jac_ax(JL, JR, qL, qR, gamma, AXIS);
+}
 
 // Shallow-water Rusanov flux Jacobian (generic normal).  deviation: pow(x,0.5)
 // -> sqrt(x); pow(2,3/2) is the correctly rounded constant 2*sqrt(2).
-template <int AXIS, typename T>
-PDA_HD void swe_flux_jac(T JL[9], T JR[9], const T qL[3],
-                         const T qR[3], T g) {
+template <typename T>
+PDA_HD void swe_flux_jac_ax(T JL[9], T JR[9], const T qL[3],
+                         const T qR[3], T g, int ax) {
   constexpr T es = T(1.e-30);
-  const T n[2] = {AXIS == 0 ? T(1.) : T(0.), AXIS == 1 ? T(1.) : T(0.)};
+  const T n[2] = {ax == 0 ? T(1.) : T(0.), ax == 1 ? T(1.) : T(0.)};
   const T hL = qL[0];
   const T uL = div_rn(qL[1], (hL + es));
   const T vL = div_rn(qL[2], (hL + es));
@@ -1179,6 +1191,11 @@ PDA_HD void swe_flux_jac(T JL[9], T JR[9], const T qL[3],
   JR[6] = T(0.5) * (g * n[1] * qR[0] - qR[2] * termR) - T(0.5) * dR[0] * (qR[2] - qL[2]);
   JR[7] = T(0.5) * n[0] * vR - T(0.5) * dR[1] * (qR[2] - qL[2]);
   JR[8] = n[1] * vR + T(0.5) * n[0] * uR - T(0.5) * smax - T(0.5) * dR[2] * (qR[2] - qL[2]);
+}
+template <int AXIS, typename T>
+PDA_HD void swe_flux_jac(T JL[9], T JR[9], const T qL[3],
+                         const T qR[3], T g) {
+  swe_flux_jac_ax(JL, JR, qL, qR, g, AXIS);
 }
 
 }  // namespace pda
