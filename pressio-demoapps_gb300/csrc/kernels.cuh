@@ -158,6 +158,19 @@ PDA_HD void reconstruct_face(double uNeg[NDPC], double uPos[NDPC], const double 
   }
 }
 
+// The Rusanov flux of a face whose axis is a runtime value, as its two sides
+// and their combination (bit-identical to flux<AXIS>): threads of one warp
+// that hold faces of different axes then run one instruction stream instead
+// of each axis's specialised flux in turn.
+template <int FAM>
+__device__ __forceinline__ void flux_ax(double fl[], const double uN[], const double uP[], const Phys &p, int ax) {
+  using F = Fam<FAM>;
+  typename F::Side L, R;
+  F::flux_side_ax(L, uN, p, ax);
+  F::flux_side_ax(R, uP, p, ax);
+  F::template flux_combine<0>(fl, uN, uP, L, R, p);
+}
+
 // Same with the gradient of each reconstructed value with respect to the 2H
 // cell values (per dof): g[d][s].  FirstOrder gradients are {1,0} / {0,1}
 // (functor_reconstruct_from_state.hpp:523-536).
@@ -598,9 +611,7 @@ k_rows_vj_inner_par(RowTable t, MeshArgs m, Phys p, const double *__restrict__ U
         uP[d] = o.uP[d];
       }
       if (part == 0) {
-        if (ax == 0) F::template flux<0>(o.fl, uN, uP, p);
-        if constexpr (DIM > 1) if (ax == 1) F::template flux<1>(o.fl, uN, uP, p);
-        if constexpr (DIM > 2) if (ax == 2) F::template flux<2>(o.fl, uN, uP, p);
+        flux_ax<FAM>(o.fl, uN, uP, p, ax);  // one stream for all axes of the warp
       } else {
         F::flux_jac_ax(o.JN, o.JP, uN, uP, p, ax);  // one stream for all axes of the warp
       }
@@ -723,9 +734,7 @@ k_rows_vj_nearbd_par(RowTable t, MeshArgs m, Phys p, const double *__restrict__ 
           uN[d] = o.uN[d];
           uP[d] = o.uP[d];
         }
-        if (ax == 0) F::template flux<0>(o.fl, uN, uP, p);
-        if constexpr (DIM > 1) if (ax == 1) F::template flux<1>(o.fl, uN, uP, p);
-        if constexpr (DIM > 2) if (ax == 2) F::template flux<2>(o.fl, uN, uP, p);
+        flux_ax<FAM>(o.fl, uN, uP, p, ax);  // one stream for all axes of the warp
       } else {
         double q1[2][NDPC];
         const size_t b1 = ((size_t)e * DIM + ax) * 3;
